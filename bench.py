@@ -1,0 +1,345 @@
+"""Benchmark of the GB300 align-to-center path.
+
+Workload (the configuration the headline metric is quoted on): 100,000
+full-length mutated copies of a 16,569 bp uniform ACGT center (seed 0; 1%
+substitutions, 0.1% + 0.1% indels of geometric length mean 3), k=15, w=10,
+stored 2-bit packed.  Synthetic, seeded; no dataset is read.
+
+One step = one pass of the hot path (minimizers -> anchors -> chain ->
+gap-fill DP -> CIGAR -> aligned rows -> per-column counters) over the whole
+batch.  Inputs (1.66 Gbp, 415 MB packed) and all intermediates exceed the
+129 MB L2, so no flush is needed between steps.
+
+  value   aligned Mbp/s with the packed batch resident in HBM (hg_run_staged),
+          CUDA events on the context stream
+  e2e     the same metric through the C ABI call a user makes
+          (hg_align_batch with pinned host buffers): packed input H2D,
+          CIGARs + insertion flags + aligned rows D2H inside the timed region
+  cpu_baseline / --impl reference: the CPU path (the oracle's restatement of
+          the reference loop, OpenMP over every host core) on a bounded sample
+
+Multi-GPU (torchrun): queries are independent, so ranks take contiguous
+shards of a fixed per-rank batch (weak scaling, no data-path collective);
+timing is max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "aligned Mbp/s (align-to-center, bit-exact)"
+UNIT = "Mbp/s"
+N_QUERIES = 100_000
+CENTER_LEN = 16_569
+MEASURED = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM = 6800.0
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world, local, use_gpu):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+            backend = "nccl" if use_gpu else "gloo"
+            if use_gpu:
+                import torch
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if self.dist.get_backend() == "nccl" else "cpu")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=6)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 5 + i and s[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def load_peaks():
+    if MEASURED.exists():
+        d = json.loads(MEASURED.read_text())
+        return float(d.get("hbm_gbs", FALLBACK_HBM)), "measured"
+    return FALLBACK_HBM, "fallback"
+
+
+def make_workload(pkg, n):
+    t = time.time()
+    w = pkg.synth.mito(n)
+    log(f"[bench] generated {w.n} queries / {w.total_bases} bases in {time.time() - t:.1f}s")
+    t = time.time()
+    b = pkg.pack(w.seqs, w.offsets)
+    log(f"[bench] packed {b.packed.nbytes} bytes in {time.time() - t:.1f}s")
+    return w, b
+
+
+def cpu_sample(oracle, w, budget_s: float, threads: int):
+    """Time the CPU path on consecutive 1000-query blocks until budget_s."""
+    done_q = done_b = 0
+    tot = 0.0
+    i = 0
+    while tot < budget_s and i < w.n:
+        j = min(i + 1000, w.n)
+        offs = w.offsets[i:j + 1] - w.offsets[i]
+        seqs = w.seqs[w.offsets[i]: w.offsets[j]]
+        t, _ = oracle.align_batch(w.center, w.center, seqs, offs, nthreads=threads)
+        tot += t
+        done_q += j - i
+        done_b += int(offs[-1])
+        i = j
+    return done_b / tot / 1e6, done_q, done_b, tot
+
+
+def algorithmic_bytes(b, n_cigar_words: int, L: int):
+    """HBM bytes the path must move: packed input + per-query arrays in, rows +
+    CIGARs + flags out."""
+    inp = b.packed.nbytes + b.exc.nbytes + 8 * b.n * 3
+    out = b.n * L + 4 * n_cigar_words + b.n
+    return inp + out
+
+
+def run_impl_reference(args, rank, world):
+    """The reference's CPU path (the oracle restatement) on the host cores."""
+    if rank != 0:
+        return 0
+    from oracle.oracle import Oracle
+    from tests.pkgload import load_package
+    pkg = load_package()
+    o = Oracle()
+    threads = os.cpu_count() or 1
+    w = pkg.synth.mito(4000)
+    for _ in range(args.warmup):
+        cpu_sample(o, w, 0.5, threads)
+    vals = []
+    for _ in range(args.steps):
+        v, nq, nb, t = cpu_sample(o, w, 5.0, threads)
+        vals.append((v, nq, nb, t))
+    value = float(np.median([v[0] for v in vals]))
+    tot_t = sum(v[3] for v in vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tot_t / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32",
+        "data": "synthetic (seeded mutated copies of a uniform ACGT center)",
+        "config": {"workload": "mito 16,569 bp center x mutated full-length queries; bounded sample per step",
+                   "k": 15, "w": 10, "sample_queries_per_step": int(np.median([v[1] for v in vals]))},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "consecutive 1000-query blocks of the mito workload, ~5 s per step"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--queries", type=int, default=N_QUERIES, help="queries per GPU")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--stage-timing", action="store_true", help="per-stage event timing pass (extra run)")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_impl_reference(args, rank, world)
+
+    from tests.pkgload import load_package
+    pkg = load_package()
+    pkg.lib()
+    if pkg.device_count() == 0:
+        raise SystemExit("bench: no CUDA device")
+    dist = Dist(world, local, use_gpu=True)
+    if world > 1:
+        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
+    w, b = make_workload(pkg, args.queries)
+    ix = pkg.Index(w.center)
+    sub = 25_000
+    ctx = pkg.Context(ix, max_queries=sub, max_bases=sub * 17_000)
+    ctx.stage(b)
+    # warm-up (also builds and caches the CUDA graphs of every sub-batch)
+    for _ in range(args.warmup):
+        ctx.run_staged()
+    ctx.last_timing()
+    dist.barrier()
+    import ctypes as C
+    L = pkg.lib()
+    # device-resident timing: CUDA events on the context stream bracket every
+    # staged run; the per-step sync sits between the events of two steps
+    dev_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            ctx.run_staged()
+            ms, _, launches = ctx.last_timing()  # synchronizes the context stream
+            dev_ms.append(ms)
+    dist.barrier()
+    step_s = dist.max(float(np.sum(dev_ms)) / 1e3 / args.steps)
+    cells_c = C.c_int64()
+    L.hg_last_timing(ctx.h, None, None, None, C.byref(cells_c))
+    cells = cells_c.value  # cells of the last step
+    value = world * b.bases / step_s / 1e6
+    # per-stage breakdown (event-timed pass; excluded from the headline number)
+    ctx.set_timing(True)
+    ctx.run_staged()
+    stage_tot, stages, _ = ctx.last_timing()
+    ctx.set_timing(False)
+    n_cig_words = None
+    # e2e: the C ABI call with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+        pb = pkg.Packed(pin(b.packed), pin(b.poff), pin(b.qlen), pin(b.exc), pin(b.exc_off))
+        rows_out = pin(np.zeros((b.n, (ix.L + 15) // 16 * 16), np.uint8))
+        cig_out = pin(np.zeros(b.bases // 8 + 64 * b.n + 1024, np.uint32))
+        off_out = np.zeros(b.n + 1, np.int64)
+        ins_out = np.zeros(b.n, np.uint8)
+        st_out = np.zeros(b.n, np.uint32)
+        P = pkg._p
+
+        def call():
+            code = L.hg_align_batch(ctx.h, P(pb.packed), P(pb.poff), P(pb.qlen), P(pb.exc), P(pb.exc_off), pb.n,
+                                    P(cig_out), len(cig_out), P(off_out), P(ins_out), P(rows_out),
+                                    rows_out.shape[1], P(st_out))
+            pkg._check(code)
+
+        call()
+        dist.barrier()
+        e2e_steps = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            call()
+        e_wall = dist.max((time.perf_counter() - t0) / e2e_steps)
+        n_cig_words = int(off_out[-1])
+        h2d = b.nbytes
+        d2h = 4 * n_cig_words + 8 * (b.n + 1) + b.n + 4 * b.n + b.n * ix.L
+        e2e = {"value": round(world * b.bases / e_wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1000 * e_wall, 3)}
+    if n_cig_words is None:
+        n_cig_words = 64 * b.n
+    peak, peak_kind = load_peaks()
+    # dominant stage
+    top = max(stages, key=lambda k: stages[k])
+    alg = algorithmic_bytes(b, n_cig_words, ix.L)
+    stage_bytes = {"seed": b.packed.nbytes + 8 * 3000 * b.n, "anchor": 16 * 3000 * b.n, "chain": 8 * 2500 * b.n,
+                   "dp_small": b.packed.nbytes + 4 * n_cig_words, "dp_large": 0, "stitch": 8 * n_cig_words,
+                   "rows": b.n * ix.L + 4 * n_cig_words, "count": b.n * ix.L}
+    top_ms = stages[top]
+    achieved = (alg / (stage_tot / 1e3) / 1e9) if stage_tot > 0 else None
+    top_achieved = (stage_bytes.get(top, 0) / (top_ms / 1e3) / 1e9) if top_ms > 0 else None
+    clocks = clk.summary()
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        from oracle.oracle import Oracle
+        v, nq, nb, t = cpu_sample(Oracle(), w, args.cpu_seconds, os.cpu_count() or 1)
+        cpu = {"value": round(v, 3), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+               "sample": f"first {nq} queries ({nb} bases) of the workload, {t:.1f} s of CPU time"}
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * step_s, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/int32",
+        "data": "synthetic (seeded mutated copies of a uniform ACGT center)",
+        "config": {"workload": f"mito: {args.queries} queries x ~16,569 bp vs a 16,569 bp center, 1% sub, "
+                               "0.1%+0.1% indels (geometric mean 3), k=15, w=10, 2-bit packed",
+                   "queries_per_gpu": args.queries, "bases_per_gpu": b.bases,
+                   "l2": "inputs and intermediates exceed L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+        "gcups": round(world * cells / step_s / 1e9, 3) if cells else None,
+        "gpu_launches": int(launches),
+        "stage_ms": {k: round(v, 3) for k, v in stages.items()},
+        "roofline": {"bound": "hbm", "kernel": "whole path (all stages)",
+                     "achieved": round(achieved, 2) if achieved else None, "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 5) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind, "dominant_stage": top,
+                     "dominant_stage_achieved_gbs": round(top_achieved, 2) if top_achieved else None,
+                     "note": "integer-issue-bound path; HBM fraction is low by construction"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,1 +1,311 @@
-"""halign_gb300: GB300-native align-to-center path of HAlign-4 (package directory ``halign-4_gb300``)."""
+"""halign_gb300 - GB300-native align-to-center path of HAlign-4.
+
+Python host binding over the C ABI of ``include/halign_gb300.h`` (the
+library ``_build/libhalign_gb300.so`` built from ``csrc/`` by ``build.py``).
+Every call here runs the CUDA kernels; there is no CPU fallback: without the
+built library or a CUDA device the calls raise ``HalignError``.
+
+Typical use (mirrors RefAligner: one center, many queries):
+
+    ix = Index(center_bytes, k=15, w=10)
+    ctx = Context(ix, max_queries=16384, max_bases=300_000_000)
+    batch = pack(seqs_bytes, offsets)
+    res = ctx.align(batch, rows=True)      # CIGARs, insertion flags, rows
+    counts, ins = ctx.counters()           # per-column SiteCount totals
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libhalign_gb300.so"
+
+HG_OK = 0
+HG_ERR_LENGTH_MISMATCH = 5
+ST_ARENA_OVERFLOW, ST_PARTIAL_CIGAR, ST_CIGAR_OVERFLOW, ST_LENGTH_MISMATCH = 0x01, 0x02, 0x08, 0x10
+STAGES = ("seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count")
+
+
+class HalignError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def lib() -> C.CDLL:
+    """Load the native library (build it first with build.py / build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise HalignError(-1, f"native library missing: {LIB_PATH} (run halign-4_gb300/build.py)")
+    L = C.CDLL(str(LIB_PATH))
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int
+    L.hg_last_error.restype = C.c_char_p
+    L.hg_device_count.restype = i32
+    L.hg_default_params.argtypes = [vp]
+    L.hg_index_create.argtypes = [C.c_char_p, i64, i32, i32, vp, C.POINTER(vp)]
+    L.hg_index_destroy.argtypes = [vp]
+    L.hg_index_info.argtypes = [vp, vp, vp, vp]
+    L.hg_ctx_create.argtypes = [vp, i64, i64, C.POINTER(vp)]
+    L.hg_ctx_destroy.argtypes = [vp]
+    L.hg_pack.argtypes = [vp, vp, i64, vp, i64, vp, vp, i64, vp, vp, vp]
+    batch_args = [vp, vp, vp, vp, vp, vp, i64, vp, i64, vp, vp, vp, i64, vp]
+    L.hg_align_batch.argtypes = batch_args
+    L.hg_align_plain.argtypes = batch_args
+    L.hg_stage.argtypes = [vp, vp, vp, vp, vp, vp, i64]
+    L.hg_run_staged.argtypes = [vp]
+    L.hg_fetch_staged.argtypes = [vp, vp, i64, vp, vp, vp, i64, vp]
+    L.hg_last_timing.argtypes = [vp, vp, vp, vp, vp]
+    L.hg_set_timing.argtypes = [vp, i32]
+    L.hg_counters.argtypes = [vp, vp, vp, i32]
+    L.hg_extract_minimizer.argtypes = [C.c_char_p, i64, i32, i32, i32, vp, vp, i64, vp]
+    L.hg_extract_minimizer.restype = i64
+    L.hg_ksw_extz2.argtypes = [i32, vp, i32, vp, C.c_int8, vp, C.c_int8, C.c_int8, i32, i32, i32, i32, vp, vp, i64]
+    L.hg_ksw_extz2.restype = i64
+    L.hg_global_align_ksw2.argtypes = [C.c_char_p, i64, C.c_char_p, i64, i32, vp, i64]
+    L.hg_global_align_ksw2.restype = i64
+    L.hg_align_query.argtypes = [vp, C.c_char_p, i64, vp, i64, vp]
+    L.hg_align_query.restype = i64
+    _lib = L
+    return L
+
+
+def _check(code: int):
+    if code != HG_OK:
+        raise HalignError(code, lib().hg_last_error().decode(errors="replace"))
+
+
+def device_count() -> int:
+    return int(lib().hg_device_count())
+
+
+def _bytes(s) -> bytes:
+    if isinstance(s, str):
+        return s.encode("latin-1")
+    if isinstance(s, np.ndarray):
+        return s.tobytes()
+    return bytes(s)
+
+
+@dataclass
+class Packed:
+    """A packed batch in the device input format (see hg_pack)."""
+    packed: np.ndarray      # uint8
+    poff: np.ndarray        # int64[n]
+    qlen: np.ndarray        # int32[n]
+    exc: np.ndarray         # int32[m*3]
+    exc_off: np.ndarray     # int64[n+1]
+
+    @property
+    def n(self) -> int:
+        return len(self.qlen)
+
+    @property
+    def bases(self) -> int:
+        return int(self.qlen.sum())
+
+    @property
+    def nbytes(self) -> int:
+        return self.packed.nbytes + self.poff.nbytes + self.qlen.nbytes + self.exc.nbytes + self.exc_off.nbytes
+
+
+def pack(seqs: bytes, offsets) -> Packed:
+    """Pack concatenated ASCII queries (``offsets``: int64[n+1])."""
+    L = lib()
+    seqs = _bytes(seqs)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    n = len(offsets) - 1
+    pb, ne = C.c_int64(0), C.c_int64(0)
+    buf = np.frombuffer(seqs, np.uint8) if seqs else np.zeros(1, np.uint8)
+    _check(L.hg_pack(_p(buf), _p(offsets), n, None, 0, None, None, 0, None, C.byref(pb), C.byref(ne)))
+    packed = np.zeros(max(pb.value, 16), np.uint8)
+    poff = np.zeros(max(n, 1), np.int64)
+    exc = np.zeros(max(ne.value, 1) * 3, np.int32)
+    exc_off = np.zeros(n + 1, np.int64)
+    _check(L.hg_pack(_p(buf), _p(offsets), n, _p(packed), len(packed), _p(poff), _p(exc), ne.value, _p(exc_off),
+                     None, None))
+    return Packed(packed, poff[:n], np.diff(offsets).astype(np.int32), exc, exc_off)
+
+
+@dataclass
+class AlignResult:
+    cigar: np.ndarray       # uint32 ops, concatenated
+    cigar_off: np.ndarray   # int64[n+1]
+    has_ins: np.ndarray     # uint8[n]
+    status: np.ndarray      # uint32[n]
+    rows: np.ndarray | None  # uint8[n, L] or None
+
+    def cigar_of(self, i: int) -> np.ndarray:
+        return self.cigar[self.cigar_off[i]: self.cigar_off[i + 1]]
+
+
+class Index:
+    """Resident center index (RefAligner's per-center set-up, kept in HBM)."""
+
+    def __init__(self, center, k: int = 15, w: int = 10):
+        L = lib()
+        self.center = _bytes(center)
+        self.k, self.w = k, w
+        h = C.c_void_p()
+        _check(L.hg_index_create(self.center, len(self.center), k, w, None, C.byref(h)))
+        self.h = h
+        self.L = len(self.center)
+
+    def info(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_uint64()
+        _check(lib().hg_index_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def align_query(self, qry) -> np.ndarray:
+        q = _bytes(qry)
+        cap = len(q) + self.L + 8
+        out = np.zeros(cap, np.uint32)
+        st = C.c_uint32()
+        n = lib().hg_align_query(self.h, q, len(q), _p(out), cap, C.byref(st))
+        if n < 0:
+            _check(-n)
+        return out[:n].copy()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hg_index_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """A stream plus device arenas for batches of up to max_queries / max_bases."""
+
+    def __init__(self, index: Index, max_queries: int = 16384, max_bases: int = 1 << 28):
+        h = C.c_void_p()
+        _check(lib().hg_ctx_create(index.h, max_queries, max_bases, C.byref(h)))
+        self.h, self.index = h, index
+
+    def _outputs(self, n: int, bases: int, rows: bool, worst: bool = False):
+        # realistic CIGARs are a few ops per kilobase; the worst case is one op
+        # per base of query + center
+        cap = (bases + n * (self.index.L + 4)) if worst else (bases // 8 + 64 * n + 1024)
+        cig = np.zeros(max(cap, 1), np.uint32)
+        off = np.zeros(n + 1, np.int64)
+        has_ins = np.zeros(max(n, 1), np.uint8)
+        status = np.zeros(max(n, 1), np.uint32)
+        stride = (self.index.L + 15) // 16 * 16
+        rbuf = np.zeros((n, stride), np.uint8) if rows else None
+        return cig, off, has_ins, status, rbuf, stride
+
+    def _result(self, cig, off, has_ins, status, rbuf, n):
+        rows = rbuf[:, : self.index.L] if rbuf is not None else None
+        return AlignResult(cig[: off[-1]] if n else cig[:0], off, has_ins[:n], status[:n], rows)
+
+    def align(self, b: Packed, rows: bool = True, plain: bool = False, check: bool = True) -> AlignResult:
+        fn = lib().hg_align_plain if plain else lib().hg_align_batch
+        for worst in (False, True):
+            cig, off, has_ins, status, rbuf, stride = self._outputs(b.n, b.bases, rows, worst)
+            code = fn(self.h, _p(b.packed), _p(b.poff), _p(b.qlen), _p(b.exc), _p(b.exc_off), b.n, _p(cig),
+                      len(cig), _p(off), _p(has_ins), _p(rbuf), stride if rows else 0, _p(status))
+            if code != 4:  # HG_ERR_CAPACITY: retry once with the worst-case buffer
+                break
+        if check or code not in (HG_OK, HG_ERR_LENGTH_MISMATCH):
+            _check(code)
+        return self._result(cig, off, has_ins, status, rbuf, b.n)
+
+    # device-resident form
+    def stage(self, b: Packed):
+        _check(lib().hg_stage(self.h, _p(b.packed), _p(b.poff), _p(b.qlen), _p(b.exc), _p(b.exc_off), b.n))
+        self._staged = b
+
+    def run_staged(self):
+        _check(lib().hg_run_staged(self.h))
+
+    def fetch_staged(self, rows: bool = True) -> AlignResult:
+        b = self._staged
+        cig, off, has_ins, status, rbuf, stride = self._outputs(b.n, b.bases, rows, worst=True)
+        _check(lib().hg_fetch_staged(self.h, _p(cig), len(cig), _p(off), _p(has_ins), _p(rbuf), stride, _p(status)))
+        return self._result(cig, off, has_ins, status, rbuf, b.n)
+
+    def set_timing(self, on: bool):
+        _check(lib().hg_set_timing(self.h, int(on)))
+
+    def last_timing(self):
+        tot = C.c_float()
+        st = np.zeros(8, np.float32)
+        la, ce = C.c_int64(), C.c_int64()
+        _check(lib().hg_last_timing(self.h, C.byref(tot), _p(st), C.byref(la), C.byref(ce)))
+        return tot.value, dict(zip(STAGES, st.tolist())), la.value
+
+    def counters(self, reset: bool = False):
+        L = self.index.L
+        cnt = np.zeros((L, 7), np.uint32)
+        ins = np.zeros(L + 1, np.uint32)
+        _check(lib().hg_counters(self.h, _p(cnt), _p(ins), int(reset)))
+        return cnt, ins
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def extract_minimizer(seq, k: int = 15, w: int = 10, non_canonical: bool = True):
+    s = _bytes(seq)
+    cap = len(s) + 1
+    xs = np.zeros(cap, np.uint64)
+    ys = np.zeros(cap, np.uint64)
+    need = C.c_int64()
+    n = lib().hg_extract_minimizer(s, len(s), k, w, int(non_canonical), _p(xs), _p(ys), cap, C.byref(need))
+    if n < 0:
+        _check(-n)
+    return xs[:n].copy(), ys[:n].copy()
+
+
+def ksw_extz2(query_codes, target_codes, m, mat, q, e, w, zdrop, end_bonus, flag):
+    qc = np.ascontiguousarray(query_codes, np.uint8)
+    tc = np.ascontiguousarray(target_codes, np.uint8)
+    mt = np.ascontiguousarray(mat, np.int8)
+    ez = np.zeros(10, np.int32)
+    cap = len(qc) + len(tc) + 4
+    cig = np.zeros(cap, np.uint32)
+    n = lib().hg_ksw_extz2(len(qc), _p(qc), len(tc), _p(tc), m, _p(mt), q, e, w, zdrop, end_bonus, flag, _p(ez),
+                           _p(cig), cap)
+    if n < 0:
+        _check(-n)
+    return ez, cig[:n].copy()
+
+
+def global_align_ksw2(ref, qry, flag: int = -1) -> np.ndarray:
+    r, q = _bytes(ref), _bytes(qry)
+    cap = len(r) + len(q) + 4
+    c = np.zeros(cap, np.uint32)
+    n = lib().hg_global_align_ksw2(r, len(r), q, len(q), flag, _p(c), cap)
+    if n < 0:
+        _check(-n)
+    return c[:n].copy()
+
+
+def build_library(force: bool = False) -> Path:
+    """Compile csrc/ into _build/libhalign_gb300.so (sm_103a)."""
+    import importlib
+    return importlib.import_module(__name__ + ".build").build(force=force)

@@ -1,0 +1,125 @@
+// hg_batch.cuh - device-side views of the resident center index and of one
+// batch of queries, passed by value to every stage kernel.
+#pragma once
+
+#include "hg_common.cuh"
+
+namespace hg {
+
+// Center index, built once per center and kept in HBM (the reference rebuilds
+// it on every collect_anchors call, src/seed/minimizer.cpp:238-265).
+struct IndexDev {
+    int L;                     // center length
+    int k, w;                  // minimizer k-mer size and window
+    int non_canonical;         // 1 on the align-to-center path (src/align/ref_aligner.cpp:83)
+    const uint8_t* center;     // DNA5 codes of the center the DP aligns to
+    const uint64_t* tab_key;   // open-addressing table: key = hash56 (kNoHash = empty)
+    const uint32_t* tab_val;   // entry id of the key
+    uint32_t tab_mask;
+    uint32_t n_ent;            // distinct center minimizer hashes
+    const uint32_t* ent_start; // into cpos
+    const uint32_t* ent_count; // reference-side occurrence count
+    const uint8_t* ent_over;   // count > occurrence threshold (sparse sampling applies)
+    const uint32_t* cpos;      // center positions grouped by hash, ascending within a hash
+    const uint32_t* cspan;     // matching spans (always k for a single center)
+    double q_occ_frac;
+    uint64_t sample_every;
+    // chain parameters (anchor::ChainParams, include/anchor.h:116-127)
+    int max_dist_x, max_dist_y, bw, max_skip, max_iter, min_cnt, min_score;
+    float gap_pen, skip_pen;
+    const float* log2tab;      // log2f(i) for i in [0, n_log2)
+    int n_log2;
+};
+
+// One gap-fill segment of globalAlignMM2 (src/align/align.cpp:221-293).
+struct Seg {
+    uint32_t rs, qs, rl, ql;  // center start/len, query start/len
+    uint32_t slot;            // op slot, relative to the query's CIGAR scratch
+    int32_t nops;             // DP result length; -1 = segment did not consume (I/D fallback)
+    uint32_t q;               // query index
+    uint32_t kind;            // low byte: SegKind; bit 8: left-aligned gaps (first segment)
+};
+
+enum SegKind : uint32_t { kSegEmpty = 0, kSegIns = 1, kSegDel = 2, kSegDpSmall = 3, kSegDpLarge = 4, kSegGlobal = 5 };
+constexpr uint32_t kSegLeft = 1u << 8;
+
+// Small-DP tier: one thread per segment, direction nibbles in shared memory.
+constexpr int kSmallMaxCells = 256;
+constexpr int kSmallMaxInner = 16;
+constexpr int kSmallMaxSide = 200;
+
+struct BatchDev {
+    int n;                       // queries in the batch
+    const uint8_t* packed;       // 2-bit packed bases
+    const int64_t* poff;         // per-query byte offset (16-byte aligned)
+    const int32_t* qlen;
+    const int32_t* exc;          // exception runs: start, len, byte
+    const int64_t* exc_off;      // per-query run range [exc_off[q], exc_off[q+1])
+    const int32_t* order;        // processing order (longest first)
+    // K1 seed
+    const int64_t* hoff;         // per-query base into the hit arrays (capacity qlen-k+1)
+    uint32_t* hit_pos;
+    uint32_t* hit_ent;
+    int32_t* n_hits;             // all minimizers of the query
+    int32_t* n_matched;          // minimizers whose hash occurs in the center
+    uint32_t* exact_list;        // queries whose window deque overflows (re-run sequentially)
+    unsigned int* n_exact;
+    uint64_t* ring_h;            // ring scratch of the sequential re-run
+    uint32_t* ring_p;
+    int ring_slots;              // ring entries per re-run thread
+    // K2 anchors (dynamic arena)
+    uint32_t* a_ref;
+    uint32_t* a_qry;
+    int32_t* a_f;
+    int32_t* a_p;
+    int32_t* a_t;
+    unsigned long long* a_tmp;   // 2 words per anchor: sort scratch
+    int64_t acap;
+    unsigned long long* a_cursor;
+    int64_t* a_base;
+    int32_t* a_n;
+    uint32_t* ent_cnt;           // per-CTA query-side counters when n_ent is large
+    // K3 chain + segments (dynamic arena)
+    Seg* seg;
+    int64_t scap;
+    unsigned long long* s_cursor;
+    int64_t* s_base;
+    int32_t* s_n;
+    int32_t* n_chain;
+    uint32_t* work_small;        // global segment ids per DP tier
+    uint32_t* work_large;
+    unsigned int* n_small;
+    unsigned int* n_large;
+    int64_t wcap;
+    // K5/K6 DP scratch for large segments (dynamic byte arena)
+    uint8_t* dp_arena;
+    int64_t dp_cap;
+    unsigned long long* dp_cursor;
+    // CIGARs
+    const int64_t* coff;         // per-query base of the op scratch (capacity qlen + L + 4)
+    uint32_t* cig_seg;           // per-segment ops, at coff[q] + seg.slot
+    uint32_t* cig;               // merged CIGAR per query, at coff[q]
+    int32_t* n_cig;
+    uint8_t* has_ins;
+    // rows + counters
+    uint8_t* rows;               // n x L
+    uint32_t* counts;            // L x 7 (A C G T U N -)
+    uint32_t* ins;               // L + 1 insertion events
+    uint32_t* status;            // per query
+    unsigned int* queues;        // work-queue heads, one per stage
+    unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
+};
+
+// Hash-table probe; returns the entry id or kEmptyKey.
+__device__ __forceinline__ uint32_t index_find(const IndexDev& ix, uint64_t h)
+{
+    uint32_t s = (uint32_t)h & ix.tab_mask;
+    for (;;) {
+        const uint64_t kk = ix.tab_key[s];
+        if (kk == h) return ix.tab_val[s];
+        if (kk == kNoHash) return kEmptyKey;
+        s = (s + 1) & ix.tab_mask;
+    }
+}
+
+}  // namespace hg

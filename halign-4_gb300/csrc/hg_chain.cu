@@ -1,0 +1,242 @@
+// hg_chain.cu - K3: anchor chaining DP + segmentation of the gap-fill.
+//
+// Chaining restates anchor::chainAnchors (src/seed/anchor.cpp:332-461) with
+// chainScoreSimple (:254-301).  One warp owns one query.  For anchor i the
+// reference scans j = i-1 down to iter_start and, in order, keeps the first
+// strictly better total (max_f), decrements n_skip on every improvement and
+// increments it when j was marked (t[j] == i, i.e. some scanned j' > j with a
+// valid score has p[j'] == j), stopping once n_skip exceeds max_skip.  The
+// warp scores 32 candidates at once and reproduces that serial order exactly:
+//   * marks: every valid lane stores t[p[j]] = i before any lane tests t[j];
+//     p[j'] < j' means a mark only ever targets a later-scanned j, and marks
+//     from lanes past the stopping point target anchors this i never tests;
+//   * improvements: lane l improves iff its total beats the running maximum
+//     of max_f and all earlier valid totals (warp prefix max);
+//   * n_skip: X_l = max(X_{l-1} + d_l, 0) with d = -1 (improvement), +1
+//     (marked, not an improvement), 0 otherwise, has the closed form
+//     X_l = S_l + max(X_in, -min_{m<=l} S_m) over the prefix sums S (warp
+//     prefix sum + prefix min); the first +1 lane with X > max_skip stops it.
+// The penalty 0.01*dd + 0.01*dg + 0.5*log2f(dd+1) is evaluated with
+// round-to-nearest products and sums (no fused multiply-add), log2f from a
+// host-built table, and truncated toward zero.
+//
+// Segmentation restates globalAlignMM2's segment walk (src/align/align.cpp:
+// 189-305): the chain comes out of the backtrack strictly increasing in both
+// coordinates, i.e. already sorted by (pos_qry, pos_ref).  Segment ends are
+// clipped to the sequence ends and every segment starts where the previous one
+// ended, so segment s covers [max_{m<s} end_m, max(end_s, start_s)) - a warp
+// prefix max.  Whether a segment's DP consumes it never moves a later
+// boundary, so all segments of all queries are independent work items.
+#include "hg_batch.cuh"
+
+namespace hg {
+
+constexpr int kChainWarps = 4;
+
+__device__ __forceinline__ int32_t chain_score(const IndexDev& ix, uint32_t ri, uint32_t qi, uint32_t rj, uint32_t qj,
+                                               int32_t span_j)
+{
+    const int32_t dq = (int32_t)qi - (int32_t)qj;
+    if (dq <= 0 || dq > ix.max_dist_x) return INT32_MIN;
+    const int32_t dr = (int32_t)ri - (int32_t)rj;
+    if (dr <= 0 || dr > ix.max_dist_y) return INT32_MIN;
+    const int32_t dd = dr > dq ? dr - dq : dq - dr;
+    if (dd > ix.bw) return INT32_MIN;
+    const int32_t dg = dr < dq ? dr : dq;
+    int32_t sc = span_j < dg ? span_j : dg;
+    if (dd > 0 || dg > span_j) {
+        const float lin = __fadd_rn(__fmul_rn(ix.gap_pen, (float)dd), __fmul_rn(ix.skip_pen, (float)dg));
+        const float lg = dd >= 1 ? ix.log2tab[dd + 1] : 0.0f;
+        sc -= __float2int_rz(__fadd_rn(lin, __fmul_rn(0.5f, lg)));
+    }
+    return sc;
+}
+
+__global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, BatchDev b)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int32_t span = ix.k;
+    for (;;) {
+        int qi = 0;
+        if (lane == 0) qi = (int)atomicAdd(&b.queues[2], 1u);
+        qi = __shfl_sync(FULL, qi, 0);
+        if (qi >= b.n) break;
+        const int q = b.order ? b.order[qi] : qi;
+        const int A = b.a_n[q];
+        const int64_t base = b.a_base[q];
+        const uint32_t* ar = b.a_ref + base;
+        const uint32_t* aq = b.a_qry + base;
+        int32_t* f = b.a_f + base;
+        int32_t* p = b.a_p + base;
+        int32_t* t = b.a_t + base;
+        for (int i = lane; i < A; i += 32) t[i] = -1;
+        __syncwarp();
+        int st = 0, best = -1;
+        int32_t best_f = 0;
+        for (int i = 0; i < A; ++i) {
+            const uint32_t ri = ar[i], qv = aq[i];
+            while (st < i && (int32_t)(ri - ar[st]) > ix.max_dist_x) ++st;
+            const int it0 = (i - st > ix.max_iter) ? i - ix.max_iter : st;
+            int32_t max_f = span;
+            int max_j = -1;
+            int n_skip = 0;
+            for (int jb = i - 1; jb >= it0; jb -= 32) {
+                const int j = jb - lane;
+                bool valid = j >= it0;
+                int32_t sc = INT32_MIN;
+                if (valid) sc = chain_score(ix, ri, qv, ar[j], aq[j], span);
+                valid = valid && sc != INT32_MIN;
+                int32_t fj = 0, pj = -1;
+                if (valid) fj = f[j], pj = p[j];
+                if (valid && pj >= 0) t[pj] = i;
+                __syncwarp();
+                const bool marked = valid && t[j] == i;
+                const int32_t tot = fj + sc;
+                const int32_t vmax = warp_incl_max(valid ? tot : INT32_MIN);
+                int32_t prev = __shfl_up_sync(FULL, vmax, 1);
+                if (lane == 0) prev = INT32_MIN;
+                prev = max(prev, max_f);
+                const bool rec = valid && tot > prev;
+                const int d = rec ? -1 : (marked ? 1 : 0);
+                const int S = warp_incl_sum(d);
+                const int mS = warp_incl_min(S);
+                const int X = S + max(n_skip, -mS);
+                const unsigned brk = __ballot_sync(FULL, d == 1 && X > ix.max_skip);
+                unsigned recm = __ballot_sync(FULL, rec);
+                if (brk) recm &= (1u << (__ffs(brk) - 1)) - 1u;
+                if (recm) {
+                    const int L = 31 - __clz(recm);
+                    max_f = __shfl_sync(FULL, tot, L);
+                    max_j = __shfl_sync(FULL, j, L);
+                }
+                if (brk) break;
+                n_skip = __shfl_sync(FULL, X, 31);
+                __syncwarp();
+            }
+            if (lane == 0) f[i] = max_f, p[i] = max_j;
+            __syncwarp();
+            if (max_f > best_f) best_f = max_f, best = i;
+        }
+        // backtrack: chain (reversed) into t[], read p[] 32 entries at a time
+        int c = 0;
+        if (!(best_f < ix.min_score || best < 0)) {
+            int cur = best;
+            while (cur >= 0) {
+                const int lo = max(cur - 31, 0);
+                const int pl = (lo + lane <= cur) ? p[lo + lane] : -1;
+                while (cur >= lo) {
+                    if (lane == 0) t[c] = cur;
+                    ++c;
+                    cur = __shfl_sync(FULL, pl, cur - lo);
+                }
+            }
+            if (c < ix.min_cnt) c = 0;
+        }
+        __syncwarp();
+        // segmentation
+        const int len = b.qlen[q];
+        const int L = ix.L;
+        const int nseg = c > 0 ? 2 * c + 1 : 1;
+        unsigned long long sb = 0;
+        if (lane == 0) {
+            sb = atomicAdd(b.s_cursor, (unsigned long long)nseg);
+            if ((int64_t)(sb + nseg) > b.scap) {
+                atomicOr(&b.status[q], kStArenaOverflow);
+                sb = ~0ull;
+            }
+        }
+        sb = __shfl_sync(FULL, sb, 0);
+        if (lane == 0) {
+            b.n_chain[q] = c;
+            b.s_base[q] = sb == ~0ull ? 0 : (int64_t)sb;
+            b.s_n[q] = sb == ~0ull ? 0 : nseg;
+        }
+        if (sb == ~0ull) continue;
+        uint32_t rpos = 0, qpos = 0, slot = 0;
+        for (int s0 = 0; s0 < nseg; s0 += 32) {
+            const int s = s0 + lane;
+            const bool act = s < nseg;
+            int64_t er = 0, eq = 0;
+            uint32_t flags = 0;
+            if (act) {
+                if (c == 0) {
+                    er = L, eq = len;
+                } else if (s == 0) {
+                    const int a = t[c - 1];
+                    er = ar[a], eq = aq[a], flags = kSegLeft;
+                } else if (s == 2 * c) {
+                    er = L, eq = len;
+                } else if (s & 1) {
+                    const int a = t[c - 1 - (s - 1) / 2];
+                    er = (int64_t)ar[a] + span, eq = (int64_t)aq[a] + span;
+                } else {
+                    const int a = t[c - 1 - s / 2];
+                    er = ar[a], eq = aq[a];
+                }
+            }
+            const int cr = act ? (int)min(er, (int64_t)L) : 0;
+            const int cq = act ? (int)min(eq, (int64_t)len) : 0;
+            const int ir = max(warp_incl_max(cr), (int)rpos);
+            const int iq = max(warp_incl_max(cq), (int)qpos);
+            int pr = __shfl_up_sync(FULL, ir, 1), pq = __shfl_up_sync(FULL, iq, 1);
+            if (lane == 0) pr = rpos, pq = qpos;
+            const uint32_t rs = (uint32_t)pr, qs = (uint32_t)pq;
+            const uint32_t rl = (uint32_t)ir - rs, ql = (uint32_t)iq - qs;
+            uint32_t kind;
+            if (rl == 0 && ql == 0) kind = kSegEmpty;
+            else if (rl == 0) kind = kSegIns;
+            else if (ql == 0) kind = kSegDel;
+            else if (c == 0) kind = kSegGlobal;
+            else if (max(rl, ql) <= (uint32_t)kSmallMaxSide && min(rl, ql) <= (uint32_t)kSmallMaxInner &&
+                     rl * ql <= (uint32_t)kSmallMaxCells)
+                kind = kSegDpSmall;
+            else
+                kind = kSegDpLarge;
+            const uint32_t need = (kind >= kSegDpSmall && act) ? rl + ql : 0;
+            const uint32_t sincl = warp_incl_sum(need);
+            const uint32_t my_slot = slot + sincl - need;
+            if (act) {
+                Seg g;
+                g.rs = rs, g.qs = qs, g.rl = rl, g.ql = ql;
+                g.slot = my_slot;
+                g.nops = 0;
+                g.q = (uint32_t)q;
+                g.kind = kind | flags;
+                b.seg[sb + s] = g;
+            }
+            // tier work lists (warp-aggregated appends)
+            const unsigned ms = __ballot_sync(FULL, act && kind == kSegDpSmall);
+            const unsigned ml = __ballot_sync(FULL, act && (kind == kSegDpLarge || kind == kSegGlobal));
+            unsigned bs = 0, bl = 0;
+            if (lane == 0) {
+                if (ms) bs = atomicAdd(b.n_small, (unsigned)__popc(ms));
+                if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
+            }
+            bs = __shfl_sync(FULL, bs, 0);
+            bl = __shfl_sync(FULL, bl, 0);
+            const unsigned below = (1u << lane) - 1u;
+            if (ms >> lane & 1u) {
+                const unsigned w = bs + __popc(ms & below);
+                if ((int64_t)w < b.wcap) b.work_small[w] = (uint32_t)(sb + s);
+                else atomicOr(&b.status[q], kStArenaOverflow);
+            }
+            if (ml >> lane & 1u) {
+                const unsigned w = bl + __popc(ml & below);
+                if ((int64_t)w < b.wcap) b.work_large[w] = (uint32_t)(sb + s);
+                else atomicOr(&b.status[q], kStArenaOverflow);
+            }
+            rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
+            qpos = (uint32_t)__shfl_sync(FULL, iq, 31);
+            slot = slot + __shfl_sync(FULL, sincl, 31);
+        }
+    }
+}
+
+}  // namespace hg
+
+extern "C" cudaError_t hg_launch_chain(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+{
+    hg::chain_kernel<<<grid, hg::kChainWarps * 32, 0, st>>>(*ix, *b);
+    return cudaGetLastError();
+}

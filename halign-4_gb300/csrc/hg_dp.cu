@@ -1,0 +1,533 @@
+// hg_dp.cu - K5/K6: KSW2 extz2 gap-fill (src/align/ksw2_extz2_sse.c:23-304)
+// and its traceback (ksw_backtrack, include/ksw2.h:129-161).
+//
+// Two tiers, both bit-exact with the SSE2 build of the reference:
+//
+// * Small tier (one thread per segment).  When the band w is at least
+//   max(qlen, tlen) it never binds (globalAlignKSW2 sets w = 200 + ... for
+//   segments up to 200 bp, or -1), and every cell the reference computes
+//   outside [st0, en0] is either overwritten by a boundary before it is read
+//   or never read by an in-band cell.  The DP is then exactly the per-cell
+//   recurrence over the in-band cells: cell (t, j) takes x, v from (t-1, j),
+//   u, y from (t, j-1), with the reference's boundaries x = 0, v = q (0 at the
+//   corner) on the left and u = q (0 at the corner), y = 0 on top.  The thread
+//   sweeps the longer side outermost, keeps the shorter side's byte state in
+//   shared memory, applies ksw_lane (the SSE2 instruction sequence) per cell
+//   and stores a 4-bit direction code per cell, word-interleaved across the
+//   CTA so every shared-memory access is bank-conflict free.
+//
+// * Large tier (one warp per segment; also every single-call ksw_extz2).  An
+//   exact emulation of the SIMD code: the anti-diagonal band rounded to whole
+//   16-lane blocks, the per-target byte arrays u, v, x, y, s living across
+//   anti-diagonals (so out-of-band lanes use stale state just as the SIMD
+//   code does), the exact int32 H row with its 4-way interleaved arg-max,
+//   z-drop, approximate-max mode and the band-exhaustion stop.  Lanes of a
+//   diagonal run 32 at a time; the byte carried from the previous 32-lane
+//   chunk plays the role of the SSE shift-in register.
+#include "hg_batch.cuh"
+
+namespace hg {
+
+constexpr int kDpSmallThreads = 128;
+constexpr int kDirWords = kSmallMaxCells / 8;       // 4-bit codes, 8 per word
+constexpr int kStateWords = kSmallMaxInner / 4 * 2; // u/y (or x/v) bytes of the inner side
+
+__device__ __forceinline__ uint32_t dna5_score(uint32_t a, uint32_t b)
+{  // dna5_simd_mat (include/align.h:109-116)
+    return (a == 4u || b == 4u) ? 0u : (a == b ? 5u : (uint32_t)(uint8_t)-4);
+}
+
+// DNA5 code of query base i (packed + exception runs).
+__device__ __forceinline__ uint32_t query_dna5(const uint8_t* pk, const int32_t* exc, int64_t e0, int64_t e1, uint32_t i)
+{
+    uint32_t c = packed_code(pk, i);
+    if (e0 < e1) {
+        int64_t lo = e0, hi = e1;
+        while (lo < hi) {  // first run starting after i
+            const int64_t mid = (lo + hi) >> 1;
+            if ((uint32_t)exc[mid * 3] <= i) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo > e0) {
+            const int64_t r = lo - 1;
+            if (i < (uint32_t)(exc[r * 3] + exc[r * 3 + 1])) c = dna5_of((uint8_t)exc[r * 3 + 2]);
+        }
+    }
+    return c;
+}
+
+__device__ __forceinline__ uint32_t nib_of(uint32_t d) { return (d & 3u) | ((d >> 3) & 1u) << 2 | ((d >> 4) & 1u) << 3; }
+
+struct CigarPush {
+    uint32_t* out;
+    int n, cap;
+    uint32_t last;
+    __device__ void push(uint32_t op, uint32_t len)
+    {
+        if (n > cap) return;
+        if (n > 0 && (last & 0xfu) == op) {
+            last += len << 4;
+            out[n - 1] = last;
+        } else if (n < cap) {
+            last = len << 4 | op;
+            out[n++] = last;
+        } else {
+            n = cap + 1;  // overflow marker
+        }
+    }
+};
+
+__global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
+{
+    __shared__ uint32_t dirs[kDirWords * kDpSmallThreads];
+    __shared__ uint32_t state[kStateWords * kDpSmallThreads];
+    const int tid = threadIdx.x;
+    const uint32_t q = 6, qe2 = 16, max_sc = 5 + 16;
+    const unsigned total = *b.n_small;
+    unsigned long long cell_sum = 0;
+    const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
+    for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
+        if (w >= total) continue;
+        const uint32_t sid = b.work_small[w];
+        Seg g = b.seg[sid];
+        const int qn = (int)g.ql, tn = (int)g.rl;
+        const int mode = (g.kind & kSegLeft) ? 1 : 2;
+        const uint8_t* pk = b.packed + b.poff[g.q];
+        const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
+        const uint8_t* tc = ix.center + g.rs;
+        const bool tinner = tn <= qn;  // inner = target side (state u,y per t), else inner = query side
+        const int inner = tinner ? tn : qn, outer = tinner ? qn : tn;
+        // inner-side codes packed 4 bits each
+        uint64_t icode = 0;
+        for (int i = 0; i < inner; ++i) {
+            const uint32_t c = tinner ? tc[i] : query_dna5(pk, b.exc, e0, e1, g.qs + i);
+            icode |= (uint64_t)c << (4 * i);
+        }
+        uint32_t wbuf = 0;
+        int widx = 0, wfill = 0;
+        for (int o = 0; o < outer; ++o) {
+            const uint32_t oc = tinner ? query_dna5(pk, b.exc, e0, e1, g.qs + o) : tc[o];
+            // carried along the inner sweep: (x, v) when inner = target, (u, y) when inner = query
+            uint32_t c1 = 0, c2 = tinner ? (o ? q : 0u) : (o ? q : 0u);
+            uint32_t sw0 = 0, sw1 = 0;  // current state words being rewritten
+            for (int i = 0; i < inner; ++i) {
+                const int wi = i >> 2, sh = (i & 3) * 8;
+                if ((i & 3) == 0) {
+                    sw0 = state[(wi * 2) * kDpSmallThreads + tid];
+                    sw1 = state[(wi * 2 + 1) * kDpSmallThreads + tid];
+                }
+                const uint32_t icv = (uint32_t)(icode >> (4 * i)) & 0xfu;
+                const uint32_t s = tinner ? dna5_score(icv, oc) : dna5_score(oc, icv);
+                LaneOut r;
+                if (tinner) {  // cell (t=i, j=o): x,v carried from t-1; u,y from row j-1
+                    const uint32_t ut = o ? (sw0 >> sh) & 0xffu : (i ? q : 0u);
+                    const uint32_t yt = o ? (sw1 >> sh) & 0xffu : 0u;
+                    r = ksw_lane(s, c1, c2, ut, yt, qe2, max_sc, q, mode);
+                    c1 = r.x, c2 = r.v;
+                    sw0 = (sw0 & ~(0xffu << sh)) | (uint32_t)r.u << sh;
+                    sw1 = (sw1 & ~(0xffu << sh)) | (uint32_t)r.y << sh;
+                } else {  // cell (t=o, j=i): u,y carried from j-1; x,v from column t-1
+                    const uint32_t xt = o ? (sw0 >> sh) & 0xffu : 0u;
+                    const uint32_t vt = o ? (sw1 >> sh) & 0xffu : (i ? q : 0u);
+                    const uint32_t ut = i ? c1 : (o ? q : 0u);
+                    const uint32_t yt = i ? c2 : 0u;
+                    r = ksw_lane(s, xt, vt, ut, yt, qe2, max_sc, q, mode);
+                    c1 = r.u, c2 = r.y;
+                    sw0 = (sw0 & ~(0xffu << sh)) | (uint32_t)r.x << sh;
+                    sw1 = (sw1 & ~(0xffu << sh)) | (uint32_t)r.v << sh;
+                }
+                if ((i & 3) == 3 || i == inner - 1) {
+                    state[(wi * 2) * kDpSmallThreads + tid] = sw0;
+                    state[(wi * 2 + 1) * kDpSmallThreads + tid] = sw1;
+                }
+                wbuf |= nib_of(r.d) << (4 * wfill);
+                if (++wfill == 8) {
+                    dirs[widx * kDpSmallThreads + tid] = wbuf;
+                    ++widx, wfill = 0, wbuf = 0;
+                }
+            }
+        }
+        if (wfill) dirs[widx * kDpSmallThreads + tid] = wbuf;
+        // traceback from (tlen-1, qlen-1); cell index = o * inner + i
+        CigarPush cp{b.cig_seg + b.coff[g.q] + g.slot, 0, tn + qn, 0};
+        int ti = tn - 1, qj = qn - 1, state_ = 0;
+        while (ti >= 0 && qj >= 0) {
+            const int cell = tinner ? (qj * inner + ti) : (ti * inner + qj);
+            const uint32_t nib = (dirs[(cell >> 3) * kDpSmallThreads + tid] >> ((cell & 7) * 4)) & 0xfu;
+            if (state_ == 0) state_ = nib & 3u;
+            else if (!((nib >> (state_ + 1)) & 1u)) state_ = 0;
+            if (state_ == 0) state_ = nib & 3u;
+            if (state_ == 0) cp.push(0, 1), --ti, --qj;
+            else if (state_ == 1) cp.push(2, 1), --ti;
+            else cp.push(1, 1), --qj;
+        }
+        if (ti >= 0) cp.push(2, (uint32_t)(ti + 1));
+        if (qj >= 0) cp.push(1, (uint32_t)(qj + 1));
+        for (int i = 0; i < cp.n / 2; ++i) {
+            const uint32_t a = cp.out[i];
+            cp.out[i] = cp.out[cp.n - 1 - i];
+            cp.out[cp.n - 1 - i] = a;
+        }
+        b.seg[sid].nops = cp.n;
+        cell_sum += (unsigned long long)(tn * qn);
+    }
+    // warp-aggregated cell count for GCUPS
+    for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
+    if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
+}
+
+// ---------------------------------------------------------------- large tier
+
+struct KswArgs {
+    int qlen, tlen;
+    const uint8_t* query;   // DNA5 codes (or nullptr: read from the packed query)
+    const uint8_t* target;
+    const uint8_t* pk;      // packed query + exceptions, when query == nullptr
+    const int32_t* exc;
+    int64_t e0, e1;
+    uint32_t qoff;          // query base offset inside the packed query
+    int m;
+    const int8_t* mat;      // m*m
+    int q, e, w, zdrop, end_bonus, flag;
+};
+
+struct KswResult {
+    int32_t max, zdropped, max_q, max_t, mqe, mqe_t, mte, mte_q, score, reach_end;
+    int n_cigar;
+    long long cells;  // sum over computed anti-diagonals of (en0 - st0 + 1)
+};
+
+__device__ __forceinline__ size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+__host__ __device__ inline size_t ksw_scratch_bytes(int qlen, int tlen, int w, int flag)
+{
+    if (qlen <= 0 || tlen <= 0) return 0;
+    if (w < 0) w = tlen > qlen ? tlen : qlen;
+    const size_t tl16 = (size_t)((tlen + 15) / 16) * 16;
+    int n_col = qlen < tlen ? qlen : tlen;
+    n_col = ((n_col < w + 1 ? n_col : w + 1) + 15) / 16 + 1;
+    size_t s = ((tl16 * 5 + 15) & ~(size_t)15) + ((tl16 * 4 + 15) & ~(size_t)15);
+    if (!(flag & kEzScoreOnly)) {
+        s += ((((size_t)(qlen + tlen - 1) * n_col + 1) * 16 + 15) & ~(size_t)15);
+        s += (((size_t)(qlen + tlen - 1) * 8 + 15) & ~(size_t)15);
+    }
+    return s;
+}
+
+__device__ __forceinline__ uint32_t ksw_qcode(const KswArgs& a, int j)
+{
+    return a.query ? a.query[j] : query_dna5(a.pk, a.exc, a.e0, a.e1, a.qoff + (uint32_t)j);
+}
+
+// Warp-cooperative ksw_extz2_sse.  All 32 lanes call it; returns the same
+// KswResult in every lane.  The CIGAR (cap entries) goes to `cig`.
+__device__ KswResult ksw_extz2_warp(const KswArgs& a, uint8_t* scratch, uint32_t* cig, int cap)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    KswResult R;
+    R.max_q = R.max_t = R.mqe_t = R.mte_q = -1;
+    R.max = 0, R.score = R.mqe = R.mte = kNegInf;
+    R.zdropped = 0, R.reach_end = 0, R.n_cigar = 0, R.cells = 0;
+    const int qlen = a.qlen, tlen = a.tlen, m = a.m, q = a.q, e = a.e;
+    if (m <= 0 || qlen <= 0 || tlen <= 0) return R;
+    const int qe = q + e, with_cigar = !(a.flag & kEzScoreOnly), approx_max = !!(a.flag & kEzApproxMax);
+    const int mode = !with_cigar ? 0 : ((a.flag & kEzRight) ? 2 : 1);
+    const uint32_t qe2 = (uint32_t)((q + e) * 2) & 0xffu, max_sc = (uint32_t)(a.mat[0] + (q + e) * 2) & 0xffu;
+    int w = a.w;
+    if (w < 0) w = tlen > qlen ? tlen : qlen;
+    const int wl = w, wr = w;
+    const int tlen_ = (tlen + 15) / 16;
+    int n_col_ = qlen < tlen ? qlen : tlen;
+    n_col_ = ((n_col_ < w + 1 ? n_col_ : w + 1) + 15) / 16 + 1;
+    int min_sc = a.mat[1];
+    for (int t = 1; t < m * m; ++t) min_sc = min(min_sc, (int)a.mat[t]);
+    if (-min_sc > 2 * (q + e)) return R;
+    const size_t Lb = (size_t)tlen_ * 16;
+    uint8_t* u = scratch;
+    uint8_t* v = u + Lb;
+    uint8_t* x = v + Lb;
+    uint8_t* y = x + Lb;
+    uint8_t* s = y + Lb;
+    int32_t* H = reinterpret_cast<int32_t*>(scratch + align16(Lb * 5));
+    uint8_t* p = scratch + align16(Lb * 5) + align16(Lb * 4);
+    const size_t ncol = (size_t)n_col_ * 16;
+    const size_t nd = (size_t)(qlen + tlen - 1);
+    int* off = reinterpret_cast<int*>(p + align16((nd * n_col_ + 1) * 16));
+    int* off_end = off + nd;
+    for (size_t i = lane; i < Lb * 5; i += 32) u[i] = 0;
+    if (!approx_max)
+        for (size_t i = lane; i < Lb; i += 32) H[i] = kNegInf;
+    __syncwarp();
+    int32_t H0 = 0, last_H0_t = 0;
+    int last_st = -1, last_en = -1;
+    for (int r = 0; r < qlen + tlen - 1; ++r) {
+        int st = 0, en = tlen - 1;
+        if (st < r - qlen + 1) st = r - qlen + 1;
+        if (en > r) en = r;
+        if (st < (r - wr + 1) >> 1) st = (r - wr + 1) >> 1;
+        if (en > (r + wl) >> 1) en = (r + wl) >> 1;
+        if (st > en) {
+            R.zdropped = 1;
+            break;
+        }
+        const int st0 = st, en0 = en;
+        R.cells += en0 - st0 + 1;
+        st = st / 16 * 16, en = (en + 16) / 16 * 16 - 1;
+        uint32_t x1, v1;
+        if (st > 0) {
+            if (st - 1 >= last_st && st - 1 <= last_en) x1 = x[st - 1], v1 = v[st - 1];
+            else x1 = v1 = 0;
+        } else
+            x1 = 0, v1 = r ? (uint32_t)q : 0u;
+        const uint32_t x1e = (x1 & 0x80u) ? 0xffu : 0u, v1e = (v1 & 0x80u) ? 0xffu : 0u;
+        __syncwarp();
+        if (lane == 0 && en >= r) y[r] = 0, u[r] = (uint8_t)(r ? q : 0);
+        for (int t = st0 + lane; t <= en0; t += 32) s[t] = (uint8_t)a.mat[a.target[t] * m + ksw_qcode(a, r - t)];
+        __syncwarp();
+        if (with_cigar && lane == 0) off[r] = st, off_end[r] = en;
+        uint8_t* pr = with_cigar ? p + (size_t)r * ncol : nullptr;
+        uint32_t cx = x1, cv = v1;
+        for (int c0 = st; c0 <= en; c0 += 32) {
+            const int t = c0 + lane;
+            const bool act = t <= en;
+            const uint32_t xo = act ? x[t] : 0u, vo = act ? v[t] : 0u, ut = act ? u[t] : 0u, yt = act ? y[t] : 0u,
+                           sv = act ? s[t] : 0u;
+            uint32_t xt1 = __shfl_up_sync(FULL, xo, 1), vt1 = __shfl_up_sync(FULL, vo, 1);
+            if (lane == 0) xt1 = cx, vt1 = cv;
+            if (c0 == st && lane >= 1 && lane <= 3) xt1 |= x1e, vt1 |= v1e;
+            cx = __shfl_sync(FULL, xo, 31);
+            cv = __shfl_sync(FULL, vo, 31);
+            __syncwarp();
+            if (act) {
+                const LaneOut o = ksw_lane(sv, xt1, vt1, ut, yt, qe2, max_sc, (uint32_t)q & 0xffu, mode);
+                u[t] = o.u, v[t] = o.v, x[t] = o.x, y[t] = o.y;
+                if (with_cigar) pr[t - st] = o.d;
+            }
+            __syncwarp();
+        }
+        if (!approx_max) {
+            int32_t max_H, max_t;
+            if (r > 0) {
+                int32_t hen = 0;
+                if (lane == 0) hen = en0 > 0 ? H[en0 - 1] + (int32_t)u[en0] - qe : H[en0] + (int32_t)v[en0] - qe;
+                hen = __shfl_sync(FULL, hen, 0);
+                __syncwarp();
+                if (lane == 0) H[en0] = hen;
+                max_H = hen, max_t = en0;
+                const int en1 = st0 + (en0 - st0) / 4 * 4;
+                // lanes t = st0 + lane + 32k: SIMD lane (t - st0) & 3 == lane & 3
+                int32_t gh = max_H, gt = max_t;
+                for (int t = st0 + lane; t < en0; t += 32) {
+                    const int32_t h = H[t] + (int32_t)v[t] - qe;
+                    H[t] = h;
+                    if (t < en1 && h > gh) gh = h, gt = t;
+                }
+                // reduce within each SIMD-lane group: larger H, then smaller t
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) {
+                    const int32_t oh = __shfl_xor_sync(FULL, gh, o), ot = __shfl_xor_sync(FULL, gt, o);
+                    const bool og = oh > max_H;   // the other side moved off the initial value
+                    const bool mg = gh > max_H;
+                    if (og && (!mg || oh > gh || (oh == gh && ot < gt))) gh = oh, gt = ot;
+                }
+                __syncwarp();
+                // combine the four groups in order, then the scalar tail
+                for (int g = 0; g < 4; ++g) {
+                    const int32_t oh = __shfl_sync(FULL, gh, g), ot = __shfl_sync(FULL, gt, g);
+                    if (max_H < oh) max_H = oh, max_t = ot;
+                }
+                for (int t = en1; t < en0; ++t) {
+                    const int32_t h = H[t];
+                    if (h > max_H) max_H = h, max_t = t;
+                }
+            } else {
+                if (lane == 0) H[0] = (int32_t)v[0] - qe - qe;
+                __syncwarp();
+                max_H = H[0], max_t = 0;
+            }
+            __syncwarp();
+            if (en0 == tlen - 1 && H[en0] > R.mte) R.mte = H[en0], R.mte_q = r - en;
+            if (r - st0 == qlen - 1 && H[st0] > R.mqe) R.mqe = H[st0], R.mqe_t = st0;
+            // ksw_apply_zdrop (include/ksw2.h:191-207)
+            bool stop = false;
+            if (max_H > R.max) {
+                R.max = max_H, R.max_t = max_t, R.max_q = r - max_t;
+            } else if (max_t >= R.max_t && r - max_t >= R.max_q) {
+                const int tl = max_t - R.max_t, ql = (r - max_t) - R.max_q;
+                const int l = tl > ql ? tl - ql : ql - tl;
+                if (a.zdrop >= 0 && R.max - max_H > a.zdrop + l * e) R.zdropped = 1, stop = true;
+            }
+            if (stop) break;
+            if (r == qlen + tlen - 2 && en0 == tlen - 1) R.score = H[tlen - 1];
+        } else {
+            __syncwarp();
+            if (r > 0) {
+                if (last_H0_t >= st0 && last_H0_t <= en0 && last_H0_t + 1 >= st0 && last_H0_t + 1 <= en0) {
+                    const int32_t d0 = (int32_t)v[last_H0_t] - qe, d1 = (int32_t)u[last_H0_t + 1] - qe;
+                    if (d0 > d1) H0 += d0;
+                    else H0 += d1, ++last_H0_t;
+                } else if (last_H0_t >= st0 && last_H0_t <= en0) {
+                    H0 += (int32_t)v[last_H0_t] - qe;
+                } else {
+                    ++last_H0_t, H0 += (int32_t)u[last_H0_t] - qe;
+                }
+                if (a.flag & kEzApproxDrop) {
+                    bool stop = false;
+                    if (H0 > R.max) {
+                        R.max = H0, R.max_t = last_H0_t, R.max_q = r - last_H0_t;
+                    } else if (last_H0_t >= R.max_t && r - last_H0_t >= R.max_q) {
+                        const int tl = last_H0_t - R.max_t, ql = (r - last_H0_t) - R.max_q;
+                        const int l = tl > ql ? tl - ql : ql - tl;
+                        if (a.zdrop >= 0 && R.max - H0 > a.zdrop + l * e) R.zdropped = 1, stop = true;
+                    }
+                    if (stop) break;
+                }
+            } else
+                H0 = (int32_t)v[0] - qe - qe, last_H0_t = 0;
+            if (r == qlen + tlen - 2 && en0 == tlen - 1) R.score = H0;
+        }
+        last_st = st, last_en = en;
+        __syncwarp();
+    }
+    __syncwarp();
+    if (with_cigar) {
+        int i0 = -1, j0 = -1;
+        if (!R.zdropped && !(a.flag & kEzExtzOnly)) i0 = tlen - 1, j0 = qlen - 1;
+        else if (!R.zdropped && (a.flag & kEzExtzOnly) && R.mqe + a.end_bonus > R.max) R.reach_end = 1, i0 = R.mqe_t, j0 = qlen - 1;
+        else if (R.max_t >= 0 && R.max_q >= 0) i0 = R.max_t, j0 = R.max_q;
+        if (i0 >= 0 || j0 >= 0) {
+            int n = 0;
+            if (lane == 0) {
+                CigarPush cp{cig, 0, cap, 0};
+                int i = i0, j = j0, state = 0;
+                while (i >= 0 && j >= 0) {
+                    const int rr = i + j;
+                    int force = -1;
+                    uint32_t tmp;
+                    if (i < off[rr]) force = 2;
+                    if (i > off_end[rr]) force = 1;
+                    tmp = force < 0 ? p[(size_t)rr * ncol + (size_t)(i - off[rr])] : 0u;
+                    if (state == 0) state = tmp & 7;
+                    else if (!(tmp >> (state + 2) & 1)) state = 0;
+                    if (state == 0) state = tmp & 7;
+                    if (force >= 0) state = force;
+                    if (state == 0) cp.push(0, 1), --i, --j;
+                    else if (state == 1 || state == 3) cp.push(2, 1), --i;
+                    else cp.push(1, 1), --j;
+                }
+                if (i >= 0) cp.push(2, (uint32_t)(i + 1));
+                if (j >= 0) cp.push(1, (uint32_t)(j + 1));
+                if (cp.n <= cap && !(a.flag & kEzRevCigar))
+                    for (int k = 0; k < cp.n / 2; ++k) {
+                        const uint32_t tt = cig[k];
+                        cig[k] = cig[cp.n - 1 - k];
+                        cig[cp.n - 1 - k] = tt;
+                    }
+                n = cp.n;
+            }
+            R.n_cigar = __shfl_sync(FULL, n, 0);
+        }
+    }
+    return R;
+}
+
+__device__ const int8_t c_dna5_mat[25] = {5, -4, -4, -4, 0, -4, 5, -4, -4, 0, -4, -4, 5, -4, 0,
+                                          -4, -4, -4, 5, 0, 0, 0, 0, 0, 0};
+
+// Large tier of the batch: one warp per segment from the work list.
+__global__ void __launch_bounds__(128) dp_large_kernel(IndexDev ix, BatchDev b)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned total = *b.n_large;
+    for (;;) {
+        unsigned wi = 0;
+        if (lane == 0) wi = atomicAdd(&b.queues[3], 1u);
+        wi = __shfl_sync(FULL, wi, 0);
+        if (wi >= total) break;
+        const uint32_t sid = b.work_large[wi];
+        const Seg g = b.seg[sid];
+        const bool global = (g.kind & 0xffu) == kSegGlobal;
+        KswArgs a;
+        a.qlen = (int)g.ql, a.tlen = (int)g.rl;
+        a.query = nullptr;
+        a.target = ix.center + g.rs;
+        a.pk = b.packed + b.poff[g.q];
+        a.exc = b.exc;
+        a.e0 = b.exc_off[g.q], a.e1 = b.exc_off[g.q + 1];
+        a.qoff = g.qs;
+        a.m = 5, a.mat = c_dna5_mat, a.q = 6, a.e = 2;
+        a.w = auto_band((int)g.rl, (int)g.ql);
+        a.zdrop = -1, a.end_bonus = 0;
+        // the left end uses left-aligned gaps; the exact max is only needed
+        // when a chainless global alignment stops at the band edge
+        a.flag = kEzGenericSc | ((g.kind & kSegLeft) ? 0 : kEzRight) | (global ? 0 : kEzApproxMax);
+        const size_t need = ksw_scratch_bytes(a.qlen, a.tlen, a.w, a.flag);
+        unsigned long long off = 0;
+        if (lane == 0) {
+            off = atomicAdd(b.dp_cursor, (unsigned long long)((need + 255) & ~(size_t)255));
+            if ((int64_t)(off + need) > b.dp_cap) off = ~0ull;
+        }
+        off = __shfl_sync(FULL, off, 0);
+        if (off == ~0ull) {
+            if (lane == 0) {
+                atomicOr(&b.status[g.q], kStArenaOverflow);
+                b.seg[sid].nops = 0;
+            }
+            continue;
+        }
+        uint32_t* out = b.cig_seg + b.coff[g.q] + g.slot;
+        const KswResult R = ksw_extz2_warp(a, b.dp_arena + off, out, (int)(g.rl + g.ql));
+        if (lane == 0 && b.cells) atomicAdd(b.cells, (unsigned long long)R.cells);
+        if (lane == 0) {
+            if (global) {
+                b.seg[sid].nops = R.n_cigar;
+                if (R.zdropped) atomicOr(&b.status[g.q], kStPartialCigar);
+            } else {
+                // a segment whose CIGAR does not consume it becomes I(q) D(t)
+                // (src/align/align.cpp:243-261); only a band stop can cause it
+                b.seg[sid].nops = R.zdropped ? -1 : R.n_cigar;
+            }
+        }
+    }
+}
+
+// Single-call ksw_extz2 entry point: one warp.
+__global__ void ksw_single_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, int cap, KswResult* res)
+{
+    if (threadIdx.x >= 32) return;
+    const KswResult R = ksw_extz2_warp(a, scratch, cig, cap);
+    if (threadIdx.x == 0) *res = R;
+}
+
+}  // namespace hg
+
+extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+{
+    hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t hg_launch_dp_large(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+{
+    hg::dp_large_kernel<<<grid, 128, 0, st>>>(*ix, *b);
+    return cudaGetLastError();
+}
+
+extern "C" size_t hg_ksw_scratch_bytes(int qlen, int tlen, int w, int flag)
+{
+    return hg::ksw_scratch_bytes(qlen, tlen, w, flag);
+}
+
+extern "C" cudaError_t hg_launch_ksw_single(int qlen, const uint8_t* d_query, int tlen, const uint8_t* d_target, int m,
+                                            const int8_t* d_mat, int q, int e, int w, int zdrop, int end_bonus,
+                                            int flag, uint8_t* d_scratch, uint32_t* d_cig, int cap, void* d_res,
+                                            cudaStream_t st)
+{
+    hg::KswArgs a{};
+    a.qlen = qlen, a.tlen = tlen, a.query = d_query, a.target = d_target;
+    a.m = m, a.mat = d_mat, a.q = q, a.e = e, a.w = w, a.zdrop = zdrop, a.end_bonus = end_bonus, a.flag = flag;
+    hg::ksw_single_kernel<<<1, 32, 0, st>>>(a, d_scratch, d_cig, cap, static_cast<hg::KswResult*>(d_res));
+    return cudaGetLastError();
+}

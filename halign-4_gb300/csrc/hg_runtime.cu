@@ -1,0 +1,1175 @@
+// hg_runtime.cu - host runtime behind the C ABI (include/halign_gb300.h).
+//
+// * hg_index: the resident center index.  The center's minimizers come from
+//   the same seed kernel the queries use; the host groups them by hash,
+//   derives the -f/-U occurrence threshold (anchor::compute_ref_occ_threshold,
+//   src/seed/anchor.cpp:73-117) and uploads an open-addressing hash table.
+//   The DP center is the consensus of the single center record
+//   (pickConsensusChar, src/consensus/consensus.cpp:18-35: A/C/G/T/U keep
+//   their letter, every other byte becomes 'A'), as RefAligner aligns queries
+//   to consensus_seq while seeding from the raw record.
+// * hg_ctx: one stream plus the sub-batch arenas in HBM.  A sub-batch runs as
+//   one captured CUDA graph (control reset + 8 stage kernels); graphs are
+//   cached per (batch view, size) and replayed.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/halign_gb300.h"
+#include "hg_batch.cuh"
+
+extern "C" {
+cudaError_t hg_launch_seed(const hg::IndexDev*, const hg::BatchDev*, int, uint64_t*, uint64_t*, int, cudaStream_t);
+cudaError_t hg_launch_anchor(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_chain(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_dp_small(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_dp_large(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_stitch(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_rows(const hg::IndexDev*, const hg::BatchDev*, int64_t, int, cudaStream_t);
+cudaError_t hg_launch_count(const uint8_t*, int64_t, int, int, uint32_t*, cudaStream_t);
+size_t hg_ksw_scratch_bytes(int, int, int, int);
+int hg_exact_ring_threads(void);
+cudaError_t hg_prepare_kernels(void);
+cudaError_t hg_launch_ksw_single(int, const uint8_t*, int, const uint8_t*, int, const int8_t*, int, int, int, int,
+                                 int, int, uint8_t*, uint32_t*, int, void*, cudaStream_t);
+}
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where)
+{
+    return fail(HG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define HG_CUDA(call)                                         \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { free(); }
+    cudaError_t alloc(size_t count)
+    {
+        free();
+        n = count;
+        return count ? cudaMalloc(&p, sizeof(T) * count) : cudaSuccess;
+    }
+    void free()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+uint8_t consensus_letter(uint8_t c)
+{  // pickConsensusChar over one record's k_base_map category
+    switch (c) {
+    case 'A': case 'a': return 'A';
+    case 'C': case 'c': return 'C';
+    case 'G': case 'g': return 'G';
+    case 'T': case 't': return 'T';
+    case 'U': case 'u': return 'U';
+    default: return 'A';
+    }
+}
+
+int sm_count(int dev)
+{
+    int n = 0;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+}
+
+}  // namespace
+
+struct hg_index {
+    int device = 0;
+    int k = 15, w = 10;
+    hg_params_t prm{};
+    std::string center_raw;
+    int L = 0;
+    uint64_t occ_thr = 0;
+    int64_t n_hits = 0;
+    DevBuf<uint8_t> center;
+    DevBuf<uint64_t> tab_key;
+    DevBuf<uint32_t> tab_val, ent_start, ent_count, cpos, cspan;
+    DevBuf<uint8_t> ent_over;
+    DevBuf<float> log2tab;
+    hg::IndexDev dev{};
+    hg_ctx_t* single = nullptr;  // lazily created context for single-query calls
+    std::mutex single_mu;
+};
+
+struct SubPlan {
+    int64_t first, n;      // queries [first, first+n)
+    int64_t bases, bytes, excs;
+};
+
+struct GraphKey {
+    hg::BatchDev b;
+    bool operator<(const GraphKey& o) const { return std::memcmp(&b, &o.b, sizeof(b)) < 0; }
+};
+
+struct hg_ctx {
+    hg_index_t* ix = nullptr;
+    cudaStream_t st = nullptr;
+    int sms = 1;
+    int64_t max_n = 0, max_bases = 0, exc_cap = 0;
+    int64_t row_stride = 0;
+    // inputs (one sub-batch)
+    DevBuf<uint8_t> packed;
+    DevBuf<int64_t> poff, exc_off, hoff, coff;
+    DevBuf<int32_t> qlen, exc, order;
+    // stage arenas
+    DevBuf<uint32_t> hit_pos, hit_ent;
+    DevBuf<int32_t> n_hits, n_matched;
+    DevBuf<uint32_t> exact_list;
+    DevBuf<uint64_t> ring_h;
+    DevBuf<uint32_t> ring_p;
+    int ring_slots = 0;
+    int64_t acap = 0;
+    DevBuf<uint32_t> a_ref, a_qry;
+    DevBuf<int32_t> a_f, a_p, a_t, a_n;
+    DevBuf<unsigned long long> a_tmp;
+    DevBuf<int64_t> a_base;
+    DevBuf<uint32_t> ent_cnt;
+    int64_t scap = 0;
+    DevBuf<hg::Seg> seg;
+    DevBuf<int64_t> s_base;
+    DevBuf<int32_t> s_n, n_chain;
+    DevBuf<uint32_t> work_small, work_large;
+    int64_t dp_cap = 0;
+    DevBuf<uint8_t> dp_arena;
+    int64_t cig_cap = 0;
+    DevBuf<uint32_t> cig_seg, cig;
+    DevBuf<int32_t> n_cig;
+    DevBuf<uint8_t> has_ins;
+    DevBuf<uint8_t> rows;
+    DevBuf<uint32_t> counts, ins, status;
+    // control block: queues[8], cursors (a, s, dp), n_small, n_large
+    DevBuf<unsigned long long> control;
+    DevBuf<unsigned long long> cells;  // accumulated DP cells (GCUPS numerator)
+    // compaction
+    DevBuf<int64_t> cig_off;
+    DevBuf<uint32_t> cig_compact;
+    // staged full batch (device-resident form)
+    std::vector<SubPlan> staged_plan;
+    std::vector<int32_t> staged_qlen;
+    DevBuf<uint8_t> s_packed;
+    DevBuf<int64_t> s_poff, s_exc_off, s_hoff, s_coff;
+    DevBuf<int32_t> s_qlen, s_exc, s_order;
+    bool staged = false;
+    // staged outputs for fetch
+    DevBuf<int32_t> s_n_cig;
+    DevBuf<uint8_t> s_has_ins, s_rows;
+    DevBuf<uint32_t> s_status, s_cig;
+    DevBuf<int64_t> s_cigoff_dev;
+    int64_t s_cig_cap = 0;
+    // pinned staging for small per-query arrays
+    std::vector<int64_t> h_i64;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    bool timing = false;
+    cudaEvent_t ev[10] = {};
+    cudaEvent_t run_ev[2] = {};
+    bool run_recorded = false;
+    float last_total_ms = 0, last_stage_ms[8] = {};
+    int64_t last_launches = 0, last_cells = 0;
+};
+
+extern "C" const char* hg_last_error(void) { return g_err.c_str(); }
+
+extern "C" int hg_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+extern "C" void hg_default_params(hg_params_t* p)
+{
+    p->f_top_frac = 2e-4;
+    p->u_floor = 10;
+    p->u_ceil = 1000000;
+    p->q_occ_frac = 0.01;
+    p->sample_every_bp = 500;
+    p->max_dist_x = 5000;
+    p->max_dist_y = 5000;
+    p->bw = 500;
+    p->max_skip = 25;
+    p->max_iter = 5000;
+    p->min_cnt = 3;
+    p->min_score = 40;
+    p->gap_penalty = 0.01f;
+    p->skip_penalty = 0.01f;
+}
+
+// ------------------------------------------------------------------ packing
+
+extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint8_t* packed, int64_t packed_cap,
+                       int64_t* poff, int32_t* exc, int64_t exc_cap, int64_t* exc_off, int64_t* packed_bytes,
+                       int64_t* n_exc)
+{
+    if (n < 0 || !offsets) return fail(HG_ERR_ARG, "hg_pack: bad arguments");
+    int64_t pb = 0, ne = 0;
+    if (exc_off) exc_off[0] = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t len = offsets[i + 1] - offsets[i];
+        if (len < 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_pack: bad query length");
+        const int64_t nbytes = ((len + 3) / 4 + 15) / 16 * 16;
+        const unsigned char* s = reinterpret_cast<const unsigned char*>(seqs) + offsets[i];
+        if (packed) {
+            if (pb + nbytes > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
+            poff[i] = pb;
+            std::memset(packed + pb, 0, (size_t)nbytes);
+        }
+        int64_t run_start = -1;
+        unsigned char run_byte = 0;
+        for (int64_t j = 0; j < len; ++j) {
+            const unsigned char c = s[j];
+            uint32_t code = 4;
+            switch (c) {
+            case 'A': code = 0; break;
+            case 'C': code = 1; break;
+            case 'G': code = 2; break;
+            case 'T': code = 3; break;
+            default: break;
+            }
+            if (code < 4) {
+                if (packed) packed[pb + (j >> 2)] |= (uint8_t)(code << ((j & 3) * 2));
+                if (run_start >= 0) {
+                    if (packed) {
+                        if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
+                        exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(j - run_start),
+                                 exc[ne * 3 + 2] = run_byte;
+                    }
+                    ++ne;
+                    run_start = -1;
+                }
+            } else {
+                if (run_start >= 0 && c != run_byte) {
+                    if (packed) {
+                        if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
+                        exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(j - run_start),
+                                 exc[ne * 3 + 2] = run_byte;
+                    }
+                    ++ne;
+                    run_start = -1;
+                }
+                if (run_start < 0) run_start = j, run_byte = c;
+            }
+        }
+        if (run_start >= 0) {
+            if (packed) {
+                if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
+                exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(len - run_start), exc[ne * 3 + 2] = run_byte;
+            }
+            ++ne;
+        }
+        pb += nbytes;
+        if (exc_off) exc_off[i + 1] = ne;
+    }
+    if (packed_bytes) *packed_bytes = pb;
+    if (n_exc) *n_exc = ne;
+    return HG_OK;
+}
+
+// ------------------------------------------------------------------- index
+
+namespace {
+
+// Minimal one-query batch on a scratch context-free buffer set, used for the
+// center and for single-call extractMinimizer.
+int run_extract(int dev_k, int dev_w, int non_canonical, const char* seq, int64_t len, std::vector<uint64_t>& xs,
+                std::vector<uint64_t>& ys, cudaStream_t st)
+{
+    xs.clear(), ys.clear();
+    if (len < dev_k || dev_k <= 0 || dev_k > 31 || dev_w <= 0 || dev_w >= 256) return HG_OK;
+    const int64_t offs[2] = {0, len};
+    int64_t pbytes = 0, nexc = 0;
+    int r = hg_pack(seq, offs, 1, nullptr, 0, nullptr, nullptr, 0, nullptr, &pbytes, &nexc);
+    if (r) return r;
+    std::vector<uint8_t> pk((size_t)pbytes);
+    std::vector<int64_t> poff(1), eoff(2);
+    std::vector<int32_t> exc((size_t)std::max<int64_t>(nexc, 1) * 3);
+    r = hg_pack(seq, offs, 1, pk.data(), pbytes, poff.data(), exc.data(), nexc, eoff.data(), nullptr, nullptr);
+    if (r) return r;
+    const int64_t cap = len - dev_k + 1;
+    DevBuf<uint8_t> d_pk;
+    DevBuf<int64_t> d_poff, d_eoff, d_hoff;
+    DevBuf<int32_t> d_qlen, d_exc, d_nh, d_nm;
+    DevBuf<uint64_t> d_x, d_y;
+    DevBuf<uint32_t> d_status, d_exact;
+    DevBuf<unsigned int> d_q;
+    DevBuf<uint64_t> d_rh;
+    DevBuf<uint32_t> d_rp;
+    const int ring_slots = 2 * dev_w + 16;
+    HG_CUDA(d_exact.alloc(1));
+    HG_CUDA(d_rh.alloc((size_t)hg_exact_ring_threads() * ring_slots));
+    HG_CUDA(d_rp.alloc((size_t)hg_exact_ring_threads() * ring_slots));
+    HG_CUDA(d_pk.alloc(pk.size()));
+    HG_CUDA(d_poff.alloc(1));
+    HG_CUDA(d_eoff.alloc(2));
+    HG_CUDA(d_hoff.alloc(1));
+    HG_CUDA(d_qlen.alloc(1));
+    HG_CUDA(d_exc.alloc(exc.size()));
+    HG_CUDA(d_nh.alloc(1));
+    HG_CUDA(d_nm.alloc(1));
+    HG_CUDA(d_x.alloc(cap));
+    HG_CUDA(d_y.alloc(cap));
+    HG_CUDA(d_q.alloc(16));
+    HG_CUDA(cudaMemcpyAsync(d_pk.p, pk.data(), pk.size(), cudaMemcpyHostToDevice, st));
+    const int32_t ql = (int32_t)len;
+    const int64_t zero = 0;
+    HG_CUDA(cudaMemcpyAsync(d_poff.p, poff.data(), 8, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(d_eoff.p, eoff.data(), 16, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(d_hoff.p, &zero, 8, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(d_qlen.p, &ql, 4, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(d_exc.p, exc.data(), exc.size() * 4, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemsetAsync(d_q.p, 0, 64, st));
+    hg::IndexDev ixd{};
+    ixd.k = dev_k, ixd.w = dev_w, ixd.non_canonical = non_canonical;
+    hg::BatchDev bd{};
+    bd.n = 1, bd.packed = d_pk.p, bd.poff = d_poff.p, bd.qlen = d_qlen.p, bd.exc = d_exc.p, bd.exc_off = d_eoff.p;
+    bd.hoff = d_hoff.p, bd.n_hits = d_nh.p, bd.n_matched = d_nm.p, bd.queues = d_q.p;
+    bd.exact_list = d_exact.p, bd.n_exact = d_q.p + 8, bd.ring_h = d_rh.p, bd.ring_p = d_rp.p;
+    bd.ring_slots = ring_slots;
+    HG_CUDA(hg_launch_seed(&ixd, &bd, 1, d_x.p, d_y.p, 1, st));
+    int32_t nh = 0;
+    HG_CUDA(cudaMemcpyAsync(&nh, d_nh.p, 4, cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaStreamSynchronize(st));
+    xs.resize(nh), ys.resize(nh);
+    if (nh) {
+        HG_CUDA(cudaMemcpy(xs.data(), d_x.p, 8 * (size_t)nh, cudaMemcpyDeviceToHost));
+        HG_CUDA(cudaMemcpy(ys.data(), d_y.p, 8 * (size_t)nh, cudaMemcpyDeviceToHost));
+    }
+    return HG_OK;
+}
+
+uint64_t occ_threshold(std::vector<uint64_t> occs, const hg_params_t& p)
+{  // compute_ref_occ_threshold (src/seed/anchor.cpp:73-117)
+    uint64_t f_cut;
+    if (occs.empty() || p.f_top_frac <= 0.0) f_cut = UINT64_MAX;
+    else if (p.f_top_frac >= 1.0) f_cut = 1;
+    else {
+        const uint64_t n_skip = (uint64_t)std::floor(p.f_top_frac * (double)occs.size());
+        if (n_skip == 0) f_cut = UINT64_MAX;
+        else {
+            std::nth_element(occs.begin(), occs.begin() + (n_skip - 1), occs.end(), std::greater<uint64_t>());
+            f_cut = occs[n_skip - 1];
+        }
+    }
+    const uint64_t capped = std::min(p.u_ceil, f_cut);
+    return std::max(p.u_floor, capped);
+}
+
+}  // namespace
+
+extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params,
+                               hg_index_t** out)
+{
+    if (!out || !center || len <= 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_index_create: bad arguments");
+    if (k <= 0 || k > 31 || w <= 0 || w >= 256) return fail(HG_ERR_ARG, "hg_index_create: need 0<k<=31, 0<w<256");
+    if (hg_device_count() <= 0) return fail(HG_ERR_CUDA, "hg_index_create: no CUDA device");
+    auto* ix = new hg_index();
+    cudaGetDevice(&ix->device);
+    ix->k = k, ix->w = w;
+    if (params) ix->prm = *params;
+    else hg_default_params(&ix->prm);
+    ix->center_raw.assign(center, (size_t)len);
+    ix->L = (int)len;
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        delete ix;
+        return fail(HG_ERR_CUDA, "hg_index_create: stream");
+    }
+    std::vector<uint64_t> xs, ys;
+    int r = run_extract(k, w, 1, center, len, xs, ys, st);
+    cudaStreamDestroy(st);
+    if (r) {
+        delete ix;
+        return r;
+    }
+    ix->n_hits = (int64_t)xs.size();
+    // group by (hash, rid, pos, strand) = (hash, pos) for one forward center
+    std::vector<uint32_t> idx(xs.size());
+    std::iota(idx.begin(), idx.end(), 0u);
+    std::stable_sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+        const uint64_t ha = xs[a] >> 8, hb = xs[b] >> 8;
+        if (ha != hb) return ha < hb;
+        return (uint32_t)ys[a] < (uint32_t)ys[b];
+    });
+    std::vector<uint32_t> cpos(idx.size()), cspan(idx.size()), est, ecnt;
+    std::vector<uint64_t> ekey, occs;
+    for (size_t i = 0; i < idx.size(); ++i) {
+        cpos[i] = (uint32_t)ys[idx[i]];
+        cspan[i] = (uint32_t)(xs[idx[i]] & 0xff);
+        const uint64_t h = xs[idx[i]] >> 8;
+        if (i == 0 || h != ekey.back()) {
+            ekey.push_back(h);
+            est.push_back((uint32_t)i);
+            ecnt.push_back(0);
+        }
+        ecnt.back()++;
+    }
+    for (auto c : ecnt) occs.push_back(c);
+    ix->occ_thr = occ_threshold(occs, ix->prm);
+    std::vector<uint8_t> over(ekey.size());
+    for (size_t e = 0; e < ekey.size(); ++e) over[e] = ecnt[e] > ix->occ_thr ? 1 : 0;
+    uint32_t tsize = 16;
+    while (tsize < 2 * ekey.size() + 16) tsize <<= 1;
+    std::vector<uint64_t> tkey(tsize, hg::kNoHash);
+    std::vector<uint32_t> tval(tsize, 0);
+    for (size_t e = 0; e < ekey.size(); ++e) {
+        uint32_t s = (uint32_t)ekey[e] & (tsize - 1);
+        while (tkey[s] != hg::kNoHash) s = (s + 1) & (tsize - 1);
+        tkey[s] = ekey[e], tval[s] = (uint32_t)e;
+    }
+    // DP center (consensus of the single record) in DNA5 codes
+    std::vector<uint8_t> cdp((size_t)len);
+    for (int64_t i = 0; i < len; ++i) cdp[i] = hg::dna5_of(consensus_letter((uint8_t)center[i]));
+    // log2f table for the chain penalty (arguments 2 .. bw+1)
+    const int nlog = std::max(ix->prm.bw + 2, 513);
+    std::vector<float> lg((size_t)nlog);
+    for (int i = 0; i < nlog; ++i) lg[i] = i >= 1 ? (float)std::log2((double)i) : 0.0f;
+    auto up = [&](auto& buf, const auto& v) -> cudaError_t {
+        cudaError_t e = buf.alloc(std::max<size_t>(v.size(), 1));
+        if (e != cudaSuccess) return e;
+        return v.empty() ? cudaSuccess
+                         : cudaMemcpy(buf.p, v.data(), sizeof(v[0]) * v.size(), cudaMemcpyHostToDevice);
+    };
+    cudaError_t e = cudaSuccess;
+    if ((e = up(ix->center, cdp)) || (e = up(ix->tab_key, tkey)) || (e = up(ix->tab_val, tval)) ||
+        (e = up(ix->ent_start, est)) || (e = up(ix->ent_count, ecnt)) || (e = up(ix->ent_over, over)) ||
+        (e = up(ix->cpos, cpos)) || (e = up(ix->cspan, cspan)) || (e = up(ix->log2tab, lg))) {
+        delete ix;
+        return cuda_fail(e, "hg_index_create: upload");
+    }
+    hg::IndexDev& d = ix->dev;
+    d.L = (int)len, d.k = k, d.w = w, d.non_canonical = 1;
+    d.center = ix->center.p;
+    d.tab_key = ix->tab_key.p, d.tab_val = ix->tab_val.p, d.tab_mask = tsize - 1;
+    d.n_ent = (uint32_t)ekey.size();
+    d.ent_start = ix->ent_start.p, d.ent_count = ix->ent_count.p, d.ent_over = ix->ent_over.p;
+    d.cpos = ix->cpos.p, d.cspan = ix->cspan.p;
+    d.q_occ_frac = ix->prm.q_occ_frac, d.sample_every = ix->prm.sample_every_bp;
+    d.max_dist_x = ix->prm.max_dist_x, d.max_dist_y = ix->prm.max_dist_y, d.bw = ix->prm.bw;
+    d.max_skip = ix->prm.max_skip, d.max_iter = ix->prm.max_iter, d.min_cnt = ix->prm.min_cnt;
+    d.min_score = ix->prm.min_score, d.gap_pen = ix->prm.gap_penalty, d.skip_pen = ix->prm.skip_penalty;
+    d.log2tab = ix->log2tab.p, d.n_log2 = nlog;
+    *out = ix;
+    return HG_OK;
+}
+
+extern "C" void hg_index_destroy(hg_index_t* ix)
+{
+    if (!ix) return;
+    if (ix->single) hg_ctx_destroy(ix->single);
+    ix->center.free(), ix->tab_key.free(), ix->tab_val.free(), ix->ent_start.free(), ix->ent_count.free();
+    ix->ent_over.free(), ix->cpos.free(), ix->cspan.free(), ix->log2tab.free();
+    delete ix;
+}
+
+extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t* n_hits, uint64_t* occ_threshold)
+{
+    if (!ix) return fail(HG_ERR_ARG, "hg_index_info: null index");
+    if (n_distinct) *n_distinct = ix->dev.n_ent;
+    if (n_hits) *n_hits = ix->n_hits;
+    if (occ_threshold) *occ_threshold = ix->occ_thr;
+    return HG_OK;
+}
+
+// ----------------------------------------------------------------- context
+
+namespace {
+
+constexpr int kControlWords = 16;  // queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact
+
+__global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
+{
+    // single CTA exclusive scan over n entries
+    __shared__ int64_t part[1024];
+    const int tid = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    const int i0 = min(tid * per, n), i1 = min(i0 + per, n);
+    int64_t s = 0;
+    for (int i = i0; i < i1; ++i) s += n_cig[i];
+    part[tid] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const int64_t v = tid >= o ? part[tid - o] : 0;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    int64_t run = part[tid] - s;
+    for (int i = i0; i < i1; ++i) {
+        off[i] = run;
+        run += n_cig[i];
+    }
+    if (tid == 1023) off[n] = part[1023];
+}
+
+__global__ void compact_copy_kernel(const uint32_t* cig, const int64_t* coff, const int32_t* n_cig,
+                                    const int64_t* off, int n, uint32_t* out, int64_t out_cap, int64_t out_base)
+{
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    for (int q = w; q < n; q += nw) {
+        const int64_t o = off[q] - out_base;
+        const int m = n_cig[q];
+        for (int i = lane; i < m; i += 32)
+            if (o + i >= 0 && o + i < out_cap) out[o + i] = cig[coff[q] + i];
+    }
+}
+
+size_t padded_bytes(int64_t len) { return (size_t)(((len + 3) / 4 + 15) / 16 * 16); }
+
+}  // namespace
+
+extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_bases, hg_ctx_t** out)
+{
+    if (!ix || !out || max_queries <= 0 || max_bases <= 0) return fail(HG_ERR_ARG, "hg_ctx_create: bad arguments");
+    auto* c = new hg_ctx();
+    c->ix = ix;
+    cudaSetDevice(ix->device);
+    if (cudaError_t pe = hg_prepare_kernels()) {
+        delete c;
+        return cuda_fail(pe, "hg_ctx_create: kernel attributes");
+    }
+    c->sms = sm_count(ix->device);
+    c->max_n = max_queries, c->max_bases = max_bases;
+    c->exc_cap = max_bases / 16 + 4096;
+    const int64_t L = ix->L;
+    c->row_stride = (L + 15) / 16 * 16;
+    c->acap = max_bases / 4 + 65536;
+    c->scap = max_bases / 2 + 4 * max_queries + 65536;
+    c->dp_cap = std::max<int64_t>((int64_t)1 << 30, max_bases * 4);
+    c->cig_cap = max_bases + max_queries * (L + 4);
+    const int64_t n_ent = ix->dev.n_ent;
+    const int grid_anchor = c->sms * 3;
+    cudaError_t e = cudaSuccess;
+    if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) ||
+        (e = c->packed.alloc(max_bases / 4 + 16 * max_queries + 64)) || (e = c->poff.alloc(max_queries)) ||
+        (e = c->exc_off.alloc(max_queries + 1)) || (e = c->hoff.alloc(max_queries)) ||
+        (e = c->coff.alloc(max_queries)) || (e = c->qlen.alloc(max_queries)) ||
+        (e = c->exc.alloc(c->exc_cap * 3)) || (e = c->order.alloc(max_queries)) ||
+        (e = c->hit_pos.alloc(max_bases)) || (e = c->hit_ent.alloc(max_bases)) ||
+        (e = c->n_hits.alloc(max_queries)) || (e = c->n_matched.alloc(max_queries)) ||
+        (e = c->exact_list.alloc(max_queries)) ||
+        (e = c->ring_h.alloc((size_t)hg_exact_ring_threads() * (2 * ix->w + 16))) ||
+        (e = c->ring_p.alloc((size_t)hg_exact_ring_threads() * (2 * ix->w + 16))) ||
+        (e = c->a_ref.alloc(c->acap)) || (e = c->a_qry.alloc(c->acap)) || (e = c->a_f.alloc(c->acap)) ||
+        (e = c->a_p.alloc(c->acap)) || (e = c->a_t.alloc(c->acap)) || (e = c->a_tmp.alloc(2 * c->acap)) ||
+        (e = c->a_base.alloc(max_queries)) || (e = c->a_n.alloc(max_queries)) ||
+        (e = c->ent_cnt.alloc(n_ent > 8192 ? (size_t)grid_anchor * n_ent : 1)) || (e = c->seg.alloc(c->scap)) ||
+        (e = c->s_base.alloc(max_queries)) || (e = c->s_n.alloc(max_queries)) ||
+        (e = c->n_chain.alloc(max_queries)) || (e = c->work_small.alloc(c->scap)) ||
+        (e = c->work_large.alloc(c->scap)) || (e = c->dp_arena.alloc(c->dp_cap)) ||
+        (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
+        (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
+        (e = c->rows.alloc((size_t)max_queries * c->row_stride)) || (e = c->counts.alloc(L * 7)) ||
+        (e = c->ins.alloc(L + 1)) || (e = c->status.alloc(max_queries)) || (e = c->control.alloc(kControlWords)) || (e = c->cells.alloc(1)) ||
+        (e = c->cig_off.alloc(max_queries + 1)) || (e = c->cig_compact.alloc(max_bases / 4 + 1024))) {
+        hg_ctx_destroy(c);
+        return cuda_fail(e, "hg_ctx_create: device allocation");
+    }
+    if (n_ent > 8192 && (e = cudaMemset(c->ent_cnt.p, 0, sizeof(uint32_t) * (size_t)grid_anchor * n_ent))) {
+        hg_ctx_destroy(c);
+        return cuda_fail(e, "hg_ctx_create: memset");
+    }
+    cudaMemset(c->counts.p, 0, sizeof(uint32_t) * L * 7);
+    cudaMemset(c->cells.p, 0, sizeof(unsigned long long));
+    cudaMemset(c->ins.p, 0, sizeof(uint32_t) * (L + 1));
+    for (auto& ev : c->ev) cudaEventCreate(&ev);
+    for (auto& ev : c->run_ev) cudaEventCreate(&ev);
+    *out = c;
+    return HG_OK;
+}
+
+extern "C" void hg_ctx_destroy(hg_ctx_t* c)
+{
+    if (!c) return;
+    if (c->st) cudaStreamSynchronize(c->st);
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    for (auto& ev : c->ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto& ev : c->run_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;  // DevBuf members are freed below via explicit frees
+}
+
+namespace {
+
+// Plan sub-batches bounded by the context capacities.
+std::vector<SubPlan> plan(hg_ctx_t* c, const int64_t* poff, const int32_t* qlen, const int64_t* exc_off, int64_t n)
+{
+    std::vector<SubPlan> out;
+    int64_t i = 0;
+    while (i < n) {
+        SubPlan p{i, 0, 0, 0, 0};
+        while (i < n) {
+            const int64_t b = qlen[i], by = (int64_t)padded_bytes(qlen[i]), ex = exc_off[i + 1] - exc_off[i];
+            if (p.n > 0 && (p.n + 1 > c->max_n || p.bases + b > c->max_bases ||
+                            p.bytes + by > (int64_t)c->packed.n || p.excs + ex > c->exc_cap))
+                break;
+            p.n++, p.bases += b, p.bytes += by, p.excs += ex, ++i;
+        }
+        out.push_back(p);
+    }
+    (void)poff;
+    return out;
+}
+
+hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                        const int32_t* exc, const int64_t* exc_off, const int32_t* order, const int64_t* hoff,
+                        const int64_t* coff)
+{
+    hg::BatchDev b;
+    std::memset(&b, 0, sizeof(b));  // graph cache keys compare the raw bytes
+    b.n = n;
+    b.packed = packed, b.poff = poff, b.qlen = qlen, b.exc = exc, b.exc_off = exc_off, b.order = order;
+    b.hoff = hoff, b.hit_pos = c->hit_pos.p, b.hit_ent = c->hit_ent.p, b.n_hits = c->n_hits.p,
+    b.n_matched = c->n_matched.p;
+    b.exact_list = c->exact_list.p, b.ring_h = c->ring_h.p, b.ring_p = c->ring_p.p;
+    b.ring_slots = 2 * c->ix->w + 16;
+    b.a_ref = c->a_ref.p, b.a_qry = c->a_qry.p, b.a_f = c->a_f.p, b.a_p = c->a_p.p, b.a_t = c->a_t.p,
+    b.a_tmp = c->a_tmp.p;
+    b.acap = c->acap;
+    unsigned long long* ctl = c->control.p;
+    b.queues = reinterpret_cast<unsigned int*>(ctl);  // 8 x uint32 in words 0..3
+    b.a_cursor = ctl + 4, b.s_cursor = ctl + 5, b.dp_cursor = ctl + 6;
+    b.n_small = reinterpret_cast<unsigned int*>(ctl + 7);
+    b.n_large = reinterpret_cast<unsigned int*>(ctl + 8);
+    b.n_exact = reinterpret_cast<unsigned int*>(ctl + 9);
+    b.cells = c->cells.p;
+    b.a_base = c->a_base.p, b.a_n = c->a_n.p, b.ent_cnt = c->ent_cnt.p;
+    b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
+    b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
+    b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
+    b.coff = coff, b.cig_seg = c->cig_seg.p, b.cig = c->cig.p, b.n_cig = c->n_cig.p, b.has_ins = c->has_ins.p;
+    b.rows = c->rows.p, b.counts = c->counts.p, b.ins = c->ins.p, b.status = c->status.p;
+    return b;
+}
+
+const char* kStageNames[8] = {"seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count"};
+
+// Enqueue the stage sequence of one sub-batch.
+int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
+{
+    const hg::IndexDev& ix = c->ix->dev;
+    const int S = c->sms;
+    cudaStream_t st = c->st;
+    HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, st));
+    HG_CUDA(cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * (size_t)b.n, st));
+    const int n = b.n;
+    auto mark = [&](int i) -> cudaError_t { return timed ? cudaEventRecord(c->ev[i], st) : cudaSuccess; };
+    HG_CUDA(mark(0));
+    HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, std::min(n, S * 6), st));
+    HG_CUDA(mark(1));
+    HG_CUDA(hg_launch_anchor(&ix, &b, std::min(n, S * 3), st));
+    HG_CUDA(mark(2));
+    HG_CUDA(hg_launch_chain(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 12)), st));
+    HG_CUDA(mark(3));
+    HG_CUDA(hg_launch_dp_small(&ix, &b, S * 8, st));
+    HG_CUDA(mark(4));
+    HG_CUDA(hg_launch_dp_large(&ix, &b, S * 4, st));
+    HG_CUDA(mark(5));
+    HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 8)), st));
+    HG_CUDA(mark(6));
+    HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, std::min(n, S * 4), st));
+    HG_CUDA(mark(7));
+    HG_CUDA(hg_launch_count(c->rows.p, c->row_stride, n, ix.L, c->counts.p, st));
+    HG_CUDA(mark(8));
+    (void)kStageNames;
+    return HG_OK;
+}
+
+int run_sub(hg_ctx_t* c, const hg::BatchDev& b, bool use_graph)
+{
+    if (c->timing || !use_graph) {
+        int r = enqueue_stages(c, b, c->timing);
+        if (r) return r;
+        if (c->timing) {
+            HG_CUDA(cudaEventSynchronize(c->ev[8]));
+            float tot = 0;
+            for (int i = 0; i < 8; ++i) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, c->ev[i], c->ev[i + 1]);
+                c->last_stage_ms[i] += ms;
+                tot += ms;
+            }
+            c->last_total_ms += tot;
+        }
+        c->last_launches += 9;
+        return HG_OK;
+    }
+    GraphKey key{b};
+    auto it = c->graphs.find(key);
+    if (it == c->graphs.end()) {
+        cudaGraph_t g;
+        HG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        int r = enqueue_stages(c, b, false);
+        cudaError_t e = cudaStreamEndCapture(c->st, &g);
+        if (r) return r;
+        if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+        cudaGraphExec_t ge;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+        it = c->graphs.emplace(key, ge).first;
+    }
+    HG_CUDA(cudaGraphLaunch(it->second, c->st));
+    c->last_launches += 9;
+    return HG_OK;
+}
+
+// Host-side per-query arrays of a sub-batch.
+void sub_arrays(hg_ctx_t* c, const int32_t* qlen, int64_t n, std::vector<int32_t>& order, std::vector<int64_t>& hoff,
+                std::vector<int64_t>& coff)
+{
+    const int k = c->ix->k;
+    const int64_t L = c->ix->L;
+    order.resize(n), hoff.resize(n), coff.resize(n);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return qlen[a] > qlen[b]; });
+    int64_t h = 0, co = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        hoff[i] = h;
+        h += std::max<int64_t>(qlen[i] - k + 1, 0);
+        coff[i] = co;
+        co += qlen[i] + L + 4;
+    }
+}
+
+// Copy back outputs of a finished sub-batch (compacted CIGARs).
+int fetch_outputs(hg_ctx_t* c, int n, const int64_t* d_coff, uint32_t* cigar, int64_t cigar_cap, int64_t cig_base, int64_t* cigar_off,
+                  uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status, int64_t* total_out)
+{
+    compact_offsets_kernel<<<1, 1024, 0, c->st>>>(c->n_cig.p, n, c->cig_off.p);
+    HG_CUDA(cudaGetLastError());
+    std::vector<int64_t> off((size_t)n + 1);
+    HG_CUDA(cudaMemcpyAsync(off.data(), c->cig_off.p, 8 * ((size_t)n + 1), cudaMemcpyDeviceToHost, c->st));
+    if (status) HG_CUDA(cudaMemcpyAsync(status, c->status.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->st));
+    if (has_ins) HG_CUDA(cudaMemcpyAsync(has_ins, c->has_ins.p, (size_t)n, cudaMemcpyDeviceToHost, c->st));
+    if (rows) {
+        const int64_t L = c->ix->L;
+        HG_CUDA(cudaMemcpy2DAsync(rows, (size_t)row_stride, c->rows.p, (size_t)c->row_stride, (size_t)L, (size_t)n,
+                                  cudaMemcpyDeviceToHost, c->st));
+    }
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    const int64_t total = off[n];
+    if (cig_base + total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_align_batch: cigar buffer too small");
+    // copy in pieces through the compact buffer
+    const int64_t piece = (int64_t)c->cig_compact.n;
+    for (int64_t done = 0; done < total; done += piece) {
+        const int64_t m = std::min(piece, total - done);
+        compact_copy_kernel<<<c->sms * 4, 256, 0, c->st>>>(c->cig.p, d_coff, c->n_cig.p, c->cig_off.p, n,
+                                                           c->cig_compact.p, m, done);
+        HG_CUDA(cudaGetLastError());
+        HG_CUDA(cudaMemcpyAsync(cigar + cig_base + done, c->cig_compact.p, 4 * (size_t)m, cudaMemcpyDeviceToHost,
+                                c->st));
+    }
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    for (int i = 0; i <= n; ++i) cigar_off[i] = cig_base + off[i];
+    *total_out = total;
+    return HG_OK;
+}
+
+int status_error(const uint32_t* status, int64_t n)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        if (status[i] & HG_ST_ARENA_OVERFLOW)
+            return fail(HG_ERR_CAPACITY, "query " + std::to_string(i) + ": device arena overflow (raise the context capacity)");
+        if (status[i] & HG_ST_CIGAR_OVERFLOW) return fail(HG_ERR_CIGAR, "query " + std::to_string(i) + ": CIGAR length overflow");
+        if (status[i] & (HG_ST_LENGTH_MISMATCH | HG_ST_PARTIAL_CIGAR))
+            return fail(HG_ERR_LENGTH_MISMATCH,
+                        "Sequence length mismatch: query " + std::to_string(i) + " does not span the center");
+    }
+    return HG_OK;
+}
+
+int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
+               const int64_t* exc_off, int64_t n, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off,
+               uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status, bool plain)
+{
+    if (!c || n < 0 || (n && (!packed || !poff || !qlen || !exc_off || !cigar || !cigar_off)))
+        return fail(HG_ERR_ARG, "hg_align_batch: bad arguments");
+    if (rows && row_stride < c->ix->L) return fail(HG_ERR_ARG, "hg_align_batch: row_stride < center length");
+    cudaSetDevice(c->ix->device);
+    std::vector<uint32_t> st_local;
+    if (!status) st_local.resize((size_t)n), status = st_local.data();
+    int64_t cig_base = 0;
+    if (n == 0) {
+        cigar_off[0] = 0;
+        return HG_OK;
+    }
+    const auto plans = plan(c, poff, qlen, exc_off, n);
+    std::vector<int32_t> order;
+    std::vector<int64_t> hoff, coff, spoff, seoff;
+    for (const SubPlan& sp : plans) {
+        const int64_t f = sp.first;
+        if (sp.n > c->max_n || sp.bases > c->max_bases)
+            return fail(HG_ERR_CAPACITY, "query " + std::to_string(f) + " exceeds the context capacity");
+        sub_arrays(c, qlen + f, sp.n, order, hoff, coff);
+        spoff.resize(sp.n), seoff.resize(sp.n + 1);
+        int64_t pb = 0;
+        for (int64_t i = 0; i < sp.n; ++i) spoff[i] = pb, pb += (int64_t)padded_bytes(qlen[f + i]);
+        for (int64_t i = 0; i <= sp.n; ++i) seoff[i] = exc_off[f + i] - exc_off[f];
+        // inputs: per-query packed blocks may be scattered in the caller's buffer
+        bool contiguous = true;
+        for (int64_t i = 1; i < sp.n && contiguous; ++i) contiguous = poff[f + i] == poff[f] + spoff[i];
+        if (contiguous) {
+            HG_CUDA(cudaMemcpyAsync(c->packed.p, packed + poff[f], (size_t)pb, cudaMemcpyHostToDevice, c->st));
+        } else {
+            for (int64_t i = 0; i < sp.n; ++i)
+                HG_CUDA(cudaMemcpyAsync(c->packed.p + spoff[i], packed + poff[f + i], padded_bytes(qlen[f + i]),
+                                        cudaMemcpyHostToDevice, c->st));
+        }
+        const int64_t ne = seoff[sp.n];
+        if (ne) HG_CUDA(cudaMemcpyAsync(c->exc.p, exc + 3 * exc_off[f], 12 * (size_t)ne, cudaMemcpyHostToDevice, c->st));
+        HG_CUDA(cudaMemcpyAsync(c->poff.p, spoff.data(), 8 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
+        HG_CUDA(cudaMemcpyAsync(c->qlen.p, qlen + f, 4 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
+        HG_CUDA(cudaMemcpyAsync(c->exc_off.p, seoff.data(), 8 * ((size_t)sp.n + 1), cudaMemcpyHostToDevice, c->st));
+        HG_CUDA(cudaMemcpyAsync(c->order.p, order.data(), 4 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
+        HG_CUDA(cudaMemcpyAsync(c->hoff.p, hoff.data(), 8 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
+        HG_CUDA(cudaMemcpyAsync(c->coff.p, coff.data(), 8 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
+        if (!plain) {
+            const hg::BatchDev b = batch_view(c, (int)sp.n, c->packed.p, c->poff.p, c->qlen.p, c->exc.p,
+                                              c->exc_off.p, c->order.p, c->hoff.p, c->coff.p);
+            int r = run_sub(c, b, true);
+            if (r) return r;
+        } else {
+            // one launch sequence per query: a one-query view of the same buffers
+            for (int64_t i = 0; i < sp.n; ++i) {
+                hg::BatchDev b = batch_view(c, 1, c->packed.p, c->poff.p + i, c->qlen.p + i, c->exc.p,
+                                            c->exc_off.p + i, nullptr, c->hoff.p + i, c->coff.p + i);
+                // per-query outputs land at index 0 of the view: shift the output arrays
+                b.n_hits = c->n_hits.p + i, b.n_matched = c->n_matched.p + i, b.a_base = c->a_base.p + i,
+                b.a_n = c->a_n.p + i, b.s_base = c->s_base.p + i, b.s_n = c->s_n.p + i, b.n_chain = c->n_chain.p + i;
+                b.n_cig = c->n_cig.p + i, b.has_ins = c->has_ins.p + i, b.status = c->status.p + i;
+                b.rows = c->rows.p + i * c->row_stride;
+                if (i == 0) HG_CUDA(cudaMemsetAsync(c->status.p, 0, 4 * (size_t)sp.n, c->st));
+                // status must survive the per-launch reset: enqueue without the batch memset
+                HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, c->st));
+                const hg::IndexDev& ix = c->ix->dev;
+                HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, 1, c->st));
+                HG_CUDA(hg_launch_anchor(&ix, &b, 1, c->st));
+                HG_CUDA(hg_launch_chain(&ix, &b, 1, c->st));
+                HG_CUDA(hg_launch_dp_small(&ix, &b, c->sms, c->st));
+                HG_CUDA(hg_launch_dp_large(&ix, &b, c->sms, c->st));
+                HG_CUDA(hg_launch_stitch(&ix, &b, 1, c->st));
+                HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, 1, c->st));
+                HG_CUDA(hg_launch_count(b.rows, c->row_stride, 1, ix.L, c->counts.p, c->st));
+                c->last_launches += 9;
+            }
+        }
+        int64_t total = 0;
+        int r = fetch_outputs(c, (int)sp.n, c->coff.p, cigar, cigar_cap, cig_base, cigar_off + f,
+                              has_ins ? has_ins + f : nullptr, rows ? rows + f * row_stride : nullptr, row_stride,
+                              status + f, &total);
+        if (r) return r;
+        cig_base += total;
+    }
+    return status_error(status, n);
+}
+
+}  // namespace
+
+extern "C" int hg_align_batch(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                              const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar,
+                              int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows,
+                              int64_t row_stride, uint32_t* status)
+{
+    return align_impl(ctx, packed, poff, qlen, exc, exc_off, n, cigar, cigar_cap, cigar_off, has_ins, rows,
+                      row_stride, status, false);
+}
+
+extern "C" int hg_align_plain(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                              const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar,
+                              int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows,
+                              int64_t row_stride, uint32_t* status)
+{
+    return align_impl(ctx, packed, poff, qlen, exc, exc_off, n, cigar, cigar_cap, cigar_off, has_ins, rows,
+                      row_stride, status, true);
+}
+
+extern "C" int hg_counters(hg_ctx_t* c, uint32_t* counts7, uint32_t* ins, int reset)
+{
+    if (!c) return fail(HG_ERR_ARG, "hg_counters: null context");
+    const int64_t L = c->ix->L;
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    if (counts7) HG_CUDA(cudaMemcpy(counts7, c->counts.p, 4 * (size_t)L * 7, cudaMemcpyDeviceToHost));
+    if (ins) HG_CUDA(cudaMemcpy(ins, c->ins.p, 4 * (size_t)(L + 1), cudaMemcpyDeviceToHost));
+    if (reset) {
+        HG_CUDA(cudaMemset(c->counts.p, 0, 4 * (size_t)L * 7));
+        HG_CUDA(cudaMemset(c->ins.p, 0, 4 * (size_t)(L + 1)));
+    }
+    return HG_OK;
+}
+
+// ------------------------------------------------------- device-resident form
+
+extern "C" int hg_stage(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                        const int32_t* exc, const int64_t* exc_off, int64_t n)
+{
+    if (!c || n <= 0) return fail(HG_ERR_ARG, "hg_stage: bad arguments");
+    cudaSetDevice(c->ix->device);
+    c->staged_plan = plan(c, poff, qlen, exc_off, n);
+    c->staged_qlen.assign(qlen, qlen + n);
+    int64_t pb = 0;
+    std::vector<int64_t> spoff(n), seoff(n + 1), hoff(n), coff(n);
+    std::vector<int32_t> order(n);
+    for (int64_t i = 0; i < n; ++i) spoff[i] = pb, pb += (int64_t)padded_bytes(qlen[i]);
+    for (int64_t i = 0; i <= n; ++i) seoff[i] = exc_off[i] - exc_off[0];
+    // per sub-batch: local order / hit / cigar offsets, kept in one array
+    for (const SubPlan& sp : c->staged_plan) {
+        std::vector<int32_t> o;
+        std::vector<int64_t> h, co;
+        sub_arrays(c, qlen + sp.first, sp.n, o, h, co);
+        for (int64_t i = 0; i < sp.n; ++i) order[sp.first + i] = o[i], hoff[sp.first + i] = h[i], coff[sp.first + i] = co[i];
+    }
+    const int64_t ne = seoff[n];
+    cudaError_t e = cudaSuccess;
+    if ((e = c->s_packed.alloc(pb)) || (e = c->s_poff.alloc(n)) || (e = c->s_exc_off.alloc(n + 1)) ||
+        (e = c->s_hoff.alloc(n)) || (e = c->s_coff.alloc(n)) || (e = c->s_qlen.alloc(n)) ||
+        (e = c->s_exc.alloc(std::max<int64_t>(ne, 1) * 3)) || (e = c->s_order.alloc(n)))
+        return cuda_fail(e, "hg_stage: allocation");
+    bool contiguous = true;
+    for (int64_t i = 1; i < n && contiguous; ++i) contiguous = poff[i] == poff[0] + spoff[i];
+    if (contiguous) HG_CUDA(cudaMemcpy(c->s_packed.p, packed + poff[0], (size_t)pb, cudaMemcpyHostToDevice));
+    else
+        for (int64_t i = 0; i < n; ++i)
+            HG_CUDA(cudaMemcpy(c->s_packed.p + spoff[i], packed + poff[i], padded_bytes(qlen[i]), cudaMemcpyHostToDevice));
+    if (ne) HG_CUDA(cudaMemcpy(c->s_exc.p, exc + 3 * exc_off[0], 12 * (size_t)ne, cudaMemcpyHostToDevice));
+    HG_CUDA(cudaMemcpy(c->s_poff.p, spoff.data(), 8 * n, cudaMemcpyHostToDevice));
+    HG_CUDA(cudaMemcpy(c->s_exc_off.p, seoff.data(), 8 * (n + 1), cudaMemcpyHostToDevice));
+    HG_CUDA(cudaMemcpy(c->s_hoff.p, hoff.data(), 8 * n, cudaMemcpyHostToDevice));
+    HG_CUDA(cudaMemcpy(c->s_coff.p, coff.data(), 8 * n, cudaMemcpyHostToDevice));
+    HG_CUDA(cudaMemcpy(c->s_qlen.p, qlen, 4 * n, cudaMemcpyHostToDevice));
+    HG_CUDA(cudaMemcpy(c->s_order.p, order.data(), 4 * n, cudaMemcpyHostToDevice));
+    c->staged = true;
+    return HG_OK;
+}
+
+extern "C" int hg_set_timing(hg_ctx_t* c, int on)
+{
+    if (!c) return fail(HG_ERR_ARG, "hg_set_timing: null context");
+    c->timing = on != 0;
+    return HG_OK;
+}
+
+extern "C" int hg_run_staged(hg_ctx_t* c)
+{
+    if (!c || !c->staged) return fail(HG_ERR_ARG, "hg_run_staged: nothing staged");
+    cudaSetDevice(c->ix->device);
+    c->last_total_ms = 0;
+    std::fill(c->last_stage_ms, c->last_stage_ms + 8, 0.0f);
+    c->last_launches = 0;
+    HG_CUDA(cudaMemsetAsync(c->cells.p, 0, sizeof(unsigned long long), c->st));
+    HG_CUDA(cudaEventRecord(c->run_ev[0], c->st));
+    for (const SubPlan& sp : c->staged_plan) {
+        const int64_t f = sp.first;
+        // exception offsets of the sub-batch are global: rebase through exc_off view
+        const hg::BatchDev b = batch_view(c, (int)sp.n, c->s_packed.p, c->s_poff.p + f, c->s_qlen.p + f, c->s_exc.p,
+                                          c->s_exc_off.p + f, c->s_order.p + f, c->s_hoff.p + f, c->s_coff.p + f);
+        int r = run_sub(c, b, true);
+        if (r) return r;
+    }
+    HG_CUDA(cudaEventRecord(c->run_ev[1], c->st));
+    c->run_recorded = true;
+    return HG_OK;
+}
+
+extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int64_t* launches, int64_t* cells)
+{
+    if (!c) return fail(HG_ERR_ARG, "hg_last_timing: null context");
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    float tot = c->last_total_ms;
+    if (!c->timing && c->run_recorded) HG_CUDA(cudaEventElapsedTime(&tot, c->run_ev[0], c->run_ev[1]));
+    if (total_ms) *total_ms = tot;
+    if (stage_ms) std::copy(c->last_stage_ms, c->last_stage_ms + 8, stage_ms);
+    if (launches) *launches = c->last_launches;
+    if (cells) {
+        unsigned long long v = 0;
+        HG_CUDA(cudaMemcpy(&v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
+        *cells = (int64_t)v;
+    }
+    return HG_OK;
+}
+
+extern "C" int hg_fetch_staged(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
+                               uint8_t* rows, int64_t row_stride, uint32_t* status)
+{
+    if (!c || !c->staged) return fail(HG_ERR_ARG, "hg_fetch_staged: nothing staged");
+    if (c->staged_plan.size() != 1)
+        return fail(HG_ERR_ARG, "hg_fetch_staged: staged batch spans several sub-batches; fetch needs one");
+    const SubPlan& sp = c->staged_plan[0];
+    int64_t total = 0;
+    return fetch_outputs(c, (int)sp.n, c->s_coff.p, cigar, cigar_cap, 0, cigar_off, has_ins, rows, row_stride,
+                         status, &total);
+}
+
+// ---------------------------------------------------------- single calls
+
+extern "C" int64_t hg_extract_minimizer(const char* seq, int64_t len, int k, int w, int non_canonical, uint64_t* xs,
+                                        uint64_t* ys, int64_t cap, int64_t* needed)
+{
+    if (!seq && len > 0) return -fail(HG_ERR_ARG, "hg_extract_minimizer: null sequence");
+    if (hg_device_count() <= 0) return -fail(HG_ERR_CUDA, "hg_extract_minimizer: no CUDA device");
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
+        return -fail(HG_ERR_CUDA, "hg_extract_minimizer: stream");
+    std::vector<uint64_t> x, y;
+    const int r = run_extract(k, w, non_canonical, seq, len, x, y, st);
+    cudaStreamDestroy(st);
+    if (r) return -r;
+    const int64_t m = (int64_t)x.size();
+    if (needed) *needed = m;
+    if (m > cap) return -fail(HG_ERR_CAPACITY, "hg_extract_minimizer: output capacity");
+    std::copy(x.begin(), x.end(), xs);
+    std::copy(y.begin(), y.end(), ys);
+    return m;
+}
+
+extern "C" int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* target, int8_t m,
+                                const int8_t* mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag,
+                                int32_t* ez_out, uint32_t* cigar, int64_t cap)
+{
+    if (!(flag & hg::kEzGenericSc)) return -fail(HG_ERR_ARG, "hg_ksw_extz2: only KSW_EZ_GENERIC_SC scoring is supported");
+    if (!ez_out || (qlen > 0 && !query) || (tlen > 0 && !target) || !mat || m <= 0 || m > 16)
+        return -fail(HG_ERR_ARG, "hg_ksw_extz2: bad arguments");
+    if (hg_device_count() <= 0) return -fail(HG_ERR_CUDA, "hg_ksw_extz2: no CUDA device");
+    for (int i = 0; i < qlen; ++i)
+        if (query[i] >= m) return -fail(HG_ERR_ARG, "hg_ksw_extz2: query symbol >= m");
+    for (int i = 0; i < tlen; ++i)
+        if (target[i] >= m) return -fail(HG_ERR_ARG, "hg_ksw_extz2: target symbol >= m");
+    const int32_t init[10] = {0, 0, -1, -1, hg::kNegInf, -1, hg::kNegInf, -1, hg::kNegInf, 0};
+    if (qlen <= 0 || tlen <= 0) {
+        std::copy(init, init + 10, ez_out);
+        return 0;
+    }
+    const size_t scratch = hg_ksw_scratch_bytes(qlen, tlen, w, flag);
+    const int ccap = qlen + tlen + 4;
+    DevBuf<uint8_t> d_q, d_t, d_s;
+    DevBuf<int8_t> d_m;
+    DevBuf<uint32_t> d_c;
+    DevBuf<int32_t> d_r;
+    cudaStream_t st;
+    HG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct Guard {
+        cudaStream_t s;
+        ~Guard() { cudaStreamDestroy(s); }
+    } guard{st};
+    HG_CUDA(d_q.alloc(qlen));
+    HG_CUDA(d_t.alloc(tlen));
+    HG_CUDA(d_s.alloc(scratch + 256));
+    HG_CUDA(d_m.alloc((size_t)m * m));
+    HG_CUDA(d_c.alloc(ccap));
+    HG_CUDA(d_r.alloc(16));
+    HG_CUDA(cudaMemcpyAsync(d_q.p, query, qlen, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(d_t.p, target, tlen, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(d_m.p, mat, (size_t)m * m, cudaMemcpyHostToDevice, st));
+    HG_CUDA(hg_launch_ksw_single(qlen, d_q.p, tlen, d_t.p, m, d_m.p, q, e, w, zdrop, end_bonus, flag, d_s.p, d_c.p,
+                                 ccap, d_r.p, st));
+    int32_t res[11];
+    HG_CUDA(cudaMemcpyAsync(res, d_r.p, sizeof(res), cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaStreamSynchronize(st));
+    std::copy(res, res + 10, ez_out);
+    const int nc = res[10];
+    if (nc > ccap) return -fail(HG_ERR_CAPACITY, "hg_ksw_extz2: internal CIGAR overflow");
+    if (nc > cap) return -fail(HG_ERR_CAPACITY, "hg_ksw_extz2: CIGAR capacity");
+    if (nc) HG_CUDA(cudaMemcpy(cigar, d_c.p, 4 * (size_t)nc, cudaMemcpyDeviceToHost));
+    return nc;
+}
+
+extern "C" int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int flag,
+                                        uint32_t* cigar, int64_t cap)
+{  // globalAlignKSW2 (src/align/align.cpp:22-65)
+    if (rlen < 0 || qlen < 0) return -fail(HG_ERR_ARG, "hg_global_align_ksw2: bad lengths");
+    if (rlen == 0 || qlen == 0) {
+        if (rlen == 0 && qlen > 0) {
+            if (cap < 1) return -fail(HG_ERR_CAPACITY, "cigar capacity");
+            cigar[0] = (uint32_t)qlen << 4 | 1u;
+            return 1;
+        }
+        if (qlen == 0 && rlen > 0) {
+            if (cap < 1) return -fail(HG_ERR_CAPACITY, "cigar capacity");
+            cigar[0] = (uint32_t)rlen << 4 | 2u;
+            return 1;
+        }
+        return 0;
+    }
+    std::vector<uint8_t> re((size_t)rlen), qe((size_t)qlen);
+    for (int64_t i = 0; i < rlen; ++i) re[i] = hg::dna5_of((uint8_t)ref[i]);
+    for (int64_t i = 0; i < qlen; ++i) qe[i] = hg::dna5_of((uint8_t)qry[i]);
+    static const int8_t mat[25] = {5, -4, -4, -4, 0, -4, 5, -4, -4, 0, -4, -4, 5, -4, 0,
+                                   -4, -4, -4, 5, 0, 0, 0, 0, 0, 0};
+    const int w = hg::auto_band((int)rlen, (int)qlen);
+    int32_t ez[10];
+    return hg_ksw_extz2((int)qlen, qe.data(), (int)rlen, re.data(), 5, mat, 6, 2, w, -1, 0,
+                        flag < 0 ? (hg::kEzGenericSc | hg::kEzRight) : flag, ez, cigar, cap);
+}
+
+extern "C" int64_t hg_align_query(hg_index_t* ix, const char* qry, int64_t qlen, uint32_t* cigar, int64_t cap,
+                                  uint32_t* status)
+{
+    if (!ix || (!qry && qlen > 0) || qlen < 0) return -fail(HG_ERR_ARG, "hg_align_query: bad arguments");
+    std::lock_guard<std::mutex> lock(ix->single_mu);
+    const int64_t need_bases = std::max<int64_t>(qlen, 1);
+    if (!ix->single || ix->single->max_bases < need_bases) {
+        if (ix->single) hg_ctx_destroy(ix->single), ix->single = nullptr;
+        int r = hg_ctx_create(ix, 1, std::max<int64_t>(need_bases, 65536), &ix->single);
+        if (r) return -r;
+    }
+    const int64_t offs[2] = {0, qlen};
+    int64_t pb = 0, ne = 0;
+    int r = hg_pack(qry, offs, 1, nullptr, 0, nullptr, nullptr, 0, nullptr, &pb, &ne);
+    if (r) return -r;
+    std::vector<uint8_t> pk((size_t)std::max<int64_t>(pb, 16));
+    std::vector<int64_t> poff(1), eoff(2);
+    std::vector<int32_t> exc((size_t)std::max<int64_t>(ne, 1) * 3);
+    r = hg_pack(qry, offs, 1, pk.data(), (int64_t)pk.size(), poff.data(), exc.data(), ne, eoff.data(), nullptr,
+                nullptr);
+    if (r) return -r;
+    const int32_t ql = (int32_t)qlen;
+    std::vector<uint32_t> cig((size_t)(qlen + ix->L + 8));
+    int64_t coff[2];
+    uint32_t st = 0;
+    r = hg_align_plain(ix->single, pk.data(), poff.data(), &ql, exc.data(), eoff.data(), 1, cig.data(),
+                       (int64_t)cig.size(), coff, nullptr, nullptr, 0, &st);
+    if (status) *status = st;
+    if (r && r != HG_ERR_LENGTH_MISMATCH) return -r;
+    const int64_t m = coff[1] - coff[0];
+    if (m > cap) return -fail(HG_ERR_CAPACITY, "hg_align_query: CIGAR capacity");
+    std::copy(cig.begin(), cig.begin() + m, cigar);
+    return m;
+}

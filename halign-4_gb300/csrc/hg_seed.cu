@@ -1,0 +1,323 @@
+// hg_seed.cu - K1: minimizer extraction + center-index lookup.
+//
+// Restates minimizer::extractMinimizer (src/seed/minimizer.cpp:103-177) as a
+// data-parallel tile computation.  For k-mer start p the reference emits
+//   m(p) = argmin h(q) over the valid k-mers q in [p-win+1, p] that share p's
+//          N-free run, ties to the largest q ("latest equal hash wins"),
+// at every p with a valid k-mer and p+1 >= win, whenever m(p) differs from
+// what it emitted at p-1 (an N clears that memory).  m(p) is monotone inside
+// a run, so the emitted list is the de-duplicated m(p) sequence in scan order.
+//
+// One CTA owns one query at a time (persistent, queue ordered longest first)
+// and sweeps it in tiles of kSeedTile k-mer positions:
+//   1. stream the packed bases of the tile (+ halo) with aligned uint4 loads,
+//      overlay exception bytes (N, U, lowercase ...), decode to nt4 codes;
+//   2. hash every k-mer (splitmix64 of the 2-bit forward code, >> 8);
+//   3. window minimum per position, emission flags;
+//   4. block-scan compaction in position order; matched hits (hash present in
+//      the resident center index) go to the hit arena, all hits are counted
+//      (the q_occ limit of collect_anchors uses |query hits|).
+//
+// Deque overflow.  RingMinQueue (src/seed/minimizer.cpp:35-97) has capacity
+// win and pushes before it expires old entries, so when w+1 consecutive
+// valid k-mers have strictly increasing hashes the push lands on the front
+// slot and the queue keeps that corrupted state for a while.  The tile pass
+// detects the first such position (the only way the queue can be full) and
+// queues the whole query for seed_exact_kernel, which replays the reference's
+// ring buffer sequentially (one thread per query) and overwrites the tile
+// pass's output for that query.
+#include "hg_batch.cuh"
+
+namespace hg {
+
+constexpr int kSeedThreads = 256;
+constexpr int kSeedPer = 8;
+constexpr int kSeedTile = kSeedThreads * kSeedPer;  // k-mer positions per tile
+constexpr int kMaxWin = 255;
+constexpr int kMaxK = 31;
+constexpr int kCodeBuf = kSeedTile + 512;
+constexpr int kHashBuf = kSeedTile + kMaxWin + 1;
+constexpr int kExactBlocks = 8, kExactThreads = 32;
+
+struct SeedOut {
+    int mode;        // 0: matched hits (pos, entry); 1: every hit as MinimizerHit words
+    uint64_t* hx;    // mode 1: x = hash56 << 8 | span
+    uint64_t* hy;    // mode 1: y = strand << 63 | rid << 32 | pos
+};
+
+__global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDev b, SeedOut so)
+{
+    __shared__ __align__(16) uint8_t codes[kCodeBuf];
+    __shared__ uint64_t hsh[kHashBuf];
+    __shared__ uint8_t strand[kHashBuf];
+    __shared__ int32_t mpos[kSeedTile + 1];
+    __shared__ int scan_s[33];
+    __shared__ int s_q, s_ovf;
+
+    const int k = ix.k;
+    const uint64_t kmask = (1ULL << (2 * k)) - 1ULL;
+    const int kshift = 2 * (k - 1);
+    const int tid = threadIdx.x;
+
+    for (;;) {
+        if (tid == 0) s_q = (int)atomicAdd(&b.queues[0], 1u), s_ovf = 0;
+        __syncthreads();
+        const int qi = s_q;
+        __syncthreads();
+        if (qi >= b.n) break;
+        const int q = b.order ? b.order[qi] : qi;
+        const int len = b.qlen[q];
+        const uint8_t* pk = b.packed + b.poff[q];
+        const int64_t e0 = b.exc_off[q], e1 = b.exc_off[q + 1];
+        int total_hits = 0, total_matched = 0;
+        if (len >= k && k > 0 && k <= kMaxK && ix.w > 0 && ix.w <= kMaxWin) {
+            const int nk = len - k + 1;
+            const int win = ix.w < nk ? ix.w : nk;
+            for (int p0 = 0; p0 < nk; p0 += kSeedTile) {
+                const int pend = min(p0 + kSeedTile, nk);
+                const int hs = max(p0 - win, 0);           // first hashed position
+                const int bstart = hs & ~63;              // 64 bases = one uint4
+                const int bend = pend + k - 1;            // one past the last base needed
+                const int nvec = (bend - bstart + 63) >> 6;
+                // 1. packed bases -> nt4 codes (codes[i] = base bstart + i)
+                const uint4* src = reinterpret_cast<const uint4*>(pk + (bstart >> 2));
+                for (int v = tid; v < nvec; v += kSeedThreads) {
+                    const uint4 word = src[v];
+                    const uint32_t wv[4] = {word.x, word.y, word.z, word.w};
+                    uint32_t* dst = reinterpret_cast<uint32_t*>(codes + v * 64);
+#pragma unroll
+                    for (int wi = 0; wi < 4; ++wi) {
+#pragma unroll
+                        for (int bq = 0; bq < 4; ++bq) {
+                            const uint32_t byte = (wv[wi] >> (8 * bq)) & 0xffu;
+                            // 4 bases of this byte -> 4 code bytes
+                            const uint32_t c4 = (byte & 3u) | ((byte >> 2) & 3u) << 8 | ((byte >> 4) & 3u) << 16 |
+                                                ((byte >> 6) & 3u) << 24;
+                            dst[wi * 4 + bq] = c4;
+                        }
+                    }
+                }
+                __syncthreads();
+                // exception bytes overlay (U counts as T for minimizers, N/other invalid)
+                for (int64_t e = e0 + tid; e < e1; e += kSeedThreads) {
+                    const int s = b.exc[e * 3], l = b.exc[e * 3 + 1];
+                    const uint8_t c = nt4_of((uint8_t)b.exc[e * 3 + 2]);
+                    const int lo = max(s, bstart), hi = min(s + l, bend);
+                    for (int i = lo; i < hi; ++i) codes[i - bstart] = c;
+                }
+                __syncthreads();
+                // 2. hashes for positions [hs, pend)
+                for (int base = hs + tid * kSeedPer; base < pend; base += kSeedThreads * kSeedPer) {
+                    uint64_t fwd = 0, rev = 0;
+                    int last_bad = -1;
+                    for (int i = 0; i < k - 1; ++i) {
+                        const int pos = base + i;
+                        const uint32_t c = codes[pos - bstart];
+                        if (c >= 4) last_bad = pos;
+                        fwd = ((fwd << 2) | (c & 3u)) & kmask;
+                        rev = (rev >> 2) | ((uint64_t)(3u ^ (c & 3u)) << kshift);
+                    }
+                    const int top = min(base + kSeedPer, pend);
+                    for (int p = base; p < top; ++p) {
+                        const int pos = p + k - 1;
+                        const uint32_t c = codes[pos - bstart];
+                        if (c >= 4) last_bad = pos;
+                        fwd = ((fwd << 2) | (c & 3u)) & kmask;
+                        rev = (rev >> 2) | ((uint64_t)(3u ^ (c & 3u)) << kshift);
+                        const bool ok = last_bad < p;
+                        const uint64_t code = ix.non_canonical ? fwd : (fwd < rev ? fwd : rev);
+                        hsh[p - hs] = ok ? (splitmix64(code) >> 8) : kNoHash;
+                        strand[p - hs] = ix.non_canonical ? 1 : (fwd <= rev);
+                    }
+                }
+                __syncthreads();
+                // 3. window minimum m(p) for p in [p0-1, pend)
+                const int mlo = p0 - 1;
+                for (int p = max(mlo, 0) + tid; p < pend; p += kSeedThreads) {
+                    int best = -1;
+                    const uint64_t hp = hsh[p - hs];
+                    if (hp != kNoHash) {
+                        best = p;
+                        uint64_t bh = hp, nxt = hp;
+                        bool inc = true;
+                        const int lo = max(p - win + 1, 0);
+                        for (int qq = p - 1; qq >= lo; --qq) {
+                            const uint64_t hq = hsh[qq - hs];
+                            if (hq == kNoHash) {
+                                inc = false;
+                                break;
+                            }
+                            if (hq < bh) bh = hq, best = qq;
+                            inc = inc && hq < nxt;
+                            nxt = hq;
+                        }
+                        // full queue before the push at p: hashes strictly increase on [p-win, p]
+                        if (p >= p0 && inc && p - win >= 0) {
+                            const uint64_t hq = hsh[p - win - hs];
+                            if (hq != kNoHash && hq < nxt) s_ovf = 1;
+                        }
+                    }
+                    mpos[p - mlo] = best;
+                }
+                __syncthreads();
+                // 4. emission + compaction in position order
+                const int my0 = p0 + tid * kSeedPer;
+                const int my1 = min(my0 + kSeedPer, pend);
+                int n_emit = 0, n_match = 0;
+                uint32_t ent[kSeedPer];
+                uint32_t emitmask = 0;
+                for (int p = my0; p < my1; ++p) {
+                    const int i = p - my0;
+                    ent[i] = kEmptyKey;
+                    const int m = mpos[p - mlo];
+                    if (m < 0 || p + 1 < win) continue;
+                    const bool prev_elig = p >= 1 && (p - 1) + 1 >= win && mpos[p - 1 - mlo] >= 0;
+                    if (prev_elig && mpos[p - 1 - mlo] == m) continue;
+                    emitmask |= 1u << i;
+                    ++n_emit;
+                    if (so.mode == 0) {
+                        ent[i] = index_find(ix, hsh[m - hs]);
+                        if (ent[i] != kEmptyKey) ++n_match;
+                    }
+                }
+                int tot_emit, tot_match;
+                const int ex_emit = block_excl_sum(n_emit, scan_s, &tot_emit);
+                const int ex_match = so.mode == 0 ? block_excl_sum(n_match, scan_s, &tot_match) : 0;
+                if (so.mode == 0) {
+                    int o = total_matched + ex_match;
+                    const int64_t hb = b.hoff[q];
+                    for (int p = my0; p < my1; ++p) {
+                        const int i = p - my0;
+                        if ((emitmask >> i & 1u) && ent[i] != kEmptyKey) {
+                            b.hit_pos[hb + o] = (uint32_t)mpos[p - mlo];
+                            b.hit_ent[hb + o] = ent[i];
+                            ++o;
+                        }
+                    }
+                    total_matched += tot_match;
+                } else {
+                    int o = total_hits + ex_emit;
+                    const int64_t hb = b.hoff[q];
+                    for (int p = my0; p < my1; ++p) {
+                        const int i = p - my0;
+                        if (emitmask >> i & 1u) {
+                            const int m = mpos[p - mlo];
+                            so.hx[hb + o] = (hsh[m - hs] << 8) | (uint64_t)(uint8_t)k;
+                            so.hy[hb + o] = ((uint64_t)(strand[p - hs] ? 0x80000000u : 0u) << 32) | (uint64_t)(uint32_t)m;
+                            ++o;
+                        }
+                    }
+                }
+                total_hits += tot_emit;
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            b.n_hits[q] = total_hits;
+            b.n_matched[q] = total_matched;
+            if (s_ovf) b.exact_list[atomicAdd(b.n_exact, 1u)] = (uint32_t)q;
+        }
+    }
+}
+
+// Sequential replay of extractMinimizer for the queries whose deque
+// overflows, with the reference's ring indexing (RingMinQueue::idx subtracts
+// the capacity once).  Ring entries past the capacity live in spare slots of
+// this thread's scratch ring, i.e. they behave as plain memory (the reference
+// writes past its vector there).
+__global__ void seed_exact_kernel(IndexDev ix, BatchDev b, SeedOut so)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nt = gridDim.x * blockDim.x;
+    const unsigned total = *b.n_exact;
+    const int k = ix.k;
+    const uint64_t kmask = (1ULL << (2 * k)) - 1ULL;
+    const int kshift = 2 * (k - 1);
+    uint64_t* rh = b.ring_h + (size_t)gt * b.ring_slots;
+    uint32_t* rp = b.ring_p + (size_t)gt * b.ring_slots;
+    for (unsigned wi = gt; wi < total; wi += nt) {
+        const int q = (int)b.exact_list[wi];
+        const uint32_t n = (uint32_t)b.qlen[q];
+        const uint8_t* pk = b.packed + b.poff[q];
+        int64_t e = b.exc_off[q];
+        const int64_t e1 = b.exc_off[q + 1];
+        const int64_t hb = b.hoff[q];
+        const uint32_t nk = n - (uint32_t)k + 1;
+        const uint32_t win = (uint32_t)ix.w < nk ? (uint32_t)ix.w : nk;
+        uint64_t fwd = 0, rev = 0, last_h = 0;
+        uint32_t valid = 0, head = 0, size = 0, last_p = 0;
+        bool has_last = false;
+        int n_hits = 0, n_match = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            while (e < e1 && (uint32_t)(b.exc[e * 3] + b.exc[e * 3 + 1]) <= i) ++e;
+            uint32_t c = packed_code(pk, i);
+            if (e < e1 && (uint32_t)b.exc[e * 3] <= i) c = nt4_of((uint8_t)b.exc[e * 3 + 2]);
+            if (c >= 4) {
+                fwd = rev = 0, valid = 0, head = size = 0, has_last = false;
+                continue;
+            }
+            fwd = ((fwd << 2) | c) & kmask;
+            rev = (rev >> 2) | ((uint64_t)(3u ^ c) << kshift);
+            if (valid < (uint32_t)k) ++valid;
+            if (valid < (uint32_t)k) continue;
+            const uint32_t pos = i + 1 - (uint32_t)k;
+            const uint64_t code = ix.non_canonical ? fwd : (fwd < rev ? fwd : rev);
+            const uint64_t h = splitmix64(code) >> 8;
+            const uint32_t last_slot = (uint32_t)b.ring_slots - 1;
+            while (size) {
+                uint32_t bi = head + size - 1;
+                if (bi >= win) bi -= win;
+                if (rh[min(bi, last_slot)] >= h) --size;
+                else break;
+            }
+            {
+                uint32_t bi = head + size;
+                if (bi >= win) bi -= win;
+                bi = min(bi, last_slot);
+                rh[bi] = h, rp[bi] = pos;
+                ++size;
+            }
+            if (pos + 1 < win) continue;
+            const uint32_t ws = pos + 1 - win;
+            while (size && rp[head] < ws) head = head + 1 >= win ? head + 1 - win : head + 1, --size;
+            if (size) {
+                const uint64_t ch = rh[head];
+                const uint32_t cp = rp[head];
+                if (!has_last || ch != last_h || cp != last_p) {
+                    if (so.mode == 0) {
+                        const uint32_t ent = index_find(ix, ch);
+                        if (ent != kEmptyKey) {
+                            b.hit_pos[hb + n_match] = cp;
+                            b.hit_ent[hb + n_match] = ent;
+                            ++n_match;
+                        }
+                    } else {
+                        const bool strand = ix.non_canonical ? true : (fwd <= rev);
+                        so.hx[hb + n_hits] = (ch << 8) | (uint64_t)(uint8_t)k;
+                        so.hy[hb + n_hits] = ((uint64_t)(strand ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
+                    }
+                    ++n_hits;
+                    last_h = ch, last_p = cp, has_last = true;
+                }
+            }
+        }
+        b.n_hits[q] = n_hits;
+        b.n_matched[q] = n_match;
+    }
+}
+
+}  // namespace hg
+
+extern "C" cudaError_t hg_launch_seed(const hg::IndexDev* ix, const hg::BatchDev* b, int mode, uint64_t* hx,
+                                      uint64_t* hy, int grid, cudaStream_t st)
+{
+    hg::SeedOut so{mode, hx, hy};
+    hg::seed_kernel<<<grid, hg::kSeedThreads, 0, st>>>(*ix, *b, so);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    hg::seed_exact_kernel<<<hg::kExactBlocks, hg::kExactThreads, 0, st>>>(*ix, *b, so);
+    return cudaGetLastError();
+}
+
+extern "C" int hg_exact_ring_threads(void) { return hg::kExactBlocks * hg::kExactThreads; }

@@ -1,0 +1,163 @@
+/* halign_gb300.h - C ABI of the GB300-native align-to-center path.
+ *
+ * Plain pointers, sizes and int status codes; no C++ or CUDA types cross the
+ * boundary.  One hg_ctx_t owns one CUDA stream and its device buffers; a
+ * host thread that shares a context with others must serialise its calls, or
+ * use its own context (contexts of one index may run concurrently).
+ *
+ * Each entry point names the reference interface it replaces (paths in the
+ * HAlign-4 source tree).
+ */
+#ifndef HALIGN_GB300_H
+#define HALIGN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_OK 0
+#define HG_ERR_CUDA 1            /* CUDA runtime error (hg_last_error has the text) */
+#define HG_ERR_ARG 2             /* invalid argument / unsupported flag */
+#define HG_ERR_NOMEM 3           /* device or host allocation failed */
+#define HG_ERR_CAPACITY 4        /* a caller buffer or a configured capacity is too small */
+#define HG_ERR_LENGTH_MISMATCH 5 /* a row does not span the center: the reference throws
+                                    "Sequence length mismatch" (src/align/ref_aligner.cpp:654-662) */
+#define HG_ERR_CIGAR 6           /* CIGAR length above 2^28-1: cigarToInt/appendCigar throw
+                                    (src/align/cigar.cpp:51-59, 319-322) */
+
+/* per-query status bits (hg_align_batch's status array) */
+#define HG_ST_ARENA_OVERFLOW 0x01u
+#define HG_ST_PARTIAL_CIGAR 0x02u
+#define HG_ST_CIGAR_OVERFLOW 0x08u
+#define HG_ST_LENGTH_MISMATCH 0x10u
+
+typedef struct hg_index hg_index_t;
+typedef struct hg_ctx hg_ctx_t;
+
+/* Seeding + chaining parameters; defaults = anchor::SeedFilterParams and
+ * anchor::ChainParams (include/anchor.h:65-71, 116-127). */
+typedef struct {
+    double f_top_frac;
+    uint64_t u_floor, u_ceil;
+    double q_occ_frac;
+    uint64_t sample_every_bp;
+    int32_t max_dist_x, max_dist_y, bw, max_skip, max_iter, min_cnt, min_score;
+    float gap_penalty, skip_penalty;
+} hg_params_t;
+
+/* Last error message of the calling thread. */
+const char* hg_last_error(void);
+void hg_default_params(hg_params_t* p);
+/* Number of visible CUDA devices (0 without a GPU); never fails. */
+int hg_device_count(void);
+
+/* ---- resident center index --------------------------------------------
+ * Replaces the per-center set-up of RefAligner (src/align/ref_aligner.cpp:
+ * 20-73: consensus of the single -c record, extractMinimizer of the center)
+ * and the per-call index build inside minimizer::collect_anchors
+ * (src/seed/minimizer.cpp:238-272), done once and kept in HBM.
+ * k, w: --kmer-size / --kmer-window.  params may be NULL. */
+int hg_index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params, hg_index_t** out);
+void hg_index_destroy(hg_index_t* ix);
+/* Distinct center minimizer hashes / total center minimizers / the -f/-U
+ * occurrence threshold (anchor::compute_ref_occ_threshold). */
+int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t* n_hits, uint64_t* occ_threshold);
+
+/* ---- batch context ------------------------------------------------------
+ * max_queries / max_bases bound one device sub-batch; hg_align_batch splits
+ * larger inputs into sub-batches internally. */
+int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_bases, hg_ctx_t** out);
+void hg_ctx_destroy(hg_ctx_t* ctx);
+
+/* Pack ASCII queries into the device input format: 2 bits per A/C/G/T
+ * (A=0 C=1 G=2 T=3, base i at bits 2*(i%4) of byte i/4), each query on a
+ * 16-byte boundary, every other byte kept as an exception run
+ * {start, len, byte}.  With packed == NULL only sizes are returned. */
+int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint8_t* packed, int64_t packed_cap,
+            int64_t* poff, int32_t* exc, int64_t exc_cap, int64_t* exc_off, int64_t* packed_bytes,
+            int64_t* n_exc);
+
+/* ---- align a batch (the align-to-center hot path) -----------------------
+ * Replaces the OpenMP query loop of RefAligner::alignQueryToRef
+ * (src/align/ref_aligner.cpp:286-398) over RefAligner::globalAlign
+ * (extractMinimizer -> collect_anchors -> globalAlignMM2, :91-125), and the
+ * per-row projection of mergeAlignedResults with --keep-length
+ * (delQueryToRefByCigar, src/align/ref_aligner.cpp:172-192).
+ * Inputs are host buffers in hg_pack's format.  Outputs (host):
+ *   cigar/cigar_off: CIGAR of query i at cigar[cigar_off[i] .. cigar_off[i+1])
+ *                    (len<<4|op, op 0=M 1=I 2=D), cigar_cap entries;
+ *   has_ins[i]:      1 when the CIGAR holds an insertion (the row goes to the
+ *                    insertion group, src/align/ref_aligner.cpp:253-259);
+ *   rows:            n x row_stride bytes, row i = query i projected onto the
+ *                    center (L bytes, then padding), or NULL to skip;
+ *   status[i]:       HG_ST_* bits.
+ * The per-column SiteCount counters of the context accumulate every row.
+ * Returns HG_OK, or the first error (HG_ERR_LENGTH_MISMATCH when a row would
+ * not span the center, as the reference's merge throws). */
+int hg_align_batch(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                   const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar, int64_t cigar_cap,
+                   int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status);
+
+/* Same computation, one launch sequence per query (the plain form). */
+int hg_align_plain(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                   const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar, int64_t cigar_cap,
+                   int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status);
+
+/* Device-resident form for throughput measurement: hg_stage copies a packed
+ * batch into HBM once; hg_run_staged aligns it (outputs stay on the device,
+ * counters accumulate); hg_fetch_staged copies the outputs of the last run
+ * back in hg_align_batch's layout. */
+int hg_stage(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
+             const int64_t* exc_off, int64_t n);
+int hg_run_staged(hg_ctx_t* ctx);
+int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
+                    uint8_t* rows, int64_t row_stride, uint32_t* status);
+/* Timing of the last hg_run_staged from CUDA events on the context stream:
+ * total device ms (start to end of the run), per-stage ms in stage order
+ * seed, anchor, chain, dp_small, dp_large, stitch, rows, count (8 entries,
+ * only with hg_set_timing on), and the kernel launches of that run. */
+int hg_last_timing(hg_ctx_t* ctx, float* total_ms, float* stage_ms, int64_t* launches, int64_t* cells);
+/* cells: extz2 band cells of the last hg_run_staged, i.e. the sum over DP
+ * calls of sum_r (en0 - st0 + 1) with the band bounds of
+ * src/align/ksw2_extz2_sse.c:107-110 (the GCUPS numerator). */
+/* Enable per-stage event timing for staged runs (off by default). */
+int hg_set_timing(hg_ctx_t* ctx, int on);
+
+/* Consensus counters: counts7 = L x {A,C,G,T,U,N,-} (consensus::SiteCount,
+ * include/consensus.h:78-99), ins = L+1 insertion events (slot c: I before
+ * center column c).  reset != 0 clears them after reading. */
+int hg_counters(hg_ctx_t* ctx, uint32_t* counts7, uint32_t* ins, int reset);
+
+/* ---- single-call entry points (the C++ drop-in shim uses these) -------- */
+
+/* minimizer::extractMinimizer (include/seed.h:283-286); writes MinimizerHit
+ * words (x = hash56<<8|span, y = strand<<63|rid<<32|pos).  Returns the hit
+ * count (>= 0) or a negative HG_ERR_* value; -HG_ERR_CAPACITY means cap is
+ * smaller than the count, which is then in *needed. */
+int64_t hg_extract_minimizer(const char* seq, int64_t len, int k, int w, int non_canonical, uint64_t* xs,
+                             uint64_t* ys, int64_t cap, int64_t* needed);
+
+/* ksw_extz2_sse (include/ksw2.h:64-65) with KSW_EZ_GENERIC_SC scoring.
+ * ez_out: {max, zdropped, max_q, max_t, mqe, mqe_t, mte, mte_q, score,
+ * reach_end}; returns the CIGAR length or a negative HG_ERR_*. */
+int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* target, int8_t m, const int8_t* mat,
+                     int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag, int32_t* ez_out, uint32_t* cigar,
+                     int64_t cap);
+
+/* align::globalAlignKSW2 (src/align/align.cpp:22-65); flag < 0 selects the
+ * default KSW_EZ_GENERIC_SC|KSW_EZ_RIGHT. */
+int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int flag, uint32_t* cigar,
+                             int64_t cap);
+
+/* RefAligner::globalAlign for one query against the index's center
+ * (src/align/ref_aligner.cpp:91-125): the plain single-query path. */
+int64_t hg_align_query(hg_index_t* ix, const char* qry, int64_t qlen, uint32_t* cigar, int64_t cap,
+                       uint32_t* status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -163,9 +163,16 @@ static inline uint64_t splitmix64(uint64_t x)
  * hash >= its own (the latest equal hash wins), an invalid base clears the
  * k-mer, the deque and the last-emitted memory, and a minimizer is emitted
  * whenever (hash,pos) differs from the last one emitted. */
+static _Thread_local int64_t g_ring_oob = 0;
+
+/* Slot indices >= win used by the last ho_extract_minimizer call on this
+ * thread (the reference writes past its buffer there: undefined behaviour). */
+int64_t ho_last_ring_oob(void) { return g_ring_oob; }
+
 int64_t ho_extract_minimizer(const char* seq, int64_t n64, int k, int w, int non_canonical,
                              uint64_t* xs, uint64_t* ys, int64_t cap)
 {
+    g_ring_oob = 0;
     const uint32_t n = (uint32_t)n64;
     if (k == 0 || w == 0 || n < (uint32_t)k) return 0;
     if (k > 31) return 0;
@@ -177,9 +184,16 @@ int64_t ho_extract_minimizer(const char* seq, int64_t n64, int k, int w, int non
     const uint64_t shift = 2ULL * (uint64_t)(k - 1);
     uint64_t fwd = 0, rev = 0;
     uint32_t valid = 0;
-    /* deque as a ring of capacity win */
-    uint64_t* qh = (uint64_t*)malloc(sizeof(uint64_t) * win);
-    uint32_t* qp = (uint32_t*)malloc(sizeof(uint32_t) * win);
+    /* Deque as a ring of capacity win with the reference's index rule
+     * (RingMinQueue::idx subtracts the capacity once).  A push happens before
+     * expiry, so after win+1 strictly increasing hashes the deque holds win+1
+     * entries and the new entry lands on the front slot; the reference keeps
+     * going from that state, and so does this restatement.  Indices past the
+     * capacity (reachable only after several such pushes in a row) address
+     * spare slots here, i.e. they behave as plain memory. */
+    const uint32_t slots = 2 * win + 16;
+    uint64_t* qh = (uint64_t*)calloc(slots, sizeof(uint64_t));
+    uint32_t* qp = (uint32_t*)calloc(slots, sizeof(uint32_t));
     uint32_t head = 0, size = 0;
     uint64_t last_h = 0;
     uint32_t last_p = 0;
@@ -204,12 +218,15 @@ int64_t ho_extract_minimizer(const char* seq, int64_t n64, int k, int w, int non
         while (size) {
             uint32_t bi = head + size - 1;
             if (bi >= win) bi -= win;
+            if (bi >= win) ++g_ring_oob;
             if (qh[bi] >= h56) --size;
             else break;
         }
         {
             uint32_t bi = head + size;
             if (bi >= win) bi -= win;
+            if (bi >= win) ++g_ring_oob;
+            if (bi >= slots) bi = slots - 1; /* never reached in practice */
             qh[bi] = h56;
             qp[bi] = pos;
             ++size;

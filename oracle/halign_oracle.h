@@ -57,6 +57,10 @@ const float* ho_log2_table(void);
 int64_t ho_extract_minimizer(const char* seq, int64_t n, int k, int w, int non_canonical,
                              uint64_t* xs, uint64_t* ys, int64_t cap);
 
+/* Ring-slot indices past the window capacity used by the last call on this
+ * thread; the reference's RingMinQueue writes past its vector there. */
+int64_t ho_last_ring_oob(void);
+
 /* A2: minimizer::collect_anchors (src/seed/minimizer.cpp:220-356). */
 int64_t ho_collect_anchors(const uint64_t* rx, const uint64_t* ry, int64_t nr,
                            const uint64_t* qx, const uint64_t* qy, int64_t nq,

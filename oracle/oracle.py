@@ -76,8 +76,12 @@ class Oracle(_Common):
         L.ho_auto_band.argtypes = [i32, i32]
         L.ho_auto_band.restype = i32
         L.ho_log2_table.restype = C.POINTER(C.c_float)
+        L.ho_last_ring_oob.restype = C.c_int64
         L.ho_cigar_has_insertion.argtypes = [vp, i64]
         L.ho_cigar_has_insertion.restype = i32
+
+    def last_ring_oob(self) -> int:
+        return int(self.lib.ho_last_ring_oob())
 
     def log2_table(self) -> np.ndarray:
         p = self.lib.ho_log2_table()

@@ -1,0 +1,209 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+golden vectors the reference produced.  Integer work, so every comparison is
+bit-exact (CIGAR words, ez fields, minimizer words, row bytes, counters)."""
+import hashlib
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MAT = np.array([5, -4, -4, -4, 0, -4, 5, -4, -4, 0, -4, -4, 5, -4, 0, -4, -4, -4, 5, 0, 0, 0, 0, 0, 0], np.int8)
+
+
+def _ragged(z, name, i):
+    off = z[name + "_off"]
+    return z[name][off[i]:off[i + 1]]
+
+
+def test_ksw_extz2_golden_vectors(gpu, golden):
+    z = golden.load("ksw_extz2.npz")
+    n = len(z["params"])
+    bad = []
+    for i in range(n):
+        w, zdrop, eb, flag = (int(x) for x in z["params"][i])
+        ez, cig = gpu.ksw_extz2(_ragged(z, "q", i), _ragged(z, "t", i), 5, MAT, 6, 2, w, zdrop, eb, flag)
+        if not (np.array_equal(ez, z["ez"][i]) and np.array_equal(cig, _ragged(z, "cigar", i))):
+            bad.append(i)
+    assert not bad, f"{len(bad)} of {n} extz2 cases differ, first {bad[:5]}"
+
+
+def test_ksw_extz2_large_banded_vs_oracle(gpu, oracle):
+    rng = np.random.default_rng(5)
+    for it in range(40):
+        ql, tl = int(rng.integers(200, 900)), int(rng.integers(200, 900))
+        q = rng.integers(0, 4, ql).astype(np.uint8)
+        t = np.resize(q, tl).copy()
+        m = rng.random(tl) < 0.1
+        t[m] = rng.integers(0, 5, int(m.sum()))
+        w = int(rng.choice([-1, 7, 33, 150, 400]))
+        flag = int(rng.choice([0x04, 0x06, 0x86, 0x0E]))
+        zdrop = int(rng.choice([-1, 100]))
+        e1, c1 = oracle.ksw_extz2(q, t, 5, MAT, 6, 2, w, zdrop, 0, flag)
+        e2, c2 = gpu.ksw_extz2(q, t, 5, MAT, 6, 2, w, zdrop, 0, flag)
+        assert np.array_equal(e1, e2) and np.array_equal(c1, c2), (it, ql, tl, w, flag)
+
+
+@pytest.mark.parametrize("non_canonical", [True, False])
+def test_minimizers_vs_oracle(gpu, oracle, non_canonical):
+    rng = np.random.default_rng(3)
+    alphabet = np.frombuffer(b"ACGTACGTACGTACGTNacgtU-", np.uint8)
+    for it in range(60):
+        n = int(rng.integers(0, 9000))
+        s = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, n)].copy()
+        if it % 3 == 0 and n:
+            m = rng.random(n) < 0.02
+            s[m] = alphabet[rng.integers(0, len(alphabet), int(m.sum()))]
+        if it % 5 == 0 and n > 300:
+            a = int(rng.integers(0, n - 200))
+            s[a:a + int(rng.integers(1, 200))] = ord("N")
+        k = int(rng.choice([15, 15, 11, 21, 31, 5]))
+        w = int(rng.choice([10, 10, 1, 5, 40, 255]))
+        ox, oy = oracle.extract_minimizer(s.tobytes(), k, w, non_canonical)
+        gx, gy = gpu.extract_minimizer(s.tobytes(), k, w, non_canonical)
+        assert np.array_equal(ox, gx) and np.array_equal(oy, gy), (it, n, k, w)
+
+
+def test_minimizers_golden_stage(gpu, golden, pkg):
+    z = golden.load("mito_stages.npz")
+    w = pkg.synth.mito(3)
+    cx, cy = gpu.extract_minimizer(w.center)
+    assert np.array_equal(cx, z["center_x"]) and np.array_equal(cy, z["center_y"])
+    for j in range(3):
+        qx, qy = gpu.extract_minimizer(w.query(j))
+        assert np.array_equal(qx, z[f"q{j}_x"]) and np.array_equal(qy, z[f"q{j}_y"])
+
+
+def _assemble_fasta(w, res, header):
+    ins = [i for i in range(w.n) if res.has_ins[i]]
+    non = [i for i in range(w.n) if not res.has_ins[i]]
+    parts = [b">" + header.encode() + b"\n" + w.center + b"\n"]
+    for i in ins + non:
+        parts.append(b">" + w.names[i].encode() + b"\n" + res.rows[i].tobytes() + b"\n")
+    return b"".join(parts)
+
+
+@pytest.fixture(scope="module")
+def mito1000(gpu, pkg):
+    w = pkg.synth.mito(1000)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=600, max_bases=600 * 17000)  # two sub-batches
+    res = ctx.align(gpu.pack(w.seqs, w.offsets), rows=True)
+    return w, ix, ctx, res
+
+
+def test_batch_mito_fasta_identical_to_reference_cli(mito1000, golden):
+    w, ix, ctx, res = mito1000
+    assert not res.status.any()
+    fa = _assemble_fasta(w, res, golden.meta["center_header"])
+    assert len(fa) == golden.meta["mito1000_cli_fasta_bytes"]
+    assert hashlib.sha256(fa).hexdigest() == golden.meta["mito1000_cli_fasta_sha256"]
+
+
+def test_batch_mito_cigars_golden_and_oracle(mito1000, golden, oracle):
+    w, ix, ctx, res = mito1000
+    z = golden.load("mito_cigars.npz")
+    for j, i in enumerate(z["idx"]):
+        assert np.array_equal(res.cigar_of(int(i)), _ragged(z, "cigar", j)), int(i)
+    _, cigs = oracle.align_batch(w.center, w.center, w.seqs, w.offsets, nthreads=8)
+    for i in range(w.n):
+        assert np.array_equal(res.cigar_of(i), cigs[i]), i
+        assert bool(res.has_ins[i]) == oracle.has_insertion(cigs[i])
+
+
+def test_counters_match_rows(mito1000, oracle):
+    w, ix, ctx, res = mito1000
+    cnt, ins = ctx.counters()
+    assert np.array_equal(cnt, oracle.count_rows(res.rows))
+    ref_ins = np.zeros(ix.L + 1, np.uint32)
+    for i in range(w.n):
+        oracle.count_insertions(res.cigar_of(i), ix.L, ref_ins)
+    assert np.array_equal(ins, ref_ins)
+    # pickConsensusChar over the counters restores the center
+    cons = bytes(ord(oracle.pick_consensus(cnt[c])) for c in range(ix.L))
+    assert cons == w.center
+
+
+@pytest.mark.parametrize("name,n", [("divergent", 40), ("uneven", 400), ("serve", 20)])
+def test_batch_workloads_golden(gpu, pkg, golden, oracle, name, n):
+    w = getattr(pkg.synth, name)(n)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=n, max_bases=int(w.total_bases) + 1024)
+    res = ctx.align(gpu.pack(w.seqs, w.offsets), rows=True)
+    z = golden.load(f"{name}_cigars.npz")
+    for j, i in enumerate(z["idx"]):
+        assert np.array_equal(res.cigar_of(int(i)), _ragged(z, "cigar", j)), (name, int(i))
+    for i in range(w.n):
+        row = oracle.del_query(w.query(i), res.cigar_of(i))
+        assert res.rows[i].tobytes() == row, (name, i)
+
+
+def test_plain_form_equals_batched(gpu, pkg):
+    w = pkg.synth.mito(24)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=32, max_bases=32 * 17000)
+    b = gpu.pack(w.seqs, w.offsets)
+    r1 = ctx.align(b, rows=True)
+    r2 = ctx.align(b, rows=True, plain=True)
+    assert np.array_equal(r1.cigar_off, r2.cigar_off) and np.array_equal(r1.cigar, r2.cigar)
+    assert np.array_equal(r1.rows, r2.rows) and np.array_equal(r1.has_ins, r2.has_ins)
+
+
+def test_staged_equals_batched(gpu, pkg):
+    w = pkg.synth.mito(64)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=64, max_bases=64 * 17000)
+    b = gpu.pack(w.seqs, w.offsets)
+    r1 = ctx.align(b, rows=True)
+    ctx.stage(b)
+    ctx.run_staged()
+    ctx.run_staged()  # replay of the captured graph
+    r2 = ctx.fetch_staged(rows=True)
+    assert np.array_equal(r1.cigar, r2.cigar) and np.array_equal(r1.rows, r2.rows)
+
+
+def test_edge_cases_vs_oracle(gpu, oracle, pkg):
+    rng = np.random.default_rng(9)
+    center = pkg.synth.random_center(3000, 77)
+    cmx, cmy = oracle.extract_minimizer(center)
+    c = np.frombuffer(center, np.uint8)
+    cases = [b"", b"A", b"ACGTACGTACGTAC", b"N" * 500, center, center + b"ACGTTTGA" * 40,
+             center[:1000], center[2000:], center[100:140], b"acgt" + center[10:900].lower(),
+             center[:500] + b"N" * 120 + center[620:1500], center[:700].replace(b"T", b"U"),
+             np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 800)].tobytes(),
+             center[:1200] + center[1700:2600],
+             # middle segment 1000 (center) vs 550 (unrelated): the band cannot reach
+             # the segment end, so the segment becomes I(q)D(t)
+             center[:1000] + np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 550)].tobytes() + center[2000:],
+             # chainless 1600 vs 3000: band-limited global alignment stops early (partial CIGAR)
+             np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, 1600)].tobytes()]
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=64, max_bases=200000)
+    res = ctx.align(gpu.pack(seqs, offs), rows=True, check=False)
+    for i, q in enumerate(cases):
+        want = oracle.align_query(center, cmx, cmy, q)
+        assert np.array_equal(res.cigar_of(i), want), (i, oracle.cigar_str(want)[:120],
+                                                        oracle.cigar_str(res.cigar_of(i))[:120])
+        if not (res.status[i] & (pkg.ST_PARTIAL_CIGAR | pkg.ST_LENGTH_MISMATCH)):
+            assert res.rows[i].tobytes() == oracle.del_query(q, want), i
+    # the single-query entry point agrees with the batch
+    for i in (2, 4, 9, 11):
+        assert np.array_equal(ix.align_query(cases[i]), res.cigar_of(i))
+    del c
+
+
+def test_global_align_ksw2_vs_oracle(gpu, oracle):
+    rng = np.random.default_rng(2)
+    for it in range(30):
+        r = np.frombuffer(b"ACGTN", np.uint8)[rng.integers(0, 5 if it % 4 == 0 else 4, int(rng.integers(0, 400)))]
+        q = r.copy()
+        if len(q):
+            m = rng.random(len(q)) < 0.05
+            q[m] = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, int(m.sum()))]
+        q = np.concatenate([q[: len(q) // 2], np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, it)],
+                            q[len(q) // 2 + it // 2:]])
+        flag = -1 if it % 2 else 0x04
+        assert np.array_equal(gpu.global_align_ksw2(r.tobytes(), q.tobytes(), flag),
+                              oracle.global_align_ksw2(r.tobytes(), q.tobytes(), flag)), it
