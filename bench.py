@@ -252,6 +252,9 @@ def main():
             ms, _, launches = ctx.last_timing()  # synchronizes the context stream
             dev_ms.append(ms)
     dist.barrier()
+    flags = ctx.staged_flags()
+    if flags:
+        raise SystemExit(f"bench: staged run reported status flags 0x{flags:x} (incomplete alignments)")
     step_s = dist.max(float(np.sum(dev_ms)) / 1e3 / args.steps)
     cells_c = C.c_int64()
     L.hg_last_timing(ctx.h, None, None, None, C.byref(cells_c))
@@ -265,6 +268,7 @@ def main():
     n_cig_words = None
     # e2e: the C ABI call with pinned host buffers
     e2e = None
+    parity = None
     if not args.no_e2e:
         import torch
         pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
@@ -290,6 +294,17 @@ def main():
             call()
         e_wall = dist.max((time.perf_counter() - t0) / e2e_steps)
         n_cig_words = int(off_out[-1])
+        # spot check of the timed output against the CPU path (bit-exact)
+        from oracle.oracle import Oracle
+        rng = np.random.default_rng(rank)
+        pick = np.sort(rng.choice(b.n, size=min(200, b.n), replace=False))
+        o = Oracle()
+        mism = 0
+        for i in pick:
+            want = o.align_query(w.center, *o.extract_minimizer(w.center), w.query(int(i)))
+            if not np.array_equal(cig_out[off_out[i]:off_out[i + 1]], want):
+                mism += 1
+        parity = {"checked_queries": int(len(pick)), "mismatches": int(mism), "against": "oracle CIGARs"}
         h2d = b.nbytes
         d2h = 4 * n_cig_words + 8 * (b.n + 1) + b.n + 4 * b.n + b.n * ix.L
         e2e = {"value": round(world * b.bases / e_wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -333,6 +348,7 @@ def main():
                      "note": "integer-issue-bound path; HBM fraction is low by construction"},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "parity_sample": parity,
         "clocks": clocks,
     }
     if rank == 0:

@@ -69,6 +69,7 @@ def lib() -> C.CDLL:
     L.hg_fetch_staged.argtypes = [vp, vp, i64, vp, vp, vp, i64, vp]
     L.hg_last_timing.argtypes = [vp, vp, vp, vp, vp]
     L.hg_set_timing.argtypes = [vp, i32]
+    L.hg_staged_flags.argtypes = [vp, vp]
     L.hg_counters.argtypes = [vp, vp, vp, i32]
     L.hg_extract_minimizer.argtypes = [C.c_char_p, i64, i32, i32, i32, vp, vp, i64, vp]
     L.hg_extract_minimizer.restype = i64
@@ -233,6 +234,12 @@ class Context:
 
     def run_staged(self):
         _check(lib().hg_run_staged(self.h))
+
+    def staged_flags(self) -> int:
+        """OR of the per-query status bits of the last staged run (0 = all complete)."""
+        f = C.c_uint32()
+        _check(lib().hg_staged_flags(self.h, C.byref(f)))
+        return f.value
 
     def fetch_staged(self, rows: bool = True) -> AlignResult:
         b = self._staged

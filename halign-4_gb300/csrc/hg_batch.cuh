@@ -91,7 +91,11 @@ struct BatchDev {
     unsigned int* n_small;
     unsigned int* n_large;
     int64_t wcap;
-    // K5/K6 DP scratch for large segments (dynamic byte arena)
+    // K6 DP scratch: one reusable slot per large-tier warp, plus a bump arena
+    // for segments whose scratch exceeds a slot
+    uint8_t* dp_slots;
+    int64_t dp_slot_bytes;
+    int dp_nslots;
     uint8_t* dp_arena;
     int64_t dp_cap;
     unsigned long long* dp_cursor;
@@ -108,6 +112,7 @@ struct BatchDev {
     uint32_t* status;            // per query
     unsigned int* queues;        // work-queue heads, one per stage
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
+    uint32_t* run_flags;         // OR of every query status since the last reset
 };
 
 // Hash-table probe; returns the entry id or kEmptyKey.

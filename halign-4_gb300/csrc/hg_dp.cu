@@ -440,6 +440,7 @@ __global__ void __launch_bounds__(128) dp_large_kernel(IndexDev ix, BatchDev b)
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
+    const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const unsigned total = *b.n_large;
     for (;;) {
         unsigned wi = 0;
@@ -464,21 +465,27 @@ __global__ void __launch_bounds__(128) dp_large_kernel(IndexDev ix, BatchDev b)
         // when a chainless global alignment stops at the band edge
         a.flag = kEzGenericSc | ((g.kind & kSegLeft) ? 0 : kEzRight) | (global ? 0 : kEzApproxMax);
         const size_t need = ksw_scratch_bytes(a.qlen, a.tlen, a.w, a.flag);
-        unsigned long long off = 0;
-        if (lane == 0) {
-            off = atomicAdd(b.dp_cursor, (unsigned long long)((need + 255) & ~(size_t)255));
-            if ((int64_t)(off + need) > b.dp_cap) off = ~0ull;
-        }
-        off = __shfl_sync(FULL, off, 0);
-        if (off == ~0ull) {
+        uint8_t* scratch;
+        if ((int64_t)need <= b.dp_slot_bytes && gw < b.dp_nslots) {
+            scratch = b.dp_slots + (size_t)gw * b.dp_slot_bytes;  // this warp's reusable slot
+        } else {
+            unsigned long long off = 0;
             if (lane == 0) {
-                atomicOr(&b.status[g.q], kStArenaOverflow);
-                b.seg[sid].nops = 0;
+                off = atomicAdd(b.dp_cursor, (unsigned long long)((need + 255) & ~(size_t)255));
+                if ((int64_t)(off + need) > b.dp_cap) off = ~0ull;
             }
-            continue;
+            off = __shfl_sync(FULL, off, 0);
+            if (off == ~0ull) {
+                if (lane == 0) {
+                    atomicOr(&b.status[g.q], kStArenaOverflow);
+                    b.seg[sid].nops = 0;
+                }
+                continue;
+            }
+            scratch = b.dp_arena + off;
         }
         uint32_t* out = b.cig_seg + b.coff[g.q] + g.slot;
-        const KswResult R = ksw_extz2_warp(a, b.dp_arena + off, out, (int)(g.rl + g.ql));
+        const KswResult R = ksw_extz2_warp(a, scratch, out, (int)(g.rl + g.ql));
         if (lane == 0 && b.cells) atomicAdd(b.cells, (unsigned long long)R.cells);
         if (lane == 0) {
             if (global) {

@@ -298,6 +298,22 @@ __global__ void __launch_bounds__(256) count_kernel(const uint8_t* rows, int64_t
 
 }  // namespace hg
 
+namespace hg {
+__global__ void status_or_kernel(const uint32_t* status, int n, uint32_t* flags)
+{
+    uint32_t v = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v |= status[i];
+    v = __reduce_or_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0 && v) atomicOr(flags, v);
+}
+}  // namespace hg
+
+extern "C" cudaError_t hg_launch_status_or(const uint32_t* status, int n, uint32_t* flags, cudaStream_t st)
+{
+    hg::status_or_kernel<<<4, 256, 0, st>>>(status, n, flags);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t hg_launch_stitch(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
     hg::stitch_kernel<<<grid, hg::kStitchWarps * 32, 0, st>>>(*ix, *b);

@@ -35,6 +35,7 @@ cudaError_t hg_launch_dp_large(const hg::IndexDev*, const hg::BatchDev*, int, cu
 cudaError_t hg_launch_stitch(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_rows(const hg::IndexDev*, const hg::BatchDev*, int64_t, int, cudaStream_t);
 cudaError_t hg_launch_count(const uint8_t*, int64_t, int, int, uint32_t*, cudaStream_t);
+cudaError_t hg_launch_status_or(const uint32_t*, int, uint32_t*, cudaStream_t);
 size_t hg_ksw_scratch_bytes(int, int, int, int);
 int hg_exact_ring_threads(void);
 cudaError_t hg_prepare_kernels(void);
@@ -164,6 +165,10 @@ struct hg_ctx {
     DevBuf<uint32_t> work_small, work_large;
     int64_t dp_cap = 0;
     DevBuf<uint8_t> dp_arena;
+    int64_t dp_slot_bytes = 0;
+    int dp_nslots = 0;
+    DevBuf<uint8_t> dp_slots;
+    DevBuf<uint32_t> run_flags;
     int64_t cig_cap = 0;
     DevBuf<uint32_t> cig_seg, cig;
     DevBuf<int32_t> n_cig;
@@ -509,7 +514,8 @@ extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t*
 
 namespace {
 
-constexpr int kControlWords = 16;  // queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact
+constexpr int kControlWords = 16;
+constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps  // queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
@@ -571,7 +577,9 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     c->row_stride = (L + 15) / 16 * 16;
     c->acap = max_bases / 4 + 65536;
     c->scap = max_bases / 2 + 4 * max_queries + 65536;
-    c->dp_cap = std::max<int64_t>((int64_t)1 << 30, max_bases * 4);
+    c->dp_cap = std::max<int64_t>((int64_t)1 << 30, max_bases);
+    c->dp_slot_bytes = (int64_t)256 << 10;
+    c->dp_nslots = c->sms * kLargeBlocksPerSm * 4;
     c->cig_cap = max_bases + max_queries * (L + 4);
     const int64_t n_ent = ix->dev.n_ent;
     const int grid_anchor = c->sms * 3;
@@ -593,6 +601,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->s_base.alloc(max_queries)) || (e = c->s_n.alloc(max_queries)) ||
         (e = c->n_chain.alloc(max_queries)) || (e = c->work_small.alloc(c->scap)) ||
         (e = c->work_large.alloc(c->scap)) || (e = c->dp_arena.alloc(c->dp_cap)) ||
+        (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) || (e = c->run_flags.alloc(1)) ||
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
         (e = c->rows.alloc((size_t)max_queries * c->row_stride)) || (e = c->counts.alloc(L * 7)) ||
@@ -675,6 +684,8 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
     b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
+    b.dp_slots = c->dp_slots.p, b.dp_slot_bytes = c->dp_slot_bytes, b.dp_nslots = c->dp_nslots;
+    b.run_flags = c->run_flags.p;
     b.coff = coff, b.cig_seg = c->cig_seg.p, b.cig = c->cig.p, b.n_cig = c->n_cig.p, b.has_ins = c->has_ins.p;
     b.rows = c->rows.p, b.counts = c->counts.p, b.ins = c->ins.p, b.status = c->status.p;
     return b;
@@ -701,7 +712,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(3));
     HG_CUDA(hg_launch_dp_small(&ix, &b, S * 8, st));
     HG_CUDA(mark(4));
-    HG_CUDA(hg_launch_dp_large(&ix, &b, S * 4, st));
+    HG_CUDA(hg_launch_dp_large(&ix, &b, S * kLargeBlocksPerSm, st));
     HG_CUDA(mark(5));
     HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 8)), st));
     HG_CUDA(mark(6));
@@ -709,6 +720,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(7));
     HG_CUDA(hg_launch_count(c->rows.p, c->row_stride, n, ix.L, c->counts.p, st));
     HG_CUDA(mark(8));
+    HG_CUDA(hg_launch_status_or(c->status.p, n, c->run_flags.p, st));
     (void)kStageNames;
     return HG_OK;
 }
@@ -995,6 +1007,7 @@ extern "C" int hg_run_staged(hg_ctx_t* c)
     std::fill(c->last_stage_ms, c->last_stage_ms + 8, 0.0f);
     c->last_launches = 0;
     HG_CUDA(cudaMemsetAsync(c->cells.p, 0, sizeof(unsigned long long), c->st));
+    HG_CUDA(cudaMemsetAsync(c->run_flags.p, 0, sizeof(uint32_t), c->st));
     HG_CUDA(cudaEventRecord(c->run_ev[0], c->st));
     for (const SubPlan& sp : c->staged_plan) {
         const int64_t f = sp.first;
@@ -1023,6 +1036,14 @@ extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int
         HG_CUDA(cudaMemcpy(&v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
         *cells = (int64_t)v;
     }
+    return HG_OK;
+}
+
+extern "C" int hg_staged_flags(hg_ctx_t* c, uint32_t* flags)
+{
+    if (!c || !flags) return fail(HG_ERR_ARG, "hg_staged_flags: bad arguments");
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    HG_CUDA(cudaMemcpy(flags, c->run_flags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return HG_OK;
 }
 

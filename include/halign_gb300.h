@@ -123,6 +123,9 @@ int hg_last_timing(hg_ctx_t* ctx, float* total_ms, float* stage_ms, int64_t* lau
 /* cells: extz2 band cells of the last hg_run_staged, i.e. the sum over DP
  * calls of sum_r (en0 - st0 + 1) with the band bounds of
  * src/align/ksw2_extz2_sse.c:107-110 (the GCUPS numerator). */
+/* OR of the HG_ST_* bits of every query of the last hg_run_staged
+ * (0 = every query aligned completely). */
+int hg_staged_flags(hg_ctx_t* ctx, uint32_t* flags);
 /* Enable per-stage event timing for staged runs (off by default). */
 int hg_set_timing(hg_ctx_t* ctx, int on);
 
