@@ -216,6 +216,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--queries", type=int, default=N_QUERIES, help="queries per GPU")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--sub-batch", type=int, default=25_000, help="queries per device sub-batch (sizes the arenas)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--stage-timing", action="store_true", help="per-stage event timing pass (extra run)")
     args = ap.parse_args()
@@ -233,7 +234,7 @@ def main():
         os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
     w, b = make_workload(pkg, args.queries)
     ix = pkg.Index(w.center)
-    sub = 25_000
+    sub = min(args.sub_batch, args.queries)
     ctx = pkg.Context(ix, max_queries=sub, max_bases=sub * 17_000)
     ctx.stage(b)
     # warm-up (also builds and caches the CUDA graphs of every sub-batch)
