@@ -24,6 +24,9 @@
 //   z-drop, approximate-max mode and the band-exhaustion stop.  Lanes of a
 //   diagonal run 32 at a time; the byte carried from the previous 32-lane
 //   chunk plays the role of the SSE shift-in register.
+#include <cstdio>
+#include <mutex>
+
 #include "hg_batch.cuh"
 
 namespace hg {
@@ -537,4 +540,94 @@ extern "C" cudaError_t hg_launch_ksw_single(int qlen, const uint8_t* d_query, in
     a.m = m, a.mat = d_mat, a.q = q, a.e = e, a.w = w, a.zdrop = zdrop, a.end_bonus = end_bonus, a.flag = flag;
     hg::ksw_single_kernel<<<1, 32, 0, st>>>(a, d_scratch, d_cig, cap, static_cast<hg::KswResult*>(d_res));
     return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
+// Allocation-free ksw_extz2 for callers that cannot allocate device memory.
+//
+// Some callers must not allocate: code whose device memory is owned by a
+// pool or caching allocator that has to account for every byte, and
+// latency-sensitive loops that cannot afford the device-wide
+// synchronisation cudaFree implies.  hg_ksw_extz2 allocates its scratch per
+// call, so those callers use this entry point instead: the caller passes
+// device buffers for the inputs and the outputs, and the DP scratch is a
+// fixed array compiled into this library.
+//
+// Limits and sharing rules:
+//   * the scratch is kNoAllocScratchBytes (1 MiB) per GPU; every GPU that
+//     loads the library keeps it until the process exits;
+//   * a call whose DP needs more scratch (hg_ksw_scratch_bytes) is rejected
+//     with HG_ERR_CAPACITY before anything is launched;
+//   * every call on a GPU uses the same array.  The kernel clears the parts
+//     that must start at zero itself, so a call never sees the previous
+//     call's data, but two calls that can overlap on the GPU (different
+//     streams, or different host threads) race on the array: serialise them.
+//   * the first call on a device looks up the array's device address
+//     (cudaGetSymbolAddress) with that device current; make that first call
+//     before any stream capture.
+constexpr size_t kNoAllocScratchBytes = (size_t)1 << 20;
+static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace hg {
+__global__ void ksw_noalloc_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, int cap, int32_t* res)
+{
+    if (threadIdx.x >= 32) return;
+    const KswResult R = ksw_extz2_warp(a, scratch, cig, cap);
+    if (threadIdx.x == 0) {
+        res[0] = R.max, res[1] = R.zdropped, res[2] = R.max_q, res[3] = R.max_t, res[4] = R.mqe;
+        res[5] = R.mqe_t, res[6] = R.mte, res[7] = R.mte_q, res[8] = R.score, res[9] = R.reach_end;
+        res[10] = R.n_cigar;
+    }
+}
+}  // namespace hg
+
+namespace {
+constexpr int kMaxNoAllocDevices = 64;
+uint8_t* g_noalloc_ptr[kMaxNoAllocDevices] = {};
+std::mutex g_noalloc_mu;
+
+int noalloc_fail(char* err, int64_t err_cap, int code, const char* fmt, size_t a = 0, size_t b = 0)
+{
+    if (err && err_cap > 0) std::snprintf(err, (size_t)err_cap, fmt, a, b);
+    return code;
+}
+}  // namespace
+
+extern "C" int hg_ksw_extz2_noalloc(int qlen, const uint8_t* d_query, int tlen, const uint8_t* d_target, int8_t m,
+                                    const int8_t* d_mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus,
+                                    int flag, int32_t* d_ez, uint32_t* d_cigar, int64_t cap, void* stream,
+                                    char* err, int64_t err_cap)
+{
+    if (err && err_cap > 0) err[0] = 0;
+    if (!(flag & hg::kEzGenericSc) || m <= 0 || m > 16 || !d_mat || !d_ez || (qlen > 0 && !d_query) ||
+        (tlen > 0 && !d_target) || cap < 0 || cap > INT32_MAX || (cap > 0 && !d_cigar))
+        return noalloc_fail(err, err_cap, 2, "hg_ksw_extz2_noalloc: bad arguments");  // HG_ERR_ARG
+    const size_t need = hg_ksw_scratch_bytes(qlen, tlen, w, flag);
+    if (need > kNoAllocScratchBytes)
+        return noalloc_fail(err, err_cap, 4,  // HG_ERR_CAPACITY
+                            "hg_ksw_extz2_noalloc: this alignment needs %zu scratch bytes, above the %zu-byte "
+                            "static limit; use hg_ksw_extz2",
+                            need, kNoAllocScratchBytes);
+    int dev = 0;
+    cudaError_t ce = cudaGetDevice(&dev);
+    if (ce != cudaSuccess || dev < 0 || dev >= kMaxNoAllocDevices)
+        return noalloc_fail(err, err_cap, 1, "hg_ksw_extz2_noalloc: no usable CUDA device");  // HG_ERR_CUDA
+    uint8_t* scratch;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (ce != cudaSuccess || !p)
+                return noalloc_fail(err, err_cap, 1, "hg_ksw_extz2_noalloc: cudaGetSymbolAddress failed");
+            g_noalloc_ptr[dev] = static_cast<uint8_t*>(p);
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    hg::KswArgs a{};
+    a.qlen = qlen, a.tlen = tlen, a.query = d_query, a.target = d_target;
+    a.m = m, a.mat = d_mat, a.q = q, a.e = e, a.w = w, a.zdrop = zdrop, a.end_bonus = end_bonus, a.flag = flag;
+    hg::ksw_noalloc_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(a, scratch, d_cigar, (int)cap, d_ez);
+    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(err, err_cap, 1, "hg_ksw_extz2_noalloc: launch failed");
+    return 0;
 }

@@ -150,6 +150,28 @@ int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
                      int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag, int32_t* ez_out, uint32_t* cigar,
                      int64_t cap);
 
+/* Allocation-free ksw_extz2 (no counterpart in the reference: the reference's
+ * ksw_extz2_sse allocates its work arrays with malloc on every call).
+ * For callers that cannot allocate device memory: code whose device memory
+ * belongs to a pool or caching allocator that must account for every byte,
+ * and latency-sensitive loops that cannot take the device-wide
+ * synchronisation of cudaFree.  Inputs and outputs are DEVICE pointers owned
+ * by the caller: d_query/d_target (codes < m), d_mat (m*m), d_ez (11 int32:
+ * the ez fields of hg_ksw_extz2 followed by the CIGAR length) and d_cigar
+ * (cap entries; a length above cap means the CIGAR did not fit).  The call
+ * only enqueues one kernel on `stream` (NULL = default stream) and allocates
+ * nothing; the DP scratch is one HG_NOALLOC_SCRATCH_BYTES array per GPU,
+ * held until the process exits.  A call whose scratch need exceeds it returns
+ * HG_ERR_CAPACITY before launching (err, when non-NULL, gets the message).
+ * All calls on a GPU share that array: calls that may overlap on the GPU
+ * race and must be serialised.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture.  Only KSW_EZ_GENERIC_SC scoring. */
+#define HG_NOALLOC_SCRATCH_BYTES (1u << 20)
+int hg_ksw_extz2_noalloc(int qlen, const uint8_t* d_query, int tlen, const uint8_t* d_target, int8_t m,
+                         const int8_t* d_mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag,
+                         int32_t* d_ez, uint32_t* d_cigar, int64_t cap, void* stream, char* err, int64_t err_cap);
+
 /* align::globalAlignKSW2 (src/align/align.cpp:22-65); flag < 0 selects the
  * default KSW_EZ_GENERIC_SC|KSW_EZ_RIGHT. */
 int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int flag, uint32_t* cigar,
