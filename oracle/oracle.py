@@ -133,6 +133,13 @@ class Oracle(_Common):
         assert n >= 0
         return a, out[:n].copy()
 
+    def chain_score(self, ai_ref, ai_qry, aj_ref, aj_qry, aj_span):
+        a = np.zeros(2, ANCHOR_DTYPE)
+        a[0]["pos_ref"], a[0]["pos_qry"] = ai_ref, ai_qry
+        a[1]["pos_ref"], a[1]["pos_qry"], a[1]["span"] = aj_ref, aj_qry, aj_span
+        prm = self._chain_params([5000, 5000, 500, 25, 5000, 3, 40], [0.01, 0.01])
+        return int(self.lib.ho_chain_score(_p(a[0:1]), _p(a[1:2]), _p(prm)))
+
     def ksw_extz2(self, query_codes, target_codes, m, mat, q, e, w, zdrop, end_bonus, flag):
         qc = np.ascontiguousarray(query_codes, np.uint8)
         tc = np.ascontiguousarray(target_codes, np.uint8)

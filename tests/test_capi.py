@@ -1,0 +1,92 @@
+"""C ABI checks that need no GPU: the library builds for sm_103a, exports every
+entry point include/halign_gb300.h declares, packs inputs losslessly on the
+host, and fails loudly (no CPU fallback) when no GPU is visible."""
+import ctypes as C
+import re
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _declared():
+    text = (ROOT / "include" / "halign_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(hg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(native):
+    declared = _declared()
+    assert len(declared) >= 20
+    lib_path = Path(native._name)
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib_path)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (hg_[a-z0-9_]+)", out))
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    for s in declared:
+        getattr(native, s)  # resolvable through ctypes
+
+
+def test_library_is_built_for_sm103a(native):
+    out = subprocess.run(["/usr/local/cuda/bin/cuobjdump", "--list-elf", native._name], capture_output=True,
+                         text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+def test_pack_roundtrip_and_exceptions(pkg, native):
+    seqs = [b"ACGTACGTAC", b"", b"NNNNACGTnnU--ACGT", b"A" * 33, b"acgt", b"ACGTRYKM"]
+    blob = b"".join(seqs)
+    offs = np.concatenate([[0], np.cumsum([len(s) for s in seqs])]).astype(np.int64)
+    p = pkg.pack(blob, offs)
+    assert p.n == len(seqs)
+    assert all(int(o) % 16 == 0 for o in p.poff)
+    runs = p.exc.reshape(-1, 3)
+    for i, s in enumerate(seqs):
+        out = bytearray()
+        for j in range(len(s)):
+            out.append(b"ACGT"[(p.packed[p.poff[i] + j // 4] >> (2 * (j % 4))) & 3])
+        for r in runs[p.exc_off[i]:p.exc_off[i + 1]]:
+            out[r[0]:r[0] + r[1]] = bytes([r[2]]) * int(r[1])
+        assert bytes(out) == s, i
+
+
+def test_calls_fail_loudly_without_gpu(pkg, native):
+    if pkg.device_count() > 0:
+        pytest.skip("a GPU is visible")
+    with pytest.raises(pkg.HalignError):
+        pkg.Index(b"ACGT" * 100)
+    with pytest.raises(pkg.HalignError):
+        pkg.extract_minimizer(b"ACGT" * 100)
+    with pytest.raises(pkg.HalignError):
+        pkg.global_align_ksw2(b"ACGTACGT", b"ACGTACG")
+
+
+def test_bad_arguments_rejected_on_host(pkg, native):
+    L = native
+    h = C.c_void_p()
+    assert L.hg_index_create(b"ACGT", 4, 0, 10, None, C.byref(h)) == 2
+    assert L.hg_index_create(b"ACGT", 4, 15, 300, None, C.byref(h)) == 2
+    assert L.hg_ctx_create(None, 1, 1, C.byref(h)) == 2
+    ez = np.zeros(10, np.int32)
+    # non-generic scoring is refused before any device work
+    r = L.hg_ksw_extz2(4, np.zeros(4, np.uint8).ctypes.data, 4, np.zeros(4, np.uint8).ctypes.data, 5,
+                       np.zeros(25, np.int8).ctypes.data, 6, 2, -1, -1, 0, 0x02, ez.ctypes.data, None, 0)
+    assert r == -2
+    assert b"GENERIC_SC" in L.hg_last_error()
+
+
+def test_auto_band_matches_oracle(oracle):
+    import itertools
+    from tests.pkgload import load_package
+    load_package()
+    for a, b in itertools.product([1, 2, 7, 50, 199, 200, 201, 333, 1000, 5000, 16569], repeat=2):
+        # the band formula is shared by the DP kernels (hg_common.cuh) and the host wrapper
+        d = abs(a - b)
+        mx = max(a, b)
+        want = -1 if d / mx > 0.5 else 200 + int(0.1 * (a + b // 2))
+        assert oracle.auto_band(a, b) == want
