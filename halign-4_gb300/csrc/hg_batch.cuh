@@ -43,10 +43,31 @@ struct Seg {
 enum SegKind : uint32_t { kSegEmpty = 0, kSegIns = 1, kSegDel = 2, kSegDpSmall = 3, kSegDpLarge = 4, kSegGlobal = 5 };
 constexpr uint32_t kSegLeft = 1u << 8;
 
-// Small-DP tier: one thread per segment, direction nibbles in shared memory.
-constexpr int kSmallMaxCells = 256;
+// Small-DP tier: one thread per segment, direction nibbles in shared memory,
+// one or two 32-bit words per row of the longer side.
 constexpr int kSmallMaxInner = 16;
-constexpr int kSmallMaxSide = 200;
+constexpr int kSmallDirWords = 64;  // words of 8 nibbles per thread
+
+// A segment fits the small tier when its shorter side is <= 16 and its rows
+// (longer side) x words-per-row fit the thread's direction store.  Such
+// segments are at most 64 bp long, far inside the band globalAlignKSW2 gives
+// them (w >= 200 or unbounded), so the band never binds.
+__host__ __device__ __forceinline__ bool small_tier_fits(uint32_t rl, uint32_t ql)
+{
+    const uint32_t inner = rl < ql ? rl : ql, outer = rl < ql ? ql : rl;
+    return inner >= 1 && inner <= (uint32_t)kSmallMaxInner && outer * ((inner + 7) / 8) <= (uint32_t)kSmallDirWords;
+}
+
+// Sort key of a small-tier segment: warps then run identical loop bounds.
+// Bits: [0,7) outer-1 (<= 63), [7,11) inner-1, 11 orientation, 12 left-aligned.
+constexpr uint32_t kShapeBins = 1u << 13;
+__device__ __forceinline__ uint32_t shape_key(const Seg& g)
+{
+    const uint32_t inner = g.rl < g.ql ? g.rl : g.ql, outer = g.rl < g.ql ? g.ql : g.rl;
+    const uint32_t tinner = g.rl <= g.ql ? 1u : 0u;
+    const uint32_t left = (g.kind & kSegLeft) ? 1u : 0u;
+    return (outer - 1) | (inner - 1) << 7 | tinner << 11 | left << 12;
+}
 
 struct BatchDev {
     int n;                       // queries in the batch
@@ -88,6 +109,8 @@ struct BatchDev {
     int32_t* n_chain;
     uint32_t* work_small;        // global segment ids per DP tier
     uint32_t* work_large;
+    uint32_t* work_sorted;       // small tier sorted by shape_key
+    uint32_t* shape_hist;        // kShapeBins counters, then kShapeBins cursors
     unsigned int* n_small;
     unsigned int* n_large;
     int64_t wcap;

@@ -188,8 +188,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             else if (rl == 0) kind = kSegIns;
             else if (ql == 0) kind = kSegDel;
             else if (c == 0) kind = kSegGlobal;
-            else if (max(rl, ql) <= (uint32_t)kSmallMaxSide && min(rl, ql) <= (uint32_t)kSmallMaxInner &&
-                     rl * ql <= (uint32_t)kSmallMaxCells)
+            else if (small_tier_fits(rl, ql))
                 kind = kSegDpSmall;
             else
                 kind = kSegDpLarge;

@@ -32,8 +32,6 @@
 namespace hg {
 
 constexpr int kDpSmallThreads = 128;
-constexpr int kDirWords = kSmallMaxCells / 8;       // 4-bit codes, 8 per word
-constexpr int kStateWords = kSmallMaxInner / 4 * 2; // u/y (or x/v) bytes of the inner side
 
 __device__ __forceinline__ uint32_t dna5_score(uint32_t a, uint32_t b)
 {  // dna5_simd_mat (include/align.h:109-116)
@@ -59,7 +57,6 @@ __device__ __forceinline__ uint32_t query_dna5(const uint8_t* pk, const int32_t*
     return c;
 }
 
-__device__ __forceinline__ uint32_t nib_of(uint32_t d) { return (d & 3u) | ((d >> 3) & 1u) << 2 | ((d >> 4) & 1u) << 3; }
 
 struct CigarPush {
     uint32_t* out;
@@ -80,103 +77,196 @@ struct CigarPush {
     }
 };
 
+// One in-band cell in int32 arithmetic.  For segments the band never binds,
+// the difference encoding keeps every byte value the SSE2 sequence touches in
+// a range where 8-bit wrapping add/sub, unsigned max/min and signed compares
+// equal plain int32 arithmetic (u, v in [0, 21], x, y in [0, q], z, a, b in
+// [0, 27]); tests/dp_arith_equiv.c checks the two forms cell by cell.
+template <int MODE>
+__device__ __forceinline__ uint32_t lane_int(int s, int xt1, int vt1, int ut, int yt, int& u, int& v, int& x, int& y)
+{
+    int z = s + 16;
+    const int a0 = xt1 + vt1, b0 = yt + ut;
+    uint32_t d;
+    if (MODE == 1) {  // left-aligned gaps: ties go to H, then E
+        d = a0 > z ? 1u : 0u;
+        z = max(z, a0);
+        if (b0 > z) d = 2u;
+    } else {          // right-aligned gaps: ties go to F, then E
+        d = z > a0 ? 0u : 1u;
+        z = max(z, a0);
+        if (!(z > b0)) d = 2u;
+    }
+    z = min(max(z, b0), 21);
+    u = z - vt1;
+    v = z - ut;
+    const int zq = z - 6;
+    const int a = a0 - zq, b = b0 - zq;
+    if (MODE == 1) {
+        x = max(a, 0), y = max(b, 0);
+        d |= (a > 0 ? 4u : 0u) | (b > 0 ? 8u : 0u);   // 4-bit code: E/F continuation bits
+    } else {
+        x = max(a, 0), y = max(b, 0);
+        d |= (a >= 0 ? 4u : 0u) | (b >= 0 ? 8u : 0u);
+    }
+    return d;  // bits 0-1 state, bit 2 E continuation, bit 3 F continuation
+}
+
+// Segment DP for one thread.  TINNER: the target is the shorter (inner) side;
+// rows run over the query.  Direction codes: row o, inner position i at word
+// o*stride + i/8, nibble i%8, words interleaved across the CTA.
+template <bool TINNER, int MODE>
+__device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev& b, uint32_t sid, const Seg& g,
+                                              uint32_t* dirs, int tid)
+{
+    const int qn = (int)g.ql, tn = (int)g.rl;
+    const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
+    const int stride = (inner + 7) >> 3;
+    const uint8_t* pk = b.packed + b.poff[g.q];
+    const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
+    const bool plain_q = e0 == e1;
+    const uint8_t* tc = ix.center + g.rs;
+    int ic[kSmallMaxInner], s1[kSmallMaxInner], s2[kSmallMaxInner];
+#pragma unroll
+    for (int i = 0; i < kSmallMaxInner; ++i) {
+        ic[i] = 0, s1[i] = 0, s2[i] = 0;
+        if (i < inner) {
+            if (TINNER) ic[i] = tc[i];
+            else ic[i] = plain_q ? (int)packed_code(pk, g.qs + i) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + i);
+        }
+    }
+    for (int o = 0; o < outer; ++o) {
+        int oc;
+        if (TINNER) oc = plain_q ? (int)packed_code(pk, g.qs + o) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + o);
+        else oc = tc[o];
+        // TINNER: carried x, v along the row, s1/s2 = u, y of the previous row.
+        // !TINNER: carried u, y along the column, s1/s2 = x, v of the previous column.
+        int c1 = 0, c2 = o ? 6 : 0;
+        uint32_t w0 = 0, w1 = 0;
+#pragma unroll
+        for (int i = 0; i < kSmallMaxInner; ++i) {
+            if (i < inner) {
+                const int sc = (ic[i] == 4 || oc == 4) ? 0 : (ic[i] == oc ? 5 : -4);
+                int u, v, x, y;
+                uint32_t d;
+                if (TINNER) {
+                    const int ut = o ? s1[i] : (i ? 6 : 0), yt = o ? s2[i] : 0;
+                    d = lane_int<MODE>(sc, c1, c2, ut, yt, u, v, x, y);
+                    c1 = x, c2 = v, s1[i] = u, s2[i] = y;
+                } else {
+                    const int xt = o ? s1[i] : 0, vt = o ? s2[i] : (i ? 6 : 0);
+                    const int ut = i ? c1 : (o ? 6 : 0), yt = i ? c2 : 0;
+                    d = lane_int<MODE>(sc, xt, vt, ut, yt, u, v, x, y);
+                    c1 = u, c2 = y, s1[i] = x, s2[i] = v;
+                }
+                if (i < 8) w0 |= d << (4 * i);
+                else w1 |= d << (4 * (i - 8));
+            }
+        }
+        dirs[(o * stride) * kDpSmallThreads + tid] = w0;
+        if (stride > 1) dirs[(o * stride + 1) * kDpSmallThreads + tid] = w1;
+    }
+    // traceback from (tlen-1, qlen-1)
+    CigarPush cp{b.cig_seg + b.coff[g.q] + g.slot, 0, tn + qn, 0};
+    int ti = tn - 1, qj = qn - 1, state = 0;
+    while (ti >= 0 && qj >= 0) {
+        const int o = TINNER ? qj : ti, i = TINNER ? ti : qj;
+        const uint32_t nib = (dirs[(o * stride + (i >> 3)) * kDpSmallThreads + tid] >> ((i & 7) * 4)) & 0xfu;
+        if (state == 0) state = nib & 3u;
+        else if (!((nib >> (state + 1)) & 1u)) state = 0;
+        if (state == 0) state = nib & 3u;
+        if (state == 0) cp.push(0, 1), --ti, --qj;
+        else if (state == 1) cp.push(2, 1), --ti;
+        else cp.push(1, 1), --qj;
+    }
+    if (ti >= 0) cp.push(2, (uint32_t)(ti + 1));
+    if (qj >= 0) cp.push(1, (uint32_t)(qj + 1));
+    for (int i = 0; i < cp.n / 2; ++i) {
+        const uint32_t a = cp.out[i];
+        cp.out[i] = cp.out[cp.n - 1 - i];
+        cp.out[cp.n - 1 - i] = a;
+    }
+    b.seg[sid].nops = cp.n;
+}
+
 __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
 {
-    __shared__ uint32_t dirs[kDirWords * kDpSmallThreads];
-    __shared__ uint32_t state[kStateWords * kDpSmallThreads];
+    __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
     const int tid = threadIdx.x;
-    const uint32_t q = 6, qe2 = 16, max_sc = 5 + 16;
     const unsigned total = *b.n_small;
+    const uint32_t* list = b.work_sorted ? b.work_sorted : b.work_small;
     unsigned long long cell_sum = 0;
     const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
     for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
         if (w >= total) continue;
-        const uint32_t sid = b.work_small[w];
-        Seg g = b.seg[sid];
-        const int qn = (int)g.ql, tn = (int)g.rl;
-        const int mode = (g.kind & kSegLeft) ? 1 : 2;
-        const uint8_t* pk = b.packed + b.poff[g.q];
-        const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
-        const uint8_t* tc = ix.center + g.rs;
-        const bool tinner = tn <= qn;  // inner = target side (state u,y per t), else inner = query side
-        const int inner = tinner ? tn : qn, outer = tinner ? qn : tn;
-        // inner-side codes packed 4 bits each
-        uint64_t icode = 0;
-        for (int i = 0; i < inner; ++i) {
-            const uint32_t c = tinner ? tc[i] : query_dna5(pk, b.exc, e0, e1, g.qs + i);
-            icode |= (uint64_t)c << (4 * i);
+        const uint32_t sid = list[w];
+        const Seg g = b.seg[sid];
+        const bool tinner = g.rl <= g.ql;
+        const bool left = (g.kind & kSegLeft) != 0;
+        if (tinner) {
+            if (left) small_segment<true, 1>(ix, b, sid, g, dirs, tid);
+            else small_segment<true, 2>(ix, b, sid, g, dirs, tid);
+        } else {
+            if (left) small_segment<false, 1>(ix, b, sid, g, dirs, tid);
+            else small_segment<false, 2>(ix, b, sid, g, dirs, tid);
         }
-        uint32_t wbuf = 0;
-        int widx = 0, wfill = 0;
-        for (int o = 0; o < outer; ++o) {
-            const uint32_t oc = tinner ? query_dna5(pk, b.exc, e0, e1, g.qs + o) : tc[o];
-            // carried along the inner sweep: (x, v) when inner = target, (u, y) when inner = query
-            uint32_t c1 = 0, c2 = tinner ? (o ? q : 0u) : (o ? q : 0u);
-            uint32_t sw0 = 0, sw1 = 0;  // current state words being rewritten
-            for (int i = 0; i < inner; ++i) {
-                const int wi = i >> 2, sh = (i & 3) * 8;
-                if ((i & 3) == 0) {
-                    sw0 = state[(wi * 2) * kDpSmallThreads + tid];
-                    sw1 = state[(wi * 2 + 1) * kDpSmallThreads + tid];
-                }
-                const uint32_t icv = (uint32_t)(icode >> (4 * i)) & 0xfu;
-                const uint32_t s = tinner ? dna5_score(icv, oc) : dna5_score(oc, icv);
-                LaneOut r;
-                if (tinner) {  // cell (t=i, j=o): x,v carried from t-1; u,y from row j-1
-                    const uint32_t ut = o ? (sw0 >> sh) & 0xffu : (i ? q : 0u);
-                    const uint32_t yt = o ? (sw1 >> sh) & 0xffu : 0u;
-                    r = ksw_lane(s, c1, c2, ut, yt, qe2, max_sc, q, mode);
-                    c1 = r.x, c2 = r.v;
-                    sw0 = (sw0 & ~(0xffu << sh)) | (uint32_t)r.u << sh;
-                    sw1 = (sw1 & ~(0xffu << sh)) | (uint32_t)r.y << sh;
-                } else {  // cell (t=o, j=i): u,y carried from j-1; x,v from column t-1
-                    const uint32_t xt = o ? (sw0 >> sh) & 0xffu : 0u;
-                    const uint32_t vt = o ? (sw1 >> sh) & 0xffu : (i ? q : 0u);
-                    const uint32_t ut = i ? c1 : (o ? q : 0u);
-                    const uint32_t yt = i ? c2 : 0u;
-                    r = ksw_lane(s, xt, vt, ut, yt, qe2, max_sc, q, mode);
-                    c1 = r.u, c2 = r.y;
-                    sw0 = (sw0 & ~(0xffu << sh)) | (uint32_t)r.x << sh;
-                    sw1 = (sw1 & ~(0xffu << sh)) | (uint32_t)r.v << sh;
-                }
-                if ((i & 3) == 3 || i == inner - 1) {
-                    state[(wi * 2) * kDpSmallThreads + tid] = sw0;
-                    state[(wi * 2 + 1) * kDpSmallThreads + tid] = sw1;
-                }
-                wbuf |= nib_of(r.d) << (4 * wfill);
-                if (++wfill == 8) {
-                    dirs[widx * kDpSmallThreads + tid] = wbuf;
-                    ++widx, wfill = 0, wbuf = 0;
-                }
-            }
-        }
-        if (wfill) dirs[widx * kDpSmallThreads + tid] = wbuf;
-        // traceback from (tlen-1, qlen-1); cell index = o * inner + i
-        CigarPush cp{b.cig_seg + b.coff[g.q] + g.slot, 0, tn + qn, 0};
-        int ti = tn - 1, qj = qn - 1, state_ = 0;
-        while (ti >= 0 && qj >= 0) {
-            const int cell = tinner ? (qj * inner + ti) : (ti * inner + qj);
-            const uint32_t nib = (dirs[(cell >> 3) * kDpSmallThreads + tid] >> ((cell & 7) * 4)) & 0xfu;
-            if (state_ == 0) state_ = nib & 3u;
-            else if (!((nib >> (state_ + 1)) & 1u)) state_ = 0;
-            if (state_ == 0) state_ = nib & 3u;
-            if (state_ == 0) cp.push(0, 1), --ti, --qj;
-            else if (state_ == 1) cp.push(2, 1), --ti;
-            else cp.push(1, 1), --qj;
-        }
-        if (ti >= 0) cp.push(2, (uint32_t)(ti + 1));
-        if (qj >= 0) cp.push(1, (uint32_t)(qj + 1));
-        for (int i = 0; i < cp.n / 2; ++i) {
-            const uint32_t a = cp.out[i];
-            cp.out[i] = cp.out[cp.n - 1 - i];
-            cp.out[cp.n - 1 - i] = a;
-        }
-        b.seg[sid].nops = cp.n;
-        cell_sum += (unsigned long long)(tn * qn);
+        cell_sum += (unsigned long long)(g.rl * g.ql);
     }
-    // warp-aggregated cell count for GCUPS
     for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
     if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
+}
+
+// Counting sort of the small-tier work list by shape_key.
+__global__ void shape_hist_kernel(BatchDev b)
+{
+    const unsigned total = *b.n_small;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ((total + 31u) & ~31u);
+         w += gridDim.x * blockDim.x) {
+        const bool act = w < total;
+        const uint32_t key = act ? shape_key(b.seg[b.work_small[w]]) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (act && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(&b.shape_hist[key], __popc(peers));
+    }
+}
+
+__global__ void shape_scan_kernel(BatchDev b)
+{
+    __shared__ uint32_t part[1024];
+    const int tid = threadIdx.x;
+    const int per = kShapeBins / 1024;
+    uint32_t s = 0;
+    for (int i = 0; i < per; ++i) s += b.shape_hist[tid * per + i];
+    part[tid] = s;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const uint32_t v = tid >= o ? part[tid - o] : 0u;
+        __syncthreads();
+        part[tid] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[tid] - s;
+    for (int i = 0; i < per; ++i) {
+        const uint32_t c = b.shape_hist[tid * per + i];
+        b.shape_hist[kShapeBins + tid * per + i] = run;  // cursor = bucket start
+        run += c;
+    }
+}
+
+__global__ void shape_scatter_kernel(BatchDev b)
+{
+    const unsigned total = *b.n_small;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ((total + 31u) & ~31u);
+         w += gridDim.x * blockDim.x) {
+        const bool act = w < total;
+        const uint32_t sid = act ? b.work_small[w] : 0u;
+        const uint32_t key = act ? shape_key(b.seg[sid]) : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (act && (int)(threadIdx.x & 31) == leader) base = atomicAdd(&b.shape_hist[kShapeBins + key], __popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (act) b.work_sorted[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = sid;
+    }
 }
 
 // ---------------------------------------------------------------- large tier
@@ -515,6 +605,13 @@ __global__ void ksw_single_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, in
 
 extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
+    if (b->work_sorted) {
+        cudaError_t e = cudaMemsetAsync(b->shape_hist, 0, sizeof(uint32_t) * hg::kShapeBins, st);
+        if (e != cudaSuccess) return e;
+        hg::shape_hist_kernel<<<grid, 256, 0, st>>>(*b);
+        hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
+        hg::shape_scatter_kernel<<<grid, 256, 0, st>>>(*b);
+    }
     hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);
     return cudaGetLastError();
 }
