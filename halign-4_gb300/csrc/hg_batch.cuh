@@ -110,6 +110,7 @@ struct BatchDev {
     uint32_t* work_small;        // global segment ids per DP tier
     uint32_t* work_large;
     uint32_t* work_sorted;       // small tier sorted by shape_key
+    uint32_t* work_key;          // shape_key of each work_small entry (written with it)
     uint32_t* shape_hist;        // kShapeBins counters, then kShapeBins cursors
     unsigned int* n_small;
     unsigned int* n_large;

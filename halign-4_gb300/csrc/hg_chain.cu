@@ -217,8 +217,27 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const unsigned below = (1u << lane) - 1u;
             if (ms >> lane & 1u) {
                 const unsigned w = bs + __popc(ms & below);
-                if ((int64_t)w < b.wcap) b.work_small[w] = (uint32_t)(sb + s);
-                else atomicOr(&b.status[q], kStArenaOverflow);
+                if ((int64_t)w < b.wcap) {
+                    b.work_small[w] = (uint32_t)(sb + s);
+                    if (b.work_key) {
+                        Seg g;
+                        g.rl = rl, g.ql = ql, g.kind = kind | flags;
+                        b.work_key[w] = shape_key(g);
+                    }
+                } else {
+                    atomicOr(&b.status[q], kStArenaOverflow);
+                }
+            }
+            // histogram of small-tier shapes (lanes with equal keys add once)
+            if (b.work_key) {
+                uint32_t key = 0xffffffffu;
+                if (ms >> lane & 1u) {
+                    Seg g;
+                    g.rl = rl, g.ql = ql, g.kind = kind | flags;
+                    key = shape_key(g);
+                }
+                const unsigned peers = __match_any_sync(FULL, key);
+                if ((ms >> lane & 1u) && lane == __ffs(peers) - 1) atomicAdd(&b.shape_hist[key], __popc(peers));
             }
             if (ml >> lane & 1u) {
                 const unsigned w = bl + __popc(ml & below);

@@ -216,19 +216,8 @@ __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, 
     if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
 }
 
-// Counting sort of the small-tier work list by shape_key.
-__global__ void shape_hist_kernel(BatchDev b)
-{
-    const unsigned total = *b.n_small;
-    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ((total + 31u) & ~31u);
-         w += gridDim.x * blockDim.x) {
-        const bool act = w < total;
-        const uint32_t key = act ? shape_key(b.seg[b.work_small[w]]) : 0xffffffffu;
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        if (act && (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(&b.shape_hist[key], __popc(peers));
-    }
-}
-
+// Counting sort of the small-tier work list by shape_key: the chain kernel
+// writes each entry's key and the histogram; scan + scatter follow.
 __global__ void shape_scan_kernel(BatchDev b)
 {
     __shared__ uint32_t part[1024];
@@ -259,7 +248,7 @@ __global__ void shape_scatter_kernel(BatchDev b)
          w += gridDim.x * blockDim.x) {
         const bool act = w < total;
         const uint32_t sid = act ? b.work_small[w] : 0u;
-        const uint32_t key = act ? shape_key(b.seg[sid]) : 0xffffffffu;
+        const uint32_t key = act ? b.work_key[w] : 0xffffffffu;
         const unsigned peers = __match_any_sync(0xffffffffu, key);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
@@ -606,9 +595,6 @@ __global__ void ksw_single_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, in
 extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
     if (b->work_sorted) {
-        cudaError_t e = cudaMemsetAsync(b->shape_hist, 0, sizeof(uint32_t) * hg::kShapeBins, st);
-        if (e != cudaSuccess) return e;
-        hg::shape_hist_kernel<<<grid, 256, 0, st>>>(*b);
         hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
         hg::shape_scatter_kernel<<<grid, 256, 0, st>>>(*b);
     }

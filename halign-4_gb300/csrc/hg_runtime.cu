@@ -162,7 +162,7 @@ struct hg_ctx {
     DevBuf<hg::Seg> seg;
     DevBuf<int64_t> s_base;
     DevBuf<int32_t> s_n, n_chain;
-    DevBuf<uint32_t> work_small, work_large, work_sorted, shape_hist;
+    DevBuf<uint32_t> work_small, work_large, work_sorted, work_key, shape_hist;
     int64_t dp_cap = 0;
     DevBuf<uint8_t> dp_arena;
     int64_t dp_slot_bytes = 0;
@@ -601,7 +601,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->s_base.alloc(max_queries)) || (e = c->s_n.alloc(max_queries)) ||
         (e = c->n_chain.alloc(max_queries)) || (e = c->work_small.alloc(c->scap)) ||
         (e = c->work_large.alloc(c->scap)) || (e = c->dp_arena.alloc(c->dp_cap)) ||
-        (e = c->work_sorted.alloc(c->scap)) || (e = c->shape_hist.alloc(2 * (size_t)hg::kShapeBins)) ||
+        (e = c->work_sorted.alloc(c->scap)) || (e = c->work_key.alloc(c->scap)) ||
+        (e = c->shape_hist.alloc(2 * (size_t)hg::kShapeBins)) ||
         (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) || (e = c->run_flags.alloc(1)) ||
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
@@ -684,7 +685,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.a_base = c->a_base.p, b.a_n = c->a_n.p, b.ent_cnt = c->ent_cnt.p;
     b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
     b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
-    b.work_sorted = c->work_sorted.p, b.shape_hist = c->shape_hist.p;
+    b.work_sorted = c->work_sorted.p, b.work_key = c->work_key.p, b.shape_hist = c->shape_hist.p;
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
     b.dp_slots = c->dp_slots.p, b.dp_slot_bytes = c->dp_slot_bytes, b.dp_nslots = c->dp_nslots;
     b.run_flags = c->run_flags.p;
@@ -703,6 +704,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     cudaStream_t st = c->st;
     HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, st));
     HG_CUDA(cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * (size_t)b.n, st));
+    HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, st));
     const int n = b.n;
     auto mark = [&](int i) -> cudaError_t { return timed ? cudaEventRecord(c->ev[i], st) : cudaSuccess; };
     HG_CUDA(mark(0));
@@ -894,6 +896,7 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
                 if (i == 0) HG_CUDA(cudaMemsetAsync(c->status.p, 0, 4 * (size_t)sp.n, c->st));
                 // status must survive the per-launch reset: enqueue without the batch memset
                 HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, c->st));
+                HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, c->st));
                 const hg::IndexDev& ix = c->ix->dev;
                 HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, 1, c->st));
                 HG_CUDA(hg_launch_anchor(&ix, &b, 1, c->st));

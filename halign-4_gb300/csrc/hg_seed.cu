@@ -51,6 +51,7 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDe
     __shared__ uint64_t hsh[kHashBuf];
     __shared__ uint8_t strand[kHashBuf];
     __shared__ int32_t mpos[kSeedTile + 1];
+    __shared__ int16_t pre[kHashBuf], suf[kHashBuf];  // block prefix / suffix arg-min (relative to hs)
     __shared__ int scan_s[33];
     __shared__ int s_q, s_ovf;
 
@@ -133,31 +134,82 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDe
                 __syncthreads();
                 // 3. window minimum m(p) for p in [p0-1, pend)
                 const int mlo = p0 - 1;
-                for (int p = max(mlo, 0) + tid; p < pend; p += kSeedThreads) {
-                    int best = -1;
-                    const uint64_t hp = hsh[p - hs];
-                    if (hp != kNoHash) {
-                        best = p;
-                        uint64_t bh = hp, nxt = hp;
-                        bool inc = true;
-                        const int lo = max(p - win + 1, 0);
-                        for (int qq = p - 1; qq >= lo; --qq) {
-                            const uint64_t hq = hsh[qq - hs];
-                            if (hq == kNoHash) {
-                                inc = false;
-                                break;
-                            }
-                            if (hq < bh) bh = hq, best = qq;
-                            inc = inc && hq < nxt;
-                            nxt = hq;
+                if (win <= k) {
+                    // Between two N-free runs lie >= k invalid k-mers, so a window of
+                    // win <= k positions only holds valid k-mers of p's own run and an
+                    // invalid k-mer can stand for +infinity (kNoHash > every hash).
+                    // Arg-min over [p-win+1, p] from block prefix/suffix minima over
+                    // blocks of win positions (ties: the later position).
+                    const int b0 = hs / win, b1 = (pend - 1) / win;
+                    for (int bb = b0 + tid; bb <= b1; bb += kSeedThreads) {
+                        const int lo = max(bb * win, hs), hi = min(bb * win + win, pend);
+                        int best = lo;
+                        uint64_t bh = hsh[lo - hs];
+                        pre[lo - hs] = (int16_t)(lo - hs);
+                        for (int x = lo + 1; x < hi; ++x) {
+                            const uint64_t h = hsh[x - hs];
+                            if (h <= bh) bh = h, best = x;
+                            pre[x - hs] = (int16_t)(best - hs);
                         }
-                        // full queue before the push at p: hashes strictly increase on [p-win, p]
-                        if (p >= p0 && inc && p - win >= 0) {
-                            const uint64_t hq = hsh[p - win - hs];
-                            if (hq != kNoHash && hq < nxt) s_ovf = 1;
+                        best = hi - 1;
+                        bh = hsh[best - hs];
+                        suf[best - hs] = (int16_t)(best - hs);
+                        for (int x = hi - 2; x >= lo; --x) {
+                            const uint64_t h = hsh[x - hs];
+                            if (h < bh) bh = h, best = x;
+                            suf[x - hs] = (int16_t)(best - hs);
                         }
                     }
-                    mpos[p - mlo] = best;
+                    __syncthreads();
+                    for (int p = max(mlo, 0) + tid; p < pend; p += kSeedThreads) {
+                        int best = -1;
+                        const uint64_t hp = hsh[p - hs];
+                        if (hp != kNoHash) {
+                            const int a = max(p - win + 1, 0);
+                            const int rp = hs + pre[p - hs];
+                            if (a / win == p / win || a < hs) {
+                                best = rp;
+                            } else {
+                                const int ls = hs + suf[a - hs];
+                                best = hsh[ls - hs] < hsh[rp - hs] ? ls : rp;
+                            }
+                            // the queue is full before the push at p when hashes strictly
+                            // increase over [p-win, p]; walk back over the increases
+                            if (p >= p0 && p - win >= 0) {
+                                int x = p;
+                                while (x > p - win && hsh[x - 1 - hs] != kNoHash && hsh[x - 1 - hs] < hsh[x - hs]) --x;
+                                if (x == p - win) s_ovf = 1;
+                            }
+                        }
+                        mpos[p - mlo] = best;
+                    }
+                } else {
+                    for (int p = max(mlo, 0) + tid; p < pend; p += kSeedThreads) {
+                        int best = -1;
+                        const uint64_t hp = hsh[p - hs];
+                        if (hp != kNoHash) {
+                            best = p;
+                            uint64_t bh = hp, nxt = hp;
+                            bool inc = true;
+                            const int lo = max(p - win + 1, 0);
+                            for (int qq = p - 1; qq >= lo; --qq) {
+                                const uint64_t hq = hsh[qq - hs];
+                                if (hq == kNoHash) {
+                                    inc = false;
+                                    break;
+                                }
+                                if (hq < bh) bh = hq, best = qq;
+                                inc = inc && hq < nxt;
+                                nxt = hq;
+                            }
+                            // full queue before the push at p: hashes strictly increase on [p-win, p]
+                            if (p >= p0 && inc && p - win >= 0) {
+                                const uint64_t hq = hsh[p - win - hs];
+                                if (hq != kNoHash && hq < nxt) s_ovf = 1;
+                            }
+                        }
+                        mpos[p - mlo] = best;
+                    }
                 }
                 __syncthreads();
                 // 4. emission + compaction in position order
