@@ -175,6 +175,51 @@ def algorithmic_bytes(b, n_cigar_words: int, L: int):
     return inp + out
 
 
+def measure_plain(pkg, ctx, w, n_plain: int):
+    """The plain form (one launch sequence per query, hg_align_plain) on the
+    first n_plain queries, and the batched form on the same queries."""
+    offs = w.offsets[: n_plain + 1]
+    b = pkg.pack(w.seqs[: offs[-1]], offs)
+    ctx.align(b, rows=True, plain=True)  # warm-up
+    t0 = time.perf_counter()
+    ctx.align(b, rows=True, plain=True)
+    t_plain = time.perf_counter() - t0
+    ctx.align(b, rows=True)
+    t0 = time.perf_counter()
+    ctx.align(b, rows=True)
+    t_batch = time.perf_counter() - t0
+    return {"queries": n_plain, "plain_mbp_per_s": round(b.bases / t_plain / 1e6, 3),
+            "batched_same_queries_mbp_per_s": round(b.bases / t_batch / 1e6, 3),
+            "note": "host-timed hg_align_plain vs hg_align_batch (both with H2D/D2H) on the same queries"}
+
+
+def measure_serving(pkg, n_req: int, rate: float):
+    """Continuous-batching loop (config: Poisson arrivals at `rate` req/s,
+    500..29,903 bp substrings of a 29,903 bp center, 0.5% divergence)."""
+    w = pkg.synth.serve(n_req, rate=rate)
+    ix = pkg.Index(w.center)
+    srv = pkg.serve.Server(ix, n_slots=4, slot_queries=256, slot_bases=8_000_000, budget_bytes=40 << 30)
+    srv.run(w.seqs, w.offsets[: min(w.n, 200) + 1], None)  # warm-up (graph-free async path)
+    st = srv.run(w.seqs, w.offsets, w.arrivals)
+    sat = srv.run(w.seqs, w.offsets, None)  # every request waiting at t=0: saturation throughput
+    ctx = pkg.Context(ix, max_queries=w.n, max_bases=int(w.total_bases) + 1024)
+    b = pkg.pack(w.seqs, w.offsets)
+    ctx.stage(b)
+    for _ in range(2):
+        ctx.run_staged()
+    ctx.last_timing()
+    ctx.run_staged()
+    ms = ctx.last_timing()[0]
+    batched = b.bases / (ms / 1e3) / 1e6
+    out = st.summary()
+    out.update({"rate_req_per_s": rate, "center_bp": len(w.center),
+                "saturation_mbp_per_s": round(sat.summary()["mbp_per_s"], 3),
+                "batched_mbp_per_s": round(batched, 3),
+                "saturation_frac_of_batched": round(sat.summary()["mbp_per_s"] / batched, 3),
+                "budget_bytes": 40 << 30})
+    return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in out.items()}
+
+
 def run_impl_reference(args, rank, world):
     """The reference's CPU path (the oracle restatement) on the host cores."""
     if rank != 0:
@@ -218,6 +263,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--sub-batch", type=int, default=25_000, help="queries per device sub-batch (sizes the arenas)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=4000)
+    ap.add_argument("--plain-queries", type=int, default=128)
     ap.add_argument("--stage-timing", action="store_true", help="per-stage event timing pass (extra run)")
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -312,6 +360,8 @@ def main():
                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1000 * e_wall, 3)}
     if n_cig_words is None:
         n_cig_words = 64 * b.n
+    plain = measure_plain(pkg, ctx, w, args.plain_queries) if args.plain_queries > 0 else None
+    serving = None if args.no_serve or rank != 0 else measure_serving(pkg, args.serve_requests, 2000.0)
     peak, peak_kind = load_peaks()
     # dominant stage
     top = max(stages, key=lambda k: stages[k])
@@ -350,6 +400,8 @@ def main():
         "cpu_baseline": cpu,
         "e2e": e2e,
         "parity_sample": parity,
+        "plain_form": plain,
+        "serve": serving,
         "clocks": clocks,
     }
     if rank == 0:

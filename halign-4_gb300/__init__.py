@@ -70,6 +70,9 @@ def lib() -> C.CDLL:
     L.hg_last_timing.argtypes = [vp, vp, vp, vp, vp]
     L.hg_set_timing.argtypes = [vp, i32]
     L.hg_staged_flags.argtypes = [vp, vp]
+    L.hg_submit.argtypes = [vp, vp, vp, vp, vp, vp, i64]
+    L.hg_poll.argtypes = [vp]
+    L.hg_collect.argtypes = [vp, vp, i64, vp, vp, vp]
     L.hg_counters.argtypes = [vp, vp, vp, i32]
     L.hg_extract_minimizer.argtypes = [C.c_char_p, i64, i32, i32, i32, vp, vp, i64, vp]
     L.hg_extract_minimizer.restype = i64
@@ -246,6 +249,25 @@ class Context:
         cig, off, has_ins, status, rbuf, stride = self._outputs(b.n, b.bases, rows, worst=True)
         _check(lib().hg_fetch_staged(self.h, _p(cig), len(cig), _p(off), _p(has_ins), _p(rbuf), stride, _p(status)))
         return self._result(cig, off, has_ins, status, rbuf, b.n)
+
+    # asynchronous form (continuous batching)
+    def submit(self, b: Packed):
+        _check(lib().hg_submit(self.h, _p(b.packed), _p(b.poff), _p(b.qlen), _p(b.exc), _p(b.exc_off), b.n))
+        self._sub = b
+
+    def poll(self) -> bool:
+        r = lib().hg_poll(self.h)
+        if r < 0:
+            _check(-r)
+        return r == 1
+
+    def collect(self, check: bool = True) -> AlignResult:
+        b = self._sub
+        cig, off, has_ins, status, _, _ = self._outputs(b.n, b.bases, False, worst=True)
+        code = lib().hg_collect(self.h, _p(cig), len(cig), _p(off), _p(has_ins), _p(status))
+        if check or code not in (HG_OK, HG_ERR_LENGTH_MISMATCH):
+            _check(code)
+        return self._result(cig, off, has_ins, status, None, b.n)
 
     def set_timing(self, on: bool):
         _check(lib().hg_set_timing(self.h, int(on)))

@@ -194,9 +194,15 @@ struct hg_ctx {
     DevBuf<uint32_t> s_status, s_cig;
     DevBuf<int64_t> s_cigoff_dev;
     int64_t s_cig_cap = 0;
-    // pinned staging for small per-query arrays
-    std::vector<int64_t> h_i64;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    // asynchronous form: pinned staging + completion event
+    uint8_t* h_packed = nullptr;
+    int64_t* h_i64 = nullptr;      // poff, exc_off, hoff, coff, cig_off (5 x (max_n + 1))
+    int32_t* h_i32 = nullptr;      // qlen, order, exc (2 x max_n + exc_cap x 3)
+    uint8_t* h_has_ins = nullptr;
+    uint32_t* h_status = nullptr;
+    cudaEvent_t done_ev = nullptr;
+    int64_t async_n = -1;
     bool timing = false;
     cudaEvent_t ev[10] = {};
     cudaEvent_t run_ev[2] = {};
@@ -237,11 +243,24 @@ extern "C" void hg_default_params(hg_params_t* p)
 
 // ------------------------------------------------------------------ packing
 
+namespace {
+struct PackLut {
+    uint8_t code[256];
+    PackLut()
+    {
+        for (int i = 0; i < 256; ++i) code[i] = 0xff;
+        code['A'] = 0, code['C'] = 1, code['G'] = 2, code['T'] = 3;
+    }
+};
+const PackLut kPackLut;
+}  // namespace
+
 extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint8_t* packed, int64_t packed_cap,
                        int64_t* poff, int32_t* exc, int64_t exc_cap, int64_t* exc_off, int64_t* packed_bytes,
                        int64_t* n_exc)
 {
     if (n < 0 || !offsets) return fail(HG_ERR_ARG, "hg_pack: bad arguments");
+    const uint8_t* lut = kPackLut.code;
     int64_t pb = 0, ne = 0;
     if (exc_off) exc_off[0] = 0;
     for (int64_t i = 0; i < n; ++i) {
@@ -249,53 +268,50 @@ extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint
         if (len < 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_pack: bad query length");
         const int64_t nbytes = ((len + 3) / 4 + 15) / 16 * 16;
         const unsigned char* s = reinterpret_cast<const unsigned char*>(seqs) + offsets[i];
+        if (packed && pb + nbytes > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
+        if (packed) poff[i] = pb;
+        bool any_exc = false;
+        // 4 bases per output byte; an exception byte packs as 0 and is listed below
+        int64_t j = 0;
+        for (; j + 4 <= len; j += 4) {
+            const uint32_t c0 = lut[s[j]], c1 = lut[s[j + 1]], c2 = lut[s[j + 2]], c3 = lut[s[j + 3]];
+            if ((c0 | c1 | c2 | c3) > 3) {  // some byte is not A/C/G/T
+                any_exc = true;
+                const uint32_t m0 = c0 < 4 ? c0 : 0, m1 = c1 < 4 ? c1 : 0, m2 = c2 < 4 ? c2 : 0, m3 = c3 < 4 ? c3 : 0;
+                if (packed) packed[pb + (j >> 2)] = (uint8_t)(m0 | m1 << 2 | m2 << 4 | m3 << 6);
+            } else if (packed) {
+                packed[pb + (j >> 2)] = (uint8_t)(c0 | c1 << 2 | c2 << 4 | c3 << 6);
+            }
+        }
+        if (j < len) {
+            uint32_t byte = 0;
+            for (int64_t t = j; t < len; ++t) {
+                const uint32_t c = lut[s[t]];
+                if (c > 3) any_exc = true;
+                else byte |= c << ((t - j) * 2);
+            }
+            if (packed) packed[pb + (j >> 2)] = (uint8_t)byte;
+        }
         if (packed) {
-            if (pb + nbytes > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
-            poff[i] = pb;
-            std::memset(packed + pb, 0, (size_t)nbytes);
+            const int64_t used = (len + 3) / 4;
+            std::memset(packed + pb + used, 0, (size_t)(nbytes - used));
         }
-        int64_t run_start = -1;
-        unsigned char run_byte = 0;
-        for (int64_t j = 0; j < len; ++j) {
-            const unsigned char c = s[j];
-            uint32_t code = 4;
-            switch (c) {
-            case 'A': code = 0; break;
-            case 'C': code = 1; break;
-            case 'G': code = 2; break;
-            case 'T': code = 3; break;
-            default: break;
-            }
-            if (code < 4) {
-                if (packed) packed[pb + (j >> 2)] |= (uint8_t)(code << ((j & 3) * 2));
-                if (run_start >= 0) {
+        if (any_exc) {
+            int64_t run_start = -1;
+            unsigned char run_byte = 0;
+            for (int64_t t = 0; t <= len; ++t) {
+                const bool isx = t < len && lut[s[t]] > 3;
+                if (run_start >= 0 && (!isx || s[t] != run_byte)) {
                     if (packed) {
                         if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
-                        exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(j - run_start),
+                        exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(t - run_start),
                                  exc[ne * 3 + 2] = run_byte;
                     }
                     ++ne;
                     run_start = -1;
                 }
-            } else {
-                if (run_start >= 0 && c != run_byte) {
-                    if (packed) {
-                        if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
-                        exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(j - run_start),
-                                 exc[ne * 3 + 2] = run_byte;
-                    }
-                    ++ne;
-                    run_start = -1;
-                }
-                if (run_start < 0) run_start = j, run_byte = c;
+                if (isx && run_start < 0) run_start = t, run_byte = s[t];
             }
-        }
-        if (run_start >= 0) {
-            if (packed) {
-                if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
-                exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(len - run_start), exc[ne * 3 + 2] = run_byte;
-            }
-            ++ne;
         }
         pb += nbytes;
         if (exc_off) exc_off[i + 1] = ne;
@@ -630,6 +646,12 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
     if (!c) return;
     if (c->st) cudaStreamSynchronize(c->st);
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    if (c->h_packed) cudaFreeHost(c->h_packed);
+    if (c->h_i64) cudaFreeHost(c->h_i64);
+    if (c->h_i32) cudaFreeHost(c->h_i32);
+    if (c->h_has_ins) cudaFreeHost(c->h_has_ins);
+    if (c->h_status) cudaFreeHost(c->h_status);
+    if (c->done_ev) cudaEventDestroy(c->done_ev);
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : c->run_ev)
@@ -1062,6 +1084,101 @@ extern "C" int hg_fetch_staged(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, 
     int64_t total = 0;
     return fetch_outputs(c, (int)sp.n, c->s_coff.p, cigar, cigar_cap, 0, cigar_off, has_ins, rows, row_stride,
                          status, &total);
+}
+
+// ------------------------------------------------------ asynchronous form
+
+extern "C" int hg_submit(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                         const int32_t* exc, const int64_t* exc_off, int64_t n)
+{
+    if (!c || n <= 0 || !packed || !poff || !qlen || !exc_off) return fail(HG_ERR_ARG, "hg_submit: bad arguments");
+    if (c->async_n >= 0) return fail(HG_ERR_ARG, "hg_submit: previous batch not collected");
+    cudaSetDevice(c->ix->device);
+    int64_t bases = 0, bytes = 0;
+    for (int64_t i = 0; i < n; ++i) bases += qlen[i], bytes += (int64_t)padded_bytes(qlen[i]);
+    const int64_t ne = exc_off[n] - exc_off[0];
+    if (n > c->max_n || bases > c->max_bases || bytes > (int64_t)c->packed.n || ne > c->exc_cap)
+        return fail(HG_ERR_CAPACITY, "hg_submit: batch exceeds the context capacity");
+    const int64_t M = c->max_n + 1;
+    if (!c->h_packed) {
+        if (cudaHostAlloc(&c->h_packed, c->packed.n, cudaHostAllocDefault) != cudaSuccess ||
+            cudaHostAlloc(&c->h_i64, sizeof(int64_t) * 5 * M, cudaHostAllocDefault) != cudaSuccess ||
+            cudaHostAlloc(&c->h_i32, sizeof(int32_t) * (2 * M + 3 * c->exc_cap), cudaHostAllocDefault) != cudaSuccess ||
+            cudaHostAlloc(&c->h_has_ins, (size_t)M, cudaHostAllocDefault) != cudaSuccess ||
+            cudaHostAlloc(&c->h_status, sizeof(uint32_t) * M, cudaHostAllocDefault) != cudaSuccess ||
+            cudaEventCreateWithFlags(&c->done_ev, cudaEventDisableTiming) != cudaSuccess)
+            return fail(HG_ERR_NOMEM, "hg_submit: pinned staging allocation");
+    }
+    int64_t *spoff = c->h_i64, *seoff = c->h_i64 + M, *shoff = c->h_i64 + 2 * M, *scoff = c->h_i64 + 3 * M;
+    int32_t *sqlen = c->h_i32, *sorder = c->h_i32 + M, *sexc = c->h_i32 + 2 * M;
+    std::vector<int32_t> order;
+    std::vector<int64_t> hoff, coff;
+    sub_arrays(c, qlen, n, order, hoff, coff);
+    int64_t pb = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const size_t nb = padded_bytes(qlen[i]);
+        std::memcpy(c->h_packed + pb, packed + poff[i], nb);
+        spoff[i] = pb, pb += (int64_t)nb;
+        sqlen[i] = qlen[i], sorder[i] = order[i], shoff[i] = hoff[i], scoff[i] = coff[i];
+    }
+    for (int64_t i = 0; i <= n; ++i) seoff[i] = exc_off[i] - exc_off[0];
+    if (ne) std::memcpy(sexc, exc + 3 * exc_off[0], 12 * (size_t)ne);
+    cudaStream_t st = c->st;
+    HG_CUDA(cudaMemcpyAsync(c->packed.p, c->h_packed, (size_t)pb, cudaMemcpyHostToDevice, st));
+    if (ne) HG_CUDA(cudaMemcpyAsync(c->exc.p, sexc, 12 * (size_t)ne, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->poff.p, spoff, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->qlen.p, sqlen, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->exc_off.p, seoff, 8 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->order.p, sorder, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->hoff.p, shoff, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->coff.p, scoff, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    const hg::BatchDev b = batch_view(c, (int)n, c->packed.p, c->poff.p, c->qlen.p, c->exc.p, c->exc_off.p,
+                                      c->order.p, c->hoff.p, c->coff.p);
+    int r = run_sub(c, b, false);
+    if (r) return r;
+    compact_offsets_kernel<<<1, 1024, 0, st>>>(c->n_cig.p, (int)n, c->cig_off.p);
+    HG_CUDA(cudaGetLastError());
+    HG_CUDA(cudaMemcpyAsync(c->h_i64 + 4 * M, c->cig_off.p, 8 * ((size_t)n + 1), cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaMemcpyAsync(c->h_has_ins, c->has_ins.p, (size_t)n, cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaMemcpyAsync(c->h_status, c->status.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaEventRecord(c->done_ev, st));
+    c->async_n = n;
+    return HG_OK;
+}
+
+extern "C" int hg_poll(hg_ctx_t* c)
+{
+    if (!c || c->async_n < 0) return -HG_ERR_ARG;
+    const cudaError_t e = cudaEventQuery(c->done_ev);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    cuda_fail(e, "hg_poll");
+    return -HG_ERR_CUDA;
+}
+
+extern "C" int hg_collect(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
+                          uint32_t* status)
+{
+    if (!c || c->async_n < 0) return fail(HG_ERR_ARG, "hg_collect: nothing submitted");
+    HG_CUDA(cudaEventSynchronize(c->done_ev));
+    const int64_t n = c->async_n, M = c->max_n + 1;
+    const int64_t* off = c->h_i64 + 4 * M;
+    const int64_t total = off[n];
+    if (total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_collect: cigar buffer too small");
+    const int64_t piece = (int64_t)c->cig_compact.n;
+    for (int64_t done = 0; done < total; done += piece) {
+        const int64_t m = std::min(piece, total - done);
+        compact_copy_kernel<<<c->sms, 256, 0, c->st>>>(c->cig.p, c->coff.p, c->n_cig.p, c->cig_off.p, (int)n,
+                                                       c->cig_compact.p, m, done);
+        HG_CUDA(cudaGetLastError());
+        HG_CUDA(cudaMemcpyAsync(cigar + done, c->cig_compact.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, c->st));
+    }
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    for (int64_t i = 0; i <= n; ++i) cigar_off[i] = off[i];
+    if (has_ins) std::memcpy(has_ins, c->h_has_ins, (size_t)n);
+    if (status) std::memcpy(status, c->h_status, 4 * (size_t)n);
+    c->async_n = -1;
+    return status_error(c->h_status, n);
 }
 
 // ---------------------------------------------------------- single calls

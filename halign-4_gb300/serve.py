@@ -1,0 +1,130 @@
+"""Continuous-batching serving loop for align-to-center requests.
+
+The center index and the per-column consensus counters stay resident on the
+GPU.  Requests (one query each) arrive over time; the loop keeps a FIFO of
+arrived requests and a pool of contexts, each with its own CUDA stream and
+arenas.  Whenever a context is free it admits the oldest waiting requests as
+one micro-batch - as many as fit its capacity and the device-memory budget
+of everything in flight - and enqueues it asynchronously (hg_submit); the
+loop polls the busy contexts and collects finished micro-batches.  Requests
+that arrive while others are on the GPU therefore join as soon as a slot and
+memory free up, and micro-batches of different contexts overlap on the
+device.  Each request's CIGAR is identical to aligning it alone: requests are
+independent and the batch kernels are order-insensitive per query.
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import Context, Index, pack
+
+# device bytes a request of L bases holds while in flight (arenas scale with
+# bases: hits, anchors, segments, CIGAR scratch, rows)
+BYTES_PER_BASE = 64
+
+
+@dataclass
+class ServeStats:
+    latencies_ms: np.ndarray
+    bases: int
+    wall_s: float
+    batches: int
+    max_inflight_bytes: int
+    results: dict = field(default_factory=dict)
+
+    def summary(self) -> dict:
+        lat = self.latencies_ms
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "requests": int(len(lat)),
+                "mbp_per_s": self.bases / self.wall_s / 1e6, "micro_batches": self.batches,
+                "max_inflight_bytes": self.max_inflight_bytes}
+
+
+class Server:
+    def __init__(self, index: Index, n_slots: int = 4, slot_queries: int = 512, slot_bases: int = 8_000_000,
+                 budget_bytes: int = 40 << 30):
+        self.index = index
+        self.budget = budget_bytes
+        self.slot_bases = slot_bases
+        self.slots = [Context(index, max_queries=slot_queries, max_bases=slot_bases) for _ in range(n_slots)]
+        self.slot_queries = slot_queries
+
+    def run(self, seqs: bytes, offsets: np.ndarray, arrivals: np.ndarray | None = None,
+            keep_results: bool = False) -> ServeStats:
+        """Serve requests i = 0..n-1 arriving at arrivals[i] seconds (None: all
+        at once).  Returns latency statistics (arrival to collected result)."""
+        n = len(offsets) - 1
+        if arrivals is None:
+            arrivals = np.zeros(n)
+        lens = np.diff(offsets).astype(np.int64)
+        pending: deque[int] = deque()
+        busy: dict[int, tuple[list[int], int]] = {}
+        free = list(range(len(self.slots)))
+        done_t = np.zeros(n)
+        results = {}
+        inflight = 0
+        max_inflight = 0
+        batches = 0
+        nxt = 0
+        finished = 0
+        t0 = time.perf_counter()
+        while finished < n:
+            now = time.perf_counter() - t0
+            while nxt < n and arrivals[nxt] <= now:
+                pending.append(nxt)
+                nxt += 1
+            # admit: fill free contexts with the oldest waiting requests
+            while free and pending:
+                take, tb = [], 0
+                while pending and len(take) < self.slot_queries:
+                    i = pending[0]
+                    need = int(lens[i]) * BYTES_PER_BASE
+                    if tb + lens[i] > self.slot_bases or inflight + need > self.budget:
+                        break
+                    take.append(pending.popleft())
+                    tb += int(lens[i])
+                    inflight += need
+                if not take:
+                    break
+                s = free.pop()
+                blob = b"".join(seqs[offsets[i]:offsets[i + 1]] for i in take)
+                offs = np.concatenate([[0], np.cumsum(lens[take])]).astype(np.int64)
+                self.slots[s].submit(pack(blob, offs))
+                busy[s] = (take, tb)
+                batches += 1
+                max_inflight = max(max_inflight, inflight)
+            # collect finished micro-batches
+            progressed = False
+            for s in list(busy):
+                if self.slots[s].poll():
+                    take, tb = busy.pop(s)
+                    res = self.slots[s].collect(check=False)
+                    t = time.perf_counter() - t0
+                    for j, i in enumerate(take):
+                        done_t[i] = t
+                        if keep_results:
+                            results[i] = res.cigar_of(j).copy()
+                    inflight -= tb * BYTES_PER_BASE
+                    finished += len(take)
+                    free.append(s)
+                    progressed = True
+            if not progressed and not (free and pending):
+                if nxt < n and not busy and not pending:
+                    time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+                else:
+                    time.sleep(20e-6)
+        wall = time.perf_counter() - t0
+        lat = (done_t - arrivals) * 1e3
+        return ServeStats(lat, int(lens.sum()), wall, batches, max_inflight, results)
+
+    def counters(self, reset: bool = False):
+        tot_c = tot_i = None
+        for c in self.slots:
+            cnt, ins = c.counters(reset)
+            tot_c = cnt if tot_c is None else tot_c + cnt
+            tot_i = ins if tot_i is None else tot_i + ins
+        return tot_c, tot_i

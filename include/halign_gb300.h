@@ -129,6 +129,18 @@ int hg_staged_flags(hg_ctx_t* ctx, uint32_t* flags);
 /* Enable per-stage event timing for staged runs (off by default). */
 int hg_set_timing(hg_ctx_t* ctx, int on);
 
+/* Asynchronous form (continuous batching): hg_submit enqueues one packed
+ * batch (within the context's capacity) on the context's stream and returns;
+ * hg_poll returns 1 once its results are ready (0 while running, < 0 on
+ * error); hg_collect copies them out in hg_align_batch's layout and frees the
+ * context for the next hg_submit.  Several contexts of one index overlap on
+ * the GPU; each keeps its own stream and arenas. */
+int hg_submit(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
+              const int64_t* exc_off, int64_t n);
+int hg_poll(hg_ctx_t* ctx);
+int hg_collect(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
+               uint32_t* status);
+
 /* Consensus counters: counts7 = L x {A,C,G,T,U,N,-} (consensus::SiteCount,
  * include/consensus.h:78-99), ins = L+1 insertion events (slot c: I before
  * center column c).  reset != 0 clears them after reading. */
