@@ -69,6 +69,50 @@ __device__ __forceinline__ uint32_t shape_key(const Seg& g)
     return (outer - 1) | (inner - 1) << 7 | tinner << 11 | left << 12;
 }
 
+// Wavefront tiers: segments the band never binds (auto_band < 0 or >= both
+// lengths) whose shorter side is at most kWaveWarpMaxInner run one warp per
+// segment; wider ones up to kWaveMaxInner run one 16-warp CTA per segment.
+constexpr int kWaveWarpMaxInner = 256;   // 32 lanes x 8 columns
+constexpr int kWaveMaxInner = 4096;      // 16 warps x 32 lanes x 8 columns
+constexpr int kWaveBins = 32;            // sort bins of the one-warp list
+constexpr int kWaveLongSteps = 2048;     // segments this long sort first
+
+__host__ __device__ __forceinline__ bool wave_eligible(uint32_t rl, uint32_t ql)
+{
+    const uint32_t inner = rl < ql ? rl : ql, outer = rl < ql ? ql : rl;
+    if (inner == 0 || inner > (uint32_t)kWaveMaxInner) return false;
+    // auto_band: -1 when (outer - inner) / outer > 0.5, which for lengths
+    // below 2^31 is exactly 2 (outer - inner) > outer; otherwise w >= 200
+    if (2 * (outer - inner) > outer || outer <= 200) return true;
+    const int w = auto_band((int)rl, (int)ql);
+    return w >= (int)outer;
+}
+
+// Columns per lane of the one-warp wavefront: the smallest power of two with
+// 32 x P >= inner.
+__host__ __device__ __forceinline__ int wave_warp_cols(int inner)
+{
+    return inner <= 32 ? 1 : inner <= 64 ? 2 : inner <= 128 ? 4 : 8;
+}
+
+// Columns per lane of the CTA wavefront: 16 warps x 32 lanes x P >= inner.
+__host__ __device__ __forceinline__ int wave_cta_cols(int inner)
+{
+    return inner <= 512 ? 1 : inner <= 1024 ? 2 : inner <= 2048 ? 4 : 8;
+}
+
+// Sort key of a one-warp wavefront segment: long ones (more than
+// kWaveLongSteps rows) first, so they do not start last; then widest first,
+// orientation and gap mode, so the warps of an SM run the same code together.
+__host__ __device__ __forceinline__ uint32_t wave_key(uint32_t rl, uint32_t ql, bool left)
+{
+    const int inner = (int)(rl < ql ? rl : ql), outer = (int)(rl < ql ? ql : rl);
+    const int P = wave_warp_cols(inner);
+    const uint32_t pidx = P == 1 ? 0u : P == 2 ? 1u : P == 4 ? 2u : 3u;
+    const uint32_t shortb = outer > kWaveLongSteps ? 0u : 1u;
+    return shortb << 4 | (3u - pidx) << 2 | (rl <= ql ? 1u : 0u) << 1 | (left ? 0u : 1u);
+}
+
 struct BatchDev {
     int n;                       // queries in the batch
     const uint8_t* packed;       // 2-bit packed bases
@@ -114,6 +158,13 @@ struct BatchDev {
     uint32_t* shape_hist;        // kShapeBins counters, then kShapeBins cursors
     unsigned int* n_small;
     unsigned int* n_large;
+    uint32_t* work_wave;         // one-warp wavefront tier, in chain order
+    uint32_t* work_wave_key;     // its wave_key per entry
+    uint32_t* work_wave_sorted;  // sorted by wave_key
+    uint32_t* wave_hist;         // kWaveBins counters, then kWaveBins cursors
+    uint32_t* work_wide;         // CTA wavefront tier
+    unsigned int* n_wave;
+    unsigned int* n_wide;
     int64_t wcap;
     // K6 DP scratch: one reusable slot per large-tier warp, plus a bump arena
     // for segments whose scratch exceeds a slot

@@ -204,16 +204,26 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 g.kind = kind | flags;
                 b.seg[sb + s] = g;
             }
-            // tier work lists (warp-aggregated appends)
+            // tier work lists (warp-aggregated appends): small, one-warp
+            // wavefront, CTA wavefront, exact
+            const bool dp_big = act && (kind == kSegDpLarge || kind == kSegGlobal);
+            const bool wv = dp_big && wave_eligible(rl, ql);
+            const bool wv_warp = wv && min(rl, ql) <= (uint32_t)kWaveWarpMaxInner;
             const unsigned ms = __ballot_sync(FULL, act && kind == kSegDpSmall);
-            const unsigned ml = __ballot_sync(FULL, act && (kind == kSegDpLarge || kind == kSegGlobal));
-            unsigned bs = 0, bl = 0;
+            const unsigned ml = __ballot_sync(FULL, dp_big && !wv);
+            const unsigned mw = __ballot_sync(FULL, wv_warp);
+            const unsigned mx = __ballot_sync(FULL, wv && !wv_warp);
+            unsigned bs = 0, bl = 0, bw = 0, bx = 0;
             if (lane == 0) {
                 if (ms) bs = atomicAdd(b.n_small, (unsigned)__popc(ms));
                 if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
+                if (mw) bw = atomicAdd(b.n_wave, (unsigned)__popc(mw));
+                if (mx) bx = atomicAdd(b.n_wide, (unsigned)__popc(mx));
             }
             bs = __shfl_sync(FULL, bs, 0);
             bl = __shfl_sync(FULL, bl, 0);
+            bw = __shfl_sync(FULL, bw, 0);
+            bx = __shfl_sync(FULL, bx, 0);
             const unsigned below = (1u << lane) - 1u;
             if (ms >> lane & 1u) {
                 const unsigned w = bs + __popc(ms & below);
@@ -242,6 +252,26 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             if (ml >> lane & 1u) {
                 const unsigned w = bl + __popc(ml & below);
                 if ((int64_t)w < b.wcap) b.work_large[w] = (uint32_t)(sb + s);
+                else atomicOr(&b.status[q], kStArenaOverflow);
+            }
+            uint32_t wkey = 0xffffffffu;
+            if (mw >> lane & 1u) {
+                const unsigned w = bw + __popc(mw & below);
+                wkey = wave_key(rl, ql, (flags & kSegLeft) != 0);
+                if ((int64_t)w < b.wcap) {
+                    b.work_wave[w] = (uint32_t)(sb + s);
+                    b.work_wave_key[w] = wkey;
+                } else {
+                    atomicOr(&b.status[q], kStArenaOverflow);
+                }
+            }
+            {
+                const unsigned peers = __match_any_sync(FULL, wkey);
+                if ((mw >> lane & 1u) && lane == __ffs(peers) - 1) atomicAdd(&b.wave_hist[wkey], __popc(peers));
+            }
+            if (mx >> lane & 1u) {
+                const unsigned w = bx + __popc(mx & below);
+                if ((int64_t)w < b.wcap) b.work_wide[w] = (uint32_t)(sb + s);
                 else atomicOr(&b.status[q], kStArenaOverflow);
             }
             rpos = (uint32_t)__shfl_sync(FULL, ir, 31);

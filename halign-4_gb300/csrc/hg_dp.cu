@@ -1,7 +1,7 @@
 // hg_dp.cu - K5/K6: KSW2 extz2 gap-fill (src/align/ksw2_extz2_sse.c:23-304)
 // and its traceback (ksw_backtrack, include/ksw2.h:129-161).
 //
-// Two tiers, both bit-exact with the SSE2 build of the reference:
+// Three tiers, all bit-exact with the SSE2 build of the reference:
 //
 // * Small tier (one thread per segment).  When the band w is at least
 //   max(qlen, tlen) it never binds (globalAlignKSW2 sets w = 200 + ... for
@@ -15,6 +15,10 @@
 //   shared memory, applies ksw_lane (the SSE2 instruction sequence) per cell
 //   and stores a 4-bit direction code per cell, word-interleaved across the
 //   CTA so every shared-memory access is bank-conflict free.
+//
+// * Wavefront tier (one warp per segment): every other segment whose band
+//   never binds and whose shorter side is at most 256; the small tier's
+//   recurrence as a register wavefront across the lanes (see wave_segment).
 //
 // * Large tier (one warp per segment; also every single-call ksw_extz2).  An
 //   exact emulation of the SIMD code: the anti-diagonal band rounded to whole
@@ -514,6 +518,444 @@ __device__ KswResult ksw_extz2_warp(const KswArgs& a, uint8_t* scratch, uint32_t
     return R;
 }
 
+// ------------------------------------------------------------------------
+// Wavefront tiers.  For every segment whose band never binds (auto_band < 0
+// or >= both lengths) the DP is the small tier's per-cell int32 recurrence
+// (lane_int), so it needs neither the anti-diagonal byte arrays nor the H row
+// of the exact emulation.  A group of GW warps (1, or a 16-warp CTA for wide
+// segments) runs it as a register wavefront: virtual lane v = 32 x warp +
+// lane owns P consecutive columns of the shorter side and at step s computes
+// row s - v of them.  The pair carried along a row and the row's outer base
+// move one lane up per step through a shuffle; across a warp boundary they
+// go through a shared-memory ring, the warps running 32-step windows with a
+// barrier between windows and warp k one window behind warp k-1.  Virtual
+// lane 0 takes the boundary column and a fresh outer base.
+//
+// Direction nibbles: one word holds 8/P steps x P columns of one virtual
+// lane; step group t of lane v is word t x LDW + v (LDW = lanes that hold
+// columns).  The traceback walks K-step blocks held in shared memory, from
+// the last block to the first (the step index o + c/P never increases along
+// the path).  A segment of one block computes straight into shared memory.
+// A longer one either writes every word to global scratch during the single
+// forward pass and copies each block back for the walk, or - when no scratch
+// of that size is left - saves each warp's state at every block start
+// (per lane: the column bytes and the outgoing carried word) and recomputes
+// each block from its saved state for the walk.
+constexpr int kWaveWarpDirWords = 2048;   // one-warp groups: 8 KB per warp
+constexpr int kWaveCtaWarps = 16;
+constexpr int kWaveCtaDirWords = 32768;   // CTA group: 128 KB
+constexpr int kWaveRing = 128;            // ring entries per warp boundary (4 windows)
+
+struct WaveGeom {
+    int P, lanes, nw, K, S, nblk, ckw;  // cols/lane, column lanes, active warps, steps/block, steps, blocks, ckpt words
+};
+
+__host__ __device__ __forceinline__ WaveGeom wave_geom(int inner, int outer, int P, int dir_words)
+{
+    WaveGeom G;
+    G.P = P;
+    G.lanes = (inner + P - 1) / P;
+    G.nw = (G.lanes + 31) / 32;
+    G.K = ((dir_words / G.lanes) * (8 / P)) & ~31;   // steps per block, a multiple of 32
+    G.S = outer + (inner - 1) / P;
+    G.nblk = (G.S + G.K - 1) / G.K;
+    G.ckw = (2 * P + 3) / 4 + 1;
+    return G;
+}
+
+// Global direction words of a segment (every step group x column lanes).
+__host__ __device__ __forceinline__ size_t wave_gdir_bytes(const WaveGeom& G)
+{
+    const int spw = 8 / G.P;
+    return G.nblk > 1 ? (size_t)((G.S + spw - 1) / spw) * G.lanes * sizeof(uint32_t) : 0;
+}
+
+// Checkpoint bytes: one record (ckw words x 32 lanes per active warp) per
+// block; blocks 0 and nblk-1 need none but keep their slots for indexing.
+__host__ __device__ __forceinline__ size_t wave_ckpt_bytes(const WaveGeom& G)
+{
+    return G.nblk > 2 ? (size_t)G.nblk * G.nw * G.ckw * 32 * sizeof(uint32_t) : 0;
+}
+
+template <int GW>
+__device__ __forceinline__ void wave_sync()
+{
+    if (GW == 1) __syncwarp();
+    else __syncthreads();
+}
+
+template <int GW, int P, bool TINNER, int MODE>
+__device__ __forceinline__ void wave_segment(const IndexDev& ix, const BatchDev& b, uint32_t sid, const Seg& g,
+                                             uint32_t* dirs, int dir_words, uint32_t* ring, uint32_t* scratch,
+                                             bool gmode, int* flag)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int wk = GW == 1 ? 0 : (int)(threadIdx.x >> 5);
+    constexpr int SPW = 8 / P;                       // steps per direction word
+    constexpr int CKW = (2 * P + 3) / 4 + 1;         // checkpoint words per lane
+    const int qn = (int)g.ql, tn = (int)g.rl;
+    const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
+    const WaveGeom G = wave_geom(inner, outer, P, dir_words);
+    const int NW = G.nw, K = G.K, S = G.S, nblk = G.nblk, LDW = G.lanes;
+    const bool active = wk < NW;
+    const int v = wk * 32 + lane;                    // virtual lane
+    const bool holds = v < LDW;                      // this lane owns columns
+    const uint8_t* pk = b.packed + b.poff[g.q];
+    const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
+    const bool plain_q = e0 == e1;
+    const uint8_t* tc = ix.center + g.rs;
+    int ic[P], s1[P], s2[P];
+#pragma unroll
+    for (int p = 0; p < P; ++p) {
+        const int c = v * P + p;
+        ic[p] = 0;
+        if (active && c < inner) {
+            if (TINNER) ic[p] = tc[c];
+            else ic[p] = plain_q ? (int)packed_code(pk, g.qs + c) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + c);
+        }
+    }
+    uint32_t cout = 0, chunk = 0;
+    auto init_state = [&]() {
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+            const int c = v * P + p;
+            if (TINNER) s1[p] = c ? 6 : 0, s2[p] = 0;   // u, y above row 0
+            else s1[p] = 0, s2[p] = c ? 6 : 0;          // x, v left of column 0
+        }
+        cout = 0;
+    };
+    auto ck = [&](int bk, int w) -> uint32_t& { return scratch[((bk * NW + wk) * CKW + w) * 32 + lane]; };
+    auto save = [&](int bk) {
+#pragma unroll
+        for (int w = 0; w < CKW - 1; ++w) {
+            uint32_t wd = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = 4 * w + j;
+                if (k < P) wd |= (uint32_t)s1[k] << (8 * j);
+                else if (k < 2 * P) wd |= (uint32_t)s2[k - P] << (8 * j);
+            }
+            ck(bk, w) = wd;
+        }
+        ck(bk, CKW - 1) = cout;
+    };
+    auto restore = [&](int bk) {
+#pragma unroll
+        for (int w = 0; w < CKW - 1; ++w) {
+            const uint32_t wd = ck(bk, w);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int k = 4 * w + j;
+                if (k < P) s1[k] = (int)((wd >> (8 * j)) & 0xffu);
+                else if (k < 2 * P) s2[k - P] = (int)((wd >> (8 * j)) & 0xffu);
+            }
+        }
+        cout = ck(bk, CKW - 1);
+    };
+    // Steps [sb, se) of every active warp, sb a multiple of 32.  Words of
+    // steps >= dbase go to shared memory (the block it holds starts at
+    // dbase); with to_global every word goes to global scratch instead; with
+    // save_ck each warp saves its state at the block starts below the last.
+    auto run = [&](int sb, int se, int dbase, bool to_global, bool save_ck) {
+        const int nwin = (se - sb + 31) / 32 + (GW > 1 ? NW - 1 : 0);
+        uint32_t acc = 0;
+        for (int j = 0; j < nwin; ++j) {
+            const int s0 = sb + (j - wk) * 32;
+            if (active && s0 >= sb && s0 < se) {
+                if (save_ck && s0 > 0 && s0 % K == 0 && s0 / K <= nblk - 2) save(s0 / K);
+                const int s1e = min(s0 + 32, se);
+                if (wk == 0) {
+                    const int o = s0 + lane;
+                    chunk = 0;
+                    if (o < outer) {
+                        if (TINNER) chunk = plain_q ? packed_code(pk, g.qs + o) : query_dna5(pk, b.exc, e0, e1, g.qs + o);
+                        else chunk = tc[o];
+                    }
+                }
+                for (int s = s0; s < s1e; ++s) {
+                    const uint32_t fresh = __shfl_sync(FULL, chunk, s & 31);
+                    uint32_t cin = __shfl_up_sync(FULL, cout, 1);
+                    if (GW > 1 && lane == 0 && wk > 0) cin = ring[(wk - 1) * kWaveRing + ((s - 1) & (kWaveRing - 1))];
+                    const int o = s - v;
+                    // virtual lane 0: left boundary column and a fresh outer base
+                    const bool first = v == 0;
+                    const int ob = o ? 6 : 0;
+                    int c1 = first ? (TINNER ? 0 : ob) : (int)(cin & 0xffu);
+                    int c2 = first ? (TINNER ? ob : 0) : (int)((cin >> 8) & 0xffu);
+                    const int oc = first ? (int)fresh : (int)(cin >> 16);
+                    uint32_t dn = 0;
+                    if (o >= 0 && o < outer) {
+#pragma unroll
+                        for (int p = 0; p < P; ++p) {
+                            if (v * P + p < inner) {
+                                const int sc = (ic[p] == 4 || oc == 4) ? 0 : (ic[p] == oc ? 5 : -4);
+                                int u, vv, x, y;
+                                uint32_t d;
+                                if (TINNER) {
+                                    d = lane_int<MODE>(sc, c1, c2, s1[p], s2[p], u, vv, x, y);
+                                    c1 = x, c2 = vv, s1[p] = u, s2[p] = y;
+                                } else {
+                                    d = lane_int<MODE>(sc, s1[p], s2[p], c1, c2, u, vv, x, y);
+                                    c1 = u, c2 = y, s1[p] = x, s2[p] = vv;
+                                }
+                                dn |= d << (4 * p);
+                            }
+                        }
+                        cout = (uint32_t)c1 | (uint32_t)c2 << 8 | (uint32_t)oc << 16;
+                    }
+                    if (GW > 1 && lane == 31) ring[wk * kWaveRing + (s & (kWaveRing - 1))] = cout;
+                    if (SPW == 1) acc = dn;
+                    else acc |= dn << (4 * P * (s % SPW));
+                    if (s % SPW == SPW - 1 || s == se - 1) {
+                        if (holds) {
+                            if (to_global) scratch[(size_t)(s / SPW) * LDW + v] = acc;
+                            else if (s >= dbase) dirs[((s - dbase) / SPW) * LDW + v] = acc;
+                        }
+                        acc = 0;
+                    }
+                }
+            }
+            if (GW > 1) __syncthreads();
+        }
+    };
+    init_state();
+    const bool ckmode = nblk > 1 && !gmode;
+    run(0, S, (nblk - 1) * K, gmode && nblk > 1, ckmode && nblk > 2);
+    wave_sync<GW>();
+    // traceback from (tlen-1, qlen-1) by the group's first thread
+    const bool lead = wk == 0 && lane == 0;
+    CigarPush cp{b.cig_seg + b.coff[g.q] + g.slot, 0, tn + qn, 0};
+    int ti = tn - 1, qj = qn - 1, state = 0;
+    for (int bk = nblk - 1;;) {
+        if (gmode && nblk > 1) {  // bring block bk's words back from global scratch
+            const int w0 = (bk * K / SPW) * LDW;
+            const int w1 = ((min((bk + 1) * K, S) + SPW - 1) / SPW) * LDW;
+            for (int i = wk * 32 + lane; i < w1 - w0; i += GW * 32) dirs[i] = scratch[(size_t)w0 + i];
+            wave_sync<GW>();
+        }
+        int done = 0;
+        if (lead) {
+            const int base = bk * K;
+            while (ti >= 0 && qj >= 0) {
+                const int o = TINNER ? qj : ti, c = TINNER ? ti : qj;
+                const int vl = c / P;
+                const int s = o + vl;
+                if (s < base) break;
+                const uint32_t word = dirs[((s - base) / SPW) * LDW + vl];
+                const uint32_t nib = (word >> (4 * (P * (s % SPW) + c % P))) & 0xfu;
+                if (state == 0) state = nib & 3u;
+                else if (!((nib >> (state + 1)) & 1u)) state = 0;
+                if (state == 0) state = nib & 3u;
+                if (state == 0) cp.push(0, 1), --ti, --qj;
+                else if (state == 1) cp.push(2, 1), --ti;
+                else cp.push(1, 1), --qj;
+            }
+            done = !(ti >= 0 && qj >= 0);
+            if (GW > 1) *flag = done;
+        }
+        if (GW == 1) {
+            done = __shfl_sync(FULL, done, 0);
+        } else {
+            __syncthreads();
+            done = *flag;
+        }
+        if (done || bk == 0) break;
+        --bk;
+        wave_sync<GW>();
+        if (!gmode) {  // recompute block bk from its saved state
+            if (active) {
+                if (bk == 0) init_state();
+                else restore(bk);
+                if (GW > 1 && lane == 31 && bk > 0) ring[wk * kWaveRing + ((bk * K - 1) & (kWaveRing - 1))] = cout;
+            }
+            wave_sync<GW>();
+            run(bk * K, (bk + 1) * K, bk * K, false, false);
+            wave_sync<GW>();
+        }
+    }
+    if (lead) {
+        if (ti >= 0) cp.push(2, (uint32_t)(ti + 1));
+        if (qj >= 0) cp.push(1, (uint32_t)(qj + 1));
+        for (int i = 0; i < cp.n / 2; ++i) {
+            const uint32_t a = cp.out[i];
+            cp.out[i] = cp.out[cp.n - 1 - i];
+            cp.out[cp.n - 1 - i] = a;
+        }
+        b.seg[sid].nops = cp.n;
+        if (b.cells) atomicAdd(b.cells, (unsigned long long)g.rl * g.ql);
+    }
+    wave_sync<GW>();
+}
+
+template <int GW, bool TINNER, int MODE>
+__device__ __forceinline__ void wave_dispatch_p(const IndexDev& ix, const BatchDev& b, uint32_t sid, const Seg& g,
+                                                int P, uint32_t* dirs, int dir_words, uint32_t* ring,
+                                                uint32_t* scratch, bool gmode, int* flag)
+{
+    if (P == 1) wave_segment<GW, 1, TINNER, MODE>(ix, b, sid, g, dirs, dir_words, ring, scratch, gmode, flag);
+    else if (P == 2) wave_segment<GW, 2, TINNER, MODE>(ix, b, sid, g, dirs, dir_words, ring, scratch, gmode, flag);
+    else if (P == 4) wave_segment<GW, 4, TINNER, MODE>(ix, b, sid, g, dirs, dir_words, ring, scratch, gmode, flag);
+    else wave_segment<GW, 8, TINNER, MODE>(ix, b, sid, g, dirs, dir_words, ring, scratch, gmode, flag);
+}
+
+template <int GW>
+__device__ __forceinline__ void wave_dispatch(const IndexDev& ix, const BatchDev& b, uint32_t sid, const Seg& g,
+                                              int P, uint32_t* dirs, int dir_words, uint32_t* ring,
+                                              uint32_t* scratch, bool gmode, int* flag)
+{
+    const bool tinner = g.rl <= g.ql;
+    const bool left = (g.kind & kSegLeft) != 0;
+    if (tinner) {
+        if (left) wave_dispatch_p<GW, true, 1>(ix, b, sid, g, P, dirs, dir_words, ring, scratch, gmode, flag);
+        else wave_dispatch_p<GW, true, 2>(ix, b, sid, g, P, dirs, dir_words, ring, scratch, gmode, flag);
+    } else {
+        if (left) wave_dispatch_p<GW, false, 1>(ix, b, sid, g, P, dirs, dir_words, ring, scratch, gmode, flag);
+        else wave_dispatch_p<GW, false, 2>(ix, b, sid, g, P, dirs, dir_words, ring, scratch, gmode, flag);
+    }
+}
+
+// Scratch of a wavefront segment, decided by the group's leader: direction
+// words in the group's reusable slot or in the bump arena when they fit
+// (gmode), else checkpoints in the slot or the arena, else the status gets
+// kStArenaOverflow.  code: 0 none needed, 1 slot, 2 arena (offset in *off),
+// 3 overflow; bit 2 set = gmode.
+__device__ __forceinline__ uint32_t wave_scratch_plan(const BatchDev& b, const WaveGeom& G, int slot,
+                                                      unsigned long long* off)
+{
+    if (G.nblk <= 1) return 0;
+    const bool slot_ok = slot < b.dp_nslots;
+    const size_t gbytes = wave_gdir_bytes(G), cbytes = wave_ckpt_bytes(G);
+    if (slot_ok && (int64_t)gbytes <= b.dp_slot_bytes) return 1 | 4;
+    const unsigned long long ga = (gbytes + 255) & ~(size_t)255;
+    if (*(volatile unsigned long long*)b.dp_cursor + ga <= (unsigned long long)b.dp_cap) {  // likely room: claim it
+        const unsigned long long o = atomicAdd(b.dp_cursor, ga);
+        if (o + gbytes <= (unsigned long long)b.dp_cap) {
+            *off = o;
+            return 2 | 4;
+        }
+    }
+    if (!cbytes) return 0;
+    if (slot_ok && (int64_t)cbytes <= b.dp_slot_bytes) return 1;
+    const unsigned long long o = atomicAdd(b.dp_cursor, (unsigned long long)((cbytes + 255) & ~(size_t)255));
+    if (o + cbytes <= (unsigned long long)b.dp_cap) {
+        *off = o;
+        return 2;
+    }
+    return 3;
+}
+
+__device__ __forceinline__ uint32_t* wave_scratch_ptr(const BatchDev& b, uint32_t code, int slot,
+                                                      unsigned long long off)
+{
+    if ((code & 3u) == 1u) return reinterpret_cast<uint32_t*>(b.dp_slots + (size_t)slot * b.dp_slot_bytes);
+    if ((code & 3u) == 2u) return reinterpret_cast<uint32_t*>(b.dp_arena + off);
+    return nullptr;
+}
+
+// Counting sort of the one-warp wavefront list by wave_key.
+__global__ void wave_scatter_kernel(BatchDev b)
+{
+    __shared__ uint32_t start[kWaveBins];
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (int k = 0; k < kWaveBins; ++k) start[k] = run, run += b.wave_hist[k];
+    }
+    __syncthreads();
+    const unsigned total = *b.n_wave;
+    const unsigned span = (total + 31u) & ~31u;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < span; w += gridDim.x * blockDim.x) {
+        const bool act = w < total && (int64_t)w < b.wcap;
+        const uint32_t key = act ? b.work_wave_key[w] : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (act && (int)(threadIdx.x & 31) == leader) base = atomicAdd(&b.wave_hist[kWaveBins + key], __popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (act) b.work_wave_sorted[start[key] + base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = b.work_wave[w];
+    }
+}
+
+// One-warp wavefront tier: 4 independent warps per CTA.
+__global__ void __launch_bounds__(128, 4) dp_wave_kernel(IndexDev ix, BatchDev b)
+{
+    __shared__ uint32_t dirs[4][kWaveWarpDirWords];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int gw = blockIdx.x * 4 + wl;
+    const unsigned total = min(*b.n_wave, (unsigned)b.wcap);
+    for (;;) {
+        unsigned wi = 0;
+        if (lane == 0) wi = atomicAdd(&b.queues[6], 1u);
+        wi = __shfl_sync(FULL, wi, 0);
+        if (wi >= total) break;
+        const uint32_t sid = b.work_wave_sorted[wi];
+        const Seg g = b.seg[sid];
+        const int inner = (int)min(g.rl, g.ql), outer = (int)max(g.rl, g.ql);
+        const int P = wave_warp_cols(inner);
+        const WaveGeom G = wave_geom(inner, outer, P, kWaveWarpDirWords);
+        unsigned long long off = 0;
+        uint32_t code = 0;
+        if (lane == 0) code = wave_scratch_plan(b, G, gw, &off);
+        code = __shfl_sync(FULL, code, 0);
+        off = __shfl_sync(FULL, off, 0);
+        if (code == 3u) {
+            if (lane == 0) {
+                atomicOr(&b.status[g.q], kStArenaOverflow);
+                b.seg[sid].nops = 0;
+            }
+            continue;
+        }
+        wave_dispatch<1>(ix, b, sid, g, P, dirs[wl], kWaveWarpDirWords, nullptr, wave_scratch_ptr(b, code, gw, off),
+                         (code & 4u) != 0, nullptr);
+    }
+}
+
+// CTA wavefront tier: one 16-warp CTA per segment (shorter side 257..4096);
+// CTA i uses checkpoint slot dp_nslots - gridDim.x + i.
+__global__ void __launch_bounds__(kWaveCtaWarps * 32, 1) dp_wave_cta_kernel(IndexDev ix, BatchDev b)
+{
+    extern __shared__ uint32_t wsm[];
+    uint32_t* dirs = wsm;
+    uint32_t* ring = wsm + kWaveCtaDirWords;
+    __shared__ unsigned s_item;
+    __shared__ int s_flag;
+    __shared__ uint32_t s_code;
+    __shared__ unsigned long long s_off;
+    const unsigned total = min(*b.n_wide, (unsigned)b.wcap);
+    const int slot = b.dp_nslots - (int)gridDim.x + (int)blockIdx.x;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&b.queues[7], 1u);
+        __syncthreads();
+        const unsigned wi = s_item;
+        __syncthreads();
+        if (wi >= total) break;
+        const uint32_t sid = b.work_wide[wi];
+        const Seg g = b.seg[sid];
+        const int inner = (int)min(g.rl, g.ql), outer = (int)max(g.rl, g.ql);
+        const int P = wave_cta_cols(inner);
+        const WaveGeom G = wave_geom(inner, outer, P, kWaveCtaDirWords);
+        if (threadIdx.x == 0) {
+            unsigned long long off = 0;
+            s_code = wave_scratch_plan(b, G, slot, &off);
+            s_off = off;
+            if (s_code == 3u) {
+                atomicOr(&b.status[g.q], kStArenaOverflow);
+                b.seg[sid].nops = 0;
+            }
+        }
+        __syncthreads();
+        const uint32_t code = s_code;
+        const unsigned long long off = s_off;
+        __syncthreads();
+        if (code == 3u) continue;
+        wave_dispatch<kWaveCtaWarps>(ix, b, sid, g, P, dirs, kWaveCtaDirWords, ring,
+                                     wave_scratch_ptr(b, code, slot, off), (code & 4u) != 0, &s_flag);
+    }
+}
+
+constexpr size_t kWaveCtaSmemBytes = sizeof(uint32_t) * ((size_t)kWaveCtaDirWords + (size_t)kWaveCtaWarps * kWaveRing);
+
 __device__ const int8_t c_dna5_mat[25] = {5, -4, -4, -4, 0, -4, 5, -4, -4, 0, -4, -4, 5, -4, 0,
                                           -4, -4, -4, 5, 0, 0, 0, 0, 0, 0};
 
@@ -606,6 +1048,30 @@ extern "C" cudaError_t hg_launch_dp_large(const hg::IndexDev* ix, const hg::Batc
 {
     hg::dp_large_kernel<<<grid, 128, 0, st>>>(*ix, *b);
     return cudaGetLastError();
+}
+
+// One-warp wavefront tier: sort its list, then run it (grid CTAs of 4
+// warps; warp i uses checkpoint slot i).
+extern "C" cudaError_t hg_launch_dp_wave(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+{
+    hg::wave_scatter_kernel<<<grid, 256, 0, st>>>(*b);
+    hg::dp_wave_kernel<<<grid, 128, 0, st>>>(*ix, *b);
+    return cudaGetLastError();
+}
+
+// CTA wavefront tier: grid CTAs (at most one per SM); CTA i uses checkpoint
+// slot dp_nslots - grid + i, above every slot the warp tiers use, so it may
+// run concurrently with them.
+extern "C" cudaError_t hg_launch_dp_wide(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+{
+    hg::dp_wave_cta_kernel<<<grid, hg::kWaveCtaWarps * 32, hg::kWaveCtaSmemBytes, st>>>(*ix, *b);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t hg_prepare_dp_kernels()
+{
+    return cudaFuncSetAttribute(hg::dp_wave_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)hg::kWaveCtaSmemBytes);
 }
 
 extern "C" size_t hg_ksw_scratch_bytes(int qlen, int tlen, int w, int flag)

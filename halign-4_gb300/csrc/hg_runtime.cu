@@ -32,6 +32,9 @@ cudaError_t hg_launch_anchor(const hg::IndexDev*, const hg::BatchDev*, int, cuda
 cudaError_t hg_launch_chain(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_dp_small(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_dp_large(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_dp_wave(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_dp_wide(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_prepare_dp_kernels(void);
 cudaError_t hg_launch_stitch(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_rows(const hg::IndexDev*, const hg::BatchDev*, int64_t, int, cudaStream_t);
 cudaError_t hg_launch_count(const uint8_t*, int64_t, int, int, uint32_t*, cudaStream_t);
@@ -138,6 +141,8 @@ struct GraphKey {
 struct hg_ctx {
     hg_index_t* ix = nullptr;
     cudaStream_t st = nullptr;
+    cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int sms = 1;
     int64_t max_n = 0, max_bases = 0, exc_cap = 0;
     int64_t row_stride = 0;
@@ -163,6 +168,7 @@ struct hg_ctx {
     DevBuf<int64_t> s_base;
     DevBuf<int32_t> s_n, n_chain;
     DevBuf<uint32_t> work_small, work_large, work_sorted, work_key, shape_hist;
+    DevBuf<uint32_t> work_wave, work_wave_key, work_wave_sorted, wave_hist, work_wide;
     int64_t dp_cap = 0;
     DevBuf<uint8_t> dp_arena;
     int64_t dp_slot_bytes = 0;
@@ -531,7 +537,13 @@ extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t*
 namespace {
 
 constexpr int kControlWords = 16;
-constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps  // queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact
+// control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide
+constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
+constexpr int kWaveBlocksPerSm = 4;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
+// kernel launches per sub-batch: seed 2, anchor, chain, dp_small 3, dp_wave 2, dp_wide,
+// dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
+constexpr int kLaunchesBatch = 16;
+constexpr int kLaunchesPlain = 15;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
@@ -582,7 +594,9 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     auto* c = new hg_ctx();
     c->ix = ix;
     cudaSetDevice(ix->device);
-    if (cudaError_t pe = hg_prepare_kernels()) {
+    cudaError_t pe = hg_prepare_kernels();
+    if (pe == cudaSuccess) pe = hg_prepare_dp_kernels();
+    if (pe != cudaSuccess) {
         delete c;
         return cuda_fail(pe, "hg_ctx_create: kernel attributes");
     }
@@ -595,12 +609,15 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     c->scap = max_bases / 2 + 4 * max_queries + 65536;
     c->dp_cap = std::max<int64_t>((int64_t)1 << 30, max_bases);
     c->dp_slot_bytes = (int64_t)256 << 10;
-    c->dp_nslots = c->sms * kLargeBlocksPerSm * 4;
+    c->dp_nslots = c->sms * kLargeBlocksPerSm * 4 + c->sms;  // warp slots, then one per CTA-tier CTA
     c->cig_cap = max_bases + max_queries * (L + 4);
     const int64_t n_ent = ix->dev.n_ent;
     const int grid_anchor = c->sms * 3;
     cudaError_t e = cudaSuccess;
     if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) ||
+        (e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming)) ||
         (e = c->packed.alloc(max_bases / 4 + 16 * max_queries + 64)) || (e = c->poff.alloc(max_queries)) ||
         (e = c->exc_off.alloc(max_queries + 1)) || (e = c->hoff.alloc(max_queries)) ||
         (e = c->coff.alloc(max_queries)) || (e = c->qlen.alloc(max_queries)) ||
@@ -619,6 +636,9 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->work_large.alloc(c->scap)) || (e = c->dp_arena.alloc(c->dp_cap)) ||
         (e = c->work_sorted.alloc(c->scap)) || (e = c->work_key.alloc(c->scap)) ||
         (e = c->shape_hist.alloc(2 * (size_t)hg::kShapeBins)) ||
+        (e = c->work_wave.alloc(c->scap)) || (e = c->work_wave_key.alloc(c->scap)) ||
+        (e = c->work_wave_sorted.alloc(c->scap)) || (e = c->wave_hist.alloc(2 * (size_t)hg::kWaveBins)) ||
+        (e = c->work_wide.alloc(c->scap)) ||
         (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) || (e = c->run_flags.alloc(1)) ||
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
@@ -656,6 +676,9 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : c->run_ev)
         if (ev) cudaEventDestroy(ev);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->st2) cudaStreamDestroy(c->st2);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;  // DevBuf members are freed below via explicit frees
 }
@@ -708,6 +731,10 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
     b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
     b.work_sorted = c->work_sorted.p, b.work_key = c->work_key.p, b.shape_hist = c->shape_hist.p;
+    b.work_wave = c->work_wave.p, b.work_wave_key = c->work_wave_key.p, b.work_wave_sorted = c->work_wave_sorted.p;
+    b.wave_hist = c->wave_hist.p, b.work_wide = c->work_wide.p;
+    b.n_wave = reinterpret_cast<unsigned int*>(ctl + 10);
+    b.n_wide = reinterpret_cast<unsigned int*>(ctl + 11);
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
     b.dp_slots = c->dp_slots.p, b.dp_slot_bytes = c->dp_slot_bytes, b.dp_nslots = c->dp_nslots;
     b.run_flags = c->run_flags.p;
@@ -727,6 +754,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, st));
     HG_CUDA(cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * (size_t)b.n, st));
     HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, st));
+    HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * 2 * hg::kWaveBins, st));
     const int n = b.n;
     auto mark = [&](int i) -> cudaError_t { return timed ? cudaEventRecord(c->ev[i], st) : cudaSuccess; };
     HG_CUDA(mark(0));
@@ -738,7 +766,14 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(3));
     HG_CUDA(hg_launch_dp_small(&ix, &b, S * 8, st));
     HG_CUDA(mark(4));
+    // the CTA wavefront tier runs on a side stream beside the warp tiers
+    HG_CUDA(cudaEventRecord(c->fork_ev, st));
+    HG_CUDA(cudaStreamWaitEvent(c->st2, c->fork_ev, 0));
+    HG_CUDA(hg_launch_dp_wide(&ix, &b, S, c->st2));
+    HG_CUDA(cudaEventRecord(c->join_ev, c->st2));
+    HG_CUDA(hg_launch_dp_wave(&ix, &b, S * kWaveBlocksPerSm, st));
     HG_CUDA(hg_launch_dp_large(&ix, &b, S * kLargeBlocksPerSm, st));
+    HG_CUDA(cudaStreamWaitEvent(st, c->join_ev, 0));
     HG_CUDA(mark(5));
     HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 8)), st));
     HG_CUDA(mark(6));
@@ -767,7 +802,7 @@ int run_sub(hg_ctx_t* c, const hg::BatchDev& b, bool use_graph)
             }
             c->last_total_ms += tot;
         }
-        c->last_launches += 9;
+        c->last_launches += kLaunchesBatch;
         return HG_OK;
     }
     GraphKey key{b};
@@ -786,7 +821,7 @@ int run_sub(hg_ctx_t* c, const hg::BatchDev& b, bool use_graph)
         it = c->graphs.emplace(key, ge).first;
     }
     HG_CUDA(cudaGraphLaunch(it->second, c->st));
-    c->last_launches += 9;
+    c->last_launches += kLaunchesBatch;
     return HG_OK;
 }
 
@@ -919,16 +954,19 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
                 // status must survive the per-launch reset: enqueue without the batch memset
                 HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, c->st));
                 HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, c->st));
+                HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * 2 * hg::kWaveBins, c->st));
                 const hg::IndexDev& ix = c->ix->dev;
                 HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, 1, c->st));
                 HG_CUDA(hg_launch_anchor(&ix, &b, 1, c->st));
                 HG_CUDA(hg_launch_chain(&ix, &b, 1, c->st));
                 HG_CUDA(hg_launch_dp_small(&ix, &b, c->sms, c->st));
+                HG_CUDA(hg_launch_dp_wave(&ix, &b, c->sms, c->st));
+                HG_CUDA(hg_launch_dp_wide(&ix, &b, c->sms, c->st));
                 HG_CUDA(hg_launch_dp_large(&ix, &b, c->sms, c->st));
                 HG_CUDA(hg_launch_stitch(&ix, &b, 1, c->st));
                 HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, 1, c->st));
                 HG_CUDA(hg_launch_count(b.rows, c->row_stride, 1, ix.L, c->counts.p, c->st));
-                c->last_launches += 9;
+                c->last_launches += kLaunchesPlain;
             }
         }
         int64_t total = 0;

@@ -194,6 +194,47 @@ def test_edge_cases_vs_oracle(gpu, oracle, pkg):
     del c
 
 
+def test_wavefront_tiers_vs_oracle(gpu, oracle, pkg):
+    """Segments of the two wavefront tiers: long thin tails (one warp, 1-8
+    columns per lane) and wide unbounded-band global alignments (16-warp CTA,
+    1-8 columns per lane, several direction blocks), with and without N
+    runs, in both orientations and both gap modes."""
+    rng = np.random.default_rng(21)
+    L = 12000
+    center = pkg.synth.random_center(L, 31)
+    cmx, cmy = oracle.extract_minimizer(center)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+
+    def rand(n):
+        return acgt[rng.integers(0, 4, n)].tobytes()
+
+    cases = []
+    for a, n in ((100, 420), (5000, 515), (9000, 540)):   # < 100 minimizers: chainless
+        cases.append(center[a:a + n])
+    for n in (300, 700, 1100, 2100, 4000):                # unrelated: chainless, unbounded band
+        cases.append(rand(n))
+    cases.append(center[5000:5600])                       # long tails both sides
+    cases.append(rand(40) + center[3000:6000])            # left tail 3000 x ~40
+    cases.append(center[200:3000] + rand(90))             # right tail
+    cases.append(center[:2000] + rand(300) + center[2000:4000])   # inserted block
+    cases.append(center[:2000] + center[2250:5000])       # deleted block
+    q = bytearray(center[1000:1510])
+    q[100:160] = b"N" * 60
+    cases.append(bytes(q))                                # chainless with an N run
+    cases.append(center[7000:11000].lower())
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=64, max_bases=200000)
+    res = ctx.align(gpu.pack(seqs, offs), rows=True, check=False)
+    for i, qq in enumerate(cases):
+        want = oracle.align_query(center, cmx, cmy, qq)
+        assert np.array_equal(res.cigar_of(i), want), (i, len(qq), oracle.cigar_str(want)[:120],
+                                                        oracle.cigar_str(res.cigar_of(i))[:120])
+        if not (res.status[i] & (pkg.ST_PARTIAL_CIGAR | pkg.ST_LENGTH_MISMATCH)):
+            assert res.rows[i].tobytes() == oracle.del_query(qq, want), i
+
+
 def test_global_align_ksw2_vs_oracle(gpu, oracle):
     rng = np.random.default_rng(2)
     for it in range(30):
