@@ -74,8 +74,7 @@ __device__ __forceinline__ uint32_t shape_key(const Seg& g)
 // segment; wider ones up to kWaveMaxInner run one 16-warp CTA per segment.
 constexpr int kWaveWarpMaxInner = 256;   // 32 lanes x 8 columns
 constexpr int kWaveMaxInner = 4096;      // 16 warps x 32 lanes x 8 columns
-constexpr int kWaveBins = 32;            // sort bins of the one-warp list
-constexpr int kWaveLongSteps = 2048;     // segments this long sort first
+constexpr int kWaveBins = 256;           // sort bins of the one-warp list
 
 __host__ __device__ __forceinline__ bool wave_eligible(uint32_t rl, uint32_t ql)
 {
@@ -101,16 +100,18 @@ __host__ __device__ __forceinline__ int wave_cta_cols(int inner)
     return inner <= 512 ? 1 : inner <= 1024 ? 2 : inner <= 2048 ? 4 : 8;
 }
 
-// Sort key of a one-warp wavefront segment: long ones (more than
-// kWaveLongSteps rows) first, so they do not start last; then widest first,
-// orientation and gap mode, so the warps of an SM run the same code together.
+// Sort key of a one-warp wavefront segment: longest first by power-of-two
+// class of rl + ql (the step count), so long segments do not start last;
+// within a class widest first, then orientation and gap mode, so the warps
+// of an SM run the same code together.
 __host__ __device__ __forceinline__ uint32_t wave_key(uint32_t rl, uint32_t ql, bool left)
 {
-    const int inner = (int)(rl < ql ? rl : ql), outer = (int)(rl < ql ? ql : rl);
+    const int inner = (int)(rl < ql ? rl : ql);
     const int P = wave_warp_cols(inner);
     const uint32_t pidx = P == 1 ? 0u : P == 2 ? 1u : P == 4 ? 2u : 3u;
-    const uint32_t shortb = outer > kWaveLongSteps ? 0u : 1u;
-    return shortb << 4 | (3u - pidx) << 2 | (rl <= ql ? 1u : 0u) << 1 | (left ? 0u : 1u);
+    uint32_t cls = 0;
+    for (uint32_t t = (rl + ql) >> 1; t && cls < 15; t >>= 1) ++cls;
+    return (15u - cls) << 4 | (3u - pidx) << 2 | (rl <= ql ? 1u : 0u) << 1 | (left ? 0u : 1u);
 }
 
 struct BatchDev {

@@ -29,6 +29,7 @@
 //   diagonal run 32 at a time; the byte carried from the previous 32-lane
 //   chunk plays the role of the SSE shift-in register.
 #include <cstdio>
+#include <type_traits>
 #include <mutex>
 
 #include "hg_batch.cuh"
@@ -114,6 +115,33 @@ __device__ __forceinline__ uint32_t lane_int(int s, int xt1, int vt1, int ut, in
         d |= (a >= 0 ? 4u : 0u) | (b >= 0 ? 8u : 0u);
     }
     return d;  // bits 0-1 state, bit 2 E continuation, bit 3 F continuation
+}
+
+// lane_int with the score already offset: z0 = score + 16, and the max
+// with the column-side term taken first so the row-carried term (xt1 + vt1)
+// is the last input on the dependency chain.
+template <int MODE>
+__device__ __forceinline__ uint32_t lane_int_z(int z0, int xt1, int vt1, int ut, int yt, int& u, int& v, int& x,
+                                               int& y)
+{
+    const int a0 = xt1 + vt1, b0 = yt + ut;
+    uint32_t d;
+    if (MODE == 1) {
+        d = a0 > z0 ? 1u : 0u;
+        if (b0 > max(z0, a0)) d = 2u;
+    } else {
+        d = z0 > a0 ? 0u : 1u;
+        if (!(max(z0, a0) > b0)) d = 2u;
+    }
+    const int z = min(max(max(z0, b0), a0), 21);
+    u = z - vt1;
+    v = z - ut;
+    const int zq = z - 6;
+    const int a = a0 - zq, b = b0 - zq;
+    x = max(a, 0), y = max(b, 0);
+    if (MODE == 1) d |= (a > 0 ? 4u : 0u) | (b > 0 ? 8u : 0u);
+    else d |= (a >= 0 ? 4u : 0u) | (b >= 0 ? 8u : 0u);
+    return d;
 }
 
 // Segment DP for one thread.  TINNER: the target is the shorter (inner) side;
@@ -523,23 +551,25 @@ __device__ KswResult ksw_extz2_warp(const KswArgs& a, uint8_t* scratch, uint32_t
 // or >= both lengths) the DP is the small tier's per-cell int32 recurrence
 // (lane_int), so it needs neither the anti-diagonal byte arrays nor the H row
 // of the exact emulation.  A group of GW warps (1, or a 16-warp CTA for wide
-// segments) runs it as a register wavefront: virtual lane v = 32 x warp +
-// lane owns P consecutive columns of the shorter side and at step s computes
-// row s - v of them.  The pair carried along a row and the row's outer base
-// move one lane up per step through a shuffle; across a warp boundary they
-// go through a shared-memory ring, the warps running 32-step windows with a
-// barrier between windows and warp k one window behind warp k-1.  Virtual
-// lane 0 takes the boundary column and a fresh outer base.
+// segments) runs it as a register wavefront over anti-diagonals: virtual
+// lane v = 32 x warp + lane owns the P consecutive columns c = vP .. vP+P-1
+// of the shorter side, and cell (o, c) runs at step o + c, so the P cells a
+// lane computes per step are independent.  The pair carried along a row and
+// the row's outer base move one column per step: inside a lane through
+// registers, to the next lane through a shuffle, across a warp boundary
+// through a shared-memory ring (the warps run 32-step windows with a barrier
+// between windows, warp k one window behind warp k-1).  Column 0 takes the
+// boundary column and a fresh outer base.
 //
 // Direction nibbles: one word holds 8/P steps x P columns of one virtual
 // lane; step group t of lane v is word t x LDW + v (LDW = lanes that hold
 // columns).  The traceback walks K-step blocks held in shared memory, from
-// the last block to the first (the step index o + c/P never increases along
+// the last block to the first (the step index o + c never increases along
 // the path).  A segment of one block computes straight into shared memory.
 // A longer one either writes every word to global scratch during the single
 // forward pass and copies each block back for the walk, or - when no scratch
 // of that size is left - saves each warp's state at every block start
-// (per lane: the column bytes and the outgoing carried word) and recomputes
+// (per column: its state and its last outputs) and recomputes
 // each block from its saved state for the walk.
 constexpr int kWaveWarpDirWords = 2048;   // one-warp groups: 8 KB per warp
 constexpr int kWaveCtaWarps = 16;
@@ -557,9 +587,9 @@ __host__ __device__ __forceinline__ WaveGeom wave_geom(int inner, int outer, int
     G.lanes = (inner + P - 1) / P;
     G.nw = (G.lanes + 31) / 32;
     G.K = ((dir_words / G.lanes) * (8 / P)) & ~31;   // steps per block, a multiple of 32
-    G.S = outer + (inner - 1) / P;
+    G.S = outer + inner - 1;                          // cell (o, c) runs at step o + c
     G.nblk = (G.S + G.K - 1) / G.K;
-    G.ckw = (2 * P + 3) / 4 + 1;
+    G.ckw = (5 * P + 3) / 4;
     return G;
 }
 
@@ -593,126 +623,169 @@ __device__ __forceinline__ void wave_segment(const IndexDev& ix, const BatchDev&
     const int lane = threadIdx.x & 31;
     const int wk = GW == 1 ? 0 : (int)(threadIdx.x >> 5);
     constexpr int SPW = 8 / P;                       // steps per direction word
-    constexpr int CKW = (2 * P + 3) / 4 + 1;         // checkpoint words per lane
+    constexpr int CKW = (5 * P + 3) / 4;             // checkpoint words per lane (5 bytes per column)
     const int qn = (int)g.ql, tn = (int)g.rl;
     const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
     const WaveGeom G = wave_geom(inner, outer, P, dir_words);
     const int NW = G.nw, K = G.K, S = G.S, nblk = G.nblk, LDW = G.lanes;
     const bool active = wk < NW;
-    const int v = wk * 32 + lane;                    // virtual lane
+    const int v = wk * 32 + lane;                    // virtual lane; columns v*P .. v*P+P-1
     const bool holds = v < LDW;                      // this lane owns columns
     const uint8_t* pk = b.packed + b.poff[g.q];
     const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
     const bool plain_q = e0 == e1;
     const uint8_t* tc = ix.center + g.rs;
-    int ic[P], s1[P], s2[P];
+    // per column: score table (z0 = score + 16 at bit 5 x outer code), column
+    // state from the row above (s1, s2) and the column's outputs of the last
+    // step (r1, r2: carried pair; r5: 5 x the row's outer code)
+    uint32_t tab[P];
+    int s1[P], s2[P], r1[P], r2[P], r5[P];
 #pragma unroll
     for (int p = 0; p < P; ++p) {
         const int c = v * P + p;
-        ic[p] = 0;
+        int ic = 0;
         if (active && c < inner) {
-            if (TINNER) ic[p] = tc[c];
-            else ic[p] = plain_q ? (int)packed_code(pk, g.qs + c) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + c);
+            if (TINNER) ic = tc[c];
+            else ic = plain_q ? (int)packed_code(pk, g.qs + c) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + c);
         }
+        uint32_t t = 0;
+#pragma unroll
+        for (int oc = 0; oc < 5; ++oc) t |= (uint32_t)((ic == 4 || oc == 4) ? 16 : (ic == oc ? 21 : 12)) << (5 * oc);
+        tab[p] = t;
     }
-    uint32_t cout = 0, chunk = 0;
+    auto pack_last = [&]() -> uint32_t {
+        return (uint32_t)r1[P - 1] | (uint32_t)r2[P - 1] << 8 | (uint32_t)r5[P - 1] << 16;
+    };
     auto init_state = [&]() {
 #pragma unroll
         for (int p = 0; p < P; ++p) {
             const int c = v * P + p;
             if (TINNER) s1[p] = c ? 6 : 0, s2[p] = 0;   // u, y above row 0
             else s1[p] = 0, s2[p] = c ? 6 : 0;          // x, v left of column 0
+            r1[p] = r2[p] = r5[p] = 0;
         }
-        cout = 0;
     };
+    // checkpoint: 5 bytes per column (s1, s2, r1, r2, r5)
     auto ck = [&](int bk, int w) -> uint32_t& { return scratch[((bk * NW + wk) * CKW + w) * 32 + lane]; };
+    auto byte_of = [&](int k) -> int {
+        const int p = k % P, f = k / P;
+        return f == 0 ? s1[p] : f == 1 ? s2[p] : f == 2 ? r1[p] : f == 3 ? r2[p] : r5[p];
+    };
+    auto set_byte = [&](int k, int val) {
+        const int p = k % P, f = k / P;
+        if (f == 0) s1[p] = val;
+        else if (f == 1) s2[p] = val;
+        else if (f == 2) r1[p] = val;
+        else if (f == 3) r2[p] = val;
+        else r5[p] = val;
+    };
     auto save = [&](int bk) {
 #pragma unroll
-        for (int w = 0; w < CKW - 1; ++w) {
+        for (int w = 0; w < CKW; ++w) {
             uint32_t wd = 0;
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int k = 4 * w + j;
-                if (k < P) wd |= (uint32_t)s1[k] << (8 * j);
-                else if (k < 2 * P) wd |= (uint32_t)s2[k - P] << (8 * j);
-            }
+            for (int j = 0; j < 4; ++j)
+                if (4 * w + j < 5 * P) wd |= (uint32_t)byte_of(4 * w + j) << (8 * j);
             ck(bk, w) = wd;
         }
-        ck(bk, CKW - 1) = cout;
     };
     auto restore = [&](int bk) {
 #pragma unroll
-        for (int w = 0; w < CKW - 1; ++w) {
+        for (int w = 0; w < CKW; ++w) {
             const uint32_t wd = ck(bk, w);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int k = 4 * w + j;
-                if (k < P) s1[k] = (int)((wd >> (8 * j)) & 0xffu);
-                else if (k < 2 * P) s2[k - P] = (int)((wd >> (8 * j)) & 0xffu);
+            for (int j = 0; j < 4; ++j)
+                if (4 * w + j < 5 * P) set_byte(4 * w + j, (int)((wd >> (8 * j)) & 0xffu));
+        }
+    };
+    // 5 x outer code of row o (0 past the end)
+    auto outer_code5 = [&](int o) -> uint32_t {
+        if (o >= outer) return 0u;
+        uint32_t c;
+        if (TINNER) c = plain_q ? packed_code(pk, g.qs + o) : query_dna5(pk, b.exc, e0, e1, g.qs + o);
+        else c = tc[o];
+        return 5u * c;
+    };
+    // One step at s: column p of lane v computes row s - (v*P + p), so the P
+    // cells of a lane are independent.  Column p takes the pair carried from
+    // column p-1's previous step (column 0: from the lane below by shuffle,
+    // across a warp boundary from the ring; virtual lane 0: the boundary and
+    // a fresh outer base).  `chunk`/`ringv` hold window values at lane s & 31.
+    auto step = [&](auto guard_tag, int s, uint32_t chunk, uint32_t ringv) -> uint32_t {
+        constexpr bool GUARD = decltype(guard_tag)::value;
+        int c1 = __shfl_up_sync(FULL, r1[P - 1], 1);
+        int c2 = __shfl_up_sync(FULL, r2[P - 1], 1);
+        int c5 = __shfl_up_sync(FULL, r5[P - 1], 1);
+        const uint32_t fresh = __shfl_sync(FULL, chunk, s & 31);
+        if (GW > 1) {
+            const uint32_t rv = __shfl_sync(FULL, ringv, s & 31);
+            if (lane == 0 && wk > 0) c1 = (int)(rv & 0xffu), c2 = (int)((rv >> 8) & 0xffu), c5 = (int)(rv >> 16);
+        }
+        if (v == 0) {
+            const int ob = s ? 6 : 0;
+            c1 = TINNER ? 0 : ob;
+            c2 = TINNER ? ob : 0;
+            c5 = (int)fresh;
+        }
+        uint32_t dn = 0;
+#pragma unroll
+        for (int p = P - 1; p >= 0; --p) {  // descending: column p reads column p-1's previous outputs
+            const int i1 = p ? r1[p - 1] : c1, i2 = p ? r2[p - 1] : c2, i5 = p ? r5[p - 1] : c5;
+            const int o = s - (v * P + p);
+            if (!GUARD || (o >= 0 && o < outer && v * P + p < inner)) {
+                const int z0 = (int)((tab[p] >> i5) & 31u);
+                int u, vv, x, y;
+                uint32_t d;
+                if (TINNER) {
+                    d = lane_int_z<MODE>(z0, i1, i2, s1[p], s2[p], u, vv, x, y);
+                    r1[p] = x, r2[p] = vv, s1[p] = u, s2[p] = y;
+                } else {
+                    d = lane_int_z<MODE>(z0, s1[p], s2[p], i1, i2, u, vv, x, y);
+                    r1[p] = u, r2[p] = y, s1[p] = x, s2[p] = vv;
+                }
+                r5[p] = i5;
+                dn |= d << (4 * p);
             }
         }
-        cout = ck(bk, CKW - 1);
+        if (GW > 1 && lane == 31) ring[wk * kWaveRing + (s & (kWaveRing - 1))] = pack_last();
+        return dn;
     };
-    // Steps [sb, se) of every active warp, sb a multiple of 32.  Words of
-    // steps >= dbase go to shared memory (the block it holds starts at
+    // Steps [sb, se) of every active warp, sb a multiple of 32; whole 32-step
+    // windows run (steps past the segment's last are inactive in every
+    // column, and recomputed blocks end on a window boundary).  Words of step
+    // groups >= dbase go to shared memory (the block it holds starts at
     // dbase); with to_global every word goes to global scratch instead; with
     // save_ck each warp saves its state at the block starts below the last.
     auto run = [&](int sb, int se, int dbase, bool to_global, bool save_ck) {
         const int nwin = (se - sb + 31) / 32 + (GW > 1 ? NW - 1 : 0);
-        uint32_t acc = 0;
+        const int clo = wk * 32 * P, chi = min(LDW, wk * 32 + 32) * P - 1;  // this warp's columns
+        uint32_t chunk_next = (active && wk == 0) ? outer_code5(sb + lane) : 0u;
         for (int j = 0; j < nwin; ++j) {
             const int s0 = sb + (j - wk) * 32;
             if (active && s0 >= sb && s0 < se) {
                 if (save_ck && s0 > 0 && s0 % K == 0 && s0 / K <= nblk - 2) save(s0 / K);
-                const int s1e = min(s0 + 32, se);
-                if (wk == 0) {
-                    const int o = s0 + lane;
-                    chunk = 0;
-                    if (o < outer) {
-                        if (TINNER) chunk = plain_q ? packed_code(pk, g.qs + o) : query_dna5(pk, b.exc, e0, e1, g.qs + o);
-                        else chunk = tc[o];
-                    }
-                }
-                for (int s = s0; s < s1e; ++s) {
-                    const uint32_t fresh = __shfl_sync(FULL, chunk, s & 31);
-                    uint32_t cin = __shfl_up_sync(FULL, cout, 1);
-                    if (GW > 1 && lane == 0 && wk > 0) cin = ring[(wk - 1) * kWaveRing + ((s - 1) & (kWaveRing - 1))];
-                    const int o = s - v;
-                    // virtual lane 0: left boundary column and a fresh outer base
-                    const bool first = v == 0;
-                    const int ob = o ? 6 : 0;
-                    int c1 = first ? (TINNER ? 0 : ob) : (int)(cin & 0xffu);
-                    int c2 = first ? (TINNER ? ob : 0) : (int)((cin >> 8) & 0xffu);
-                    const int oc = first ? (int)fresh : (int)(cin >> 16);
-                    uint32_t dn = 0;
-                    if (o >= 0 && o < outer) {
+                const uint32_t chunk = chunk_next;
+                if (wk == 0) chunk_next = outer_code5(s0 + 32 + lane);
+                uint32_t ringv = 0;
+                if (GW > 1 && wk > 0) ringv = ring[(wk - 1) * kWaveRing + ((s0 - 1 + lane) & (kWaveRing - 1))];
+                // every real column of the warp on a row inside the segment for the
+                // whole window (columns past the last only feed columns past the last)
+                const bool fast = s0 - min(chi, inner - 1) >= 0 && s0 + 31 - clo <= outer - 1;
+                for (int gq = 0; gq < 32 / SPW; ++gq) {
+                    const int sg = s0 + gq * SPW;
+                    uint32_t acc = 0;
+                    if (fast) {
 #pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            if (v * P + p < inner) {
-                                const int sc = (ic[p] == 4 || oc == 4) ? 0 : (ic[p] == oc ? 5 : -4);
-                                int u, vv, x, y;
-                                uint32_t d;
-                                if (TINNER) {
-                                    d = lane_int<MODE>(sc, c1, c2, s1[p], s2[p], u, vv, x, y);
-                                    c1 = x, c2 = vv, s1[p] = u, s2[p] = y;
-                                } else {
-                                    d = lane_int<MODE>(sc, s1[p], s2[p], c1, c2, u, vv, x, y);
-                                    c1 = u, c2 = y, s1[p] = x, s2[p] = vv;
-                                }
-                                dn |= d << (4 * p);
-                            }
-                        }
-                        cout = (uint32_t)c1 | (uint32_t)c2 << 8 | (uint32_t)oc << 16;
+                        for (int k = 0; k < SPW; ++k)
+                            acc |= step(std::false_type{}, sg + k, chunk, ringv) << (4 * P * k);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < SPW; ++k)
+                            acc |= step(std::true_type{}, sg + k, chunk, ringv) << (4 * P * k);
                     }
-                    if (GW > 1 && lane == 31) ring[wk * kWaveRing + (s & (kWaveRing - 1))] = cout;
-                    if (SPW == 1) acc = dn;
-                    else acc |= dn << (4 * P * (s % SPW));
-                    if (s % SPW == SPW - 1 || s == se - 1) {
-                        if (holds) {
-                            if (to_global) scratch[(size_t)(s / SPW) * LDW + v] = acc;
-                            else if (s >= dbase) dirs[((s - dbase) / SPW) * LDW + v] = acc;
-                        }
-                        acc = 0;
+                    if (holds && sg < se) {
+                        if (to_global) scratch[(size_t)(sg / SPW) * LDW + v] = acc;
+                        else if (sg >= dbase) dirs[((sg - dbase) / SPW) * LDW + v] = acc;
                     }
                 }
             }
@@ -739,10 +812,9 @@ __device__ __forceinline__ void wave_segment(const IndexDev& ix, const BatchDev&
             const int base = bk * K;
             while (ti >= 0 && qj >= 0) {
                 const int o = TINNER ? qj : ti, c = TINNER ? ti : qj;
-                const int vl = c / P;
-                const int s = o + vl;
+                const int s = o + c;
                 if (s < base) break;
-                const uint32_t word = dirs[((s - base) / SPW) * LDW + vl];
+                const uint32_t word = dirs[((s - base) / SPW) * LDW + c / P];
                 const uint32_t nib = (word >> (4 * (P * (s % SPW) + c % P))) & 0xfu;
                 if (state == 0) state = nib & 3u;
                 else if (!((nib >> (state + 1)) & 1u)) state = 0;
@@ -767,7 +839,7 @@ __device__ __forceinline__ void wave_segment(const IndexDev& ix, const BatchDev&
             if (active) {
                 if (bk == 0) init_state();
                 else restore(bk);
-                if (GW > 1 && lane == 31 && bk > 0) ring[wk * kWaveRing + ((bk * K - 1) & (kWaveRing - 1))] = cout;
+                if (GW > 1 && lane == 31 && bk > 0) ring[wk * kWaveRing + ((bk * K - 1) & (kWaveRing - 1))] = pack_last();
             }
             wave_sync<GW>();
             run(bk * K, (bk + 1) * K, bk * K, false, false);
