@@ -33,27 +33,33 @@ namespace hg {
 
 constexpr int kChainWarps = 4;
 
-__device__ __forceinline__ int32_t chain_score(const IndexDev& ix, uint32_t ri, uint32_t qi, uint32_t rj, uint32_t qj,
-                                               int32_t span_j)
+// chainScoreSimple; lg2 = log2f table (shared memory copy of ix.log2tab).
+__device__ __forceinline__ int32_t chain_score(const IndexDev& ix, const float* lg2, uint32_t ri, uint32_t qi,
+                                               uint32_t rj, uint32_t qj, int32_t span_j)
 {
     const int32_t dq = (int32_t)qi - (int32_t)qj;
-    if (dq <= 0 || dq > ix.max_dist_x) return INT32_MIN;
     const int32_t dr = (int32_t)ri - (int32_t)rj;
-    if (dr <= 0 || dr > ix.max_dist_y) return INT32_MIN;
     const int32_t dd = dr > dq ? dr - dq : dq - dr;
-    if (dd > ix.bw) return INT32_MIN;
+    const bool ok = dq > 0 && dq <= ix.max_dist_x && dr > 0 && dr <= ix.max_dist_y && dd <= ix.bw;
     const int32_t dg = dr < dq ? dr : dq;
     int32_t sc = span_j < dg ? span_j : dg;
-    if (dd > 0 || dg > span_j) {
+    if (ok && (dd > 0 || dg > span_j)) {
         const float lin = __fadd_rn(__fmul_rn(ix.gap_pen, (float)dd), __fmul_rn(ix.skip_pen, (float)dg));
-        const float lg = dd >= 1 ? ix.log2tab[dd + 1] : 0.0f;
+        const float lg = dd >= 1 ? lg2[dd + 1] : 0.0f;
         sc -= __float2int_rz(__fadd_rn(lin, __fmul_rn(0.5f, lg)));
     }
-    return sc;
+    return ok ? sc : INT32_MIN;
 }
+
+constexpr int kLog2Max = 512;  // dd <= bw (500), index dd + 1
 
 __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, BatchDev b)
 {
+    __shared__ float lg2s[kLog2Max + 1];
+    for (int k = threadIdx.x; k <= kLog2Max; k += blockDim.x) lg2s[k] = k < ix.n_log2 ? ix.log2tab[k] : 0.0f;
+    __syncthreads();
+    // a band wider than the shared copy (bw > kLog2Max - 1) reads the table in global memory
+    const float* lg2 = ix.n_log2 <= kLog2Max + 1 ? lg2s : ix.log2tab;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int32_t span = ix.k;
@@ -74,50 +80,122 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         __syncwarp();
         int st = 0, best = -1;
         int32_t best_f = 0;
+        // register windows: lane l holds candidate j = i-1-l (position pair,
+        // f, p) and the positions of anchor i0 + l of the current 32-anchor block
+        uint32_t w_ar = 0, w_aq = 0, nx_ar = 0, nx_aq = 0;
+        int32_t w_f = 0, w_p = -1;
         for (int i = 0; i < A; ++i) {
-            const uint32_t ri = ar[i], qv = aq[i];
+            if ((i & 31) == 0) {
+                nx_ar = i + lane < A ? ar[i + lane] : 0u;
+                nx_aq = i + lane < A ? aq[i + lane] : 0u;
+            }
+            const uint32_t ri = __shfl_sync(FULL, nx_ar, i & 31), qv = __shfl_sync(FULL, nx_aq, i & 31);
             while (st < i && (int32_t)(ri - ar[st]) > ix.max_dist_x) ++st;
             const int it0 = (i - st > ix.max_iter) ? i - ix.max_iter : st;
             int32_t max_f = span;
             int max_j = -1;
             int n_skip = 0;
-            for (int jb = i - 1; jb >= it0; jb -= 32) {
-                const int j = jb - lane;
-                bool valid = j >= it0;
-                int32_t sc = INT32_MIN;
-                if (valid) sc = chain_score(ix, ri, qv, ar[j], aq[j], span);
-                valid = valid && sc != INT32_MIN;
-                int32_t fj = 0, pj = -1;
-                if (valid) fj = f[j], pj = p[j];
-                if (valid && pj >= 0) t[pj] = i;
-                __syncwarp();
-                const bool marked = valid && t[j] == i;
-                const int32_t tot = fj + sc;
-                const int32_t vmax = warp_incl_max(valid ? tot : INT32_MIN);
-                int32_t prev = __shfl_up_sync(FULL, vmax, 1);
-                if (lane == 0) prev = INT32_MIN;
-                prev = max(prev, max_f);
-                const bool rec = valid && tot > prev;
-                const int d = rec ? -1 : (marked ? 1 : 0);
-                const int S = warp_incl_sum(d);
-                const int mS = warp_incl_min(S);
-                const int X = S + max(n_skip, -mS);
-                const unsigned brk = __ballot_sync(FULL, d == 1 && X > ix.max_skip);
-                unsigned recm = __ballot_sync(FULL, rec);
-                if (brk) recm &= (1u << (__ffs(brk) - 1)) - 1u;
-                if (recm) {
-                    const int L = 31 - __clz(recm);
-                    max_f = __shfl_sync(FULL, tot, L);
-                    max_j = __shfl_sync(FULL, j, L);
+            bool done = true;
+            if (i > it0) {
+                // first chunk (j = i-1 .. i-32) from the register window
+                const int j = i - 1 - lane;
+                const int32_t sc = j >= it0 ? chain_score(ix, lg2, ri, qv, w_ar, w_aq, span) : INT32_MIN;
+                const bool valid = sc != INT32_MIN;
+                const int32_t tot = w_f + sc;
+                const int32_t vt = valid ? tot : INT32_MIN;
+                // marks: a valid lane marks p[j], i.e. lane i-1-p[j] (always a
+                // later lane); marks past this chunk go to t[] for the next one
+                uint32_t bits = 0;
+                if (valid && w_p >= 0) {
+                    const int tl = i - 1 - w_p;
+                    if (tl < 32) bits = 1u << tl;
+                    else t[w_p] = i;
                 }
-                if (brk) break;
-                n_skip = __shfl_sync(FULL, X, 31);
+                const uint32_t vmask = __ballot_sync(FULL, valid);
+                const uint32_t mk = __reduce_or_sync(FULL, bits) & vmask;
+                const int32_t M = __reduce_max_sync(FULL, vt);
+                const uint32_t lead = __ballot_sync(FULL, vt == M);
+                if (M <= span) {
+                    // no improvement: n_skip counts the marked lanes
+                    const int cnt = __popc(mk);
+                    done = cnt > ix.max_skip || i - 32 <= it0;
+                    n_skip = cnt;
+                } else if (lead & 1u) {
+                    // lane 0 holds the maximum: the only improvement; after it
+                    // n_skip = max(0 - 1, 0) = 0 and counts the marked lanes
+                    max_f = __shfl_sync(FULL, tot, 0);
+                    max_j = i - 1;
+                    const int cnt = __popc(mk & ~1u);
+                    done = cnt > ix.max_skip || i - 32 <= it0;
+                    n_skip = cnt;
+                } else {
+                    const bool marked = (mk >> lane) & 1u;
+                    const int32_t vmax = warp_incl_max(vt);
+                    int32_t prev = __shfl_up_sync(FULL, vmax, 1);
+                    if (lane == 0) prev = INT32_MIN;
+                    const bool rec = valid && tot > max(prev, max_f);
+                    const int d = rec ? -1 : (marked ? 1 : 0);
+                    const int S = warp_incl_sum(d);
+                    const int mS = warp_incl_min(S);
+                    const int X = S + max(0, -mS);
+                    const unsigned brk = __ballot_sync(FULL, d == 1 && X > ix.max_skip);
+                    unsigned recm = __ballot_sync(FULL, rec);
+                    if (brk) recm &= (1u << (__ffs(brk) - 1)) - 1u;
+                    if (recm) {
+                        const int L = 31 - __clz(recm);
+                        max_f = __shfl_sync(FULL, tot, L);
+                        max_j = i - 1 - L;
+                    }
+                    done = brk != 0 || i - 32 <= it0;
+                    n_skip = __shfl_sync(FULL, X, 31);
+                }
+            }
+            // later chunks: marks through t[], warp scans
+            if (!done) {
                 __syncwarp();
+                for (int jb = i - 33; jb >= it0; jb -= 32) {
+                    const int j = jb - lane;
+                    int32_t sc = INT32_MIN;
+                    if (j >= it0) sc = chain_score(ix, lg2, ri, qv, ar[j], aq[j], span);
+                    const bool valid = sc != INT32_MIN;
+                    int32_t fj = 0, pj = -1;
+                    if (valid) fj = f[j], pj = p[j];
+                    if (valid && pj >= 0) t[pj] = i;
+                    __syncwarp();
+                    const bool marked = valid && t[j] == i;
+                    const int32_t tot = fj + sc;
+                    const int32_t vmax = warp_incl_max(valid ? tot : INT32_MIN);
+                    int32_t prev = __shfl_up_sync(FULL, vmax, 1);
+                    if (lane == 0) prev = INT32_MIN;
+                    prev = max(prev, max_f);
+                    const bool rec = valid && tot > prev;
+                    const int d = rec ? -1 : (marked ? 1 : 0);
+                    const int S = warp_incl_sum(d);
+                    const int mS = warp_incl_min(S);
+                    const int X = S + max(n_skip, -mS);
+                    const unsigned brk = __ballot_sync(FULL, d == 1 && X > ix.max_skip);
+                    unsigned recm = __ballot_sync(FULL, rec);
+                    if (brk) recm &= (1u << (__ffs(brk) - 1)) - 1u;
+                    if (recm) {
+                        const int L = 31 - __clz(recm);
+                        max_f = __shfl_sync(FULL, tot, L);
+                        max_j = __shfl_sync(FULL, j, L);
+                    }
+                    if (brk) break;
+                    n_skip = __shfl_sync(FULL, X, 31);
+                    __syncwarp();
+                }
             }
             if (lane == 0) f[i] = max_f, p[i] = max_j;
-            __syncwarp();
             if (max_f > best_f) best_f = max_f, best = i;
+            // shift the window: lane l takes lane l-1's anchor, lane 0 anchor i
+            w_ar = __shfl_up_sync(FULL, w_ar, 1);
+            w_aq = __shfl_up_sync(FULL, w_aq, 1);
+            w_f = __shfl_up_sync(FULL, w_f, 1);
+            w_p = __shfl_up_sync(FULL, w_p, 1);
+            if (lane == 0) w_ar = ri, w_aq = qv, w_f = max_f, w_p = max_j;
         }
+        __syncwarp();
         // backtrack: chain (reversed) into t[], read p[] 32 entries at a time
         int c = 0;
         if (!(best_f < ix.min_score || best < 0)) {
