@@ -13,6 +13,8 @@ struct IndexDev {
     int k, w;                  // minimizer k-mer size and window
     int non_canonical;         // 1 on the align-to-center path (src/align/ref_aligner.cpp:83)
     const uint8_t* center;     // DNA5 codes of the center the DP aligns to
+    const uint8_t* center2;    // the same center 2-bit packed (base i at bits 2(i&3) of byte i>>2), 64 B slack
+    int center_plain;          // 1 when every center code is A/C/G/T (center2 is exact)
     const uint64_t* tab_key;   // open-addressing table: key = hash56 (kNoHash = empty)
     const uint32_t* tab_val;   // entry id of the key
     uint32_t tab_mask;
@@ -187,6 +189,7 @@ struct BatchDev {
     uint32_t* ins;               // L + 1 insertion events
     uint32_t* status;            // per query
     unsigned int* queues;        // work-queue heads, one per stage
+    unsigned int* queues2;       // more work-queue heads: [0] seed fast path
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };

@@ -144,10 +144,26 @@ __device__ __forceinline__ uint32_t lane_int_z(int z0, int xt1, int vt1, int ut,
     return d;
 }
 
+// 64 bases of 2-bit codes from base `pos` of a packed stream (base i at bits
+// 2(i&3) of byte i>>2): base pos+m at bits 2m of lo (m < 32) / 2(m-32) of hi.
+// The stream is 8-byte aligned and readable 24 bytes past byte (pos/4 & ~7).
+__device__ __forceinline__ void load_bases64(const uint8_t* pk, uint32_t pos, uint64_t& lo, uint64_t& hi)
+{
+    const uint32_t wb = (pos >> 2) & ~7u;
+    const uint64_t* w = reinterpret_cast<const uint64_t*>(pk + wb);
+    const uint64_t w0 = w[0], w1 = w[1], w2 = w[2];
+    const uint32_t sh = 2u * (pos - wb * 4u);  // 0 .. 62
+    lo = sh ? (w0 >> sh) | (w1 << (64u - sh)) : w0;
+    hi = sh ? (w1 >> sh) | (w2 << (64u - sh)) : w1;
+}
+
 // Segment DP for one thread.  TINNER: the target is the shorter (inner) side;
 // rows run over the query.  Direction codes: row o, inner position i at word
-// o*stride + i/8, nibble i%8, words interleaved across the CTA.
-template <bool TINNER, int MODE>
+// o*stride + i/8, nibble i%8, words interleaved across the CTA.  FAST: the
+// query has no exception bytes and the center is all A/C/G/T, so both sides
+// come from 2-bit packed words held in registers.  The traceback writes each
+// op run once, last-first (the stitch reads small-tier segments backwards).
+template <bool TINNER, int MODE, bool FAST>
 __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev& b, uint32_t sid, const Seg& g,
                                               uint32_t* dirs, int tid)
 {
@@ -155,22 +171,40 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
     const int stride = (inner + 7) >> 3;
     const uint8_t* pk = b.packed + b.poff[g.q];
-    const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
+    const int64_t e0 = FAST ? 0 : b.exc_off[g.q], e1 = FAST ? 0 : b.exc_off[g.q + 1];
     const bool plain_q = e0 == e1;
     const uint8_t* tc = ix.center + g.rs;
     int ic[kSmallMaxInner], s1[kSmallMaxInner], s2[kSmallMaxInner];
+    uint64_t olo = 0, ohi = 0;
+    if (FAST) {
+        uint64_t qlo, qhi, tlo, thi;
+        load_bases64(pk, g.qs, qlo, qhi);
+        load_bases64(ix.center2, g.rs, tlo, thi);
+        const uint64_t ilo = TINNER ? tlo : qlo;
+        olo = TINNER ? qlo : tlo;
+        ohi = TINNER ? qhi : thi;
 #pragma unroll
-    for (int i = 0; i < kSmallMaxInner; ++i) {
-        ic[i] = 0, s1[i] = 0, s2[i] = 0;
-        if (i < inner) {
-            if (TINNER) ic[i] = tc[i];
-            else ic[i] = plain_q ? (int)packed_code(pk, g.qs + i) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + i);
+        for (int i = 0; i < kSmallMaxInner; ++i) ic[i] = (int)((ilo >> (2 * i)) & 3u);
+    } else {
+#pragma unroll
+        for (int i = 0; i < kSmallMaxInner; ++i) {
+            ic[i] = 0;
+            if (i < inner) {
+                if (TINNER) ic[i] = tc[i];
+                else ic[i] = plain_q ? (int)packed_code(pk, g.qs + i) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + i);
+            }
         }
     }
+#pragma unroll
+    for (int i = 0; i < kSmallMaxInner; ++i) s1[i] = 0, s2[i] = 0;
     for (int o = 0; o < outer; ++o) {
         int oc;
-        if (TINNER) oc = plain_q ? (int)packed_code(pk, g.qs + o) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + o);
-        else oc = tc[o];
+        if (FAST) {
+            oc = (int)(((o < 32 ? olo : ohi) >> (2 * (o & 31))) & 3u);
+        } else {
+            if (TINNER) oc = plain_q ? (int)packed_code(pk, g.qs + o) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + o);
+            else oc = tc[o];
+        }
         // TINNER: carried x, v along the row, s1/s2 = u, y of the previous row.
         // !TINNER: carried u, y along the column, s1/s2 = x, v of the previous column.
         int c1 = 0, c2 = o ? 6 : 0;
@@ -178,17 +212,18 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
 #pragma unroll
         for (int i = 0; i < kSmallMaxInner; ++i) {
             if (i < inner) {
-                const int sc = (ic[i] == 4 || oc == 4) ? 0 : (ic[i] == oc ? 5 : -4);
+                const int z0 = FAST ? (ic[i] == oc ? 21 : 12)
+                                    : ((ic[i] == 4 || oc == 4) ? 16 : (ic[i] == oc ? 21 : 12));
                 int u, v, x, y;
                 uint32_t d;
                 if (TINNER) {
                     const int ut = o ? s1[i] : (i ? 6 : 0), yt = o ? s2[i] : 0;
-                    d = lane_int<MODE>(sc, c1, c2, ut, yt, u, v, x, y);
+                    d = lane_int_z<MODE>(z0, c1, c2, ut, yt, u, v, x, y);
                     c1 = x, c2 = v, s1[i] = u, s2[i] = y;
                 } else {
                     const int xt = o ? s1[i] : 0, vt = o ? s2[i] : (i ? 6 : 0);
                     const int ut = i ? c1 : (o ? 6 : 0), yt = i ? c2 : 0;
-                    d = lane_int<MODE>(sc, xt, vt, ut, yt, u, v, x, y);
+                    d = lane_int_z<MODE>(z0, xt, vt, ut, yt, u, v, x, y);
                     c1 = u, c2 = y, s1[i] = x, s2[i] = v;
                 }
                 if (i < 8) w0 |= d << (4 * i);
@@ -198,8 +233,18 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         dirs[(o * stride) * kDpSmallThreads + tid] = w0;
         if (stride > 1) dirs[(o * stride + 1) * kDpSmallThreads + tid] = w1;
     }
-    // traceback from (tlen-1, qlen-1)
-    CigarPush cp{b.cig_seg + b.coff[g.q] + g.slot, 0, tn + qn, 0};
+    // traceback from (tlen-1, qlen-1); runs written once, last-first
+    uint32_t* out = b.cig_seg + b.coff[g.q] + g.slot;
+    int n = 0;
+    uint32_t run_op = 0xffu, run_len = 0;
+    auto push = [&](uint32_t op, uint32_t len) {
+        if (op == run_op) {
+            run_len += len;
+        } else {
+            if (run_len) out[n++] = run_len << 4 | run_op;
+            run_op = op, run_len = len;
+        }
+    };
     int ti = tn - 1, qj = qn - 1, state = 0;
     while (ti >= 0 && qj >= 0) {
         const int o = TINNER ? qj : ti, i = TINNER ? ti : qj;
@@ -207,18 +252,14 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         if (state == 0) state = nib & 3u;
         else if (!((nib >> (state + 1)) & 1u)) state = 0;
         if (state == 0) state = nib & 3u;
-        if (state == 0) cp.push(0, 1), --ti, --qj;
-        else if (state == 1) cp.push(2, 1), --ti;
-        else cp.push(1, 1), --qj;
+        if (state == 0) push(0, 1), --ti, --qj;
+        else if (state == 1) push(2, 1), --ti;
+        else push(1, 1), --qj;
     }
-    if (ti >= 0) cp.push(2, (uint32_t)(ti + 1));
-    if (qj >= 0) cp.push(1, (uint32_t)(qj + 1));
-    for (int i = 0; i < cp.n / 2; ++i) {
-        const uint32_t a = cp.out[i];
-        cp.out[i] = cp.out[cp.n - 1 - i];
-        cp.out[cp.n - 1 - i] = a;
-    }
-    b.seg[sid].nops = cp.n;
+    if (ti >= 0) push(2, (uint32_t)(ti + 1));
+    if (qj >= 0) push(1, (uint32_t)(qj + 1));
+    if (run_len) out[n++] = run_len << 4 | run_op;
+    b.seg[sid].nops = n;
 }
 
 __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
@@ -235,12 +276,23 @@ __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, 
         const Seg g = b.seg[sid];
         const bool tinner = g.rl <= g.ql;
         const bool left = (g.kind & kSegLeft) != 0;
-        if (tinner) {
-            if (left) small_segment<true, 1>(ix, b, sid, g, dirs, tid);
-            else small_segment<true, 2>(ix, b, sid, g, dirs, tid);
+        const bool fast = ix.center_plain && b.exc_off[g.q] == b.exc_off[g.q + 1];
+        if (fast) {
+            if (tinner) {
+                if (left) small_segment<true, 1, true>(ix, b, sid, g, dirs, tid);
+                else small_segment<true, 2, true>(ix, b, sid, g, dirs, tid);
+            } else {
+                if (left) small_segment<false, 1, true>(ix, b, sid, g, dirs, tid);
+                else small_segment<false, 2, true>(ix, b, sid, g, dirs, tid);
+            }
         } else {
-            if (left) small_segment<false, 1>(ix, b, sid, g, dirs, tid);
-            else small_segment<false, 2>(ix, b, sid, g, dirs, tid);
+            if (tinner) {
+                if (left) small_segment<true, 1, false>(ix, b, sid, g, dirs, tid);
+                else small_segment<true, 2, false>(ix, b, sid, g, dirs, tid);
+            } else {
+                if (left) small_segment<false, 1, false>(ix, b, sid, g, dirs, tid);
+                else small_segment<false, 2, false>(ix, b, sid, g, dirs, tid);
+            }
         }
         cell_sum += (unsigned long long)(g.rl * g.ql);
     }
@@ -643,6 +695,7 @@ __device__ __forceinline__ void wave_segment(const IndexDev& ix, const BatchDev&
 #pragma unroll
     for (int p = 0; p < P; ++p) {
         const int c = v * P + p;
+        s1[p] = s2[p] = r1[p] = r2[p] = r5[p] = 0;
         int ic = 0;
         if (active && c < inner) {
             if (TINNER) ic = tc[c];

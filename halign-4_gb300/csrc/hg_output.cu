@@ -1,6 +1,7 @@
 // hg_output.cu - K7 stitch, K8 row projection, K9 per-column counters.
 //
-// K7 concatenates the segment CIGARs of a query in segment order with
+// K7 concatenates the segment CIGARs of a query in segment order (the small
+// DP tier leaves its ops last-first, as its traceback produces them) with
 // cigar::appendCigar semantics (src/align/cigar.cpp:302-329: zero lengths
 // dropped, a run continuing the previous op merges into it, merged lengths
 // above 2^28-1 are an error).  The op stream of all segments is flattened
@@ -91,7 +92,9 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
                         if (rel == 0) op = 1, len = s_ql[wib][lo];
                         else op = 2, len = s_rl[wib][lo];
                     } else {
-                        const uint32_t c = src[s_slot[wib][lo] + rel];
+                        // the small DP tier stores its ops last-first
+                        const uint32_t at = kind == kSegDpSmall ? (uint32_t)s_nops[wib][lo] - 1u - rel : rel;
+                        const uint32_t c = src[s_slot[wib][lo] + at];
                         op = c & 0xfu, len = c >> 4;
                     }
                 }

@@ -118,7 +118,7 @@ struct hg_index {
     int L = 0;
     uint64_t occ_thr = 0;
     int64_t n_hits = 0;
-    DevBuf<uint8_t> center;
+    DevBuf<uint8_t> center, center2;
     DevBuf<uint64_t> tab_key;
     DevBuf<uint32_t> tab_val, ent_start, ent_count, cpos, cspan;
     DevBuf<uint8_t> ent_over;
@@ -481,6 +481,13 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     // DP center (consensus of the single record) in DNA5 codes
     std::vector<uint8_t> cdp((size_t)len);
     for (int64_t i = 0; i < len; ++i) cdp[i] = hg::dna5_of(consensus_letter((uint8_t)center[i]));
+    // 2-bit copy for the small DP tier's register loads (64 bytes of slack: it reads 24 bytes at a time)
+    std::vector<uint8_t> c2((size_t)(len + 3) / 4 + 64, 0);
+    int cplain = 1;
+    for (int64_t i = 0; i < len; ++i) {
+        if (cdp[i] > 3) cplain = 0;
+        c2[(size_t)i >> 2] |= (uint8_t)((cdp[i] & 3u) << (2 * (i & 3)));
+    }
     // log2f table for the chain penalty (arguments 2 .. bw+1)
     const int nlog = std::max(ix->prm.bw + 2, 513);
     std::vector<float> lg((size_t)nlog);
@@ -492,7 +499,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
                          : cudaMemcpy(buf.p, v.data(), sizeof(v[0]) * v.size(), cudaMemcpyHostToDevice);
     };
     cudaError_t e = cudaSuccess;
-    if ((e = up(ix->center, cdp)) || (e = up(ix->tab_key, tkey)) || (e = up(ix->tab_val, tval)) ||
+    if ((e = up(ix->center, cdp)) || (e = up(ix->center2, c2)) || (e = up(ix->tab_key, tkey)) || (e = up(ix->tab_val, tval)) ||
         (e = up(ix->ent_start, est)) || (e = up(ix->ent_count, ecnt)) || (e = up(ix->ent_over, over)) ||
         (e = up(ix->cpos, cpos)) || (e = up(ix->cspan, cspan)) || (e = up(ix->log2tab, lg))) {
         delete ix;
@@ -500,7 +507,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     }
     hg::IndexDev& d = ix->dev;
     d.L = (int)len, d.k = k, d.w = w, d.non_canonical = 1;
-    d.center = ix->center.p;
+    d.center = ix->center.p, d.center2 = ix->center2.p, d.center_plain = cplain;
     d.tab_key = ix->tab_key.p, d.tab_val = ix->tab_val.p, d.tab_mask = tsize - 1;
     d.n_ent = (uint32_t)ekey.size();
     d.ent_start = ix->ent_start.p, d.ent_count = ix->ent_count.p, d.ent_over = ix->ent_over.p;
@@ -519,7 +526,7 @@ extern "C" void hg_index_destroy(hg_index_t* ix)
     if (!ix) return;
     if (ix->single) hg_ctx_destroy(ix->single);
     ix->center.free(), ix->tab_key.free(), ix->tab_val.free(), ix->ent_start.free(), ix->ent_count.free();
-    ix->ent_over.free(), ix->cpos.free(), ix->cspan.free(), ix->log2tab.free();
+    ix->ent_over.free(), ix->cpos.free(), ix->cspan.free(), ix->log2tab.free(), ix->center2.free();
     delete ix;
 }
 
@@ -537,13 +544,14 @@ extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t*
 namespace {
 
 constexpr int kControlWords = 16;
-// control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide
+// control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide |
+// queues2[4]
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
 constexpr int kWaveBlocksPerSm = 4;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
-// kernel launches per sub-batch: seed 2, anchor, chain, dp_small 3, dp_wave 2, dp_wide,
+// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 3, dp_wave 2, dp_wide,
 // dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
-constexpr int kLaunchesBatch = 16;
-constexpr int kLaunchesPlain = 15;
+constexpr int kLaunchesBatch = 17;
+constexpr int kLaunchesPlain = 16;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
@@ -722,6 +730,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.acap = c->acap;
     unsigned long long* ctl = c->control.p;
     b.queues = reinterpret_cast<unsigned int*>(ctl);  // 8 x uint32 in words 0..3
+    b.queues2 = reinterpret_cast<unsigned int*>(ctl + 12);  // 4 x uint32 in words 12..13
     b.a_cursor = ctl + 4, b.s_cursor = ctl + 5, b.dp_cursor = ctl + 6;
     b.n_small = reinterpret_cast<unsigned int*>(ctl + 7);
     b.n_large = reinterpret_cast<unsigned int*>(ctl + 8);

@@ -45,6 +45,149 @@ struct SeedOut {
     uint64_t* hy;    // mode 1: y = strand << 63 | rid << 32 | pos
 };
 
+// Fast path for a query without exception bytes at window 10 and k <= 24
+// (the align-to-center defaults).  Thread t of a tile owns k-mer starts
+// P0 = tile + 8t .. P0+7:
+//   * the 2-bit forward codes come from one 64-bit packed word: bit-reversed
+//     and pair-swapped it holds base P0 in its top two bits, so the k-mer at
+//     P0+i is (X << 2i) >> (64 - 2k);
+//   * window minimum in registers over 64-bit keys (hash << 8 | 254 - idx):
+//     key order is hash order with ties to the later position, so "latest
+//     equal hash wins" is a plain minimum; pairs -> quads -> octets, and a
+//     window of 10 is an octet plus a pair (the 16 hashes before P0 come
+//     from shared memory);
+//   * the deque-overflow test (10 strict increases ending at a position) is
+//     a run of ten ones in the increase bitmask.
+constexpr int kFastWin = 10;
+constexpr int kFastMaxK = 24;
+
+__device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+
+__device__ __forceinline__ bool seed_fast_eligible(const IndexDev& ix, int len, int64_t e0, int64_t e1)
+{
+    return e0 == e1 && ix.non_canonical && ix.w == kFastWin && ix.k > 0 && ix.k <= kFastMaxK &&
+           len - ix.k + 1 >= kFastWin;
+}
+
+constexpr int kSeedFastWarps = 8;
+constexpr int kSeedFastChunk = 32 * kSeedPer;  // k-mer starts per warp step
+
+// One warp per query (no block barriers); each warp's shared buffer holds
+// the hashes of its current chunk after the 16 that precede it.
+__global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(IndexDev ix, BatchDev b)
+{
+    __shared__ uint64_t hbuf[kSeedFastWarps][16 + kSeedFastChunk];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    uint64_t* hs = hbuf[threadIdx.x >> 5];
+    const int k = ix.k;
+    const int lsh = 64 - 2 * k;
+    for (;;) {
+        int qi = 0;
+        if (lane == 0) qi = (int)atomicAdd(&b.queues2[0], 1u);
+        qi = __shfl_sync(FULL, qi, 0);
+        if (qi >= b.n) break;
+        const int q = b.order ? b.order[qi] : qi;
+        const int len = b.qlen[q];
+        if (!seed_fast_eligible(ix, len, b.exc_off[q], b.exc_off[q + 1])) continue;
+        const uint8_t* pk = b.packed + b.poff[q];
+        const int nk = len - k + 1;
+        const int64_t hb = b.hoff[q];
+        if (lane < 16) hs[lane] = kNoHash;  // positions before 0
+        int total_hits = 0, total_matched = 0;
+        bool ovf_any = false;
+        for (int t0 = 0; t0 < nk; t0 += kSeedFastChunk) {
+            const int P0 = t0 + lane * kSeedPer;
+            uint64_t h[kSeedPer];
+            if (P0 < nk) {
+                const uint32_t wb = ((uint32_t)P0 >> 2) & ~7u;
+                const uint64_t* w = reinterpret_cast<const uint64_t*>(pk + wb);
+                const uint64_t w0 = w[0], w1 = w[1];
+                const uint32_t sh = 2u * ((uint32_t)P0 - wb * 4u);
+                const uint64_t lo = sh ? (w0 >> sh) | (w1 << (64u - sh)) : w0;
+                uint64_t x = __brevll(lo);
+                x = ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
+#pragma unroll
+                for (int i = 0; i < kSeedPer; ++i)
+                    h[i] = P0 + i < nk ? splitmix64((x << (2 * i)) >> lsh) >> 8 : kNoHash;
+            } else {
+#pragma unroll
+                for (int i = 0; i < kSeedPer; ++i) h[i] = kNoHash;
+            }
+#pragma unroll
+            for (int i = 0; i < kSeedPer; ++i) hs[16 + lane * kSeedPer + i] = h[i];
+            __syncwarp();
+            uint64_t A[24];
+#pragma unroll
+            for (int i = 0; i < 16; ++i) A[i] = hs[lane * kSeedPer + i];
+#pragma unroll
+            for (int i = 0; i < kSeedPer; ++i) A[16 + i] = h[i];
+            __syncwarp();
+            if (lane < 16) hs[lane] = hs[kSeedFastChunk + lane];  // carry the last 16 hashes
+            __syncwarp();
+            // window minimum over keys
+            uint64_t key[24], Pm[24], Qm[24], Om[24];
+#pragma unroll
+            for (int i = 0; i < 24; ++i) key[i] = A[i] == kNoHash ? ~0ull : (A[i] << 8) | (uint64_t)(254 - i);
+#pragma unroll
+            for (int i = 7; i < 24; ++i) Pm[i] = umin64(key[i - 1], key[i]);
+#pragma unroll
+            for (int i = 9; i < 24; ++i) Qm[i] = umin64(Pm[i], Pm[i - 2]);
+#pragma unroll
+            for (int i = 13; i < 24; ++i) Om[i] = umin64(Qm[i], Qm[i - 4]);
+            int mp[kSeedPer + 1];  // minimizer positions of P0-1 .. P0+7
+#pragma unroll
+            for (int e = 15; e < 24; ++e) {
+                const uint64_t m = umin64(Om[e], Pm[e - 8]);
+                mp[e - 15] = P0 - 16 + (254 - (int)(m & 0xffu));
+                Om[e] = m;
+            }
+            // deque overflow: 10 strict increases ending at P0 + i (P0 + i - 10 >= 0, P0 + i < nk)
+            uint32_t inc = 0;
+#pragma unroll
+            for (int i = 1; i < 24; ++i)
+                inc |= (A[i - 1] != kNoHash && A[i] != kNoHash && A[i - 1] < A[i]) ? (1u << i) : 0u;
+            const uint32_t r2 = inc & (inc >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4), r10 = r8 & (r2 >> 8);
+            const uint32_t ovf = (r10 >> 7) & 0xffu;  // run of ten starting at bit 7+i ends at bit 16+i
+            // emission and index lookups
+            int n_emit = 0, n_match = 0;
+            uint32_t ent[kSeedPer];
+            uint32_t emask = 0;
+#pragma unroll
+            for (int i = 0; i < kSeedPer; ++i) {
+                const int p = P0 + i;
+                ent[i] = kEmptyKey;
+                if (((ovf >> i) & 1u) && p - kFastWin >= 0 && p < nk) ovf_any = true;
+                if (p >= nk || p < kFastWin - 1) continue;
+                if (p > kFastWin - 1 && mp[i + 1] == mp[i]) continue;
+                emask |= 1u << i;
+                ++n_emit;
+                ent[i] = index_find(ix, Om[16 + i] >> 8);
+                if (ent[i] != kEmptyKey) ++n_match;
+            }
+            const int incl = warp_incl_sum(n_match);
+            int o = total_matched + incl - n_match;
+#pragma unroll
+            for (int i = 0; i < kSeedPer; ++i) {
+                if ((emask >> i & 1u) && ent[i] != kEmptyKey) {
+                    b.hit_pos[hb + o] = (uint32_t)mp[i + 1];
+                    b.hit_ent[hb + o] = ent[i];
+                    ++o;
+                }
+            }
+            total_matched += __shfl_sync(FULL, incl, 31);
+            total_hits += __reduce_add_sync(FULL, (unsigned)n_emit);
+        }
+        const bool ovf_q = __any_sync(FULL, ovf_any);
+        if (lane == 0) {
+            b.n_hits[q] = total_hits;
+            b.n_matched[q] = total_matched;
+            if (ovf_q) b.exact_list[atomicAdd(b.n_exact, 1u)] = (uint32_t)q;
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDev b, SeedOut so)
 {
     __shared__ __align__(16) uint8_t codes[kCodeBuf];
@@ -70,6 +213,7 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDe
         const int len = b.qlen[q];
         const uint8_t* pk = b.packed + b.poff[q];
         const int64_t e0 = b.exc_off[q], e1 = b.exc_off[q + 1];
+        if (so.mode == 0 && seed_fast_eligible(ix, len, e0, e1)) continue;  // seed_fast_kernel's query
         int total_hits = 0, total_matched = 0;
         if (len >= k && k > 0 && k <= kMaxK && ix.w > 0 && ix.w <= kMaxWin) {
             const int nk = len - k + 1;
@@ -368,6 +512,10 @@ extern "C" cudaError_t hg_launch_seed(const hg::IndexDev* ix, const hg::BatchDev
     hg::seed_kernel<<<grid, hg::kSeedThreads, 0, st>>>(*ix, *b, so);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
+    if (mode == 0) {
+        hg::seed_fast_kernel<<<grid, hg::kSeedFastWarps * 32, 0, st>>>(*ix, *b);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
     hg::seed_exact_kernel<<<hg::kExactBlocks, hg::kExactThreads, 0, st>>>(*ix, *b, so);
     return cudaGetLastError();
 }

@@ -235,6 +235,31 @@ def test_wavefront_tiers_vs_oracle(gpu, oracle, pkg):
             assert res.rows[i].tobytes() == oracle.del_query(qq, want), i
 
 
+def test_batch_window_overflow_vs_oracle(gpu, oracle, pkg):
+    """Queries holding 10+ consecutive strictly increasing k-mer hashes at the
+    default k=15, w=10: the reference's window deque overflows there, the
+    tile pass must detect it and the sequential replay must reproduce the
+    reference's minimizers (checked through the whole alignment)."""
+    from tests.test_oracle_pin import increasing_run
+    rng = np.random.default_rng(44)
+    center = pkg.synth.random_center(6000, 8)
+    cmx, cmy = oracle.extract_minimizer(center)
+    cases = []
+    for it in range(6):
+        run = increasing_run(rng, 15, 10 + it % 3)
+        assert run is not None
+        a = int(rng.integers(0, 4000))
+        cases.append(center[a:a + 800] + run.encode() + center[a + 800:a + 1800])
+    cases.append(center[1000:5000])
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=16, max_bases=100000)
+    res = ctx.align(gpu.pack(seqs, offs), rows=False, check=False)
+    for i, q in enumerate(cases):
+        assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
+
+
 def test_global_align_ksw2_vs_oracle(gpu, oracle):
     rng = np.random.default_rng(2)
     for it in range(30):
