@@ -29,6 +29,7 @@ struct IndexDev {
     // chain parameters (anchor::ChainParams, include/anchor.h:116-127)
     int max_dist_x, max_dist_y, bw, max_skip, max_iter, min_cnt, min_score;
     float gap_pen, skip_pen;
+    int dg_nopen;              // with dd == 0 the chain penalty is 0 for every dg <= dg_nopen (>= k)
     const float* log2tab;      // log2f(i) for i in [0, n_log2)
     int n_log2;
 };
@@ -116,6 +117,21 @@ __host__ __device__ __forceinline__ uint32_t wave_key(uint32_t rl, uint32_t ql, 
     return (15u - cls) << 4 | (3u - pidx) << 2 | (rl <= ql ? 1u : 0u) << 1 | (left ? 0u : 1u);
 }
 
+// Small-tier work record, written in shape-sorted order by the sort pass so
+// the DP reads it sequentially: absolute base position of the segment's
+// query start in the packed stream, absolute op-word offset of its CIGAR
+// slot, center start, shape and flags.
+struct SmallRec {
+    uint64_t qpos;      // poff[q] * 4 + qs
+    uint32_t sid;       // segment id (the DP writes seg[sid].nops)
+    uint32_t out;       // coff[q] + slot
+    uint32_t rs;        // center start
+    uint32_t shape;     // rl | ql << 8 | left << 16 | fast << 17 (fast: no query exception, plain center)
+    uint32_t q;         // query index (exception lookups off the fast path)
+    uint32_t pad;
+};
+constexpr uint32_t kRecLeft = 1u << 16, kRecFast = 1u << 17;
+
 struct BatchDev {
     int n;                       // queries in the batch
     const uint8_t* packed;       // 2-bit packed bases
@@ -156,7 +172,8 @@ struct BatchDev {
     int32_t* n_chain;
     uint32_t* work_small;        // global segment ids per DP tier
     uint32_t* work_large;
-    uint32_t* work_sorted;       // small tier sorted by shape_key
+    uint32_t* work_sorted;       // small tier sorted by shape_key (unused when work_rec is set)
+    SmallRec* work_rec;          // small tier records in shape-sorted order
     uint32_t* work_key;          // shape_key of each work_small entry (written with it)
     uint32_t* shape_hist;        // kShapeBins counters, then kShapeBins cursors
     unsigned int* n_small;

@@ -43,7 +43,9 @@ __device__ __forceinline__ int32_t chain_score(const IndexDev& ix, const float* 
     const bool ok = dq > 0 && dq <= ix.max_dist_x && dr > 0 && dr <= ix.max_dist_y && dd <= ix.bw;
     const int32_t dg = dr < dq ? dr : dq;
     int32_t sc = span_j < dg ? span_j : dg;
-    if (ok && (dd > 0 || dg > span_j)) {
+    // the reference subtracts when dd > 0 || dg > span_j; with dd == 0 the
+    // penalty is 0 up to dg_nopen (>= span_j), so those lanes skip the float path
+    if (ok && (dd > 0 || dg > ix.dg_nopen)) {
         const float lin = __fadd_rn(__fmul_rn(ix.gap_pen, (float)dd), __fmul_rn(ix.skip_pen, (float)dg));
         const float lg = dd >= 1 ? lg2[dd + 1] : 0.0f;
         sc -= __float2int_rz(__fadd_rn(lin, __fmul_rn(0.5f, lg)));
@@ -90,8 +92,18 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 nx_aq = i + lane < A ? aq[i + lane] : 0u;
             }
             const uint32_t ri = __shfl_sync(FULL, nx_ar, i & 31), qv = __shfl_sync(FULL, nx_aq, i & 31);
-            while (st < i && (int32_t)(ri - ar[st]) > ix.max_dist_x) ++st;
-            const int it0 = (i - st > ix.max_iter) ? i - ix.max_iter : st;
+            if ((i & 31) == 0 && i > 0) {
+                // the window holds anchors i-1 .. i-32: write their f and p back
+                f[i - 1 - lane] = w_f;
+                p[i - 1 - lane] = w_p;
+            }
+            // the window start st is brought up to date only when the window's
+            // last candidate may be out of range; a stale (smaller) st changes
+            // nothing in the first chunk, and later chunks refresh it first
+            const uint32_t ar31 = __shfl_sync(FULL, w_ar, 31);
+            if (i <= 32 || (int32_t)(ri - ar31) > ix.max_dist_x)
+                while (st < i && (int32_t)(ri - ar[st]) > ix.max_dist_x) ++st;
+            int it0 = (i - st > ix.max_iter) ? i - ix.max_iter : st;
             int32_t max_f = span;
             int max_j = -1;
             int n_skip = 0;
@@ -152,6 +164,8 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             }
             // later chunks: marks through t[], warp scans
             if (!done) {
+                while (st < i && (int32_t)(ri - ar[st]) > ix.max_dist_x) ++st;
+                it0 = (i - st > ix.max_iter) ? i - ix.max_iter : st;
                 __syncwarp();
                 for (int jb = i - 33; jb >= it0; jb -= 32) {
                     const int j = jb - lane;
@@ -186,7 +200,6 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                     __syncwarp();
                 }
             }
-            if (lane == 0) f[i] = max_f, p[i] = max_j;
             if (max_f > best_f) best_f = max_f, best = i;
             // shift the window: lane l takes lane l-1's anchor, lane 0 anchor i
             w_ar = __shfl_up_sync(FULL, w_ar, 1);
@@ -195,6 +208,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             w_p = __shfl_up_sync(FULL, w_p, 1);
             if (lane == 0) w_ar = ri, w_aq = qv, w_f = max_f, w_p = max_j;
         }
+        if (A > 0 && A - 1 - lane >= 0) f[A - 1 - lane] = w_f, p[A - 1 - lane] = w_p;  // the last window
         __syncwarp();
         // backtrack: chain (reversed) into t[], read p[] 32 entries at a time
         int c = 0;

@@ -147,12 +147,12 @@ __device__ __forceinline__ uint32_t lane_int_z(int z0, int xt1, int vt1, int ut,
 // 64 bases of 2-bit codes from base `pos` of a packed stream (base i at bits
 // 2(i&3) of byte i>>2): base pos+m at bits 2m of lo (m < 32) / 2(m-32) of hi.
 // The stream is 8-byte aligned and readable 24 bytes past byte (pos/4 & ~7).
-__device__ __forceinline__ void load_bases64(const uint8_t* pk, uint32_t pos, uint64_t& lo, uint64_t& hi)
+__device__ __forceinline__ void load_bases64(const uint8_t* pk, uint64_t pos, uint64_t& lo, uint64_t& hi)
 {
-    const uint32_t wb = (pos >> 2) & ~7u;
+    const uint64_t wb = (pos >> 2) & ~(uint64_t)7;
     const uint64_t* w = reinterpret_cast<const uint64_t*>(pk + wb);
     const uint64_t w0 = w[0], w1 = w[1], w2 = w[2];
-    const uint32_t sh = 2u * (pos - wb * 4u);  // 0 .. 62
+    const uint32_t sh = 2u * (uint32_t)(pos - wb * 4u);  // 0 .. 62
     lo = sh ? (w0 >> sh) | (w1 << (64u - sh)) : w0;
     hi = sh ? (w1 >> sh) | (w2 << (64u - sh)) : w1;
 }
@@ -164,22 +164,24 @@ __device__ __forceinline__ void load_bases64(const uint8_t* pk, uint32_t pos, ui
 // come from 2-bit packed words held in registers.  The traceback writes each
 // op run once, last-first (the stitch reads small-tier segments backwards).
 template <bool TINNER, int MODE, bool FAST>
-__device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev& b, uint32_t sid, const Seg& g,
+__device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev& b, const SmallRec& r,
                                               uint32_t* dirs, int tid)
 {
-    const int qn = (int)g.ql, tn = (int)g.rl;
+    const int qn = (int)((r.shape >> 8) & 0xffu), tn = (int)(r.shape & 0xffu);
     const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
     const int stride = (inner + 7) >> 3;
-    const uint8_t* pk = b.packed + b.poff[g.q];
-    const int64_t e0 = FAST ? 0 : b.exc_off[g.q], e1 = FAST ? 0 : b.exc_off[g.q + 1];
+    // off the fast path: query-relative positions, exception runs
+    const uint32_t qs = FAST ? 0u : (uint32_t)(r.qpos - (uint64_t)b.poff[r.q] * 4u);
+    const uint8_t* pk = FAST ? b.packed : b.packed + b.poff[r.q];
+    const int64_t e0 = FAST ? 0 : b.exc_off[r.q], e1 = FAST ? 0 : b.exc_off[r.q + 1];
     const bool plain_q = e0 == e1;
-    const uint8_t* tc = ix.center + g.rs;
+    const uint8_t* tc = ix.center + r.rs;
     int ic[kSmallMaxInner], s1[kSmallMaxInner], s2[kSmallMaxInner];
     uint64_t olo = 0, ohi = 0;
     if (FAST) {
         uint64_t qlo, qhi, tlo, thi;
-        load_bases64(pk, g.qs, qlo, qhi);
-        load_bases64(ix.center2, g.rs, tlo, thi);
+        load_bases64(b.packed, r.qpos, qlo, qhi);
+        load_bases64(ix.center2, r.rs, tlo, thi);
         const uint64_t ilo = TINNER ? tlo : qlo;
         olo = TINNER ? qlo : tlo;
         ohi = TINNER ? qhi : thi;
@@ -191,7 +193,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
             ic[i] = 0;
             if (i < inner) {
                 if (TINNER) ic[i] = tc[i];
-                else ic[i] = plain_q ? (int)packed_code(pk, g.qs + i) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + i);
+                else ic[i] = plain_q ? (int)packed_code(pk, qs + i) : (int)query_dna5(pk, b.exc, e0, e1, qs + i);
             }
         }
     }
@@ -202,7 +204,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         if (FAST) {
             oc = (int)(((o < 32 ? olo : ohi) >> (2 * (o & 31))) & 3u);
         } else {
-            if (TINNER) oc = plain_q ? (int)packed_code(pk, g.qs + o) : (int)query_dna5(pk, b.exc, e0, e1, g.qs + o);
+            if (TINNER) oc = plain_q ? (int)packed_code(pk, qs + o) : (int)query_dna5(pk, b.exc, e0, e1, qs + o);
             else oc = tc[o];
         }
         // TINNER: carried x, v along the row, s1/s2 = u, y of the previous row.
@@ -234,7 +236,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         if (stride > 1) dirs[(o * stride + 1) * kDpSmallThreads + tid] = w1;
     }
     // traceback from (tlen-1, qlen-1); runs written once, last-first
-    uint32_t* out = b.cig_seg + b.coff[g.q] + g.slot;
+    uint32_t* out = b.cig_seg + r.out;
     int n = 0;
     uint32_t run_op = 0xffu, run_len = 0;
     auto push = [&](uint32_t op, uint32_t len) {
@@ -259,42 +261,40 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     if (ti >= 0) push(2, (uint32_t)(ti + 1));
     if (qj >= 0) push(1, (uint32_t)(qj + 1));
     if (run_len) out[n++] = run_len << 4 | run_op;
-    b.seg[sid].nops = n;
+    b.seg[r.sid].nops = n;
 }
 
 __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
 {
     __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
     const int tid = threadIdx.x;
-    const unsigned total = *b.n_small;
-    const uint32_t* list = b.work_sorted ? b.work_sorted : b.work_small;
+    const unsigned total = min(*b.n_small, (unsigned)b.wcap);
     unsigned long long cell_sum = 0;
     const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
     for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
         if (w >= total) continue;
-        const uint32_t sid = list[w];
-        const Seg g = b.seg[sid];
-        const bool tinner = g.rl <= g.ql;
-        const bool left = (g.kind & kSegLeft) != 0;
-        const bool fast = ix.center_plain && b.exc_off[g.q] == b.exc_off[g.q + 1];
-        if (fast) {
+        const SmallRec r = b.work_rec[w];
+        const uint32_t rl = r.shape & 0xffu, ql = (r.shape >> 8) & 0xffu;
+        const bool tinner = rl <= ql;
+        const bool left = (r.shape & kRecLeft) != 0;
+        if (r.shape & kRecFast) {
             if (tinner) {
-                if (left) small_segment<true, 1, true>(ix, b, sid, g, dirs, tid);
-                else small_segment<true, 2, true>(ix, b, sid, g, dirs, tid);
+                if (left) small_segment<true, 1, true>(ix, b, r, dirs, tid);
+                else small_segment<true, 2, true>(ix, b, r, dirs, tid);
             } else {
-                if (left) small_segment<false, 1, true>(ix, b, sid, g, dirs, tid);
-                else small_segment<false, 2, true>(ix, b, sid, g, dirs, tid);
+                if (left) small_segment<false, 1, true>(ix, b, r, dirs, tid);
+                else small_segment<false, 2, true>(ix, b, r, dirs, tid);
             }
         } else {
             if (tinner) {
-                if (left) small_segment<true, 1, false>(ix, b, sid, g, dirs, tid);
-                else small_segment<true, 2, false>(ix, b, sid, g, dirs, tid);
+                if (left) small_segment<true, 1, false>(ix, b, r, dirs, tid);
+                else small_segment<true, 2, false>(ix, b, r, dirs, tid);
             } else {
-                if (left) small_segment<false, 1, false>(ix, b, sid, g, dirs, tid);
-                else small_segment<false, 2, false>(ix, b, sid, g, dirs, tid);
+                if (left) small_segment<false, 1, false>(ix, b, r, dirs, tid);
+                else small_segment<false, 2, false>(ix, b, r, dirs, tid);
             }
         }
-        cell_sum += (unsigned long long)(g.rl * g.ql);
+        cell_sum += (unsigned long long)(rl * ql);
     }
     for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
     if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
@@ -325,22 +325,51 @@ __global__ void shape_scan_kernel(BatchDev b)
     }
 }
 
-__global__ void shape_scatter_kernel(BatchDev b)
+// Scatter into shape order.  CTA c takes a contiguous chunk of the chain-
+// ordered list, counts its keys in shared memory, reserves one range per
+// non-empty key with a single global atomic, then places its items; each
+// item becomes a SmallRec (the segment record is read here, in chain order,
+// so mostly coalesced).
+constexpr int kScatterThreads = 512;
+
+__global__ void __launch_bounds__(kScatterThreads) shape_scatter_kernel(IndexDev ix, BatchDev b)
 {
-    const unsigned total = *b.n_small;
-    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < ((total + 31u) & ~31u);
-         w += gridDim.x * blockDim.x) {
-        const bool act = w < total;
-        const uint32_t sid = act ? b.work_small[w] : 0u;
-        const uint32_t key = act ? b.work_key[w] : 0xffffffffu;
-        const unsigned peers = __match_any_sync(0xffffffffu, key);
-        const int leader = __ffs(peers) - 1;
-        uint32_t base = 0;
-        if (act && (int)(threadIdx.x & 31) == leader) base = atomicAdd(&b.shape_hist[kShapeBins + key], __popc(peers));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (act) b.work_sorted[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = sid;
+    extern __shared__ uint32_t sh[];  // [kShapeBins] counts, then [kShapeBins] reserved bases
+    uint32_t* cnt = sh;
+    uint32_t* base = sh + kShapeBins;
+    const unsigned total = min(*b.n_small, (unsigned)b.wcap);
+    const unsigned chunk = (total + gridDim.x - 1) / gridDim.x;
+    const unsigned w0 = blockIdx.x * chunk, w1 = min(w0 + chunk, total);
+    if (w0 >= w1) return;
+    for (int i = threadIdx.x; i < kShapeBins; i += kScatterThreads) cnt[i] = 0;
+    __syncthreads();
+    for (unsigned w = w0 + threadIdx.x; w < w1; w += kScatterThreads) atomicAdd(&cnt[b.work_key[w]], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kShapeBins; i += kScatterThreads) {
+        const uint32_t c = cnt[i];
+        base[i] = c ? atomicAdd(&b.shape_hist[kShapeBins + i], c) : 0u;
+        cnt[i] = 0;
+    }
+    __syncthreads();
+    for (unsigned w = w0 + threadIdx.x; w < w1; w += kScatterThreads) {
+        const uint32_t key = b.work_key[w];
+        const uint32_t sid = b.work_small[w];
+        const uint32_t pos = base[key] + atomicAdd(&cnt[key], 1u);
+        const Seg g = b.seg[sid];
+        SmallRec r;
+        r.qpos = (uint64_t)b.poff[g.q] * 4u + g.qs;
+        r.sid = sid;
+        r.out = (uint32_t)(b.coff[g.q] + g.slot);
+        r.rs = g.rs;
+        const bool fast = ix.center_plain && b.exc_off[g.q] == b.exc_off[g.q + 1];
+        r.shape = g.rl | g.ql << 8 | ((g.kind & kSegLeft) ? kRecLeft : 0u) | (fast ? kRecFast : 0u);
+        r.q = g.q;
+        r.pad = 0;
+        b.work_rec[pos] = r;
     }
 }
+
+constexpr size_t kScatterSmem = 2 * sizeof(uint32_t) * (size_t)kShapeBins;
 
 // ---------------------------------------------------------------- large tier
 
@@ -1161,10 +1190,8 @@ __global__ void ksw_single_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, in
 
 extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
-    if (b->work_sorted) {
-        hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
-        hg::shape_scatter_kernel<<<grid, 256, 0, st>>>(*b);
-    }
+    hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
+    hg::shape_scatter_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kScatterThreads, hg::kScatterSmem, st>>>(*ix, *b);
     hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);
     return cudaGetLastError();
 }
@@ -1195,8 +1222,11 @@ extern "C" cudaError_t hg_launch_dp_wide(const hg::IndexDev* ix, const hg::Batch
 
 extern "C" cudaError_t hg_prepare_dp_kernels()
 {
-    return cudaFuncSetAttribute(hg::dp_wave_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)hg::kWaveCtaSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute(hg::dp_wave_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)hg::kWaveCtaSmemBytes);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(hg::shape_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)hg::kScatterSmem);
 }
 
 extern "C" size_t hg_ksw_scratch_bytes(int qlen, int tlen, int w, int flag)

@@ -169,6 +169,7 @@ struct hg_ctx {
     DevBuf<int32_t> s_n, n_chain;
     DevBuf<uint32_t> work_small, work_large, work_sorted, work_key, shape_hist;
     DevBuf<uint32_t> work_wave, work_wave_key, work_wave_sorted, wave_hist, work_wide;
+    DevBuf<hg::SmallRec> work_rec;
     int64_t dp_cap = 0;
     DevBuf<uint8_t> dp_arena;
     int64_t dp_slot_bytes = 0;
@@ -517,6 +518,21 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     d.max_skip = ix->prm.max_skip, d.max_iter = ix->prm.max_iter, d.min_cnt = ix->prm.min_cnt;
     d.min_score = ix->prm.min_score, d.gap_pen = ix->prm.gap_penalty, d.skip_pen = ix->prm.skip_penalty;
     d.log2tab = ix->log2tab.p, d.n_log2 = nlog;
+    // largest dg whose penalty (dd = 0) truncates to 0, evaluated as the kernel
+    // does: separate round-to-nearest products and sums
+    {
+        int z = k;
+        for (int dg = k + 1; dg <= (1 << 20); ++dg) {
+            volatile float a = ix->prm.gap_penalty * 0.0f;
+            volatile float c = ix->prm.skip_penalty * (float)dg;
+            volatile float lin = a + c;
+            volatile float h = 0.5f * 0.0f;
+            volatile float t = lin + h;
+            if ((int)t != 0) break;
+            z = dg;
+        }
+        d.dg_nopen = z;
+    }
     *out = ix;
     return HG_OK;
 }
@@ -619,6 +635,10 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     c->dp_slot_bytes = (int64_t)256 << 10;
     c->dp_nslots = c->sms * kLargeBlocksPerSm * 4 + c->sms;  // warp slots, then one per CTA-tier CTA
     c->cig_cap = max_bases + max_queries * (L + 4);
+    if (c->cig_cap >= ((int64_t)1 << 32)) {  // SmallRec holds 32-bit op offsets
+        delete c;
+        return fail(HG_ERR_ARG, "hg_ctx_create: max_bases + max_queries * (center length + 4) must stay below 2^32");
+    }
     const int64_t n_ent = ix->dev.n_ent;
     const int grid_anchor = c->sms * 3;
     cudaError_t e = cudaSuccess;
@@ -646,7 +666,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->shape_hist.alloc(2 * (size_t)hg::kShapeBins)) ||
         (e = c->work_wave.alloc(c->scap)) || (e = c->work_wave_key.alloc(c->scap)) ||
         (e = c->work_wave_sorted.alloc(c->scap)) || (e = c->wave_hist.alloc(2 * (size_t)hg::kWaveBins)) ||
-        (e = c->work_wide.alloc(c->scap)) ||
+        (e = c->work_wide.alloc(c->scap)) || (e = c->work_rec.alloc(c->scap)) ||
         (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) || (e = c->run_flags.alloc(1)) ||
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
@@ -741,7 +761,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
     b.work_sorted = c->work_sorted.p, b.work_key = c->work_key.p, b.shape_hist = c->shape_hist.p;
     b.work_wave = c->work_wave.p, b.work_wave_key = c->work_wave_key.p, b.work_wave_sorted = c->work_wave_sorted.p;
-    b.wave_hist = c->wave_hist.p, b.work_wide = c->work_wide.p;
+    b.wave_hist = c->wave_hist.p, b.work_wide = c->work_wide.p, b.work_rec = c->work_rec.p;
     b.n_wave = reinterpret_cast<unsigned int*>(ctl + 10);
     b.n_wide = reinterpret_cast<unsigned int*>(ctl + 11);
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
