@@ -128,13 +128,14 @@ class Packed:
 def pack(seqs: bytes, offsets) -> Packed:
     """Pack concatenated ASCII queries (``offsets``: int64[n+1])."""
     L = lib()
-    seqs = _bytes(seqs)
+    if not isinstance(seqs, (bytes, bytearray, memoryview)):
+        seqs = _bytes(seqs)
     offsets = np.ascontiguousarray(offsets, np.int64)
     n = len(offsets) - 1
     pb, ne = C.c_int64(0), C.c_int64(0)
-    buf = np.frombuffer(seqs, np.uint8) if seqs else np.zeros(1, np.uint8)
+    buf = np.frombuffer(seqs, np.uint8) if len(seqs) else np.zeros(1, np.uint8)  # no copy
     _check(L.hg_pack(_p(buf), _p(offsets), n, None, 0, None, None, 0, None, C.byref(pb), C.byref(ne)))
-    packed = np.zeros(max(pb.value, 16), np.uint8)
+    packed = np.empty(max(pb.value, 16), np.uint8)  # every byte is written (padding zeroed)
     poff = np.zeros(max(n, 1), np.int64)
     exc = np.zeros(max(ne.value, 1) * 3, np.int32)
     exc_off = np.zeros(n + 1, np.int64)

@@ -18,7 +18,8 @@ BUILD = HERE / "_build"
 LIB = BUILD / "libhalign_gb300.so"
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", f"-I{ROOT / 'include'}"]
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-fopenmp",
+         f"-I{ROOT / 'include'}"]
 
 
 def _sources():
@@ -54,7 +55,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             print(lg)
     objs = [str(BUILD / (s.stem + ".o")) for s in srcs]
     if jobs or not LIB.exists():
-        _run([NVCC, *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart"])
+        _run([NVCC, *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart", "-lgomp"])
     return LIB
 
 

@@ -262,69 +262,134 @@ struct PackLut {
 const PackLut kPackLut;
 }  // namespace
 
+namespace {
+
+// Eight ASCII bytes -> 16 bits of 2-bit codes (base j at bits 2j) when all
+// eight are A/C/G/T: ((c >> 1) ^ (c >> 2)) & 3 maps A C G T to 0 1 2 3, and
+// rebuilding the bytes from the codes (0x41 + 2 b0 + 6 b1 + 11 b0 b1)
+// confirms the input.  Returns false (out untouched) otherwise.
+inline bool pack8(const unsigned char* s, uint32_t* out16)
+{
+    uint64_t w;
+    std::memcpy(&w, s, 8);
+    const uint64_t c = ((w >> 1) ^ (w >> 2)) & 0x0303030303030303ULL;
+    const uint64_t b0 = c & 0x0101010101010101ULL, b1 = (c >> 1) & 0x0101010101010101ULL;
+    const uint64_t e = 0x4141414141414141ULL + 2 * b0 + 6 * b1 + 11 * (b0 & b1);
+    if (e != w) return false;
+    uint64_t x = c;
+    x = (x | (x >> 6)) & 0x000F000F000F000FULL;
+    x = (x | (x >> 12)) & 0x000000FF000000FFULL;
+    x = (x | (x >> 24)) & 0xFFFFULL;
+    *out16 = (uint32_t)x;
+    return true;
+}
+
+// Pack one query into `out` (nullptr: only detect exceptions).  Returns
+// whether any byte is not A/C/G/T (such bytes pack as 0).
+bool pack_one(const unsigned char* s, int64_t len, uint8_t* out)
+{
+    const uint8_t* lut = kPackLut.code;
+    bool any_exc = false;
+    int64_t j = 0;
+    for (; j + 8 <= len; j += 8) {
+        uint32_t v;
+        if (pack8(s + j, &v)) {
+            if (out) out[j >> 2] = (uint8_t)v, out[(j >> 2) + 1] = (uint8_t)(v >> 8);
+            continue;
+        }
+        any_exc = true;
+        if (!out) continue;
+        for (int64_t t = j; t < j + 8; t += 4) {
+            const uint32_t c0 = lut[s[t]], c1 = lut[s[t + 1]], c2 = lut[s[t + 2]], c3 = lut[s[t + 3]];
+            const uint32_t m0 = c0 < 4 ? c0 : 0, m1 = c1 < 4 ? c1 : 0, m2 = c2 < 4 ? c2 : 0, m3 = c3 < 4 ? c3 : 0;
+            out[t >> 2] = (uint8_t)(m0 | m1 << 2 | m2 << 4 | m3 << 6);
+        }
+    }
+    for (; j < len; j += 4) {
+        uint32_t byte = 0;
+        for (int64_t t = j; t < len && t < j + 4; ++t) {
+            const uint32_t c = lut[s[t]];
+            if (c > 3) any_exc = true;
+            else byte |= c << ((t - j) * 2);
+        }
+        if (out) out[j >> 2] = (uint8_t)byte;
+    }
+    return any_exc;
+}
+
+}  // namespace
+
+namespace {
+
+// Exception runs (maximal runs of one non-A/C/G/T byte) of one query; writes
+// them to `exc` when it is given.  Returns the number of runs.
+int64_t exc_runs(const unsigned char* s, int64_t len, int32_t* exc)
+{
+    const uint8_t* lut = kPackLut.code;
+    int64_t ne = 0, run_start = -1;
+    unsigned char run_byte = 0;
+    for (int64_t t = 0; t <= len; ++t) {
+        const bool isx = t < len && lut[s[t]] > 3;
+        if (run_start >= 0 && (!isx || s[t] != run_byte)) {
+            if (exc) exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(t - run_start),
+                     exc[ne * 3 + 2] = run_byte;
+            ++ne;
+            run_start = -1;
+        }
+        if (isx && run_start < 0) run_start = t, run_byte = s[t];
+    }
+    return ne;
+}
+
+}  // namespace
+
+// Queries are packed independently (OpenMP over queries): a sizing pass gives
+// each query's padded byte count and exception-run count, prefix sums place
+// them, and a second pass writes bases and runs.
 extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint8_t* packed, int64_t packed_cap,
                        int64_t* poff, int32_t* exc, int64_t exc_cap, int64_t* exc_off, int64_t* packed_bytes,
                        int64_t* n_exc)
 {
     if (n < 0 || !offsets) return fail(HG_ERR_ARG, "hg_pack: bad arguments");
-    const uint8_t* lut = kPackLut.code;
-    int64_t pb = 0, ne = 0;
-    if (exc_off) exc_off[0] = 0;
     for (int64_t i = 0; i < n; ++i) {
         const int64_t len = offsets[i + 1] - offsets[i];
         if (len < 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_pack: bad query length");
-        const int64_t nbytes = ((len + 3) / 4 + 15) / 16 * 16;
-        const unsigned char* s = reinterpret_cast<const unsigned char*>(seqs) + offsets[i];
-        if (packed && pb + nbytes > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
-        if (packed) poff[i] = pb;
-        bool any_exc = false;
-        // 4 bases per output byte; an exception byte packs as 0 and is listed below
-        int64_t j = 0;
-        for (; j + 4 <= len; j += 4) {
-            const uint32_t c0 = lut[s[j]], c1 = lut[s[j + 1]], c2 = lut[s[j + 2]], c3 = lut[s[j + 3]];
-            if ((c0 | c1 | c2 | c3) > 3) {  // some byte is not A/C/G/T
-                any_exc = true;
-                const uint32_t m0 = c0 < 4 ? c0 : 0, m1 = c1 < 4 ? c1 : 0, m2 = c2 < 4 ? c2 : 0, m3 = c3 < 4 ? c3 : 0;
-                if (packed) packed[pb + (j >> 2)] = (uint8_t)(m0 | m1 << 2 | m2 << 4 | m3 << 6);
-            } else if (packed) {
-                packed[pb + (j >> 2)] = (uint8_t)(c0 | c1 << 2 | c2 << 4 | c3 << 6);
-            }
-        }
-        if (j < len) {
-            uint32_t byte = 0;
-            for (int64_t t = j; t < len; ++t) {
-                const uint32_t c = lut[s[t]];
-                if (c > 3) any_exc = true;
-                else byte |= c << ((t - j) * 2);
-            }
-            if (packed) packed[pb + (j >> 2)] = (uint8_t)byte;
-        }
-        if (packed) {
-            const int64_t used = (len + 3) / 4;
-            std::memset(packed + pb + used, 0, (size_t)(nbytes - used));
-        }
-        if (any_exc) {
-            int64_t run_start = -1;
-            unsigned char run_byte = 0;
-            for (int64_t t = 0; t <= len; ++t) {
-                const bool isx = t < len && lut[s[t]] > 3;
-                if (run_start >= 0 && (!isx || s[t] != run_byte)) {
-                    if (packed) {
-                        if (ne >= exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
-                        exc[ne * 3] = (int32_t)run_start, exc[ne * 3 + 1] = (int32_t)(t - run_start),
-                                 exc[ne * 3 + 2] = run_byte;
-                    }
-                    ++ne;
-                    run_start = -1;
-                }
-                if (isx && run_start < 0) run_start = t, run_byte = s[t];
-            }
-        }
-        pb += nbytes;
-        if (exc_off) exc_off[i + 1] = ne;
     }
+    const unsigned char* base = reinterpret_cast<const unsigned char*>(seqs);
+    std::vector<int64_t> nrun((size_t)n);
+    const bool par = n >= 64;
+#pragma omp parallel for schedule(dynamic, 16) if (par)
+    for (int64_t i = 0; i < n; ++i) {
+        const unsigned char* s = base + offsets[i];
+        const int64_t len = offsets[i + 1] - offsets[i];
+        nrun[(size_t)i] = pack_one(s, len, nullptr) ? exc_runs(s, len, nullptr) : 0;
+    }
+    int64_t pb = 0, ne = 0;
+    std::vector<int64_t> qoff((size_t)n), eo((size_t)n + 1);
+    for (int64_t i = 0; i < n; ++i) {
+        qoff[(size_t)i] = pb, eo[(size_t)i] = ne;
+        pb += (((offsets[i + 1] - offsets[i]) + 3) / 4 + 15) / 16 * 16;
+        ne += nrun[(size_t)i];
+    }
+    eo[(size_t)n] = ne;
     if (packed_bytes) *packed_bytes = pb;
     if (n_exc) *n_exc = ne;
+    if (exc_off)
+        for (int64_t i = 0; i <= n; ++i) exc_off[i] = eo[(size_t)i];
+    if (!packed) return HG_OK;
+    if (pb > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
+    if (ne > exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
+#pragma omp parallel for schedule(dynamic, 16) if (par)
+    for (int64_t i = 0; i < n; ++i) {
+        const unsigned char* s = base + offsets[i];
+        const int64_t len = offsets[i + 1] - offsets[i];
+        uint8_t* out = packed + qoff[(size_t)i];
+        poff[i] = qoff[(size_t)i];
+        pack_one(s, len, out);  // 4 bases per byte; an exception byte packs as 0 and is listed below
+        const int64_t used = (len + 3) / 4, nbytes = (used + 15) / 16 * 16;
+        std::memset(out + used, 0, (size_t)(nbytes - used));
+        if (nrun[(size_t)i]) exc_runs(s, len, exc + 3 * eo[(size_t)i]);
+    }
     return HG_OK;
 }
 

@@ -91,8 +91,13 @@ class Server:
                 if not take:
                     break
                 s = free.pop()
-                blob = b"".join(seqs[offsets[i]:offsets[i + 1]] for i in take)
-                offs = np.concatenate([[0], np.cumsum(lens[take])]).astype(np.int64)
+                a, z = take[0], take[-1]
+                if z - a + 1 == len(take):  # consecutive requests: pack straight from the source buffer
+                    blob = memoryview(seqs)[offsets[a]:offsets[z + 1]]
+                    offs = (offsets[a:z + 2] - offsets[a]).astype(np.int64)
+                else:
+                    blob = b"".join(seqs[offsets[i]:offsets[i + 1]] for i in take)
+                    offs = np.concatenate([[0], np.cumsum(lens[take])]).astype(np.int64)
                 self.slots[s].submit(pack(blob, offs))
                 busy[s] = (take, tb)
                 batches += 1
