@@ -226,8 +226,52 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
             }
             if (tid == kRowThreads - 1) s_r[cn] = ar, s_q[cn] = aq;
             __syncthreads();
-            const uint32_t col0 = s_r[0], col1 = s_r[cn];
-            for (uint32_t col = col0 + tid; col < col1 && col < (uint32_t)L; col += kRowThreads) {
+            const uint32_t col0 = s_r[0], col1 = min(s_r[cn], (uint32_t)L);
+            // exception-free query: 16 whole columns per thread, one 16-byte store
+            uint32_t vb = col0, ve = col0;  // [vb, ve): columns written by the vector path
+            if (e0 == e1) {
+                vb = (col0 + 15u) & ~15u;
+                ve = col1 & ~15u;
+                if (ve < vb) ve = vb;
+                for (uint32_t g0 = vb + 16u * tid; g0 < ve; g0 += 16u * kRowThreads) {
+                    int lo = 0, hi = cn - 1;  // last op with s_r <= g0
+                    while (lo < hi) {
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (s_r[mid] <= g0) lo = mid;
+                        else hi = mid - 1;
+                    }
+                    uint64_t wlo = 0, whi = 0;
+                    uint32_t qw = 0xffffffffu;  // first base of the 64-base window held in wlo/whi
+                    uint32_t word[4] = {0, 0, 0, 0};
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) {
+                        const uint32_t col = g0 + k;
+                        while (lo < cn - 1 && s_r[lo + 1] <= col) ++lo;
+                        const uint32_t c = s_op[lo];
+                        const uint32_t op = c & 0xfu;
+                        uint32_t ch = '-';
+                        if (op == 0 || op == 7 || op == 8) {
+                            const uint32_t qp = s_q[lo] + (col - s_r[lo]);
+                            if (qw == 0xffffffffu || qp < qw || qp >= qw + 64u) {
+                                const uint64_t wb = (((uint64_t)b.poff[q] * 4u + qp) >> 2) & ~(uint64_t)7;
+                                const uint64_t* w = reinterpret_cast<const uint64_t*>(b.packed + wb);
+                                const uint64_t w0 = w[0], w1 = w[1], w2 = w[2];
+                                const uint32_t sh = 2u * (uint32_t)((uint64_t)b.poff[q] * 4u + qp - wb * 4u);
+                                wlo = sh ? (w0 >> sh) | (w1 << (64u - sh)) : w0;
+                                whi = sh ? (w1 >> sh) | (w2 << (64u - sh)) : w1;
+                                qw = qp;
+                            }
+                            const uint32_t m = qp - qw;
+                            const uint32_t code = (uint32_t)(((m < 32u ? wlo : whi) >> (2u * (m & 31u))) & 3u);
+                            ch = 0x54474341u >> (8u * code) & 0xffu;  // "ACGT"
+                        }
+                        word[k >> 2] |= ch << (8 * (k & 3));
+                    }
+                    *reinterpret_cast<uint4*>(row + g0) = make_uint4(word[0], word[1], word[2], word[3]);
+                }
+            }
+            for (uint32_t col = col0 + tid; col < col1; col += kRowThreads) {
+                if (col >= vb && col < ve) continue;
                 int lo = 0, hi = cn - 1;  // last op with s_r <= col and nonzero ref length
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
@@ -269,33 +313,74 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
     }
 }
 
-// K9: SiteCount over rows [r0, r1) for 4 columns per thread.
+// K9: SiteCount over rows [r0, r1) for 8 columns per thread.  Per 4-byte
+// word and class, an exact zero-byte test marks the bytes of that class
+// (letters case-folded: 'a' | 0x20 == 'A' | 0x20, and only those two bytes
+// fold to it; '-' and '.' unfolded); the marks add into byte-lane counters
+// flushed to 32-bit totals every 255 rows.  N (every other byte) is the
+// row count minus the other classes.
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t x)  // 0x01 in each zero byte of x
+{
+    const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+    return (~(t | x | 0x7F7F7F7Fu)) >> 7;
+}
+
+constexpr int kCountCols = 8;
+
 __global__ void __launch_bounds__(256) count_kernel(const uint8_t* rows, int64_t row_stride, int n_rows, int L,
                                                     int rows_per_block, uint32_t* counts)
 {
-    const int col = (blockIdx.x * 256 + threadIdx.x) * 4;
+    const int col = (blockIdx.x * 256 + threadIdx.x) * kCountCols;
     if (col >= L) return;
     const int r0 = blockIdx.y * rows_per_block, r1 = min(r0 + rows_per_block, n_rows);
-    uint32_t acc[4][7];
+    uint32_t tot[kCountCols][6];
 #pragma unroll
-    for (int c = 0; c < 4; ++c)
+    for (int c = 0; c < kCountCols; ++c)
 #pragma unroll
-        for (int k = 0; k < 7; ++k) acc[c][k] = 0;
-    for (int r = r0; r < r1; ++r) {
-        const uint32_t wv = *reinterpret_cast<const uint32_t*>(rows + (int64_t)r * row_stride + col);
+        for (int k = 0; k < 6; ++k) tot[c][k] = 0;
+    const uint32_t kA = 0x61616161u, kC = 0x63636363u, kG = 0x67676767u, kT = 0x74747474u, kU = 0x75757575u;
+    for (int rb = r0; rb < r1; rb += 255) {
+        const int re = min(rb + 255, r1);
+        uint32_t acc[2][6];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t k = site_of((uint8_t)(wv >> (8 * c)));
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int z = 0; z < 7; ++z) acc[c][z] += (k == (uint32_t)z);
+            for (int k = 0; k < 6; ++k) acc[h][k] = 0;
+#pragma unroll 4
+        for (int r = rb; r < re; ++r) {
+            const uint2 v = *reinterpret_cast<const uint2*>(rows + (int64_t)r * row_stride + col);
+            const uint32_t wv[2] = {v.x, v.y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t w = wv[h], f = w | 0x20202020u;
+                acc[h][0] += zero_bytes(f ^ kA);
+                acc[h][1] += zero_bytes(f ^ kC);
+                acc[h][2] += zero_bytes(f ^ kG);
+                acc[h][3] += zero_bytes(f ^ kT);
+                acc[h][4] += zero_bytes(f ^ kU);
+                acc[h][5] += zero_bytes(w ^ 0x2D2D2D2Du) + zero_bytes(w ^ 0x2E2E2E2Eu);
+            }
         }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int bq = 0; bq < 4; ++bq) tot[h * 4 + bq][k] += (acc[h][k] >> (8 * bq)) & 0xffu;
     }
+    const uint32_t nr = (uint32_t)(r1 - r0);
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < kCountCols; ++c) {
         if (col + c >= L) break;
-#pragma unroll
-        for (int k = 0; k < 7; ++k)
-            if (acc[c][k]) atomicAdd(&counts[(int64_t)(col + c) * 7 + k], acc[c][k]);
+        uint32_t* cc = counts + (int64_t)(col + c) * 7;
+        const uint32_t other = nr - tot[c][0] - tot[c][1] - tot[c][2] - tot[c][3] - tot[c][4] - tot[c][5];
+        if (tot[c][0]) atomicAdd(cc + 0, tot[c][0]);
+        if (tot[c][1]) atomicAdd(cc + 1, tot[c][1]);
+        if (tot[c][2]) atomicAdd(cc + 2, tot[c][2]);
+        if (tot[c][3]) atomicAdd(cc + 3, tot[c][3]);
+        if (tot[c][4]) atomicAdd(cc + 4, tot[c][4]);
+        if (other) atomicAdd(cc + 5, other);
+        if (tot[c][5]) atomicAdd(cc + 6, tot[c][5]);
     }
 }
 
@@ -335,7 +420,7 @@ extern "C" cudaError_t hg_launch_count(const uint8_t* rows, int64_t row_stride, 
 {
     if (n_rows <= 0) return cudaSuccess;
     const int rows_per_block = 512;
-    dim3 grid((L + 1023) / 1024, (n_rows + rows_per_block - 1) / rows_per_block);
+    dim3 grid((L + 256 * hg::kCountCols - 1) / (256 * hg::kCountCols), (n_rows + rows_per_block - 1) / rows_per_block);
     hg::count_kernel<<<grid, 256, 0, st>>>(rows, row_stride, n_rows, L, rows_per_block, counts);
     return cudaGetLastError();
 }

@@ -1130,7 +1130,8 @@ extern "C" int hg_stage(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff,
     }
     const int64_t ne = seoff[n];
     cudaError_t e = cudaSuccess;
-    if ((e = c->s_packed.alloc(pb)) || (e = c->s_poff.alloc(n)) || (e = c->s_exc_off.alloc(n + 1)) ||
+    // 64 bytes of slack: kernels read packed bases as aligned 24-byte windows
+    if ((e = c->s_packed.alloc(pb + 64)) || (e = c->s_poff.alloc(n)) || (e = c->s_exc_off.alloc(n + 1)) ||
         (e = c->s_hoff.alloc(n)) || (e = c->s_coff.alloc(n)) || (e = c->s_qlen.alloc(n)) ||
         (e = c->s_exc.alloc(std::max<int64_t>(ne, 1) * 3)) || (e = c->s_order.alloc(n)))
         return cuda_fail(e, "hg_stage: allocation");
