@@ -180,7 +180,9 @@ struct hg_ctx {
     DevBuf<uint32_t> cig_seg, cig;
     DevBuf<int32_t> n_cig;
     DevBuf<uint8_t> has_ins;
-    DevBuf<uint8_t> rows;
+    DevBuf<uint8_t> rows, rows2;                         // rows2: second buffer while rows of the previous sub-batch copy out
+    cudaStream_t cst = nullptr;                          // copy stream for row read-back
+    cudaEvent_t rows_ev[2] = {nullptr, nullptr}, comp_ev = nullptr;
     DevBuf<uint32_t> counts, ins, status;
     // control block: queues[8], cursors (a, s, dp), n_small, n_large
     DevBuf<unsigned long long> control;
@@ -711,6 +713,10 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking)) ||
         (e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming)) ||
+        (e = cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&c->rows_ev[0], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&c->rows_ev[1], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&c->comp_ev, cudaEventDisableTiming)) ||
         (e = c->packed.alloc(max_bases / 4 + 16 * max_queries + 64)) || (e = c->poff.alloc(max_queries)) ||
         (e = c->exc_off.alloc(max_queries + 1)) || (e = c->hoff.alloc(max_queries)) ||
         (e = c->coff.alloc(max_queries)) || (e = c->qlen.alloc(max_queries)) ||
@@ -770,6 +776,10 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
     for (auto& ev : c->run_ev)
         if (ev) cudaEventDestroy(ev);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->cst) cudaStreamSynchronize(c->cst), cudaStreamDestroy(c->cst);
+    for (auto& ev : c->rows_ev)
+        if (ev) cudaEventDestroy(ev);
+    if (c->comp_ev) cudaEventDestroy(c->comp_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->st2) cudaStreamDestroy(c->st2);
     if (c->st) cudaStreamDestroy(c->st);
@@ -873,7 +883,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(6));
     HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, std::min(n, S * 4), st));
     HG_CUDA(mark(7));
-    HG_CUDA(hg_launch_count(c->rows.p, c->row_stride, n, ix.L, c->counts.p, st));
+    HG_CUDA(hg_launch_count(b.rows, c->row_stride, n, ix.L, c->counts.p, st));
     HG_CUDA(mark(8));
     HG_CUDA(hg_launch_status_or(c->status.p, n, c->run_flags.p, st));
     (void)kStageNames;
@@ -939,7 +949,8 @@ void sub_arrays(hg_ctx_t* c, const int32_t* qlen, int64_t n, std::vector<int32_t
 
 // Copy back outputs of a finished sub-batch (compacted CIGARs).
 int fetch_outputs(hg_ctx_t* c, int n, const int64_t* d_coff, uint32_t* cigar, int64_t cigar_cap, int64_t cig_base, int64_t* cigar_off,
-                  uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status, int64_t* total_out)
+                  uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status, int64_t* total_out,
+                  const uint8_t* d_rows)
 {
     compact_offsets_kernel<<<1, 1024, 0, c->st>>>(c->n_cig.p, n, c->cig_off.p);
     HG_CUDA(cudaGetLastError());
@@ -948,9 +959,17 @@ int fetch_outputs(hg_ctx_t* c, int n, const int64_t* d_coff, uint32_t* cigar, in
     if (status) HG_CUDA(cudaMemcpyAsync(status, c->status.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, c->st));
     if (has_ins) HG_CUDA(cudaMemcpyAsync(has_ins, c->has_ins.p, (size_t)n, cudaMemcpyDeviceToHost, c->st));
     if (rows) {
+        // row read-back runs on the copy stream, overlapping the next sub-batch
         const int64_t L = c->ix->L;
-        HG_CUDA(cudaMemcpy2DAsync(rows, (size_t)row_stride, c->rows.p, (size_t)c->row_stride, (size_t)L, (size_t)n,
-                                  cudaMemcpyDeviceToHost, c->st));
+        const int slot = (d_rows == c->rows2.p && c->rows2.p) ? 1 : 0;
+        HG_CUDA(cudaEventRecord(c->comp_ev, c->st));
+        HG_CUDA(cudaStreamWaitEvent(c->cst, c->comp_ev, 0));
+        if ((int64_t)row_stride == c->row_stride)
+            HG_CUDA(cudaMemcpyAsync(rows, d_rows, (size_t)row_stride * (size_t)n, cudaMemcpyDeviceToHost, c->cst));
+        else
+            HG_CUDA(cudaMemcpy2DAsync(rows, (size_t)row_stride, d_rows, (size_t)c->row_stride, (size_t)L, (size_t)n,
+                                      cudaMemcpyDeviceToHost, c->cst));
+        HG_CUDA(cudaEventRecord(c->rows_ev[slot], c->cst));
     }
     HG_CUDA(cudaStreamSynchronize(c->st));
     const int64_t total = off[n];
@@ -1000,6 +1019,11 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
         return HG_OK;
     }
     const auto plans = plan(c, poff, qlen, exc_off, n);
+    // two row buffers alternate between sub-batches so the read-back of one
+    // overlaps the next sub-batch's compute
+    if (rows && !plain && plans.size() > 1 && !c->rows2.p)
+        HG_CUDA(c->rows2.alloc((size_t)c->max_n * c->row_stride));
+    size_t sub_i = 0;
     std::vector<int32_t> order;
     std::vector<int64_t> hoff, coff, spoff, seoff;
     for (const SubPlan& sp : plans) {
@@ -1029,9 +1053,13 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
         HG_CUDA(cudaMemcpyAsync(c->order.p, order.data(), 4 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
         HG_CUDA(cudaMemcpyAsync(c->hoff.p, hoff.data(), 8 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
         HG_CUDA(cudaMemcpyAsync(c->coff.p, coff.data(), 8 * (size_t)sp.n, cudaMemcpyHostToDevice, c->st));
+        const int rslot = (c->rows2.p && (sub_i & 1)) ? 1 : 0;
+        uint8_t* rbuf = rslot ? c->rows2.p : c->rows.p;
+        HG_CUDA(cudaStreamWaitEvent(c->st, c->rows_ev[rslot], 0));  // its last read-back is done
         if (!plain) {
-            const hg::BatchDev b = batch_view(c, (int)sp.n, c->packed.p, c->poff.p, c->qlen.p, c->exc.p,
-                                              c->exc_off.p, c->order.p, c->hoff.p, c->coff.p);
+            hg::BatchDev b = batch_view(c, (int)sp.n, c->packed.p, c->poff.p, c->qlen.p, c->exc.p,
+                                        c->exc_off.p, c->order.p, c->hoff.p, c->coff.p);
+            b.rows = rbuf;
             int r = run_sub(c, b, true);
             if (r) return r;
         } else {
@@ -1066,10 +1094,12 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
         int64_t total = 0;
         int r = fetch_outputs(c, (int)sp.n, c->coff.p, cigar, cigar_cap, cig_base, cigar_off + f,
                               has_ins ? has_ins + f : nullptr, rows ? rows + f * row_stride : nullptr, row_stride,
-                              status + f, &total);
+                              status + f, &total, rbuf);
         if (r) return r;
         cig_base += total;
+        ++sub_i;
     }
+    HG_CUDA(cudaStreamSynchronize(c->cst));
     return status_error(status, n);
 }
 
@@ -1215,8 +1245,11 @@ extern "C" int hg_fetch_staged(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, 
         return fail(HG_ERR_ARG, "hg_fetch_staged: staged batch spans several sub-batches; fetch needs one");
     const SubPlan& sp = c->staged_plan[0];
     int64_t total = 0;
-    return fetch_outputs(c, (int)sp.n, c->s_coff.p, cigar, cigar_cap, 0, cigar_off, has_ins, rows, row_stride,
-                         status, &total);
+    const int r = fetch_outputs(c, (int)sp.n, c->s_coff.p, cigar, cigar_cap, 0, cigar_off, has_ins, rows, row_stride,
+                                status, &total, c->rows.p);
+    if (r) return r;
+    HG_CUDA(cudaStreamSynchronize(c->cst));
+    return HG_OK;
 }
 
 // ------------------------------------------------------ asynchronous form
