@@ -242,10 +242,12 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         if (lane == 0) {
             b.n_chain[q] = c;
             b.s_base[q] = sb == ~0ull ? 0 : (int64_t)sb;
-            b.s_n[q] = sb == ~0ull ? 0 : nseg;
+            b.s_n[q] = 0;
         }
         if (sb == ~0ull) continue;
-        uint32_t rpos = 0, qpos = 0, slot = 0;
+        // empty segments (both lengths 0) contribute no op: only the others
+        // are stored, in order
+        uint32_t rpos = 0, qpos = 0, slot = 0, nkept = 0;
         for (int s0 = 0; s0 < nseg; s0 += 32) {
             const int s = s0 + lane;
             const bool act = s < nseg;
@@ -284,18 +286,22 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 kind = kSegDpSmall;
             else
                 kind = kSegDpLarge;
+            const bool keep = act && kind != kSegEmpty;
+            const unsigned kmask = __ballot_sync(FULL, keep);
+            const uint32_t sid = (uint32_t)sb + nkept + (uint32_t)__popc(kmask & ((1u << lane) - 1u));
             const uint32_t need = (kind >= kSegDpSmall && act) ? rl + ql : 0;
             const uint32_t sincl = warp_incl_sum(need);
             const uint32_t my_slot = slot + sincl - need;
-            if (act) {
+            if (keep) {
                 Seg g;
                 g.rs = rs, g.qs = qs, g.rl = rl, g.ql = ql;
                 g.slot = my_slot;
                 g.nops = 0;
                 g.q = (uint32_t)q;
                 g.kind = kind | flags;
-                b.seg[sb + s] = g;
+                b.seg[sid] = g;
             }
+            nkept += (uint32_t)__popc(kmask);
             // tier work lists (warp-aggregated appends): small, one-warp
             // wavefront, CTA wavefront, exact
             const bool dp_big = act && (kind == kSegDpLarge || kind == kSegGlobal);
@@ -320,7 +326,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             if (ms >> lane & 1u) {
                 const unsigned w = bs + __popc(ms & below);
                 if ((int64_t)w < b.wcap) {
-                    b.work_small[w] = (uint32_t)(sb + s);
+                    b.work_small[w] = sid;
                     if (b.work_key) {
                         Seg g;
                         g.rl = rl, g.ql = ql, g.kind = kind | flags;
@@ -343,7 +349,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             }
             if (ml >> lane & 1u) {
                 const unsigned w = bl + __popc(ml & below);
-                if ((int64_t)w < b.wcap) b.work_large[w] = (uint32_t)(sb + s);
+                if ((int64_t)w < b.wcap) b.work_large[w] = sid;
                 else atomicOr(&b.status[q], kStArenaOverflow);
             }
             uint32_t wkey = 0xffffffffu;
@@ -351,7 +357,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 const unsigned w = bw + __popc(mw & below);
                 wkey = wave_key(rl, ql, (flags & kSegLeft) != 0);
                 if ((int64_t)w < b.wcap) {
-                    b.work_wave[w] = (uint32_t)(sb + s);
+                    b.work_wave[w] = sid;
                     b.work_wave_key[w] = wkey;
                 } else {
                     atomicOr(&b.status[q], kStArenaOverflow);
@@ -363,13 +369,14 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             }
             if (mx >> lane & 1u) {
                 const unsigned w = bx + __popc(mx & below);
-                if ((int64_t)w < b.wcap) b.work_wide[w] = (uint32_t)(sb + s);
+                if ((int64_t)w < b.wcap) b.work_wide[w] = sid;
                 else atomicOr(&b.status[q], kStArenaOverflow);
             }
             rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
             qpos = (uint32_t)__shfl_sync(FULL, iq, 31);
             slot = slot + __shfl_sync(FULL, sincl, 31);
         }
+        if (lane == 0) b.s_n[q] = (int32_t)nkept;
     }
 }
 
