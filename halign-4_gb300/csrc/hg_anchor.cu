@@ -22,7 +22,6 @@ namespace hg {
 
 constexpr int kAnchorThreads = 256;
 constexpr int kSmemEnt = 8192;
-constexpr int kSmemSort = 4096;
 
 __device__ void bitonic_sort_u64(unsigned long long* key, int N)
 {
@@ -49,7 +48,6 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
     __shared__ unsigned long long s_base;
     uint32_t* cnt = (ix.n_ent <= (uint32_t)kSmemEnt) ? reinterpret_cast<uint32_t*>(dsm)
                                                      : b.ent_cnt + (size_t)blockIdx.x * ix.n_ent;
-    unsigned long long* skey = reinterpret_cast<unsigned long long*>(dsm + kSmemEnt * 4);
     const int tid = threadIdx.x;
     if (ix.n_ent <= (uint32_t)kSmemEnt)
         for (int i = tid; i < (int)ix.n_ent; i += kAnchorThreads) cnt[i] = 0;
@@ -69,18 +67,27 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
         for (int i = tid; i < nm; i += kAnchorThreads) atomicAdd(&cnt[he[i]], 1u);
         __syncthreads();
         const double limit = ix.q_occ_frac > 0.0 ? ix.q_occ_frac * (double)nh : 0.0;
-        // each thread owns a contiguous run of hits so the scan keeps hit order
-        const int per = (nm + kAnchorThreads - 1) / kAnchorThreads;
-        const int i0 = min(tid * per, nm), i1 = min(i0 + per, nm);
-        int my = 0;
-        for (int i = i0; i < i1; ++i) {
+        // anchors of hit i: its center occurrences if the hit survives the filters
+        auto n_out = [&](int i) -> int {
             const uint32_t d = he[i];
             bool keep = !(ix.q_occ_frac > 0.0 && (double)cnt[d] > limit);
             if (keep && ix.ent_over[d]) keep = ix.sample_every != 0 && (hp[i] % ix.sample_every) == 0;
-            if (keep) my += (int)ix.ent_count[d];
+            return keep ? (int)ix.ent_count[d] : 0;
+        };
+        // total (coalesced: thread t takes hits t, t+256, ...); the counts of the
+        // first kKeep chunks stay in registers for the emission pass
+        constexpr int kKeep = 16;
+        int keepn[kKeep];
+        int my = 0;
+#pragma unroll
+        for (int r = 0; r < kKeep; ++r) {
+            const int i = tid + r * kAnchorThreads;
+            keepn[r] = i < nm ? n_out(i) : 0;
+            my += keepn[r];
         }
+        for (int i = tid + kKeep * kAnchorThreads; i < nm; i += kAnchorThreads) my += n_out(i);
         int A;
-        const int ex = block_excl_sum(my, scan_s, &A);
+        block_excl_sum(my, scan_s, &A);
         if (tid == 0) {
             unsigned long long base = atomicAdd(b.a_cursor, (unsigned long long)A);
             if ((int64_t)(base + A) > b.acap) {
@@ -92,17 +99,28 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
         __syncthreads();
         const unsigned long long base = s_base;
         if (base != ~0ull) {
-            int o = ex;
-            for (int i = i0; i < i1; ++i) {
-                const uint32_t d = he[i];
-                bool keep = !(ix.q_occ_frac > 0.0 && (double)cnt[d] > limit);
-                if (keep && ix.ent_over[d]) keep = ix.sample_every != 0 && (hp[i] % ix.sample_every) == 0;
-                if (!keep) continue;
-                const uint32_t st = ix.ent_start[d], c = ix.ent_count[d];
-                for (uint32_t j = 0; j < c; ++j, ++o) {
-                    b.a_ref[base + o] = ix.cpos[st + j];
-                    b.a_qry[base + o] = hp[i];
+            // hits in chunks of 256, a block scan per chunk keeps hit order
+            int carry = 0;
+            for (int c0 = 0, r = 0; c0 < nm; c0 += kAnchorThreads, ++r) {
+                const int i = c0 + tid;
+                int k = 0;
+                if (r < kKeep) {
+#pragma unroll
+                    for (int rr = 0; rr < kKeep; ++rr)
+                        if (rr == r) k = keepn[rr];
+                } else {
+                    k = i < nm ? n_out(i) : 0;
                 }
+                int tot;
+                const int ex = block_excl_sum(k, scan_s, &tot);
+                if (k) {
+                    const uint32_t d = he[i], st = ix.ent_start[d], qp = hp[i];
+                    for (int j = 0; j < k; ++j) {
+                        b.a_ref[base + carry + ex + j] = ix.cpos[st + j];
+                        b.a_qry[base + carry + ex + j] = qp;
+                    }
+                }
+                carry += tot;
             }
         }
         __syncthreads();
@@ -125,7 +143,7 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
         if (s_flag) {
             int N = 1;
             while (N < A) N <<= 1;
-            unsigned long long* key = (N <= kSmemSort) ? skey : b.a_tmp + 2 * base;
+            unsigned long long* key = b.a_tmp + 2 * base;  // rare: only when an inversion exists
             for (int i = tid; i < N; i += kAnchorThreads)
                 key[i] = i < A ? ((unsigned long long)ar[i] << 32 | aq[i]) : ~0ull;
             __syncthreads();
@@ -142,7 +160,7 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
 
 }  // namespace hg
 
-static constexpr size_t kAnchorSmem = hg::kSmemEnt * 4 + hg::kSmemSort * 8;
+static constexpr size_t kAnchorSmem = hg::kSmemEnt * 4;  // per-entry counters (at most kSmemEnt entries)
 
 // Raises the dynamic shared-memory limit of the anchor kernel; called once
 // per context before any launch or graph capture.
@@ -153,6 +171,8 @@ extern "C" cudaError_t hg_prepare_kernels(void)
 
 extern "C" cudaError_t hg_launch_anchor(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
-    hg::anchor_kernel<<<grid, hg::kAnchorThreads, kAnchorSmem, st>>>(*ix, *b);
+    // counters for the center's entries live in shared memory when they fit
+    const size_t smem = ix->n_ent <= (uint32_t)hg::kSmemEnt ? ((size_t)ix->n_ent * 4 + 15) & ~(size_t)15 : 16;
+    hg::anchor_kernel<<<grid, hg::kAnchorThreads, smem, st>>>(*ix, *b);
     return cudaGetLastError();
 }

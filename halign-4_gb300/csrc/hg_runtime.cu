@@ -707,7 +707,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         return fail(HG_ERR_ARG, "hg_ctx_create: max_bases + max_queries * (center length + 4) must stay below 2^32");
     }
     const int64_t n_ent = ix->dev.n_ent;
-    const int grid_anchor = c->sms * 3;
+    const int grid_anchor = c->sms * 6;  // the anchor kernel's largest grid
     cudaError_t e = cudaSuccess;
     if ((e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking)) ||
         (e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking)) ||
@@ -864,7 +864,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(0));
     HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, std::min(n, S * 6), st));
     HG_CUDA(mark(1));
-    HG_CUDA(hg_launch_anchor(&ix, &b, std::min(n, S * 3), st));
+    HG_CUDA(hg_launch_anchor(&ix, &b, std::min(n, S * 6), st));
     HG_CUDA(mark(2));
     HG_CUDA(hg_launch_chain(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 12)), st));
     HG_CUDA(mark(3));
