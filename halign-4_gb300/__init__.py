@@ -82,6 +82,8 @@ def lib() -> C.CDLL:
     L.hg_global_align_ksw2.restype = i64
     L.hg_align_query.argtypes = [vp, C.c_char_p, i64, vp, i64, vp]
     L.hg_align_query.restype = i64
+    L.hg_global_align_mm2.argtypes = [vp, C.c_char_p, i64, vp, vp, i64, vp, i64, vp]
+    L.hg_global_align_mm2.restype = i64
     _lib = L
     return L
 
@@ -179,6 +181,20 @@ class Index:
         out = np.zeros(cap, np.uint32)
         st = C.c_uint32()
         n = lib().hg_align_query(self.h, q, len(q), _p(out), cap, C.byref(st))
+        if n < 0:
+            _check(-n)
+        return out[:n].copy()
+
+    def global_align_mm2(self, qry, anchor_ref, anchor_qry) -> np.ndarray:
+        """align::globalAlignMM2 against the center with the caller's anchors
+        (one center, forward strand, span k); returns the CIGAR words."""
+        q = _bytes(qry)
+        ar = np.ascontiguousarray(anchor_ref, np.uint32)
+        aq = np.ascontiguousarray(anchor_qry, np.uint32)
+        cap = len(q) + self.L + 8
+        out = np.zeros(cap, np.uint32)
+        st = C.c_uint32()
+        n = lib().hg_global_align_mm2(self.h, q, len(q), _p(ar), _p(aq), len(ar), _p(out), cap, C.byref(st))
         if n < 0:
             _check(-n)
         return out[:n].copy()

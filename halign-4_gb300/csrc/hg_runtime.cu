@@ -1448,6 +1448,100 @@ extern "C" int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const cha
                         flag < 0 ? (hg::kEzGenericSc | hg::kEzRight) : flag, ez, cigar, cap);
 }
 
+// align::globalAlignMM2 with the caller's anchors against the index's center
+// (src/align/align.cpp:189-305): the anchors are sorted as chainAnchors sorts
+// them (pos_ref, pos_qry; one center, forward strand), then the chain, gap-
+// fill and stitch stages run on one query without minimizer extraction.
+namespace {
+int global_align_mm2_impl(hg_index_t* ix, const char* qry, int64_t qlen, const uint32_t* anchor_ref,
+                          const uint32_t* anchor_qry, int64_t n_anchors, uint32_t* cigar, int64_t cap,
+                          uint32_t* status, int64_t* n_out)
+{
+    if (!ix || (!qry && qlen > 0) || qlen < 0 || qlen > INT32_MAX || n_anchors < 0 ||
+        (n_anchors > 0 && (!anchor_ref || !anchor_qry)) || (cap > 0 && !cigar))
+        return fail(HG_ERR_ARG, "hg_global_align_mm2: bad arguments");
+    std::lock_guard<std::mutex> lock(ix->single_mu);
+    const int64_t need_bases = std::max<int64_t>(qlen, 1);
+    const int64_t need_bases_for_anchors = (std::max<int64_t>(n_anchors - 65536, 0)) * 4;
+    const int64_t want = std::max({need_bases, need_bases_for_anchors, (int64_t)65536});
+    if (!ix->single || ix->single->max_bases < want) {
+        if (ix->single) hg_ctx_destroy(ix->single), ix->single = nullptr;
+        int r = hg_ctx_create(ix, 1, want, &ix->single);
+        if (r) return r;
+    }
+    hg_ctx_t* c = ix->single;
+    if (n_anchors > c->acap) return fail(HG_ERR_CAPACITY, "hg_global_align_mm2: too many anchors");
+    cudaSetDevice(ix->device);
+    const int64_t offs[2] = {0, qlen};
+    int64_t pb = 0, ne = 0;
+    int r = hg_pack(qry, offs, 1, nullptr, 0, nullptr, nullptr, 0, nullptr, &pb, &ne);
+    if (r) return r;
+    std::vector<uint8_t> pk((size_t)std::max<int64_t>(pb, 16));
+    std::vector<int64_t> poff(1), eoff(2);
+    std::vector<int32_t> exc((size_t)std::max<int64_t>(ne, 1) * 3);
+    r = hg_pack(qry, offs, 1, pk.data(), (int64_t)pk.size(), poff.data(), exc.data(), ne, eoff.data(), nullptr,
+                nullptr);
+    if (r) return r;
+    // chainAnchors' order for one center on the forward strand: (pos_ref, pos_qry)
+    std::vector<uint64_t> key((size_t)n_anchors);
+    for (int64_t i = 0; i < n_anchors; ++i) key[i] = (uint64_t)anchor_ref[i] << 32 | anchor_qry[i];
+    std::sort(key.begin(), key.end());
+    std::vector<uint32_t> ar((size_t)n_anchors), aq((size_t)n_anchors);
+    for (int64_t i = 0; i < n_anchors; ++i) ar[i] = (uint32_t)(key[i] >> 32), aq[i] = (uint32_t)key[i];
+    const int32_t ql = (int32_t)qlen;
+    const int64_t zero64 = 0, coff0 = 0;
+    const int32_t na = (int32_t)n_anchors;
+    cudaStream_t st = c->st;
+    HG_CUDA(cudaMemcpyAsync(c->packed.p, pk.data(), pk.size(), cudaMemcpyHostToDevice, st));
+    if (ne) HG_CUDA(cudaMemcpyAsync(c->exc.p, exc.data(), 12 * (size_t)ne, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->poff.p, &zero64, 8, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->qlen.p, &ql, 4, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->exc_off.p, eoff.data(), 16, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->coff.p, &coff0, 8, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->hoff.p, &zero64, 8, cudaMemcpyHostToDevice, st));
+    if (n_anchors) {
+        HG_CUDA(cudaMemcpyAsync(c->a_ref.p, ar.data(), 4 * (size_t)n_anchors, cudaMemcpyHostToDevice, st));
+        HG_CUDA(cudaMemcpyAsync(c->a_qry.p, aq.data(), 4 * (size_t)n_anchors, cudaMemcpyHostToDevice, st));
+    }
+    HG_CUDA(cudaMemcpyAsync(c->a_base.p, &zero64, 8, cudaMemcpyHostToDevice, st));
+    HG_CUDA(cudaMemcpyAsync(c->a_n.p, &na, 4, cudaMemcpyHostToDevice, st));
+    hg::BatchDev b = batch_view(c, 1, c->packed.p, c->poff.p, c->qlen.p, c->exc.p, c->exc_off.p, nullptr, c->hoff.p,
+                                c->coff.p);
+    HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, st));
+    HG_CUDA(cudaMemsetAsync(c->status.p, 0, 4, st));
+    HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, st));
+    HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * 2 * hg::kWaveBins, st));
+    const hg::IndexDev& d = ix->dev;
+    HG_CUDA(hg_launch_chain(&d, &b, 1, st));
+    HG_CUDA(hg_launch_dp_small(&d, &b, c->sms, st));
+    HG_CUDA(hg_launch_dp_wave(&d, &b, c->sms, st));
+    HG_CUDA(hg_launch_dp_wide(&d, &b, c->sms, st));
+    HG_CUDA(hg_launch_dp_large(&d, &b, c->sms, st));
+    HG_CUDA(hg_launch_stitch(&d, &b, 1, st));
+    int32_t ncig = 0;
+    uint32_t stv = 0;
+    HG_CUDA(cudaMemcpyAsync(&ncig, c->n_cig.p, 4, cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaMemcpyAsync(&stv, c->status.p, 4, cudaMemcpyDeviceToHost, st));
+    HG_CUDA(cudaStreamSynchronize(st));
+    if (status) *status = stv;
+    if (stv & HG_ST_ARENA_OVERFLOW) return fail(HG_ERR_CAPACITY, "hg_global_align_mm2: device arena overflow");
+    if (stv & HG_ST_CIGAR_OVERFLOW) return fail(HG_ERR_CIGAR, "hg_global_align_mm2: CIGAR length overflow");
+    if (ncig > cap) return fail(HG_ERR_CAPACITY, "hg_global_align_mm2: CIGAR capacity");
+    if (ncig) HG_CUDA(cudaMemcpy(cigar, c->cig.p, 4 * (size_t)ncig, cudaMemcpyDeviceToHost));
+    *n_out = ncig;
+    return HG_OK;
+}
+}  // namespace
+
+extern "C" int64_t hg_global_align_mm2(hg_index_t* ix, const char* qry, int64_t qlen, const uint32_t* anchor_ref,
+                                       const uint32_t* anchor_qry, int64_t n_anchors, uint32_t* cigar, int64_t cap,
+                                       uint32_t* status)
+{
+    int64_t n = 0;
+    const int r = global_align_mm2_impl(ix, qry, qlen, anchor_ref, anchor_qry, n_anchors, cigar, cap, status, &n);
+    return r ? -(int64_t)r : n;
+}
+
 extern "C" int64_t hg_align_query(hg_index_t* ix, const char* qry, int64_t qlen, uint32_t* cigar, int64_t cap,
                                   uint32_t* status)
 {

@@ -189,6 +189,18 @@ int hg_ksw_extz2_noalloc(int qlen, const uint8_t* d_query, int tlen, const uint8
 int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int flag, uint32_t* cigar,
                              int64_t cap);
 
+/* align::globalAlignMM2 (src/align/align.cpp:189-305, include/align.h) with
+ * the caller's anchors (anchor::Anchor pos_ref / pos_qry, include/anchor.h:
+ * 39-50) against the index's center: anchors of one center on the forward
+ * strand with span = the index's k, as collect_anchors makes them on the
+ * align-to-center path.  The anchors are sorted as chainAnchors sorts them
+ * (the reference sorts the caller's vector in place; here the input arrays are
+ * left untouched).  Returns the CIGAR length, or -status.  *status gets the
+ * HG_ST_* bits (partial CIGAR / length mismatch as in hg_align_query). */
+int64_t hg_global_align_mm2(hg_index_t* ix, const char* qry, int64_t qlen, const uint32_t* anchor_ref,
+                            const uint32_t* anchor_qry, int64_t n_anchors, uint32_t* cigar, int64_t cap,
+                            uint32_t* status);
+
 /* RefAligner::globalAlign for one query against the index's center
  * (src/align/ref_aligner.cpp:91-125): the plain single-query path. */
 int64_t hg_align_query(hg_index_t* ix, const char* qry, int64_t qlen, uint32_t* cigar, int64_t cap,

@@ -260,6 +260,28 @@ def test_batch_window_overflow_vs_oracle(gpu, oracle, pkg):
         assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
 
 
+def test_global_align_mm2_vs_oracle(gpu, oracle, pkg):
+    """The single-call globalAlignMM2 with caller anchors (the anchors
+    collect_anchors makes for each query, shuffled: the call sorts them as
+    chainAnchors does), against the oracle's globalAlignMM2."""
+    rng = np.random.default_rng(17)
+    w = pkg.synth.divergent(6)
+    ix = gpu.Index(w.center)
+    cmx, cmy = oracle.extract_minimizer(w.center)
+    center_dp = w.center  # uniform ACGT center: its consensus is itself
+    for i in range(w.n):
+        q = w.query(i)
+        qx, qy = oracle.extract_minimizer(q)
+        an = oracle.collect_anchors(cmx, cmy, qx, qy)
+        an = an[rng.permutation(len(an))]
+        want = oracle.global_align_mm2(center_dp, q, an)
+        got = ix.global_align_mm2(q, an["pos_ref"], an["pos_qry"])
+        assert np.array_equal(got, want), i
+    # chainless: no anchors at all
+    q = w.query(0)[:300]
+    assert np.array_equal(ix.global_align_mm2(q, [], []), oracle.global_align_mm2(center_dp, q, an[:0]))
+
+
 def test_global_align_ksw2_vs_oracle(gpu, oracle):
     rng = np.random.default_rng(2)
     for it in range(30):
