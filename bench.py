@@ -293,6 +293,7 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=4000)
     ap.add_argument("--plain-queries", type=int, default=128)
     ap.add_argument("--stage-timing", action="store_true", help="per-stage event timing pass (extra run)")
+    ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--workload", default="mito", choices=sorted(WORKLOADS),
                     help="synthetic workload (the headline metric is quoted on mito)")
     args = ap.parse_args()
@@ -314,6 +315,17 @@ def main():
     lens = np.diff(w.offsets)
     ctx = pkg.Context(ix, max_queries=sub, max_bases=int(min(lens.sum(), sub * int(lens.max()))) + 1024)
     ctx.stage(b)
+    tuning = None
+    if not args.no_tune:
+        # launch-shape autotuner (coordinate descent on CTAs per SM, staged runs)
+        t0 = time.perf_counter()
+        default = ctx.get_launch()
+        best, best_ms, tried = pkg.autotune.tune(pkg.autotune.staged_measure(ctx, reps=1), default, rounds=1)
+        ctx.set_launch(best)
+        tuning = {"knobs": dict(zip(pkg.LAUNCH_KNOBS, best)), "default_knobs": dict(zip(pkg.LAUNCH_KNOBS, default)),
+                  "default_ms": round(tried[0][1], 3), "tuned_ms": round(best_ms, 3), "candidates": len(tried),
+                  "seconds": round(time.perf_counter() - t0, 1)}
+        log(f"[bench] tuned launch {best} ({tried[0][1]:.1f} -> {best_ms:.1f} ms, {len(tried)} candidates)")
     # warm-up (also builds and caches the CUDA graphs of every sub-batch)
     for _ in range(args.warmup):
         ctx.run_staged()
@@ -415,7 +427,8 @@ def main():
         "data": "synthetic (seeded mutated copies of a uniform ACGT center)",
         "config": {"workload": WORKLOADS[args.workload].format(n=args.queries),
                    "queries_per_gpu": args.queries, "bases_per_gpu": b.bases,
-                   "l2": "inputs and intermediates exceed L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+                   "l2": "inputs and intermediates exceed L2 (no flush needed)", "parallelism": f"replicas x{world}",
+                   "launch_tuning": tuning},
         "gcups": round(world * cells / step_s / 1e9, 3) if cells else None,
         "gpu_launches": int(launches),
         "stage_ms": {k: round(v, 3) for k, v in stages.items()},

@@ -27,6 +27,8 @@ LIB_PATH = HERE / "_build" / "libhalign_gb300.so"
 HG_OK = 0
 HG_ERR_LENGTH_MISMATCH = 5
 ST_ARENA_OVERFLOW, ST_PARTIAL_CIGAR, ST_CIGAR_OVERFLOW, ST_LENGTH_MISMATCH = 0x01, 0x02, 0x08, 0x10
+LAUNCH_KNOBS = ("seed", "anchor", "chain", "dp_small", "stitch", "rows")  # hg_ctx_set_launch order
+LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32))
 STAGES = ("seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count")
 
 
@@ -84,6 +86,8 @@ def lib() -> C.CDLL:
     L.hg_align_query.restype = i64
     L.hg_global_align_mm2.argtypes = [vp, C.c_char_p, i64, vp, vp, i64, vp, i64, vp]
     L.hg_global_align_mm2.restype = i64
+    L.hg_ctx_set_launch.argtypes = [vp, vp, i32]
+    L.hg_ctx_get_launch.argtypes = [vp, vp, i32]
     _lib = L
     return L
 
@@ -285,6 +289,16 @@ class Context:
         if check or code not in (HG_OK, HG_ERR_LENGTH_MISMATCH):
             _check(code)
         return self._result(cig, off, has_ins, status, None, b.n)
+
+    def set_launch(self, knobs) -> None:
+        """CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows stages."""
+        k = np.ascontiguousarray([int(x) for x in knobs], np.int32)
+        _check(lib().hg_ctx_set_launch(self.h, _p(k), len(k)))
+
+    def get_launch(self) -> list[int]:
+        k = np.zeros(len(LAUNCH_KNOBS), np.int32)
+        _check(lib().hg_ctx_get_launch(self.h, _p(k), len(k)))
+        return [int(x) for x in k]
 
     def set_timing(self, on: bool):
         _check(lib().hg_set_timing(self.h, int(on)))

@@ -142,6 +142,8 @@ struct hg_ctx {
     hg_index_t* ix = nullptr;
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
+    // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
+    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 4};
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int sms = 1;
     int64_t max_n = 0, max_bases = 0, exc_cap = 0;
@@ -760,6 +762,30 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     return HG_OK;
 }
 
+// Launch shape of the sub-batch stages (CTAs per SM); bounds keep every
+// per-CTA scratch slice in range.  Cached graphs are dropped.
+extern "C" int hg_ctx_set_launch(hg_ctx_t* c, const int32_t* ctas_per_sm, int n)
+{
+    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1};
+    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32};
+    if (!c || !ctas_per_sm || n < 0 || n > HG_LAUNCH_KNOBS) return fail(HG_ERR_ARG, "hg_ctx_set_launch: bad arguments");
+    for (int i = 0; i < n; ++i)
+        if (ctas_per_sm[i] < lo[i] || ctas_per_sm[i] > hi[i])
+            return fail(HG_ERR_ARG, "hg_ctx_set_launch: knob " + std::to_string(i) + " out of range");
+    cudaStreamSynchronize(c->st);
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    for (int i = 0; i < n; ++i) c->launch[i] = ctas_per_sm[i];
+    return HG_OK;
+}
+
+extern "C" int hg_ctx_get_launch(const hg_ctx_t* c, int32_t* ctas_per_sm, int n)
+{
+    if (!c || !ctas_per_sm || n < 0 || n > HG_LAUNCH_KNOBS) return fail(HG_ERR_ARG, "hg_ctx_get_launch: bad arguments");
+    for (int i = 0; i < n; ++i) ctas_per_sm[i] = c->launch[i];
+    return HG_OK;
+}
+
 extern "C" void hg_ctx_destroy(hg_ctx_t* c)
 {
     if (!c) return;
@@ -862,13 +888,14 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     const int n = b.n;
     auto mark = [&](int i) -> cudaError_t { return timed ? cudaEventRecord(c->ev[i], st) : cudaSuccess; };
     HG_CUDA(mark(0));
-    HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, std::min(n, S * 6), st));
+    const int32_t* K = c->launch;
+    HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, std::min(n, S * K[0]), st));
     HG_CUDA(mark(1));
-    HG_CUDA(hg_launch_anchor(&ix, &b, std::min(n, S * 6), st));
+    HG_CUDA(hg_launch_anchor(&ix, &b, std::min(n, S * K[1]), st));
     HG_CUDA(mark(2));
-    HG_CUDA(hg_launch_chain(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 12)), st));
+    HG_CUDA(hg_launch_chain(&ix, &b, std::max(1, std::min((n + 3) / 4, S * K[2])), st));
     HG_CUDA(mark(3));
-    HG_CUDA(hg_launch_dp_small(&ix, &b, S * 8, st));
+    HG_CUDA(hg_launch_dp_small(&ix, &b, S * K[3], st));
     HG_CUDA(mark(4));
     // the CTA wavefront tier runs on a side stream beside the warp tiers
     HG_CUDA(cudaEventRecord(c->fork_ev, st));
@@ -879,9 +906,9 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(hg_launch_dp_large(&ix, &b, S * kLargeBlocksPerSm, st));
     HG_CUDA(cudaStreamWaitEvent(st, c->join_ev, 0));
     HG_CUDA(mark(5));
-    HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * 8)), st));
+    HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * K[4])), st));
     HG_CUDA(mark(6));
-    HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, std::min(n, S * 4), st));
+    HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, std::min(n, S * K[5]), st));
     HG_CUDA(mark(7));
     HG_CUDA(hg_launch_count(b.rows, c->row_stride, n, ix.L, c->counts.p, st));
     HG_CUDA(mark(8));

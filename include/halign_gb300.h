@@ -115,6 +115,15 @@ int hg_stage(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const in
 int hg_run_staged(hg_ctx_t* ctx);
 int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
                     uint8_t* rows, int64_t row_stride, uint32_t* status);
+/* Launch shape of the sub-batch stages, in CTAs per SM: [0] seed (1..32),
+ * [1] anchor (1..6), [2] chain (1..64), [3] dp_small (1..32), [4] stitch
+ * (1..32), [5] rows (1..32).  Defaults 6 6 12 12 8 4.  Setting them drops the
+ * context's cached CUDA graphs (the autotuner, halign-4_gb300/autotune.py,
+ * searches them).  No reference counterpart: launch geometry. */
+#define HG_LAUNCH_KNOBS 6
+int hg_ctx_set_launch(hg_ctx_t* ctx, const int32_t* ctas_per_sm, int n);
+int hg_ctx_get_launch(const hg_ctx_t* ctx, int32_t* ctas_per_sm, int n);
+
 /* Timing of the last hg_run_staged from CUDA events on the context stream:
  * total device ms (start to end of the run), per-stage ms in stage order
  * seed, anchor, chain, dp_small, dp_large, stitch, rows, count (8 entries,
@@ -194,7 +203,7 @@ int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int
  * 39-50) against the index's center: anchors of one center on the forward
  * strand with span = the index's k, as collect_anchors makes them on the
  * align-to-center path.  The anchors are sorted as chainAnchors sorts them
- * (the reference sorts the caller's vector in place; here the input arrays are
+ * (globalAlignMM2 takes them const and chains a copy; the input arrays are
  * left untouched).  Returns the CIGAR length, or -status.  *status gets the
  * HG_ST_* bits (partial CIGAR / length mismatch as in hg_align_query). */
 int64_t hg_global_align_mm2(hg_index_t* ix, const char* qry, int64_t qlen, const uint32_t* anchor_ref,

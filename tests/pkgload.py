@@ -22,7 +22,8 @@ def load_package():
     mod = importlib.util.module_from_spec(spec)
     sys.modules["halign_gb300"] = mod
     spec.loader.exec_module(mod)
-    import halign_gb300.serve  # noqa: F401  (attach the submodules)
+    import halign_gb300.autotune  # noqa: F401  (attach the submodules)
+    import halign_gb300.serve  # noqa: F401
     import halign_gb300.shard  # noqa: F401
     import halign_gb300.synth  # noqa: F401
     return mod
