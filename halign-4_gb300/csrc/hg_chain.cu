@@ -78,15 +78,97 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         int32_t* f = b.a_f + base;
         int32_t* p = b.a_p + base;
         int32_t* t = b.a_t + base;
-        for (int i = lane; i < A; i += 32) t[i] = -1;
+        // ---- speculation: every anchor's predecessor is the previous anchor.
+        // Then f is a (max, +) scan, f_i = max(span, f_{i-1} + s_i) with
+        // s_i = score(i-1 -> i) (-inf when i-1 is not a candidate of i), and
+        // p_i = i-1 exactly when f_{i-1} + s_i > span.  Anchors go in chunks
+        // of 32 (lane l takes anchor 32c + l, so loads are coalesced): a warp
+        // scan composes the steps x -> max(span, x + s) and applies them to the
+        // last f of the previous chunk.
+        constexpr int64_t kNeg = -((int64_t)1 << 40);
+        int64_t carry = kNeg;
+        for (int c0 = 0; c0 < A; c0 += 32) {
+            const int i = c0 + lane;
+            int64_t sv = kNeg;
+            if (i > 0 && i < A) {
+                const uint32_t ri = ar[i], rj = ar[i - 1];
+                if ((int32_t)(ri - rj) <= ix.max_dist_x) {  // i-1 inside the window of i
+                    const int32_t sc = chain_score(ix, lg2, ri, aq[i], rj, aq[i - 1], span);
+                    if (sc != INT32_MIN) sv = sc;
+                }
+            }
+            int64_t fa = i < A ? (int64_t)span : kNeg, fb = i < A ? sv : 0;  // lanes past the end: identity
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {  // inclusive scan: compose left steps first
+                const int64_t la = __shfl_up_sync(FULL, fa, o), lb = __shfl_up_sync(FULL, fb, o);
+                if (lane >= o) fa = max(fa, la + fb), fb = max(lb + fb, 2 * kNeg);
+            }
+            const int64_t fi = max(fa, carry + fb);
+            int64_t fprev = __shfl_up_sync(FULL, fi, 1);
+            if (lane == 0) fprev = carry;
+            if (i < A) {
+                f[i] = (int32_t)fi;
+                p[i] = (sv > kNeg / 2 && fprev + sv > span) ? i - 1 : -1;
+            }
+            carry = __shfl_sync(FULL, fi, 31);
+        }
         __syncwarp();
+        // ---- verification: the reference's candidate scan for every anchor
+        // with the speculated f and p (whose marks then only ever target the
+        // next candidate); lane l takes anchor ib + l; the first anchor whose
+        // result differs ends it
+        int bad = A;
+        for (int ib = 0; ib < A && bad == A; ib += 32) {
+            const int i = ib + lane;
+            int mine = A;
+            if (i > 0 && i < A) {
+                const uint32_t ri = ar[i], qv = aq[i];
+                const int jmin = max(0, i - ix.max_iter);
+                int32_t max_f = span;
+                int max_j = -1, n_skip = 0;
+                bool mark_next = false;
+                for (int j = i - 1; j >= jmin; --j) {
+                    const uint32_t rj = ar[j];
+                    if ((int32_t)(ri - rj) > ix.max_dist_x) break;  // before the window start
+                    const bool marked = mark_next;
+                    mark_next = false;
+                    const int32_t sc = chain_score(ix, lg2, ri, qv, rj, aq[j], span);
+                    if (sc == INT32_MIN) continue;
+                    const int32_t tot = f[j] + sc;
+                    const int32_t pj = p[j];
+                    if (tot > max_f) {
+                        max_f = tot, max_j = j;
+                        if (n_skip > 0) --n_skip;
+                    } else if (marked) {
+                        if (++n_skip > ix.max_skip) break;
+                    }
+                    mark_next = pj == j - 1;
+                }
+                if (max_f != f[i] || max_j != p[i]) mine = i;
+            }
+            bad = __reduce_min_sync(FULL, mine);
+        }
         int st = 0, best = -1;
         int32_t best_f = 0;
+        // ---- fallback from the first anchor the speculation got wrong: the
+        // serial warp scan (register window of the 32 previous anchors)
+        const int k0 = bad;
+        if (k0 < A) {
+            for (int i = lane; i < A; i += 32) t[i] = -1;
+            __syncwarp();
+        }
         // register windows: lane l holds candidate j = i-1-l (position pair,
         // f, p) and the positions of anchor i0 + l of the current 32-anchor block
         uint32_t w_ar = 0, w_aq = 0, nx_ar = 0, nx_aq = 0;
         int32_t w_f = 0, w_p = -1;
-        for (int i = 0; i < A; ++i) {
+        if (k0 < A) {
+            const int j = k0 - 1 - lane;
+            if (j >= 0) w_ar = ar[j], w_aq = aq[j], w_f = f[j], w_p = p[j];
+            const int nb = k0 & ~31;
+            nx_ar = nb + lane < A ? ar[nb + lane] : 0u;
+            nx_aq = nb + lane < A ? aq[nb + lane] : 0u;
+        }
+        for (int i = k0; i < A; ++i) {
             if ((i & 31) == 0) {
                 nx_ar = i + lane < A ? ar[i + lane] : 0u;
                 nx_aq = i + lane < A ? aq[i + lane] : 0u;
@@ -200,7 +282,6 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                     __syncwarp();
                 }
             }
-            if (max_f > best_f) best_f = max_f, best = i;
             // shift the window: lane l takes lane l-1's anchor, lane 0 anchor i
             w_ar = __shfl_up_sync(FULL, w_ar, 1);
             w_aq = __shfl_up_sync(FULL, w_aq, 1);
@@ -208,8 +289,23 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             w_p = __shfl_up_sync(FULL, w_p, 1);
             if (lane == 0) w_ar = ri, w_aq = qv, w_f = max_f, w_p = max_j;
         }
-        if (A > 0 && A - 1 - lane >= 0) f[A - 1 - lane] = w_f, p[A - 1 - lane] = w_p;  // the last window
+        if (k0 < A && A - 1 - lane >= 0) f[A - 1 - lane] = w_f, p[A - 1 - lane] = w_p;  // the last window
         __syncwarp();
+        // best chain end: the first anchor with the largest f (strictly greater
+        // than every earlier one, starting from 0)
+        {
+            int32_t mf = 0;
+            int mi = -1;
+            for (int i = lane; i < A; i += 32) {  // first index of this lane's maximum
+                const int32_t fv = f[i];
+                if (fv > mf) mf = fv, mi = i;
+            }
+            const int32_t gmax = __reduce_max_sync(FULL, mf);
+            const int cand = (gmax > 0 && mf == gmax) ? mi : INT32_MAX;
+            const int gi = __reduce_min_sync(FULL, cand);
+            best_f = gmax;
+            best = gi == INT32_MAX ? -1 : gi;
+        }
         // backtrack: chain (reversed) into t[], read p[] 32 entries at a time
         int c = 0;
         if (!(best_f < ix.min_score || best < 0)) {
