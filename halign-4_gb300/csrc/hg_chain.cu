@@ -127,22 +127,29 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 int32_t max_f = span;
                 int max_j = -1, n_skip = 0;
                 bool mark_next = false;
+                // candidate j's fields, the next candidate's loaded one step ahead
+                uint32_t rj = ar[i - 1], qj = aq[i - 1];
+                int32_t fj = f[i - 1], pj = p[i - 1];
                 for (int j = i - 1; j >= jmin; --j) {
-                    const uint32_t rj = ar[j];
-                    if ((int32_t)(ri - rj) > ix.max_dist_x) break;  // before the window start
+                    const int jn = j > 0 ? j - 1 : 0;
+                    const uint32_t rn = ar[jn], qn = aq[jn];
+                    const int32_t fn = f[jn], pn = p[jn];
+                    const uint32_t rc = rj, qc = qj;
+                    const int32_t fc = fj, pc = pj;
+                    rj = rn, qj = qn, fj = fn, pj = pn;
+                    if ((int32_t)(ri - rc) > ix.max_dist_x) break;  // before the window start
                     const bool marked = mark_next;
                     mark_next = false;
-                    const int32_t sc = chain_score(ix, lg2, ri, qv, rj, aq[j], span);
+                    const int32_t sc = chain_score(ix, lg2, ri, qv, rc, qc, span);
                     if (sc == INT32_MIN) continue;
-                    const int32_t tot = f[j] + sc;
-                    const int32_t pj = p[j];
+                    const int32_t tot = fc + sc;
                     if (tot > max_f) {
                         max_f = tot, max_j = j;
                         if (n_skip > 0) --n_skip;
                     } else if (marked) {
                         if (++n_skip > ix.max_skip) break;
                     }
-                    mark_next = pj == j - 1;
+                    mark_next = pc == j - 1;
                 }
                 if (max_f != f[i] || max_j != p[i]) mine = i;
             }
