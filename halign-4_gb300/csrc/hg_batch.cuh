@@ -15,8 +15,8 @@ struct IndexDev {
     const uint8_t* center;     // DNA5 codes of the center the DP aligns to
     const uint8_t* center2;    // the same center 2-bit packed (base i at bits 2(i&3) of byte i>>2), 64 B slack
     int center_plain;          // 1 when every center code is A/C/G/T (center2 is exact)
-    const uint64_t* tab_key;   // open-addressing table: key = hash56 (kNoHash = empty)
-    const uint32_t* tab_val;   // entry id of the key
+    const ulonglong2* tab;     // open-addressing table, one 16-byte slot per probe:
+                               // {key = hash56 (kNoHash = empty), entry id of the key}
     uint32_t tab_mask;
     uint32_t n_ent;            // distinct center minimizer hashes
     const uint32_t* ent_start; // into cpos
@@ -216,8 +216,9 @@ __device__ __forceinline__ uint32_t index_find(const IndexDev& ix, uint64_t h)
 {
     uint32_t s = (uint32_t)h & ix.tab_mask;
     for (;;) {
-        const uint64_t kk = ix.tab_key[s];
-        if (kk == h) return ix.tab_val[s];
+        const ulonglong2 e = ix.tab[s];
+        const uint64_t kk = e.x;
+        if (kk == h) return (uint32_t)e.y;
         if (kk == kNoHash) return kEmptyKey;
         s = (s + 1) & ix.tab_mask;
     }

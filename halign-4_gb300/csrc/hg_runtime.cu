@@ -119,8 +119,8 @@ struct hg_index {
     uint64_t occ_thr = 0;
     int64_t n_hits = 0;
     DevBuf<uint8_t> center, center2;
-    DevBuf<uint64_t> tab_key;
-    DevBuf<uint32_t> tab_val, ent_start, ent_count, cpos, cspan;
+    DevBuf<ulonglong2> tab;
+    DevBuf<uint32_t> ent_start, ent_count, cpos, cspan;
     DevBuf<uint8_t> ent_over;
     DevBuf<float> log2tab;
     hg::IndexDev dev{};
@@ -548,6 +548,8 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
         while (tkey[s] != hg::kNoHash) s = (s + 1) & (tsize - 1);
         tkey[s] = ekey[e], tval[s] = (uint32_t)e;
     }
+    std::vector<ulonglong2> tab(tsize);
+    for (uint32_t i = 0; i < tsize; ++i) tab[i].x = tkey[i], tab[i].y = tval[i];
     // DP center (consensus of the single record) in DNA5 codes
     std::vector<uint8_t> cdp((size_t)len);
     for (int64_t i = 0; i < len; ++i) cdp[i] = hg::dna5_of(consensus_letter((uint8_t)center[i]));
@@ -569,7 +571,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
                          : cudaMemcpy(buf.p, v.data(), sizeof(v[0]) * v.size(), cudaMemcpyHostToDevice);
     };
     cudaError_t e = cudaSuccess;
-    if ((e = up(ix->center, cdp)) || (e = up(ix->center2, c2)) || (e = up(ix->tab_key, tkey)) || (e = up(ix->tab_val, tval)) ||
+    if ((e = up(ix->center, cdp)) || (e = up(ix->center2, c2)) || (e = up(ix->tab, tab)) ||
         (e = up(ix->ent_start, est)) || (e = up(ix->ent_count, ecnt)) || (e = up(ix->ent_over, over)) ||
         (e = up(ix->cpos, cpos)) || (e = up(ix->cspan, cspan)) || (e = up(ix->log2tab, lg))) {
         delete ix;
@@ -578,7 +580,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     hg::IndexDev& d = ix->dev;
     d.L = (int)len, d.k = k, d.w = w, d.non_canonical = 1;
     d.center = ix->center.p, d.center2 = ix->center2.p, d.center_plain = cplain;
-    d.tab_key = ix->tab_key.p, d.tab_val = ix->tab_val.p, d.tab_mask = tsize - 1;
+    d.tab = ix->tab.p, d.tab_mask = tsize - 1;
     d.n_ent = (uint32_t)ekey.size();
     d.ent_start = ix->ent_start.p, d.ent_count = ix->ent_count.p, d.ent_over = ix->ent_over.p;
     d.cpos = ix->cpos.p, d.cspan = ix->cspan.p;
@@ -610,7 +612,7 @@ extern "C" void hg_index_destroy(hg_index_t* ix)
 {
     if (!ix) return;
     if (ix->single) hg_ctx_destroy(ix->single);
-    ix->center.free(), ix->tab_key.free(), ix->tab_val.free(), ix->ent_start.free(), ix->ent_count.free();
+    ix->center.free(), ix->tab.free(), ix->ent_start.free(), ix->ent_count.free();
     ix->ent_over.free(), ix->cpos.free(), ix->cspan.free(), ix->log2tab.free(), ix->center2.free();
     delete ix;
 }
