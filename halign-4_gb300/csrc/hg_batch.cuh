@@ -43,7 +43,16 @@ struct Seg {
     uint32_t kind;            // low byte: SegKind; bit 8: left-aligned gaps (first segment)
 };
 
-enum SegKind : uint32_t { kSegEmpty = 0, kSegIns = 1, kSegDel = 2, kSegDpSmall = 3, kSegDpLarge = 4, kSegGlobal = 5 };
+enum SegKind : uint32_t {
+    kSegEmpty = 0, kSegIns = 1, kSegDel = 2, kSegDpSmall = 3, kSegDpLarge = 4, kSegGlobal = 5,
+    kSegMatch = 6  // equal lengths, identical A/C/G/T on both sides: the extz2 CIGAR is rl M
+};
+
+// True for the gap-fill kinds that run an extz2 DP (and own a CIGAR slot).
+__host__ __device__ __forceinline__ bool seg_is_dp(uint32_t kind)
+{
+    return kind == kSegDpSmall || kind == kSegDpLarge || kind == kSegGlobal;
+}
 constexpr uint32_t kSegLeft = 1u << 8;
 
 // Small-DP tier: one thread per segment, direction nibbles in shared memory,

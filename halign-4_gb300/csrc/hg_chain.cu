@@ -351,6 +351,24 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         // empty segments (both lengths 0) contribute no op: only the others
         // are stored, in order
         uint32_t rpos = 0, qpos = 0, slot = 0, nkept = 0;
+        // Equal-length segments whose sides are identical A/C/G/T strings (the
+        // span of an exact k-mer anchor after overlap clipping) align as rl M:
+        // the diagonal scores 5 rl, any other path needs an insertion and a
+        // deletion (>= 16 in gap costs) and has fewer matches, so every
+        // diagonal cell's direction is M and the traceback from the corner
+        // follows it.  Checked on 2-bit words of the query and the center.
+        const bool plain = ix.center_plain && b.exc_off[q] == b.exc_off[q + 1];
+        const uint64_t qbase = (uint64_t)b.poff[q] * 4u;
+        auto same_bases = [&](uint64_t qp, uint32_t rp, uint32_t n) -> bool {
+            auto window = [](const uint8_t* pk, uint64_t pos) -> uint64_t {
+                const uint64_t wb = (pos >> 2) & ~(uint64_t)7;
+                const uint64_t* w = reinterpret_cast<const uint64_t*>(pk + wb);
+                const uint32_t sh = 2u * (uint32_t)(pos - wb * 4u);
+                return sh ? (w[0] >> sh) | (w[1] << (64u - sh)) : w[0];
+            };
+            const uint64_t m = n >= 32 ? ~0ull : ((1ull << (2 * n)) - 1ull);
+            return ((window(b.packed, qp) ^ window(ix.center2, rp)) & m) == 0;
+        };
         for (int s0 = 0; s0 < nseg; s0 += 32) {
             const int s = s0 + lane;
             const bool act = s < nseg;
@@ -385,14 +403,23 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             else if (rl == 0) kind = kSegIns;
             else if (ql == 0) kind = kSegDel;
             else if (c == 0) kind = kSegGlobal;
+            else if (rl == ql && rl <= 32 && plain && same_bases(qbase + qs, rs, rl))
+                kind = kSegMatch;  // identical equal-length sides: the DP's CIGAR is rl M
             else if (small_tier_fits(rl, ql))
                 kind = kSegDpSmall;
             else
                 kind = kSegDpLarge;
+            // the reference runs extz2 on a match segment too (full band: rl x rl
+            // cells); count them so the cell total stays the reference's work unit
+            if (b.cells) {
+                const unsigned long long mc = act && kind == kSegMatch ? (unsigned long long)rl * rl : 0ull;
+                const unsigned long long tot = __reduce_add_sync(FULL, (unsigned)mc);
+                if (lane == 0 && tot) atomicAdd(b.cells, tot);
+            }
             const bool keep = act && kind != kSegEmpty;
             const unsigned kmask = __ballot_sync(FULL, keep);
             const uint32_t sid = (uint32_t)sb + nkept + (uint32_t)__popc(kmask & ((1u << lane) - 1u));
-            const uint32_t need = (kind >= kSegDpSmall && act) ? rl + ql : 0;
+            const uint32_t need = (seg_is_dp(kind) && act) ? rl + ql : 0;
             const uint32_t sincl = warp_incl_sum(need);
             const uint32_t my_slot = slot + sincl - need;
             if (keep) {

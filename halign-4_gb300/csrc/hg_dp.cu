@@ -163,10 +163,12 @@ __device__ __forceinline__ void load_bases64(const uint8_t* pk, uint64_t pos, ui
 // query has no exception bytes and the center is all A/C/G/T, so both sides
 // come from 2-bit packed words held in registers.  The traceback writes each
 // op run once, last-first (the stitch reads small-tier segments backwards).
-template <bool TINNER, int MODE, bool FAST>
+template <bool TINNER, int MODE, bool FAST, int IMAX>
 __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev& b, const SmallRec& r,
                                               uint32_t* dirs, int tid)
 {
+    // IMAX: unroll bound of the inner side (4, 8 or 16 >= inner), so short
+    // segments do not pay for 16 guarded columns per row
     const int qn = (int)((r.shape >> 8) & 0xffu), tn = (int)(r.shape & 0xffu);
     const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
     const int stride = (inner + 7) >> 3;
@@ -176,7 +178,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     const int64_t e0 = FAST ? 0 : b.exc_off[r.q], e1 = FAST ? 0 : b.exc_off[r.q + 1];
     const bool plain_q = e0 == e1;
     const uint8_t* tc = ix.center + r.rs;
-    int ic[kSmallMaxInner], s1[kSmallMaxInner], s2[kSmallMaxInner];
+    int ic[IMAX], s1[IMAX], s2[IMAX];
     uint64_t olo = 0, ohi = 0;
     if (FAST) {
         uint64_t qlo, qhi, tlo, thi;
@@ -186,10 +188,10 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         olo = TINNER ? qlo : tlo;
         ohi = TINNER ? qhi : thi;
 #pragma unroll
-        for (int i = 0; i < kSmallMaxInner; ++i) ic[i] = (int)((ilo >> (2 * i)) & 3u);
+        for (int i = 0; i < IMAX; ++i) ic[i] = (int)((ilo >> (2 * i)) & 3u);
     } else {
 #pragma unroll
-        for (int i = 0; i < kSmallMaxInner; ++i) {
+        for (int i = 0; i < IMAX; ++i) {
             ic[i] = 0;
             if (i < inner) {
                 if (TINNER) ic[i] = tc[i];
@@ -198,7 +200,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         }
     }
 #pragma unroll
-    for (int i = 0; i < kSmallMaxInner; ++i) s1[i] = 0, s2[i] = 0;
+    for (int i = 0; i < IMAX; ++i) s1[i] = 0, s2[i] = 0;
     for (int o = 0; o < outer; ++o) {
         int oc;
         if (FAST) {
@@ -212,7 +214,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         int c1 = 0, c2 = o ? 6 : 0;
         uint32_t w0 = 0, w1 = 0;
 #pragma unroll
-        for (int i = 0; i < kSmallMaxInner; ++i) {
+        for (int i = 0; i < IMAX; ++i) {
             if (i < inner) {
                 const int z0 = FAST ? (ic[i] == oc ? 21 : 12)
                                     : ((ic[i] == 4 || oc == 4) ? 16 : (ic[i] == oc ? 21 : 12));
@@ -229,7 +231,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
                     c1 = u, c2 = y, s1[i] = x, s2[i] = v;
                 }
                 if (i < 8) w0 |= d << (4 * i);
-                else w1 |= d << (4 * (i - 8));
+                else w1 |= d << (4 * (i - 8 < 0 ? 0 : i - 8));
             }
         }
         dirs[(o * stride) * kDpSmallThreads + tid] = w0;
@@ -264,6 +266,19 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     b.seg[r.sid].nops = n;
 }
 
+template <bool FAST, int IMAX>
+__device__ __forceinline__ void small_dispatch(const IndexDev& ix, const BatchDev& b, const SmallRec& r,
+                                               uint32_t* dirs, int tid, bool tinner, bool left)
+{
+    if (tinner) {
+        if (left) small_segment<true, 1, FAST, IMAX>(ix, b, r, dirs, tid);
+        else small_segment<true, 2, FAST, IMAX>(ix, b, r, dirs, tid);
+    } else {
+        if (left) small_segment<false, 1, FAST, IMAX>(ix, b, r, dirs, tid);
+        else small_segment<false, 2, FAST, IMAX>(ix, b, r, dirs, tid);
+    }
+}
+
 __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
 {
     __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
@@ -277,22 +292,13 @@ __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, 
         const uint32_t rl = r.shape & 0xffu, ql = (r.shape >> 8) & 0xffu;
         const bool tinner = rl <= ql;
         const bool left = (r.shape & kRecLeft) != 0;
+        const uint32_t inner = tinner ? rl : ql;
         if (r.shape & kRecFast) {
-            if (tinner) {
-                if (left) small_segment<true, 1, true>(ix, b, r, dirs, tid);
-                else small_segment<true, 2, true>(ix, b, r, dirs, tid);
-            } else {
-                if (left) small_segment<false, 1, true>(ix, b, r, dirs, tid);
-                else small_segment<false, 2, true>(ix, b, r, dirs, tid);
-            }
+            if (inner <= 4) small_dispatch<true, 4>(ix, b, r, dirs, tid, tinner, left);
+            else if (inner <= 8) small_dispatch<true, 8>(ix, b, r, dirs, tid, tinner, left);
+            else small_dispatch<true, 16>(ix, b, r, dirs, tid, tinner, left);
         } else {
-            if (tinner) {
-                if (left) small_segment<true, 1, false>(ix, b, r, dirs, tid);
-                else small_segment<true, 2, false>(ix, b, r, dirs, tid);
-            } else {
-                if (left) small_segment<false, 1, false>(ix, b, r, dirs, tid);
-                else small_segment<false, 2, false>(ix, b, r, dirs, tid);
-            }
+            small_dispatch<false, 16>(ix, b, r, dirs, tid, tinner, left);
         }
         cell_sum += (unsigned long long)(rl * ql);
     }

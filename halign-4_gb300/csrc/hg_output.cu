@@ -63,8 +63,8 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
                 const uint32_t kind = g.kind & 0xffu;
                 s_kind[wib][lane] = kind, s_slot[wib][lane] = g.slot, s_rl[wib][lane] = g.rl, s_ql[wib][lane] = g.ql;
                 s_nops[wib][lane] = g.nops;
-                if (kind == kSegIns || kind == kSegDel) cnt = 1;
-                else if (kind >= kSegDpSmall) cnt = g.nops < 0 ? 2u : (uint32_t)g.nops;
+                if (kind == kSegIns || kind == kSegDel || kind == kSegMatch) cnt = 1;
+                else if (seg_is_dp(kind)) cnt = g.nops < 0 ? 2u : (uint32_t)g.nops;
                 if (kind == kSegGlobal) global_seg = true;
             }
             const uint32_t incl = warp_incl_sum(cnt);
@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
                     const uint32_t kind = s_kind[wib][lo];
                     if (kind == kSegIns) op = 1, len = s_ql[wib][lo];
                     else if (kind == kSegDel) op = 2, len = s_rl[wib][lo];
+                    else if (kind == kSegMatch) op = 0, len = s_rl[wib][lo];
                     else if (s_nops[wib][lo] < 0) {  // forced I(q) D(t) (src/align/align.cpp:248-256)
                         if (rel == 0) op = 1, len = s_ql[wib][lo];
                         else op = 2, len = s_rl[wib][lo];
