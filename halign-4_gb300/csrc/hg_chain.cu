@@ -315,7 +315,17 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         }
         // backtrack: chain (reversed) into t[], read p[] 32 entries at a time
         int c = 0;
-        if (!(best_f < ix.min_score || best < 0)) {
+        if (!(best_f < ix.min_score || best < 0) && k0 == A) {
+            // speculation held: every p is i-1 or -1, so the chain is the run
+            // [s, best] with s the last anchor at or before best whose p is -1
+            int sl = -1;
+            for (int i = lane; i <= best; i += 32)
+                if (p[i] < 0) sl = i;
+            const int s0 = __reduce_max_sync(FULL, sl);
+            c = best - s0 + 1;
+            for (int m = lane; m < c; m += 32) t[m] = best - m;
+            if (c < ix.min_cnt) c = 0;
+        } else if (!(best_f < ix.min_score || best < 0)) {
             int cur = best;
             while (cur >= 0) {
                 const int lo = max(cur - 31, 0);
