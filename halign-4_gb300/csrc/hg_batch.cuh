@@ -56,29 +56,42 @@ __host__ __device__ __forceinline__ bool seg_is_dp(uint32_t kind)
 constexpr uint32_t kSegLeft = 1u << 8;
 
 // Small-DP tier: one thread per segment, direction nibbles in shared memory,
-// one or two 32-bit words per row of the longer side.
+// one to four 32-bit words per row of the longer side.  Two shape ranges:
+// small (shorter side <= 16, rows x words <= 64) and medium (shorter side
+// 17..32, rows x words <= 160); both are far inside the band
+// globalAlignKSW2 gives them (w >= 200 or unbounded), so the band never binds.
 constexpr int kSmallMaxInner = 16;
-constexpr int kSmallDirWords = 64;  // words of 8 nibbles per thread
+constexpr int kSmallDirWords = 64;   // words of 8 nibbles per thread, small range
+constexpr int kMedMaxInner = 32;
+constexpr int kMedDirWords = 160;    // words per thread, medium range
 
-// A segment fits the small tier when its shorter side is <= 16 and its rows
-// (longer side) x words-per-row fit the thread's direction store.  Such
-// segments are at most 64 bp long, far inside the band globalAlignKSW2 gives
-// them (w >= 200 or unbounded), so the band never binds.
 __host__ __device__ __forceinline__ bool small_tier_fits(uint32_t rl, uint32_t ql)
 {
     const uint32_t inner = rl < ql ? rl : ql, outer = rl < ql ? ql : rl;
     return inner >= 1 && inner <= (uint32_t)kSmallMaxInner && outer * ((inner + 7) / 8) <= (uint32_t)kSmallDirWords;
 }
 
+__host__ __device__ __forceinline__ bool medium_tier_fits(uint32_t rl, uint32_t ql)
+{
+    const uint32_t inner = rl < ql ? rl : ql, outer = rl < ql ? ql : rl;
+    return inner > (uint32_t)kSmallMaxInner && inner <= (uint32_t)kMedMaxInner &&
+           outer * ((inner + 7) / 8) <= (uint32_t)kMedDirWords;
+}
+
 // Sort key of a small-tier segment: warps then run identical loop bounds.
-// Bits: [0,7) outer-1 (<= 63), [7,11) inner-1, 11 orientation, 12 left-aligned.
+// Both ranges keep the longer side <= 64 (rows x words bound), so the key is
+// [0,6) outer-1, [6,10) inner-1 (small) or inner-17 (medium), 10 orientation,
+// 11 left-aligned, 12 medium range (sorts after every small shape).
 constexpr uint32_t kShapeBins = 1u << 13;
+constexpr uint32_t kShapeMedium = 1u << 12;
 __device__ __forceinline__ uint32_t shape_key(const Seg& g)
 {
     const uint32_t inner = g.rl < g.ql ? g.rl : g.ql, outer = g.rl < g.ql ? g.ql : g.rl;
     const uint32_t tinner = g.rl <= g.ql ? 1u : 0u;
     const uint32_t left = (g.kind & kSegLeft) ? 1u : 0u;
-    return (outer - 1) | (inner - 1) << 7 | tinner << 11 | left << 12;
+    const uint32_t med = inner > (uint32_t)kSmallMaxInner ? 1u : 0u;
+    const uint32_t icode = med ? inner - 17u : inner - 1u;
+    return (outer - 1) | icode << 6 | tinner << 10 | left << 11 | med << 12;
 }
 
 // Wavefront tiers: segments the band never binds (auto_band < 0 or >= both
@@ -215,7 +228,7 @@ struct BatchDev {
     uint32_t* ins;               // L + 1 insertion events
     uint32_t* status;            // per query
     unsigned int* queues;        // work-queue heads, one per stage
-    unsigned int* queues2;       // more work-queue heads: [0] seed fast path
+    unsigned int* queues2;       // more work-queue heads: [0] seed fast path; [1] start of the medium small-tier records
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };

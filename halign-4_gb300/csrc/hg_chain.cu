@@ -415,7 +415,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             else if (c == 0) kind = kSegGlobal;
             else if (rl == ql && rl <= 32 && plain && same_bases(qbase + qs, rs, rl))
                 kind = kSegMatch;  // identical equal-length sides: the DP's CIGAR is rl M
-            else if (small_tier_fits(rl, ql))
+            else if (small_tier_fits(rl, ql) || medium_tier_fits(rl, ql))
                 kind = kSegDpSmall;
             else
                 kind = kSegDpLarge;

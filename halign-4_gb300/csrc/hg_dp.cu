@@ -163,12 +163,14 @@ __device__ __forceinline__ void load_bases64(const uint8_t* pk, uint64_t pos, ui
 // query has no exception bytes and the center is all A/C/G/T, so both sides
 // come from 2-bit packed words held in registers.  The traceback writes each
 // op run once, last-first (the stitch reads small-tier segments backwards).
-template <bool TINNER, int MODE, bool FAST, int IMAX>
+template <bool TINNER, int MODE, bool FAST, int IMAX, int T>
 __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev& b, const SmallRec& r,
                                               uint32_t* dirs, int tid)
 {
-    // IMAX: unroll bound of the inner side (4, 8 or 16 >= inner), so short
-    // segments do not pay for 16 guarded columns per row
+    // IMAX: unroll bound of the inner side (4, 8, 16 or 32 >= inner), so short
+    // segments do not pay for wider guarded rows; T: threads per CTA (the
+    // direction words of a row are interleaved across them)
+    constexpr int NW = (IMAX + 7) / 8;  // direction words per row at most
     const int qn = (int)((r.shape >> 8) & 0xffu), tn = (int)(r.shape & 0xffu);
     const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
     const int stride = (inner + 7) >> 3;
@@ -212,7 +214,9 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
         // TINNER: carried x, v along the row, s1/s2 = u, y of the previous row.
         // !TINNER: carried u, y along the column, s1/s2 = x, v of the previous column.
         int c1 = 0, c2 = o ? 6 : 0;
-        uint32_t w0 = 0, w1 = 0;
+        uint32_t wd[NW];
+#pragma unroll
+        for (int k = 0; k < NW; ++k) wd[k] = 0;
 #pragma unroll
         for (int i = 0; i < IMAX; ++i) {
             if (i < inner) {
@@ -230,12 +234,12 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
                     d = lane_int_z<MODE>(z0, xt, vt, ut, yt, u, v, x, y);
                     c1 = u, c2 = y, s1[i] = x, s2[i] = v;
                 }
-                if (i < 8) w0 |= d << (4 * i);
-                else w1 |= d << (4 * (i - 8 < 0 ? 0 : i - 8));
+                wd[i >> 3] |= d << (4 * (i & 7));
             }
         }
-        dirs[(o * stride) * kDpSmallThreads + tid] = w0;
-        if (stride > 1) dirs[(o * stride + 1) * kDpSmallThreads + tid] = w1;
+#pragma unroll
+        for (int k = 0; k < NW; ++k)
+            if (k < stride) dirs[(o * stride + k) * T + tid] = wd[k];
     }
     // traceback from (tlen-1, qlen-1); runs written once, last-first
     uint32_t* out = b.cig_seg + r.out;
@@ -252,7 +256,7 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     int ti = tn - 1, qj = qn - 1, state = 0;
     while (ti >= 0 && qj >= 0) {
         const int o = TINNER ? qj : ti, i = TINNER ? ti : qj;
-        const uint32_t nib = (dirs[(o * stride + (i >> 3)) * kDpSmallThreads + tid] >> ((i & 7) * 4)) & 0xfu;
+        const uint32_t nib = (dirs[(o * stride + (i >> 3)) * T + tid] >> ((i & 7) * 4)) & 0xfu;
         if (state == 0) state = nib & 3u;
         else if (!((nib >> (state + 1)) & 1u)) state = 0;
         if (state == 0) state = nib & 3u;
@@ -266,16 +270,16 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     b.seg[r.sid].nops = n;
 }
 
-template <bool FAST, int IMAX>
+template <bool FAST, int IMAX, int T>
 __device__ __forceinline__ void small_dispatch(const IndexDev& ix, const BatchDev& b, const SmallRec& r,
                                                uint32_t* dirs, int tid, bool tinner, bool left)
 {
     if (tinner) {
-        if (left) small_segment<true, 1, FAST, IMAX>(ix, b, r, dirs, tid);
-        else small_segment<true, 2, FAST, IMAX>(ix, b, r, dirs, tid);
+        if (left) small_segment<true, 1, FAST, IMAX, T>(ix, b, r, dirs, tid);
+        else small_segment<true, 2, FAST, IMAX, T>(ix, b, r, dirs, tid);
     } else {
-        if (left) small_segment<false, 1, FAST, IMAX>(ix, b, r, dirs, tid);
-        else small_segment<false, 2, FAST, IMAX>(ix, b, r, dirs, tid);
+        if (left) small_segment<false, 1, FAST, IMAX, T>(ix, b, r, dirs, tid);
+        else small_segment<false, 2, FAST, IMAX, T>(ix, b, r, dirs, tid);
     }
 }
 
@@ -283,7 +287,7 @@ __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, 
 {
     __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
     const int tid = threadIdx.x;
-    const unsigned total = min(*b.n_small, (unsigned)b.wcap);
+    const unsigned total = min(b.queues2[1], min(*b.n_small, (unsigned)b.wcap));  // small shapes only
     unsigned long long cell_sum = 0;
     const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
     for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
@@ -294,12 +298,41 @@ __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, 
         const bool left = (r.shape & kRecLeft) != 0;
         const uint32_t inner = tinner ? rl : ql;
         if (r.shape & kRecFast) {
-            if (inner <= 4) small_dispatch<true, 4>(ix, b, r, dirs, tid, tinner, left);
-            else if (inner <= 8) small_dispatch<true, 8>(ix, b, r, dirs, tid, tinner, left);
-            else small_dispatch<true, 16>(ix, b, r, dirs, tid, tinner, left);
+            if (inner <= 4) small_dispatch<true, 4, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+            else if (inner <= 8) small_dispatch<true, 8, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+            else small_dispatch<true, 16, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
         } else {
-            small_dispatch<false, 16>(ix, b, r, dirs, tid, tinner, left);
+            small_dispatch<false, 16, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
         }
+        cell_sum += (unsigned long long)(rl * ql);
+    }
+    for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
+    if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
+}
+
+// Medium shapes of the small tier (shorter side 17..32): the same thread-
+// per-segment DP with up to four direction words per row, 64 threads per CTA
+// so the per-thread store (kMedDirWords) fits shared memory.  Its records
+// follow every small shape in the sorted list.
+constexpr int kDpMedThreads = 64;
+
+__global__ void __launch_bounds__(kDpMedThreads) dp_medium_kernel(IndexDev ix, BatchDev b)
+{
+    __shared__ uint32_t dirs[kMedDirWords * kDpMedThreads];
+    const int tid = threadIdx.x;
+    const unsigned total = min(*b.n_small, (unsigned)b.wcap);
+    const unsigned first = min(b.queues2[1], total);
+    unsigned long long cell_sum = 0;
+    const unsigned span = ((total - first) + 31u) & ~31u;
+    for (unsigned k = blockIdx.x * kDpMedThreads + tid; k < span; k += gridDim.x * kDpMedThreads) {
+        const unsigned w = first + k;
+        if (w >= total) continue;
+        const SmallRec r = b.work_rec[w];
+        const uint32_t rl = r.shape & 0xffu, ql = (r.shape >> 8) & 0xffu;
+        const bool tinner = rl <= ql;
+        const bool left = (r.shape & kRecLeft) != 0;
+        if (r.shape & kRecFast) small_dispatch<true, 32, kDpMedThreads>(ix, b, r, dirs, tid, tinner, left);
+        else small_dispatch<false, 32, kDpMedThreads>(ix, b, r, dirs, tid, tinner, left);
         cell_sum += (unsigned long long)(rl * ql);
     }
     for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
@@ -326,6 +359,7 @@ __global__ void shape_scan_kernel(BatchDev b)
     uint32_t run = part[tid] - s;
     for (int i = 0; i < per; ++i) {
         const uint32_t c = b.shape_hist[tid * per + i];
+        if ((uint32_t)(tid * per + i) == kShapeMedium) b.queues2[1] = run;  // first medium record
         b.shape_hist[kShapeBins + tid * per + i] = run;  // cursor = bucket start
         run += c;
     }
@@ -1199,6 +1233,7 @@ extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::Batc
     hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
     hg::shape_scatter_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kScatterThreads, hg::kScatterSmem, st>>>(*ix, *b);
     hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);
+    hg::dp_medium_kernel<<<grid, hg::kDpMedThreads, 0, st>>>(*ix, *b);
     return cudaGetLastError();
 }
 

@@ -635,10 +635,10 @@ constexpr int kControlWords = 16;
 // queues2[4]
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
 constexpr int kWaveBlocksPerSm = 4;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
-// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 3, dp_wave 2, dp_wide,
+// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, dp_wave 2, dp_wide,
 // dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
-constexpr int kLaunchesBatch = 17;
-constexpr int kLaunchesPlain = 16;
+constexpr int kLaunchesBatch = 18;
+constexpr int kLaunchesPlain = 17;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
