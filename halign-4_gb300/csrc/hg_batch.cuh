@@ -45,13 +45,14 @@ struct Seg {
 
 enum SegKind : uint32_t {
     kSegEmpty = 0, kSegIns = 1, kSegDel = 2, kSegDpSmall = 3, kSegDpLarge = 4, kSegGlobal = 5,
-    kSegMatch = 6  // equal lengths, identical A/C/G/T on both sides: the extz2 CIGAR is rl M
+    kSegMatch = 6,  // equal lengths, identical A/C/G/T on both sides: the extz2 CIGAR is rl M
+    kSegDpThin = 7  // query side <= 16, long center side: grouped wavefront, ops stored last-first
 };
 
 // True for the gap-fill kinds that run an extz2 DP (and own a CIGAR slot).
 __host__ __device__ __forceinline__ bool seg_is_dp(uint32_t kind)
 {
-    return kind == kSegDpSmall || kind == kSegDpLarge || kind == kSegGlobal;
+    return kind == kSegDpSmall || kind == kSegDpLarge || kind == kSegGlobal || kind == kSegDpThin;
 }
 constexpr uint32_t kSegLeft = 1u << 8;
 
@@ -92,6 +93,38 @@ __device__ __forceinline__ uint32_t shape_key(const Seg& g)
     const uint32_t med = inner > (uint32_t)kSmallMaxInner ? 1u : 0u;
     const uint32_t icode = med ? inner - 17u : inner - 1u;
     return (outer - 1) | icode << 6 | tinner << 10 | left << 11 | med << 12;
+}
+
+// Thin tier: the query side 1..16 bases against a center side beyond the
+// small and medium bounds (so more than twice as long, and auto_band gives an
+// unbounded band).  Several such segments share a warp, one lane per query
+// column: a group of W = 4, 8 or 16 lanes runs one segment's anti-diagonal
+// wavefront, so a step costs one cell per lane however short the query side
+// is.  Direction nibbles go to a two-slot scratch region per warp, which
+// bounds the steps (rl + ql - 1) of a thin segment.
+constexpr int kThinMaxInner = 16;
+constexpr int kThinBins = 512;       // sort bins of the thin list (key < 3 << 7)
+constexpr int kThinKeyClassShift = 7;  // key bits above it: the group width class
+
+__host__ __device__ __forceinline__ int thin_width_class(uint32_t inner) { return inner <= 4 ? 0 : inner <= 8 ? 1 : 2; }
+
+__host__ __device__ __forceinline__ bool thin_tier_fits(uint32_t rl, uint32_t ql, int64_t slot_bytes)
+{
+    if (ql < 1 || ql > (uint32_t)kThinMaxInner || rl <= ql || small_tier_fits(rl, ql)) return false;
+    return ((int64_t)rl + ql - 1) * 16 <= 2 * slot_bytes;  // 16 bytes of direction nibbles per warp step
+}
+
+// Sort key of a thin segment: group width class first (a warp takes
+// segments of one class), then longest first by quarter-octave class of the
+// center side, then gap mode.
+__host__ __device__ __forceinline__ uint32_t thin_key(uint32_t rl, uint32_t ql, bool left)
+{
+    uint32_t lg = 0;
+    for (uint32_t t = rl; t > 1; t >>= 1) ++lg;  // floor(log2(rl)), rl >= 33
+    const uint32_t frac = lg >= 2 ? (rl >> (lg - 2)) & 3u : 0u;
+    uint32_t cls = lg >= 5 ? (lg - 5) * 4 + frac : 0u;
+    cls = cls > 63 ? 63 : cls;
+    return (uint32_t)thin_width_class(ql) << kThinKeyClassShift | (63u - cls) << 1 | (left ? 0u : 1u);
 }
 
 // Wavefront tiers: segments the band never binds (auto_band < 0 or >= both
@@ -207,6 +240,12 @@ struct BatchDev {
     uint32_t* work_wide;         // CTA wavefront tier
     unsigned int* n_wave;
     unsigned int* n_wide;
+    uint32_t* work_thin;         // thin tier: segment ids, keys, sorted ids
+    uint32_t* work_thin_key;
+    uint32_t* work_thin_sorted;
+    uint32_t* thin_hist;         // kThinBins counters, then kThinBins cursors
+    unsigned int* n_thin;
+    unsigned int* thin_q;        // three queue heads of the thin tier, one per group width class
     int64_t wcap;
     // K6 DP scratch: one reusable slot per large-tier warp, plus a bump arena
     // for segments whose scratch exceeds a slot
@@ -228,7 +267,7 @@ struct BatchDev {
     uint32_t* ins;               // L + 1 insertion events
     uint32_t* status;            // per query
     unsigned int* queues;        // work-queue heads, one per stage
-    unsigned int* queues2;       // more work-queue heads: [0] seed fast path; [1] start of the medium small-tier records
+    unsigned int* queues2;       // [0] seed fast-path queue; [1] start of the medium small-tier records
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };

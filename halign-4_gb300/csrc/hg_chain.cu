@@ -417,6 +417,8 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 kind = kSegMatch;  // identical equal-length sides: the DP's CIGAR is rl M
             else if (small_tier_fits(rl, ql) || medium_tier_fits(rl, ql))
                 kind = kSegDpSmall;
+            else if (thin_tier_fits(rl, ql, b.dp_slot_bytes))
+                kind = kSegDpThin;
             else
                 kind = kSegDpLarge;
             // the reference runs extz2 on a match segment too (full band: rl x rl
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 b.seg[sid] = g;
             }
             nkept += (uint32_t)__popc(kmask);
-            // tier work lists (warp-aggregated appends): small, one-warp
+            // tier work lists (warp-aggregated appends): small, thin, one-warp
             // wavefront, CTA wavefront, exact
             const bool dp_big = act && (kind == kSegDpLarge || kind == kSegGlobal);
             const bool wv = dp_big && wave_eligible(rl, ql);
@@ -451,8 +453,10 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const unsigned ml = __ballot_sync(FULL, dp_big && !wv);
             const unsigned mw = __ballot_sync(FULL, wv_warp);
             const unsigned mx = __ballot_sync(FULL, wv && !wv_warp);
-            unsigned bs = 0, bl = 0, bw = 0, bx = 0;
+            const unsigned mt = __ballot_sync(FULL, act && kind == kSegDpThin);
+            unsigned bs = 0, bl = 0, bw = 0, bx = 0, bt = 0;
             if (lane == 0) {
+                if (mt) bt = atomicAdd(b.n_thin, (unsigned)__popc(mt));
                 if (ms) bs = atomicAdd(b.n_small, (unsigned)__popc(ms));
                 if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
                 if (mw) bw = atomicAdd(b.n_wave, (unsigned)__popc(mw));
@@ -462,6 +466,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             bl = __shfl_sync(FULL, bl, 0);
             bw = __shfl_sync(FULL, bw, 0);
             bx = __shfl_sync(FULL, bx, 0);
+            bt = __shfl_sync(FULL, bt, 0);
             const unsigned below = (1u << lane) - 1u;
             if (ms >> lane & 1u) {
                 const unsigned w = bs + __popc(ms & below);
@@ -511,6 +516,21 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 const unsigned w = bx + __popc(mx & below);
                 if ((int64_t)w < b.wcap) b.work_wide[w] = sid;
                 else atomicOr(&b.status[q], kStArenaOverflow);
+            }
+            uint32_t tkey = 0xffffffffu;  // counted in the histogram only when placed
+            if (mt >> lane & 1u) {
+                const unsigned w = bt + __popc(mt & below);
+                if ((int64_t)w < b.wcap) {
+                    tkey = thin_key(rl, ql, (flags & kSegLeft) != 0);
+                    b.work_thin[w] = sid;
+                    b.work_thin_key[w] = tkey;
+                } else {
+                    atomicOr(&b.status[q], kStArenaOverflow);
+                }
+            }
+            if (mt) {
+                const unsigned peers = __match_any_sync(FULL, tkey);
+                if (tkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.thin_hist[tkey], __popc(peers));
             }
             rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
             qpos = (uint32_t)__shfl_sync(FULL, iq, 31);

@@ -339,6 +339,208 @@ __global__ void __launch_bounds__(kDpMedThreads) dp_medium_kernel(IndexDev ix, B
     if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
 }
 
+// lane_int_z with the gap mode as a value: nl = 0 left-aligned (MODE 1),
+// nl = 1 right-aligned (MODE 2); "> t - 1" is ">= t" for integers.
+__device__ __forceinline__ uint32_t lane_int_nl(int z0, int xt1, int vt1, int ut, int yt, int nl, int& u, int& v,
+                                                int& x, int& y)
+{
+    const int a0 = xt1 + vt1, b0 = yt + ut;
+    const int m = max(z0, a0);
+    uint32_t d = a0 > z0 - nl ? 1u : 0u;
+    if (b0 > m - nl) d = 2u;
+    const int z = min(max(m, b0), 21);
+    u = z - vt1;
+    v = z - ut;
+    const int zq = z - 6;
+    const int a = a0 - zq, b = b0 - zq;
+    x = max(a, 0), y = max(b, 0);
+    d |= (a > -nl ? 4u : 0u) | (b > -nl ? 8u : 0u);
+    return d;
+}
+
+// Thin tier: G = 32 / W segments per warp, lane j of group g owns query
+// column j of the group's segment and computes cell (s - j, j) at step s.
+// A cell takes its left neighbour's outputs of the previous step by one
+// shuffle (u, y and the row's center code, packed), its own previous outputs
+// as the cell above, and lane 0 of a group reads the center base of a new
+// row.  Direction nibbles of 8 steps make one word per lane in the warp's
+// scratch; the traceback copies blocks of kThinBlockSteps steps back to
+// shared memory and each group's lane 0 walks its segment there, writing op
+// runs last-first (as the small tier does).
+constexpr int kThinWarps = 4;
+constexpr int kThinBlockSteps = 1024;
+constexpr int kThinBlockWords = kThinBlockSteps / 8 * 32;  // per warp
+constexpr size_t kThinSmemBytes = (size_t)kThinWarps * kThinBlockWords * sizeof(uint32_t);
+
+template <int W>
+__device__ __forceinline__ void thin_group(const IndexDev& ix, const BatchDev& b, unsigned first, unsigned cnt,
+                                           uint32_t* scratch, uint32_t* buf, unsigned long long& cells)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, j = lane % W, g = lane / W;
+    const bool has = (unsigned)g < cnt;
+    uint32_t sid = 0;
+    Seg sg;
+    sg.rs = sg.qs = sg.rl = sg.ql = sg.slot = sg.q = sg.kind = 0;
+    if (has) {
+        sid = b.work_thin_sorted[first + g];
+        sg = b.seg[sid];
+    }
+    const int inner = (int)sg.ql, outer = (int)sg.rl;
+    const int nl = (sg.kind & kSegLeft) ? 0 : 1;
+    int smax = has ? outer + inner - 1 : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) smax = max(smax, __shfl_xor_sync(FULL, smax, o));
+    // z0 by the row's center code (0..4, at 5 bits each) for this lane's query base
+    uint32_t tab = 0;
+    {
+        int ic = 0;
+        if (has && j < inner) {
+            const uint8_t* pk = b.packed + b.poff[sg.q];
+            const int64_t e0 = b.exc_off[sg.q], e1 = b.exc_off[sg.q + 1];
+            ic = e0 == e1 ? (int)packed_code(pk, sg.qs + j) : (int)query_dna5(pk, b.exc, e0, e1, sg.qs + j);
+        }
+#pragma unroll
+        for (int oc = 0; oc < 5; ++oc) tab |= (uint32_t)((ic == 4 || oc == 4) ? 16 : (ic == oc ? 21 : 12)) << (5 * oc);
+    }
+    const uint8_t* tc = ix.center + sg.rs;
+    int s1 = 0, s2 = j ? 6 : 0;  // x, v of the cell above row 0
+    uint32_t outp = 0;           // u | y << 8 | 5 x center code << 16, toward the right neighbour
+    uint32_t chunk = 0, acc = 0;
+    for (int s = 0; s < smax; ++s) {
+        const int sm = s % W;
+        if (sm == 0) {
+            const int o = s + j;
+            chunk = (has && o < outer) ? 5u * (uint32_t)tc[o] : 0u;
+        }
+        const uint32_t fresh = __shfl_sync(FULL, chunk, g * W + sm);
+        const uint32_t inp = __shfl_up_sync(FULL, outp, 1, W);
+        int c1, c2, c5;
+        if (j == 0) {
+            c1 = s ? 6 : 0, c2 = 0, c5 = (int)fresh;  // left of column 0 on row s
+        } else {
+            c1 = (int)(inp & 0xffu), c2 = (int)((inp >> 8) & 0xffu), c5 = (int)(inp >> 16);
+        }
+        const int o = s - j;
+        const int z0 = (int)((tab >> c5) & 31u);
+        int u, v, x, y;
+        const uint32_t d = lane_int_nl(z0, s1, s2, c1, c2, nl, u, v, x, y);
+        if (o >= 0 && o < outer && j < inner) {
+            s1 = x, s2 = v;
+            outp = (uint32_t)u | (uint32_t)y << 8 | (uint32_t)c5 << 16;
+            acc |= d << (4 * (s & 7));
+        }
+        if ((s & 7) == 7 || s == smax - 1) {
+            scratch[(size_t)(s >> 3) * 32 + lane] = acc;
+            acc = 0;
+        }
+    }
+    __syncwarp();
+    // traceback from (rl-1, ql-1), block by block from the last
+    const bool lead = has && j == 0;
+    uint32_t* out = b.cig_seg + (has ? b.coff[sg.q] + sg.slot : 0);
+    int n = 0;
+    uint32_t run_op = 0xffu, run_len = 0;
+    auto push = [&](uint32_t op, uint32_t len) {
+        if (op == run_op) {
+            run_len += len;
+        } else {
+            if (run_len) out[n++] = run_len << 4 | run_op;
+            run_op = op, run_len = len;
+        }
+    };
+    int ti = outer - 1, qj = inner - 1, state = 0;
+    for (int bk = (smax - 1) / kThinBlockSteps; bk >= 0; --bk) {
+        const int base = bk * kThinBlockSteps;
+        const int need = (lead && ti >= 0 && qj >= 0) ? ti + qj : -1;
+        int mx = need;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(FULL, mx, o));
+        if (mx < 0) break;
+        if (mx < base) continue;
+        const int rows = (min(smax, base + kThinBlockSteps) - base + 7) / 8;
+        const uint32_t* src = scratch + (size_t)(base / 8) * 32;
+        for (int w = lane; w < rows * 32; w += 32) buf[w] = src[w];
+        __syncwarp();
+        if (lead) {
+            while (ti >= 0 && qj >= 0) {
+                const int s = ti + qj;
+                if (s < base) break;
+                const uint32_t word = buf[((s - base) >> 3) * 32 + g * W + qj];
+                const uint32_t nib = (word >> (4 * (s & 7))) & 0xfu;
+                if (state == 0) state = nib & 3u;
+                else if (!((nib >> (state + 1)) & 1u)) state = 0;
+                if (state == 0) state = nib & 3u;
+                if (state == 0) push(0, 1), --ti, --qj;
+                else if (state == 1) push(2, 1), --ti;
+                else push(1, 1), --qj;
+            }
+        }
+        __syncwarp();
+    }
+    if (lead) {
+        if (ti >= 0) push(2, (uint32_t)(ti + 1));
+        if (qj >= 0) push(1, (uint32_t)(qj + 1));
+        if (run_len) out[n++] = run_len << 4 | run_op;
+        b.seg[sid].nops = n;
+        cells += (unsigned long long)sg.rl * sg.ql;
+    }
+}
+
+// Persistent warps; warp gw owns scratch slots 2gw and 2gw+1 (contiguous).
+// Each warp starts on width class gw % 3 and moves on when its queue is
+// drained; a queue hands out G consecutive entries of its class's range of
+// the sorted list (longest first).
+__global__ void __launch_bounds__(kThinWarps * 32, 4) dp_thin_kernel(IndexDev ix, BatchDev b)
+{
+    extern __shared__ uint32_t thin_smem[];
+    __shared__ unsigned rng[4];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int gw = blockIdx.x * kThinWarps + wl;
+    if (threadIdx.x < 32) {  // class ranges of the sorted list from the key counters
+        constexpr int per = (3 << kThinKeyClassShift) / 32;
+        unsigned c0 = 0, c1 = 0, c2 = 0;
+#pragma unroll
+        for (int k = 0; k < per; ++k) {
+            const int bin = lane * per + k;
+            const unsigned v = b.thin_hist[bin];
+            const int cls = bin >> kThinKeyClassShift;
+            c0 += cls == 0 ? v : 0u, c1 += cls == 1 ? v : 0u, c2 += cls == 2 ? v : 0u;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            c0 += __shfl_xor_sync(FULL, c0, o);
+            c1 += __shfl_xor_sync(FULL, c1, o);
+            c2 += __shfl_xor_sync(FULL, c2, o);
+        }
+        if (lane == 0) rng[0] = 0, rng[1] = c0, rng[2] = c0 + c1, rng[3] = c0 + c1 + c2;
+    }
+    __syncthreads();
+    if (2 * gw + 1 >= b.dp_nslots) return;
+    uint32_t* scratch = reinterpret_cast<uint32_t*>(b.dp_slots + (size_t)(2 * gw) * b.dp_slot_bytes);
+    uint32_t* buf = thin_smem + wl * kThinBlockWords;
+    unsigned long long cells = 0;
+    for (int k = 0; k < 3; ++k) {
+        const int cls = (gw + k) % 3;
+        const unsigned G = cls == 0 ? 8u : cls == 1 ? 4u : 2u;
+        const unsigned lo = rng[cls], hi = rng[cls + 1];
+        for (;;) {
+            unsigned t = 0;
+            if (lane == 0) t = atomicAdd(&b.thin_q[cls], 1u);
+            t = __shfl_sync(FULL, t, 0);
+            const unsigned long long f = (unsigned long long)lo + (unsigned long long)t * G;
+            if (f >= hi) break;
+            const unsigned cnt = min(G, hi - (unsigned)f);
+            if (cls == 0) thin_group<4>(ix, b, (unsigned)f, cnt, scratch, buf, cells);
+            else if (cls == 1) thin_group<8>(ix, b, (unsigned)f, cnt, scratch, buf, cells);
+            else thin_group<16>(ix, b, (unsigned)f, cnt, scratch, buf, cells);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_xor_sync(FULL, cells, o);
+    if (lane == 0 && cells && b.cells) atomicAdd(b.cells, cells);
+}
+
 // Counting sort of the small-tier work list by shape_key: the chain kernel
 // writes each entry's key and the histogram; scan + scatter follow.
 __global__ void shape_scan_kernel(BatchDev b)
@@ -1047,26 +1249,47 @@ __device__ __forceinline__ uint32_t* wave_scratch_ptr(const BatchDev& b, uint32_
     return nullptr;
 }
 
-// Counting sort of the one-warp wavefront list by wave_key.
-__global__ void wave_scatter_kernel(BatchDev b)
+// Counting-sort placement of a work list by key (the chain kernel built the
+// key histogram): bucket starts by a block scan of the counters, then one
+// atomic per run of equal keys in a warp.  Cursors follow the counters.
+constexpr int kKeyScatterThreads = 256;
+__global__ void __launch_bounds__(kKeyScatterThreads)
+    key_scatter_kernel(const uint32_t* list, const uint32_t* keys, uint32_t* hist, uint32_t* sorted,
+                       const unsigned* n_list, int64_t wcap, int bins)
 {
-    __shared__ uint32_t start[kWaveBins];
-    if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int k = 0; k < kWaveBins; ++k) start[k] = run, run += b.wave_hist[k];
+    __shared__ uint32_t start[kThinBins];
+    __shared__ uint32_t part[kKeyScatterThreads];
+    const int per = (bins + kKeyScatterThreads - 1) / kKeyScatterThreads;
+    uint32_t s = 0;
+    for (int k = 0; k < per; ++k) {
+        const int i = threadIdx.x * per + k;
+        if (i < bins) s += hist[i];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < kKeyScatterThreads; o <<= 1) {
+        const uint32_t v = (int)threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (int k = 0; k < per; ++k) {
+        const int i = threadIdx.x * per + k;
+        if (i < bins) start[i] = run, run += hist[i];
     }
     __syncthreads();
-    const unsigned total = *b.n_wave;
+    const unsigned total = *n_list;
     const unsigned span = (total + 31u) & ~31u;
     for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < span; w += gridDim.x * blockDim.x) {
-        const bool act = w < total && (int64_t)w < b.wcap;
-        const uint32_t key = act ? b.work_wave_key[w] : 0xffffffffu;
+        const bool act = w < total && (int64_t)w < wcap;
+        const uint32_t key = act ? keys[w] : 0xffffffffu;
         const unsigned peers = __match_any_sync(0xffffffffu, key);
         const int leader = __ffs(peers) - 1;
         uint32_t base = 0;
-        if (act && (int)(threadIdx.x & 31) == leader) base = atomicAdd(&b.wave_hist[kWaveBins + key], __popc(peers));
+        if (act && (int)(threadIdx.x & 31) == leader) base = atomicAdd(&hist[bins + key], __popc(peers));
         base = __shfl_sync(0xffffffffu, base, leader);
-        if (act) b.work_wave_sorted[start[key] + base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = b.work_wave[w];
+        if (act) sorted[start[key] + base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = list[w];
     }
 }
 
@@ -1245,9 +1468,19 @@ extern "C" cudaError_t hg_launch_dp_large(const hg::IndexDev* ix, const hg::Batc
 
 // One-warp wavefront tier: sort its list, then run it (grid CTAs of 4
 // warps; warp i uses checkpoint slot i).
+// Thin tier (sort, then CTAs of kThinWarps warps; warp i uses slots 2i and
+// 2i+1, all below the slots of the CTA tier) followed by the one-warp
+// wavefront tier.
 extern "C" cudaError_t hg_launch_dp_wave(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
-    hg::wave_scatter_kernel<<<grid, 256, 0, st>>>(*b);
+    hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_thin, b->work_thin_key, b->thin_hist,
+                                                                    b->work_thin_sorted, b->n_thin, b->wcap,
+                                                                    hg::kThinBins);
+    const int tgrid = grid / 2 > 0 ? grid / 2 : 1;
+    hg::dp_thin_kernel<<<tgrid, hg::kThinWarps * 32, hg::kThinSmemBytes, st>>>(*ix, *b);
+    hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_wave, b->work_wave_key, b->wave_hist,
+                                                                    b->work_wave_sorted, b->n_wave, b->wcap,
+                                                                    hg::kWaveBins);
     hg::dp_wave_kernel<<<grid, 128, 0, st>>>(*ix, *b);
     return cudaGetLastError();
 }
@@ -1265,6 +1498,9 @@ extern "C" cudaError_t hg_prepare_dp_kernels()
 {
     cudaError_t e = cudaFuncSetAttribute(hg::dp_wave_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)hg::kWaveCtaSmemBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(hg::dp_thin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hg::kThinSmemBytes);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(hg::shape_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)hg::kScatterSmem);

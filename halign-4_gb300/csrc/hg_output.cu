@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
                         else op = 2, len = s_rl[wib][lo];
                     } else {
                         // the small DP tier stores its ops last-first
-                        const uint32_t at = kind == kSegDpSmall ? (uint32_t)s_nops[wib][lo] - 1u - rel : rel;
+                        const uint32_t at = (kind == kSegDpSmall || kind == kSegDpThin) ? (uint32_t)s_nops[wib][lo] - 1u - rel : rel;
                         const uint32_t c = src[s_slot[wib][lo] + at];
                         op = c & 0xfu, len = c >> 4;
                     }

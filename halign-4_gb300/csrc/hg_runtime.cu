@@ -171,6 +171,7 @@ struct hg_ctx {
     DevBuf<int32_t> s_n, n_chain;
     DevBuf<uint32_t> work_small, work_large, work_sorted, work_key, shape_hist;
     DevBuf<uint32_t> work_wave, work_wave_key, work_wave_sorted, wave_hist, work_wide;
+    DevBuf<uint32_t> work_thin, work_thin_key, work_thin_sorted;  // thin_hist lives in wave_hist
     DevBuf<hg::SmallRec> work_rec;
     int64_t dp_cap = 0;
     DevBuf<uint8_t> dp_arena;
@@ -632,13 +633,15 @@ namespace {
 
 constexpr int kControlWords = 16;
 // control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide |
-// queues2[4]
+// queues2[4] | n_thin, thin_q[3]
+// sort counters of the one-warp wavefront list, then of the thin list (counters and cursors each)
+constexpr size_t kSortHistWords = 2 * (size_t)hg::kWaveBins + 2 * (size_t)hg::kThinBins;
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
 constexpr int kWaveBlocksPerSm = 4;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
-// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, dp_wave 2, dp_wide,
+// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, thin + dp_wave 4, dp_wide,
 // dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
-constexpr int kLaunchesBatch = 18;
-constexpr int kLaunchesPlain = 17;
+constexpr int kLaunchesBatch = 20;
+constexpr int kLaunchesPlain = 19;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
@@ -740,7 +743,9 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->work_sorted.alloc(c->scap)) || (e = c->work_key.alloc(c->scap)) ||
         (e = c->shape_hist.alloc(2 * (size_t)hg::kShapeBins)) ||
         (e = c->work_wave.alloc(c->scap)) || (e = c->work_wave_key.alloc(c->scap)) ||
-        (e = c->work_wave_sorted.alloc(c->scap)) || (e = c->wave_hist.alloc(2 * (size_t)hg::kWaveBins)) ||
+        (e = c->work_wave_sorted.alloc(c->scap)) || (e = c->wave_hist.alloc(kSortHistWords)) ||
+        (e = c->work_thin.alloc(c->scap)) || (e = c->work_thin_key.alloc(c->scap)) ||
+        (e = c->work_thin_sorted.alloc(c->scap)) ||
         (e = c->work_wide.alloc(c->scap)) || (e = c->work_rec.alloc(c->scap)) ||
         (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) || (e = c->run_flags.alloc(1)) ||
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
@@ -867,6 +872,10 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.wave_hist = c->wave_hist.p, b.work_wide = c->work_wide.p, b.work_rec = c->work_rec.p;
     b.n_wave = reinterpret_cast<unsigned int*>(ctl + 10);
     b.n_wide = reinterpret_cast<unsigned int*>(ctl + 11);
+    b.n_thin = reinterpret_cast<unsigned int*>(ctl + 14);     // low half of word 14
+    b.thin_q = reinterpret_cast<unsigned int*>(ctl + 14) + 1;  // high half of 14, word 15
+    b.work_thin = c->work_thin.p, b.work_thin_key = c->work_thin_key.p, b.work_thin_sorted = c->work_thin_sorted.p;
+    b.thin_hist = c->wave_hist.p + 2 * hg::kWaveBins;
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
     b.dp_slots = c->dp_slots.p, b.dp_slot_bytes = c->dp_slot_bytes, b.dp_nslots = c->dp_nslots;
     b.run_flags = c->run_flags.p;
@@ -886,7 +895,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, st));
     HG_CUDA(cudaMemsetAsync(c->status.p, 0, sizeof(uint32_t) * (size_t)b.n, st));
     HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, st));
-    HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * 2 * hg::kWaveBins, st));
+    HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * kSortHistWords, st));
     const int n = b.n;
     auto mark = [&](int i) -> cudaError_t { return timed ? cudaEventRecord(c->ev[i], st) : cudaSuccess; };
     HG_CUDA(mark(0));
@@ -1105,7 +1114,7 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
                 // status must survive the per-launch reset: enqueue without the batch memset
                 HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, c->st));
                 HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, c->st));
-                HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * 2 * hg::kWaveBins, c->st));
+                HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * kSortHistWords, c->st));
                 const hg::IndexDev& ix = c->ix->dev;
                 HG_CUDA(hg_launch_seed(&ix, &b, 0, nullptr, nullptr, 1, c->st));
                 HG_CUDA(hg_launch_anchor(&ix, &b, 1, c->st));
@@ -1539,7 +1548,7 @@ int global_align_mm2_impl(hg_index_t* ix, const char* qry, int64_t qlen, const u
     HG_CUDA(cudaMemsetAsync(c->control.p, 0, sizeof(unsigned long long) * kControlWords, st));
     HG_CUDA(cudaMemsetAsync(c->status.p, 0, 4, st));
     HG_CUDA(cudaMemsetAsync(c->shape_hist.p, 0, sizeof(uint32_t) * hg::kShapeBins, st));
-    HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * 2 * hg::kWaveBins, st));
+    HG_CUDA(cudaMemsetAsync(c->wave_hist.p, 0, sizeof(uint32_t) * kSortHistWords, st));
     const hg::IndexDev& d = ix->dev;
     HG_CUDA(hg_launch_chain(&d, &b, 1, st));
     HG_CUDA(hg_launch_dp_small(&d, &b, c->sms, st));

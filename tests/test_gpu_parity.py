@@ -235,6 +235,69 @@ def test_wavefront_tiers_vs_oracle(gpu, oracle, pkg):
             assert res.rows[i].tobytes() == oracle.del_query(qq, want), i
 
 
+def thin_cases(pkg, seed=5, L=12000):
+    """Queries whose end segments are thin: a short side of 1..16 bases against
+    up to ~12 kb of the other side, in both orientations, both gap modes, with
+    plain and N-carrying ends, and a second center carrying N runs."""
+    rng = np.random.default_rng(seed)
+    center = pkg.synth.random_center(L, 57)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+
+    def rand(n, alpha=acgt):
+        return alpha[rng.integers(0, len(alpha), n)].tobytes()
+
+    cases = []
+    for _ in range(40):                                   # substrings with short random ends
+        a = int(rng.integers(0, L - 300))
+        b = int(min(L, a + rng.integers(200, 7000)))
+        cases.append(rand(int(rng.integers(0, 14))) + center[a:b] + rand(int(rng.integers(0, 14))))
+    for _ in range(10):                                   # N inside the short ends
+        a = int(rng.integers(0, L - 3000))
+        cases.append(rand(6, np.frombuffer(b"ACGTN", np.uint8)) + center[a:a + 2500] +
+                     rand(9, np.frombuffer(b"ACGTN", np.uint8)))
+    for s in (0, 2, 5, 8, 10, 12, 14, 16):                # long query ends against a short center end
+        cases.append(rand(int(rng.integers(100, 3000))) + center[s:4000])
+        cases.append(center[L - 4000:L - s] + rand(int(rng.integers(100, 3000))))
+    for d in range(0, 16, 2):                             # inserted blocks: short center gap inside
+        a = int(rng.integers(0, L - 3200))
+        cases.append(center[a:a + 1500] + rand(int(rng.integers(35, 70))) + center[a + 1500 + d:a + 3000])
+    cases.append(center[3000:9000].lower())
+    return center, cases
+
+
+def dp_center(raw: bytes) -> bytes:
+    """The center the DP aligns against: the consensus of the single center
+    record (pickConsensusChar: A/C/G/T/U of either case upper-cased, any other
+    letter becomes A).  Minimizers still come from the raw center."""
+    t = bytearray(b"A" * 256)
+    for c in b"ACGTU":
+        t[c] = t[c + 32] = c
+    return raw.translate(bytes(t))
+
+
+def test_thin_tier_vs_oracle(gpu, oracle, pkg):
+    """Thin end segments (thread DP with checkpointed rows): every CIGAR and
+    row equals the oracle's, on a plain center and on one carrying N runs."""
+    center, cases = thin_cases(pkg)
+    c2 = bytearray(center)
+    for a in (700, 4100, 8800):
+        c2[a:a + 30] = b"N" * 30
+    for raw in (center, bytes(c2)):
+        cmx, cmy = oracle.extract_minimizer(raw)
+        cen = dp_center(raw)
+        seqs = b"".join(cases)
+        offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+        ix = gpu.Index(raw)
+        ctx = gpu.Context(ix, max_queries=128, max_bases=len(seqs) + 1024)
+        res = ctx.align(gpu.pack(seqs, offs), rows=True, check=False)
+        for i, qq in enumerate(cases):
+            want = oracle.align_query(cen, cmx, cmy, qq)
+            assert np.array_equal(res.cigar_of(i), want), (i, len(qq), oracle.cigar_str(want)[:120],
+                                                            oracle.cigar_str(res.cigar_of(i))[:120])
+            if not (res.status[i] & (pkg.ST_PARTIAL_CIGAR | pkg.ST_LENGTH_MISMATCH)):
+                assert res.rows[i].tobytes() == oracle.del_query(qq, want), i
+
+
 def test_batch_window_overflow_vs_oracle(gpu, oracle, pkg):
     """Queries holding 10+ consecutive strictly increasing k-mer hashes at the
     default k=15, w=10: the reference's window deque overflows there, the
