@@ -98,25 +98,26 @@ __device__ __forceinline__ uint32_t shape_key(const Seg& g)
 // Thin tier: the query side 1..16 bases against a center side beyond the
 // small and medium bounds (so more than twice as long, and auto_band gives an
 // unbounded band).  Several such segments share a warp, one lane per query
-// column: a group of W = 4, 8 or 16 lanes runs one segment's anti-diagonal
-// wavefront, so a step costs one cell per lane however short the query side
-// is.  Direction nibbles go to a two-slot scratch region per warp, which
-// bounds the steps (rl + ql - 1) of a thin segment.
+// column: a group of W = ql lanes runs one segment's anti-diagonal wavefront
+// (floor(32 / W) groups per warp), so a step costs one cell per lane however
+// short the query side is.  Direction nibbles go to the warp's own scratch
+// region (16 bytes per step), which bounds the steps (rl + ql - 1) of a thin
+// segment.
 constexpr int kThinMaxInner = 16;
-constexpr int kThinBins = 512;       // sort bins of the thin list (key < 3 << 7)
-constexpr int kThinKeyClassShift = 7;  // key bits above it: the group width class
+constexpr int kThinMaxSteps = 32768;
+constexpr size_t kThinWarpBytes = (size_t)kThinMaxSteps * 16;
+constexpr int kThinKeyClassShift = 7;  // key bits above it: the query length - 1 (the group width)
+constexpr int kThinBins = kThinMaxInner << kThinKeyClassShift;
 
-__host__ __device__ __forceinline__ int thin_width_class(uint32_t inner) { return inner <= 4 ? 0 : inner <= 8 ? 1 : 2; }
-
-__host__ __device__ __forceinline__ bool thin_tier_fits(uint32_t rl, uint32_t ql, int64_t slot_bytes)
+__host__ __device__ __forceinline__ bool thin_tier_fits(uint32_t rl, uint32_t ql)
 {
     if (ql < 1 || ql > (uint32_t)kThinMaxInner || rl <= ql || small_tier_fits(rl, ql)) return false;
-    return ((int64_t)rl + ql - 1) * 16 <= 2 * slot_bytes;  // 16 bytes of direction nibbles per warp step
+    return (int64_t)rl + ql - 1 <= kThinMaxSteps;
 }
 
-// Sort key of a thin segment: group width class first (a warp takes
-// segments of one class), then longest first by quarter-octave class of the
-// center side, then gap mode.
+// Sort key of a thin segment: query length first (a warp takes segments of
+// one length), then longest first by quarter-octave class of the center
+// side, then gap mode.
 __host__ __device__ __forceinline__ uint32_t thin_key(uint32_t rl, uint32_t ql, bool left)
 {
     uint32_t lg = 0;
@@ -124,7 +125,7 @@ __host__ __device__ __forceinline__ uint32_t thin_key(uint32_t rl, uint32_t ql, 
     const uint32_t frac = lg >= 2 ? (rl >> (lg - 2)) & 3u : 0u;
     uint32_t cls = lg >= 5 ? (lg - 5) * 4 + frac : 0u;
     cls = cls > 63 ? 63 : cls;
-    return (uint32_t)thin_width_class(ql) << kThinKeyClassShift | (63u - cls) << 1 | (left ? 0u : 1u);
+    return (ql - 1) << kThinKeyClassShift | (63u - cls) << 1 | (left ? 0u : 1u);
 }
 
 // Wavefront tiers: segments the band never binds (auto_band < 0 or >= both
@@ -245,11 +246,13 @@ struct BatchDev {
     uint32_t* work_thin_sorted;
     uint32_t* thin_hist;         // kThinBins counters, then kThinBins cursors
     unsigned int* n_thin;
-    unsigned int* thin_q;        // three queue heads of the thin tier, one per group width class
+    unsigned int* thin_q;        // kThinMaxInner queue heads of the thin tier, one per query length
     int64_t wcap;
     // K6 DP scratch: one reusable slot per large-tier warp, plus a bump arena
     // for segments whose scratch exceeds a slot
     uint8_t* dp_slots;
+    uint8_t* thin_scratch;       // kThinWarpBytes per warp of the thin tier
+    int thin_nwarps;
     int64_t dp_slot_bytes;
     int dp_nslots;
     uint8_t* dp_arena;

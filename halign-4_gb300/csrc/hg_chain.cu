@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 kind = kSegMatch;  // identical equal-length sides: the DP's CIGAR is rl M
             else if (small_tier_fits(rl, ql) || medium_tier_fits(rl, ql))
                 kind = kSegDpSmall;
-            else if (thin_tier_fits(rl, ql, b.dp_slot_bytes))
+            else if (thin_tier_fits(rl, ql))
                 kind = kSegDpThin;
             else
                 kind = kSegDpLarge;

@@ -358,17 +358,20 @@ __device__ __forceinline__ uint32_t lane_int_nl(int z0, int xt1, int vt1, int ut
     return d;
 }
 
-// Thin tier: G = 32 / W segments per warp, lane j of group g owns query
-// column j of the group's segment and computes cell (s - j, j) at step s.
+// Thin tier: G = floor(32 / W) segments of query length W per warp, lane j
+// of group g owns query column j of the group's segment and computes cell
+// (s - j, j) at step s.
 // A cell takes its left neighbour's outputs of the previous step by one
 // shuffle (u, y and the row's center code, packed), its own previous outputs
 // as the cell above, and lane 0 of a group reads the center base of a new
 // row.  Direction nibbles of 8 steps make one word per lane in the warp's
 // scratch; the traceback copies blocks of kThinBlockSteps steps back to
 // shared memory and each group's lane 0 walks its segment there, writing op
-// runs last-first (as the small tier does).
+// runs last-first (as the small tier does).  A deletion run (the bulk of a
+// thin segment's path) stays in one column, so its nibbles sit side by side
+// in one word: the walk takes all of a word's continuing ones at once.
 constexpr int kThinWarps = 4;
-constexpr int kThinBlockSteps = 1024;
+constexpr int kThinBlockSteps = 512;
 constexpr int kThinBlockWords = kThinBlockSteps / 8 * 32;  // per warp
 constexpr size_t kThinSmemBytes = (size_t)kThinWarps * kThinBlockWords * sizeof(uint32_t);
 
@@ -378,7 +381,7 @@ __device__ __forceinline__ void thin_group(const IndexDev& ix, const BatchDev& b
 {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, j = lane % W, g = lane / W;
-    const bool has = (unsigned)g < cnt;
+    const bool has = (unsigned)g < cnt;  // cnt <= 32 / W
     uint32_t sid = 0;
     Seg sg;
     sg.rs = sg.qs = sg.rl = sg.ql = sg.slot = sg.q = sg.kind = 0;
@@ -407,25 +410,25 @@ __device__ __forceinline__ void thin_group(const IndexDev& ix, const BatchDev& b
     int s1 = 0, s2 = j ? 6 : 0;  // x, v of the cell above row 0
     uint32_t outp = 0;           // u | y << 8 | 5 x center code << 16, toward the right neighbour
     uint32_t chunk = 0, acc = 0;
-    for (int s = 0; s < smax; ++s) {
-        const int sm = s % W;
+    const unsigned span = has ? (unsigned)outer : 0u;  // cell (s - j, j) exists for s - j in [0, span)
+    for (int s = 0, sm = 0; s < smax; ++s) {
         if (sm == 0) {
             const int o = s + j;
             chunk = (has && o < outer) ? 5u * (uint32_t)tc[o] : 0u;
         }
         const uint32_t fresh = __shfl_sync(FULL, chunk, g * W + sm);
-        const uint32_t inp = __shfl_up_sync(FULL, outp, 1, W);
+        const uint32_t inp = __shfl_sync(FULL, outp, lane - 1);  // lane 0 of a group ignores it
+        sm = sm == W - 1 ? 0 : sm + 1;
         int c1, c2, c5;
         if (j == 0) {
             c1 = s ? 6 : 0, c2 = 0, c5 = (int)fresh;  // left of column 0 on row s
         } else {
             c1 = (int)(inp & 0xffu), c2 = (int)((inp >> 8) & 0xffu), c5 = (int)(inp >> 16);
         }
-        const int o = s - j;
         const int z0 = (int)((tab >> c5) & 31u);
         int u, v, x, y;
         const uint32_t d = lane_int_nl(z0, s1, s2, c1, c2, nl, u, v, x, y);
-        if (o >= 0 && o < outer && j < inner) {
+        if ((unsigned)(s - j) < span) {
             s1 = x, s2 = v;
             outp = (uint32_t)u | (uint32_t)y << 8 | (uint32_t)c5 << 16;
             acc |= d << (4 * (s & 7));
@@ -467,7 +470,18 @@ __device__ __forceinline__ void thin_group(const IndexDev& ix, const BatchDev& b
                 const int s = ti + qj;
                 if (s < base) break;
                 const uint32_t word = buf[((s - base) >> 3) * 32 + g * W + qj];
-                const uint32_t nib = (word >> (4 * (s & 7))) & 0xfu;
+                const int p = s & 7;
+                if (state == 1) {  // nibbles p, p-1, .. with the E bit set continue the deletion
+                    const uint32_t stop = ~word & (0x44444444u >> (4 * (7 - p)));
+                    int run = stop ? p - ((31 - __clz(stop)) >> 2) : p + 1;
+                    run = min(run, ti + 1);
+                    if (run > 0) {
+                        push(2, (uint32_t)run);
+                        ti -= run;
+                        continue;
+                    }
+                }
+                const uint32_t nib = (word >> (4 * p)) & 0xfu;
                 if (state == 0) state = nib & 3u;
                 else if (!((nib >> (state + 1)) & 1u)) state = 0;
                 if (state == 0) state = nib & 3u;
@@ -487,54 +501,72 @@ __device__ __forceinline__ void thin_group(const IndexDev& ix, const BatchDev& b
     }
 }
 
-// Persistent warps; warp gw owns scratch slots 2gw and 2gw+1 (contiguous).
-// Each warp starts on width class gw % 3 and moves on when its queue is
-// drained; a queue hands out G consecutive entries of its class's range of
-// the sorted list (longest first).
+// Persistent warps; warp gw owns thin scratch region gw.
+// Each warp starts on query length gw % 16 + 1 and moves on when that queue
+// is drained; a queue hands out G consecutive entries of its length's range
+// of the sorted list (longest first).
+template <int W>
+__device__ __forceinline__ void thin_drain(const IndexDev& ix, const BatchDev& b, unsigned lo, unsigned hi,
+                                           uint32_t* scratch, uint32_t* buf, unsigned long long& cells)
+{
+    constexpr unsigned G = 32 / W;
+    for (;;) {
+        unsigned t = 0;
+        if ((threadIdx.x & 31) == 0) t = atomicAdd(&b.thin_q[W - 1], 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        const unsigned long long f = (unsigned long long)lo + (unsigned long long)t * G;
+        if (f >= hi) break;
+        thin_group<W>(ix, b, (unsigned)f, min(G, hi - (unsigned)f), scratch, buf, cells);
+    }
+}
+
 __global__ void __launch_bounds__(kThinWarps * 32, 4) dp_thin_kernel(IndexDev ix, BatchDev b)
 {
     extern __shared__ uint32_t thin_smem[];
-    __shared__ unsigned rng[4];
+    __shared__ unsigned rng[kThinMaxInner + 1];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int gw = blockIdx.x * kThinWarps + wl;
-    if (threadIdx.x < 32) {  // class ranges of the sorted list from the key counters
-        constexpr int per = (3 << kThinKeyClassShift) / 32;
-        unsigned c0 = 0, c1 = 0, c2 = 0;
+    if (threadIdx.x < 32) {  // per-length ranges of the sorted list from the key counters
+        constexpr int per = kThinBins / 32;  // lanes 2c and 2c+1 cover length c + 1
+        unsigned c = 0;
+        for (int k = 0; k < per; ++k) c += b.thin_hist[lane * per + k];
+        c += __shfl_down_sync(FULL, c, 1);
+        unsigned incl = (lane & 1) ? 0u : c;  // count of length lane/2 + 1 on even lanes
 #pragma unroll
-        for (int k = 0; k < per; ++k) {
-            const int bin = lane * per + k;
-            const unsigned v = b.thin_hist[bin];
-            const int cls = bin >> kThinKeyClassShift;
-            c0 += cls == 0 ? v : 0u, c1 += cls == 1 ? v : 0u, c2 += cls == 2 ? v : 0u;
+        for (int o = 2; o < 32; o <<= 1) {
+            const unsigned v = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += v;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            c0 += __shfl_xor_sync(FULL, c0, o);
-            c1 += __shfl_xor_sync(FULL, c1, o);
-            c2 += __shfl_xor_sync(FULL, c2, o);
-        }
-        if (lane == 0) rng[0] = 0, rng[1] = c0, rng[2] = c0 + c1, rng[3] = c0 + c1 + c2;
+        if (lane == 0) rng[0] = 0;
+        if (!(lane & 1)) rng[lane / 2 + 1] = incl;
     }
     __syncthreads();
-    if (2 * gw + 1 >= b.dp_nslots) return;
-    uint32_t* scratch = reinterpret_cast<uint32_t*>(b.dp_slots + (size_t)(2 * gw) * b.dp_slot_bytes);
+    if (gw >= b.thin_nwarps) return;
+    uint32_t* scratch = reinterpret_cast<uint32_t*>(b.thin_scratch + (size_t)gw * kThinWarpBytes);
     uint32_t* buf = thin_smem + wl * kThinBlockWords;
     unsigned long long cells = 0;
-    for (int k = 0; k < 3; ++k) {
-        const int cls = (gw + k) % 3;
-        const unsigned G = cls == 0 ? 8u : cls == 1 ? 4u : 2u;
-        const unsigned lo = rng[cls], hi = rng[cls + 1];
-        for (;;) {
-            unsigned t = 0;
-            if (lane == 0) t = atomicAdd(&b.thin_q[cls], 1u);
-            t = __shfl_sync(FULL, t, 0);
-            const unsigned long long f = (unsigned long long)lo + (unsigned long long)t * G;
-            if (f >= hi) break;
-            const unsigned cnt = min(G, hi - (unsigned)f);
-            if (cls == 0) thin_group<4>(ix, b, (unsigned)f, cnt, scratch, buf, cells);
-            else if (cls == 1) thin_group<8>(ix, b, (unsigned)f, cnt, scratch, buf, cells);
-            else thin_group<16>(ix, b, (unsigned)f, cnt, scratch, buf, cells);
+    for (int k = 0; k < kThinMaxInner; ++k) {
+        const int c = (gw + k) % kThinMaxInner;
+        const unsigned lo = rng[c], hi = rng[c + 1];
+        if (lo >= hi) continue;
+        switch (c + 1) {
+        case 1: thin_drain<1>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 2: thin_drain<2>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 3: thin_drain<3>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 4: thin_drain<4>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 5: thin_drain<5>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 6: thin_drain<6>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 7: thin_drain<7>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 8: thin_drain<8>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 9: thin_drain<9>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 10: thin_drain<10>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 11: thin_drain<11>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 12: thin_drain<12>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 13: thin_drain<13>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 14: thin_drain<14>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 15: thin_drain<15>(ix, b, lo, hi, scratch, buf, cells); break;
+        default: thin_drain<16>(ix, b, lo, hi, scratch, buf, cells); break;
         }
     }
     for (int o = 16; o > 0; o >>= 1) cells += __shfl_xor_sync(FULL, cells, o);
@@ -1468,15 +1500,14 @@ extern "C" cudaError_t hg_launch_dp_large(const hg::IndexDev* ix, const hg::Batc
 
 // One-warp wavefront tier: sort its list, then run it (grid CTAs of 4
 // warps; warp i uses checkpoint slot i).
-// Thin tier (sort, then CTAs of kThinWarps warps; warp i uses slots 2i and
-// 2i+1, all below the slots of the CTA tier) followed by the one-warp
-// wavefront tier.
+// Thin tier (sort, then one warp per thin scratch region) followed by the
+// one-warp wavefront tier.
 extern "C" cudaError_t hg_launch_dp_wave(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
     hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_thin, b->work_thin_key, b->thin_hist,
                                                                     b->work_thin_sorted, b->n_thin, b->wcap,
                                                                     hg::kThinBins);
-    const int tgrid = grid / 2 > 0 ? grid / 2 : 1;
+    const int tgrid = (b->thin_nwarps + hg::kThinWarps - 1) / hg::kThinWarps;
     hg::dp_thin_kernel<<<tgrid, hg::kThinWarps * 32, hg::kThinSmemBytes, st>>>(*ix, *b);
     hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_wave, b->work_wave_key, b->wave_hist,
                                                                     b->work_wave_sorted, b->n_wave, b->wcap,

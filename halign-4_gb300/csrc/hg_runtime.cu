@@ -178,6 +178,8 @@ struct hg_ctx {
     int64_t dp_slot_bytes = 0;
     int dp_nslots = 0;
     DevBuf<uint8_t> dp_slots;
+    DevBuf<uint8_t> thin_scratch;  // direction nibbles of the thin tier, one region per warp
+    int thin_nwarps = 0;
     DevBuf<uint32_t> run_flags;
     int64_t cig_cap = 0;
     DevBuf<uint32_t> cig_seg, cig;
@@ -631,13 +633,14 @@ extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t*
 
 namespace {
 
-constexpr int kControlWords = 16;
+constexpr int kControlWords = 24;
 // control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide |
-// queues2[4] | n_thin, thin_q[3]
+// queues2[4] | n_thin | (free) | thin_q[16]
 // sort counters of the one-warp wavefront list, then of the thin list (counters and cursors each)
 constexpr size_t kSortHistWords = 2 * (size_t)hg::kWaveBins + 2 * (size_t)hg::kThinBins;
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
-constexpr int kWaveBlocksPerSm = 4;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
+constexpr int kWaveBlocksPerSm = 4;
+constexpr int kThinWarpsPerSm = 16;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
 // kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, thin + dp_wave 4, dp_wide,
 // dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
 constexpr int kLaunchesBatch = 20;
@@ -708,6 +711,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     c->dp_cap = std::max<int64_t>((int64_t)1 << 30, max_bases);
     c->dp_slot_bytes = (int64_t)256 << 10;
     c->dp_nslots = c->sms * kLargeBlocksPerSm * 4 + c->sms;  // warp slots, then one per CTA-tier CTA
+    // thin tier: 16 warps per SM, fewer for a small context (a warp takes 2+ segments at a time)
+    c->thin_nwarps = (int)std::min<int64_t>((int64_t)c->sms * kThinWarpsPerSm, (max_queries + 3) / 4 * 4);
     c->cig_cap = max_bases + max_queries * (L + 4);
     if (c->cig_cap >= ((int64_t)1 << 32)) {  // SmallRec holds 32-bit op offsets
         delete c;
@@ -747,7 +752,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->work_thin.alloc(c->scap)) || (e = c->work_thin_key.alloc(c->scap)) ||
         (e = c->work_thin_sorted.alloc(c->scap)) ||
         (e = c->work_wide.alloc(c->scap)) || (e = c->work_rec.alloc(c->scap)) ||
-        (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) || (e = c->run_flags.alloc(1)) ||
+        (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) ||
+        (e = c->thin_scratch.alloc((size_t)c->thin_nwarps * hg::kThinWarpBytes)) || (e = c->run_flags.alloc(1)) ||
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
         (e = c->rows.alloc((size_t)max_queries * c->row_stride)) || (e = c->counts.alloc(L * 7)) ||
@@ -872,12 +878,13 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.wave_hist = c->wave_hist.p, b.work_wide = c->work_wide.p, b.work_rec = c->work_rec.p;
     b.n_wave = reinterpret_cast<unsigned int*>(ctl + 10);
     b.n_wide = reinterpret_cast<unsigned int*>(ctl + 11);
-    b.n_thin = reinterpret_cast<unsigned int*>(ctl + 14);     // low half of word 14
-    b.thin_q = reinterpret_cast<unsigned int*>(ctl + 14) + 1;  // high half of 14, word 15
+    b.n_thin = reinterpret_cast<unsigned int*>(ctl + 14);
+    b.thin_q = reinterpret_cast<unsigned int*>(ctl + 16);  // 16 x uint32 in words 16..23
     b.work_thin = c->work_thin.p, b.work_thin_key = c->work_thin_key.p, b.work_thin_sorted = c->work_thin_sorted.p;
     b.thin_hist = c->wave_hist.p + 2 * hg::kWaveBins;
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
     b.dp_slots = c->dp_slots.p, b.dp_slot_bytes = c->dp_slot_bytes, b.dp_nslots = c->dp_nslots;
+    b.thin_scratch = c->thin_scratch.p, b.thin_nwarps = c->thin_nwarps;
     b.run_flags = c->run_flags.p;
     b.coff = coff, b.cig_seg = c->cig_seg.p, b.cig = c->cig.p, b.n_cig = c->n_cig.p, b.has_ins = c->has_ins.p;
     b.rows = c->rows.p, b.counts = c->counts.p, b.ins = c->ins.p, b.status = c->status.p;
