@@ -204,9 +204,7 @@ struct BatchDev {
     int32_t* n_matched;          // minimizers whose hash occurs in the center
     uint32_t* exact_list;        // queries whose window deque overflows (re-run sequentially)
     unsigned int* n_exact;
-    uint64_t* ring_h;            // ring scratch of the sequential re-run
-    uint32_t* ring_p;
-    int ring_slots;              // ring entries per re-run thread
+    int ring_slots;              // ring entries of the sequential re-run (2 w + 16)
     // K2 anchors (dynamic arena)
     uint32_t* a_ref;
     uint32_t* a_qry;

@@ -40,7 +40,6 @@ cudaError_t hg_launch_rows(const hg::IndexDev*, const hg::BatchDev*, int64_t, in
 cudaError_t hg_launch_count(const uint8_t*, int64_t, int, int, uint32_t*, cudaStream_t);
 cudaError_t hg_launch_status_or(const uint32_t*, int, uint32_t*, cudaStream_t);
 size_t hg_ksw_scratch_bytes(int, int, int, int);
-int hg_exact_ring_threads(void);
 cudaError_t hg_prepare_kernels(void);
 cudaError_t hg_launch_ksw_single(int, const uint8_t*, int, const uint8_t*, int, const int8_t*, int, int, int, int,
                                  int, int, uint8_t*, uint32_t*, int, void*, cudaStream_t);
@@ -156,9 +155,6 @@ struct hg_ctx {
     DevBuf<uint32_t> hit_pos, hit_ent;
     DevBuf<int32_t> n_hits, n_matched;
     DevBuf<uint32_t> exact_list;
-    DevBuf<uint64_t> ring_h;
-    DevBuf<uint32_t> ring_p;
-    int ring_slots = 0;
     int64_t acap = 0;
     DevBuf<uint32_t> a_ref, a_qry;
     DevBuf<int32_t> a_f, a_p, a_t, a_n;
@@ -427,12 +423,8 @@ int run_extract(int dev_k, int dev_w, int non_canonical, const char* seq, int64_
     DevBuf<uint64_t> d_x, d_y;
     DevBuf<uint32_t> d_status, d_exact;
     DevBuf<unsigned int> d_q;
-    DevBuf<uint64_t> d_rh;
-    DevBuf<uint32_t> d_rp;
     const int ring_slots = 2 * dev_w + 16;
     HG_CUDA(d_exact.alloc(1));
-    HG_CUDA(d_rh.alloc((size_t)hg_exact_ring_threads() * ring_slots));
-    HG_CUDA(d_rp.alloc((size_t)hg_exact_ring_threads() * ring_slots));
     HG_CUDA(d_pk.alloc(pk.size()));
     HG_CUDA(d_poff.alloc(1));
     HG_CUDA(d_eoff.alloc(2));
@@ -458,7 +450,7 @@ int run_extract(int dev_k, int dev_w, int non_canonical, const char* seq, int64_
     hg::BatchDev bd{};
     bd.n = 1, bd.packed = d_pk.p, bd.poff = d_poff.p, bd.qlen = d_qlen.p, bd.exc = d_exc.p, bd.exc_off = d_eoff.p;
     bd.hoff = d_hoff.p, bd.n_hits = d_nh.p, bd.n_matched = d_nm.p, bd.queues = d_q.p;
-    bd.exact_list = d_exact.p, bd.n_exact = d_q.p + 8, bd.ring_h = d_rh.p, bd.ring_p = d_rp.p;
+    bd.exact_list = d_exact.p, bd.n_exact = d_q.p + 8;
     bd.ring_slots = ring_slots;
     HG_CUDA(hg_launch_seed(&ixd, &bd, 1, d_x.p, d_y.p, 1, st));
     int32_t nh = 0;
@@ -736,8 +728,6 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->hit_pos.alloc(max_bases)) || (e = c->hit_ent.alloc(max_bases)) ||
         (e = c->n_hits.alloc(max_queries)) || (e = c->n_matched.alloc(max_queries)) ||
         (e = c->exact_list.alloc(max_queries)) ||
-        (e = c->ring_h.alloc((size_t)hg_exact_ring_threads() * (2 * ix->w + 16))) ||
-        (e = c->ring_p.alloc((size_t)hg_exact_ring_threads() * (2 * ix->w + 16))) ||
         (e = c->a_ref.alloc(c->acap)) || (e = c->a_qry.alloc(c->acap)) || (e = c->a_f.alloc(c->acap)) ||
         (e = c->a_p.alloc(c->acap)) || (e = c->a_t.alloc(c->acap)) || (e = c->a_tmp.alloc(2 * c->acap)) ||
         (e = c->a_base.alloc(max_queries)) || (e = c->a_n.alloc(max_queries)) ||
@@ -857,7 +847,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.packed = packed, b.poff = poff, b.qlen = qlen, b.exc = exc, b.exc_off = exc_off, b.order = order;
     b.hoff = hoff, b.hit_pos = c->hit_pos.p, b.hit_ent = c->hit_ent.p, b.n_hits = c->n_hits.p,
     b.n_matched = c->n_matched.p;
-    b.exact_list = c->exact_list.p, b.ring_h = c->ring_h.p, b.ring_p = c->ring_p.p;
+    b.exact_list = c->exact_list.p;
     b.ring_slots = 2 * c->ix->w + 16;
     b.a_ref = c->a_ref.p, b.a_qry = c->a_qry.p, b.a_f = c->a_f.p, b.a_p = c->a_p.p, b.a_t = c->a_t.p,
     b.a_tmp = c->a_tmp.p;

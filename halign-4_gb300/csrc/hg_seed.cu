@@ -24,8 +24,8 @@
 // slot and the queue keeps that corrupted state for a while.  The tile pass
 // detects the first such position (the only way the queue can be full) and
 // queues the whole query for seed_exact_kernel, which replays the reference's
-// ring buffer sequentially (one thread per query) and overwrites the tile
-// pass's output for that query.
+// ring buffer sequentially (one warp per query, the ring walk on one lane)
+// and overwrites the tile pass's output for that query.
 #include "hg_batch.cuh"
 
 namespace hg {
@@ -37,7 +37,6 @@ constexpr int kMaxWin = 255;
 constexpr int kMaxK = 31;
 constexpr int kCodeBuf = kSeedTile + 512;
 constexpr int kHashBuf = kSeedTile + kMaxWin + 1;
-constexpr int kExactBlocks = 8, kExactThreads = 32;
 
 struct SeedOut {
     int mode;        // 0: matched hits (pos, entry); 1: every hit as MinimizerHit words
@@ -420,86 +419,152 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDe
 // Sequential replay of extractMinimizer for the queries whose deque
 // overflows, with the reference's ring indexing (RingMinQueue::idx subtracts
 // the capacity once).  Ring entries past the capacity live in spare slots of
-// this thread's scratch ring, i.e. they behave as plain memory (the reference
-// writes past its vector there).
-__global__ void seed_exact_kernel(IndexDev ix, BatchDev b, SeedOut so)
+// the warp's ring, i.e. they behave as plain memory (the reference writes
+// past its vector there).  One warp per query: per chunk of 32 positions the
+// lanes decode the bases, build the k-mer codes by a shuffle scan and hash
+// them; lane 0 runs the ring over the chunk in shared memory (the only
+// sequential part); the lanes then look the chunk's emitted minimizers up in
+// the center index together and write them in order.
+constexpr int kExactWarps = 4;
+constexpr int kExactBlocks = 64;
+
+__host__ __device__ __forceinline__ size_t exact_warp_bytes(int ring_slots)
 {
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nt = gridDim.x * blockDim.x;
+    return ((size_t)ring_slots * 12 + 32 * 20 + 15) & ~(size_t)15;
+}
+
+__global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev ix, BatchDev b, SeedOut so)
+{
+    extern __shared__ uint64_t ex_smem[];
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const int RS = b.ring_slots;
+    uint64_t* hs = ex_smem + wl * (exact_warp_bytes(RS) / 8);  // chunk hashes
+    uint64_t* eh = hs + 32;                                     // chunk emissions: hash
+    uint64_t* rh = eh + 32;                                     // ring: hash
+    uint32_t* ep = reinterpret_cast<uint32_t*>(rh + RS);        // chunk emissions: position
+    uint32_t* rp = ep + 32;                                     // ring: position
     const unsigned total = *b.n_exact;
     const int k = ix.k;
     const uint64_t kmask = (1ULL << (2 * k)) - 1ULL;
-    const int kshift = 2 * (k - 1);
-    uint64_t* rh = b.ring_h + (size_t)gt * b.ring_slots;
-    uint32_t* rp = b.ring_p + (size_t)gt * b.ring_slots;
-    for (unsigned wi = gt; wi < total; wi += nt) {
+    const uint32_t last_slot = (uint32_t)RS - 1;
+    for (unsigned wi = blockIdx.x * kExactWarps + wl; wi < total; wi += gridDim.x * kExactWarps) {
         const int q = (int)b.exact_list[wi];
         const uint32_t n = (uint32_t)b.qlen[q];
         const uint8_t* pk = b.packed + b.poff[q];
-        int64_t e = b.exc_off[q];
+        int64_t ecur = b.exc_off[q];
         const int64_t e1 = b.exc_off[q + 1];
         const int64_t hb = b.hoff[q];
         const uint32_t nk = n - (uint32_t)k + 1;
         const uint32_t win = (uint32_t)ix.w < nk ? (uint32_t)ix.w : nk;
-        uint64_t fwd = 0, rev = 0, last_h = 0;
+        for (int t = lane; t < RS; t += 32) rh[t] = 0, rp[t] = 0;
+        uint64_t last_h = 0, prev = 0;
         uint32_t valid = 0, head = 0, size = 0, last_p = 0;
         bool has_last = false;
         int n_hits = 0, n_match = 0;
-        for (uint32_t i = 0; i < n; ++i) {
-            while (e < e1 && (uint32_t)(b.exc[e * 3] + b.exc[e * 3 + 1]) <= i) ++e;
-            uint32_t c = packed_code(pk, i);
-            if (e < e1 && (uint32_t)b.exc[e * 3] <= i) c = nt4_of((uint8_t)b.exc[e * 3 + 2]);
-            if (c >= 4) {
-                fwd = rev = 0, valid = 0, head = size = 0, has_last = false;
-                continue;
+        __syncwarp();
+        for (uint32_t i0 = 0; i0 < n; i0 += 32) {
+            const uint32_t i = i0 + (uint32_t)lane;
+            uint32_t c = 0;
+            if (i < n) {
+                c = packed_code(pk, i);
+                for (int64_t ee = ecur; ee < e1 && (uint32_t)b.exc[ee * 3] <= i; ++ee)
+                    if (i < (uint32_t)(b.exc[ee * 3] + b.exc[ee * 3 + 1])) c = nt4_of((uint8_t)b.exc[ee * 3 + 2]);
             }
-            fwd = ((fwd << 2) | c) & kmask;
-            rev = (rev >> 2) | ((uint64_t)(3u ^ c) << kshift);
-            if (valid < (uint32_t)k) ++valid;
-            if (valid < (uint32_t)k) continue;
-            const uint32_t pos = i + 1 - (uint32_t)k;
-            const uint64_t code = ix.non_canonical ? fwd : (fwd < rev ? fwd : rev);
-            const uint64_t h = splitmix64(code) >> 8;
-            const uint32_t last_slot = (uint32_t)b.ring_slots - 1;
-            while (size) {
-                uint32_t bi = head + size - 1;
-                if (bi >= win) bi -= win;
-                if (rh[min(bi, last_slot)] >= h) --size;
-                else break;
+            while (ecur < e1 && (uint32_t)(b.exc[ecur * 3] + b.exc[ecur * 3 + 1]) <= i0 + 32u) ++ecur;
+            const unsigned badm = __ballot_sync(FULL, i < n && c >= 4);
+            // codes of positions i0 .. i, newest in the low bits
+            uint64_t x = (uint64_t)(c & 3u);
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint64_t y = __shfl_up_sync(FULL, x, d);
+                if (lane >= d) x |= y << (2 * d);
             }
-            {
-                uint32_t bi = head + size;
-                if (bi >= win) bi -= win;
-                bi = min(bi, last_slot);
-                rh[bi] = h, rp[bi] = pos;
-                ++size;
+            const uint64_t fwd = (lane == 31 ? x : (prev << (2 * (lane + 1))) | x) & kmask;
+            prev = __shfl_sync(FULL, x, 31);
+            uint64_t code = fwd;
+            bool strand = true;
+            if (!ix.non_canonical) {  // reverse complement: 2-bit groups reversed, complemented
+                uint64_t r = __brevll(fwd);
+                r = ((r >> 1) & 0x5555555555555555ULL) | ((r & 0x5555555555555555ULL) << 1);
+                r = (r >> (64 - 2 * k)) ^ kmask;
+                strand = fwd <= r;
+                code = fwd < r ? fwd : r;
             }
-            if (pos + 1 < win) continue;
-            const uint32_t ws = pos + 1 - win;
-            while (size && rp[head] < ws) head = head + 1 >= win ? head + 1 - win : head + 1, --size;
-            if (size) {
-                const uint64_t ch = rh[head];
-                const uint32_t cp = rp[head];
-                if (!has_last || ch != last_h || cp != last_p) {
-                    if (so.mode == 0) {
-                        const uint32_t ent = index_find(ix, ch);
-                        if (ent != kEmptyKey) {
-                            b.hit_pos[hb + n_match] = cp;
-                            b.hit_ent[hb + n_match] = ent;
-                            ++n_match;
-                        }
-                    } else {
-                        const bool strand = ix.non_canonical ? true : (fwd <= rev);
-                        so.hx[hb + n_hits] = (ch << 8) | (uint64_t)(uint8_t)k;
-                        so.hy[hb + n_hits] = ((uint64_t)(strand ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
+            const unsigned strm = __ballot_sync(FULL, strand);
+            hs[lane] = splitmix64(code) >> 8;
+            __syncwarp();
+            int ne = 0;
+            unsigned esm = 0;  // strand bit of each emission
+            if (lane == 0) {
+                const uint32_t lim = min(32u, n - i0);
+                for (uint32_t l = 0; l < lim; ++l) {
+                    if (badm >> l & 1u) {
+                        valid = 0, head = size = 0, has_last = false;
+                        continue;
                     }
-                    ++n_hits;
-                    last_h = ch, last_p = cp, has_last = true;
+                    if (valid < (uint32_t)k) ++valid;
+                    if (valid < (uint32_t)k) continue;
+                    const uint32_t pos = i0 + l + 1 - (uint32_t)k;
+                    const uint64_t h = hs[l];
+                    while (size) {
+                        uint32_t bi = head + size - 1;
+                        if (bi >= win) bi -= win;
+                        if (rh[min(bi, last_slot)] >= h) --size;
+                        else break;
+                    }
+                    {
+                        uint32_t bi = head + size;
+                        if (bi >= win) bi -= win;
+                        bi = min(bi, last_slot);
+                        rh[bi] = h, rp[bi] = pos;
+                        ++size;
+                    }
+                    if (pos + 1 < win) continue;
+                    const uint32_t ws = pos + 1 - win;
+                    while (size && rp[head] < ws) head = head + 1 >= win ? head + 1 - win : head + 1, --size;
+                    if (size) {
+                        const uint64_t ch = rh[head];
+                        const uint32_t cp = rp[head];
+                        if (!has_last || ch != last_h || cp != last_p) {
+                            eh[ne] = ch, ep[ne] = cp;
+                            esm |= (strm >> l & 1u) << ne;
+                            ++ne;
+                            last_h = ch, last_p = cp, has_last = true;
+                        }
+                    }
                 }
             }
+            ne = __shfl_sync(FULL, ne, 0);
+            esm = __shfl_sync(FULL, esm, 0);
+            __syncwarp();
+            if (ne) {
+                const bool act = lane < ne;
+                const uint64_t ch = act ? eh[lane] : 0;
+                const uint32_t cp = act ? ep[lane] : 0;
+                if (so.mode == 0) {
+                    const uint32_t ent = act ? index_find(ix, ch) : kEmptyKey;
+                    const bool hit = act && ent != kEmptyKey;
+                    const unsigned mm = __ballot_sync(FULL, hit);
+                    if (hit) {
+                        const int r = n_match + __popc(mm & ((1u << lane) - 1u));
+                        b.hit_pos[hb + r] = cp;
+                        b.hit_ent[hb + r] = ent;
+                    }
+                    n_match += __popc(mm);
+                } else if (act) {
+                    so.hx[hb + n_hits + lane] = (ch << 8) | (uint64_t)(uint8_t)k;
+                    so.hy[hb + n_hits + lane] =
+                        ((uint64_t)((esm >> lane & 1u) ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
+                }
+                n_hits += ne;
+            }
+            __syncwarp();
         }
-        b.n_hits[q] = n_hits;
-        b.n_matched[q] = n_match;
+        if (lane == 0) {
+            b.n_hits[q] = n_hits;
+            b.n_matched[q] = n_match;
+        }
     }
 }
 
@@ -516,8 +581,7 @@ extern "C" cudaError_t hg_launch_seed(const hg::IndexDev* ix, const hg::BatchDev
         hg::seed_fast_kernel<<<grid, hg::kSeedFastWarps * 32, 0, st>>>(*ix, *b);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    hg::seed_exact_kernel<<<hg::kExactBlocks, hg::kExactThreads, 0, st>>>(*ix, *b, so);
+    hg::seed_exact_kernel<<<hg::kExactBlocks, hg::kExactWarps * 32,
+                            hg::kExactWarps * hg::exact_warp_bytes(b->ring_slots), st>>>(*ix, *b, so);
     return cudaGetLastError();
 }
-
-extern "C" int hg_exact_ring_threads(void) { return hg::kExactBlocks * hg::kExactThreads; }

@@ -276,13 +276,15 @@ def dp_center(raw: bytes) -> bytes:
 
 
 def test_thin_tier_vs_oracle(gpu, oracle, pkg):
-    """Thin end segments (thread DP with checkpointed rows): every CIGAR and
-    row equals the oracle's, on a plain center and on one carrying N runs."""
+    """Thin end segments (grouped wavefronts): every CIGAR and row equals the
+    oracle's, on a plain center, one carrying N runs and one carrying U."""
     center, cases = thin_cases(pkg)
     c2 = bytearray(center)
     for a in (700, 4100, 8800):
         c2[a:a + 30] = b"N" * 30
-    for raw in (center, bytes(c2)):
+    # U stays U in the DP center, a non-A/C/G/T code there
+    c3 = center[:3000].replace(b"T", b"U") + center[3000:9000] + center[9000:].replace(b"T", b"U")
+    for raw in (center, bytes(c2), c3):
         cmx, cmy = oracle.extract_minimizer(raw)
         cen = dp_center(raw)
         seqs = b"".join(cases)
@@ -313,6 +315,10 @@ def test_batch_window_overflow_vs_oracle(gpu, oracle, pkg):
         assert run is not None
         a = int(rng.integers(0, 4000))
         cases.append(center[a:a + 800] + run.encode() + center[a + 800:a + 1800])
+        if it < 2:  # exception bytes around the run: lowercase, an N run, U
+            cases.append((center[a:a + 800] + run.encode() + center[a + 800:a + 1800]).lower())
+            cases.append(center[a:a + 700] + b"N" * 40 + center[a + 740:a + 800] + run.encode() +
+                         center[a + 800:a + 1800].replace(b"T", b"U"))
     cases.append(center[1000:5000])
     seqs = b"".join(cases)
     offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
