@@ -113,45 +113,76 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             carry = __shfl_sync(FULL, fi, 31);
         }
         __syncwarp();
-        // ---- verification: the reference's candidate scan for every anchor
-        // with the speculated f and p (whose marks then only ever target the
-        // next candidate); lane l takes anchor ib + l; the first anchor whose
-        // result differs ends it
+        // ---- verification.  With the speculated f, anchor i's reference scan
+        // keeps (f_i, p_i) unless some candidate j <= i-2 totals more than f_i
+        // (ties do not improve; where the scan stops then does not matter).
+        // A total is at most f_j + min(span, dg) (the gap penalty is >= 0), so
+        // the candidates i-kNear .. i-2 are bounded one by one (scored exactly
+        // only when the bound fails) and all older ones at once through the
+        // prefix maximum of f; an anchor the bounds do not clear runs the
+        // reference's scan (lane l takes anchor ib + l; the first anchor whose
+        // result differs ends it).
+        constexpr int kNear = 8;
         int bad = A;
+        int32_t mcarry = INT32_MIN;  // max f over anchors 0 .. ib - kNear - 2
         for (int ib = 0; ib < A && bad == A; ib += 32) {
             const int i = ib + lane;
+            const int jf = i - kNear - 1;  // max f over 0 .. jf: the bound of the older candidates
+            int32_t mf = (jf >= 0 && jf < A) ? f[jf] : INT32_MIN;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t v = __shfl_up_sync(FULL, mf, o);
+                if (lane >= o) mf = max(mf, v);
+            }
+            mf = max(mf, mcarry);
+            mcarry = __shfl_sync(FULL, mf, 31);
             int mine = A;
             if (i > 0 && i < A) {
                 const uint32_t ri = ar[i], qv = aq[i];
-                const int jmin = max(0, i - ix.max_iter);
-                int32_t max_f = span;
-                int max_j = -1, n_skip = 0;
-                bool mark_next = false;
-                // candidate j's fields, the next candidate's loaded one step ahead
-                uint32_t rj = ar[i - 1], qj = aq[i - 1];
-                int32_t fj = f[i - 1], pj = p[i - 1];
-                for (int j = i - 1; j >= jmin; --j) {
-                    const int jn = j > 0 ? j - 1 : 0;
-                    const uint32_t rn = ar[jn], qn = aq[jn];
-                    const int32_t fn = f[jn], pn = p[jn];
-                    const uint32_t rc = rj, qc = qj;
-                    const int32_t fc = fj, pc = pj;
-                    rj = rn, qj = qn, fj = fn, pj = pn;
-                    if ((int32_t)(ri - rc) > ix.max_dist_x) break;  // before the window start
-                    const bool marked = mark_next;
-                    mark_next = false;
+                const int32_t fi = f[i];
+                bool ok = mf == INT32_MIN || (int64_t)mf + span <= (int64_t)fi;
+#pragma unroll
+                for (int d = 2; d <= kNear; ++d) {
+                    const int j = i - d;
+                    if (!ok || j < 0) break;
+                    const uint32_t rc = ar[j], qc = aq[j];
+                    const int32_t fc = f[j];
+                    const int32_t dg = min((int32_t)(qv - qc), (int32_t)(ri - rc));
+                    if ((int64_t)fc + min(span, dg) <= (int64_t)fi) continue;
                     const int32_t sc = chain_score(ix, lg2, ri, qv, rc, qc, span);
-                    if (sc == INT32_MIN) continue;
-                    const int32_t tot = fc + sc;
-                    if (tot > max_f) {
-                        max_f = tot, max_j = j;
-                        if (n_skip > 0) --n_skip;
-                    } else if (marked) {
-                        if (++n_skip > ix.max_skip) break;
-                    }
-                    mark_next = pc == j - 1;
+                    if (sc != INT32_MIN && (int64_t)fc + sc > (int64_t)fi) ok = false;
                 }
-                if (max_f != f[i] || max_j != p[i]) mine = i;
+                if (!ok) {
+                    const int jmin = max(0, i - ix.max_iter);
+                    int32_t max_f = span;
+                    int max_j = -1, n_skip = 0;
+                    bool mark_next = false;
+                    // candidate j's fields, the next candidate's loaded one step ahead
+                    uint32_t rj = ar[i - 1], qj = aq[i - 1];
+                    int32_t fj = f[i - 1], pj = p[i - 1];
+                    for (int j = i - 1; j >= jmin; --j) {
+                        const int jn = j > 0 ? j - 1 : 0;
+                        const uint32_t rn = ar[jn], qn = aq[jn];
+                        const int32_t fn = f[jn], pn = p[jn];
+                        const uint32_t rc = rj, qc = qj;
+                        const int32_t fc = fj, pc = pj;
+                        rj = rn, qj = qn, fj = fn, pj = pn;
+                        if ((int32_t)(ri - rc) > ix.max_dist_x) break;  // before the window start
+                        const bool marked = mark_next;
+                        mark_next = false;
+                        const int32_t sc = chain_score(ix, lg2, ri, qv, rc, qc, span);
+                        if (sc == INT32_MIN) continue;
+                        const int32_t tot = fc + sc;
+                        if (tot > max_f) {
+                            max_f = tot, max_j = j;
+                            if (n_skip > 0) --n_skip;
+                        } else if (marked) {
+                            if (++n_skip > ix.max_skip) break;
+                        }
+                        mark_next = pc == j - 1;
+                    }
+                    if (max_f != fi || max_j != p[i]) mine = i;
+                }
             }
             bad = __reduce_min_sync(FULL, mine);
         }
