@@ -392,6 +392,21 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         // empty segments (both lengths 0) contribute no op: only the others
         // are stored, in order
         uint32_t rpos = 0, qpos = 0, slot = 0, nkept = 0;
+        // consecutive match segments (and anchor spans, which are match
+        // segments) become one record of their summed length: their ops are
+        // all M and merge in the CIGAR anyway.  A run still open at the end of
+        // a 32-segment chunk is carried (record id, start, length so far).
+        bool open = false;
+        uint32_t o_sid = 0, o_rs = 0, o_qs = 0, o_len = 0;
+        auto put_match = [&](uint32_t id, uint32_t mrs, uint32_t mqs, uint32_t mlen) {
+            Seg g;
+            g.rs = mrs, g.qs = mqs, g.rl = mlen, g.ql = mlen;
+            g.slot = 0;
+            g.nops = 0;
+            g.q = (uint32_t)q;
+            g.kind = kSegMatch;
+            b.seg[id] = g;
+        };
         // Equal-length segments whose sides are identical A/C/G/T strings (the
         // span of an exact k-mer anchor after overlap clipping) align as rl M:
         // the diagonal scores 5 rl, any other path needs an insertion and a
@@ -461,11 +476,50 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             }
             const bool keep = act && kind != kSegEmpty;
             const unsigned kmask = __ballot_sync(FULL, keep);
-            const uint32_t sid = (uint32_t)sb + nkept + (uint32_t)__popc(kmask & ((1u << lane) - 1u));
+            const bool isM = keep && kind == kSegMatch;
+            const unsigned mmask = __ballot_sync(FULL, isM);
+            const unsigned below = (1u << lane) - 1u;
+            const unsigned kb = kmask & below;
+            const bool prev_m = kb ? ((mmask >> (31 - __clz(kb))) & 1u) != 0 : open;
+            const bool cont = isM && prev_m;  // continues the match run before it
+            const bool rec = keep && !cont;   // starts a record
+            const unsigned rmask = __ballot_sync(FULL, rec);
+            const uint32_t sid = (uint32_t)sb + nkept + (uint32_t)__popc(rmask & below);
+            // a carried run ends where this chunk's first kept segment is not a match
+            if (open && kmask && !((mmask >> (__ffs(kmask) - 1)) & 1u)) {
+                if (lane == 0) put_match(o_sid, o_rs, o_qs, o_len);
+                open = false;
+            }
+            // match runs: length so far = prefix sum since the run head (or the carried run)
+            const uint32_t mlen = isM ? rl : 0u;
+            const uint32_t minc = warp_incl_sum(mlen);
+            const unsigned hm = __ballot_sync(FULL, isM && !cont);
+            const unsigned hup = hm & ((2u << lane) - 1u);
+            const int h = hup ? 31 - __clz(hup) : -1;  // this lane's run head (-1: the carried run)
+            const int hs = h >= 0 ? h : 0;
+            const uint32_t h_exc = __shfl_sync(FULL, minc - mlen, hs);
+            const uint32_t h_sid = __shfl_sync(FULL, sid, hs), h_rs = __shfl_sync(FULL, rs, hs),
+                           h_qs = __shfl_sync(FULL, qs, hs);
+            const uint32_t run_len = h >= 0 ? minc - h_exc : o_len + minc;
+            const uint32_t r_sid = h >= 0 ? h_sid : o_sid, r_rs = h >= 0 ? h_rs : o_rs, r_qs = h >= 0 ? h_qs : o_qs;
+            const unsigned ka = kmask & ~((2u << lane) - 1u);  // kept segments after this one
+            if (isM && ka && !((mmask >> (__ffs(ka) - 1)) & 1u)) put_match(r_sid, r_rs, r_qs, run_len);
+            if (kmask) {  // the chunk's last kept segment decides what is carried
+                const int last = 31 - __clz(kmask);
+                if ((mmask >> last) & 1u) {
+                    o_len = __shfl_sync(FULL, run_len, last);
+                    o_sid = __shfl_sync(FULL, r_sid, last);
+                    o_rs = __shfl_sync(FULL, r_rs, last);
+                    o_qs = __shfl_sync(FULL, r_qs, last);
+                    open = true;
+                } else {
+                    open = false;
+                }
+            }
             const uint32_t need = (seg_is_dp(kind) && act) ? rl + ql : 0;
             const uint32_t sincl = warp_incl_sum(need);
             const uint32_t my_slot = slot + sincl - need;
-            if (keep) {
+            if (rec && !isM) {
                 Seg g;
                 g.rs = rs, g.qs = qs, g.rl = rl, g.ql = ql;
                 g.slot = my_slot;
@@ -474,7 +528,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 g.kind = kind | flags;
                 b.seg[sid] = g;
             }
-            nkept += (uint32_t)__popc(kmask);
+            nkept += (uint32_t)__popc(rmask);
             // tier work lists (warp-aggregated appends): small, thin, one-warp
             // wavefront, CTA wavefront, exact
             const bool dp_big = act && (kind == kSegDpLarge || kind == kSegGlobal);
@@ -498,7 +552,6 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             bw = __shfl_sync(FULL, bw, 0);
             bx = __shfl_sync(FULL, bx, 0);
             bt = __shfl_sync(FULL, bt, 0);
-            const unsigned below = (1u << lane) - 1u;
             if (ms >> lane & 1u) {
                 const unsigned w = bs + __popc(ms & below);
                 if ((int64_t)w < b.wcap) {
@@ -567,6 +620,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             qpos = (uint32_t)__shfl_sync(FULL, iq, 31);
             slot = slot + __shfl_sync(FULL, sincl, 31);
         }
+        if (open && lane == 0) put_match(o_sid, o_rs, o_qs, o_len);
         if (lane == 0) b.s_n[q] = (int32_t)nkept;
     }
 }
