@@ -87,13 +87,20 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         // last f of the previous chunk.
         constexpr int64_t kNeg = -((int64_t)1 << 40);
         int64_t carry = kNeg;
+        uint32_t pr = 0, pqv = 0;  // positions of anchor c0 - 1 (the previous chunk's last)
+        uint32_t nar = lane < A ? ar[lane] : 0u, naq = lane < A ? aq[lane] : 0u;  // chunk 0
         for (int c0 = 0; c0 < A; c0 += 32) {
             const int i = c0 + lane;
+            const uint32_t ri = nar, qv = naq;
+            nar = i + 32 < A ? ar[i + 32] : 0u;  // next chunk, loaded ahead
+            naq = i + 32 < A ? aq[i + 32] : 0u;
+            uint32_t rj = __shfl_up_sync(FULL, ri, 1), qj = __shfl_up_sync(FULL, qv, 1);
+            if (lane == 0) rj = pr, qj = pqv;
+            pr = __shfl_sync(FULL, ri, 31), pqv = __shfl_sync(FULL, qv, 31);
             int64_t sv = kNeg;
             if (i > 0 && i < A) {
-                const uint32_t ri = ar[i], rj = ar[i - 1];
                 if ((int32_t)(ri - rj) <= ix.max_dist_x) {  // i-1 inside the window of i
-                    const int32_t sc = chain_score(ix, lg2, ri, aq[i], rj, aq[i - 1], span);
+                    const int32_t sc = chain_score(ix, lg2, ri, qv, rj, qj, span);
                     if (sc != INT32_MIN) sv = sc;
                 }
             }
@@ -141,12 +148,19 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 const uint32_t ri = ar[i], qv = aq[i];
                 const int32_t fi = f[i];
                 bool ok = mf == INT32_MIN || (int64_t)mf + span <= (int64_t)fi;
+                // all near candidates' fields are loaded before any is tested
+                uint32_t nr[kNear - 1], nq[kNear - 1];
+                int32_t nf[kNear - 1];
 #pragma unroll
                 for (int d = 2; d <= kNear; ++d) {
-                    const int j = i - d;
-                    if (!ok || j < 0) break;
-                    const uint32_t rc = ar[j], qc = aq[j];
-                    const int32_t fc = f[j];
+                    const int j = max(i - d, 0);
+                    nr[d - 2] = ar[j], nq[d - 2] = aq[j], nf[d - 2] = f[j];
+                }
+#pragma unroll
+                for (int d = 2; d <= kNear; ++d) {
+                    if (i - d < 0) break;
+                    const uint32_t rc = nr[d - 2], qc = nq[d - 2];
+                    const int32_t fc = nf[d - 2];
                     const int32_t dg = min((int32_t)(qv - qc), (int32_t)(ri - rc));
                     if ((int64_t)fc + min(span, dg) <= (int64_t)fi) continue;
                     const int32_t sc = chain_score(ix, lg2, ri, qv, rc, qc, span);
