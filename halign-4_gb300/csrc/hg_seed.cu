@@ -76,9 +76,11 @@ constexpr int kSeedFastChunk = 32 * kSeedPer;  // k-mer starts per warp step
 __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(IndexDev ix, BatchDev b)
 {
     __shared__ uint64_t hbuf[kSeedFastWarps][16 + kSeedFastChunk];
+    __shared__ uint32_t pbuf[kSeedFastWarps][kSeedFastChunk];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     uint64_t* hs = hbuf[threadIdx.x >> 5];
+    uint32_t* ps = pbuf[threadIdx.x >> 5];
     const int k = ix.k;
     const int lsh = 64 - 2 * k;
     for (;;) {
@@ -148,34 +150,45 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
                 inc |= (A[i - 1] != kNoHash && A[i] != kNoHash && A[i - 1] < A[i]) ? (1u << i) : 0u;
             const uint32_t r2 = inc & (inc >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4), r10 = r8 & (r2 >> 8);
             const uint32_t ovf = (r10 >> 7) & 0xffu;  // run of ten starting at bit 7+i ends at bit 16+i
-            // emission and index lookups
-            int n_emit = 0, n_match = 0;
-            uint32_t ent[kSeedPer];
+            // emission; the chunk's emitted minimizers are compacted (in position
+            // order) into the free part of the warp's buffers, then probed in the
+            // index densely, one per lane
             uint32_t emask = 0;
 #pragma unroll
             for (int i = 0; i < kSeedPer; ++i) {
                 const int p = P0 + i;
-                ent[i] = kEmptyKey;
                 if (((ovf >> i) & 1u) && p - kFastWin >= 0 && p < nk) ovf_any = true;
                 if (p >= nk || p < kFastWin - 1) continue;
                 if (p > kFastWin - 1 && mp[i + 1] == mp[i]) continue;
                 emask |= 1u << i;
-                ++n_emit;
-                ent[i] = index_find(ix, Om[16 + i] >> 8);
-                if (ent[i] != kEmptyKey) ++n_match;
             }
-            const int incl = warp_incl_sum(n_match);
-            int o = total_matched + incl - n_match;
+            const int n_emit = __popc(emask);
+            const int eincl = warp_incl_sum(n_emit);
+            const int n_chunk = __shfl_sync(FULL, eincl, 31);
+            int e = eincl - n_emit;
 #pragma unroll
             for (int i = 0; i < kSeedPer; ++i) {
-                if ((emask >> i & 1u) && ent[i] != kEmptyKey) {
-                    b.hit_pos[hb + o] = (uint32_t)mp[i + 1];
-                    b.hit_ent[hb + o] = ent[i];
-                    ++o;
+                if (emask >> i & 1u) {
+                    hs[16 + e] = Om[16 + i] >> 8;
+                    ps[e] = (uint32_t)mp[i + 1];
+                    ++e;
                 }
             }
-            total_matched += __shfl_sync(FULL, incl, 31);
-            total_hits += __reduce_add_sync(FULL, (unsigned)n_emit);
+            __syncwarp();
+            for (int e0 = 0; e0 < n_chunk; e0 += 32) {
+                const int ei = e0 + lane;
+                const uint32_t ent = ei < n_chunk ? index_find(ix, hs[16 + ei]) : kEmptyKey;
+                const bool hit = ent != kEmptyKey;
+                const unsigned hm = __ballot_sync(FULL, hit);
+                if (hit) {
+                    const int o = total_matched + __popc(hm & ((1u << lane) - 1u));
+                    b.hit_pos[hb + o] = ps[ei];
+                    b.hit_ent[hb + o] = ent;
+                }
+                total_matched += __popc(hm);
+            }
+            __syncwarp();
+            total_hits += n_chunk;
         }
         const bool ovf_q = __any_sync(FULL, ovf_any);
         if (lane == 0) {
