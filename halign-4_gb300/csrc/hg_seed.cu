@@ -26,6 +26,8 @@
 // queues the whole query for seed_exact_kernel, which replays the reference's
 // ring buffer sequentially (one warp per query, the ring walk on one lane)
 // and overwrites the tile pass's output for that query.
+#include <type_traits>
+
 #include "hg_batch.cuh"
 
 namespace hg {
@@ -97,10 +99,13 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
         if (lane < 16) hs[lane] = kNoHash;  // positions before 0
         int total_hits = 0, total_matched = 0;
         bool ovf_any = false;
-        for (int t0 = 0; t0 < nk; t0 += kSeedFastChunk) {
+        // EDGE: a chunk touching position 0 or the query end (hashes past either
+        // end are kNoHash); interior chunks skip those tests
+        auto chunk = [&](auto edge_tag, const int t0) {
+            constexpr bool EDGE = decltype(edge_tag)::value;
             const int P0 = t0 + lane * kSeedPer;
             uint64_t h[kSeedPer];
-            if (P0 < nk) {
+            if (!EDGE || P0 < nk) {
                 const uint32_t wb = ((uint32_t)P0 >> 2) & ~7u;
                 const uint64_t* w = reinterpret_cast<const uint64_t*>(pk + wb);
                 const uint64_t w0 = w[0], w1 = w[1];
@@ -110,7 +115,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
                 x = ((x >> 1) & 0x5555555555555555ULL) | ((x & 0x5555555555555555ULL) << 1);
 #pragma unroll
                 for (int i = 0; i < kSeedPer; ++i)
-                    h[i] = P0 + i < nk ? splitmix64((x << (2 * i)) >> lsh) >> 8 : kNoHash;
+                    h[i] = (!EDGE || P0 + i < nk) ? splitmix64((x << (2 * i)) >> lsh) >> 8 : kNoHash;
             } else {
 #pragma unroll
                 for (int i = 0; i < kSeedPer; ++i) h[i] = kNoHash;
@@ -129,7 +134,8 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
             // window minimum over keys
             uint64_t key[24], Pm[24], Qm[24], Om[24];
 #pragma unroll
-            for (int i = 0; i < 24; ++i) key[i] = A[i] == kNoHash ? ~0ull : (A[i] << 8) | (uint64_t)(254 - i);
+            for (int i = 0; i < 24; ++i)
+                key[i] = (EDGE && A[i] == kNoHash) ? ~0ull : (A[i] << 8) | (uint64_t)(254 - i);
 #pragma unroll
             for (int i = 7; i < 24; ++i) Pm[i] = umin64(key[i - 1], key[i]);
 #pragma unroll
@@ -147,7 +153,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
             uint32_t inc = 0;
 #pragma unroll
             for (int i = 1; i < 24; ++i)
-                inc |= (A[i - 1] != kNoHash && A[i] != kNoHash && A[i - 1] < A[i]) ? (1u << i) : 0u;
+                inc |= ((!EDGE || (A[i - 1] != kNoHash && A[i] != kNoHash)) && A[i - 1] < A[i]) ? (1u << i) : 0u;
             const uint32_t r2 = inc & (inc >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4), r10 = r8 & (r2 >> 8);
             const uint32_t ovf = (r10 >> 7) & 0xffu;  // run of ten starting at bit 7+i ends at bit 16+i
             // emission; the chunk's emitted minimizers are compacted (in position
@@ -157,9 +163,9 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
 #pragma unroll
             for (int i = 0; i < kSeedPer; ++i) {
                 const int p = P0 + i;
-                if (((ovf >> i) & 1u) && p - kFastWin >= 0 && p < nk) ovf_any = true;
-                if (p >= nk || p < kFastWin - 1) continue;
-                if (p > kFastWin - 1 && mp[i + 1] == mp[i]) continue;
+                if (((ovf >> i) & 1u) && (!EDGE || (p - kFastWin >= 0 && p < nk))) ovf_any = true;
+                if (EDGE && (p >= nk || p < kFastWin - 1)) continue;
+                if ((!EDGE || p > kFastWin - 1) && mp[i + 1] == mp[i]) continue;
                 emask |= 1u << i;
             }
             const int n_emit = __popc(emask);
@@ -189,6 +195,10 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
             }
             __syncwarp();
             total_hits += n_chunk;
+        };
+        for (int t0 = 0; t0 < nk; t0 += kSeedFastChunk) {
+            if (t0 > 0 && t0 + kSeedFastChunk <= nk) chunk(std::false_type{}, t0);
+            else chunk(std::true_type{}, t0);
         }
         const bool ovf_q = __any_sync(FULL, ovf_any);
         if (lane == 0) {
