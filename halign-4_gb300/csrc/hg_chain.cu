@@ -439,27 +439,34 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const uint64_t m = n >= 32 ? ~0ull : ((1ull << (2 * n)) - 1ull);
             return ((window(b.packed, qp) ^ window(ix.center2, rp)) & m) == 0;
         };
+        // raw end of segment s (before clipping and the prefix max)
+        auto seg_end = [&](int s, int64_t& er, int64_t& eq, uint32_t& flags) {
+            er = 0, eq = 0, flags = 0;
+            if (s >= nseg) return;
+            if (c == 0) {
+                er = L, eq = len;
+            } else if (s == 0) {
+                const int a = t[c - 1];
+                er = ar[a], eq = aq[a], flags = kSegLeft;
+            } else if (s == 2 * c) {
+                er = L, eq = len;
+            } else if (s & 1) {
+                const int a = t[c - 1 - (s - 1) / 2];
+                er = (int64_t)ar[a] + span, eq = (int64_t)aq[a] + span;
+            } else {
+                const int a = t[c - 1 - s / 2];
+                er = ar[a], eq = aq[a];
+            }
+        };
+        int64_t n_er, n_eq;
+        uint32_t n_flags;
+        seg_end(lane, n_er, n_eq, n_flags);
         for (int s0 = 0; s0 < nseg; s0 += 32) {
             const int s = s0 + lane;
             const bool act = s < nseg;
-            int64_t er = 0, eq = 0;
-            uint32_t flags = 0;
-            if (act) {
-                if (c == 0) {
-                    er = L, eq = len;
-                } else if (s == 0) {
-                    const int a = t[c - 1];
-                    er = ar[a], eq = aq[a], flags = kSegLeft;
-                } else if (s == 2 * c) {
-                    er = L, eq = len;
-                } else if (s & 1) {
-                    const int a = t[c - 1 - (s - 1) / 2];
-                    er = (int64_t)ar[a] + span, eq = (int64_t)aq[a] + span;
-                } else {
-                    const int a = t[c - 1 - s / 2];
-                    er = ar[a], eq = aq[a];
-                }
-            }
+            const int64_t er = n_er, eq = n_eq;
+            const uint32_t flags = n_flags;
+            seg_end(s + 32, n_er, n_eq, n_flags);  // the next chunk's ends, loaded ahead
             const int cr = act ? (int)min(er, (int64_t)L) : 0;
             const int cq = act ? (int)min(eq, (int64_t)len) : 0;
             const int ir = max(warp_incl_max(cr), (int)rpos);
@@ -580,7 +587,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 }
             }
             // histogram of small-tier shapes (lanes with equal keys add once)
-            if (b.work_key) {
+            if (ms && b.work_key) {
                 uint32_t key = 0xffffffffu;
                 if (ms >> lane & 1u) {
                     Seg g;
@@ -606,7 +613,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                     atomicOr(&b.status[q], kStArenaOverflow);
                 }
             }
-            {
+            if (mw) {
                 const unsigned peers = __match_any_sync(FULL, wkey);
                 if ((mw >> lane & 1u) && lane == __ffs(peers) - 1) atomicAdd(&b.wave_hist[wkey], __popc(peers));
             }

@@ -178,8 +178,15 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
     __shared__ int scan_s[33];
     __shared__ int s_qi;
     __shared__ uint32_t s_carry_r, s_carry_q;
+    __shared__ uint32_t lut[256];  // 4 packed 2-bit codes -> their 4 ASCII bases
     const int tid = threadIdx.x;
     const int L = ix.L;
+    for (int i = tid; i < 256; i += kRowThreads) {
+        uint32_t v = 0;
+        for (int k = 0; k < 4; ++k) v |= ((0x54474341u >> (8u * ((i >> (2 * k)) & 3))) & 0xffu) << (8 * k);
+        lut[i] = v;
+    }
+    __syncthreads();
     for (;;) {
         if (tid == 0) s_qi = (int)atomicAdd(&b.queues[5], 1u);
         __syncthreads();
@@ -227,11 +234,11 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
             }
             if (tid == kRowThreads - 1) s_r[cn] = ar, s_q[cn] = aq;
             __syncthreads();
-            const uint32_t col0 = s_r[0], col1 = min(s_r[cn], (uint32_t)L);
+            const uint32_t col0 = s_r[0], col1 = max(col0, min(s_r[cn], (uint32_t)L));
             // exception-free query: 16 whole columns per thread, one 16-byte store
             uint32_t vb = col0, ve = col0;  // [vb, ve): columns written by the vector path
             if (e0 == e1) {
-                vb = (col0 + 15u) & ~15u;
+                vb = min((col0 + 15u) & ~15u, col1);
                 ve = col1 & ~15u;
                 if (ve < vb) ve = vb;
                 for (uint32_t g0 = vb + 16u * tid; g0 < ve; g0 += 16u * kRowThreads) {
@@ -240,6 +247,25 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
                         const int mid = (lo + hi + 1) >> 1;
                         if (s_r[mid] <= g0) lo = mid;
                         else hi = mid - 1;
+                    }
+                    {  // the 16 columns inside one op: 16 query bases (one packed word) or 16 gaps
+                        const uint32_t c = s_op[lo], op = c & 0xfu;
+                        if (s_r[lo] <= g0 && s_r[lo + 1] >= g0 + 16u) {
+                            uint4 v;
+                            if (op == 0 || op == 7 || op == 8) {
+                                const uint64_t base = (uint64_t)b.poff[q] * 4u + s_q[lo] + (g0 - s_r[lo]);
+                                const uint32_t* W = reinterpret_cast<const uint32_t*>(b.packed) + (base >> 4);
+                                const uint32_t sh = 2u * (uint32_t)(base & 15u);
+                                const uint32_t w0 = W[0], w1 = W[1];
+                                const uint32_t codes = sh ? (w0 >> sh) | (w1 << (32u - sh)) : w0;
+                                v = make_uint4(lut[codes & 0xffu], lut[(codes >> 8) & 0xffu], lut[(codes >> 16) & 0xffu],
+                                               lut[codes >> 24]);
+                            } else {
+                                v = make_uint4(0x2d2d2d2du, 0x2d2d2d2du, 0x2d2d2d2du, 0x2d2d2d2du);
+                            }
+                            *reinterpret_cast<uint4*>(row + g0) = v;
+                            continue;
+                        }
                     }
                     uint64_t wlo = 0, whi = 0;
                     uint32_t qw = 0xffffffffu;  // first base of the 64-base window held in wlo/whi
@@ -271,8 +297,10 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
                     *reinterpret_cast<uint4*>(row + g0) = make_uint4(word[0], word[1], word[2], word[3]);
                 }
             }
-            for (uint32_t col = col0 + tid; col < col1; col += kRowThreads) {
-                if (col >= vb && col < ve) continue;
+            // the columns the vector path left: [col0, vb) and [ve, col1)
+            const uint32_t head = vb - col0, nrest = head + (col1 - ve);
+            for (uint32_t t = tid; t < nrest; t += kRowThreads) {
+                const uint32_t col = t < head ? col0 + t : ve + (t - head);
                 int lo = 0, hi = cn - 1;  // last op with s_r <= col and nonzero ref length
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
