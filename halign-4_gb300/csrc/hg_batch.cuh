@@ -95,25 +95,19 @@ __device__ __forceinline__ uint32_t shape_key(const Seg& g)
     return (outer - 1) | icode << 6 | tinner << 10 | left << 11 | med << 12;
 }
 
-// Thin tier: the query side 1..16 bases against a center side beyond the
-// small and medium bounds (so more than twice as long, and auto_band gives an
-// unbounded band).  Several such segments share a warp, one lane per query
-// column: a group of W = ql lanes runs one segment's anti-diagonal wavefront
-// (floor(32 / W) groups per warp), so a step costs one cell per lane however
-// short the query side is.  Direction nibbles go to the warp's own scratch
-// region (16 bytes per step), which bounds the steps (rl + ql - 1) of a thin
-// segment.
-constexpr int kThinMaxInner = 16;
+// Thin tier: the query side 1..32 bases against a longer center side beyond
+// the small and medium bounds, with a band that never binds (as for the
+// wavefront tiers).  Several such segments share a warp, one lane per query
+// column: a group of W = ql lanes (W = 32 above 16) runs one segment's
+// anti-diagonal wavefront (floor(32 / W) groups per warp), so a step costs
+// one cell per lane however short the query side is.  Direction nibbles go to
+// the warp's own scratch region (16 bytes per step), which bounds the steps
+// (rl + ql - 1) of a thin segment.
+constexpr int kThinMaxInner = 32;
 constexpr int kThinMaxSteps = 32768;
 constexpr size_t kThinWarpBytes = (size_t)kThinMaxSteps * 16;
 constexpr int kThinKeyClassShift = 7;  // key bits above it: the query length - 1 (the group width)
 constexpr int kThinBins = kThinMaxInner << kThinKeyClassShift;
-
-__host__ __device__ __forceinline__ bool thin_tier_fits(uint32_t rl, uint32_t ql)
-{
-    if (ql < 1 || ql > (uint32_t)kThinMaxInner || rl <= ql || small_tier_fits(rl, ql)) return false;
-    return (int64_t)rl + ql - 1 <= kThinMaxSteps;
-}
 
 // Sort key of a thin segment: query length first (a warp takes segments of
 // one length), then longest first by quarter-octave class of the center
@@ -144,6 +138,13 @@ __host__ __device__ __forceinline__ bool wave_eligible(uint32_t rl, uint32_t ql)
     if (2 * (outer - inner) > outer || outer <= 200) return true;
     const int w = auto_band((int)rl, (int)ql);
     return w >= (int)outer;
+}
+
+__host__ __device__ __forceinline__ bool thin_tier_fits(uint32_t rl, uint32_t ql)
+{
+    if (ql < 1 || ql > (uint32_t)kThinMaxInner || rl <= ql) return false;
+    if (small_tier_fits(rl, ql) || medium_tier_fits(rl, ql) || !wave_eligible(rl, ql)) return false;
+    return (int64_t)rl + ql - 1 <= kThinMaxSteps;
 }
 
 // Columns per lane of the one-warp wavefront: the smallest power of two with

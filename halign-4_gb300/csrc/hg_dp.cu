@@ -358,9 +358,9 @@ __device__ __forceinline__ uint32_t lane_int_nl(int z0, int xt1, int vt1, int ut
     return d;
 }
 
-// Thin tier: G = floor(32 / W) segments of query length W per warp, lane j
-// of group g owns query column j of the group's segment and computes cell
-// (s - j, j) at step s.
+// Thin tier: G = floor(32 / W) segments of query length <= W per warp (W is
+// the query length up to 16, and 32 above), lane j of group g owns query
+// column j of the group's segment and computes cell (s - j, j) at step s.
 // A cell takes its left neighbour's outputs of the previous step by one
 // shuffle (u, y and the row's center code, packed), its own previous outputs
 // as the cell above, and lane 0 of a group reads the center base of a new
@@ -502,17 +502,17 @@ __device__ __forceinline__ void thin_group(const IndexDev& ix, const BatchDev& b
 }
 
 // Persistent warps; warp gw owns thin scratch region gw.
-// Each warp starts on query length gw % 16 + 1 and moves on when that queue
+// Each warp starts on query length gw % 32 + 1 and moves on when that queue
 // is drained; a queue hands out G consecutive entries of its length's range
 // of the sorted list (longest first).
 template <int W>
-__device__ __forceinline__ void thin_drain(const IndexDev& ix, const BatchDev& b, unsigned lo, unsigned hi,
+__device__ __forceinline__ void thin_drain(const IndexDev& ix, const BatchDev& b, int cls, unsigned lo, unsigned hi,
                                            uint32_t* scratch, uint32_t* buf, unsigned long long& cells)
 {
     constexpr unsigned G = 32 / W;
     for (;;) {
         unsigned t = 0;
-        if ((threadIdx.x & 31) == 0) t = atomicAdd(&b.thin_q[W - 1], 1u);
+        if ((threadIdx.x & 31) == 0) t = atomicAdd(&b.thin_q[cls], 1u);
         t = __shfl_sync(0xffffffffu, t, 0);
         const unsigned long long f = (unsigned long long)lo + (unsigned long long)t * G;
         if (f >= hi) break;
@@ -528,18 +528,17 @@ __global__ void __launch_bounds__(kThinWarps * 32, 4) dp_thin_kernel(IndexDev ix
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int gw = blockIdx.x * kThinWarps + wl;
     if (threadIdx.x < 32) {  // per-length ranges of the sorted list from the key counters
-        constexpr int per = kThinBins / 32;  // lanes 2c and 2c+1 cover length c + 1
-        unsigned c = 0;
-        for (int k = 0; k < per; ++k) c += b.thin_hist[lane * per + k];
-        c += __shfl_down_sync(FULL, c, 1);
-        unsigned incl = (lane & 1) ? 0u : c;  // count of length lane/2 + 1 on even lanes
+        constexpr int per = kThinBins / kThinMaxInner;  // lane c covers length c + 1
+        static_assert(kThinMaxInner == 32, "one lane per query length");
+        unsigned incl = 0;
+        for (int k = 0; k < per; ++k) incl += b.thin_hist[lane * per + k];
 #pragma unroll
-        for (int o = 2; o < 32; o <<= 1) {
+        for (int o = 1; o < 32; o <<= 1) {
             const unsigned v = __shfl_up_sync(FULL, incl, o);
             if (lane >= o) incl += v;
         }
         if (lane == 0) rng[0] = 0;
-        if (!(lane & 1)) rng[lane / 2 + 1] = incl;
+        rng[lane + 1] = incl;
     }
     __syncthreads();
     if (gw >= b.thin_nwarps) return;
@@ -551,22 +550,23 @@ __global__ void __launch_bounds__(kThinWarps * 32, 4) dp_thin_kernel(IndexDev ix
         const unsigned lo = rng[c], hi = rng[c + 1];
         if (lo >= hi) continue;
         switch (c + 1) {
-        case 1: thin_drain<1>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 2: thin_drain<2>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 3: thin_drain<3>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 4: thin_drain<4>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 5: thin_drain<5>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 6: thin_drain<6>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 7: thin_drain<7>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 8: thin_drain<8>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 9: thin_drain<9>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 10: thin_drain<10>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 11: thin_drain<11>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 12: thin_drain<12>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 13: thin_drain<13>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 14: thin_drain<14>(ix, b, lo, hi, scratch, buf, cells); break;
-        case 15: thin_drain<15>(ix, b, lo, hi, scratch, buf, cells); break;
-        default: thin_drain<16>(ix, b, lo, hi, scratch, buf, cells); break;
+        case 1: thin_drain<1>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 2: thin_drain<2>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 3: thin_drain<3>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 4: thin_drain<4>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 5: thin_drain<5>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 6: thin_drain<6>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 7: thin_drain<7>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 8: thin_drain<8>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 9: thin_drain<9>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 10: thin_drain<10>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 11: thin_drain<11>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 12: thin_drain<12>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 13: thin_drain<13>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 14: thin_drain<14>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 15: thin_drain<15>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        case 16: thin_drain<16>(ix, b, c, lo, hi, scratch, buf, cells); break;
+        default: thin_drain<32>(ix, b, c, lo, hi, scratch, buf, cells); break;
         }
     }
     for (int o = 16; o > 0; o >>= 1) cells += __shfl_xor_sync(FULL, cells, o);
@@ -1498,17 +1498,20 @@ extern "C" cudaError_t hg_launch_dp_large(const hg::IndexDev* ix, const hg::Batc
     return cudaGetLastError();
 }
 
-// One-warp wavefront tier: sort its list, then run it (grid CTAs of 4
-// warps; warp i uses checkpoint slot i).
-// Thin tier (sort, then one warp per thin scratch region) followed by the
-// one-warp wavefront tier.
-extern "C" cudaError_t hg_launch_dp_wave(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+// Thin tier: sort, then one warp per thin scratch region.
+extern "C" cudaError_t hg_launch_dp_thin(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
     hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_thin, b->work_thin_key, b->thin_hist,
                                                                     b->work_thin_sorted, b->n_thin, b->wcap,
                                                                     hg::kThinBins);
     const int tgrid = (b->thin_nwarps + hg::kThinWarps - 1) / hg::kThinWarps;
     hg::dp_thin_kernel<<<tgrid, hg::kThinWarps * 32, hg::kThinSmemBytes, st>>>(*ix, *b);
+    return cudaGetLastError();
+}
+
+// One-warp wavefront tier: sort, then grid CTAs of 4 warps (warp i uses slot i).
+extern "C" cudaError_t hg_launch_dp_wave(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
+{
     hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_wave, b->work_wave_key, b->wave_hist,
                                                                     b->work_wave_sorted, b->n_wave, b->wcap,
                                                                     hg::kWaveBins);

@@ -33,6 +33,7 @@ cudaError_t hg_launch_chain(const hg::IndexDev*, const hg::BatchDev*, int, cudaS
 cudaError_t hg_launch_dp_small(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_dp_large(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_dp_wave(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
+cudaError_t hg_launch_dp_thin(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_dp_wide(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_prepare_dp_kernels(void);
 cudaError_t hg_launch_stitch(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
@@ -141,9 +142,10 @@ struct hg_ctx {
     hg_index_t* ix = nullptr;
     cudaStream_t st = nullptr;
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
+    cudaStream_t st3 = nullptr;                            // side stream of the one-warp wavefront and exact tiers
     // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
     int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 4};
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, join3_ev = nullptr;
     int sms = 1;
     int64_t max_n = 0, max_bases = 0, exc_cap = 0;
     int64_t row_stride = 0;
@@ -625,9 +627,9 @@ extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t*
 
 namespace {
 
-constexpr int kControlWords = 24;
+constexpr int kControlWords = 32;
 // control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide |
-// queues2[4] | n_thin | (free) | thin_q[16]
+// queues2[4] | n_thin | (free) | thin_q[32]
 // sort counters of the one-warp wavefront list, then of the thin list (counters and cursors each)
 constexpr size_t kSortHistWords = 2 * (size_t)hg::kWaveBins + 2 * (size_t)hg::kThinBins;
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
@@ -717,6 +719,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking)) ||
         (e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming)) ||
+        (e = cudaStreamCreateWithFlags(&c->st3, cudaStreamNonBlocking)) ||
+        (e = cudaEventCreateWithFlags(&c->join3_ev, cudaEventDisableTiming)) ||
         (e = cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking)) ||
         (e = cudaEventCreateWithFlags(&c->rows_ev[0], cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&c->rows_ev[1], cudaEventDisableTiming)) ||
@@ -810,6 +814,8 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
         if (ev) cudaEventDestroy(ev);
     if (c->comp_ev) cudaEventDestroy(c->comp_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->join3_ev) cudaEventDestroy(c->join3_ev);
+    if (c->st3) cudaStreamDestroy(c->st3);
     if (c->st2) cudaStreamDestroy(c->st2);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;  // DevBuf members are freed below via explicit frees
@@ -869,7 +875,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.n_wave = reinterpret_cast<unsigned int*>(ctl + 10);
     b.n_wide = reinterpret_cast<unsigned int*>(ctl + 11);
     b.n_thin = reinterpret_cast<unsigned int*>(ctl + 14);
-    b.thin_q = reinterpret_cast<unsigned int*>(ctl + 16);  // 16 x uint32 in words 16..23
+    b.thin_q = reinterpret_cast<unsigned int*>(ctl + 16);  // 32 x uint32 in words 16..31
     b.work_thin = c->work_thin.p, b.work_thin_key = c->work_thin_key.p, b.work_thin_sorted = c->work_thin_sorted.p;
     b.thin_hist = c->wave_hist.p + 2 * hg::kWaveBins;
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
@@ -903,16 +909,22 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(2));
     HG_CUDA(hg_launch_chain(&ix, &b, std::max(1, std::min((n + 3) / 4, S * K[2])), st));
     HG_CUDA(mark(3));
-    HG_CUDA(hg_launch_dp_small(&ix, &b, S * K[3], st));
-    HG_CUDA(mark(4));
-    // the CTA wavefront tier runs on a side stream beside the warp tiers
+    // the DP tiers are independent work lists with disjoint scratch: the CTA
+    // wavefront tier runs on st2, the one-warp wavefront and exact tiers on
+    // st3, the small and thin tiers on st (their tails overlap)
     HG_CUDA(cudaEventRecord(c->fork_ev, st));
     HG_CUDA(cudaStreamWaitEvent(c->st2, c->fork_ev, 0));
+    HG_CUDA(cudaStreamWaitEvent(c->st3, c->fork_ev, 0));
     HG_CUDA(hg_launch_dp_wide(&ix, &b, S, c->st2));
     HG_CUDA(cudaEventRecord(c->join_ev, c->st2));
-    HG_CUDA(hg_launch_dp_wave(&ix, &b, S * kWaveBlocksPerSm, st));
-    HG_CUDA(hg_launch_dp_large(&ix, &b, S * kLargeBlocksPerSm, st));
+    HG_CUDA(hg_launch_dp_wave(&ix, &b, S * kWaveBlocksPerSm, c->st3));
+    HG_CUDA(hg_launch_dp_large(&ix, &b, S * kLargeBlocksPerSm, c->st3));
+    HG_CUDA(cudaEventRecord(c->join3_ev, c->st3));
+    HG_CUDA(hg_launch_dp_small(&ix, &b, S * K[3], st));
+    HG_CUDA(hg_launch_dp_thin(&ix, &b, S * kWaveBlocksPerSm, st));
+    HG_CUDA(mark(4));
     HG_CUDA(cudaStreamWaitEvent(st, c->join_ev, 0));
+    HG_CUDA(cudaStreamWaitEvent(st, c->join3_ev, 0));
     HG_CUDA(mark(5));
     HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * K[4])), st));
     HG_CUDA(mark(6));
@@ -1117,6 +1129,7 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
                 HG_CUDA(hg_launch_anchor(&ix, &b, 1, c->st));
                 HG_CUDA(hg_launch_chain(&ix, &b, 1, c->st));
                 HG_CUDA(hg_launch_dp_small(&ix, &b, c->sms, c->st));
+                HG_CUDA(hg_launch_dp_thin(&ix, &b, c->sms, c->st));
                 HG_CUDA(hg_launch_dp_wave(&ix, &b, c->sms, c->st));
                 HG_CUDA(hg_launch_dp_wide(&ix, &b, c->sms, c->st));
                 HG_CUDA(hg_launch_dp_large(&ix, &b, c->sms, c->st));
@@ -1549,6 +1562,7 @@ int global_align_mm2_impl(hg_index_t* ix, const char* qry, int64_t qlen, const u
     const hg::IndexDev& d = ix->dev;
     HG_CUDA(hg_launch_chain(&d, &b, 1, st));
     HG_CUDA(hg_launch_dp_small(&d, &b, c->sms, st));
+    HG_CUDA(hg_launch_dp_thin(&d, &b, c->sms, st));
     HG_CUDA(hg_launch_dp_wave(&d, &b, c->sms, st));
     HG_CUDA(hg_launch_dp_wide(&d, &b, c->sms, st));
     HG_CUDA(hg_launch_dp_large(&d, &b, c->sms, st));

@@ -236,9 +236,9 @@ def test_wavefront_tiers_vs_oracle(gpu, oracle, pkg):
 
 
 def thin_cases(pkg, seed=5, L=12000):
-    """Queries whose end segments are thin: a short side of 1..16 bases against
+    """Queries whose end segments are thin: a short side of 1..32 bases against
     up to ~12 kb of the other side, in both orientations, both gap modes, with
-    plain and N-carrying ends, and a second center carrying N runs."""
+    plain and N-carrying ends."""
     rng = np.random.default_rng(seed)
     center = pkg.synth.random_center(L, 57)
     acgt = np.frombuffer(b"ACGT", np.uint8)
@@ -251,6 +251,9 @@ def thin_cases(pkg, seed=5, L=12000):
         a = int(rng.integers(0, L - 300))
         b = int(min(L, a + rng.integers(200, 7000)))
         cases.append(rand(int(rng.integers(0, 14))) + center[a:b] + rand(int(rng.integers(0, 14))))
+    for _ in range(8):                                    # query ends of 17..32 bases
+        a = int(rng.integers(0, L - 3000))
+        cases.append(rand(int(rng.integers(14, 30))) + center[a:a + 2500] + rand(int(rng.integers(14, 30))))
     for _ in range(10):                                   # N inside the short ends
         a = int(rng.integers(0, L - 3000))
         cases.append(rand(6, np.frombuffer(b"ACGTN", np.uint8)) + center[a:a + 2500] +
