@@ -178,6 +178,14 @@ def cpu_sample(oracle, w, budget_s: float, threads: int):
     return done_b / tot / 1e6, done_q, done_b, tot
 
 
+# the kernel behind each event-timed stage (dp_small: the small, medium and
+# thin tiers on the main stream; dp_large: the wait for the two side streams)
+STAGE_KERNEL = {"seed": "seed_fast_kernel", "anchor": "anchor_kernel", "chain": "chain_kernel",
+                "dp_small": "dp_small_kernel + dp_medium_kernel + dp_thin_kernel",
+                "dp_large": "dp_wave_kernel + dp_large_kernel + dp_wave_cta_kernel",
+                "stitch": "stitch_kernel", "rows": "row_kernel", "count": "count_kernel"}
+
+
 def algorithmic_bytes(b, n_cigar_words: int, L: int):
     """HBM bytes the path must move: packed input + per-query arrays in, rows +
     CIGARs + flags out."""
@@ -351,10 +359,14 @@ def main():
     cells = cells_c.value  # cells of the last step
     value = world * b.bases / step_s / 1e6
     # per-stage breakdown (event-timed pass; excluded from the headline number)
+    # and the pass's unit counts (anchors, segment records, DP segments)
+    work0 = ctx.work()
     ctx.set_timing(True)
     ctx.run_staged()
     stage_tot, stages, _ = ctx.last_timing()
     ctx.set_timing(False)
+    work1 = ctx.work()
+    work = {k: work1[k] - work0[k] for k in work0}
     n_cig_words = None
     # e2e: the C ABI call with pinned host buffers
     e2e = None
@@ -404,15 +416,29 @@ def main():
     plain = measure_plain(pkg, ctx, w, args.plain_queries) if args.plain_queries > 0 else None
     serving = None if args.no_serve or rank != 0 else measure_serving(pkg, args.serve_requests, 2000.0)
     peak, peak_kind = load_peaks()
-    # dominant stage
+    # dominant stage (one kernel launch per sub-batch) and its algorithmic
+    # bytes from the pass's unit counts: A anchors, R segment records, B bases
     top = max(stages, key=lambda k: stages[k])
     alg = algorithmic_bytes(b, n_cig_words, ix.L)
-    stage_bytes = {"seed": b.packed.nbytes + 8 * 3000 * b.n, "anchor": 16 * 3000 * b.n, "chain": 8 * 2500 * b.n,
-                   "dp_small": b.packed.nbytes + 4 * n_cig_words, "dp_large": 0, "stitch": 8 * n_cig_words,
-                   "rows": b.n * ix.L + 4 * n_cig_words, "count": b.n * ix.L}
+    A, R, B = work["anchors"], work["records"], b.bases
+    stage_bytes = {"seed": b.packed.nbytes + 8 * A,           # packed in; (pos, entry) hits out
+                   "anchor": 8 * A + 8 * A,                    # hits in; (pos_ref, pos_qry) out
+                   "chain": 16 * A + 32 * R + b.packed.nbytes,  # positions in, f/p out; records out; 2-bit windows
+                   "dp_small": b.packed.nbytes + 4 * n_cig_words, "dp_large": b.packed.nbytes + 4 * n_cig_words,
+                   "stitch": 32 * R + 8 * n_cig_words,
+                   "rows": b.n * ix.L + b.packed.nbytes + 4 * n_cig_words, "count": b.n * ix.L}
     top_ms = stages[top]
+    n_sub = max(1, -(-b.n // sub))
     achieved = (alg / (stage_tot / 1e3) / 1e9) if stage_tot > 0 else None
     top_achieved = (stage_bytes.get(top, 0) / (top_ms / 1e3) / 1e9) if top_ms > 0 else None
+    # DRAM bytes (read + written) per query base of each dominant-stage kernel
+    # from its ncu capture on the mito workload (4,000 queries, 66.3 Mbp),
+    # scaled to one launch (one sub-batch) of this run
+    mito_dram_per_base = {"seed": (17.1e6 + 24.2e6) / 66.3e6, "anchor": (81.1e6 + 37.3e6) / 66.3e6,
+                          "chain": (380.6e6 + 146.7e6) / 66.3e6, "rows": (18.4e6 + 7.8e6) / 66.3e6}
+    traffic = None
+    if args.workload == "mito" and top in mito_dram_per_base:
+        traffic = int(round(mito_dram_per_base[top] * B / n_sub))
     clocks = clk.summary()
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
@@ -432,12 +458,15 @@ def main():
         "gcups": round(world * cells / step_s / 1e9, 3) if cells else None,
         "gpu_launches": int(launches),
         "stage_ms": {k: round(v, 3) for k, v in stages.items()},
-        "roofline": {"bound": "hbm", "kernel": "whole path (all stages)",
-                     "achieved": round(achieved, 2) if achieved else None, "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5) if achieved else None, "traffic": None,
-                     "peak_source": peak_kind, "dominant_stage": top,
-                     "dominant_stage_achieved_gbs": round(top_achieved, 2) if top_achieved else None,
-                     "note": "integer-issue-bound path; HBM fraction is low by construction"},
+        "roofline": {"bound": "hbm", "kernel": STAGE_KERNEL.get(top, top),
+                     "achieved": round(top_achieved, 2) if top_achieved else None, "peak": peak, "unit": "GB/s",
+                     "frac": round(top_achieved / peak, 5) if top_achieved else None, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": int(stage_bytes.get(top, 0) / n_sub),
+                     "launch_ms": round(top_ms / n_sub, 3), "launches": n_sub,
+                     "units": {"anchors": A, "segment_records": R, "dp_segments": work["dp_segments"], "bases": B},
+                     "peak_source": peak_kind,
+                     "whole_path_achieved_gbs": round(achieved, 2) if achieved else None,
+                     "note": "latency-bound integer path; the HBM fraction is low by construction"},
         "cpu_baseline": cpu,
         "e2e": e2e,
         "parity_sample": parity,

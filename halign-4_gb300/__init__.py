@@ -70,6 +70,7 @@ def lib() -> C.CDLL:
     L.hg_run_staged.argtypes = [vp]
     L.hg_fetch_staged.argtypes = [vp, vp, i64, vp, vp, vp, i64, vp]
     L.hg_last_timing.argtypes = [vp, vp, vp, vp, vp]
+    L.hg_ctx_work.argtypes = [vp, vp, C.c_int]
     L.hg_set_timing.argtypes = [vp, i32]
     L.hg_staged_flags.argtypes = [vp, vp]
     L.hg_submit.argtypes = [vp, vp, vp, vp, vp, vp, i64]
@@ -309,6 +310,13 @@ class Context:
         la, ce = C.c_int64(), C.c_int64()
         _check(lib().hg_last_timing(self.h, C.byref(tot), _p(st), C.byref(la), C.byref(ce)))
         return tot.value, dict(zip(STAGES, st.tolist())), la.value
+
+    def work(self):
+        """Work totals since the context was created: anchors, segment
+        records, DP segments (hg_ctx_work)."""
+        v = np.zeros(3, np.int64)
+        _check(lib().hg_ctx_work(self.h, _p(v), 3))
+        return {"anchors": int(v[0]), "records": int(v[1]), "dp_segments": int(v[2])}
 
     def counters(self, reset: bool = False):
         L = self.index.L

@@ -416,18 +416,35 @@ __global__ void __launch_bounds__(256) count_kernel(const uint8_t* rows, int64_t
 }  // namespace hg
 
 namespace hg {
-__global__ void status_or_kernel(const uint32_t* status, int n, uint32_t* flags)
+// End of a sub-batch: OR of the per-query status words, and the work totals
+// (anchors, segment records, DP segments) added to the context's counters.
+__global__ void status_or_kernel(const uint32_t* status, int n, uint32_t* flags, const unsigned long long* ctl,
+                                 const int32_t* s_n, unsigned long long* work)
 {
     uint32_t v = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v |= status[i];
+    unsigned long long recs = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        v |= status[i];
+        recs += (unsigned long long)max(s_n[i], 0);
+    }
     v = __reduce_or_sync(0xffffffffu, v);
+    for (int o = 16; o > 0; o >>= 1) recs += __shfl_xor_sync(0xffffffffu, recs, o);
     if ((threadIdx.x & 31) == 0 && v) atomicOr(flags, v);
+    if ((threadIdx.x & 31) == 0 && recs) atomicAdd(&work[1], recs);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const uint32_t* c32 = reinterpret_cast<const uint32_t*>(ctl);
+        atomicAdd(&work[0], ctl[4]);  // anchor cursor
+        // small, large, wavefront, CTA wavefront, thin list lengths
+        atomicAdd(&work[2], (unsigned long long)c32[14] + c32[16] + c32[20] + c32[22] + c32[28]);
+    }
 }
 }  // namespace hg
 
-extern "C" cudaError_t hg_launch_status_or(const uint32_t* status, int n, uint32_t* flags, cudaStream_t st)
+extern "C" cudaError_t hg_launch_status_or(const uint32_t* status, int n, uint32_t* flags,
+                                           const unsigned long long* ctl, const int32_t* s_n, unsigned long long* work,
+                                           cudaStream_t st)
 {
-    hg::status_or_kernel<<<4, 256, 0, st>>>(status, n, flags);
+    hg::status_or_kernel<<<4, 256, 0, st>>>(status, n, flags, ctl, s_n, work);
     return cudaGetLastError();
 }
 

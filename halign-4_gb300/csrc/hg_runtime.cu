@@ -39,7 +39,8 @@ cudaError_t hg_prepare_dp_kernels(void);
 cudaError_t hg_launch_stitch(const hg::IndexDev*, const hg::BatchDev*, int, cudaStream_t);
 cudaError_t hg_launch_rows(const hg::IndexDev*, const hg::BatchDev*, int64_t, int, cudaStream_t);
 cudaError_t hg_launch_count(const uint8_t*, int64_t, int, int, uint32_t*, cudaStream_t);
-cudaError_t hg_launch_status_or(const uint32_t*, int, uint32_t*, cudaStream_t);
+cudaError_t hg_launch_status_or(const uint32_t*, int, uint32_t*, const unsigned long long*, const int32_t*,
+                                unsigned long long*, cudaStream_t);
 size_t hg_ksw_scratch_bytes(int, int, int, int);
 cudaError_t hg_prepare_kernels(void);
 cudaError_t hg_launch_ksw_single(int, const uint8_t*, int, const uint8_t*, int, const int8_t*, int, int, int, int,
@@ -190,6 +191,7 @@ struct hg_ctx {
     // control block: queues[8], cursors (a, s, dp), n_small, n_large
     DevBuf<unsigned long long> control;
     DevBuf<unsigned long long> cells;  // accumulated DP cells (GCUPS numerator)
+    DevBuf<unsigned long long> work;   // accumulated anchors, segment records, DP segments
     // compaction
     DevBuf<int64_t> cig_off;
     DevBuf<uint32_t> cig_compact;
@@ -751,7 +753,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
         (e = c->rows.alloc((size_t)max_queries * c->row_stride)) || (e = c->counts.alloc(L * 7)) ||
-        (e = c->ins.alloc(L + 1)) || (e = c->status.alloc(max_queries)) || (e = c->control.alloc(kControlWords)) || (e = c->cells.alloc(1)) ||
+        (e = c->ins.alloc(L + 1)) || (e = c->status.alloc(max_queries)) || (e = c->control.alloc(kControlWords)) || (e = c->cells.alloc(1)) || (e = c->work.alloc(4)) ||
         (e = c->cig_off.alloc(max_queries + 1)) || (e = c->cig_compact.alloc(max_bases / 4 + 1024))) {
         hg_ctx_destroy(c);
         return cuda_fail(e, "hg_ctx_create: device allocation");
@@ -762,6 +764,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
     }
     cudaMemset(c->counts.p, 0, sizeof(uint32_t) * L * 7);
     cudaMemset(c->cells.p, 0, sizeof(unsigned long long));
+    cudaMemset(c->work.p, 0, 4 * sizeof(unsigned long long));
     cudaMemset(c->ins.p, 0, sizeof(uint32_t) * (L + 1));
     for (auto& ev : c->ev) cudaEventCreate(&ev);
     for (auto& ev : c->run_ev) cudaEventCreate(&ev);
@@ -932,7 +935,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(7));
     HG_CUDA(hg_launch_count(b.rows, c->row_stride, n, ix.L, c->counts.p, st));
     HG_CUDA(mark(8));
-    HG_CUDA(hg_launch_status_or(c->status.p, n, c->run_flags.p, st));
+    HG_CUDA(hg_launch_status_or(c->status.p, n, c->run_flags.p, c->control.p, b.s_n, c->work.p, st));
     (void)kStageNames;
     return HG_OK;
 }
@@ -1274,6 +1277,16 @@ extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int
         HG_CUDA(cudaMemcpy(&v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
         *cells = (int64_t)v;
     }
+    return HG_OK;
+}
+
+extern "C" int hg_ctx_work(hg_ctx_t* c, int64_t* counts, int n)
+{
+    if (!c || !counts || n < 0) return fail(HG_ERR_ARG, "hg_ctx_work: bad arguments");
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    unsigned long long v[4] = {0, 0, 0, 0};
+    HG_CUDA(cudaMemcpy(v, c->work.p, sizeof(v), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n && i < 4; ++i) counts[i] = (int64_t)v[i];
     return HG_OK;
 }
 

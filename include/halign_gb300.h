@@ -132,6 +132,13 @@ int hg_last_timing(hg_ctx_t* ctx, float* total_ms, float* stage_ms, int64_t* lau
 /* cells: extz2 band cells of the last hg_run_staged, i.e. the sum over DP
  * calls of sum_r (en0 - st0 + 1) with the band bounds of
  * src/align/ksw2_extz2_sse.c:107-110 (the GCUPS numerator). */
+/* Work totals of every batched sub-batch since the context was created:
+ * counts[0] anchors (after the collect_anchors filters), counts[1] segment
+ * records (a run of match segments and anchor spans counts once),
+ * counts[2] DP segments (work-list entries of all tiers).  n <= 4 words are
+ * written; the difference of two reads is the work of the runs between
+ * them (the measurement's unit counts). */
+int hg_ctx_work(hg_ctx_t* ctx, int64_t* counts, int n);
 /* OR of the HG_ST_* bits of every query of the last hg_run_staged
  * (0 = every query aligned completely). */
 int hg_staged_flags(hg_ctx_t* ctx, uint32_t* flags);
