@@ -195,6 +195,22 @@ struct hg_ctx {
     // compaction
     DevBuf<int64_t> cig_off;
     DevBuf<uint32_t> cig_compact;
+    // pipelined host-buffer path (hg_align_batch over several sub-batches):
+    // the second input set and compaction buffer (slot 0 uses the ones above),
+    // pinned per-slot copies of the offsets, status and insertion flags, and
+    // the events between the input stream, the compute stream and the copy stream
+    struct PipeSlot {
+        DevBuf<uint8_t> packed;
+        DevBuf<int64_t> poff, exc_off, hoff, coff;
+        DevBuf<int32_t> qlen, exc, order;
+        DevBuf<uint32_t> compact;
+        int64_t* h_off = nullptr;
+        uint32_t* h_status = nullptr;
+        uint8_t* h_ins = nullptr;
+        cudaEvent_t in_ready = nullptr, in_free = nullptr, off_ev = nullptr, done = nullptr, cfree = nullptr;
+    } pipe[2];
+    cudaStream_t ist = nullptr;
+    bool pipe_ready = false;
     // staged full batch (device-resident form)
     std::vector<SubPlan> staged_plan;
     std::vector<int32_t> staged_qlen;
@@ -807,6 +823,14 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
     if (c->h_has_ins) cudaFreeHost(c->h_has_ins);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->done_ev) cudaEventDestroy(c->done_ev);
+    if (c->ist) cudaStreamSynchronize(c->ist), cudaStreamDestroy(c->ist);
+    for (auto& ps : c->pipe) {
+        if (ps.h_off) cudaFreeHost(ps.h_off);
+        if (ps.h_status) cudaFreeHost(ps.h_status);
+        if (ps.h_ins) cudaFreeHost(ps.h_ins);
+        for (cudaEvent_t e : {ps.in_ready, ps.in_free, ps.off_ev, ps.done, ps.cfree})
+            if (e) cudaEventDestroy(e);
+    }
     for (auto& ev : c->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : c->run_ev)
@@ -1053,6 +1077,172 @@ int status_error(const uint32_t* status, int64_t n)
     return HG_OK;
 }
 
+// Device input set and compaction buffer of pipeline slot 0 or 1.
+struct InView {
+    uint8_t* packed;
+    int64_t *poff, *exc_off, *hoff, *coff;
+    int32_t *qlen, *exc, *order;
+    uint32_t* compact;
+    size_t compact_n;
+};
+
+InView in_view(hg_ctx_t* c, int slot)
+{
+    if (slot == 0)
+        return {c->packed.p, c->poff.p, c->exc_off.p, c->hoff.p, c->coff.p, c->qlen.p, c->exc.p, c->order.p,
+                c->cig_compact.p, c->cig_compact.n};
+    auto& q = c->pipe[1];
+    return {q.packed.p, q.poff.p, q.exc_off.p, q.hoff.p, q.coff.p, q.qlen.p, q.exc.p, q.order.p, q.compact.p, q.compact.n};
+}
+
+int pipe_setup(hg_ctx_t* c)
+{
+    if (c->pipe_ready) return HG_OK;
+    const size_t M = (size_t)c->max_n;
+    auto& q = c->pipe[1];
+    cudaError_t e;
+    if ((e = q.packed.alloc(c->packed.n)) || (e = q.poff.alloc(M)) || (e = q.exc_off.alloc(M + 1)) ||
+        (e = q.hoff.alloc(M)) || (e = q.coff.alloc(M)) || (e = q.qlen.alloc(M)) || (e = q.exc.alloc(c->exc.n)) ||
+        (e = q.order.alloc(M)) || (e = q.compact.alloc(c->cig_compact.n)) ||
+        (e = cudaStreamCreateWithFlags(&c->ist, cudaStreamNonBlocking)))
+        return cuda_fail(e, "hg_align_batch: pipeline buffers");
+    for (auto& ps : c->pipe) {
+        if ((e = cudaHostAlloc(&ps.h_off, 8 * (M + 1), cudaHostAllocDefault)) ||
+            (e = cudaHostAlloc(&ps.h_status, 4 * M, cudaHostAllocDefault)) ||
+            (e = cudaHostAlloc(&ps.h_ins, M, cudaHostAllocDefault)))
+            return cuda_fail(e, "hg_align_batch: pinned pipeline staging");
+        for (cudaEvent_t* ev : {&ps.in_ready, &ps.in_free, &ps.off_ev, &ps.done, &ps.cfree})
+            if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming))) return cuda_fail(e, "hg_align_batch: events");
+    }
+    c->pipe_ready = true;
+    return HG_OK;
+}
+
+// hg_align_batch over several sub-batches: sub-batch k+1's inputs upload on
+// the input stream while k computes; after k the compute stream compacts
+// its CIGARs into the slot's buffer (bounded by its size) and copies the
+// offsets, status and flags to pinned memory; the host reads the offsets
+// before launching k+1 (the uncompacted CIGAR scratch is still intact
+// then, so a sub-batch whose CIGARs exceed the buffer is copied in pieces
+// instead), and the compacted CIGARs and the rows copy out on the copy
+// stream while k+1 computes.
+int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_t* packed, const int64_t* poff,
+                    const int32_t* qlen, const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar,
+                    int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows, int64_t row_stride,
+                    uint32_t* status)
+{
+    int r = pipe_setup(c);
+    if (r) return r;
+    if (rows && !c->rows2.p) HG_CUDA(c->rows2.alloc((size_t)c->max_n * c->row_stride));
+    const int K = (int)plans.size();
+    std::vector<int32_t> order[2];
+    std::vector<int64_t> hoff[2], coff[2], spoff[2], seoff[2];
+    for (const SubPlan& sp : plans)
+        if (sp.n > c->max_n || sp.bases > c->max_bases)
+            return fail(HG_ERR_CAPACITY, "query " + std::to_string(sp.first) + " exceeds the context capacity");
+    auto issue_inputs = [&](int k) -> int {
+        const SubPlan& sp = plans[(size_t)k];
+        const int slot = k & 1;
+        const InView V = in_view(c, slot);
+        const int64_t f = sp.first, m = sp.n;
+        sub_arrays(c, qlen + f, m, order[slot], hoff[slot], coff[slot]);
+        spoff[slot].resize((size_t)m), seoff[slot].resize((size_t)m + 1);
+        int64_t pb = 0;
+        for (int64_t i = 0; i < m; ++i) spoff[slot][i] = pb, pb += (int64_t)padded_bytes(qlen[f + i]);
+        for (int64_t i = 0; i <= m; ++i) seoff[slot][i] = exc_off[f + i] - exc_off[f];
+        cudaStream_t is = c->ist;
+        HG_CUDA(cudaStreamWaitEvent(is, c->pipe[slot].in_free, 0));  // sub-batch k-2 is done with the slot
+        bool contiguous = true;
+        for (int64_t i = 1; i < m && contiguous; ++i) contiguous = poff[f + i] == poff[f] + spoff[slot][i];
+        if (contiguous) {
+            HG_CUDA(cudaMemcpyAsync(V.packed, packed + poff[f], (size_t)pb, cudaMemcpyHostToDevice, is));
+        } else {
+            for (int64_t i = 0; i < m; ++i)
+                HG_CUDA(cudaMemcpyAsync(V.packed + spoff[slot][i], packed + poff[f + i], padded_bytes(qlen[f + i]),
+                                        cudaMemcpyHostToDevice, is));
+        }
+        const int64_t ne = seoff[slot][m];
+        if (ne) HG_CUDA(cudaMemcpyAsync(V.exc, exc + 3 * exc_off[f], 12 * (size_t)ne, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.poff, spoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.qlen, qlen + f, 4 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.exc_off, seoff[slot].data(), 8 * ((size_t)m + 1), cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.order, order[slot].data(), 4 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.hoff, hoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.coff, coff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaEventRecord(c->pipe[slot].in_ready, is));
+        return HG_OK;
+    };
+    if ((r = issue_inputs(0))) return r;
+    int64_t cig_base = 0;
+    for (int k = 0; k < K; ++k) {
+        const SubPlan& sp = plans[(size_t)k];
+        const int slot = k & 1;
+        auto& PS = c->pipe[slot];
+        const InView V = in_view(c, slot);
+        const int64_t f = sp.first, m = sp.n;
+        uint8_t* rbuf = slot ? c->rows2.p : c->rows.p;
+        cudaStream_t st = c->st;
+        HG_CUDA(cudaStreamWaitEvent(st, PS.in_ready, 0));
+        if (rows) HG_CUDA(cudaStreamWaitEvent(st, c->rows_ev[slot], 0));  // its last read-back is done
+        hg::BatchDev b = batch_view(c, (int)m, V.packed, V.poff, V.qlen, V.exc, V.exc_off, V.order, V.hoff, V.coff);
+        if (rbuf) b.rows = rbuf;
+        if ((r = run_sub(c, b, true))) return r;
+        compact_offsets_kernel<<<1, 1024, 0, st>>>(c->n_cig.p, (int)m, c->cig_off.p);
+        HG_CUDA(cudaGetLastError());
+        HG_CUDA(cudaMemcpyAsync(PS.h_off, c->cig_off.p, 8 * ((size_t)m + 1), cudaMemcpyDeviceToHost, st));
+        HG_CUDA(cudaMemcpyAsync(PS.h_status, c->status.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, st));
+        if (has_ins) HG_CUDA(cudaMemcpyAsync(PS.h_ins, c->has_ins.p, (size_t)m, cudaMemcpyDeviceToHost, st));
+        HG_CUDA(cudaEventRecord(PS.off_ev, st));
+        HG_CUDA(cudaStreamWaitEvent(st, PS.cfree, 0));  // the slot's previous CIGARs have copied out
+        compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(c->cig.p, V.coff, c->n_cig.p, c->cig_off.p, (int)m, V.compact,
+                                                        (int64_t)V.compact_n, 0);
+        HG_CUDA(cudaGetLastError());
+        HG_CUDA(cudaEventRecord(PS.in_free, st));
+        HG_CUDA(cudaEventRecord(PS.done, st));
+        // the rows copy out behind the small read-backs above (copies in one
+        // direction share an engine in order, and the offsets gate the next launch)
+        if (rows) {
+            HG_CUDA(cudaStreamWaitEvent(c->cst, PS.done, 0));
+            if (row_stride == c->row_stride)
+                HG_CUDA(cudaMemcpyAsync(rows + f * row_stride, rbuf, (size_t)row_stride * (size_t)m,
+                                        cudaMemcpyDeviceToHost, c->cst));
+            else
+                HG_CUDA(cudaMemcpy2DAsync(rows + f * row_stride, (size_t)row_stride, rbuf, (size_t)c->row_stride,
+                                          (size_t)c->ix->L, (size_t)m, cudaMemcpyDeviceToHost, c->cst));
+            HG_CUDA(cudaEventRecord(c->rows_ev[slot], c->cst));
+        }
+        if (k + 1 < K && (r = issue_inputs(k + 1))) return r;  // host work and upload overlap this compute
+        // the offsets decide the copy before the next sub-batch may overwrite the scratch
+        HG_CUDA(cudaEventSynchronize(PS.off_ev));
+        const int64_t total = PS.h_off[m];
+        if (cig_base + total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_align_batch: cigar buffer too small");
+        if (total <= (int64_t)V.compact_n) {
+            HG_CUDA(cudaStreamWaitEvent(c->cst, PS.done, 0));
+            if (total)
+                HG_CUDA(cudaMemcpyAsync(cigar + cig_base, V.compact, 4 * (size_t)total, cudaMemcpyDeviceToHost, c->cst));
+            HG_CUDA(cudaEventRecord(PS.cfree, c->cst));
+        } else {  // more CIGAR words than the buffer: copy in pieces now
+            HG_CUDA(cudaStreamSynchronize(st));
+            for (int64_t done = 0; done < total; done += (int64_t)V.compact_n) {
+                const int64_t cnt = std::min((int64_t)V.compact_n, total - done);
+                compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(c->cig.p, V.coff, c->n_cig.p, c->cig_off.p, (int)m,
+                                                                V.compact, cnt, done);
+                HG_CUDA(cudaGetLastError());
+                HG_CUDA(cudaMemcpyAsync(cigar + cig_base + done, V.compact, 4 * (size_t)cnt, cudaMemcpyDeviceToHost,
+                                        st));
+            }
+            HG_CUDA(cudaStreamSynchronize(st));
+        }
+        for (int64_t i = 0; i <= m; ++i) cigar_off[f + i] = cig_base + PS.h_off[i];
+        std::memcpy(status + f, PS.h_status, 4 * (size_t)m);
+        if (has_ins) std::memcpy(has_ins + f, PS.h_ins, (size_t)m);
+        cig_base += total;
+    }
+    HG_CUDA(cudaStreamSynchronize(c->cst));
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    return status_error(status, n);
+}
+
 int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
                const int64_t* exc_off, int64_t n, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off,
                uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status, bool plain)
@@ -1069,6 +1259,9 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
         return HG_OK;
     }
     const auto plans = plan(c, poff, qlen, exc_off, n);
+    if (!plain && plans.size() > 1)
+        return align_pipelined(c, plans, packed, poff, qlen, exc, exc_off, n, cigar, cigar_cap, cigar_off, has_ins,
+                               rows, row_stride, status);
     // two row buffers alternate between sub-batches so the read-back of one
     // overlaps the next sub-batch's compute
     if (rows && !plain && plans.size() > 1 && !c->rows2.p)

@@ -367,3 +367,44 @@ def test_global_align_ksw2_vs_oracle(gpu, oracle):
         flag = -1 if it % 2 else 0x04
         assert np.array_equal(gpu.global_align_ksw2(r.tobytes(), q.tobytes(), flag),
                               oracle.global_align_ksw2(r.tobytes(), q.tobytes(), flag)), it
+
+
+def _same_result(a, b, n):
+    for i in range(n):
+        assert np.array_equal(a.cigar_of(i), b.cigar_of(i)), i
+    assert np.array_equal(a.status, b.status) and np.array_equal(a.has_ins, b.has_ins)
+    assert np.array_equal(a.rows, b.rows)
+
+
+def test_pipelined_sub_batches_equal_one_batch(gpu, pkg):
+    """hg_align_batch over several sub-batches (inputs of the next uploaded
+    while one computes, CIGARs compacted and copied out behind it) returns
+    exactly what one sub-batch returns."""
+    w = pkg.synth.uneven(600)
+    b = gpu.pack(w.seqs, w.offsets)
+    ix = gpu.Index(w.center)
+    one = gpu.Context(ix, max_queries=w.n, max_bases=int(w.total_bases) + 1024).align(b, rows=True, check=False)
+    lens = np.diff(w.offsets)
+    sub = gpu.Context(ix, max_queries=130, max_bases=int(130 * lens.max()) + 1024)
+    _same_result(sub.align(b, rows=True, check=False), one, w.n)
+    _same_result(sub.align(b, rows=True, check=False), one, w.n)  # reused pipeline buffers and graphs
+
+
+def test_pipelined_cigar_overflow_copies_in_pieces(gpu, pkg, oracle):
+    """Sub-batches whose CIGARs outgrow the compaction buffer (short unrelated
+    queries against a long center: global alignments with many ops) are
+    copied in pieces and still equal the oracle."""
+    rng = np.random.default_rng(12)
+    center = pkg.synth.random_center(3000, 5)
+    cmx, cmy = oracle.extract_minimizer(center)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    cases = [acgt[rng.integers(0, 4, 64)].tobytes() for _ in range(300)]
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=100, max_bases=100 * 64 + 64)
+    res = ctx.align(gpu.pack(seqs, offs), rows=True, check=False)
+    words = int(res.cigar_off[100])  # CIGAR words of the first sub-batch
+    assert words > (100 * 64 + 64) // 4 + 1024  # more than the compaction buffer holds
+    for i, q in enumerate(cases):
+        assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
