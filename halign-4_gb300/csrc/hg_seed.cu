@@ -78,11 +78,13 @@ constexpr int kSeedFastChunk = 32 * kSeedPer;  // k-mer starts per warp step
 __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(IndexDev ix, BatchDev b)
 {
     __shared__ uint64_t hbuf[kSeedFastWarps][16 + kSeedFastChunk];
+    __shared__ uint64_t ebuf[kSeedFastWarps][kSeedFastChunk];
     __shared__ uint32_t pbuf[kSeedFastWarps][kSeedFastChunk];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     uint64_t* hs = hbuf[threadIdx.x >> 5];
     uint32_t* ps = pbuf[threadIdx.x >> 5];
+    uint64_t* es = ebuf[threadIdx.x >> 5];
     const int k = ix.k;
     const int lsh = 64 - 2 * k;
     for (;;) {
@@ -123,41 +125,62 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
 #pragma unroll
             for (int i = 0; i < kSeedPer; ++i) hs[16 + lane * kSeedPer + i] = h[i];
             __syncwarp();
-            uint64_t A[24];
+            // the hashes of P0-16 .. P0+7 are hs[lane * kSeedPer + i], i < 24
+            const uint64_t* A = hs + lane * kSeedPer;
+            // window minimum on 32-bit keys: the top 26 bits of the 56-bit hash
+            // above a 5-bit index, once with ties to the later index (A, the
+            // reference's "latest equal wins") and once to the earlier (B).
+            // Where the two disagree, two k-mers of the window share the 26-bit
+            // prefix (or the window has no k-mer) and the exact 64-bit minimum
+            // over keys hash << 8 | (254 - idx) decides.  Valid prefixes are
+            // < 2^31, so kNoHash (key 0xffffffff) loses to every k-mer.
+            uint32_t tp[24], kA[24], kB[24];  // tp = 0xffffffff exactly for kNoHash
 #pragma unroll
-            for (int i = 0; i < 16; ++i) A[i] = hs[lane * kSeedPer + i];
+            for (int i = 6; i < 24; ++i) {
+                tp[i] = (uint32_t)((i < 16 ? A[i] : h[i - 16]) >> 25);
+                const bool nh = EDGE && tp[i] == ~0u;
+                kA[i] = nh ? ~0u : (tp[i] & ~31u) | (uint32_t)(31 - i);
+                kB[i] = nh ? ~0u : (tp[i] & ~31u) | (uint32_t)i;
+            }
+            uint32_t PA[24], QA[24], OA[24], PB[24], QB[24], OB[24];
 #pragma unroll
-            for (int i = 0; i < kSeedPer; ++i) A[16 + i] = h[i];
-            __syncwarp();
-            if (lane < 16) hs[lane] = hs[kSeedFastChunk + lane];  // carry the last 16 hashes
-            __syncwarp();
-            // window minimum over keys
-            uint64_t key[24], Pm[24], Qm[24], Om[24];
+            for (int i = 7; i < 24; ++i) PA[i] = min(kA[i - 1], kA[i]), PB[i] = min(kB[i - 1], kB[i]);
 #pragma unroll
-            for (int i = 0; i < 24; ++i)
-                key[i] = (EDGE && A[i] == kNoHash) ? ~0ull : (A[i] << 8) | (uint64_t)(254 - i);
+            for (int i = 9; i < 24; ++i) QA[i] = min(PA[i], PA[i - 2]), QB[i] = min(PB[i], PB[i - 2]);
 #pragma unroll
-            for (int i = 7; i < 24; ++i) Pm[i] = umin64(key[i - 1], key[i]);
-#pragma unroll
-            for (int i = 9; i < 24; ++i) Qm[i] = umin64(Pm[i], Pm[i - 2]);
-#pragma unroll
-            for (int i = 13; i < 24; ++i) Om[i] = umin64(Qm[i], Qm[i - 4]);
-            int mp[kSeedPer + 1];  // minimizer positions of P0-1 .. P0+7
+            for (int i = 13; i < 24; ++i) OA[i] = min(QA[i], QA[i - 4]), OB[i] = min(QB[i], QB[i - 4]);
+            int mi[kSeedPer + 1];  // minimizer of P0-1 .. P0+7 as an index into A (position P0 - 16 + index)
 #pragma unroll
             for (int e = 15; e < 24; ++e) {
-                const uint64_t m = umin64(Om[e], Pm[e - 8]);
-                mp[e - 15] = P0 - 16 + (254 - (int)(m & 0xffu));
-                Om[e] = m;
-            }
-            // deque overflow: 10 strict increases ending at P0 + i (P0 + i - 10 >= 0, P0 + i < nk)
-            uint32_t inc = 0;
+                const uint32_t mA = min(OA[e], PA[e - 8]), mB = min(OB[e], PB[e - 8]);
+                int idx = 31 - (int)(mA & 31u);
+                if (idx != (int)(mB & 31u)) {
+                    uint64_t best = ~0ull;
 #pragma unroll
-            for (int i = 1; i < 24; ++i)
-                inc |= ((!EDGE || (A[i - 1] != kNoHash && A[i] != kNoHash)) && A[i - 1] < A[i]) ? (1u << i) : 0u;
+                    for (int j = e - 9; j <= e; ++j)
+                        best = umin64(best, (EDGE && A[j] == kNoHash) ? ~0ull : (A[j] << 8) | (uint64_t)(254 - j));
+                    idx = 254 - (int)(best & 0xffu);
+                }
+                mi[e - 15] = idx;
+            }
+            // deque overflow: 10 strict increases ending at P0 + i (P0 + i - 10 >= 0,
+            // P0 + i < nk); equal prefixes compare the whole hashes
+            uint32_t inc = 0, tie = 0;
+#pragma unroll
+            for (int i = 7; i < 24; ++i) {
+                const bool ok = !EDGE || (tp[i - 1] != ~0u && tp[i] != ~0u);
+                inc |= (ok && tp[i - 1] < tp[i]) ? (1u << i) : 0u;
+                tie |= (ok && tp[i - 1] == tp[i]) ? (1u << i) : 0u;
+            }
+            if (tie) {
+#pragma unroll
+                for (int i = 7; i < 24; ++i)
+                    if ((tie >> i & 1u) && A[i - 1] < A[i]) inc |= 1u << i;
+            }
             const uint32_t r2 = inc & (inc >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4), r10 = r8 & (r2 >> 8);
             const uint32_t ovf = (r10 >> 7) & 0xffu;  // run of ten starting at bit 7+i ends at bit 16+i
-            // emission; the chunk's emitted minimizers are compacted (in position
-            // order) into the free part of the warp's buffers, then probed in the
+            // emission; the chunk's emitted minimizers (hash read back from the
+            // warp's buffer) are compacted in position order, then probed in the
             // index densely, one per lane
             uint32_t emask = 0;
 #pragma unroll
@@ -165,7 +188,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
                 const int p = P0 + i;
                 if (((ovf >> i) & 1u) && (!EDGE || (p - kFastWin >= 0 && p < nk))) ovf_any = true;
                 if (EDGE && (p >= nk || p < kFastWin - 1)) continue;
-                if ((!EDGE || p > kFastWin - 1) && mp[i + 1] == mp[i]) continue;
+                if ((!EDGE || p > kFastWin - 1) && mi[i + 1] == mi[i]) continue;
                 emask |= 1u << i;
             }
             const int n_emit = __popc(emask);
@@ -175,15 +198,17 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
 #pragma unroll
             for (int i = 0; i < kSeedPer; ++i) {
                 if (emask >> i & 1u) {
-                    hs[16 + e] = Om[16 + i] >> 8;
-                    ps[e] = (uint32_t)mp[i + 1];
+                    es[e] = hs[lane * kSeedPer + mi[i + 1]];
+                    ps[e] = (uint32_t)(P0 - 16 + mi[i + 1]);
                     ++e;
                 }
             }
             __syncwarp();
+            if (lane < 16) hs[lane] = hs[kSeedFastChunk + lane];  // carry the last 16 hashes
+            __syncwarp();
             for (int e0 = 0; e0 < n_chunk; e0 += 32) {
                 const int ei = e0 + lane;
-                const uint32_t ent = ei < n_chunk ? index_find(ix, hs[16 + ei]) : kEmptyKey;
+                const uint32_t ent = ei < n_chunk ? index_find(ix, es[ei]) : kEmptyKey;
                 const bool hit = ent != kEmptyKey;
                 const unsigned hm = __ballot_sync(FULL, hit);
                 if (hit) {

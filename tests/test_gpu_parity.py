@@ -408,3 +408,25 @@ def test_pipelined_cigar_overflow_copies_in_pieces(gpu, pkg, oracle):
     assert words > (100 * 64 + 64) // 4 + 1024  # more than the compaction buffer holds
     for i, q in enumerate(cases):
         assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
+
+
+def test_low_complexity_vs_oracle(gpu, oracle, pkg):
+    """Repeats inside the minimizer window (equal hashes: the reference's
+    latest-equal-wins ties, equal hash prefixes in the increase test) in the
+    batched fast path: poly-A, short tandem repeats, and repeats spliced into
+    center substrings."""
+    rng = np.random.default_rng(31)
+    center = pkg.synth.random_center(8000, 13)
+    cmx, cmy = oracle.extract_minimizer(center)
+    cases = [b"A" * 3000, b"AC" * 1500, b"ACG" * 1000, b"ACGTTTGA" * 400, b"AACCGGTTA" * 300]
+    for period in (2, 3, 5, 7, 11, 13):
+        unit = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, period)].tobytes()
+        a = int(rng.integers(0, 5000))
+        cases.append(center[a:a + 1500] + unit * (600 // period) + center[a + 1500:a + 3000])
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=32, max_bases=len(seqs) + 1024)
+    res = ctx.align(gpu.pack(seqs, offs), rows=False, check=False)
+    for i, q in enumerate(cases):
+        assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
