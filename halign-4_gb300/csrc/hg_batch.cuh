@@ -46,13 +46,15 @@ struct Seg {
 enum SegKind : uint32_t {
     kSegEmpty = 0, kSegIns = 1, kSegDel = 2, kSegDpSmall = 3, kSegDpLarge = 4, kSegGlobal = 5,
     kSegMatch = 6,  // equal lengths, identical A/C/G/T on both sides: the extz2 CIGAR is rl M
-    kSegDpThin = 7  // query side <= 16, long center side: grouped wavefront, ops stored last-first
+    kSegDpThin = 7,  // query side <= 32, long center side: grouped wavefront, ops stored last-first
+    kSegDpSquare = 8  // both sides moderate: thread DP, directions in the warp's slot, ops stored last-first
 };
 
 // True for the gap-fill kinds that run an extz2 DP (and own a CIGAR slot).
 __host__ __device__ __forceinline__ bool seg_is_dp(uint32_t kind)
 {
-    return kind == kSegDpSmall || kind == kSegDpLarge || kind == kSegGlobal || kind == kSegDpThin;
+    return kind == kSegDpSmall || kind == kSegDpLarge || kind == kSegGlobal || kind == kSegDpThin ||
+           kind == kSegDpSquare;
 }
 constexpr uint32_t kSegLeft = 1u << 8;
 
@@ -145,6 +147,34 @@ __host__ __device__ __forceinline__ bool thin_tier_fits(uint32_t rl, uint32_t ql
     if (ql < 1 || ql > (uint32_t)kThinMaxInner || rl <= ql) return false;
     if (small_tier_fits(rl, ql) || medium_tier_fits(rl, ql) || !wave_eligible(rl, ql)) return false;
     return (int64_t)rl + ql - 1 <= kThinMaxSteps;
+}
+
+// Square tier: a segment the band never binds with the shorter side <= 128
+// that no tier above takes, whose directions (4 bits per cell, rows of
+// ceil(inner / 8) words) fit the warp's scratch slot for 32 segments: rows x
+// words <= kSquareRowWords.  One thread per segment, so its latency grows
+// with the cells: above kSquareMaxCells the one-warp wavefront keeps it.
+constexpr int kSquareMaxInner = 128;
+constexpr int kSquareRowWords = 2048;  // 32 lanes x 2048 words x 4 B = one 256 KB slot
+constexpr int kSquareMaxCells = 12288;
+constexpr int kSquareBins = 2048;      // sort bins of the square list
+
+__host__ __device__ __forceinline__ bool square_tier_fits(uint32_t rl, uint32_t ql)
+{
+    const uint32_t inner = rl < ql ? rl : ql, outer = rl < ql ? ql : rl;
+    if (inner < 1 || inner > (uint32_t)kSquareMaxInner || !wave_eligible(rl, ql)) return false;
+    if ((uint64_t)rl * ql > (uint64_t)kSquareMaxCells) return false;
+    return outer * ((inner + 7) / 8) <= (uint32_t)kSquareRowWords;
+}
+
+// Sort key of a square segment: rows x words class first (longest first), then
+// orientation and gap mode, so a warp's 32 segments have similar loop bounds.
+__host__ __device__ __forceinline__ uint32_t square_key(uint32_t rl, uint32_t ql, bool left)
+{
+    const uint32_t inner = rl < ql ? rl : ql, outer = rl < ql ? ql : rl;
+    uint32_t cost = outer * ((inner + 3) / 4);  // state words touched per segment, <= 2 kSquareRowWords
+    cost = cost > 4095 ? 4095 : cost;
+    return (511u - (cost >> 3)) << 2 | (rl <= ql ? 1u : 0u) << 1 | (left ? 0u : 1u);
 }
 
 // Columns per lane of the one-warp wavefront: the smallest power of two with
@@ -246,6 +276,11 @@ struct BatchDev {
     uint32_t* thin_hist;         // kThinBins counters, then kThinBins cursors
     unsigned int* n_thin;
     unsigned int* thin_q;        // kThinMaxInner queue heads of the thin tier, one per query length
+    uint32_t* work_sq;           // square tier: segment ids, keys, sorted ids
+    uint32_t* work_sq_key;
+    uint32_t* work_sq_sorted;
+    uint32_t* sq_hist;           // kSquareBins counters, then kSquareBins cursors
+    unsigned int* n_sq;
     int64_t wcap;
     // K6 DP scratch: one reusable slot per large-tier warp, plus a bump arena
     // for segments whose scratch exceeds a slot
@@ -269,7 +304,7 @@ struct BatchDev {
     uint32_t* ins;               // L + 1 insertion events
     uint32_t* status;            // per query
     unsigned int* queues;        // work-queue heads, one per stage
-    unsigned int* queues2;       // [0] seed fast-path queue; [1] start of the medium small-tier records
+    unsigned int* queues2;       // [0] seed fast-path queue; [1] start of the medium small-tier records; [2] square queue
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };

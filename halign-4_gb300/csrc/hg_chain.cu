@@ -486,6 +486,8 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 kind = kSegDpSmall;
             else if (thin_tier_fits(rl, ql))
                 kind = kSegDpThin;
+            else if (square_tier_fits(rl, ql))
+                kind = kSegDpSquare;
             else
                 kind = kSegDpLarge;
             // the reference runs extz2 on a match segment too (full band: rl x rl
@@ -560,8 +562,10 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const unsigned mw = __ballot_sync(FULL, wv_warp);
             const unsigned mx = __ballot_sync(FULL, wv && !wv_warp);
             const unsigned mt = __ballot_sync(FULL, act && kind == kSegDpThin);
-            unsigned bs = 0, bl = 0, bw = 0, bx = 0, bt = 0;
+            const unsigned mq = __ballot_sync(FULL, act && kind == kSegDpSquare);
+            unsigned bs = 0, bl = 0, bw = 0, bx = 0, bt = 0, bq = 0;
             if (lane == 0) {
+                if (mq) bq = atomicAdd(b.n_sq, (unsigned)__popc(mq));
                 if (mt) bt = atomicAdd(b.n_thin, (unsigned)__popc(mt));
                 if (ms) bs = atomicAdd(b.n_small, (unsigned)__popc(ms));
                 if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
@@ -573,6 +577,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             bw = __shfl_sync(FULL, bw, 0);
             bx = __shfl_sync(FULL, bx, 0);
             bt = __shfl_sync(FULL, bt, 0);
+            bq = __shfl_sync(FULL, bq, 0);
             if (ms >> lane & 1u) {
                 const unsigned w = bs + __popc(ms & below);
                 if ((int64_t)w < b.wcap) {
@@ -636,6 +641,21 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             if (mt) {
                 const unsigned peers = __match_any_sync(FULL, tkey);
                 if (tkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.thin_hist[tkey], __popc(peers));
+            }
+            if (mq) {
+                uint32_t qkey = 0xffffffffu;  // counted in the histogram only when placed
+                if (mq >> lane & 1u) {
+                    const unsigned w = bq + __popc(mq & below);
+                    if ((int64_t)w < b.wcap) {
+                        qkey = square_key(rl, ql, (flags & kSegLeft) != 0);
+                        b.work_sq[w] = sid;
+                        b.work_sq_key[w] = qkey;
+                    } else {
+                        atomicOr(&b.status[q], kStArenaOverflow);
+                    }
+                }
+                const unsigned peers = __match_any_sync(FULL, qkey);
+                if (qkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.sq_hist[qkey], __popc(peers));
             }
             rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
             qpos = (uint32_t)__shfl_sync(FULL, iq, 31);

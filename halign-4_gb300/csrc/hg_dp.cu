@@ -573,6 +573,151 @@ __global__ void __launch_bounds__(kThinWarps * 32, 4) dp_thin_kernel(IndexDev ix
     if (lane == 0 && cells && b.cells) atomicAdd(b.cells, cells);
 }
 
+// Square tier: one thread per segment the band never binds, shorter side up
+// to 128.  The row state (s1, s2: one byte per column, 4 columns per word)
+// and the inner side's base codes live in shared memory, the thread's words
+// interleaved across the CTA; a row is swept 8 columns (one direction word)
+// at a time.  Directions go to the warp's scratch slot, interleaved by lane
+// (word (o * stride + k) of lane l at [(o * stride + k) * 32 + l]); the
+// traceback reads them back there and writes op runs last-first as the small
+// tier does.  Values stay in bytes: u, v in [0, 21], x, y in [0, 6].
+constexpr int kSquareWarps = 4;
+constexpr int kSquareStateWords = kSquareMaxInner / 4;  // per thread and array
+constexpr size_t kSquareSmemBytes = (size_t)3 * kSquareStateWords * kSquareWarps * 32 * sizeof(uint32_t);
+
+template <bool TINNER, int MODE>
+__device__ __forceinline__ void square_segment(const IndexDev& ix, const BatchDev& b, const Seg& g, uint32_t sid,
+                                               uint32_t* S1, uint32_t* S2, uint32_t* IC, uint32_t* dirs)
+{
+    constexpr int T = kSquareWarps * 32;
+    const int qn = (int)g.ql, tn = (int)g.rl;
+    const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
+    const int stride = (inner + 7) >> 3;
+    const uint8_t* pk = b.packed + b.poff[g.q];
+    const int64_t e0 = b.exc_off[g.q], e1 = b.exc_off[g.q + 1];
+    const bool plain_q = e0 == e1;
+    const uint8_t* tc = ix.center + g.rs;
+    auto qbase = [&](int j) -> uint32_t {
+        return plain_q ? packed_code(pk, g.qs + j) : query_dna5(pk, b.exc, e0, e1, g.qs + j);
+    };
+    for (int w = 0; w < 2 * stride; ++w) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = 4 * w + k;
+            const uint32_t c = i < inner ? (TINNER ? (uint32_t)tc[i] : qbase(i)) : 0u;
+            v |= c << (8 * k);
+        }
+        IC[w * T] = v, S1[w * T] = 0, S2[w * T] = 0;
+    }
+    for (int o = 0; o < outer; ++o) {
+        const int oc = TINNER ? (int)qbase(o) : (int)tc[o];
+        int c1 = 0, c2 = o ? 6 : 0;
+        for (int k8 = 0; k8 < stride; ++k8) {
+            uint32_t dw = 0;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int w = 2 * k8 + h;
+                const uint32_t icw = IC[w * T], s1w = S1[w * T], s2w = S2[w * T];
+                uint32_t n1 = 0, n2 = 0;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int i = 4 * w + k;
+                    if (i < inner) {
+                        const int ic = (int)((icw >> (8 * k)) & 0xffu);
+                        const int s1 = (int)((s1w >> (8 * k)) & 0xffu), s2 = (int)((s2w >> (8 * k)) & 0xffu);
+                        const int z0 = (ic == 4 || oc == 4) ? 16 : (ic == oc ? 21 : 12);
+                        int u, v, x, y;
+                        uint32_t d;
+                        if (TINNER) {
+                            const int ut = o ? s1 : (i ? 6 : 0), yt = o ? s2 : 0;
+                            d = lane_int_z<MODE>(z0, c1, c2, ut, yt, u, v, x, y);
+                            c1 = x, c2 = v;
+                            n1 |= (uint32_t)u << (8 * k), n2 |= (uint32_t)y << (8 * k);
+                        } else {
+                            const int xt = o ? s1 : 0, vt = o ? s2 : (i ? 6 : 0);
+                            const int ut = i ? c1 : (o ? 6 : 0), yt = i ? c2 : 0;
+                            d = lane_int_z<MODE>(z0, xt, vt, ut, yt, u, v, x, y);
+                            c1 = u, c2 = y;
+                            n1 |= (uint32_t)x << (8 * k), n2 |= (uint32_t)v << (8 * k);
+                        }
+                        dw |= d << (4 * (4 * h + k));
+                    }
+                }
+                S1[w * T] = n1, S2[w * T] = n2;
+            }
+            dirs[(size_t)(o * stride + k8) * 32] = dw;
+        }
+    }
+    // traceback from (tlen-1, qlen-1); runs written once, last-first
+    uint32_t* out = b.cig_seg + b.coff[g.q] + g.slot;
+    int n = 0;
+    uint32_t run_op = 0xffu, run_len = 0;
+    auto push = [&](uint32_t op, uint32_t len) {
+        if (op == run_op) {
+            run_len += len;
+        } else {
+            if (run_len) out[n++] = run_len << 4 | run_op;
+            run_op = op, run_len = len;
+        }
+    };
+    int ti = tn - 1, qj = qn - 1, state = 0;
+    while (ti >= 0 && qj >= 0) {
+        const int o = TINNER ? qj : ti, i = TINNER ? ti : qj;
+        const uint32_t nib = (dirs[(size_t)(o * stride + (i >> 3)) * 32] >> ((i & 7) * 4)) & 0xfu;
+        if (state == 0) state = nib & 3u;
+        else if (!((nib >> (state + 1)) & 1u)) state = 0;
+        if (state == 0) state = nib & 3u;
+        if (state == 0) push(0, 1), --ti, --qj;
+        else if (state == 1) push(2, 1), --ti;
+        else push(1, 1), --qj;
+    }
+    if (ti >= 0) push(2, (uint32_t)(ti + 1));
+    if (qj >= 0) push(1, (uint32_t)(qj + 1));
+    if (run_len) out[n++] = run_len << 4 | run_op;
+    b.seg[sid].nops = n;
+}
+
+// Persistent warps take 32 consecutive entries of the sorted square list at a
+// time (queue queues2[2]); warp gw owns scratch slot gw.
+__global__ void __launch_bounds__(kSquareWarps * 32, 4) dp_square_kernel(IndexDev ix, BatchDev b)
+{
+    extern __shared__ uint32_t sq_smem[];
+    const unsigned FULL = 0xffffffffu;
+    const int tid = threadIdx.x, lane = tid & 31, wl = tid >> 5;
+    const int gw = blockIdx.x * kSquareWarps + wl;
+    if (gw >= b.dp_nslots) return;
+    constexpr int T = kSquareWarps * 32;
+    uint32_t* S1 = sq_smem + tid;
+    uint32_t* S2 = sq_smem + kSquareStateWords * T + tid;
+    uint32_t* IC = sq_smem + 2 * kSquareStateWords * T + tid;
+    uint32_t* dirs = reinterpret_cast<uint32_t*>(b.dp_slots + (size_t)gw * b.dp_slot_bytes) + lane;
+    const unsigned total = min(*b.n_sq, (unsigned)b.wcap);
+    unsigned long long cells = 0;
+    for (;;) {
+        unsigned t = 0;
+        if (lane == 0) t = atomicAdd(&b.queues2[2], 1u);
+        t = __shfl_sync(FULL, t, 0);
+        if ((unsigned long long)t * 32u >= total) break;
+        const unsigned w = t * 32u + (unsigned)lane;
+        if (w < total) {
+            const uint32_t sid = b.work_sq_sorted[w];
+            const Seg g = b.seg[sid];
+            const bool tinner = g.rl <= g.ql, left = (g.kind & kSegLeft) != 0;
+            if (tinner) {
+                if (left) square_segment<true, 1>(ix, b, g, sid, S1, S2, IC, dirs);
+                else square_segment<true, 2>(ix, b, g, sid, S1, S2, IC, dirs);
+            } else {
+                if (left) square_segment<false, 1>(ix, b, g, sid, S1, S2, IC, dirs);
+                else square_segment<false, 2>(ix, b, g, sid, S1, S2, IC, dirs);
+            }
+            cells += (unsigned long long)g.rl * g.ql;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) cells += __shfl_xor_sync(FULL, cells, o);
+    if (lane == 0 && cells && b.cells) atomicAdd(b.cells, cells);
+}
+
 // Counting sort of the small-tier work list by shape_key: the chain kernel
 // writes each entry's key and the histogram; scan + scatter follow.
 __global__ void shape_scan_kernel(BatchDev b)
@@ -1509,9 +1654,15 @@ extern "C" cudaError_t hg_launch_dp_thin(const hg::IndexDev* ix, const hg::Batch
     return cudaGetLastError();
 }
 
-// One-warp wavefront tier: sort, then grid CTAs of 4 warps (warp i uses slot i).
+// Square tier (sort, then grid CTAs of 4 warps; warp i uses slot i), then the
+// one-warp wavefront tier (sort, then grid CTAs of 4 warps; warp i uses slot
+// i): one after the other on one stream, as they share the slots.
 extern "C" cudaError_t hg_launch_dp_wave(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
+    hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_sq, b->work_sq_key, b->sq_hist,
+                                                                    b->work_sq_sorted, b->n_sq, b->wcap,
+                                                                    hg::kSquareBins);
+    hg::dp_square_kernel<<<grid, hg::kSquareWarps * 32, hg::kSquareSmemBytes, st>>>(*ix, *b);
     hg::key_scatter_kernel<<<grid, hg::kKeyScatterThreads, 0, st>>>(b->work_wave, b->work_wave_key, b->wave_hist,
                                                                     b->work_wave_sorted, b->n_wave, b->wcap,
                                                                     hg::kWaveBins);
@@ -1535,6 +1686,9 @@ extern "C" cudaError_t hg_prepare_dp_kernels()
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(hg::dp_thin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)hg::kThinSmemBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(hg::dp_square_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)hg::kSquareSmemBytes);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(hg::shape_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)hg::kScatterSmem);

@@ -94,7 +94,9 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
                         else op = 2, len = s_rl[wib][lo];
                     } else {
                         // the small DP tier stores its ops last-first
-                        const uint32_t at = (kind == kSegDpSmall || kind == kSegDpThin) ? (uint32_t)s_nops[wib][lo] - 1u - rel : rel;
+                        const uint32_t at = (kind == kSegDpSmall || kind == kSegDpThin || kind == kSegDpSquare)
+                                                  ? (uint32_t)s_nops[wib][lo] - 1u - rel
+                                                  : rel;
                         const uint32_t c = src[s_slot[wib][lo] + at];
                         op = c & 0xfu, len = c >> 4;
                     }
@@ -434,8 +436,8 @@ __global__ void status_or_kernel(const uint32_t* status, int n, uint32_t* flags,
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const uint32_t* c32 = reinterpret_cast<const uint32_t*>(ctl);
         atomicAdd(&work[0], ctl[4]);  // anchor cursor
-        // small, large, wavefront, CTA wavefront, thin list lengths
-        atomicAdd(&work[2], (unsigned long long)c32[14] + c32[16] + c32[20] + c32[22] + c32[28]);
+        // small, large, wavefront, CTA wavefront, thin, square list lengths
+        atomicAdd(&work[2], (unsigned long long)c32[14] + c32[16] + c32[20] + c32[22] + c32[28] + c32[30]);
     }
 }
 }  // namespace hg

@@ -171,6 +171,7 @@ struct hg_ctx {
     DevBuf<uint32_t> work_small, work_large, work_sorted, work_key, shape_hist;
     DevBuf<uint32_t> work_wave, work_wave_key, work_wave_sorted, wave_hist, work_wide;
     DevBuf<uint32_t> work_thin, work_thin_key, work_thin_sorted;  // thin_hist lives in wave_hist
+    DevBuf<uint32_t> work_sq, work_sq_key, work_sq_sorted;        // and so does sq_hist
     DevBuf<hg::SmallRec> work_rec;
     int64_t dp_cap = 0;
     DevBuf<uint8_t> dp_arena;
@@ -647,16 +648,16 @@ namespace {
 
 constexpr int kControlWords = 32;
 // control words: queues[8] | a_cursor | s_cursor | dp_cursor | n_small | n_large | n_exact | n_wave | n_wide |
-// queues2[4] | n_thin | (free) | thin_q[32]
+// queues2[4] | n_thin | n_sq | thin_q[32]
 // sort counters of the one-warp wavefront list, then of the thin list (counters and cursors each)
-constexpr size_t kSortHistWords = 2 * (size_t)hg::kWaveBins + 2 * (size_t)hg::kThinBins;
+constexpr size_t kSortHistWords = 2 * (size_t)hg::kWaveBins + 2 * (size_t)hg::kThinBins + 2 * (size_t)hg::kSquareBins;
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
 constexpr int kWaveBlocksPerSm = 4;
 constexpr int kThinWarpsPerSm = 16;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
-// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, thin + dp_wave 4, dp_wide,
-// dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
-constexpr int kLaunchesBatch = 20;
-constexpr int kLaunchesPlain = 19;
+// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, thin 2, square + dp_wave 4,
+// dp_wide, dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
+constexpr int kLaunchesBatch = 22;
+constexpr int kLaunchesPlain = 21;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
@@ -762,7 +763,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->work_wave.alloc(c->scap)) || (e = c->work_wave_key.alloc(c->scap)) ||
         (e = c->work_wave_sorted.alloc(c->scap)) || (e = c->wave_hist.alloc(kSortHistWords)) ||
         (e = c->work_thin.alloc(c->scap)) || (e = c->work_thin_key.alloc(c->scap)) ||
-        (e = c->work_thin_sorted.alloc(c->scap)) ||
+        (e = c->work_thin_sorted.alloc(c->scap)) || (e = c->work_sq.alloc(c->scap)) ||
+        (e = c->work_sq_key.alloc(c->scap)) || (e = c->work_sq_sorted.alloc(c->scap)) ||
         (e = c->work_wide.alloc(c->scap)) || (e = c->work_rec.alloc(c->scap)) ||
         (e = c->dp_slots.alloc((size_t)c->dp_nslots * c->dp_slot_bytes)) ||
         (e = c->thin_scratch.alloc((size_t)c->thin_nwarps * hg::kThinWarpBytes)) || (e = c->run_flags.alloc(1)) ||
@@ -905,6 +907,9 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.thin_q = reinterpret_cast<unsigned int*>(ctl + 16);  // 32 x uint32 in words 16..31
     b.work_thin = c->work_thin.p, b.work_thin_key = c->work_thin_key.p, b.work_thin_sorted = c->work_thin_sorted.p;
     b.thin_hist = c->wave_hist.p + 2 * hg::kWaveBins;
+    b.work_sq = c->work_sq.p, b.work_sq_key = c->work_sq_key.p, b.work_sq_sorted = c->work_sq_sorted.p;
+    b.sq_hist = c->wave_hist.p + 2 * hg::kWaveBins + 2 * hg::kThinBins;
+    b.n_sq = reinterpret_cast<unsigned int*>(ctl + 15);
     b.dp_arena = c->dp_arena.p, b.dp_cap = c->dp_cap;
     b.dp_slots = c->dp_slots.p, b.dp_slot_bytes = c->dp_slot_bytes, b.dp_nslots = c->dp_nslots;
     b.thin_scratch = c->thin_scratch.p, b.thin_nwarps = c->thin_nwarps;
