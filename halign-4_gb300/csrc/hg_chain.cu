@@ -113,13 +113,15 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const int64_t fi = max(fa, carry + fb);
             int64_t fprev = __shfl_up_sync(FULL, fi, 1);
             if (lane == 0) fprev = carry;
-            if (i < A) {
-                f[i] = (int32_t)fi;
-                p[i] = (sv > kNeg / 2 && fprev + sv > span) ? i - 1 : -1;
-            }
+            // p_i = i-1 exactly when fprev + sv > span, i.e. when f_i > span:
+            // p is not stored, spec_p() derives it from f
+            if (i < A) f[i] = (int32_t)fi;
+            (void)fprev;
             carry = __shfl_sync(FULL, fi, 31);
         }
         __syncwarp();
+        // the speculated predecessor of anchor j (f_j > span: j-1, else none)
+        auto spec_p = [&](int j, int32_t fj) -> int32_t { return fj > span ? j - 1 : -1; };
         // ---- verification.  With the speculated f, anchor i's reference scan
         // keeps (f_i, p_i) unless some candidate j <= i-2 totals more than f_i
         // (ties do not improve; where the scan stops then does not matter).
@@ -173,11 +175,11 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                     bool mark_next = false;
                     // candidate j's fields, the next candidate's loaded one step ahead
                     uint32_t rj = ar[i - 1], qj = aq[i - 1];
-                    int32_t fj = f[i - 1], pj = p[i - 1];
+                    int32_t fj = f[i - 1], pj = spec_p(i - 1, fj);
                     for (int j = i - 1; j >= jmin; --j) {
                         const int jn = j > 0 ? j - 1 : 0;
                         const uint32_t rn = ar[jn], qn = aq[jn];
-                        const int32_t fn = f[jn], pn = p[jn];
+                        const int32_t fn = f[jn], pn = spec_p(jn, fn);
                         const uint32_t rc = rj, qc = qj;
                         const int32_t fc = fj, pc = pj;
                         rj = rn, qj = qn, fj = fn, pj = pn;
@@ -195,7 +197,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                         }
                         mark_next = pc == j - 1;
                     }
-                    if (max_f != fi || max_j != p[i]) mine = i;
+                    if (max_f != fi || max_j != spec_p(i, fi)) mine = i;
                 }
             }
             bad = __reduce_min_sync(FULL, mine);
@@ -215,7 +217,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         int32_t w_f = 0, w_p = -1;
         if (k0 < A) {
             const int j = k0 - 1 - lane;
-            if (j >= 0) w_ar = ar[j], w_aq = aq[j], w_f = f[j], w_p = p[j];
+            if (j >= 0) w_ar = ar[j], w_aq = aq[j], w_f = f[j], w_p = spec_p(j, w_f);
             const int nb = k0 & ~31;
             nx_ar = nb + lane < A ? ar[nb + lane] : 0u;
             nx_aq = nb + lane < A ? aq[nb + lane] : 0u;
@@ -307,7 +309,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                     if (j >= it0) sc = chain_score(ix, lg2, ri, qv, ar[j], aq[j], span);
                     const bool valid = sc != INT32_MIN;
                     int32_t fj = 0, pj = -1;
-                    if (valid) fj = f[j], pj = p[j];
+                    if (valid) fj = f[j], pj = j < k0 ? spec_p(j, fj) : p[j];
                     if (valid && pj >= 0) t[pj] = i;
                     __syncwarp();
                     const bool marked = valid && t[j] == i;
@@ -359,22 +361,23 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             best = gi == INT32_MAX ? -1 : gi;
         }
         // backtrack: chain (reversed) into t[], read p[] 32 entries at a time
-        int c = 0;
+        int c = 0, s0c = -1;  // s0c >= 0: the chain is the run s0c .. s0c + c - 1 (t[] unused)
         if (!(best_f < ix.min_score || best < 0) && k0 == A) {
             // speculation held: every p is i-1 or -1, so the chain is the run
-            // [s, best] with s the last anchor at or before best whose p is -1
+            // [s, best] with s the last anchor at or before best whose p is -1,
+            // i.e. whose f is span (f_0 = span, so s exists)
             int sl = -1;
             for (int i = lane; i <= best; i += 32)
-                if (p[i] < 0) sl = i;
-            const int s0 = __reduce_max_sync(FULL, sl);
-            c = best - s0 + 1;
-            for (int m = lane; m < c; m += 32) t[m] = best - m;
+                if (f[i] <= span) sl = i;
+            s0c = __reduce_max_sync(FULL, sl);
+            c = best - s0c + 1;
             if (c < ix.min_cnt) c = 0;
         } else if (!(best_f < ix.min_score || best < 0)) {
             int cur = best;
             while (cur >= 0) {
                 const int lo = max(cur - 31, 0);
-                const int pl = (lo + lane <= cur) ? p[lo + lane] : -1;
+                const int ip = lo + lane;
+                const int pl = ip <= cur ? (ip < k0 ? spec_p(ip, f[ip]) : p[ip]) : -1;
                 while (cur >= lo) {
                     if (lane == 0) t[c] = cur;
                     ++c;
@@ -439,6 +442,8 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const uint64_t m = n >= 32 ? ~0ull : ((1ull << (2 * n)) - 1ull);
             return ((window(b.packed, qp) ^ window(ix.center2, rp)) & m) == 0;
         };
+        // the x-th chain anchor in increasing order
+        auto chain_at = [&](int x) -> int { return s0c >= 0 ? s0c + x : t[c - 1 - x]; };
         // raw end of segment s (before clipping and the prefix max)
         auto seg_end = [&](int s, int64_t& er, int64_t& eq, uint32_t& flags) {
             er = 0, eq = 0, flags = 0;
@@ -446,15 +451,15 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             if (c == 0) {
                 er = L, eq = len;
             } else if (s == 0) {
-                const int a = t[c - 1];
+                const int a = chain_at(0);
                 er = ar[a], eq = aq[a], flags = kSegLeft;
             } else if (s == 2 * c) {
                 er = L, eq = len;
             } else if (s & 1) {
-                const int a = t[c - 1 - (s - 1) / 2];
+                const int a = chain_at((s - 1) / 2);
                 er = (int64_t)ar[a] + span, eq = (int64_t)aq[a] + span;
             } else {
-                const int a = t[c - 1 - s / 2];
+                const int a = chain_at(s / 2);
                 er = ar[a], eq = aq[a];
             }
         };
