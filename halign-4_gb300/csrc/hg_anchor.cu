@@ -70,9 +70,10 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
         // anchors of hit i: its center occurrences if the hit survives the filters
         auto n_out = [&](int i) -> int {
             const uint32_t d = he[i];
+            const uint32_t my = ix.ent_meta[d].y;
             bool keep = !(ix.q_occ_frac > 0.0 && (double)cnt[d] > limit);
-            if (keep && ix.ent_over[d]) keep = ix.sample_every != 0 && (hp[i] % ix.sample_every) == 0;
-            return keep ? (int)ix.ent_count[d] : 0;
+            if (keep && (my >> 31)) keep = ix.sample_every != 0 && (hp[i] % ix.sample_every) == 0;
+            return keep ? (int)(my & 0x7fffffffu) : 0;
         };
         // total (coalesced: thread t takes hits t, t+256, ...); the counts of the
         // first kKeep chunks stay in registers for the emission pass
@@ -114,9 +115,11 @@ __global__ void __launch_bounds__(kAnchorThreads) anchor_kernel(IndexDev ix, Bat
                 int tot;
                 const int ex = block_excl_sum(k, scan_s, &tot);
                 if (k) {
-                    const uint32_t d = he[i], st = ix.ent_start[d], qp = hp[i];
+                    const uint2 m = ix.ent_meta[he[i]];
+                    const uint32_t qp = hp[i];
+                    const bool once = (m.y & 0x7fffffffu) == 1u;
                     for (int j = 0; j < k; ++j) {
-                        b.a_ref[base + carry + ex + j] = ix.cpos[st + j];
+                        b.a_ref[base + carry + ex + j] = once ? m.x : ix.cpos[m.x + j];
                         b.a_qry[base + carry + ex + j] = qp;
                     }
                 }

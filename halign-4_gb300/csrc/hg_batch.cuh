@@ -19,9 +19,8 @@ struct IndexDev {
                                // {key = hash56 (kNoHash = empty), entry id of the key}
     uint32_t tab_mask;
     uint32_t n_ent;            // distinct center minimizer hashes
-    const uint32_t* ent_start; // into cpos
-    const uint32_t* ent_count; // reference-side occurrence count
-    const uint8_t* ent_over;   // count > occurrence threshold (sparse sampling applies)
+    const uint2* ent_meta;     // x: the center position if the entry occurs once, else its start in cpos;
+                               // y: occurrence count | 1 << 31 if count > the occurrence threshold
     const uint32_t* cpos;      // center positions grouped by hash, ascending within a hash
     const uint32_t* cspan;     // matching spans (always k for a single center)
     double q_occ_frac;

@@ -121,8 +121,8 @@ struct hg_index {
     int64_t n_hits = 0;
     DevBuf<uint8_t> center, center2;
     DevBuf<ulonglong2> tab;
-    DevBuf<uint32_t> ent_start, ent_count, cpos, cspan;
-    DevBuf<uint8_t> ent_over;
+    DevBuf<uint2> ent_meta;
+    DevBuf<uint32_t> cpos, cspan;
     DevBuf<float> log2tab;
     hg::IndexDev dev{};
     hg_ctx_t* single = nullptr;  // lazily created context for single-query calls
@@ -580,6 +580,13 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     const int nlog = std::max(ix->prm.bw + 2, 513);
     std::vector<float> lg((size_t)nlog);
     for (int i = 0; i < nlog; ++i) lg[i] = i >= 1 ? (float)std::log2((double)i) : 0.0f;
+    // per entry: its center position when it occurs once (the common case),
+    // else its start in cpos; the occurrence count with the over-threshold bit
+    std::vector<uint2> meta(ekey.size());
+    for (size_t e = 0; e < ekey.size(); ++e) {
+        meta[e].x = ecnt[e] == 1 ? cpos[est[e]] : est[e];
+        meta[e].y = ecnt[e] | (over[e] ? 0x80000000u : 0u);
+    }
     auto up = [&](auto& buf, const auto& v) -> cudaError_t {
         cudaError_t e = buf.alloc(std::max<size_t>(v.size(), 1));
         if (e != cudaSuccess) return e;
@@ -588,7 +595,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     };
     cudaError_t e = cudaSuccess;
     if ((e = up(ix->center, cdp)) || (e = up(ix->center2, c2)) || (e = up(ix->tab, tab)) ||
-        (e = up(ix->ent_start, est)) || (e = up(ix->ent_count, ecnt)) || (e = up(ix->ent_over, over)) ||
+        (e = up(ix->ent_meta, meta)) ||
         (e = up(ix->cpos, cpos)) || (e = up(ix->cspan, cspan)) || (e = up(ix->log2tab, lg))) {
         delete ix;
         return cuda_fail(e, "hg_index_create: upload");
@@ -598,7 +605,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     d.center = ix->center.p, d.center2 = ix->center2.p, d.center_plain = cplain;
     d.tab = ix->tab.p, d.tab_mask = tsize - 1;
     d.n_ent = (uint32_t)ekey.size();
-    d.ent_start = ix->ent_start.p, d.ent_count = ix->ent_count.p, d.ent_over = ix->ent_over.p;
+    d.ent_meta = ix->ent_meta.p;
     d.cpos = ix->cpos.p, d.cspan = ix->cspan.p;
     d.q_occ_frac = ix->prm.q_occ_frac, d.sample_every = ix->prm.sample_every_bp;
     d.max_dist_x = ix->prm.max_dist_x, d.max_dist_y = ix->prm.max_dist_y, d.bw = ix->prm.bw;
@@ -628,8 +635,8 @@ extern "C" void hg_index_destroy(hg_index_t* ix)
 {
     if (!ix) return;
     if (ix->single) hg_ctx_destroy(ix->single);
-    ix->center.free(), ix->tab.free(), ix->ent_start.free(), ix->ent_count.free();
-    ix->ent_over.free(), ix->cpos.free(), ix->cspan.free(), ix->log2tab.free(), ix->center2.free();
+    ix->center.free(), ix->tab.free(), ix->ent_meta.free();
+    ix->cpos.free(), ix->cspan.free(), ix->log2tab.free(), ix->center2.free();
     delete ix;
 }
 
