@@ -506,6 +506,22 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             const unsigned kmask = __ballot_sync(FULL, keep);
             const bool isM = keep && kind == kSegMatch;
             const unsigned mmask = __ballot_sync(FULL, isM);
+            if (kmask == mmask) {  // every kept segment is a match (or none is kept): one run, no DP
+                if (mmask) {
+                    const uint32_t tot = __reduce_add_sync(FULL, isM ? rl : 0u);
+                    if (!open) {
+                        const int h = __ffs(mmask) - 1;
+                        o_rs = __shfl_sync(FULL, rs, h), o_qs = __shfl_sync(FULL, qs, h);
+                        o_sid = (uint32_t)sb + nkept, o_len = 0;
+                        ++nkept;
+                        open = true;
+                    }
+                    o_len += tot;
+                }
+                rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
+                qpos = (uint32_t)__shfl_sync(FULL, iq, 31);
+                continue;
+            }
             const unsigned below = (1u << lane) - 1u;
             const unsigned kb = kmask & below;
             const bool prev_m = kb ? ((mmask >> (31 - __clz(kb))) & 1u) != 0 : open;

@@ -145,7 +145,7 @@ struct hg_ctx {
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
     cudaStream_t st3 = nullptr;                            // side stream of the one-warp wavefront and exact tiers
     // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
-    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 4};
+    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6};
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, join3_ev = nullptr;
     int sms = 1;
     int64_t max_n = 0, max_bases = 0, exc_cap = 0;

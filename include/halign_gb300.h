@@ -117,7 +117,7 @@ int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* 
                     uint8_t* rows, int64_t row_stride, uint32_t* status);
 /* Launch shape of the sub-batch stages, in CTAs per SM: [0] seed (1..32),
  * [1] anchor (1..6), [2] chain (1..64), [3] dp_small (1..32), [4] stitch
- * (1..32), [5] rows (1..32).  Defaults 6 6 12 12 8 4.  Setting them drops the
+ * (1..32), [5] rows (1..32).  Defaults 6 6 12 12 8 6.  Setting them drops the
  * context's cached CUDA graphs (the autotuner, halign-4_gb300/autotune.py,
  * searches them).  No reference counterpart: launch geometry. */
 #define HG_LAUNCH_KNOBS 6
