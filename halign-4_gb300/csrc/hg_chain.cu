@@ -415,6 +415,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         // a 32-segment chunk is carried (record id, start, length so far).
         bool open = false;
         uint32_t o_sid = 0, o_rs = 0, o_qs = 0, o_len = 0;
+        unsigned long long match_cells = 0;  // added to the cell total once per query
         auto put_match = [&](uint32_t id, uint32_t mrs, uint32_t mqs, uint32_t mlen) {
             Seg g;
             g.rs = mrs, g.qs = mqs, g.rl = mlen, g.ql = mlen;
@@ -497,11 +498,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                 kind = kSegDpLarge;
             // the reference runs extz2 on a match segment too (full band: rl x rl
             // cells); count them so the cell total stays the reference's work unit
-            if (b.cells) {
-                const unsigned long long mc = act && kind == kSegMatch ? (unsigned long long)rl * rl : 0ull;
-                const unsigned long long tot = __reduce_add_sync(FULL, (unsigned)mc);
-                if (lane == 0 && tot) atomicAdd(b.cells, tot);
-            }
+            match_cells += __reduce_add_sync(FULL, act && kind == kSegMatch ? rl * rl : 0u);
             const bool keep = act && kind != kSegEmpty;
             const unsigned kmask = __ballot_sync(FULL, keep);
             const bool isM = keep && kind == kSegMatch;
@@ -683,6 +680,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             slot = slot + __shfl_sync(FULL, sincl, 31);
         }
         if (open && lane == 0) put_match(o_sid, o_rs, o_qs, o_len);
+        if (lane == 0 && match_cells && b.cells) atomicAdd(b.cells, match_cells);
         if (lane == 0) b.s_n[q] = (int32_t)nkept;
     }
 }
