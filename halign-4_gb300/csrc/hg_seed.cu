@@ -77,12 +77,16 @@ constexpr int kSeedFastChunk = 32 * kSeedPer;  // k-mer starts per warp step
 // the hashes of its current chunk after the 16 that precede it.
 __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(IndexDev ix, BatchDev b)
 {
-    __shared__ uint64_t hbuf[kSeedFastWarps][16 + kSeedFastChunk];
+    // the hashes of a warp's chunk after the 16 before it; element idx lives at
+    // idx + idx / 8 (one pad word per 8) so that lane l's 8 consecutive
+    // elements start 72 bytes after lane l-1's: no bank conflicts
+    __shared__ uint64_t hbuf[kSeedFastWarps][(16 + kSeedFastChunk) * 9 / 8];
     __shared__ uint64_t ebuf[kSeedFastWarps][kSeedFastChunk];
     __shared__ uint32_t pbuf[kSeedFastWarps][kSeedFastChunk];
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    uint64_t* hs = hbuf[threadIdx.x >> 5];
+    uint64_t* hsb = hbuf[threadIdx.x >> 5];
+    auto H = [hsb](int idx) -> uint64_t& { return hsb[idx + (idx >> 3)]; };
     uint32_t* ps = pbuf[threadIdx.x >> 5];
     uint64_t* es = ebuf[threadIdx.x >> 5];
     const int k = ix.k;
@@ -98,7 +102,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
         const uint8_t* pk = b.packed + b.poff[q];
         const int nk = len - k + 1;
         const int64_t hb = b.hoff[q];
-        if (lane < 16) hs[lane] = kNoHash;  // positions before 0
+        if (lane < 16) H(lane) = kNoHash;  // positions before 0
         int total_hits = 0, total_matched = 0;
         bool ovf_any = false;
         // EDGE: a chunk touching position 0 or the query end (hashes past either
@@ -123,10 +127,10 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
                 for (int i = 0; i < kSeedPer; ++i) h[i] = kNoHash;
             }
 #pragma unroll
-            for (int i = 0; i < kSeedPer; ++i) hs[16 + lane * kSeedPer + i] = h[i];
+            for (int i = 0; i < kSeedPer; ++i) H(16 + lane * kSeedPer + i) = h[i];
             __syncwarp();
-            // the hashes of P0-16 .. P0+7 are hs[lane * kSeedPer + i], i < 24
-            const uint64_t* A = hs + lane * kSeedPer;
+            // the hashes of P0-16 .. P0+7 are A(i) = H(lane * kSeedPer + i), i < 24
+            auto A = [&](int i) -> uint64_t { return H(lane * kSeedPer + i); };
             // window minimum on 32-bit keys: the top 26 bits of the 56-bit hash
             // above a 5-bit index, once with ties to the later index (A, the
             // reference's "latest equal wins") and once to the earlier (B).
@@ -137,7 +141,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
             uint32_t tp[24], kA[24], kB[24];  // tp = 0xffffffff exactly for kNoHash
 #pragma unroll
             for (int i = 6; i < 24; ++i) {
-                tp[i] = (uint32_t)((i < 16 ? A[i] : h[i - 16]) >> 25);
+                tp[i] = (uint32_t)((i < 16 ? A(i) : h[i - 16]) >> 25);
                 const bool nh = EDGE && tp[i] == ~0u;
                 kA[i] = nh ? ~0u : (tp[i] & ~31u) | (uint32_t)(31 - i);
                 kB[i] = nh ? ~0u : (tp[i] & ~31u) | (uint32_t)i;
@@ -158,7 +162,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
                     uint64_t best = ~0ull;
 #pragma unroll
                     for (int j = e - 9; j <= e; ++j)
-                        best = umin64(best, (EDGE && A[j] == kNoHash) ? ~0ull : (A[j] << 8) | (uint64_t)(254 - j));
+                        best = umin64(best, (EDGE && A(j) == kNoHash) ? ~0ull : (A(j) << 8) | (uint64_t)(254 - j));
                     idx = 254 - (int)(best & 0xffu);
                 }
                 mi[e - 15] = idx;
@@ -175,7 +179,7 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
             if (tie) {
 #pragma unroll
                 for (int i = 7; i < 24; ++i)
-                    if ((tie >> i & 1u) && A[i - 1] < A[i]) inc |= 1u << i;
+                    if ((tie >> i & 1u) && A(i - 1) < A(i)) inc |= 1u << i;
             }
             const uint32_t r2 = inc & (inc >> 1), r4 = r2 & (r2 >> 2), r8 = r4 & (r4 >> 4), r10 = r8 & (r2 >> 8);
             const uint32_t ovf = (r10 >> 7) & 0xffu;  // run of ten starting at bit 7+i ends at bit 16+i
@@ -198,13 +202,13 @@ __global__ void __launch_bounds__(kSeedFastWarps * 32, 3) seed_fast_kernel(Index
 #pragma unroll
             for (int i = 0; i < kSeedPer; ++i) {
                 if (emask >> i & 1u) {
-                    es[e] = hs[lane * kSeedPer + mi[i + 1]];
+                    es[e] = H(lane * kSeedPer + mi[i + 1]);
                     ps[e] = (uint32_t)(P0 - 16 + mi[i + 1]);
                     ++e;
                 }
             }
             __syncwarp();
-            if (lane < 16) hs[lane] = hs[kSeedFastChunk + lane];  // carry the last 16 hashes
+            if (lane < 16) H(lane) = H(kSeedFastChunk + lane);  // carry the last 16 hashes
             __syncwarp();
             for (int e0 = 0; e0 < n_chunk; e0 += 32) {
                 const int ei = e0 + lane;
