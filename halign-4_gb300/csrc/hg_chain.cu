@@ -609,17 +609,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
                     atomicOr(&b.status[q], kStArenaOverflow);
                 }
             }
-            // histogram of small-tier shapes (lanes with equal keys add once)
-            if (ms && b.work_key) {
-                uint32_t key = 0xffffffffu;
-                if (ms >> lane & 1u) {
-                    Seg g;
-                    g.rl = rl, g.ql = ql, g.kind = kind | flags;
-                    key = shape_key(g);
-                }
-                const unsigned peers = __match_any_sync(FULL, key);
-                if ((ms >> lane & 1u) && lane == __ffs(peers) - 1) atomicAdd(&b.shape_hist[key], __popc(peers));
-            }
+            // (the small-tier shape histogram is counted from work_key by shape_hist_kernel)
             if (ml >> lane & 1u) {
                 const unsigned w = bl + __popc(ml & below);
                 if ((int64_t)w < b.wcap) b.work_large[w] = sid;

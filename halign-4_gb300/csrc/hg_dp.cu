@@ -718,6 +718,23 @@ __global__ void __launch_bounds__(kSquareWarps * 32, 4) dp_square_kernel(IndexDe
     if (lane == 0 && cells && b.cells) atomicAdd(b.cells, cells);
 }
 
+// Histogram of the small-tier shape keys (the chain kernel writes one key
+// per work-list entry): per-CTA counters in shared memory, one global atomic
+// per non-empty bin and CTA.
+constexpr int kShapeHistThreads = 512;
+__global__ void __launch_bounds__(kShapeHistThreads) shape_hist_kernel(BatchDev b)
+{
+    __shared__ uint32_t h[kShapeBins];
+    for (int i = threadIdx.x; i < (int)kShapeBins; i += kShapeHistThreads) h[i] = 0;
+    __syncthreads();
+    const unsigned total = min(*b.n_small, (unsigned)b.wcap);
+    for (unsigned w = blockIdx.x * kShapeHistThreads + threadIdx.x; w < total; w += gridDim.x * kShapeHistThreads)
+        atomicAdd(&h[b.work_key[w]], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < (int)kShapeBins; i += kShapeHistThreads)
+        if (h[i]) atomicAdd(&b.shape_hist[i], h[i]);
+}
+
 // Counting sort of the small-tier work list by shape_key: the chain kernel
 // writes each entry's key and the histogram; scan + scatter follow.
 __global__ void shape_scan_kernel(BatchDev b)
@@ -1630,6 +1647,7 @@ __global__ void ksw_single_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, in
 
 extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::BatchDev* b, int grid, cudaStream_t st)
 {
+    hg::shape_hist_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kShapeHistThreads, 0, st>>>(*b);
     hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
     hg::shape_scatter_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kScatterThreads, hg::kScatterSmem, st>>>(*ix, *b);
     hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);

@@ -661,10 +661,10 @@ constexpr size_t kSortHistWords = 2 * (size_t)hg::kWaveBins + 2 * (size_t)hg::kT
 constexpr int kLargeBlocksPerSm = 4;  // dp_large grid = SMs x 4 CTAs x 4 warps
 constexpr int kWaveBlocksPerSm = 4;
 constexpr int kThinWarpsPerSm = 16;   // dp_wave grid = SMs x 4 CTAs x 4 warps (one checkpoint slot per warp)
-// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 4, thin 2, square + dp_wave 4,
+// kernel launches per sub-batch: seed 3, anchor, chain, dp_small 5, thin 2, square + dp_wave 4,
 // dp_wide, dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
-constexpr int kLaunchesBatch = 22;
-constexpr int kLaunchesPlain = 21;
+constexpr int kLaunchesBatch = 23;
+constexpr int kLaunchesPlain = 22;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
 {
