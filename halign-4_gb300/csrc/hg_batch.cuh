@@ -85,6 +85,8 @@ __host__ __device__ __forceinline__ bool medium_tier_fits(uint32_t rl, uint32_t 
 // [0,6) outer-1, [6,10) inner-1 (small) or inner-17 (medium), 10 orientation,
 // 11 left-aligned, 12 medium range (sorts after every small shape).
 constexpr uint32_t kShapeBins = 1u << 13;
+constexpr uint32_t kNoShape = 0xffffffffu;  // key of an unused small-list entry (a hole)
+constexpr uint32_t kSmallBlock = 64;        // small-list entries a chain warp reserves at a time
 constexpr uint32_t kShapeMedium = 1u << 12;
 __device__ __forceinline__ uint32_t shape_key(const Seg& g)
 {
@@ -303,7 +305,8 @@ struct BatchDev {
     uint32_t* ins;               // L + 1 insertion events
     uint32_t* status;            // per query
     unsigned int* queues;        // work-queue heads, one per stage
-    unsigned int* queues2;       // [0] seed fast-path queue; [1] start of the medium small-tier records; [2] square queue
+    unsigned int* queues2;       // [0] seed fast-path queue; [1] start of the medium small-tier records; [2] square queue;
+                                 // [3] small-tier records (the small list without its holes)
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };

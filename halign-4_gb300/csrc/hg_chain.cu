@@ -65,6 +65,14 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int32_t span = ix.k;
+    // small-list entries come from a block this warp reserved (kSmallBlock at a
+    // time: far fewer contended atomics); unused entries of a block are holes
+    // (key kNoShape) that the sort skips
+    uint32_t sm_base = 0, sm_left = 0;
+    auto small_holes = [&]() {
+        for (uint32_t k = (uint32_t)lane; k < sm_left; k += 32)
+            if ((int64_t)(sm_base + k) < b.wcap) b.work_key[sm_base + k] = kNoShape;
+    };
     for (;;) {
         int qi = 0;
         if (lane == 0) qi = (int)atomicAdd(&b.queues[2], 1u);
@@ -585,12 +593,21 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
             if (lane == 0) {
                 if (mq) bq = atomicAdd(b.n_sq, (unsigned)__popc(mq));
                 if (mt) bt = atomicAdd(b.n_thin, (unsigned)__popc(mt));
-                if (ms) bs = atomicAdd(b.n_small, (unsigned)__popc(ms));
+
                 if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
                 if (mw) bw = atomicAdd(b.n_wave, (unsigned)__popc(mw));
                 if (mx) bx = atomicAdd(b.n_wide, (unsigned)__popc(mx));
             }
-            bs = __shfl_sync(FULL, bs, 0);
+            if (ms) {
+                const uint32_t nms = (uint32_t)__popc(ms);
+                if (nms > sm_left) {
+                    small_holes();
+                    uint32_t nb = 0;
+                    if (lane == 0) nb = atomicAdd(b.n_small, kSmallBlock);
+                    sm_base = __shfl_sync(FULL, nb, 0), sm_left = kSmallBlock;
+                }
+                bs = sm_base, sm_base += nms, sm_left -= nms;
+            }
             bl = __shfl_sync(FULL, bl, 0);
             bw = __shfl_sync(FULL, bw, 0);
             bx = __shfl_sync(FULL, bx, 0);
@@ -673,6 +690,7 @@ __global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, Ba
         if (lane == 0 && match_cells && b.cells) atomicAdd(b.cells, match_cells);
         if (lane == 0) b.s_n[q] = (int32_t)nkept;
     }
+    small_holes();  // the rest of this warp's last block
 }
 
 }  // namespace hg

@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, 
 {
     __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
     const int tid = threadIdx.x;
-    const unsigned total = min(b.queues2[1], min(*b.n_small, (unsigned)b.wcap));  // small shapes only
+    const unsigned total = min(b.queues2[1], b.queues2[3]);  // small shapes only
     unsigned long long cell_sum = 0;
     const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
     for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(kDpMedThreads) dp_medium_kernel(IndexDev ix, B
 {
     __shared__ uint32_t dirs[kMedDirWords * kDpMedThreads];
     const int tid = threadIdx.x;
-    const unsigned total = min(*b.n_small, (unsigned)b.wcap);
+    const unsigned total = b.queues2[3];  // small-tier records (the list without holes)
     const unsigned first = min(b.queues2[1], total);
     unsigned long long cell_sum = 0;
     const unsigned span = ((total - first) + 31u) & ~31u;
@@ -728,15 +728,18 @@ __global__ void __launch_bounds__(kShapeHistThreads) shape_hist_kernel(BatchDev 
     for (int i = threadIdx.x; i < (int)kShapeBins; i += kShapeHistThreads) h[i] = 0;
     __syncthreads();
     const unsigned total = min(*b.n_small, (unsigned)b.wcap);
-    for (unsigned w = blockIdx.x * kShapeHistThreads + threadIdx.x; w < total; w += gridDim.x * kShapeHistThreads)
-        atomicAdd(&h[b.work_key[w]], 1u);
+    for (unsigned w = blockIdx.x * kShapeHistThreads + threadIdx.x; w < total; w += gridDim.x * kShapeHistThreads) {
+        const uint32_t key = b.work_key[w];
+        if (key != kNoShape) atomicAdd(&h[key], 1u);  // holes carry kNoShape
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < (int)kShapeBins; i += kShapeHistThreads)
         if (h[i]) atomicAdd(&b.shape_hist[i], h[i]);
 }
 
 // Counting sort of the small-tier work list by shape_key: the chain kernel
-// writes each entry's key and the histogram; scan + scatter follow.
+// writes each entry's key, shape_hist_kernel the histogram; scan + scatter
+// follow.
 __global__ void shape_scan_kernel(BatchDev b)
 {
     __shared__ uint32_t part[1024];
@@ -759,6 +762,7 @@ __global__ void shape_scan_kernel(BatchDev b)
         b.shape_hist[kShapeBins + tid * per + i] = run;  // cursor = bucket start
         run += c;
     }
+    if (tid == 1023) b.queues2[3] = run;  // all records
 }
 
 // Scatter into shape order.  CTA c takes a contiguous chunk of the chain-
@@ -779,7 +783,10 @@ __global__ void __launch_bounds__(kScatterThreads) shape_scatter_kernel(IndexDev
     if (w0 >= w1) return;
     for (int i = threadIdx.x; i < kShapeBins; i += kScatterThreads) cnt[i] = 0;
     __syncthreads();
-    for (unsigned w = w0 + threadIdx.x; w < w1; w += kScatterThreads) atomicAdd(&cnt[b.work_key[w]], 1u);
+    for (unsigned w = w0 + threadIdx.x; w < w1; w += kScatterThreads) {
+        const uint32_t key = b.work_key[w];
+        if (key != kNoShape) atomicAdd(&cnt[key], 1u);
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < kShapeBins; i += kScatterThreads) {
         const uint32_t c = cnt[i];
@@ -789,6 +796,7 @@ __global__ void __launch_bounds__(kScatterThreads) shape_scatter_kernel(IndexDev
     __syncthreads();
     for (unsigned w = w0 + threadIdx.x; w < w1; w += kScatterThreads) {
         const uint32_t key = b.work_key[w];
+        if (key == kNoShape) continue;  // a hole of a chain warp's block
         const uint32_t sid = b.work_small[w];
         const uint32_t pos = base[key] + atomicAdd(&cnt[key], 1u);
         const Seg g = b.seg[sid];

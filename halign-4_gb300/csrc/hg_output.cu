@@ -436,8 +436,8 @@ __global__ void status_or_kernel(const uint32_t* status, int n, uint32_t* flags,
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         const uint32_t* c32 = reinterpret_cast<const uint32_t*>(ctl);
         atomicAdd(&work[0], ctl[4]);  // anchor cursor
-        // small, large, wavefront, CTA wavefront, thin, square list lengths
-        atomicAdd(&work[2], (unsigned long long)c32[14] + c32[16] + c32[20] + c32[22] + c32[28] + c32[30]);
+        // small records, large, wavefront, CTA wavefront, thin, square list lengths
+        atomicAdd(&work[2], (unsigned long long)c32[27] + c32[16] + c32[20] + c32[22] + c32[28] + c32[30]);
     }
 }
 }  // namespace hg
