@@ -170,30 +170,34 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
 }
 
 // K8: row projection, one CTA per query (persistent).
-constexpr int kRowThreads = 256;
-constexpr int kRowOps = 1024;
+constexpr int kRowWarps = 8;
+constexpr int kRowOps = 256;  // ops per chunk (per warp)
 
-__global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev b, int64_t row_stride)
+// One warp per query (no block barriers): each chunk of up to kRowOps ops
+// gets its reference / query prefix sums by warp scans into the warp's shared
+// arrays; columns are then written lane-parallel, 16 at a time with one
+// packed-word decode where the 16 columns sit inside one op.
+__global__ void __launch_bounds__(kRowWarps * 32) row_kernel(IndexDev ix, BatchDev b, int64_t row_stride)
 {
-    __shared__ uint32_t s_r[kRowOps + 1], s_q[kRowOps + 1];
-    __shared__ uint32_t s_op[kRowOps];
-    __shared__ int scan_s[33];
-    __shared__ int s_qi;
-    __shared__ uint32_t s_carry_r, s_carry_q;
+    __shared__ uint32_t s_r_all[kRowWarps][kRowOps + 1], s_q_all[kRowWarps][kRowOps + 1];
+    __shared__ uint32_t s_op_all[kRowWarps][kRowOps];
     __shared__ uint32_t lut[256];  // 4 packed 2-bit codes -> their 4 ASCII bases
-    const int tid = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    uint32_t* s_r = s_r_all[wl];
+    uint32_t* s_q = s_q_all[wl];
+    uint32_t* s_op = s_op_all[wl];
     const int L = ix.L;
-    for (int i = tid; i < 256; i += kRowThreads) {
+    for (int i = threadIdx.x; i < 256; i += kRowWarps * 32) {
         uint32_t v = 0;
         for (int k = 0; k < 4; ++k) v |= ((0x54474341u >> (8u * ((i >> (2 * k)) & 3))) & 0xffu) << (8 * k);
         lut[i] = v;
     }
     __syncthreads();
     for (;;) {
-        if (tid == 0) s_qi = (int)atomicAdd(&b.queues[5], 1u);
-        __syncthreads();
-        const int qi = s_qi;
-        __syncthreads();
+        int qi = 0;
+        if (lane == 0) qi = (int)atomicAdd(&b.queues[5], 1u);
+        qi = __shfl_sync(FULL, qi, 0);
         if (qi >= b.n) break;
         const int q = b.order ? b.order[qi] : qi;
         const int n = b.n_cig[q];
@@ -201,15 +205,15 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
         const uint8_t* pk = b.packed + b.poff[q];
         const int64_t e0 = b.exc_off[q], e1 = b.exc_off[q + 1];
         uint8_t* row = b.rows + (int64_t)q * row_stride;
-        if (tid == 0) s_carry_r = 0, s_carry_q = 0;
-        __syncthreads();
+        uint32_t carry_r = 0, carry_q = 0;
         for (int c0 = 0; c0 < n; c0 += kRowOps) {
             const int cn = min(kRowOps, n - c0);
-            // prefix sums of reference / query consumption (4 ops per thread)
-            uint32_t lr[4], lq[4], sr = 0, sq = 0;
+            // prefix sums of reference / query consumption: lane l takes ops 8l .. 8l+7
+            constexpr int PER = kRowOps / 32;
+            uint32_t lr[PER], lq[PER], sr = 0, sq = 0;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int i = tid * 4 + k;
+            for (int k = 0; k < PER; ++k) {
+                const int i = lane * PER + k;
                 uint32_t rr = 0, qq = 0;
                 if (i < cn) {
                     const uint32_t c = cg[c0 + i];
@@ -220,30 +224,28 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
                 }
                 lr[k] = rr, lq[k] = qq, sr += rr, sq += qq;
             }
-            int tr, tq;
-            const int er = block_excl_sum((int)sr, scan_s, &tr);
-            const int eq = block_excl_sum((int)sq, scan_s, &tq);
-            uint32_t ar = s_carry_r + (uint32_t)er, aq = s_carry_q + (uint32_t)eq;
+            const uint32_t ir = warp_incl_sum(sr), iq = warp_incl_sum(sq);
+            uint32_t ar = carry_r + ir - sr, aq = carry_q + iq - sq;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int i = tid * 4 + k;
+            for (int k = 0; k < PER; ++k) {
+                const int i = lane * PER + k;
                 if (i < cn) {
                     s_r[i] = ar, s_q[i] = aq;
-                    const uint32_t c = s_op[i];
-                    if ((c & 0xfu) == 1 && ar <= (uint32_t)L) atomicAdd(&b.ins[ar], 1u);
+                    if ((s_op[i] & 0xfu) == 1 && ar <= (uint32_t)L) atomicAdd(&b.ins[ar], 1u);
                 }
                 ar += lr[k], aq += lq[k];
             }
-            if (tid == kRowThreads - 1) s_r[cn] = ar, s_q[cn] = aq;
-            __syncthreads();
+            const uint32_t tot_r = __shfl_sync(FULL, ir, 31), tot_q = __shfl_sync(FULL, iq, 31);
+            if (lane == 0) s_r[cn] = carry_r + tot_r, s_q[cn] = carry_q + tot_q;
+            __syncwarp();
             const uint32_t col0 = s_r[0], col1 = max(col0, min(s_r[cn], (uint32_t)L));
-            // exception-free query: 16 whole columns per thread, one 16-byte store
+            // exception-free query: 16 whole columns per lane, one 16-byte store
             uint32_t vb = col0, ve = col0;  // [vb, ve): columns written by the vector path
             if (e0 == e1) {
                 vb = min((col0 + 15u) & ~15u, col1);
                 ve = col1 & ~15u;
                 if (ve < vb) ve = vb;
-                for (uint32_t g0 = vb + 16u * tid; g0 < ve; g0 += 16u * kRowThreads) {
+                for (uint32_t g0 = vb + 16u * lane; g0 < ve; g0 += 16u * 32u) {
                     int lo = 0, hi = cn - 1;  // last op with s_r <= g0
                     while (lo < hi) {
                         const int mid = (lo + hi + 1) >> 1;
@@ -301,7 +303,7 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
             }
             // the columns the vector path left: [col0, vb) and [ve, col1)
             const uint32_t head = vb - col0, nrest = head + (col1 - ve);
-            for (uint32_t t = tid; t < nrest; t += kRowThreads) {
+            for (uint32_t t = lane; t < nrest; t += 32) {
                 const uint32_t col = t < head ? col0 + t : ve + (t - head);
                 int lo = 0, hi = cn - 1;  // last op with s_r <= col and nonzero ref length
                 while (lo < hi) {
@@ -331,16 +333,14 @@ __global__ void __launch_bounds__(kRowThreads) row_kernel(IndexDev ix, BatchDev 
                 }
                 row[col] = ch;
             }
-            __syncthreads();
-            if (tid == 0) s_carry_r = s_r[cn], s_carry_q = s_q[cn];
-            __syncthreads();
+            carry_r += tot_r, carry_q += tot_q;
+            __syncwarp();
         }
         // a CIGAR that stops short of the center (chainless alignment cut at
         // the band edge) leaves a shorter row; pad so the buffer is defined
-        const uint32_t done = s_carry_r;
-        for (uint32_t col = done + tid; col < (uint32_t)L; col += kRowThreads) row[col] = '-';
-        if (tid == 0 && done != (uint32_t)L) atomicOr(&b.status[q], kStLengthMismatch);
-        __syncthreads();
+        const uint32_t done = carry_r;
+        for (uint32_t col = done + lane; col < (uint32_t)L; col += 32) row[col] = '-';
+        if (lane == 0 && done != (uint32_t)L) atomicOr(&b.status[q], kStLengthMismatch);
     }
 }
 
@@ -459,7 +459,7 @@ extern "C" cudaError_t hg_launch_stitch(const hg::IndexDev* ix, const hg::BatchD
 extern "C" cudaError_t hg_launch_rows(const hg::IndexDev* ix, const hg::BatchDev* b, int64_t row_stride, int grid,
                                       cudaStream_t st)
 {
-    hg::row_kernel<<<grid, hg::kRowThreads, 0, st>>>(*ix, *b, row_stride);
+    hg::row_kernel<<<grid, hg::kRowWarps * 32, 0, st>>>(*ix, *b, row_stride);
     return cudaGetLastError();
 }
 

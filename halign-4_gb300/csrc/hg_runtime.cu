@@ -967,7 +967,7 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(mark(5));
     HG_CUDA(hg_launch_stitch(&ix, &b, std::max(1, std::min((n + 3) / 4, S * K[4])), st));
     HG_CUDA(mark(6));
-    HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, std::min(n, S * K[5]), st));
+    HG_CUDA(hg_launch_rows(&ix, &b, c->row_stride, std::max(1, std::min((n + 7) / 8, S * K[5])), st));
     HG_CUDA(mark(7));
     HG_CUDA(hg_launch_count(b.rows, c->row_stride, n, ix.L, c->counts.p, st));
     HG_CUDA(mark(8));
