@@ -252,11 +252,18 @@ __global__ void __launch_bounds__(kRowWarps * 32) row_kernel(IndexDev ix, BatchD
                         if (s_r[mid] <= g0) lo = mid;
                         else hi = mid - 1;
                     }
-                    {  // the 16 columns inside one op: 16 query bases (one packed word) or 16 gaps
-                        const uint32_t c = s_op[lo], op = c & 0xfu;
-                        if (s_r[lo] <= g0 && s_r[lo + 1] >= g0 + 16u) {
+                    {  // 16 columns over copy ops only (M, =, X: one query offset, so 16
+                       // consecutive query bases in one packed word) or over no copy op (16 gaps)
+                        bool allcopy = true, nocopy = true;
+                        for (int h = lo;; ++h) {
+                            const uint32_t op = s_op[h] & 0xfu;
+                            const bool cp = op == 0 || op == 7 || op == 8;
+                            allcopy &= cp, nocopy &= !cp;
+                            if (h >= cn - 1 || s_r[h + 1] >= g0 + 16u) break;
+                        }
+                        if (allcopy || nocopy) {
                             uint4 v;
-                            if (op == 0 || op == 7 || op == 8) {
+                            if (allcopy) {
                                 const uint64_t base = (uint64_t)b.poff[q] * 4u + s_q[lo] + (g0 - s_r[lo]);
                                 const uint32_t* W = reinterpret_cast<const uint32_t*>(b.packed) + (base >> 4);
                                 const uint32_t sh = 2u * (uint32_t)(base & 15u);
