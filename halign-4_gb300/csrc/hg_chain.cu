@@ -55,7 +55,7 @@ __device__ __forceinline__ int32_t chain_score(const IndexDev& ix, const float* 
 
 constexpr int kLog2Max = 512;  // dd <= bw (500), index dd + 1
 
-__global__ void __launch_bounds__(kChainWarps * 32) chain_kernel(IndexDev ix, BatchDev b)
+__global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix, BatchDev b)
 {
     __shared__ float lg2s[kLog2Max + 1];
     for (int k = threadIdx.x; k <= kLog2Max; k += blockDim.x) lg2s[k] = k < ix.n_log2 ? ix.log2tab[k] : 0.0f;
