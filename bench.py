@@ -295,7 +295,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--queries", type=int, default=N_QUERIES, help="queries per GPU")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--sub-batch", type=int, default=25_000, help="queries per device sub-batch (sizes the arenas)")
+    ap.add_argument("--sub-batch", type=int, default=50_000,
+                    help="queries per device sub-batch (sizes the arenas; fewer, larger sub-batches shorten the per-kernel tails, two still overlap copies with compute)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=4000)
