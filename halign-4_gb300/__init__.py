@@ -16,16 +16,25 @@ Typical use (mirrors RefAligner: one center, many queries):
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 from pathlib import Path
 
 import numpy as np
+
+# Each context drives five streams (three DP streams, the input and the copy
+# stream) and a serving pool runs several contexts at once: with the default
+# eight hardware work queues their kernels alias onto shared queues and
+# serialise.  Read when the process creates its CUDA context, so it is set
+# before the library makes its first call (a value already set is kept).
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "libhalign_gb300.so"
 
 HG_OK = 0
 HG_ERR_LENGTH_MISMATCH = 5
+HG_ERR_CAPACITY = 4
 ST_ARENA_OVERFLOW, ST_PARTIAL_CIGAR, ST_CIGAR_OVERFLOW, ST_LENGTH_MISMATCH = 0x01, 0x02, 0x08, 0x10
 LAUNCH_KNOBS = ("seed", "anchor", "chain", "dp_small", "stitch", "rows")  # hg_ctx_set_launch order
 LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32))
@@ -139,16 +148,23 @@ def pack(seqs: bytes, offsets) -> Packed:
         seqs = _bytes(seqs)
     offsets = np.ascontiguousarray(offsets, np.int64)
     n = len(offsets) - 1
-    pb, ne = C.c_int64(0), C.c_int64(0)
+    ne = C.c_int64(0)
     buf = np.frombuffer(seqs, np.uint8) if len(seqs) else np.zeros(1, np.uint8)  # no copy
-    _check(L.hg_pack(_p(buf), _p(offsets), n, None, 0, None, None, 0, None, C.byref(pb), C.byref(ne)))
-    packed = np.empty(max(pb.value, 16), np.uint8)  # every byte is written (padding zeroed)
+    lens = np.diff(offsets)
+    pbytes = int((((lens + 3) // 4 + 15) // 16 * 16).sum()) if n else 0
+    packed = np.empty(max(pbytes, 16), np.uint8)  # every byte is written (padding zeroed)
     poff = np.zeros(max(n, 1), np.int64)
-    exc = np.zeros(max(ne.value, 1) * 3, np.int32)
+    exc = np.zeros(3, np.int32)
     exc_off = np.zeros(n + 1, np.int64)
-    _check(L.hg_pack(_p(buf), _p(offsets), n, _p(packed), len(packed), _p(poff), _p(exc), ne.value, _p(exc_off),
-                     None, None))
-    return Packed(packed, poff[:n], np.diff(offsets).astype(np.int32), exc, exc_off)
+    # one packing pass; a batch with exception runs packs again into a sized list
+    code = L.hg_pack(_p(buf), _p(offsets), n, _p(packed), len(packed), _p(poff), None, 0, _p(exc_off), None,
+                     C.byref(ne))
+    if code == HG_ERR_CAPACITY and ne.value > 0:
+        exc = np.zeros(ne.value * 3, np.int32)
+        code = L.hg_pack(_p(buf), _p(offsets), n, _p(packed), len(packed), _p(poff), _p(exc), ne.value,
+                         _p(exc_off), None, None)
+    _check(code)
+    return Packed(packed, poff[:n], lens.astype(np.int32), exc, exc_off)
 
 
 @dataclass

@@ -367,9 +367,11 @@ int64_t exc_runs(const unsigned char* s, int64_t len, int32_t* exc)
 
 }  // namespace
 
-// Queries are packed independently (OpenMP over queries): a sizing pass gives
-// each query's padded byte count and exception-run count, prefix sums place
-// them, and a second pass writes bases and runs.
+// Queries are packed independently (OpenMP over queries).  Padded byte
+// offsets follow from the lengths alone.  With `packed` given, one pass packs
+// the bases and counts the exception runs of the queries that hold any; a
+// second pass over only those queries writes the runs.  With packed == NULL a
+// pass only counts (sizes for a caller that allocates everything up front).
 extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint8_t* packed, int64_t packed_cap,
                        int64_t* poff, int32_t* exc, int64_t exc_cap, int64_t* exc_off, int64_t* packed_bytes,
                        int64_t* n_exc)
@@ -380,40 +382,43 @@ extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint
         if (len < 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_pack: bad query length");
     }
     const unsigned char* base = reinterpret_cast<const unsigned char*>(seqs);
+    std::vector<int64_t> qoff((size_t)n);
+    int64_t pb = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        qoff[(size_t)i] = pb;
+        pb += (((offsets[i + 1] - offsets[i]) + 3) / 4 + 15) / 16 * 16;
+    }
+    if (packed_bytes) *packed_bytes = pb;
+    if (packed && pb > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
     std::vector<int64_t> nrun((size_t)n);
     const bool par = n >= 64;
 #pragma omp parallel for schedule(dynamic, 16) if (par)
     for (int64_t i = 0; i < n; ++i) {
         const unsigned char* s = base + offsets[i];
         const int64_t len = offsets[i + 1] - offsets[i];
-        nrun[(size_t)i] = pack_one(s, len, nullptr) ? exc_runs(s, len, nullptr) : 0;
+        uint8_t* out = packed ? packed + qoff[(size_t)i] : nullptr;
+        // 4 bases per byte; an exception byte packs as 0 and is listed as a run
+        const bool any_exc = pack_one(s, len, out);
+        if (out) {
+            poff[i] = qoff[(size_t)i];
+            const int64_t used = (len + 3) / 4, nbytes = (used + 15) / 16 * 16;
+            std::memset(out + used, 0, (size_t)(nbytes - used));
+        }
+        nrun[(size_t)i] = any_exc ? exc_runs(s, len, nullptr) : 0;
     }
-    int64_t pb = 0, ne = 0;
-    std::vector<int64_t> qoff((size_t)n), eo((size_t)n + 1);
-    for (int64_t i = 0; i < n; ++i) {
-        qoff[(size_t)i] = pb, eo[(size_t)i] = ne;
-        pb += (((offsets[i + 1] - offsets[i]) + 3) / 4 + 15) / 16 * 16;
-        ne += nrun[(size_t)i];
-    }
+    std::vector<int64_t> eo((size_t)n + 1);
+    int64_t ne = 0;
+    for (int64_t i = 0; i < n; ++i) eo[(size_t)i] = ne, ne += nrun[(size_t)i];
     eo[(size_t)n] = ne;
-    if (packed_bytes) *packed_bytes = pb;
     if (n_exc) *n_exc = ne;
     if (exc_off)
         for (int64_t i = 0; i <= n; ++i) exc_off[i] = eo[(size_t)i];
     if (!packed) return HG_OK;
-    if (pb > packed_cap) return fail(HG_ERR_CAPACITY, "hg_pack: packed buffer too small");
-    if (ne > exc_cap) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
+    if (ne > exc_cap || (ne > 0 && !exc)) return fail(HG_ERR_CAPACITY, "hg_pack: exception buffer too small");
+    if (ne == 0) return HG_OK;
 #pragma omp parallel for schedule(dynamic, 16) if (par)
-    for (int64_t i = 0; i < n; ++i) {
-        const unsigned char* s = base + offsets[i];
-        const int64_t len = offsets[i + 1] - offsets[i];
-        uint8_t* out = packed + qoff[(size_t)i];
-        poff[i] = qoff[(size_t)i];
-        pack_one(s, len, out);  // 4 bases per byte; an exception byte packs as 0 and is listed below
-        const int64_t used = (len + 3) / 4, nbytes = (used + 15) / 16 * 16;
-        std::memset(out + used, 0, (size_t)(nbytes - used));
-        if (nrun[(size_t)i]) exc_runs(s, len, exc + 3 * eo[(size_t)i]);
-    }
+    for (int64_t i = 0; i < n; ++i)
+        if (nrun[(size_t)i]) exc_runs(base + offsets[i], offsets[i + 1] - offsets[i], exc + 3 * eo[(size_t)i]);
     return HG_OK;
 }
 

@@ -6,7 +6,10 @@ arrived requests and a pool of contexts, each with its own CUDA stream and
 arenas.  Whenever a context is free it admits the oldest waiting requests as
 one micro-batch - as many as fit its capacity and the device-memory budget
 of everything in flight - and enqueues it asynchronously (hg_submit); the
-loop polls the busy contexts and collects finished micro-batches.  Requests
+loop polls the busy contexts and collects finished micro-batches.  Packing a
+micro-batch (ASCII to the 2-bit input format, a native call that releases
+the interpreter lock) runs on a worker thread, so the loop keeps submitting
+and collecting while the next micro-batch is packed.  Requests
 that arrive while others are on the GPU therefore join as soon as a slot and
 memory free up, and micro-batches of different contexts overlap on the
 device.  Each request's CIGAR is identical to aligning it alone: requests are
@@ -16,6 +19,7 @@ from __future__ import annotations
 
 import time
 from collections import deque
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -52,6 +56,18 @@ class Server:
         self.slot_bases = slot_bases
         self.slots = [Context(index, max_queries=slot_queries, max_bases=slot_bases) for _ in range(n_slots)]
         self.slot_queries = slot_queries
+        self.packer = ThreadPoolExecutor(max_workers=1)
+
+    @staticmethod
+    def _pack(seqs, offsets, lens, take):
+        a, z = take[0], take[-1]
+        if z - a + 1 == len(take):  # consecutive requests: pack straight from the source buffer
+            blob = memoryview(seqs)[offsets[a]:offsets[z + 1]]
+            offs = (offsets[a:z + 2] - offsets[a]).astype(np.int64)
+        else:
+            blob = b"".join(seqs[offsets[i]:offsets[i + 1]] for i in take)
+            offs = np.concatenate([[0], np.cumsum(lens[take])]).astype(np.int64)
+        return pack(blob, offs)
 
     def run(self, seqs: bytes, offsets: np.ndarray, arrivals: np.ndarray | None = None,
             keep_results: bool = False) -> ServeStats:
@@ -63,6 +79,7 @@ class Server:
         lens = np.diff(offsets).astype(np.int64)
         pending: deque[int] = deque()
         busy: dict[int, tuple[list[int], int]] = {}
+        packing: dict = {}  # slot -> (pack future, requests, bases)
         free = list(range(len(self.slots)))
         done_t = np.zeros(n)
         results = {}
@@ -90,20 +107,19 @@ class Server:
                     inflight += need
                 if not take:
                     break
-                s = free.pop()
-                a, z = take[0], take[-1]
-                if z - a + 1 == len(take):  # consecutive requests: pack straight from the source buffer
-                    blob = memoryview(seqs)[offsets[a]:offsets[z + 1]]
-                    offs = (offsets[a:z + 2] - offsets[a]).astype(np.int64)
-                else:
-                    blob = b"".join(seqs[offsets[i]:offsets[i + 1]] for i in take)
-                    offs = np.concatenate([[0], np.cumsum(lens[take])]).astype(np.int64)
-                self.slots[s].submit(pack(blob, offs))
-                busy[s] = (take, tb)
+                s = free.pop()  # reserved; submitted once its micro-batch is packed
+                packing[s] = (self.packer.submit(self._pack, seqs, offsets, lens, take), take, tb)
                 batches += 1
                 max_inflight = max(max_inflight, inflight)
-            # collect finished micro-batches
             progressed = False
+            for s in list(packing):
+                fut, take, tb = packing[s]
+                if fut.done():
+                    del packing[s]
+                    self.slots[s].submit(fut.result())
+                    busy[s] = (take, tb)
+                    progressed = True
+            # collect finished micro-batches
             for s in list(busy):
                 if self.slots[s].poll():
                     take, tb = busy.pop(s)
@@ -118,7 +134,7 @@ class Server:
                     free.append(s)
                     progressed = True
             if not progressed and not (free and pending):
-                if nxt < n and not busy and not pending:
+                if nxt < n and not busy and not pending and not packing:
                     time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
                 else:
                     time.sleep(20e-6)

@@ -75,7 +75,10 @@ void hg_ctx_destroy(hg_ctx_t* ctx);
 /* Pack ASCII queries into the device input format: 2 bits per A/C/G/T
  * (A=0 C=1 G=2 T=3, base i at bits 2*(i%4) of byte i/4), each query on a
  * 16-byte boundary, every other byte kept as an exception run
- * {start, len, byte}.  With packed == NULL only sizes are returned. */
+ * {start, len, byte}.  With packed == NULL only sizes are returned.  With
+ * packed given and exc too small (or NULL), the bases are packed, *n_exc and
+ * exc_off are set and HG_ERR_CAPACITY is returned: a caller may size `exc`
+ * from *n_exc and call again. */
 int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint8_t* packed, int64_t packed_cap,
             int64_t* poff, int32_t* exc, int64_t exc_cap, int64_t* exc_off, int64_t* packed_bytes,
             int64_t* n_exc);
