@@ -245,15 +245,19 @@ __global__ void __launch_bounds__(kRowWarps * 32) row_kernel(IndexDev ix, BatchD
                 vb = min((col0 + 15u) & ~15u, col1);
                 ve = col1 & ~15u;
                 if (ve < vb) ve = vb;
-                for (uint32_t g0 = vb + 16u * lane; g0 < ve; g0 += 16u * 32u) {
-                    int lo = 0, hi = cn - 1;  // last op with s_r <= g0
-                    while (lo < hi) {
-                        const int mid = (lo + hi + 1) >> 1;
-                        if (s_r[mid] <= g0) lo = mid;
-                        else hi = mid - 1;
-                    }
-                    {  // 16 columns over copy ops only (M, =, X: one query offset, so 16
-                       // consecutive query bases in one packed word) or over no copy op (16 gaps)
+                for (uint32_t gb = vb; gb < ve; gb += 16u * 32u) {  // warp-uniform passes
+                    const uint32_t g0 = gb + 16u * lane;
+                    bool mixed = false;
+                    int lo = 0;
+                    if (g0 < ve) {
+                        int hi = cn - 1;  // last op with s_r <= g0
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (s_r[mid] <= g0) lo = mid;
+                            else hi = mid - 1;
+                        }
+                        // 16 columns over copy ops only (M, =, X: one query offset, so 16
+                        // consecutive query bases in one packed word) or over no copy op (16 gaps)
                         bool allcopy = true, nocopy = true;
                         for (int h = lo;; ++h) {
                             const uint32_t op = s_op[h] & 0xfu;
@@ -261,51 +265,41 @@ __global__ void __launch_bounds__(kRowWarps * 32) row_kernel(IndexDev ix, BatchD
                             allcopy &= cp, nocopy &= !cp;
                             if (h >= cn - 1 || s_r[h + 1] >= g0 + 16u) break;
                         }
-                        if (allcopy || nocopy) {
-                            uint4 v;
-                            if (allcopy) {
-                                const uint64_t base = (uint64_t)b.poff[q] * 4u + s_q[lo] + (g0 - s_r[lo]);
-                                const uint32_t* W = reinterpret_cast<const uint32_t*>(b.packed) + (base >> 4);
-                                const uint32_t sh = 2u * (uint32_t)(base & 15u);
-                                const uint32_t w0 = W[0], w1 = W[1];
-                                const uint32_t codes = sh ? (w0 >> sh) | (w1 << (32u - sh)) : w0;
-                                v = make_uint4(lut[codes & 0xffu], lut[(codes >> 8) & 0xffu], lut[(codes >> 16) & 0xffu],
-                                               lut[codes >> 24]);
-                            } else {
-                                v = make_uint4(0x2d2d2d2du, 0x2d2d2d2du, 0x2d2d2d2du, 0x2d2d2d2du);
-                            }
-                            *reinterpret_cast<uint4*>(row + g0) = v;
-                            continue;
+                        if (allcopy) {
+                            const uint64_t base = (uint64_t)b.poff[q] * 4u + s_q[lo] + (g0 - s_r[lo]);
+                            const uint32_t* W = reinterpret_cast<const uint32_t*>(b.packed) + (base >> 4);
+                            const uint32_t sh = 2u * (uint32_t)(base & 15u);
+                            const uint32_t w0 = W[0], w1 = W[1];
+                            const uint32_t codes = sh ? (w0 >> sh) | (w1 << (32u - sh)) : w0;
+                            *reinterpret_cast<uint4*>(row + g0) = make_uint4(
+                                lut[codes & 0xffu], lut[(codes >> 8) & 0xffu], lut[(codes >> 16) & 0xffu], lut[codes >> 24]);
+                        } else if (nocopy) {
+                            *reinterpret_cast<uint4*>(row + g0) =
+                                make_uint4(0x2d2d2d2du, 0x2d2d2d2du, 0x2d2d2d2du, 0x2d2d2d2du);
+                        } else {
+                            mixed = true;
                         }
                     }
-                    uint64_t wlo = 0, whi = 0;
-                    uint32_t qw = 0xffffffffu;  // first base of the 64-base window held in wlo/whi
-                    uint32_t word[4] = {0, 0, 0, 0};
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        const uint32_t col = g0 + k;
-                        while (lo < cn - 1 && s_r[lo + 1] <= col) ++lo;
-                        const uint32_t c = s_op[lo];
-                        const uint32_t op = c & 0xfu;
-                        uint32_t ch = '-';
-                        if (op == 0 || op == 7 || op == 8) {
-                            const uint32_t qp = s_q[lo] + (col - s_r[lo]);
-                            if (qw == 0xffffffffu || qp < qw || qp >= qw + 64u) {
-                                const uint64_t wb = (((uint64_t)b.poff[q] * 4u + qp) >> 2) & ~(uint64_t)7;
-                                const uint64_t* w = reinterpret_cast<const uint64_t*>(b.packed + wb);
-                                const uint64_t w0 = w[0], w1 = w[1], w2 = w[2];
-                                const uint32_t sh = 2u * (uint32_t)((uint64_t)b.poff[q] * 4u + qp - wb * 4u);
-                                wlo = sh ? (w0 >> sh) | (w1 << (64u - sh)) : w0;
-                                whi = sh ? (w1 >> sh) | (w2 << (64u - sh)) : w1;
-                                qw = qp;
-                            }
-                            const uint32_t m = qp - qw;
-                            const uint32_t code = (uint32_t)(((m < 32u ? wlo : whi) >> (2u * (m & 31u))) & 3u);
-                            ch = 0x54474341u >> (8u * code) & 0xffu;  // "ACGT"
+                    // groups that cross an insertion, a deletion or a clip: two at a
+                    // time, a half-warp per group and a lane per column
+                    unsigned mm = __ballot_sync(FULL, mixed);
+                    while (mm) {
+                        const int l0 = __ffs(mm) - 1;
+                        mm &= mm - 1u;
+                        int l1 = -1;
+                        if (mm) l1 = __ffs(mm) - 1, mm &= mm - 1u;
+                        const int src = lane < 16 ? l0 : l1;
+                        const uint32_t gg = __shfl_sync(FULL, g0, src < 0 ? l0 : src);
+                        int glo = __shfl_sync(FULL, lo, src < 0 ? l0 : src);
+                        if (src >= 0) {
+                            const uint32_t col = gg + (uint32_t)(lane & 15);
+                            while (glo < cn - 1 && s_r[glo + 1] <= col) ++glo;
+                            const uint32_t op = s_op[glo] & 0xfu;
+                            uint8_t ch = '-';
+                            if (op == 0 || op == 7 || op == 8) ch = "ACGT"[packed_code(pk, s_q[glo] + (col - s_r[glo]))];
+                            row[col] = ch;
                         }
-                        word[k >> 2] |= ch << (8 * (k & 3));
                     }
-                    *reinterpret_cast<uint4*>(row + g0) = make_uint4(word[0], word[1], word[2], word[3]);
                 }
             }
             // the columns the vector path left: [col0, vb) and [ve, col1)
