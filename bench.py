@@ -435,8 +435,8 @@ def main():
     # DRAM bytes (read + written) per query base of each dominant-stage kernel
     # from its ncu capture on the mito workload (4,000 queries, 66.3 Mbp),
     # scaled to one launch (one sub-batch) of this run
-    mito_dram_per_base = {"seed": (17.1e6 + 24.2e6) / 66.3e6, "anchor": (81.1e6 + 37.3e6) / 66.3e6,
-                          "chain": (380.6e6 + 146.7e6) / 66.3e6, "rows": (18.4e6 + 7.8e6) / 66.3e6}
+    mito_dram_per_base = {"seed": (17.17e6 + 24.66e6) / 66.3e6, "anchor": (81.10e6 + 38.27e6) / 66.3e6,
+                          "chain": (279.47e6 + 61.87e6) / 66.3e6, "rows": (18.44e6 + 7.78e6) / 66.3e6}
     traffic = None
     if args.workload == "mito" and top in mito_dram_per_base:
         traffic = int(round(mito_dram_per_base[top] * B / n_sub))
