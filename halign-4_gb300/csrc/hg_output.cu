@@ -12,11 +12,12 @@
 // src/align/cigar.cpp:212-299, as mergeConsensusAndSamToFasta calls it with
 // keep=true): M copies the original query byte, D writes '-', I drops query
 // bytes.  Rows are written column-parallel with a binary search over the op
-// prefix sums; insertion events are counted at the center column they
-// precede.
+// prefix sums, 16 columns per lane where they share one query offset and a
+// lane per column where a group crosses an insertion or deletion; insertion
+// events are counted at the center column they precede.
 //
 // K9 accumulates consensus::SiteCount (include/consensus.h:78-99, k_base_map
-// :126-145) for every center column over all rows: each thread owns four
+// :126-145) for every center column over all rows: each thread owns eight
 // columns and a block of rows and adds its register totals once.
 #include "hg_batch.cuh"
 
@@ -169,7 +170,7 @@ __global__ void __launch_bounds__(kStitchWarps * 32) stitch_kernel(IndexDev ix, 
     }
 }
 
-// K8: row projection, one CTA per query (persistent).
+// K8: row projection, one warp per query (persistent CTAs of kRowWarps warps).
 constexpr int kRowWarps = 8;
 constexpr int kRowOps = 256;  // ops per chunk (per warp)
 
