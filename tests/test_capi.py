@@ -55,6 +55,51 @@ def test_pack_roundtrip_and_exceptions(pkg, native):
         assert bytes(out) == s, i
 
 
+def test_pack_single_pass_matches_sizing_protocol(pkg, native):
+    """hg_pack with a packed buffer and no exception list packs in one pass and
+    reports the run count through HG_ERR_CAPACITY; the sized second call and
+    the sizing-first protocol give the same bytes and runs."""
+    L = native
+    rng = np.random.default_rng(3)
+    seqs = []
+    for i in range(200):  # >= 64 queries: the OpenMP loops run
+        s = bytearray(rng.choice(list(b"ACGT"), int(rng.integers(0, 300))).astype(np.uint8).tobytes())
+        if i % 5 == 0 and len(s) > 12:
+            s[3:7] = b"NNNN"
+            s[10] = ord("n")
+        seqs.append(bytes(s))
+    blob = b"".join(seqs)
+    offs = np.concatenate([[0], np.cumsum([len(s) for s in seqs])]).astype(np.int64)
+    buf = np.frombuffer(blob, np.uint8)
+    n = len(seqs)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    pb, ne = C.c_int64(0), C.c_int64(0)
+    assert L.hg_pack(P(buf), P(offs), n, None, 0, None, None, 0, None, C.byref(pb), C.byref(ne)) == 0
+    assert ne.value > 0
+    ref_packed = np.zeros(pb.value, np.uint8)
+    ref_poff, ref_eoff = np.zeros(n, np.int64), np.zeros(n + 1, np.int64)
+    ref_exc = np.zeros(3 * ne.value, np.int32)
+    assert L.hg_pack(P(buf), P(offs), n, P(ref_packed), pb.value, P(ref_poff), P(ref_exc), ne.value, P(ref_eoff),
+                     None, None) == 0
+    packed = np.zeros(pb.value, np.uint8)
+    poff, eoff = np.zeros(n, np.int64), np.zeros(n + 1, np.int64)
+    ne1 = C.c_int64(0)
+    assert L.hg_pack(P(buf), P(offs), n, P(packed), pb.value, P(poff), None, 0, P(eoff), None,
+                     C.byref(ne1)) == 4  # HG_ERR_CAPACITY: runs present, no list given
+    assert ne1.value == ne.value
+    assert np.array_equal(packed, ref_packed) and np.array_equal(poff, ref_poff) and np.array_equal(eoff, ref_eoff)
+    exc = np.zeros(3 * ne1.value, np.int32)
+    assert L.hg_pack(P(buf), P(offs), n, P(packed), pb.value, P(poff), P(exc), ne1.value, P(eoff), None, None) == 0
+    assert np.array_equal(exc, ref_exc)
+    p = pkg.pack(blob, offs)  # the Python wrapper takes the single-pass route
+    assert np.array_equal(p.packed[: pb.value], ref_packed) and np.array_equal(p.exc, ref_exc)
+    assert np.array_equal(p.exc_off, ref_eoff)
+    clean = np.concatenate([[0], np.cumsum([len(s) for s in seqs if b"N" not in s and b"n" not in s])])
+    cblob = b"".join(s for s in seqs if b"N" not in s and b"n" not in s)
+    q = pkg.pack(cblob, clean.astype(np.int64))
+    assert q.exc_off[-1] == 0
+
+
 def test_calls_fail_loudly_without_gpu(pkg, native):
     if pkg.device_count() > 0:
         pytest.skip("a GPU is visible")
