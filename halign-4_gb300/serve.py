@@ -77,6 +77,11 @@ class Server:
         if arrivals is None:
             arrivals = np.zeros(n)
         lens = np.diff(offsets).astype(np.int64)
+        # a request that no context or budget can ever hold would wait forever
+        if n and int(lens.max()) > self.slot_bases:
+            raise ValueError(f"request of {int(lens.max())} bases exceeds the context capacity ({self.slot_bases})")
+        if n and int(lens.max()) * BYTES_PER_BASE > self.budget:
+            raise ValueError("request exceeds the device-memory budget")
         pending: deque[int] = deque()
         busy: dict[int, tuple[list[int], int]] = {}
         packing: dict = {}  # slot -> (pack future, requests, bases)
