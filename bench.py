@@ -7,8 +7,9 @@ stored 2-bit packed.  Synthetic, seeded; no dataset is read.
 
 One step = one pass of the hot path (minimizers -> anchors -> chain ->
 gap-fill DP -> CIGAR -> aligned rows -> per-column counters) over the whole
-batch.  Inputs (1.66 Gbp, 415 MB packed) and all intermediates exceed the
-129 MB L2, so no flush is needed between steps.
+batch, run as two 50,000-query sub-batches (`--sub-batch`; each stage is
+one launch per sub-batch).  Inputs (1.66 Gbp, 415 MB packed) and all
+intermediates exceed the 129 MB L2, so no flush is needed between steps.
 
   value   aligned Mbp/s with the packed batch resident in HBM (hg_run_staged),
           CUDA events on the context stream
