@@ -152,9 +152,14 @@ WORKLOADS = {
 }
 
 
-def make_workload(pkg, n, name="mito"):
+def make_workload(pkg, n, name="mito", rank=0):
+    """Rank r's shard of the seeded workload: queries [r*n, (r+1)*n) (mito:
+    1000-query generator blocks; the others: generator chunk r)."""
     t = time.time()
-    w = getattr(pkg.synth, name)(n)
+    if name == "mito":
+        w = pkg.synth.mito(n, block0=rank * (-(-n // pkg.synth.MITO_CHUNK)))
+    else:
+        w = getattr(pkg.synth, name)(n, chunk=rank)
     log(f"[bench] generated {w.n} queries / {w.total_bases} bases in {time.time() - t:.1f}s")
     t = time.time()
     b = pkg.pack(w.seqs, w.offsets)
@@ -318,9 +323,13 @@ def main():
         raise SystemExit("bench: no CUDA device")
     dist = Dist(world, local, use_gpu=True)
     if world > 1:
-        os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local))
-    w, b = make_workload(pkg, args.queries, args.workload)
+        pkg.set_device(local)  # the library's current device for this process: its index and contexts live there
+    w, b = make_workload(pkg, args.queries, args.workload, rank)
     ix = pkg.Index(w.center)
+    gpu_ordinal, gpu_bus = ix.device()
+    if world > 1:
+        from halign_gb300 import shard
+        shard.check_distinct_devices(gpu_bus, dist.dist)  # two ranks on one GPU would overstate throughput
     sub = min(args.sub_batch, args.queries)
     lens = np.diff(w.offsets)
     ctx = pkg.Context(ix, max_queries=sub, max_bases=int(min(lens.sum(), sub * int(lens.max()))) + 1024)
@@ -455,7 +464,10 @@ def main():
         "data": "synthetic (seeded mutated copies of a uniform ACGT center)",
         "config": {"workload": WORKLOADS[args.workload].format(n=args.queries),
                    "queries_per_gpu": args.queries, "bases_per_gpu": b.bases,
-                   "l2": "inputs and intermediates exceed L2 (no flush needed)", "parallelism": f"replicas x{world}",
+                   "l2": "inputs and intermediates exceed L2 (no flush needed)",
+                   "parallelism": f"dp{world}: rank r aligns queries [r*n, (r+1)*n) of the seeded workload, "
+                                  "center index replicated, no data-path collective",
+                   "device": {"ordinal": gpu_ordinal, "pci_bus_id": gpu_bus},
                    "launch_tuning": tuning},
         "gcups": round(world * cells / step_s / 1e9, 3) if cells else None,
         "gpu_launches": int(launches),

@@ -127,22 +127,25 @@ def _names(prefix: str, i0: int, n: int) -> list[str]:
 MITO_CHUNK = 1000
 
 
-def mito(n: int = 1000, seed: int = 0, center_len: int = 16569) -> Workload:
+def mito(n: int = 1000, seed: int = 0, center_len: int = 16569, block0: int = 0) -> Workload:
     """Full-length mutated copies of a 16,569 bp center (configs 1 and 2).
 
     Queries are drawn in blocks of 1000 with one generator per block, so the
-    first 1000 queries of the 100,000-query workload are the 1000-query one."""
+    first 1000 queries of the 100,000-query workload are the 1000-query one.
+    ``block0`` starts at block ``block0`` (query 1000 * block0) of the same
+    sequence: a rank's shard of a larger workload."""
     center = random_center(center_len, seed)
     src = np.frombuffer(center, np.uint8)
     parts, offs = [], [np.zeros(1, np.int64)]
     for c in range((n + MITO_CHUNK - 1) // MITO_CHUNK):
         m = min(MITO_CHUNK, n - c * MITO_CHUNK)
-        rng = np.random.Generator(np.random.PCG64([seed, 1, c]))
+        rng = np.random.Generator(np.random.PCG64([seed, 1, block0 + c]))
         out, o = mutate_batch(src, np.zeros(MITO_CHUNK, np.int64), np.full(MITO_CHUNK, center_len, np.int64), rng,
                               0.01, 0.001, 0.001, 3.0)
         parts.append(out[: o[m]])
         offs.append(o[1: m + 1] + offs[-1][-1])
-    return Workload("mito", center, np.concatenate(parts).tobytes(), np.concatenate(offs), _names("q", 0, n))
+    return Workload("mito", center, np.concatenate(parts).tobytes(), np.concatenate(offs),
+                    _names("q", block0 * MITO_CHUNK, n))
 
 
 def divergent(n: int = 50000, seed: int = 4, center_len: int = 5000, chunk: int = 0) -> Workload:

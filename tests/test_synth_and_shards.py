@@ -15,6 +15,10 @@ def test_mito_blocks_are_prefix_stable(pkg):
     lens = np.diff(a.offsets)
     assert abs(lens.mean() - 16569) < 40
     assert set(a.seqs) <= set(b"ACGT")
+    # a rank's shard starting at block 1 is the tail of the longer workload
+    c = pkg.synth.mito(200, block0=1)
+    assert c.seqs == a.seqs[a.offsets[1000]:]
+    assert c.names[0] == "q1000"
 
 
 def test_workload_shapes(pkg):
@@ -63,7 +67,14 @@ def _rank_main(rank, world, port, out_q):
     counts = o.count_rows(rows)
     merged = shard.allreduce_counts(counts, dist, torch)
     order = shard.merge_output_order(has_ins, lo, dist, torch)
-    out_q.put((rank, merged, order))
+    # device check of the multi-rank bench: distinct GPUs pass, a shared one fails
+    ids = shard.check_distinct_devices(f"0000:{rank:02x}:00.0", dist)
+    try:
+        shard.check_distinct_devices("0000:01:00.0", dist)
+        shared_refused = False
+    except RuntimeError:
+        shared_refused = True
+    out_q.put((rank, merged, order, ids, shared_refused))
     dist.destroy_process_group()
 
 
@@ -90,3 +101,5 @@ def test_two_rank_shard_and_merge(pkg, oracle):
     for r in res:
         assert np.array_equal(r[1], want_counts)
         assert list(r[2]) == ins + non
+        assert r[3] == ["0000:00:00.0", "0000:01:00.0"]
+        assert r[4]
