@@ -41,6 +41,31 @@ LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32))
 STAGES = ("seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count")
 
 
+# anchor::Anchor as the C ABI's hg_anchor_t (32 bytes)
+ANCHOR_DTYPE = np.dtype([("hash", "<u8"), ("rid_ref", "<u4"), ("pos_ref", "<u4"), ("rid_qry", "<u4"),
+                         ("pos_qry", "<u4"), ("span", "<u4"), ("is_rev", "<u4")])
+
+
+class Params(C.Structure):
+    """hg_params_t: anchor::SeedFilterParams + anchor::ChainParams."""
+    _fields_ = [("f_top_frac", C.c_double), ("u_floor", C.c_uint64), ("u_ceil", C.c_uint64),
+                ("q_occ_frac", C.c_double), ("sample_every_bp", C.c_uint64), ("max_dist_x", C.c_int32),
+                ("max_dist_y", C.c_int32), ("bw", C.c_int32), ("max_skip", C.c_int32), ("max_iter", C.c_int32),
+                ("min_cnt", C.c_int32), ("min_score", C.c_int32), ("gap_penalty", C.c_float),
+                ("skip_penalty", C.c_float)]
+
+
+def params(**overrides) -> Params:
+    """The reference's default seeding and chaining parameters with overrides."""
+    p = Params()
+    lib().hg_default_params(C.byref(p))
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
 class HalignError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"[{code}] {msg}")
@@ -65,6 +90,8 @@ def lib() -> C.CDLL:
     vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int
     L.hg_last_error.restype = C.c_char_p
     L.hg_device_count.restype = i32
+    L.hg_set_device.argtypes = [i32]
+    L.hg_index_device.argtypes = [vp, vp, C.c_char_p, i32]
     L.hg_default_params.argtypes = [vp]
     L.hg_index_create.argtypes = [C.c_char_p, i64, i32, i32, vp, C.POINTER(vp)]
     L.hg_index_destroy.argtypes = [vp]
@@ -98,6 +125,16 @@ def lib() -> C.CDLL:
     L.hg_global_align_mm2.restype = i64
     L.hg_ctx_set_launch.argtypes = [vp, vp, i32]
     L.hg_ctx_get_launch.argtypes = [vp, vp, i32]
+    L.hg_fetch_chain.argtypes = [vp, i64, vp, vp, vp, vp, i64, vp, vp, vp]
+    L.hg_hits_create.argtypes = [vp, vp, i64, vp, C.POINTER(vp)]
+    L.hg_hits_destroy.argtypes = [vp]
+    L.hg_collect_anchors.argtypes = [vp, vp, vp, i64, vp, vp, i64, vp]
+    L.hg_collect_anchors.restype = i64
+    L.hg_chain_anchors.argtypes = [vp, i64, vp, vp, i64, vp, vp]
+    L.hg_chain_anchors.restype = i64
+    L.hg_project_row.argtypes = [C.c_char_p, i64, vp, i64, i32, vp, i64]
+    L.hg_project_row.restype = i64
+    L.hg_count_rows.argtypes = [vp, i64, i64, i64, vp, i32]
     _lib = L
     return L
 
@@ -109,6 +146,12 @@ def _check(code: int):
 
 def device_count() -> int:
     return int(lib().hg_device_count())
+
+
+def set_device(ordinal: int) -> None:
+    """Make CUDA device `ordinal` current for this thread (hg_set_device):
+    indexes created afterwards, and their contexts, live on it."""
+    _check(lib().hg_set_device(int(ordinal)))
 
 
 def _bytes(s) -> bytes:
@@ -182,12 +225,13 @@ class AlignResult:
 class Index:
     """Resident center index (RefAligner's per-center set-up, kept in HBM)."""
 
-    def __init__(self, center, k: int = 15, w: int = 10):
+    def __init__(self, center, k: int = 15, w: int = 10, prm: Params | None = None):
         L = lib()
         self.center = _bytes(center)
         self.k, self.w = k, w
         h = C.c_void_p()
-        _check(L.hg_index_create(self.center, len(self.center), k, w, None, C.byref(h)))
+        _check(L.hg_index_create(self.center, len(self.center), k, w, C.byref(prm) if prm is not None else None,
+                                 C.byref(h)))
         self.h = h
         self.L = len(self.center)
 
@@ -195,6 +239,13 @@ class Index:
         a, b, c = C.c_int64(), C.c_int64(), C.c_uint64()
         _check(lib().hg_index_info(self.h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
+
+    def device(self) -> tuple[int, str]:
+        """(ordinal, PCI bus id) of the GPU this index lives on."""
+        o = C.c_int()
+        bus = C.create_string_buffer(32)
+        _check(lib().hg_index_device(self.h, C.byref(o), bus, 32))
+        return o.value, bus.value.decode()
 
     def align_query(self, qry) -> np.ndarray:
         q = _bytes(qry)
@@ -334,6 +385,26 @@ class Context:
         _check(lib().hg_ctx_work(self.h, _p(v), 3))
         return {"anchors": int(v[0]), "records": int(v[1]), "dp_segments": int(v[2])}
 
+    def fetch_chain(self, q: int):
+        """Anchors (sorted as chainAnchors sorts them), the chain DP arrays and
+        the best chain of staged query q (hg_fetch_chain)."""
+        na, end, nc = C.c_int64(), C.c_int64(), C.c_int64()
+        _check(lib().hg_fetch_chain(self.h, q, None, None, None, None, 0, C.byref(na), C.byref(end), C.byref(nc)))
+        A = na.value
+        r, qq = np.zeros(A, np.uint32), np.zeros(A, np.uint32)
+        f, pp = np.zeros(A, np.int32), np.zeros(A, np.int32)
+        _check(lib().hg_fetch_chain(self.h, q, _p(r), _p(qq), _p(f), _p(pp), A, C.byref(na), C.byref(end),
+                                    C.byref(nc)))
+        chain = []
+        if nc.value > 0:
+            c = end.value
+            while c >= 0:
+                chain.append(c)
+                c = int(pp[c])
+            chain.reverse()
+        return {"pos_ref": r, "pos_qry": qq, "f": f, "p": pp, "chain_end": end.value, "n_chain": nc.value,
+                "chain": np.asarray(chain, np.int64)}
+
     def counters(self, reset: bool = False):
         L = self.index.L
         cnt = np.zeros((L, 7), np.uint32)
@@ -387,6 +458,83 @@ def global_align_ksw2(ref, qry, flag: int = -1) -> np.ndarray:
     if n < 0:
         _check(-n)
     return c[:n].copy()
+
+
+class Hits:
+    """Reference-side minimizer hits of collect_anchors, resident on the GPU
+    (hg_hits_create); collect() runs collect_anchors for a query hit list."""
+
+    def __init__(self, ref_x, ref_y, prm: Params | None = None):
+        rx = np.ascontiguousarray(ref_x, np.uint64)
+        ry = np.ascontiguousarray(ref_y, np.uint64)
+        h = C.c_void_p()
+        _check(lib().hg_hits_create(_p(rx), _p(ry), len(rx), C.byref(prm) if prm is not None else None,
+                                    C.byref(h)))
+        self.h = h
+
+    def collect(self, qry_x, qry_y, prm: Params | None = None) -> np.ndarray:
+        qx = np.ascontiguousarray(qry_x, np.uint64)
+        qy = np.ascontiguousarray(qry_y, np.uint64)
+        cap = max(16, 2 * len(qx))
+        for _ in range(2):
+            out = np.zeros(cap, ANCHOR_DTYPE)
+            need = C.c_int64()
+            n = lib().hg_collect_anchors(self.h, _p(qx), _p(qy), len(qx), C.byref(prm) if prm is not None else None,
+                                         _p(out), cap, C.byref(need))
+            if n >= 0:
+                return out[:n].copy()
+            if n != -HG_ERR_CAPACITY:
+                _check(-n)
+            cap = need.value
+        _check(-n)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hg_hits_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def chain_anchors(anchors, prm: Params | None = None):
+    """anchor::chainAnchors on the GPU: (anchors sorted in place, chain
+    indices into them, f, p)."""
+    a = np.ascontiguousarray(anchors, ANCHOR_DTYPE).copy()
+    n = len(a)
+    chain = np.zeros(max(n, 1), np.int64)
+    f = np.zeros(max(n, 1), np.int32)
+    pp = np.zeros(max(n, 1), np.int64)
+    m = lib().hg_chain_anchors(_p(a), n, C.byref(prm) if prm is not None else None, _p(chain), len(chain), _p(f),
+                               _p(pp))
+    if m < 0:
+        _check(-m)
+    return a, chain[:m].copy(), f[:n].copy(), pp[:n].copy()
+
+
+def project_row(qry, cigar, pad: bool = False) -> bytes:
+    """delQueryToRefByCigar (pad=False) / padQueryToRefByCigar (pad=True) on the GPU."""
+    q = _bytes(qry)
+    c = np.ascontiguousarray(cigar, np.uint32)
+    cap = len(q) + int(sum(int(x) >> 4 for x in c)) + 16
+    out = np.zeros(max(cap, 1), np.uint8)
+    n = lib().hg_project_row(q, len(q), _p(c), len(c), int(pad), _p(out), cap)
+    if n < 0:
+        _check(-n)
+    return out[:n].tobytes()
+
+
+def count_rows(rows: np.ndarray, counts: np.ndarray | None = None) -> np.ndarray:
+    """SiteCount totals (L x 7: A C G T U N -) of the rows of a 2-D uint8
+    array, added to `counts` when given."""
+    r = np.ascontiguousarray(rows, np.uint8)
+    n, L = r.shape
+    out = np.zeros((L, 7), np.uint32) if counts is None else np.ascontiguousarray(counts, np.uint32).copy()
+    _check(lib().hg_count_rows(_p(r), n, L, L, _p(out), int(counts is not None)))
+    return out
 
 
 def build_library(force: bool = False) -> Path:

@@ -256,6 +256,8 @@ struct BatchDev {
     int64_t* s_base;
     int32_t* s_n;
     int32_t* n_chain;
+    int32_t* chain_meta;         // per query: best chain end (-1: none), first anchor whose speculated
+                                 // predecessor was wrong (the anchor count if none); p is stored from there on
     uint32_t* work_small;        // global segment ids per DP tier
     uint32_t* work_large;
     uint32_t* work_sorted;       // small tier sorted by shape_key (unused when work_rec is set)

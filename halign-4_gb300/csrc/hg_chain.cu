@@ -410,6 +410,7 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
         sb = __shfl_sync(FULL, sb, 0);
         if (lane == 0) {
             b.n_chain[q] = c;
+            if (b.chain_meta) b.chain_meta[2 * q] = best, b.chain_meta[2 * q + 1] = k0;
             b.s_base[q] = sb == ~0ull ? 0 : (int64_t)sb;
             b.s_n[q] = 0;
         }

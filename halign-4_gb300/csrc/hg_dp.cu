@@ -32,6 +32,7 @@
 #include <type_traits>
 #include <mutex>
 
+#include "../../include/halign_gb300.h"
 #include "hg_batch.cuh"
 
 namespace hg {
@@ -922,7 +923,31 @@ __device__ KswResult ksw_extz2_warp(const KswArgs& a, uint8_t* scratch, uint32_t
         const uint32_t x1e = (x1 & 0x80u) ? 0xffu : 0u, v1e = (v1 & 0x80u) ? 0xffu : 0u;
         __syncwarp();
         if (lane == 0 && en >= r) y[r] = 0, u[r] = (uint8_t)(r ? q : 0);
-        for (int t = st0 + lane; t <= en0; t += 32) s[t] = (uint8_t)a.mat[a.target[t] * m + ksw_qcode(a, r - t)];
+        if (a.flag & kEzGenericSc) {
+            for (int t = st0 + lane; t <= en0; t += 32) s[t] = (uint8_t)a.mat[a.target[t] * m + ksw_qcode(a, r - t)];
+        } else {
+            // match/mismatch scoring with symbol m-1 as the wildcard
+            // (ksw2_extz2_sse.c:123-137): the reference fills whole 16-byte
+            // blocks from st0, so lanes past en0 up to the block end get a
+            // score too, from what its buffers hold there - the target copy's
+            // zero padding up to Lb, then the reversed query (zeros past its
+            // end).  Those lanes are stale state for later anti-diagonals.
+            // Lanes at or past Lb are never computed, so they are not stored.
+            const int mch = a.mat[0], mis = a.mat[1];
+            const int scn = a.mat[m * m - 1] == 0 ? -e : a.mat[m * m - 1];
+            const int tend = min(st0 + ((en0 - st0) / 16 + 1) * 16 - 1, (int)Lb - 1);
+            for (int t = st0 + lane; t <= tend; t += 32) {
+                int sq;  // the target copy at t
+                if (t < tlen) sq = a.target[t];
+                else if (t < (int)Lb) sq = 0;
+                else sq = t - (int)Lb < qlen ? ksw_qcode(a, qlen - 1 - (t - (int)Lb)) : 0;
+                const int kq = qlen - 1 - r + t;  // the reversed query at qlen-1-r+t
+                const int sr = kq < qlen ? ksw_qcode(a, qlen - 1 - kq) : 0;
+                int sc = sq == sr ? mch : mis;
+                if (sq == m - 1 || sr == m - 1) sc = scn;
+                s[t] = (uint8_t)sc;
+            }
+        }
         __syncwarp();
         if (with_cigar && lane == 0) off[r] = st, off_end[r] = en;
         uint8_t* pr = with_cigar ? p + (size_t)r * ncol : nullptr;
@@ -1759,14 +1784,31 @@ extern "C" cudaError_t hg_launch_ksw_single(int qlen, const uint8_t* d_query, in
 //     streams, or different host threads) race on the array: serialise them.
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current; make that first call
-//     before any stream capture.
+//     before any stream capture.  The address is kept per device ordinal for
+//     the process's primary context: it is not valid in another driver
+//     context of that device, nor after cudaDeviceReset.
 constexpr size_t kNoAllocScratchBytes = (size_t)1 << 20;
+static_assert(kNoAllocScratchBytes == HG_NOALLOC_SCRATCH_BYTES, "scratch size and its public limit disagree");
 static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes];
 
 namespace hg {
 __global__ void ksw_noalloc_kernel(KswArgs a, uint8_t* scratch, uint32_t* cig, int cap, int32_t* res)
 {
     if (threadIdx.x >= 32) return;
+    // The sequences are device memory, so the host cannot check them: a
+    // symbol >= m would index past the m x m matrix.  Such a call computes
+    // nothing, leaves the CIGAR buffer untouched and reports length -1.
+    bool bad = false;
+    for (int i = threadIdx.x; i < a.qlen; i += 32) bad |= a.query[i] >= a.m;
+    for (int i = threadIdx.x; i < a.tlen; i += 32) bad |= a.target[i] >= a.m;
+    if (__any_sync(0xffffffffu, bad)) {
+        if (threadIdx.x == 0) {
+            res[0] = 0, res[1] = 0, res[2] = -1, res[3] = -1, res[4] = kNegInf;
+            res[5] = -1, res[6] = kNegInf, res[7] = -1, res[8] = kNegInf, res[9] = 0;
+            res[10] = -1;
+        }
+        return;
+    }
     const KswResult R = ksw_extz2_warp(a, scratch, cig, cap);
     if (threadIdx.x == 0) {
         res[0] = R.max, res[1] = R.zdropped, res[2] = R.max_q, res[3] = R.max_t, res[4] = R.mqe;
@@ -1794,7 +1836,7 @@ extern "C" int hg_ksw_extz2_noalloc(int qlen, const uint8_t* d_query, int tlen, 
                                     char* err, int64_t err_cap)
 {
     if (err && err_cap > 0) err[0] = 0;
-    if (!(flag & hg::kEzGenericSc) || m <= 0 || m > 16 || !d_mat || !d_ez || (qlen > 0 && !d_query) ||
+    if (m <= 0 || m > 16 || !d_mat || !d_ez || (qlen > 0 && !d_query) ||
         (tlen > 0 && !d_target) || cap < 0 || cap > INT32_MAX || (cap > 0 && !d_cigar))
         return noalloc_fail(err, err_cap, 2, "hg_ksw_extz2_noalloc: bad arguments");  // HG_ERR_ARG
     const size_t need = hg_ksw_scratch_bytes(qlen, tlen, w, flag);

@@ -25,6 +25,7 @@
 
 #include "../../include/halign_gb300.h"
 #include "hg_batch.cuh"
+#include "hg_internal.h"
 
 extern "C" {
 cudaError_t hg_launch_seed(const hg::IndexDev*, const hg::BatchDev*, int, uint64_t*, uint64_t*, int, cudaStream_t);
@@ -47,48 +48,21 @@ cudaError_t hg_launch_ksw_single(int, const uint8_t*, int, const uint8_t*, int, 
                                  int, int, uint8_t*, uint32_t*, int, void*, cudaStream_t);
 }
 
-namespace {
-
 thread_local std::string g_err;
 
-int fail(int code, const std::string& msg)
+int hg::set_error(int code, const std::string& msg)
 {
     g_err = msg;
     return code;
 }
 
-int cuda_fail(cudaError_t e, const char* where)
-{
-    return fail(HG_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
-}
+namespace {
 
-#define HG_CUDA(call)                                         \
-    do {                                                      \
-        cudaError_t e_ = (call);                              \
-        if (e_ != cudaSuccess) return cuda_fail(e_, #call);   \
-    } while (0)
+using hg::DevBuf;
 
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { free(); }
-    cudaError_t alloc(size_t count)
-    {
-        free();
-        n = count;
-        return count ? cudaMalloc(&p, sizeof(T) * count) : cudaSuccess;
-    }
-    void free()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
+int fail(int code, const std::string& msg) { return hg::set_error(code, msg); }
+
+int cuda_fail(cudaError_t e, const char* where) { return hg::cuda_error(e, where); }
 
 uint8_t consensus_letter(uint8_t c)
 {  // pickConsensusChar over one record's k_base_map category
@@ -167,7 +141,7 @@ struct hg_ctx {
     int64_t scap = 0;
     DevBuf<hg::Seg> seg;
     DevBuf<int64_t> s_base;
-    DevBuf<int32_t> s_n, n_chain;
+    DevBuf<int32_t> s_n, n_chain, chain_meta;
     DevBuf<uint32_t> work_small, work_large, work_sorted, work_key, shape_hist;
     DevBuf<uint32_t> work_wave, work_wave_key, work_wave_sorted, wave_hist, work_wide;
     DevBuf<uint32_t> work_thin, work_thin_key, work_thin_sorted;  // thin_hist lives in wave_hist
@@ -252,6 +226,15 @@ extern "C" int hg_device_count(void)
         return 0;
     }
     return n;
+}
+
+extern "C" int hg_set_device(int ordinal)
+{
+    const int n = hg_device_count();
+    if (ordinal < 0 || ordinal >= n) return fail(HG_ERR_ARG, "hg_set_device: ordinal out of range");
+    const cudaError_t e = cudaSetDevice(ordinal);
+    if (e != cudaSuccess) return cuda_fail(e, "hg_set_device");
+    return HG_OK;
 }
 
 extern "C" void hg_default_params(hg_params_t* p)
@@ -426,71 +409,9 @@ extern "C" int hg_pack(const char* seqs, const int64_t* offsets, int64_t n, uint
 
 namespace {
 
-// Minimal one-query batch on a scratch context-free buffer set, used for the
-// center and for single-call extractMinimizer.
-int run_extract(int dev_k, int dev_w, int non_canonical, const char* seq, int64_t len, std::vector<uint64_t>& xs,
-                std::vector<uint64_t>& ys, cudaStream_t st)
-{
-    xs.clear(), ys.clear();
-    if (len < dev_k || dev_k <= 0 || dev_k > 31 || dev_w <= 0 || dev_w >= 256) return HG_OK;
-    const int64_t offs[2] = {0, len};
-    int64_t pbytes = 0, nexc = 0;
-    int r = hg_pack(seq, offs, 1, nullptr, 0, nullptr, nullptr, 0, nullptr, &pbytes, &nexc);
-    if (r) return r;
-    std::vector<uint8_t> pk((size_t)pbytes);
-    std::vector<int64_t> poff(1), eoff(2);
-    std::vector<int32_t> exc((size_t)std::max<int64_t>(nexc, 1) * 3);
-    r = hg_pack(seq, offs, 1, pk.data(), pbytes, poff.data(), exc.data(), nexc, eoff.data(), nullptr, nullptr);
-    if (r) return r;
-    const int64_t cap = len - dev_k + 1;
-    DevBuf<uint8_t> d_pk;
-    DevBuf<int64_t> d_poff, d_eoff, d_hoff;
-    DevBuf<int32_t> d_qlen, d_exc, d_nh, d_nm;
-    DevBuf<uint64_t> d_x, d_y;
-    DevBuf<uint32_t> d_status, d_exact;
-    DevBuf<unsigned int> d_q;
-    const int ring_slots = 2 * dev_w + 16;
-    HG_CUDA(d_exact.alloc(1));
-    HG_CUDA(d_pk.alloc(pk.size()));
-    HG_CUDA(d_poff.alloc(1));
-    HG_CUDA(d_eoff.alloc(2));
-    HG_CUDA(d_hoff.alloc(1));
-    HG_CUDA(d_qlen.alloc(1));
-    HG_CUDA(d_exc.alloc(exc.size()));
-    HG_CUDA(d_nh.alloc(1));
-    HG_CUDA(d_nm.alloc(1));
-    HG_CUDA(d_x.alloc(cap));
-    HG_CUDA(d_y.alloc(cap));
-    HG_CUDA(d_q.alloc(16));
-    HG_CUDA(cudaMemcpyAsync(d_pk.p, pk.data(), pk.size(), cudaMemcpyHostToDevice, st));
-    const int32_t ql = (int32_t)len;
-    const int64_t zero = 0;
-    HG_CUDA(cudaMemcpyAsync(d_poff.p, poff.data(), 8, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(d_eoff.p, eoff.data(), 16, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(d_hoff.p, &zero, 8, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(d_qlen.p, &ql, 4, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(d_exc.p, exc.data(), exc.size() * 4, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemsetAsync(d_q.p, 0, 64, st));
-    hg::IndexDev ixd{};
-    ixd.k = dev_k, ixd.w = dev_w, ixd.non_canonical = non_canonical;
-    hg::BatchDev bd{};
-    bd.n = 1, bd.packed = d_pk.p, bd.poff = d_poff.p, bd.qlen = d_qlen.p, bd.exc = d_exc.p, bd.exc_off = d_eoff.p;
-    bd.hoff = d_hoff.p, bd.n_hits = d_nh.p, bd.n_matched = d_nm.p, bd.queues = d_q.p;
-    bd.exact_list = d_exact.p, bd.n_exact = d_q.p + 8;
-    bd.ring_slots = ring_slots;
-    HG_CUDA(hg_launch_seed(&ixd, &bd, 1, d_x.p, d_y.p, 1, st));
-    int32_t nh = 0;
-    HG_CUDA(cudaMemcpyAsync(&nh, d_nh.p, 4, cudaMemcpyDeviceToHost, st));
-    HG_CUDA(cudaStreamSynchronize(st));
-    xs.resize(nh), ys.resize(nh);
-    if (nh) {
-        HG_CUDA(cudaMemcpy(xs.data(), d_x.p, 8 * (size_t)nh, cudaMemcpyDeviceToHost));
-        HG_CUDA(cudaMemcpy(ys.data(), d_y.p, 8 * (size_t)nh, cudaMemcpyDeviceToHost));
-    }
-    return HG_OK;
-}
+}  // namespace
 
-uint64_t occ_threshold(std::vector<uint64_t> occs, const hg_params_t& p)
+uint64_t hg::occ_threshold(std::vector<uint64_t> occs, const hg_params_t& p)
 {  // compute_ref_occ_threshold (src/seed/anchor.cpp:73-117)
     uint64_t f_cut;
     if (occs.empty() || p.f_top_frac <= 0.0) f_cut = UINT64_MAX;
@@ -507,7 +428,27 @@ uint64_t occ_threshold(std::vector<uint64_t> occs, const hg_params_t& p)
     return std::max(p.u_floor, capped);
 }
 
-}  // namespace
+extern "C" uint64_t hg_occ_threshold(const uint64_t* occs, int64_t n, const hg_params_t* params,
+                                     uint64_t* cutoff_top_frac)
+{
+    hg_params_t p;
+    if (params) p = *params;
+    else hg_default_params(&p);
+    std::vector<uint64_t> v(occs, occs + (n > 0 ? n : 0));
+    if (cutoff_top_frac) {
+        hg_params_t q = p;  // the -f cutoff alone: no -U bounds
+        q.u_floor = 0, q.u_ceil = UINT64_MAX;
+        *cutoff_top_frac = hg::occ_threshold(v, q);
+    }
+    return hg::occ_threshold(std::move(v), p);
+}
+
+std::vector<float> hg::log2_table(int n)
+{
+    std::vector<float> lg((size_t)n);
+    for (int i = 0; i < n; ++i) lg[i] = i >= 1 ? (float)std::log2((double)i) : 0.0f;
+    return lg;
+}
 
 extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params,
                                hg_index_t** out)
@@ -522,14 +463,8 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     else hg_default_params(&ix->prm);
     ix->center_raw.assign(center, (size_t)len);
     ix->L = (int)len;
-    cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
-        delete ix;
-        return fail(HG_ERR_CUDA, "hg_index_create: stream");
-    }
     std::vector<uint64_t> xs, ys;
-    int r = run_extract(k, w, 1, center, len, xs, ys, st);
-    cudaStreamDestroy(st);
+    int r = hg::run_extract(k, w, 1, center, len, xs, ys);
     if (r) {
         delete ix;
         return r;
@@ -557,7 +492,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
         ecnt.back()++;
     }
     for (auto c : ecnt) occs.push_back(c);
-    ix->occ_thr = occ_threshold(occs, ix->prm);
+    ix->occ_thr = hg::occ_threshold(occs, ix->prm);
     std::vector<uint8_t> over(ekey.size());
     for (size_t e = 0; e < ekey.size(); ++e) over[e] = ecnt[e] > ix->occ_thr ? 1 : 0;
     uint32_t tsize = 16;
@@ -583,8 +518,7 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     }
     // log2f table for the chain penalty (arguments 2 .. bw+1)
     const int nlog = std::max(ix->prm.bw + 2, 513);
-    std::vector<float> lg((size_t)nlog);
-    for (int i = 0; i < nlog; ++i) lg[i] = i >= 1 ? (float)std::log2((double)i) : 0.0f;
+    const std::vector<float> lg = hg::log2_table(nlog);
     // per entry: its center position when it occurs once (the common case),
     // else its start in cpos; the occurrence count with the over-threshold bit
     std::vector<uint2> meta(ekey.size());
@@ -639,10 +573,22 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
 extern "C" void hg_index_destroy(hg_index_t* ix)
 {
     if (!ix) return;
+    cudaSetDevice(ix->device);
     if (ix->single) hg_ctx_destroy(ix->single);
     ix->center.free(), ix->tab.free(), ix->ent_meta.free();
     ix->cpos.free(), ix->cspan.free(), ix->log2tab.free(), ix->center2.free();
     delete ix;
+}
+
+extern "C" int hg_index_device(const hg_index_t* ix, int* ordinal, char* pci_bus_id, int len)
+{
+    if (!ix) return fail(HG_ERR_ARG, "hg_index_device: null index");
+    if (ordinal) *ordinal = ix->device;
+    if (pci_bus_id && len > 0) {
+        const cudaError_t e = cudaDeviceGetPCIBusId(pci_bus_id, len, ix->device);
+        if (e != cudaSuccess) return cuda_fail(e, "hg_index_device");
+    }
+    return HG_OK;
 }
 
 extern "C" int hg_index_info(const hg_index_t* ix, int64_t* n_distinct, int64_t* n_hits, uint64_t* occ_threshold)
@@ -768,7 +714,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->a_base.alloc(max_queries)) || (e = c->a_n.alloc(max_queries)) ||
         (e = c->ent_cnt.alloc(n_ent > 8192 ? (size_t)grid_anchor * n_ent : 1)) || (e = c->seg.alloc(c->scap)) ||
         (e = c->s_base.alloc(max_queries)) || (e = c->s_n.alloc(max_queries)) ||
-        (e = c->n_chain.alloc(max_queries)) || (e = c->work_small.alloc(c->scap)) ||
+        (e = c->n_chain.alloc(max_queries)) || (e = c->chain_meta.alloc(2 * max_queries)) || (e = c->work_small.alloc(c->scap)) ||
         (e = c->work_large.alloc(c->scap)) || (e = c->dp_arena.alloc(c->dp_cap)) ||
         (e = c->work_sorted.alloc(c->scap)) || (e = c->work_key.alloc(c->scap)) ||
         (e = c->shape_hist.alloc(2 * (size_t)hg::kShapeBins)) ||
@@ -829,6 +775,7 @@ extern "C" int hg_ctx_get_launch(const hg_ctx_t* c, int32_t* ctas_per_sm, int n)
 extern "C" void hg_ctx_destroy(hg_ctx_t* c)
 {
     if (!c) return;
+    cudaSetDevice(c->ix->device);
     if (c->st) cudaStreamSynchronize(c->st);
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     if (c->h_packed) cudaFreeHost(c->h_packed);
@@ -909,6 +856,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.cells = c->cells.p;
     b.a_base = c->a_base.p, b.a_n = c->a_n.p, b.ent_cnt = c->ent_cnt.p;
     b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
+    b.chain_meta = c->chain_meta.p;
     b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
     b.work_sorted = c->work_sorted.p, b.work_key = c->work_key.p, b.shape_hist = c->shape_hist.p;
     b.work_wave = c->work_wave.p, b.work_wave_key = c->work_wave_key.p, b.work_wave_sorted = c->work_wave_sorted.p;
@@ -1330,6 +1278,7 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
                 // per-query outputs land at index 0 of the view: shift the output arrays
                 b.n_hits = c->n_hits.p + i, b.n_matched = c->n_matched.p + i, b.a_base = c->a_base.p + i,
                 b.a_n = c->a_n.p + i, b.s_base = c->s_base.p + i, b.s_n = c->s_n.p + i, b.n_chain = c->n_chain.p + i;
+                b.chain_meta = c->chain_meta.p + 2 * i;
                 b.n_cig = c->n_cig.p + i, b.has_ins = c->has_ins.p + i, b.status = c->status.p + i;
                 b.rows = c->rows.p + i * c->row_stride;
                 if (i == 0) HG_CUDA(cudaMemsetAsync(c->status.p, 0, 4 * (size_t)sp.n, c->st));
@@ -1384,9 +1333,43 @@ extern "C" int hg_align_plain(hg_ctx_t* ctx, const uint8_t* packed, const int64_
                       row_stride, status, true);
 }
 
+extern "C" int hg_fetch_chain(hg_ctx_t* c, int64_t query, uint32_t* pos_ref, uint32_t* pos_qry, int32_t* f,
+                              int32_t* p, int64_t cap, int64_t* n_anchors, int64_t* chain_end, int64_t* n_chain)
+{
+    if (!c || !c->staged || !n_anchors || query < 0 || query >= (int64_t)c->staged_qlen.size())
+        return fail(HG_ERR_ARG, "hg_fetch_chain: bad arguments or nothing staged");
+    if (c->staged_plan.size() != 1)
+        return fail(HG_ERR_ARG, "hg_fetch_chain: the staged batch spans several sub-batches");
+    cudaSetDevice(c->ix->device);
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    int64_t base = 0;
+    int32_t A = 0, nc = 0, meta[2] = {-1, 0};
+    HG_CUDA(cudaMemcpy(&base, c->a_base.p + query, 8, cudaMemcpyDeviceToHost));
+    HG_CUDA(cudaMemcpy(&A, c->a_n.p + query, 4, cudaMemcpyDeviceToHost));
+    HG_CUDA(cudaMemcpy(&nc, c->n_chain.p + query, 4, cudaMemcpyDeviceToHost));
+    HG_CUDA(cudaMemcpy(meta, c->chain_meta.p + 2 * query, 8, cudaMemcpyDeviceToHost));
+    *n_anchors = A;
+    if (chain_end) *chain_end = meta[0];
+    if (n_chain) *n_chain = nc;
+    if (A > cap || A == 0) return HG_OK;
+    std::vector<int32_t> fv((size_t)A), pv((size_t)A);
+    if (pos_ref) HG_CUDA(cudaMemcpy(pos_ref, c->a_ref.p + base, 4 * (size_t)A, cudaMemcpyDeviceToHost));
+    if (pos_qry) HG_CUDA(cudaMemcpy(pos_qry, c->a_qry.p + base, 4 * (size_t)A, cudaMemcpyDeviceToHost));
+    HG_CUDA(cudaMemcpy(fv.data(), c->a_f.p + base, 4 * (size_t)A, cudaMemcpyDeviceToHost));
+    HG_CUDA(cudaMemcpy(pv.data(), c->a_p.p + base, 4 * (size_t)A, cudaMemcpyDeviceToHost));
+    // below the first wrong speculation the kernel keeps p implicit: the
+    // previous anchor when f exceeds the lone-anchor score (the span, k)
+    const int32_t k0 = std::min(std::max(meta[1], 0), A);
+    for (int32_t i = 0; i < k0; ++i) pv[i] = fv[i] > c->ix->k ? i - 1 : -1;
+    if (f) std::copy(fv.begin(), fv.end(), f);
+    if (p) std::copy(pv.begin(), pv.end(), p);
+    return HG_OK;
+}
+
 extern "C" int hg_counters(hg_ctx_t* c, uint32_t* counts7, uint32_t* ins, int reset)
 {
     if (!c) return fail(HG_ERR_ARG, "hg_counters: null context");
+    cudaSetDevice(c->ix->device);
     const int64_t L = c->ix->L;
     HG_CUDA(cudaStreamSynchronize(c->st));
     if (counts7) HG_CUDA(cudaMemcpy(counts7, c->counts.p, 4 * (size_t)L * 7, cudaMemcpyDeviceToHost));
@@ -1476,6 +1459,7 @@ extern "C" int hg_run_staged(hg_ctx_t* c)
 extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int64_t* launches, int64_t* cells)
 {
     if (!c) return fail(HG_ERR_ARG, "hg_last_timing: null context");
+    cudaSetDevice(c->ix->device);
     HG_CUDA(cudaStreamSynchronize(c->st));
     float tot = c->last_total_ms;
     if (!c->timing && c->run_recorded) HG_CUDA(cudaEventElapsedTime(&tot, c->run_ev[0], c->run_ev[1]));
@@ -1493,6 +1477,7 @@ extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int
 extern "C" int hg_ctx_work(hg_ctx_t* c, int64_t* counts, int n)
 {
     if (!c || !counts || n < 0) return fail(HG_ERR_ARG, "hg_ctx_work: bad arguments");
+    cudaSetDevice(c->ix->device);
     HG_CUDA(cudaStreamSynchronize(c->st));
     unsigned long long v[4] = {0, 0, 0, 0};
     HG_CUDA(cudaMemcpy(v, c->work.p, sizeof(v), cudaMemcpyDeviceToHost));
@@ -1503,6 +1488,7 @@ extern "C" int hg_ctx_work(hg_ctx_t* c, int64_t* counts, int n)
 extern "C" int hg_staged_flags(hg_ctx_t* c, uint32_t* flags)
 {
     if (!c || !flags) return fail(HG_ERR_ARG, "hg_staged_flags: bad arguments");
+    cudaSetDevice(c->ix->device);
     HG_CUDA(cudaStreamSynchronize(c->st));
     HG_CUDA(cudaMemcpy(flags, c->run_flags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
     return HG_OK;
@@ -1512,6 +1498,7 @@ extern "C" int hg_fetch_staged(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, 
                                uint8_t* rows, int64_t row_stride, uint32_t* status)
 {
     if (!c || !c->staged) return fail(HG_ERR_ARG, "hg_fetch_staged: nothing staged");
+    cudaSetDevice(c->ix->device);
     if (c->staged_plan.size() != 1)
         return fail(HG_ERR_ARG, "hg_fetch_staged: staged batch spans several sub-batches; fetch needs one");
     const SubPlan& sp = c->staged_plan[0];
@@ -1586,6 +1573,7 @@ extern "C" int hg_submit(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff
 extern "C" int hg_poll(hg_ctx_t* c)
 {
     if (!c || c->async_n < 0) return -HG_ERR_ARG;
+    cudaSetDevice(c->ix->device);
     const cudaError_t e = cudaEventQuery(c->done_ev);
     if (e == cudaSuccess) return 1;
     if (e == cudaErrorNotReady) return 0;
@@ -1597,6 +1585,7 @@ extern "C" int hg_collect(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64
                           uint32_t* status)
 {
     if (!c || c->async_n < 0) return fail(HG_ERR_ARG, "hg_collect: nothing submitted");
+    cudaSetDevice(c->ix->device);
     HG_CUDA(cudaEventSynchronize(c->done_ev));
     const int64_t n = c->async_n, M = c->max_n + 1;
     const int64_t* off = c->h_i64 + 4 * M;
@@ -1619,77 +1608,6 @@ extern "C" int hg_collect(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64
 }
 
 // ---------------------------------------------------------- single calls
-
-extern "C" int64_t hg_extract_minimizer(const char* seq, int64_t len, int k, int w, int non_canonical, uint64_t* xs,
-                                        uint64_t* ys, int64_t cap, int64_t* needed)
-{
-    if (!seq && len > 0) return -fail(HG_ERR_ARG, "hg_extract_minimizer: null sequence");
-    if (hg_device_count() <= 0) return -fail(HG_ERR_CUDA, "hg_extract_minimizer: no CUDA device");
-    cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
-        return -fail(HG_ERR_CUDA, "hg_extract_minimizer: stream");
-    std::vector<uint64_t> x, y;
-    const int r = run_extract(k, w, non_canonical, seq, len, x, y, st);
-    cudaStreamDestroy(st);
-    if (r) return -r;
-    const int64_t m = (int64_t)x.size();
-    if (needed) *needed = m;
-    if (m > cap) return -fail(HG_ERR_CAPACITY, "hg_extract_minimizer: output capacity");
-    std::copy(x.begin(), x.end(), xs);
-    std::copy(y.begin(), y.end(), ys);
-    return m;
-}
-
-extern "C" int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* target, int8_t m,
-                                const int8_t* mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag,
-                                int32_t* ez_out, uint32_t* cigar, int64_t cap)
-{
-    if (!(flag & hg::kEzGenericSc)) return -fail(HG_ERR_ARG, "hg_ksw_extz2: only KSW_EZ_GENERIC_SC scoring is supported");
-    if (!ez_out || (qlen > 0 && !query) || (tlen > 0 && !target) || !mat || m <= 0 || m > 16)
-        return -fail(HG_ERR_ARG, "hg_ksw_extz2: bad arguments");
-    if (hg_device_count() <= 0) return -fail(HG_ERR_CUDA, "hg_ksw_extz2: no CUDA device");
-    for (int i = 0; i < qlen; ++i)
-        if (query[i] >= m) return -fail(HG_ERR_ARG, "hg_ksw_extz2: query symbol >= m");
-    for (int i = 0; i < tlen; ++i)
-        if (target[i] >= m) return -fail(HG_ERR_ARG, "hg_ksw_extz2: target symbol >= m");
-    const int32_t init[10] = {0, 0, -1, -1, hg::kNegInf, -1, hg::kNegInf, -1, hg::kNegInf, 0};
-    if (qlen <= 0 || tlen <= 0) {
-        std::copy(init, init + 10, ez_out);
-        return 0;
-    }
-    const size_t scratch = hg_ksw_scratch_bytes(qlen, tlen, w, flag);
-    const int ccap = qlen + tlen + 4;
-    DevBuf<uint8_t> d_q, d_t, d_s;
-    DevBuf<int8_t> d_m;
-    DevBuf<uint32_t> d_c;
-    DevBuf<int32_t> d_r;
-    cudaStream_t st;
-    HG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    struct Guard {
-        cudaStream_t s;
-        ~Guard() { cudaStreamDestroy(s); }
-    } guard{st};
-    HG_CUDA(d_q.alloc(qlen));
-    HG_CUDA(d_t.alloc(tlen));
-    HG_CUDA(d_s.alloc(scratch + 256));
-    HG_CUDA(d_m.alloc((size_t)m * m));
-    HG_CUDA(d_c.alloc(ccap));
-    HG_CUDA(d_r.alloc(16));
-    HG_CUDA(cudaMemcpyAsync(d_q.p, query, qlen, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(d_t.p, target, tlen, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(d_m.p, mat, (size_t)m * m, cudaMemcpyHostToDevice, st));
-    HG_CUDA(hg_launch_ksw_single(qlen, d_q.p, tlen, d_t.p, m, d_m.p, q, e, w, zdrop, end_bonus, flag, d_s.p, d_c.p,
-                                 ccap, d_r.p, st));
-    int32_t res[11];
-    HG_CUDA(cudaMemcpyAsync(res, d_r.p, sizeof(res), cudaMemcpyDeviceToHost, st));
-    HG_CUDA(cudaStreamSynchronize(st));
-    std::copy(res, res + 10, ez_out);
-    const int nc = res[10];
-    if (nc > ccap) return -fail(HG_ERR_CAPACITY, "hg_ksw_extz2: internal CIGAR overflow");
-    if (nc > cap) return -fail(HG_ERR_CAPACITY, "hg_ksw_extz2: CIGAR capacity");
-    if (nc) HG_CUDA(cudaMemcpy(cigar, d_c.p, 4 * (size_t)nc, cudaMemcpyDeviceToHost));
-    return nc;
-}
 
 extern "C" int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int flag,
                                         uint32_t* cigar, int64_t cap)
@@ -1717,6 +1635,22 @@ extern "C" int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const cha
     int32_t ez[10];
     return hg_ksw_extz2((int)qlen, qe.data(), (int)rlen, re.data(), 5, mat, 6, 2, w, -1, 0,
                         flag < 0 ? (hg::kEzGenericSc | hg::kEzRight) : flag, ez, cigar, cap);
+}
+
+extern "C" int64_t hg_extend_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int zdrop,
+                                        uint32_t* cigar, int64_t cap)
+{  // extendAlignKSW2 (src/align/align.cpp:68-107)
+    if (rlen < 0 || qlen < 0 || (rlen > 0 && !ref) || (qlen > 0 && !qry))
+        return -fail(HG_ERR_ARG, "hg_extend_align_ksw2: bad arguments");
+    if (rlen == 0 || qlen == 0) return 0;  // ksw_extz2_sse returns an empty result
+    std::vector<uint8_t> re((size_t)rlen), qe((size_t)qlen);
+    for (int64_t i = 0; i < rlen; ++i) re[i] = hg::dna5_of((uint8_t)ref[i]);
+    for (int64_t i = 0; i < qlen; ++i) qe[i] = hg::dna5_of((uint8_t)qry[i]);
+    static const int8_t mat[25] = {5, -4, -4, -4, 0, -4, 5, -4, -4, 0, -4, -4, 5, -4, 0,
+                                   -4, -4, -4, 5, 0, 0, 0, 0, 0, 0};
+    int32_t ez[10];
+    return hg_ksw_extz2((int)qlen, qe.data(), (int)rlen, re.data(), 5, mat, 6, 2, hg::auto_band((int)rlen, (int)qlen),
+                        zdrop, 50, hg::kEzExtzOnly | hg::kEzRight | hg::kEzApproxDrop, ez, cigar, cap);
 }
 
 // align::globalAlignMM2 with the caller's anchors against the index's center

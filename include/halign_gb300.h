@@ -53,6 +53,15 @@ const char* hg_last_error(void);
 void hg_default_params(hg_params_t* p);
 /* Number of visible CUDA devices (0 without a GPU); never fails. */
 int hg_device_count(void);
+/* Make device `ordinal` current for the calling thread: hg_index_create then
+ * places the index (and every context made from it) there, and every later
+ * call on that index or its contexts switches to it first.  One process per
+ * GPU calls this with its local rank before creating an index.  No reference
+ * counterpart (the reference runs on the host). */
+int hg_set_device(int ordinal);
+/* The device an index lives on: its ordinal and (when pci_bus_id is given)
+ * its PCI bus id string, e.g. "0000:1B:00.0" (len >= 13). */
+int hg_index_device(const hg_index_t* ix, int* ordinal, char* pci_bus_id, int len);
 
 /* ---- resident center index --------------------------------------------
  * Replaces the per-center set-up of RefAligner (src/align/ref_aligner.cpp:
@@ -160,6 +169,18 @@ int hg_poll(hg_ctx_t* ctx);
 int hg_collect(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
                uint32_t* status);
 
+/* Stage outputs of one query of the last hg_run_staged (the staged batch
+ * must fit one sub-batch): its anchors as the chain stage saw them - the
+ * collect_anchors output (src/seed/minimizer.cpp:220-356) in chainAnchors'
+ * sorted order (src/seed/anchor.cpp:343-349), as center / query positions -
+ * the chain DP arrays f and p over those anchors (p[i] = -1: no
+ * predecessor) and the best chain (chain_end: its last anchor, -1 if none;
+ * n_chain: its length after the min_score / min_cnt checks, 0 = rejected).
+ * *n_anchors is always set; arrays are written when cap >= *n_anchors.
+ * A test and debugging view of the batch kernels; no reference counterpart. */
+int hg_fetch_chain(hg_ctx_t* ctx, int64_t query, uint32_t* pos_ref, uint32_t* pos_qry, int32_t* f, int32_t* p,
+                   int64_t cap, int64_t* n_anchors, int64_t* chain_end, int64_t* n_chain);
+
 /* Consensus counters: counts7 = L x {A,C,G,T,U,N,-} (consensus::SiteCount,
  * include/consensus.h:78-99), ins = L+1 insertion events (slot c: I before
  * center column c).  reset != 0 clears them after reading. */
@@ -174,9 +195,15 @@ int hg_counters(hg_ctx_t* ctx, uint32_t* counts7, uint32_t* ins, int reset);
 int64_t hg_extract_minimizer(const char* seq, int64_t len, int k, int w, int non_canonical, uint64_t* xs,
                              uint64_t* ys, int64_t cap, int64_t* needed);
 
-/* ksw_extz2_sse (include/ksw2.h:64-65) with KSW_EZ_GENERIC_SC scoring.
+/* ksw_extz2_sse (include/ksw2.h:64-65): the full m x m matrix with
+ * KSW_EZ_GENERIC_SC, otherwise match (mat[0]) / mismatch (mat[1]) scoring
+ * with symbol m-1 as the wildcard, as the reference's SSE2 kernel.
  * ez_out: {max, zdropped, max_q, max_t, mqe, mqe_t, mte, mte_q, score,
- * reach_end}; returns the CIGAR length or a negative HG_ERR_*. */
+ * reach_end}; returns the CIGAR length or a negative HG_ERR_*.  Single calls
+ * (this one, hg_extract_minimizer, hg_collect_anchors, hg_chain_anchors,
+ * hg_project_row, hg_count_rows) run on a per-thread, per-device stream and
+ * grow-only scratch, so repeated calls allocate nothing once the scratch has
+ * grown to the largest call; each host thread may call them concurrently. */
 int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* target, int8_t m, const int8_t* mat,
                      int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag, int32_t* ez_out, uint32_t* cigar,
                      int64_t cap);
@@ -189,7 +216,10 @@ int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
  * synchronisation of cudaFree.  Inputs and outputs are DEVICE pointers owned
  * by the caller: d_query/d_target (codes < m), d_mat (m*m), d_ez (11 int32:
  * the ez fields of hg_ksw_extz2 followed by the CIGAR length) and d_cigar
- * (cap entries; a length above cap means the CIGAR did not fit).  The call
+ * (cap entries; a length above cap means the CIGAR did not fit, and nothing
+ * is written past cap).  The sequences live on the device, so the host cannot
+ * check them: the kernel does, and a code >= m makes the call compute nothing
+ * and write -1 as the CIGAR length (d_ez[10]).  The call
  * only enqueues one kernel on `stream` (NULL = default stream) and allocates
  * nothing; the DP scratch is one HG_NOALLOC_SCRATCH_BYTES array per GPU,
  * held until the process exits.  A call whose scratch need exceeds it returns
@@ -197,16 +227,94 @@ int64_t hg_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
  * All calls on a GPU share that array: calls that may overlap on the GPU
  * race and must be serialised.  The first call on a device looks up the
  * array's address with that device current; make it before any stream
- * capture.  Only KSW_EZ_GENERIC_SC scoring. */
+ * capture.  That address is kept per device ordinal for the primary context:
+ * it does not carry over to another driver context or past cudaDeviceReset. */
 #define HG_NOALLOC_SCRATCH_BYTES (1u << 20)
 int hg_ksw_extz2_noalloc(int qlen, const uint8_t* d_query, int tlen, const uint8_t* d_target, int8_t m,
                          const int8_t* d_mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag,
                          int32_t* d_ez, uint32_t* d_cigar, int64_t cap, void* stream, char* err, int64_t err_cap);
 
+/* anchor::Anchor (include/anchor.h:39-50) as a C record (32 bytes; is_rev
+ * is 0 or 1). */
+typedef struct {
+    uint64_t hash;
+    uint32_t rid_ref, pos_ref, rid_qry, pos_qry, span;
+    uint32_t is_rev;
+} hg_anchor_t;
+
+/* Reference-side half of minimizer::collect_anchors (src/seed/minimizer.cpp:
+ * 238-272) for any hit list (several sequences, both strands): the hits
+ * sorted by (hash, rid, pos, strand), grouped by hash, the -f/-U occurrence
+ * threshold from params (f_top_frac, u_floor, u_ceil; NULL = defaults) and a
+ * hash table, built once and kept on the current device.  The reference
+ * rebuilds this on every call; a caller keeps the handle while its reference
+ * hits stay the same.  Hits of equal sort key keep their input order (the
+ * reference's std::sort leaves that order unspecified). */
+typedef struct hg_hits hg_hits_t;
+int hg_hits_create(const uint64_t* ref_x, const uint64_t* ref_y, int64_t n, const hg_params_t* params,
+                   hg_hits_t** out);
+void hg_hits_destroy(hg_hits_t* h);
+
+/* anchor::compute_ref_occ_threshold and compute_occ_cutoff_top_frac
+ * (src/seed/anchor.cpp:73-117) over n per-hash occurrence counts with
+ * params' f_top_frac, u_floor, u_ceil (NULL = defaults): returns the
+ * threshold; *cutoff_top_frac (may be NULL) gets the -f cutoff alone
+ * (UINT64_MAX when nothing is skipped).  Host arithmetic of the index
+ * set-up; it never fails. */
+uint64_t hg_occ_threshold(const uint64_t* occs, int64_t n, const hg_params_t* params, uint64_t* cutoff_top_frac);
+
+/* minimizer::collect_anchors (src/seed/minimizer.cpp:220-356) against a
+ * hits handle, on the GPU: the --q-occ-frac and -e filters (params'
+ * q_occ_frac, sample_every_bp; NULL = defaults), then one anchor per kept
+ * query hit and reference occurrence, in the reference's order (query-hit
+ * order, occurrences in sorted order).  Returns the anchor count, or a
+ * negative HG_ERR_*; -HG_ERR_CAPACITY when cap is below the count, which is
+ * then in *needed. */
+int64_t hg_collect_anchors(const hg_hits_t* h, const uint64_t* qry_x, const uint64_t* qry_y, int64_t n_qry,
+                           const hg_params_t* params, hg_anchor_t* out, int64_t cap, int64_t* needed);
+
+/* anchor::chainAnchors (src/seed/anchor.cpp:332-461) with chainScoreSimple
+ * (:254-301), on the GPU: anchors[] is sorted in place by (rid_ref, is_rev,
+ * pos_ref, pos_qry) as the reference sorts it (equal keys keep their input
+ * order), the DP runs with params' chain fields (NULL = defaults) and chain[]
+ * gets the best chain as ascending indices into the sorted anchors.  Returns
+ * the chain length (0: no chain passes min_score / min_cnt) or a negative
+ * HG_ERR_*; -HG_ERR_CAPACITY when cap is below the length.  f and p (each n
+ * entries, may be NULL) get the DP arrays of the sorted anchors.  rid_ref
+ * must be below 2^31 (MinimizerHit's rid field). */
+int64_t hg_chain_anchors(hg_anchor_t* anchors, int64_t n, const hg_params_t* params, int64_t* chain, int64_t cap,
+                         int32_t* f, int64_t* p);
+
+/* cigar::delQueryToRefByCigar (pad == 0; src/align/cigar.cpp:212-299) and
+ * cigar::padQueryToRefByCigar (pad != 0; :150-209) on the GPU: the query
+ * projected onto the reference by its CIGAR.  An empty CIGAR leaves the query
+ * as it is.  Returns the row length or a negative HG_ERR_*: HG_ERR_ARG when
+ * the CIGAR does not consume exactly qlen query bases (the reference asserts)
+ * or holds an op code above 8 (intToCigar throws), HG_ERR_CAPACITY when cap
+ * is below the row length. */
+int64_t hg_project_row(const char* qry, int64_t qlen, const uint32_t* cigar, int64_t n_cigar, int pad, char* out,
+                       int64_t cap);
+
+/* SiteCount accumulation (consensus::processBatchParallelWithLocals,
+ * src/consensus/consensus.cpp:304-411) of n_rows aligned rows of L columns
+ * (row i at rows + i * row_stride) on the GPU, with k_base_map's classes
+ * (include/consensus.h:126-145).  counts7 is L x {A,C,G,T,U,N,-} uint32;
+ * accumulate != 0 adds to its values, else it is overwritten. */
+int hg_count_rows(const char* rows, int64_t n_rows, int64_t L, int64_t row_stride, uint32_t* counts7,
+                  int accumulate);
+
 /* align::globalAlignKSW2 (src/align/align.cpp:22-65); flag < 0 selects the
  * default KSW_EZ_GENERIC_SC|KSW_EZ_RIGHT. */
 int64_t hg_global_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int flag, uint32_t* cigar,
                              int64_t cap);
+
+/* align::extendAlignKSW2 (src/align/align.cpp:68-107): DNA5 codes, the
+ * default matrix and gaps, match/mismatch scoring with N the wildcard (no
+ * KSW_EZ_GENERIC_SC), KSW_EZ_EXTZ_ONLY | RIGHT | APPROX_DROP, end bonus 50,
+ * the caller's z-drop, auto_band.  Returns the CIGAR length (0 for an empty
+ * sequence) or a negative HG_ERR_*. */
+int64_t hg_extend_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int zdrop,
+                             uint32_t* cigar, int64_t cap);
 
 /* align::globalAlignMM2 (src/align/align.cpp:189-305, include/align.h) with
  * the caller's anchors (anchor::Anchor pos_ref / pos_qry, include/anchor.h:

@@ -481,6 +481,12 @@ static void anchor_merge_sort(ho_anchor* a, ho_anchor* tmp, int64_t n)
  * best with strict '>', backtrack, min_score / min_cnt rejection. */
 int64_t ho_chain_anchors(ho_anchor* a, int64_t n, const ho_chain_params* p_in, ho_anchor* out, int64_t cap)
 {
+    return ho_chain_anchors_fp(a, n, p_in, out, cap, 0, 0);
+}
+
+int64_t ho_chain_anchors_fp(ho_anchor* a, int64_t n, const ho_chain_params* p_in, ho_anchor* out, int64_t cap,
+                            int32_t* f_out, int64_t* p_out)
+{
     if (n == 0) return 0;
     ho_chain_params p;
     if (p_in) p = *p_in;
@@ -524,6 +530,8 @@ int64_t ho_chain_anchors(ho_anchor* a, int64_t n, const ho_chain_params* p_in, h
         pr[i] = max_j;
         if (max_f > best_f) best_f = max_f, best = i;
     }
+    if (f_out) memcpy(f_out, f, sizeof(int32_t) * (size_t)n);
+    if (p_out) memcpy(p_out, pr, sizeof(int64_t) * (size_t)n);
     int64_t m = 0;
     if (!(best_f < p.min_score || best < 0)) {
         int64_t len = 0;
@@ -625,7 +633,6 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
     ez->max = 0, ez->score = ez->mqe = ez->mte = KSW_NEG_INF;
     ez->zdropped = 0, ez->reach_end = 0;
     if (m <= 0 || qlen <= 0 || tlen <= 0) return 0;
-    if (!(flag & EZ_GENERIC_SC)) return -0x7fffffff; /* not restated */
     const uint8_t qe2 = (uint8_t)((q + e) * 2);
     const uint8_t max_sc = (uint8_t)(mat[0] + (q + e) * 2);
     if (w < 0) w = tlen > qlen ? tlen : qlen;
@@ -674,7 +681,27 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
         } else
             x1 = 0, v1 = (uint8_t)(r ? q : 0);
         if (en >= r) y[r] = 0, u[r] = (uint8_t)(r ? q : 0);
-        for (int t = st0; t <= en0; ++t) s[t] = (uint8_t)mat[target[t] * m + query[r - t]];
+        if (flag & EZ_GENERIC_SC) {
+            for (int t = st0; t <= en0; ++t) s[t] = (uint8_t)mat[target[t] * m + query[r - t]];
+        } else {
+            /* Match/mismatch scoring, symbol m-1 the wildcard (ksw2_extz2_sse.c:
+             * 123-137): 16-byte blocks from st0, so up to 15 lanes past en0 are
+             * scored from the reference's buffers - the zero-padded target copy
+             * (sf, L bytes) and, past it, the reversed query qr (zeros past
+             * qlen).  Lanes at or past L are never computed; not stored. */
+            const int scn = mat[m * m - 1] == 0 ? -e : mat[m * m - 1];
+            int tend = st0 + ((en0 - st0) / 16 + 1) * 16 - 1;
+            if (tend > (int)L - 1) tend = (int)L - 1;
+            for (int t = st0; t <= tend; ++t) {
+                const int kr = t - (int)L;
+                const int sq = t < tlen ? target[t] : t < (int)L ? 0 : (kr < qlen ? query[qlen - 1 - kr] : 0);
+                const int kq = qlen - 1 - r + t;
+                const int sr = kq < qlen ? query[qlen - 1 - kq] : 0;
+                int sc = sq == sr ? mat[0] : mat[1];
+                if (sq == m - 1 || sr == m - 1) sc = scn;
+                s[t] = (uint8_t)sc;
+            }
+        }
         uint8_t* pr = with_cigar ? p + (size_t)r * ncol : 0;
         if (with_cigar) off[r] = st, off_end[r] = en;
         /* The SIMD code seeds the first block's shifted-in byte with

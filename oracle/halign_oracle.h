@@ -71,10 +71,15 @@ uint64_t ho_ref_occ_threshold(const uint64_t* occs, int64_t n, const ho_filter_p
 int32_t ho_chain_score(const ho_anchor* ai, const ho_anchor* aj, const ho_chain_params* p);
 /* A4: anchor::chainAnchors (src/seed/anchor.cpp:332-461). Sorts a[] in place. */
 int64_t ho_chain_anchors(ho_anchor* a, int64_t n, const ho_chain_params* p, ho_anchor* out, int64_t cap);
+/* The same, also returning the DP arrays of the sorted anchors: f (best chain
+ * score ending at each anchor) and p (its predecessor, -1 if none). */
+int64_t ho_chain_anchors_fp(ho_anchor* a, int64_t n, const ho_chain_params* p, ho_anchor* out, int64_t cap,
+                            int32_t* f_out, int64_t* p_out);
 
 /* A7+A8: ksw_extz2_sse (src/align/ksw2_extz2_sse.c:23-304, SSE2 build) with
- * ksw_backtrack (include/ksw2.h:129-161). Only KSW_EZ_GENERIC_SC scoring is
- * restated. Returns the CIGAR length (or -len when cap is too small). */
+ * ksw_backtrack (include/ksw2.h:129-161), with the full matrix
+ * (KSW_EZ_GENERIC_SC) or match/mismatch scoring (extendAlignKSW2's).
+ * Returns the CIGAR length (or -len when cap is too small). */
 int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* target, int8_t m,
                      const int8_t* mat, int8_t q, int8_t e, int w, int zdrop, int end_bonus, int flag,
                      ho_extz* ez, uint32_t* cigar, int64_t cap);

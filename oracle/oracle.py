@@ -54,6 +54,8 @@ class Oracle(_Common):
         L.ho_collect_anchors.restype = i64
         L.ho_chain_anchors.argtypes = [vp, i64, vp, vp, i64]
         L.ho_chain_anchors.restype = i64
+        L.ho_chain_anchors_fp.argtypes = [vp, i64, vp, vp, i64, vp, vp]
+        L.ho_chain_anchors_fp.restype = i64
         L.ho_chain_score.argtypes = [vp, vp, vp]
         L.ho_chain_score.restype = C.c_int32
         L.ho_ksw_extz2.argtypes = [i32, vp, i32, vp, C.c_int8, vp, C.c_int8, C.c_int8, i32, i32, i32, i32, vp,
@@ -132,6 +134,18 @@ class Oracle(_Common):
         n = self.lib.ho_chain_anchors(_p(a), len(a), _p(prm) if prm is not None else None, _p(out), len(out))
         assert n >= 0
         return a, out[:n].copy()
+
+    def chain_anchors_fp(self, anchors, iparams=None, fparams=None):
+        """chainAnchors plus its DP arrays: (sorted anchors, chain, f, p)."""
+        a = np.ascontiguousarray(anchors, ANCHOR_DTYPE).copy()
+        out = np.zeros(max(1, len(a)), ANCHOR_DTYPE)
+        f = np.zeros(max(1, len(a)), np.int32)
+        pr = np.zeros(max(1, len(a)), np.int64)
+        prm = self._chain_params(iparams, fparams)
+        n = self.lib.ho_chain_anchors_fp(_p(a), len(a), _p(prm) if prm is not None else None, _p(out), len(out),
+                                         _p(f), _p(pr))
+        assert n >= 0
+        return a, out[:n].copy(), f[:len(a)].copy(), pr[:len(a)].copy()
 
     def chain_score(self, ai_ref, ai_qry, aj_ref, aj_qry, aj_span):
         a = np.zeros(2, ANCHOR_DTYPE)
@@ -260,6 +274,12 @@ class Reference(_Common):
         L.ref_auto_band.restype = i32
         L.ref_chain_score.argtypes = [C.c_uint32] * 5
         L.ref_chain_score.restype = C.c_int32
+        L.ref_pad_query.argtypes = [C.c_char_p, i64, vp, i64, vp, i64]
+        L.ref_pad_query.restype = i64
+        L.ref_extend_align_ksw2.argtypes = [C.c_char_p, i64, C.c_char_p, i64, i32, vp, i64]
+        L.ref_extend_align_ksw2.restype = i64
+        L.ref_generate_consensus.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint64, i64, vp, i64]
+        L.ref_generate_consensus.restype = i64
 
     @staticmethod
     def _split(a):
@@ -370,6 +390,31 @@ class Reference(_Common):
         cap = len(q) + int(sum(int(x) >> 4 for x in c)) + 1
         out = np.zeros(cap, np.uint8)
         n = self.lib.ref_del_query(q, len(q), _p(c), len(c), _p(out), cap)
+        assert n >= 0
+        return out[:n].tobytes()
+
+    def pad_query(self, qry, cigar):
+        q = _bytes(qry)
+        c = np.ascontiguousarray(cigar, np.uint32)
+        cap = len(q) + int(sum(int(x) >> 4 for x in c)) + 1
+        out = np.zeros(cap, np.uint8)
+        n = self.lib.ref_pad_query(q, len(q), _p(c), len(c), _p(out), cap)
+        assert n >= 0
+        return out[:n].tobytes()
+
+    def extend_align_ksw2(self, ref, qry, zdrop=200):
+        r, q = _bytes(ref), _bytes(qry)
+        cap = len(r) + len(q) + 4
+        c = np.zeros(cap, np.uint32)
+        n = self.lib.ref_extend_align_ksw2(r, len(r), q, len(q), zdrop, _p(c), cap)
+        assert n >= 0
+        return c[:n].copy()
+
+    def generate_consensus(self, aligned_fasta, out_fasta, out_json, seq_limit=0, batch_size=4096):
+        cap = 1 << 24
+        out = np.zeros(cap, np.uint8)
+        n = self.lib.ref_generate_consensus(str(aligned_fasta).encode(), str(out_fasta).encode(),
+                                            str(out_json).encode(), seq_limit, batch_size, _p(out), cap)
         assert n >= 0
         return out[:n].tobytes()
 

@@ -285,6 +285,37 @@ int64_t ref_del_query(const char* qry, int64_t qlen, const uint32_t* cigar, int6
     return m;
 }
 
+// padQueryToRefByCigar (insertions kept, D -> '-').
+int64_t ref_pad_query(const char* qry, int64_t qlen, const uint32_t* cigar, int64_t n_cigar, char* out, int64_t cap)
+{
+    std::string q(qry, qlen);
+    cigar::padQueryToRefByCigar(q, cigar::Cigar_t(cigar, cigar + n_cigar));
+    const int64_t m = static_cast<int64_t>(q.size());
+    if (m > cap) return -m;
+    std::memcpy(out, q.data(), static_cast<size_t>(m));
+    return m;
+}
+
+int64_t ref_extend_align_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t qlen, int zdrop,
+                              uint32_t* cigar, int64_t cap)
+{
+    const auto c = align::extendAlignKSW2(std::string(ref, rlen), std::string(qry, qlen), zdrop);
+    return store_cigar(c, cigar, cap);
+}
+
+// generateConsensusSequence on an aligned FASTA; the consensus goes to out
+// (capacity cap), the files to out_fasta / out_json.  Returns its length.
+int64_t ref_generate_consensus(const char* aligned_fasta, const char* out_fasta, const char* out_json,
+                               uint64_t seq_limit, int64_t batch_size, char* out, int64_t cap)
+{
+    const std::string s = consensus::generateConsensusSequence(aligned_fasta, out_fasta, out_json, seq_limit, 1,
+                                                               static_cast<size_t>(batch_size));
+    const int64_t m = static_cast<int64_t>(s.size());
+    if (m > cap) return -m;
+    std::memcpy(out, s.data(), static_cast<size_t>(m));
+    return m;
+}
+
 int64_t ref_cigar_to_string(const uint32_t* cigar, int64_t n, char* out, int64_t cap)
 {
     const auto s = cigar::cigarToString(cigar::Cigar_t(cigar, cigar + n));

@@ -118,11 +118,12 @@ def test_bad_arguments_rejected_on_host(pkg, native):
     assert L.hg_index_create(b"ACGT", 4, 15, 300, None, C.byref(h)) == 2
     assert L.hg_ctx_create(None, 1, 1, C.byref(h)) == 2
     ez = np.zeros(10, np.int32)
-    # non-generic scoring is refused before any device work
-    r = L.hg_ksw_extz2(4, np.zeros(4, np.uint8).ctypes.data, 4, np.zeros(4, np.uint8).ctypes.data, 5,
+    # a symbol outside the alphabet is refused before any device work
+    bad = np.array([0, 1, 7, 2], np.uint8)
+    r = L.hg_ksw_extz2(4, bad.ctypes.data, 4, np.zeros(4, np.uint8).ctypes.data, 5,
                        np.zeros(25, np.int8).ctypes.data, 6, 2, -1, -1, 0, 0x02, ez.ctypes.data, None, 0)
     assert r == -2
-    assert b"GENERIC_SC" in L.hg_last_error()
+    assert b"symbol >= m" in L.hg_last_error()
 
 
 def test_auto_band_matches_oracle(oracle):

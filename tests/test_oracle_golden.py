@@ -181,3 +181,19 @@ def test_consensus_known_answers(oracle):
     assert pick([b"ACGTACGT"]) == "ACGTACGT"
     assert pick([b"U", b"U", b"A"]) == "U"
     assert pick([b"C", b"C", b"a"]) == "C" and pick([b"N", b"n", b"A"]) == "A"
+
+
+def test_oracle_extz2_match_mismatch_golden(oracle, golden):
+    """extz2 without KSW_EZ_GENERIC_SC (extendAlignKSW2's scoring) against the
+    reference's own outputs: the 16-byte score blocks reach past the band end
+    into the target copy's padding and the reversed query."""
+    z = golden.load("ksw_extz2_ng.npz")
+    bad = []
+    for i in range(len(z["params"])):
+        w, zdrop, eb, flag = (int(x) for x in z["params"][i])
+        q = z["q"][z["q_off"][i]:z["q_off"][i + 1]]
+        t = z["t"][z["t_off"][i]:z["t_off"][i + 1]]
+        ez, cig = oracle.ksw_extz2(q, t, 5, MAT, 6, 2, w, zdrop, eb, flag)
+        if not (np.array_equal(ez, z["ez"][i]) and np.array_equal(cig, z["cigar"][z["cigar_off"][i]:z["cigar_off"][i + 1]])):
+            bad.append(i)
+    assert not bad, f"{len(bad)} of {len(z['params'])} differ, first {bad[:5]}"
