@@ -1,8 +1,11 @@
-"""Build the GB300 library ``_build/libhalign_gb300.so`` from ``csrc/``.
+"""Build the GB300 libraries.
 
-nvcc compiles every translation unit for sm_103a only (one -gencode, in
-parallel) and links one shared library exporting the C ABI of
-include/halign_gb300.h and the C++ drop-in surface of include/*.h.
+* ``_build/libhalign_gb300.so`` from ``csrc/``: nvcc compiles every
+  translation unit for sm_103a only (one -gencode, in parallel) and links one
+  shared library exporting the C ABI of include/halign_gb300.h.
+* ``_build/libhalign4_dropin.so`` from ``dropin/hg_shim.cpp``: g++ builds
+  HAlign-4's C++ call surface (include/halign4/*.h) over that C ABI; it
+  links libhalign_gb300.so and finds it next to itself.
 """
 from __future__ import annotations
 
@@ -16,6 +19,9 @@ ROOT = HERE.parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = BUILD / "libhalign_gb300.so"
+DROPIN = BUILD / "libhalign4_dropin.so"
+DROPIN_SRC = HERE / "dropin" / "hg_shim.cpp"
+CXX = os.environ.get("CXX", "g++")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3", "-Xcompiler", "-fopenmp",
@@ -27,7 +33,7 @@ def _sources():
 
 
 def _headers():
-    return sorted(CSRC.glob("*.cuh")) + sorted((ROOT / "include").glob("*.h"))
+    return sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) + sorted((ROOT / "include").glob("*.h"))
 
 
 def _run(cmd):
@@ -56,7 +62,17 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     objs = [str(BUILD / (s.stem + ".o")) for s in srcs]
     if jobs or not LIB.exists():
         _run([NVCC, *ARCH, "-shared", "-o", str(LIB), *objs, "-lcudart", "-lgomp"])
+    build_dropin(force)
     return LIB
+
+
+def build_dropin(force: bool = False) -> Path:
+    """The C++ drop-in library over the C ABI (host code only)."""
+    deps = [DROPIN_SRC, LIB, *sorted((ROOT / "include" / "halign4").glob("*.h")), ROOT / "include" / "halign_gb300.h"]
+    if force or not DROPIN.exists() or DROPIN.stat().st_mtime < max(p.stat().st_mtime for p in deps):
+        _run([CXX, "-std=c++17", "-O2", "-fPIC", "-shared", "-Wall", f"-I{ROOT / 'include'}", str(DROPIN_SRC),
+              "-o", str(DROPIN), f"-L{BUILD}", "-lhalign_gb300", "-Wl,-rpath,$ORIGIN"])
+    return DROPIN
 
 
 if __name__ == "__main__":

@@ -90,6 +90,147 @@ def stages(R: Reference, w, idx):
     np.savez_compressed(OUT / "mito_stages.npz", **rec)
 
 
+def ksw_nongeneric_vectors(R: Reference, n=400, seed=12):
+    """extz2 without KSW_EZ_GENERIC_SC (match/mismatch scoring, symbol m-1 the
+    wildcard): the scoring extendAlignKSW2 uses."""
+    rng = np.random.default_rng(seed)
+    qs, ts, ezs, cigs, prm = [], [], [], [], []
+    for it in range(n):
+        ql = int(rng.integers(1, 200))
+        tl = int(rng.integers(1, 200))
+        q = rng.integers(0, 5 if it % 3 == 0 else 4, ql).astype(np.uint8)
+        if it % 2 == 0:
+            t = np.resize(q, tl).copy()
+            m = rng.random(tl) < 0.12
+            t[m] = rng.integers(0, 5, int(m.sum()))
+        else:
+            t = rng.integers(0, 4, tl).astype(np.uint8)
+        w = int(rng.choice([-1, 0, 1, 3, 5, 10, 17, 30, 200]))
+        flag = int(rng.choice([0x00, 0x02, 0x01, 0x40, 0x42, 0x52, 0x08, 0x82, 0x12]))
+        zdrop = int(rng.choice([-1, -1, 10, 50, 200]))
+        eb = int(rng.choice([0, 5, 50]))
+        ez, c = R.ksw_extz2(q, t, 5, MAT, 6, 2, w, zdrop, eb, flag)
+        qs.append(q), ts.append(t), ezs.append(ez), cigs.append(c), prm.append([w, zdrop, eb, flag])
+    qf, qo = ragged(qs, np.uint8)
+    tf, to = ragged(ts, np.uint8)
+    cf, co = ragged(cigs, np.uint32)
+    np.savez_compressed(OUT / "ksw_extz2_ng.npz", q=qf, q_off=qo, t=tf, t_off=to, cigar=cf, cigar_off=co,
+                        ez=np.array(ezs, np.int32), params=np.array(prm, np.int32))
+
+
+def _seq(rng, n, noisy=True):
+    s = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, n)].copy()
+    if noisy and n:
+        m = rng.random(n) < 0.02
+        s[m] = np.frombuffer(b"NacgtU", np.uint8)[rng.integers(0, 6, int(m.sum()))]
+    return s.tobytes()
+
+
+def _mutate(rng, src: bytes, p=0.02):
+    out = bytearray()
+    for c in src:
+        r = rng.random()
+        if r < p / 2:
+            continue
+        if r < p:
+            out += bytes([c]) + _seq(rng, int(rng.integers(1, 4)), False)
+            continue
+        out.append(c if rng.random() > p else b"ACGT"[int(rng.integers(0, 4))])
+    return bytes(out)
+
+
+def dropin_cases(R: Reference):
+    """Inputs and the reference's outputs of the C++ call surface
+    (include/halign4/*.h) for tests/dropin/test_dropin.cpp: one case per line,
+    space-separated fields, integer lists as a count followed by the values,
+    sequences as raw bytes.  The aligned FASTA and the consensus outputs of
+    generateConsensusSequence are written next to it."""
+    rng = np.random.default_rng(77)
+    L = []
+    arr = lambda v: " ".join([str(len(v))] + [str(int(x)) for x in v])  # noqa: E731
+
+    def anchors_line(a):
+        cols = [a[f] for f in ("hash", "rid_ref", "pos_ref", "rid_qry", "pos_qry", "span", "is_rev")]
+        return str(len(a)) + "".join(" " + " ".join(str(int(c[i])) for c in cols) for i in range(len(a)))
+
+    # extractMinimizer
+    for it in range(8):
+        s = _seq(rng, int(rng.integers(0, 3000)))
+        k, w = int(rng.choice([15, 11, 21, 31])), int(rng.choice([10, 40, 16]))
+        nc = int(it % 2 == 0)
+        x, y = R.extract_minimizer(s, k, w, bool(nc))
+        L.append(f"MZ {k} {w} {nc} {len(s)} {s.decode() if s else '-'} {arr(x)} {arr(y)}")
+    # collect_anchors + chainAnchors on hits with several ids and both strands
+    for it in range(5):
+        ref = _seq(rng, int(rng.integers(2000, 6000)), False)
+        qry = _mutate(rng, ref[int(rng.integers(0, 500)):])
+        rx, ry = R.extract_minimizer(ref, 15, 10, True)
+        qx, qy = R.extract_minimizer(qry, 15, 10, True)
+        if it % 2:  # a second reference id and reverse strands on part of the hits
+            ry = ry.copy()
+            flip = rng.random(len(ry)) < 0.3
+            ry[flip] ^= np.uint64(1) << np.uint64(63)
+            ry[rng.random(len(ry)) < 0.2] += np.uint64(1) << np.uint64(32)
+        fp = [float(rng.choice([2e-4, 0.05])), int(rng.choice([1, 10])), int(rng.choice([2, 1000000])),
+              float(rng.choice([0.01, 0.0, 0.002])), int(rng.choice([500, 0, 3]))]
+        a = R.collect_anchors(rx, ry, qx, qy, fp)
+        L.append(f"CA {' '.join(repr(v) for v in fp)} {arr(rx)} {arr(ry)} {arr(qx)} {arr(qy)} {anchors_line(a)}")
+        ip = [5000, 5000, int(rng.choice([500, 50])), int(rng.choice([25, 2])), int(rng.choice([5000, 30])),
+              int(rng.choice([3, 1])), int(rng.choice([40, 10]))]
+        fpp = [float(rng.choice([0.01, 0.05])), 0.01]
+        srt, ch = R.chain_anchors(a, ip, fpp)
+        L.append(f"CH {' '.join(map(str, ip))} {fpp[0]!r} {fpp[1]!r} {anchors_line(a)} {anchors_line(srt)} "
+                 f"{anchors_line(ch)}")
+        # globalAlignMM2 with these anchors (general shape) and with the
+        # align-to-center shape
+        c = R.global_align_mm2(ref, qry, a)
+        L.append(f"MM {ref.decode()} {qry.decode()} {anchors_line(a)} {arr(c)}")
+        a2 = R.collect_anchors(*R.extract_minimizer(ref), qx, qy)
+        c2 = R.global_align_mm2(ref, qry, a2)
+        L.append(f"MM {ref.decode()} {qry.decode()} {anchors_line(a2)} {arr(c2)}")
+        # projections of the query by that CIGAR
+        L.append(f"DQ {qry.decode()} {arr(c2)} {R.del_query(qry, c2).decode()}")
+        L.append(f"PQ {qry.decode()} {arr(c2)} {R.pad_query(qry, c2).decode()}")
+    # ksw_extz2_sse, generic and match/mismatch scoring
+    for it in range(60):
+        ql, tl = int(rng.integers(1, 300)), int(rng.integers(1, 300))
+        q = rng.integers(0, 5, ql).astype(np.uint8)
+        t = np.resize(q, tl).copy()
+        m = rng.random(tl) < 0.1
+        t[m] = rng.integers(0, 5, int(m.sum()))
+        w = int(rng.choice([-1, 5, 30, 120]))
+        flag = int(rng.choice([0x04, 0x06, 0x46, 0x00, 0x02, 0x52, 0x05]))
+        zdrop = int(rng.choice([-1, 40]))
+        eb = int(rng.choice([0, 50]))
+        ez, c = R.ksw_extz2(q, t, 5, MAT, 6, 2, w, zdrop, eb, flag)
+        L.append(f"KS {w} {zdrop} {eb} {flag} {arr(q)} {arr(t)} {arr(ez)} {arr(c)}")
+    # globalAlignKSW2 (default and caller flags) and extendAlignKSW2
+    for it in range(12):
+        ref = _seq(rng, int(rng.integers(0, 400)))
+        qry = _mutate(rng, ref) if it % 3 else _seq(rng, int(rng.integers(0, 300)))
+        flag = int(rng.choice([-1, 0x04, 0x06]))
+        c = R.global_align_ksw2(ref, qry, flag)
+        L.append(f"GK {flag} {ref.decode() or '-'} {qry.decode() or '-'} {arr(c)}")
+        if ref and qry:
+            zd = int(rng.choice([200, 20]))
+            L.append(f"EX {zd} {ref.decode()} {qry.decode()} {arr(R.extend_align_ksw2(ref, qry, zd))}")
+    # CIGAR strings
+    for it in range(6):
+        c = R.global_align_ksw2(_seq(rng, 200), _seq(rng, 180))
+        L.append(f"CS {arr(c)} {R.cigar_str(c)}")
+    (OUT / "dropin_cases.txt").write_text("\n".join(L) + "\n")
+    # generateConsensusSequence: batches of 3 (the reference skips one record
+    # between full batches) and a record limit
+    alpha = np.frombuffer(b"ACGTACGTACGTacgtUuNn-.XR", np.uint8)
+    with open(OUT / "dropin_aln.fa", "wb") as f:
+        for i in range(13):
+            row = alpha[rng.integers(0, len(alpha), 41)].tobytes()
+            f.write(b">r%d sample\n" % i + row[:25] + b"\n" + row[25:] + b"\n")
+    for tag, limit, bs in (("b3", 0, 3), ("l5", 5, 4096)):
+        R.generate_consensus(OUT / "dropin_aln.fa", OUT / f"dropin_cons_{tag}.fa", OUT / f"dropin_cons_{tag}.json",
+                             limit, bs)
+
+
 def cli_fasta_digest(w, threads=1):
     d = Path(tempfile.mkdtemp(prefix="halign_golden_"))
     try:
@@ -106,7 +247,13 @@ def cli_fasta_digest(w, threads=1):
 
 def main():
     R = Reference()
+    if sys.argv[1:] == ["--dropin"]:  # only the C++-surface fixtures
+        ksw_nongeneric_vectors(R)
+        dropin_cases(R)
+        return
     ksw_vectors(R)
+    ksw_nongeneric_vectors(R)
+    dropin_cases(R)
     mito = synth.mito(1000)
     workload_cigars(R, "mito", mito, np.arange(0, 1000, 10))
     stages(R, mito, [0, 1, 2])
