@@ -135,6 +135,9 @@ def lib() -> C.CDLL:
     L.hg_project_row.argtypes = [C.c_char_p, i64, vp, i64, i32, vp, i64]
     L.hg_project_row.restype = i64
     L.hg_count_rows.argtypes = [vp, i64, i64, i64, vp, i32]
+    L.hg_int_peaks.argtypes = [vp, i32]
+    L.hg_extend_align_ksw2.argtypes = [C.c_char_p, i64, C.c_char_p, i64, i32, vp, i64]
+    L.hg_extend_align_ksw2.restype = i64
     _lib = L
     return L
 
@@ -525,6 +528,28 @@ def project_row(qry, cigar, pad: bool = False) -> bytes:
     if n < 0:
         _check(-n)
     return out[:n].tobytes()
+
+
+INT_PEAK_KEYS = ("int32_add_max_ops", "dpx_s32_ops", "dpx_s16x2_ops", "dpx_max3_s16x2_ops", "mul64_ops",
+                 "issue_warp_inst")
+
+
+def int_peaks() -> dict:
+    """Measured integer / DPX throughput ceilings of the current GPU (per second)."""
+    v = np.zeros(len(INT_PEAK_KEYS), np.float64)
+    _check(lib().hg_int_peaks(_p(v), len(v)))
+    return dict(zip(INT_PEAK_KEYS, (float(x) for x in v)))
+
+
+def extend_align_ksw2(ref, qry, zdrop: int = 200) -> np.ndarray:
+    """align::extendAlignKSW2 on the GPU."""
+    r, q = _bytes(ref), _bytes(qry)
+    cap = len(r) + len(q) + 4
+    c = np.zeros(cap, np.uint32)
+    n = lib().hg_extend_align_ksw2(r, len(r), q, len(q), zdrop, _p(c), cap)
+    if n < 0:
+        _check(-n)
+    return c[:n].copy()
 
 
 def count_rows(rows: np.ndarray, counts: np.ndarray | None = None) -> np.ndarray:

@@ -154,6 +154,15 @@ int hg_ctx_work(hg_ctx_t* ctx, int64_t* counts, int n);
 /* OR of the HG_ST_* bits of every query of the last hg_run_staged
  * (0 = every query aligned completely). */
 int hg_staged_flags(hg_ctx_t* ctx, uint32_t* flags);
+/* Integer throughput ceilings of the current GPU, measured by short
+ * full-grid kernels (about 20 ms in all): out[0] int32 add + max element
+ * operations per second, out[1] DPX max(a + b, c) on int32, out[2] the same
+ * on int16x2, out[3] DPX three-way max on int16x2, out[4] 64-bit
+ * multiply-adds, out[5] warp instructions per second of out[0]'s kernel.
+ * n <= 6 values are written.  The roofline of this integer path; no
+ * reference counterpart. */
+int hg_int_peaks(double* out, int n);
+
 /* Enable per-stage event timing for staged runs (off by default). */
 int hg_set_timing(hg_ctx_t* ctx, int on);
 

@@ -282,6 +282,15 @@ static int hit_less(const hit_t* a, const hit_t* b)
 static void hit_merge_sort(hit_t* a, hit_t* tmp, int64_t n)
 {
     if (n < 2) return;
+    if (n <= 16) { /* insertion sort below 16 elements: stable as the merge */
+        for (int64_t i = 1; i < n; ++i) {
+            const hit_t k = a[i];
+            int64_t j = i - 1;
+            while (j >= 0 && hit_less(&k, &a[j])) a[j + 1] = a[j], --j;
+            a[j + 1] = k;
+        }
+        return;
+    }
     const int64_t h = n / 2;
     hit_merge_sort(a, tmp, h);
     hit_merge_sort(a + h, tmp, n - h);
@@ -617,6 +626,38 @@ static int apply_zdrop(ho_extz* ez, int32_t H, int r, int t, int zdrop, int8_t e
 
 static inline int8_t s8(uint8_t v) { return (int8_t)v; }
 
+/* 16 byte lanes with GCC vector extensions (SSE2 on x86-64, NEON on
+ * aarch64): the SSE2 kernel's operations - wrapping add/sub, unsigned
+ * max/min, signed greater-than as an all-ones mask - one block at a time. */
+typedef uint8_t u8x16 __attribute__((vector_size(16)));
+typedef uint8_t u8x4 __attribute__((vector_size(4)));
+typedef int32_t i32x4 __attribute__((vector_size(16)));
+typedef int8_t i8x16 __attribute__((vector_size(16)));
+
+static inline u8x16 v16_set(uint8_t c)
+{
+    const u8x16 zero = {0};
+    return zero + c; /* the scalar is broadcast to every lane */
+}
+static inline u8x16 v16_load(const uint8_t* p)
+{
+    u8x16 r;
+    memcpy(&r, p, 16);
+    return r;
+}
+static inline void v16_store(uint8_t* p, u8x16 v) { memcpy(p, &v, 16); }
+static inline u8x16 v16_gts(u8x16 a, u8x16 b) { return (u8x16)((i8x16)a > (i8x16)b); }
+static inline u8x16 v16_sel(u8x16 m, u8x16 a, u8x16 b) { return (m & a) | (~m & b); }
+static inline u8x16 v16_maxu(u8x16 a, u8x16 b) { return v16_sel((u8x16)(a > b), a, b); }
+static inline u8x16 v16_minu(u8x16 a, u8x16 b) { return v16_sel((u8x16)(a < b), a, b); }
+/* lane i <- lane i-1, lane 0 <- 0 */
+static inline u8x16 v16_shift_in(u8x16 a)
+{
+    const u8x16 zero = {0};
+    const u8x16 idx = {16, 0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14};
+    return __builtin_shuffle(a, zero, idx);
+}
+
 /* ksw_extz2_sse (src/align/ksw2_extz2_sse.c:23-304) as compiled for plain
  * SSE2, restated one byte lane at a time.  The anti-diagonal sweep keeps the
  * reference's per-target-position byte arrays u, v, x, y, s and its rounding
@@ -645,23 +686,32 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
     if (-min_sc > 2 * (q + e)) return 0;
 
     const size_t L = (size_t)tlen_ * 16;
-    uint8_t* u = (uint8_t*)calloc(L * 5, 1);
+    /* one block: u v x y s (L bytes each), H (L int32), off/off_end, p */
+    const size_t ncol = (size_t)n_col_ * 16;
+    const size_t nd = (size_t)(qlen + tlen - 1);
+    const size_t p_bytes = with_cigar ? (nd * (size_t)n_col_ + 1) * 16 : 0;
+    uint8_t* blk = (uint8_t*)malloc(L * 5 + sizeof(int32_t) * L + (with_cigar ? sizeof(int) * nd * 2 : 0) + p_bytes);
+    uint8_t* u = blk;
+    memset(u, 0, L * 5);
     uint8_t *v = u + L, *x = v + L, *y = x + L, *s = y + L;
     int32_t* H = 0;
     int32_t H0 = 0, last_H0_t = 0;
     if (!approx_max) {
-        H = (int32_t*)malloc(sizeof(int32_t) * L);
+        H = (int32_t*)(blk + L * 5);
         for (size_t t = 0; t < L; ++t) H[t] = KSW_NEG_INF;
     }
     uint8_t* p = 0;
     int *off = 0, *off_end = 0;
-    const size_t ncol = (size_t)n_col_ * 16;
     if (with_cigar) {
-        p = (uint8_t*)calloc(((size_t)(qlen + tlen - 1) * (size_t)n_col_ + 1) * 16, 1);
-        off = (int*)malloc(sizeof(int) * (size_t)(qlen + tlen - 1) * 2);
-        off_end = off + qlen + tlen - 1;
+        off = (int*)(blk + L * 5 + sizeof(int32_t) * L);
+        off_end = off + nd;
+        p = (uint8_t*)(off + 2 * nd);
     }
     int last_st = -1, last_en = -1;
+    const int mode = !with_cigar ? 0 : !(flag & EZ_RIGHT) ? 1 : 2;
+    const u8x16 k0 = v16_set(0), kqe2 = v16_set(qe2), kq = v16_set((uint8_t)q), kmax = v16_set(max_sc);
+    const u8x16 k1 = v16_set(1), k2 = v16_set(2), k8 = v16_set(0x08), k16 = v16_set(0x10);
+    const u8x16 m0 = {0xff}, m123 = {0, 0xff, 0xff, 0xff};
     for (int r = 0; r < qlen + tlen - 1; ++r) {
         int st = 0, en = tlen - 1;
         if (st < r - qlen + 1) st = r - qlen + 1;
@@ -708,52 +758,53 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
          * _mm_cvtsi32_si128(int8): the value is sign-extended into bytes 0-3,
          * so a negative boundary byte ORs 0xFF into lanes st+1..st+3. */
         const uint8_t x1_ext = s8(x1) < 0 ? 0xff : 0, v1_ext = s8(v1) < 0 ? 0xff : 0;
-        for (int t = st; t <= en; ++t) {
-            /* block1: old state of the previous anti-diagonal */
-            uint8_t z = (uint8_t)(s[t] + qe2);
-            uint8_t xt1 = x1, vt1 = v1;
-            if (t > st && t <= st + 3) xt1 |= x1_ext, vt1 |= v1_ext;
-            x1 = x[t], v1 = v[t]; /* carried to lane t+1 (read before overwrite) */
-            uint8_t a = (uint8_t)(xt1 + vt1);
-            const uint8_t ut = u[t];
-            uint8_t b = (uint8_t)(y[t] + ut);
-            uint8_t d = 0;
-            if (!with_cigar) {
-                z = s8(z) > 0 ? z : 0;
-                z = z > a ? z : a;
-            } else if (!(flag & EZ_RIGHT)) {
-                d = s8(a) > s8(z) ? 1 : 0;
-                z = s8(z) > 0 ? z : 0;
-                z = z > a ? z : a;
-                if (s8(b) > s8(z)) d = 2;
+        /* 16 lanes per step, as the SSE2 code (st and en + 1 are multiples of
+         * 16): lane i of a block reads lane i-1 of the previous anti-diagonal,
+         * lane 0 the carried byte of the block before. */
+        for (int t = st; t <= en; t += 16) {
+            /* carried byte in lane 0 (and, in the first block, the sign
+             * extension in lanes 1-3), built with masks: element insertion
+             * would go through memory */
+            u8x16 cx = v16_set(x1) & m0, cv = v16_set(v1) & m0;
+            if (t == st) cx |= v16_set(x1_ext) & m123, cv |= v16_set(v1_ext) & m123;
+            const u8x16 X = v16_load(x + t), Vv = v16_load(v + t), ut = v16_load(u + t), yt = v16_load(y + t);
+            x1 = x[t + 15], v1 = v[t + 15];
+            const u8x16 xt1 = v16_shift_in(X) | cx, vt1 = v16_shift_in(Vv) | cv;
+            u8x16 z = v16_load(s + t) + kqe2;
+            u8x16 a = xt1 + vt1, b = yt + ut, d = k0;
+            if (mode == 0) {
+                z = v16_sel(v16_gts(z, k0), z, k0);
+                z = v16_maxu(z, a);
+            } else if (mode == 1) {
+                d = v16_gts(a, z) & k1;
+                z = v16_sel(v16_gts(z, k0), z, k0);
+                z = v16_maxu(z, a);
+                d = v16_sel(v16_gts(b, z), k2, d);
             } else {
-                d = s8(z) > s8(a) ? 0 : 1;
-                z = s8(z) > 0 ? z : 0;
-                z = z > a ? z : a;
-                if (!(s8(z) > s8(b))) d = 2;
+                d = ~v16_gts(z, a) & k1;
+                z = v16_sel(v16_gts(z, k0), z, k0);
+                z = v16_maxu(z, a);
+                d = v16_sel(v16_gts(z, b), d, k2);
             }
-            /* block2 */
-            z = z > b ? z : b;
-            z = z < max_sc ? z : max_sc;
-            u[t] = (uint8_t)(z - vt1);
-            v[t] = (uint8_t)(z - ut);
-            z = (uint8_t)(z - (uint8_t)q);
-            a = (uint8_t)(a - z);
-            b = (uint8_t)(b - z);
-            if (!with_cigar || !(flag & EZ_RIGHT)) {
-                x[t] = s8(a) > 0 ? a : 0;
-                y[t] = s8(b) > 0 ? b : 0;
-                if (with_cigar) {
-                    if (s8(a) > 0) d |= 0x08;
-                    if (s8(b) > 0) d |= 0x10;
-                }
+            z = v16_maxu(z, b);
+            z = v16_minu(z, kmax);
+            v16_store(u + t, z - vt1);
+            v16_store(v + t, z - ut);
+            z = z - kq;
+            a = a - z;
+            b = b - z;
+            if (mode != 2) {
+                const u8x16 pa = v16_gts(a, k0), pb = v16_gts(b, k0);
+                v16_store(x + t, a & pa);
+                v16_store(y + t, b & pb);
+                d |= (pa & k8) | (pb & k16);
             } else {
-                x[t] = s8(a) < 0 ? 0 : a;
-                y[t] = s8(b) < 0 ? 0 : b;
-                if (!(s8(a) < 0)) d |= 0x08;
-                if (!(s8(b) < 0)) d |= 0x10;
+                const u8x16 na = v16_gts(k0, a), nb = v16_gts(k0, b);
+                v16_store(x + t, a & ~na);
+                v16_store(y + t, b & ~nb);
+                d |= (~na & k8) | (~nb & k16);
             }
-            if (with_cigar) pr[t - st] = d;
+            if (with_cigar) v16_store(pr + (t - st), d);
         }
         if (!approx_max) {
             int32_t max_H, max_t;
@@ -763,13 +814,21 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
                 /* four interleaved running maxima (one per 32-bit SIMD lane),
                  * each keeping its first maximum, then combined in lane order */
                 const int en1 = st0 + (en0 - st0) / 4 * 4;
-                int32_t lh[4] = {max_H, max_H, max_H, max_H}, lt[4] = {max_t, max_t, max_t, max_t};
+                const i32x4 zero4 = {0};
+                i32x4 lh = zero4 + max_H, lt = zero4 + max_t;
+                const i32x4 kqe = zero4 + qe;
                 int t;
-                for (t = st0; t < en1; t += 4)
-                    for (int i = 0; i < 4; ++i) {
-                        H[t + i] += (int32_t)v[t + i] - qe;
-                        if (H[t + i] > lh[i]) lh[i] = H[t + i], lt[i] = t;
-                    }
+                for (t = st0; t < en1; t += 4) {
+                    u8x4 vb;
+                    memcpy(&vb, v + t, 4);
+                    i32x4 h;
+                    memcpy(&h, H + t, 16);
+                    h += __builtin_convertvector(vb, i32x4) - kqe;
+                    memcpy(H + t, &h, 16);
+                    const i32x4 gt = h > lh;
+                    lh = (gt & h) | (~gt & lh);
+                    lt = (gt & (zero4 + t)) | (~gt & lt);
+                }
                 for (int i = 0; i < 4; ++i)
                     if (max_H < lh[i]) max_H = lh[i], max_t = lt[i] + i;
                 for (; t < en0; ++t) {
@@ -801,8 +860,6 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
         }
         last_st = st, last_en = en;
     }
-    free(u);
-    free(H);
     cig_t c = {0, 0, 0};
     if (with_cigar) {
         const int rev = !!(flag & EZ_REV_CIGAR);
@@ -814,9 +871,8 @@ int64_t ho_ksw_extz2(int qlen, const uint8_t* query, int tlen, const uint8_t* ta
         } else if (ez->max_t >= 0 && ez->max_q >= 0) {
             backtrack(rev, p, off, off_end, ncol, ez->max_t, ez->max_q, &c);
         }
-        free(p);
-        free(off);
     }
+    free(blk);
     const int64_t nc = c.n;
     if (nc <= cap && nc) memcpy(cigar_out, c.v, sizeof(uint32_t) * (size_t)nc);
     free(c.v);
@@ -891,14 +947,17 @@ static void global_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t 
         }
         return;
     }
-    uint8_t* re = (uint8_t*)malloc((size_t)rlen);
-    uint8_t* qe = (uint8_t*)malloc((size_t)qlen);
+    /* codes and the CIGAR in one buffer (on the stack for small segments) */
+    const int64_t cap = qlen + rlen + 2;
+    uint32_t small[256];
+    const size_t need = (size_t)cap * 4 + (size_t)rlen + (size_t)qlen;
+    uint32_t* c = need <= sizeof(small) ? small : (uint32_t*)malloc(need);
+    uint8_t* re = (uint8_t*)(c + cap);
+    uint8_t* qe = re + rlen;
     for (int64_t i = 0; i < rlen; ++i) re[i] = dna5((unsigned char)ref[i]);
     for (int64_t i = 0; i < qlen; ++i) qe[i] = dna5((unsigned char)qry[i]);
     const int w = ho_auto_band((int)rlen, (int)qlen);
     ho_extz ez;
-    const int64_t cap = qlen + rlen + 2;
-    uint32_t* c = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)cap);
     const int64_t nc = ho_ksw_extz2((int)qlen, qe, (int)rlen, re, 5, k_dna5_mat, 6, 2, w, -1, 0,
                                     flag < 0 ? (EZ_GENERIC_SC | EZ_RIGHT) : flag, &ez, c, cap);
     /* the wrapper copies ez.cigar verbatim; no merging */
@@ -909,9 +968,7 @@ static void global_ksw2(const char* ref, int64_t rlen, const char* qry, int64_t 
         }
         out->v[out->n++] = c[i];
     }
-    free(c);
-    free(re);
-    free(qe);
+    if (c != small) free(c);
 }
 
 static int64_t emit(const cig_t* c, uint32_t* out, int64_t cap)

@@ -122,7 +122,8 @@ def test_noalloc_cigar_capacity_marker(gpu):
     torch = pytest.importorskip("torch")
     fn = _entry(gpu.lib())
     rng = np.random.default_rng(7)
-    q, t = _case(rng, 300, 280, 0.02)
+    q = rng.integers(0, 4, 300).astype(np.uint8)  # unrelated sequences: a long CIGAR
+    t = rng.integers(0, 4, 280).astype(np.uint8)
     _, full = gpu.ksw_extz2(q, t, 5, MAT, 6, 2, -1, -1, 0, 0x06)
     assert len(full) > 6
     cap = 4
