@@ -47,6 +47,17 @@ MEASURED = ROOT / "MEASURED_PEAKS.json"
 FALLBACK_HBM = 6800.0
 
 
+# Speed of the oracle port relative to the unmodified reference build on the
+# same queries and threads (x86-64, where the reference's SSE2 KSW2 builds;
+# interleaved 50-query blocks of the mito workload, tests/test_port_speed.py).
+PORT_VS_REF_X86 = {"threads_1": 0.98, "threads_8": 0.96}
+
+# Warp instructions per query base of the stage kernels, from their ncu
+# captures on the mito workload (profiles/kernels_mito4k.md).
+MITO_INST_PER_BASE = {"seed": 273.3e6 / 66.3e6, "anchor": 71.0e6 / 66.3e6, "chain": 420.3e6 / 66.3e6,
+                      "rows": 92.9e6 / 66.3e6}
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -200,6 +211,33 @@ def algorithmic_bytes(b, n_cigar_words: int, L: int):
     return inp + out
 
 
+def integer_roofline(pkg, args, stages, top, top_ms, bases, local, clocks):
+    """The dominant kernel's warp-instruction rate against the issue ceiling
+    and the measured integer-pipe ceiling (hg_int_peaks)."""
+    peaks = pkg.int_peaks()
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+    except Exception:
+        pass
+    sm_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    issue_peak = 4.0 * sms * sm_mhz * 1e6
+    roof = {"bound": "int-issue", "kernel": STAGE_KERNEL.get(top, top), "unit": "warp-inst/s",
+            "peak": round(issue_peak, 1), "peak_source": f"4 warp-inst/clk/SM x {sms} SMs x {sm_mhz:.0f} MHz (sampled)",
+            "int_pipe_peak_warp_inst": round(peaks["int_pipe_warp_inst"], 1),
+            "measured_int_peaks_per_s": {k: round(v, 1) for k, v in peaks.items()}}
+    if args.workload == "mito" and top in MITO_INST_PER_BASE and top_ms > 0:
+        ach = MITO_INST_PER_BASE[top] * bases / (top_ms / 1e3)
+        roof.update({"achieved": round(ach, 1), "frac": round(ach / issue_peak, 4),
+                     "frac_of_int_pipe_peak": round(ach / peaks["int_pipe_warp_inst"], 4),
+                     "inst_per_base": round(MITO_INST_PER_BASE[top], 3)})
+    if args.workload == "mito":
+        roof["stage_issue_frac"] = {k: round(v * bases / (stages[k] / 1e3) / issue_peak, 4)
+                                    for k, v in MITO_INST_PER_BASE.items() if stages.get(k, 0) > 0}
+    return roof
+
+
 def measure_plain(pkg, ctx, w, n_plain: int):
     """The plain form (one launch sequence per query, hg_align_plain) on the
     first n_plain queries, and the batched form on the same queries."""
@@ -260,6 +298,89 @@ def measure_serving(pkg, n_req: int, rate: float):
     return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in out.items()}
 
 
+def _oracle_check(args_tuple):
+    """CIGARs and rows of sampled queries against the oracle (pool worker)."""
+    center, queries, cigs, rows = args_tuple
+    from oracle.oracle import Oracle
+    o = Oracle()
+    cx, cy = o.extract_minimizer(center)
+    bad_c = bad_r = 0
+    for j, q in enumerate(queries):
+        want = o.align_query(center, cx, cy, q)
+        if not np.array_equal(cigs[j], want):
+            bad_c += 1
+        if rows[j] != o.del_query(q, want):
+            bad_r += 1
+    return bad_c, bad_r, len(queries)
+
+
+def run_stream(args, pkg):
+    """A workload at its stated size, streamed: chunk c of the seeded
+    workload is generated, packed (hg_pack) and aligned through
+    hg_align_batch with host buffers (CIGARs, insertion flags and rows come
+    back); a fixed sample of every chunk - every query with an N-run plus a
+    stride - is checked against the oracle (CIGARs and rows) on the host
+    cores (a spawned pool) while later chunks align.  The value is aligned
+    Mbp/s over all chunks (packing, copies and alignment; generation
+    excluded)."""
+    import multiprocessing as mp
+    name, n_total, chunk = args.workload, args.queries, args.stream_chunk
+    n_chunks = -(-n_total // chunk)
+    if name == "mito":
+        def gen(c, m):
+            return pkg.synth.mito(m, block0=c * (-(-chunk // pkg.synth.MITO_CHUNK)))
+    else:
+        def gen(c, m):
+            return getattr(pkg.synth, name)(m, chunk=c)
+    pool = mp.get_context("spawn").Pool(max(1, (os.cpu_count() or 2) - 2))
+    w0 = gen(0, min(chunk, n_total))
+    ix = pkg.Index(w0.center)
+    longest = 29903 if name in ("uneven", "serve") else len(w0.center) + 64
+    sub = min(chunk, 50000)
+    ctx = pkg.Context(ix, max_queries=sub, max_bases=min(sub * longest, 900_000_000))
+    pending = []
+    t_align = 0.0
+    bases = queries = 0
+    per_chunk = max(1, args.check_sample // n_chunks)
+    for c in range(n_chunks):
+        m = min(chunk, n_total - c * chunk)
+        w = w0 if c == 0 else gen(c, m)
+        t0 = time.perf_counter()
+        b = pkg.pack(w.seqs, w.offsets)
+        res = ctx.align(b, rows=True)
+        t_align += time.perf_counter() - t0
+        if res.status.any():
+            raise SystemExit(f"stream: chunk {c} reported status flags")
+        bases += b.bases
+        queries += b.n
+        # sample: every query with an N-run, plus a stride over the rest
+        has_n = [i for i in range(w.n) if b.exc_off[i + 1] > b.exc_off[i]]
+        stride = list(range(0, w.n, max(1, w.n // per_chunk)))[:per_chunk]
+        idx = sorted(set(has_n) | set(stride))
+        for a in range(0, len(idx), 200):  # tasks of 200 queries spread over the pool
+            part = idx[a:a + 200]
+            pending.append(pool.apply_async(_oracle_check, ((w.center, [w.query(i) for i in part],
+                                                             [res.cigar_of(i).copy() for i in part],
+                                                             [res.rows[i].tobytes() for i in part]),)))
+        log(f"[stream] chunk {c + 1}/{n_chunks}: {b.n} queries, {b.bases / 1e6:.1f} Mbp, {len(idx)} sampled")
+        del res, b
+    bad_c = bad_r = n_chk = 0
+    for r in pending:
+        bc, br, nn = r.get()
+        bad_c, bad_r, n_chk = bad_c + bc, bad_r + br, n_chk + nn
+    pool.close()
+    line = {"metric": METRIC, "value": round(bases / t_align / 1e6, 3), "unit": UNIT, "n_gpus": 1,
+            "mode": "stream", "higher_is_better": True, "dtype": "u8/int32", "data": "synthetic",
+            "config": {"workload": WORKLOADS[name].format(n=n_total), "queries": queries, "bases": bases,
+                       "chunk_queries": chunk, "chunks": n_chunks,
+                       "timed": "hg_pack + hg_align_batch with host buffers (rows back) per chunk; generation "
+                                "excluded"},
+            "parity_full_size": {"checked_queries": n_chk, "cigar_mismatches": bad_c, "row_mismatches": bad_r,
+                                 "against": "oracle CIGARs and rows; every N-run query plus a stride sample"}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_impl_reference(args, rank, world):
     """The reference's CPU path (the oracle restatement) on the host cores."""
     if rank != 0:
@@ -286,7 +407,8 @@ def run_impl_reference(args, rank, world):
         "config": {"workload": "mito 16,569 bp center x mutated full-length queries; bounded sample per step",
                    "k": 15, "w": 10, "sample_queries_per_step": int(np.median([v[1] for v in vals]))},
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "consecutive 1000-query blocks of the mito workload, ~5 s per step"},
+                         "sample": "consecutive 1000-query blocks of the mito workload, ~5 s per step",
+                         "port_vs_reference_x86": PORT_VS_REF_X86},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -311,6 +433,11 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the launch-shape autotuner")
     ap.add_argument("--workload", default="mito", choices=sorted(WORKLOADS),
                     help="synthetic workload (the headline metric is quoted on mito)")
+    ap.add_argument("--stream-chunk", type=int, default=0,
+                    help="stream the workload in generated chunks of this many queries and check a full-size "
+                         "sample against the oracle (the stated-size checks)")
+    ap.add_argument("--check-sample", type=int, default=10000,
+                    help="queries checked against the oracle in stream mode (plus every N-run query)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -321,6 +448,8 @@ def main():
     pkg.lib()
     if pkg.device_count() == 0:
         raise SystemExit("bench: no CUDA device")
+    if args.stream_chunk > 0:
+        return run_stream(args, pkg)
     dist = Dist(world, local, use_gpu=True)
     if world > 1:
         pkg.set_device(local)  # the library's current device for this process: its index and contexts live there
@@ -401,11 +530,21 @@ def main():
 
         call()
         dist.barrier()
-        e2e_steps = max(1, min(args.steps, 3))
+        e2e_steps = args.steps
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
             call()
         e_wall = dist.max((time.perf_counter() - t0) / e2e_steps)
+        # from ASCII: the caller's hg_pack (OpenMP over queries) into the
+        # pinned input, then the same call, every step
+        asc_steps = max(1, min(args.steps, 3))
+        seqs_u8 = np.frombuffer(w.seqs, np.uint8)
+        t0 = time.perf_counter()
+        for _ in range(asc_steps):
+            pkg._check(L.hg_pack(P(seqs_u8), P(w.offsets), b.n, P(pb.packed), len(pb.packed), P(pb.poff),
+                                 P(pb.exc), len(pb.exc) // 3, P(pb.exc_off), None, None))
+            call()
+        a_wall = dist.max((time.perf_counter() - t0) / asc_steps)
         n_cig_words = int(off_out[-1])
         # spot check of the timed output against the CPU path (bit-exact)
         from oracle.oracle import Oracle
@@ -421,7 +560,11 @@ def main():
         h2d = b.nbytes
         d2h = 4 * n_cig_words + 8 * (b.n + 1) + b.n + 4 * b.n + b.n * ix.L
         e2e = {"value": round(world * b.bases / e_wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1000 * e_wall, 3)}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1000 * e_wall, 3), "steps": e2e_steps,
+               "input": "2-bit packed host buffers (the C ABI's input format)",
+               "from_ascii": {"value": round(world * b.bases / a_wall / 1e6, 3), "unit": UNIT,
+                              "ms_per_step": round(1000 * a_wall, 3), "steps": asc_steps,
+                              "note": "hg_pack of the ASCII queries on the host cores inside the timed region"}}
     if n_cig_words is None:
         n_cig_words = 64 * b.n
     plain = measure_plain(pkg, ctx, w, args.plain_queries) if args.plain_queries > 0 else None
@@ -451,12 +594,22 @@ def main():
     if args.workload == "mito" and top in mito_dram_per_base:
         traffic = int(round(mito_dram_per_base[top] * B / n_sub))
     clocks = clk.summary()
+    # integer roofline: the path is bound by integer instruction issue.  Warp
+    # instructions per query base of each stage's kernel from its ncu capture
+    # on the mito workload (4,000 queries, 66.3 Mbp; profiles/), times the
+    # bases of this run, over the stage's event time, against the issue
+    # ceiling (4 warp instructions per clock per SM at the sampled SM clock)
+    # and the measured integer-pipe ceiling (hg_int_peaks: 2 per clock per
+    # SM; kernels that also use the FMA, load/store and uniform pipes can
+    # exceed it).
+    int_roof = integer_roofline(pkg, args, stages, top, top_ms, B, local, clocks)
     cpu = None
     if rank == 0 and args.cpu_seconds > 0:
         from oracle.oracle import Oracle
         v, nq, nb, t = cpu_sample(Oracle(), w, args.cpu_seconds, os.cpu_count() or 1)
         cpu = {"value": round(v, 3), "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
-               "sample": f"first {nq} queries ({nb} bases) of the workload, {t:.1f} s of CPU time"}
+               "sample": f"first {nq} queries ({nb} bases) of the workload, {t:.1f} s of CPU time",
+               "port_vs_reference_x86": PORT_VS_REF_X86}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1000 * step_s, 3), "higher_is_better": True,
@@ -472,6 +625,7 @@ def main():
         "gcups": round(world * cells / step_s / 1e9, 3) if cells else None,
         "gpu_launches": int(launches),
         "stage_ms": {k: round(v, 3) for k, v in stages.items()},
+        "int_roofline": int_roof,
         "roofline": {"bound": "hbm", "kernel": STAGE_KERNEL.get(top, top),
                      "achieved": round(top_achieved, 2) if top_achieved else None, "peak": peak, "unit": "GB/s",
                      "frac": round(top_achieved / peak, 5) if top_achieved else None, "traffic": traffic,

@@ -531,7 +531,7 @@ def project_row(qry, cigar, pad: bool = False) -> bytes:
 
 
 INT_PEAK_KEYS = ("int32_add_max_ops", "dpx_s32_ops", "dpx_s16x2_ops", "dpx_max3_s16x2_ops", "mul64_ops",
-                 "issue_warp_inst")
+                 "int_pipe_warp_inst")
 
 
 def int_peaks() -> dict:

@@ -5,15 +5,18 @@
 // kernel below runs one instruction class in 8 independent chains per
 // thread over a full grid (every SM, 2048 threads each) and reports element
 // operations per second:
-//   [0] int32 add + max pairs (the DP cell's plain form), ops = 2 per pair
+//   [0] int32 max(a + b, c) written as plain add and max, ops = 2
 //   [1] DPX __viaddmax_s32 (max(a + b, c) in one instruction), ops = 2
 //   [2] DPX __viaddmax_s16x2 (two 16-bit lanes), ops = 4
 //   [3] DPX __vimax3_s16x2 (three-way max of two 16-bit lanes), ops = 4
 //   [4] 64-bit multiply-add (splitmix64's multiplies), ops = 1
-//   [5] warp-instruction issue rate of [0]'s kernel (instructions per second
-//       from the pair count, two instructions per pair)
+//   [5] integer-pipe warp instructions per second: [1]'s kernel issues one
+//       instruction per step and chain
 // The chains feed on values loaded at run time and the results are stored,
-// so nothing folds away.
+// so nothing folds away.  Measured on GB300 (ncu instruction counts): the
+// compiler fuses [0]'s add and max into one integer-pipe instruction, so [0]
+// and [1] run at the same rate, two warp instructions per clock per SM; the
+// 16x2 forms issue at that rate too and do twice the element operations.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -156,7 +159,7 @@ extern "C" int hg_int_peaks(double* out, int n)
         }
         res[k] = (double)blocks * threads * hg::kPeakChains * iters[k] * ops[k] / (best * 1e-3);
     }
-    res[5] = res[0] / 32.0;  // two instructions (add, max) per two element ops, 32 lanes per warp instruction
+    res[5] = res[1] / 2.0 / 32.0;  // one instruction (two element ops) per lane and step, 32 lanes per warp
     cleanup();
     for (int i = 0; i < n && i < 6; ++i) out[i] = res[i];
     return rc;

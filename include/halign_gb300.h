@@ -158,7 +158,7 @@ int hg_staged_flags(hg_ctx_t* ctx, uint32_t* flags);
  * full-grid kernels (about 20 ms in all): out[0] int32 add + max element
  * operations per second, out[1] DPX max(a + b, c) on int32, out[2] the same
  * on int16x2, out[3] DPX three-way max on int16x2, out[4] 64-bit
- * multiply-adds, out[5] warp instructions per second of out[0]'s kernel.
+ * multiply-adds, out[5] integer-pipe warp instructions per second.
  * n <= 6 values are written.  The roofline of this integer path; no
  * reference counterpart. */
 int hg_int_peaks(double* out, int n);
