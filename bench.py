@@ -256,17 +256,23 @@ def measure_plain(pkg, ctx, w, n_plain: int):
             "note": "host-timed hg_align_plain vs hg_align_batch (both with H2D/D2H) on the same queries"}
 
 
-def measure_serving(pkg, n_req: int, rate: float):
-    """Continuous-batching loop (config: Poisson arrivals at `rate` req/s,
-    500..29,903 bp substrings of a 29,903 bp center, 0.5% divergence)."""
+def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 20000):
+    """The serving loop (hg_serve_*, scheduler in the library) on the serve
+    workload (Poisson arrivals, 500..29,903 bp substrings of a 29,903 bp
+    center, 0.5% divergence): p50/p99 at `rate` req/s; saturation (n_sat
+    requests all waiting at t=0) against the same n_sat requests aligned as
+    one device-resident batch; and an offered load of 70% of that batched
+    rate (Poisson arrivals) for latency at load."""
     w = pkg.synth.serve(n_req, rate=rate)
     ix = pkg.Index(w.center)
-    srv = pkg.serve.Server(ix, n_slots=8, slot_queries=512, slot_bases=8_000_000, budget_bytes=40 << 30)
-    srv.run(w.seqs, w.offsets[: min(w.n, 200) + 1], None)  # warm-up (graph-free async path)
+    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=1024, slot_bases=16_000_000, budget_bytes=40 << 30)
+    srv.run(w.seqs, w.offsets[: min(w.n, 400) + 1], None)  # warm-up
     st = srv.run(w.seqs, w.offsets, w.arrivals)
-    sat = srv.run(w.seqs, w.offsets, None)  # every request waiting at t=0: saturation throughput
-    ctx = pkg.Context(ix, max_queries=w.n, max_bases=int(w.total_bases) + 1024)
-    b = pkg.pack(w.seqs, w.offsets)
+    ws = pkg.synth.serve(n_sat, rate=rate, chunk=1)
+    sat = srv.run(ws.seqs, ws.offsets, None)
+    # the same requests as one batch, device-resident and through the host-buffer call
+    ctx = pkg.Context(ix, max_queries=ws.n, max_bases=int(ws.total_bases) + 1024)
+    b = pkg.pack(ws.seqs, ws.offsets)
     ctx.stage(b)
     for _ in range(2):
         ctx.run_staged()
@@ -274,28 +280,88 @@ def measure_serving(pkg, n_req: int, rate: float):
     ctx.run_staged()
     ms = ctx.last_timing()[0]
     batched = b.bases / (ms / 1e3) / 1e6
-    # the same batch through the host-buffer call (packing, H2D, D2H of CIGARs)
     ctx.align(b, rows=False, check=False)
     t0 = time.perf_counter()
-    ctx.align(pkg.pack(w.seqs, w.offsets), rows=False, check=False)
+    ctx.align(pkg.pack(ws.seqs, ws.offsets), rows=False, check=False)
     batched_e2e = b.bases / (time.perf_counter() - t0) / 1e6
-    # offered load at 70% of the batched device rate (Poisson arrivals)
-    rate_hi = 0.7 * batched * 1e6 / (b.bases / w.n)
-    w_hi = pkg.synth.serve(n_req, rate=rate_hi)
-    hi = srv.run(w_hi.seqs, w_hi.offsets, w_hi.arrivals).summary()
-    out = st.summary()
-    out.update({"high_load": {"rate_req_per_s": round(rate_hi, 1), "offered_frac_of_batched": 0.7,
-                              "p50_ms": round(hi["p50_ms"], 3), "p99_ms": round(hi["p99_ms"], 3),
-                              "mbp_per_s": round(hi["mbp_per_s"], 3)}})
-    out.update({"rate_req_per_s": rate, "center_bp": len(w.center),
-                "saturation_mbp_per_s": round(sat.summary()["mbp_per_s"], 3),
-                "batched_mbp_per_s": round(batched, 3),
-                "saturation_frac_of_batched": round(sat.summary()["mbp_per_s"] / batched, 3),
-                "batched_e2e_mbp_per_s": round(batched_e2e, 3),
-                "saturation_frac_of_batched_e2e": round(sat.summary()["mbp_per_s"] / batched_e2e, 3),
-                "saturation_p99_ms": round(sat.summary()["p99_ms"], 3),
-                "budget_bytes": 40 << 30})
-    return {k: (round(v, 3) if isinstance(v, float) else v) for k, v in out.items()}
+    ctx.close()
+    # offered load at 70% of the batched device rate
+    rate_hi = 0.7 * batched * 1e6 / (b.bases / ws.n)
+    wh = pkg.synth.serve(n_sat, rate=rate_hi, chunk=2)
+    hi = srv.run(wh.seqs, wh.offsets, wh.arrivals)
+    keep = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "requests", "micro_batches", "mbp_per_s", "status_or")
+    out = {k: st[k] for k in keep}
+    out.update({"rate_req_per_s": rate, "center_bp": len(w.center), "loop": "native (hg_serve_*)",
+                "contexts": int(st["contexts"]), "device_bytes": int(st["device_bytes"]), "budget_bytes": 40 << 30,
+                "saturation": {k: sat[k] for k in keep},
+                "batched_same_requests_mbp_per_s": batched, "batched_same_requests_e2e_mbp_per_s": batched_e2e,
+                "saturation_frac_of_batched": sat["mbp_per_s"] / batched,
+                "saturation_frac_of_batched_e2e": sat["mbp_per_s"] / batched_e2e,
+                "high_load": {"offered_frac_of_batched": 0.7, "rate_req_per_s": rate_hi,
+                              **{k: hi[k] for k in keep}}})
+    srv.close()
+    return _round(out)
+
+
+def _round(d):
+    if isinstance(d, dict):
+        return {k: _round(v) for k, v in d.items()}
+    return round(d, 3) if isinstance(d, float) else d
+
+
+def run_serve_million(args, pkg):
+    """The serving loop over args.serve_requests requests generated in
+    chunks (the stated 10^6), all waiting: the resident counters of the
+    served rows must equal those of the batch path over the same requests,
+    and a sample of the served CIGARs must equal the oracle's."""
+    import multiprocessing as mp
+    pool = mp.get_context("spawn").Pool(max(1, (os.cpu_count() or 2) - 2))
+    chunk = 50000
+    n_chunks = -(-args.serve_requests // chunk)
+    w0 = pkg.synth.serve(min(chunk, args.serve_requests), chunk=0)
+    ix = pkg.Index(w0.center)
+    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=1024, slot_bases=16_000_000, budget_bytes=40 << 30)
+    ctx = pkg.Context(ix, max_queries=chunk, max_bases=chunk * 29903)
+    pending, served, bases, t_serve, p99s, st_or = [], 0, 0, 0.0, [], 0
+    for c in range(n_chunks):
+        m = min(chunk, args.serve_requests - c * chunk)
+        w = w0 if c == 0 else pkg.synth.serve(m, chunk=c)
+        out = srv.run(w.seqs, w.offsets, None, keep_results=True)
+        t_serve += out["wall_s"]
+        p99s.append(out["p99_ms"])
+        st_or |= out["status_or"]
+        ctx.align(pkg.pack(w.seqs, w.offsets), rows=False, check=False)  # batch path: its own counters
+        served += w.n
+        bases += int(w.total_bases)
+        idx = list(range(0, w.n, max(1, w.n // max(1, args.check_sample // n_chunks))))
+        for a in range(0, len(idx), 100):
+            part = idx[a:a + 100]
+            pending.append(pool.apply_async(_oracle_check_cigars, ((w.center, [w.query(i) for i in part],
+                                                                    [out["results"][i] for i in part]),)))
+        log(f"[serve] chunk {c + 1}/{n_chunks}: {w.n} requests served")
+    cs, ins_s = srv.counters()
+    cb, ins_b = ctx.counters()
+    bad = sum(r.get() for r in pending)
+    pool.close()
+    line = {"metric": "serving loop over a stated-size request stream", "mode": "serve", "requests": served,
+            "bases": bases, "mbp_per_s_saturated": round(bases / t_serve / 1e6, 3),
+            "p99_ms_worst_chunk": round(max(p99s), 3), "status_or": st_or,
+            "counters_equal_batch_path": bool(np.array_equal(cs, cb) and np.array_equal(ins_s, ins_b)),
+            "counters_total": int(cs.astype(np.uint64).sum()),
+            "cigar_sample_checked": args.check_sample, "cigar_sample_mismatches": int(bad),
+            "note": "chunks of 50,000 requests, all waiting; counters of the serving contexts vs a batch context "
+                    "over the same requests; CIGAR sample vs the oracle"}
+    srv.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def _oracle_check_cigars(args_tuple):
+    center, queries, cigs = args_tuple
+    from oracle.oracle import Oracle
+    o = Oracle()
+    cx, cy = o.extract_minimizer(center)
+    return sum(0 if np.array_equal(c, o.align_query(center, cx, cy, q)) else 1 for q, c in zip(queries, cigs))
 
 
 def _oracle_check(args_tuple):
@@ -436,6 +502,8 @@ def main():
     ap.add_argument("--stream-chunk", type=int, default=0,
                     help="stream the workload in generated chunks of this many queries and check a full-size "
                          "sample against the oracle (the stated-size checks)")
+    ap.add_argument("--serve-million", action="store_true",
+                    help="serve --serve-requests requests (10^6 stated) and check the resident counters")
     ap.add_argument("--check-sample", type=int, default=10000,
                     help="queries checked against the oracle in stream mode (plus every N-run query)")
     args = ap.parse_args()
@@ -450,6 +518,8 @@ def main():
         raise SystemExit("bench: no CUDA device")
     if args.stream_chunk > 0:
         return run_stream(args, pkg)
+    if args.serve_million:
+        return run_serve_million(args, pkg)
     dist = Dist(world, local, use_gpu=True)
     if world > 1:
         pkg.set_device(local)  # the library's current device for this process: its index and contexts live there

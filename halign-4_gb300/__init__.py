@@ -136,6 +136,14 @@ def lib() -> C.CDLL:
     L.hg_project_row.restype = i64
     L.hg_count_rows.argtypes = [vp, i64, i64, i64, vp, i32]
     L.hg_int_peaks.argtypes = [vp, i32]
+    L.hg_submit_ascii.argtypes = [vp, vp, vp, i64]
+    L.hg_serve_create.argtypes = [vp, i32, i64, i64, i64, C.POINTER(vp)]
+    L.hg_serve_destroy.argtypes = [vp]
+    L.hg_serve_submit.argtypes = [vp, C.c_char_p, i64]
+    L.hg_serve_submit.restype = i64
+    L.hg_serve_result.argtypes = [vp, vp, vp, vp, vp, i64, vp, i32]
+    L.hg_serve_stats.argtypes = [vp, vp, i32, i32]
+    L.hg_serve_counters.argtypes = [vp, vp, vp, i32]
     L.hg_extend_align_ksw2.argtypes = [C.c_char_p, i64, C.c_char_p, i64, i32, vp, i64]
     L.hg_extend_align_ksw2.restype = i64
     _lib = L

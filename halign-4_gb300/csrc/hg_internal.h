@@ -78,6 +78,9 @@ struct Workspace {
 // The calling thread's workspace for the current device (created on first use).
 int workspace(Workspace** out);
 
+// Length of an index's center.
+int64_t index_length(const hg_index_t* ix);
+
 // Minimizers of one sequence through the batch seed kernel (hg_index_create
 // and hg_extract_minimizer).
 int run_extract(int k, int w, int non_canonical, const char* seq, int64_t len, std::vector<uint64_t>& xs,

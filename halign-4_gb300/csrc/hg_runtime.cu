@@ -580,6 +580,8 @@ extern "C" void hg_index_destroy(hg_index_t* ix)
     delete ix;
 }
 
+int64_t hg::index_length(const hg_index_t* ix) { return ix ? ix->L : 0; }
+
 extern "C" int hg_index_device(const hg_index_t* ix, int* ordinal, char* pci_bus_id, int len)
 {
     if (!ix) return fail(HG_ERR_ARG, "hg_index_device: null index");
@@ -1512,41 +1514,35 @@ extern "C" int hg_fetch_staged(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, 
 
 // ------------------------------------------------------ asynchronous form
 
-extern "C" int hg_submit(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
-                         const int32_t* exc, const int64_t* exc_off, int64_t n)
+namespace {
+
+// Pinned staging of the asynchronous form, allocated on first use.
+int async_staging(hg_ctx_t* c)
 {
-    if (!c || n <= 0 || !packed || !poff || !qlen || !exc_off) return fail(HG_ERR_ARG, "hg_submit: bad arguments");
-    if (c->async_n >= 0) return fail(HG_ERR_ARG, "hg_submit: previous batch not collected");
-    cudaSetDevice(c->ix->device);
-    int64_t bases = 0, bytes = 0;
-    for (int64_t i = 0; i < n; ++i) bases += qlen[i], bytes += (int64_t)padded_bytes(qlen[i]);
-    const int64_t ne = exc_off[n] - exc_off[0];
-    if (n > c->max_n || bases > c->max_bases || bytes > (int64_t)c->packed.n || ne > c->exc_cap)
-        return fail(HG_ERR_CAPACITY, "hg_submit: batch exceeds the context capacity");
+    if (c->h_packed) return HG_OK;
     const int64_t M = c->max_n + 1;
-    if (!c->h_packed) {
-        if (cudaHostAlloc(&c->h_packed, c->packed.n, cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc(&c->h_i64, sizeof(int64_t) * 5 * M, cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc(&c->h_i32, sizeof(int32_t) * (2 * M + 3 * c->exc_cap), cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc(&c->h_has_ins, (size_t)M, cudaHostAllocDefault) != cudaSuccess ||
-            cudaHostAlloc(&c->h_status, sizeof(uint32_t) * M, cudaHostAllocDefault) != cudaSuccess ||
-            cudaEventCreateWithFlags(&c->done_ev, cudaEventDisableTiming) != cudaSuccess)
-            return fail(HG_ERR_NOMEM, "hg_submit: pinned staging allocation");
-    }
+    if (cudaHostAlloc(&c->h_packed, c->packed.n, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc(&c->h_i64, sizeof(int64_t) * 5 * M, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc(&c->h_i32, sizeof(int32_t) * (2 * M + 3 * c->exc_cap), cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc(&c->h_has_ins, (size_t)M, cudaHostAllocDefault) != cudaSuccess ||
+        cudaHostAlloc(&c->h_status, sizeof(uint32_t) * M, cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->done_ev, cudaEventDisableTiming) != cudaSuccess)
+        return fail(HG_ERR_NOMEM, "hg_submit: pinned staging allocation");
+    return HG_OK;
+}
+
+// The staged micro-batch (packed bases at h_packed, per-query offsets,
+// lengths and exception runs in h_i64 / h_i32) goes up and through the
+// stages on the context stream; results come back behind done_ev.
+int submit_tail(hg_ctx_t* c, int64_t n, int64_t pb, int64_t ne)
+{
+    const int64_t M = c->max_n + 1;
     int64_t *spoff = c->h_i64, *seoff = c->h_i64 + M, *shoff = c->h_i64 + 2 * M, *scoff = c->h_i64 + 3 * M;
     int32_t *sqlen = c->h_i32, *sorder = c->h_i32 + M, *sexc = c->h_i32 + 2 * M;
     std::vector<int32_t> order;
     std::vector<int64_t> hoff, coff;
-    sub_arrays(c, qlen, n, order, hoff, coff);
-    int64_t pb = 0;
-    for (int64_t i = 0; i < n; ++i) {
-        const size_t nb = padded_bytes(qlen[i]);
-        std::memcpy(c->h_packed + pb, packed + poff[i], nb);
-        spoff[i] = pb, pb += (int64_t)nb;
-        sqlen[i] = qlen[i], sorder[i] = order[i], shoff[i] = hoff[i], scoff[i] = coff[i];
-    }
-    for (int64_t i = 0; i <= n; ++i) seoff[i] = exc_off[i] - exc_off[0];
-    if (ne) std::memcpy(sexc, exc + 3 * exc_off[0], 12 * (size_t)ne);
+    sub_arrays(c, sqlen, n, order, hoff, coff);
+    for (int64_t i = 0; i < n; ++i) sorder[i] = order[i], shoff[i] = hoff[i], scoff[i] = coff[i];
     cudaStream_t st = c->st;
     HG_CUDA(cudaMemcpyAsync(c->packed.p, c->h_packed, (size_t)pb, cudaMemcpyHostToDevice, st));
     if (ne) HG_CUDA(cudaMemcpyAsync(c->exc.p, sexc, 12 * (size_t)ne, cudaMemcpyHostToDevice, st));
@@ -1568,6 +1564,80 @@ extern "C" int hg_submit(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff
     HG_CUDA(cudaEventRecord(c->done_ev, st));
     c->async_n = n;
     return HG_OK;
+}
+
+}  // namespace
+
+extern "C" int hg_submit(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                         const int32_t* exc, const int64_t* exc_off, int64_t n)
+{
+    if (!c || n <= 0 || !packed || !poff || !qlen || !exc_off) return fail(HG_ERR_ARG, "hg_submit: bad arguments");
+    if (c->async_n >= 0) return fail(HG_ERR_ARG, "hg_submit: previous batch not collected");
+    cudaSetDevice(c->ix->device);
+    int64_t bases = 0, bytes = 0;
+    for (int64_t i = 0; i < n; ++i) bases += qlen[i], bytes += (int64_t)padded_bytes(qlen[i]);
+    const int64_t ne = exc_off[n] - exc_off[0];
+    if (n > c->max_n || bases > c->max_bases || bytes > (int64_t)c->packed.n || ne > c->exc_cap)
+        return fail(HG_ERR_CAPACITY, "hg_submit: batch exceeds the context capacity");
+    int r = async_staging(c);
+    if (r) return r;
+    const int64_t M = c->max_n + 1;
+    int64_t *spoff = c->h_i64, *seoff = c->h_i64 + M;
+    int32_t *sqlen = c->h_i32, *sexc = c->h_i32 + 2 * M;
+    int64_t pb = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const size_t nb = padded_bytes(qlen[i]);
+        std::memcpy(c->h_packed + pb, packed + poff[i], nb);
+        spoff[i] = pb, pb += (int64_t)nb;
+        sqlen[i] = qlen[i];
+    }
+    for (int64_t i = 0; i <= n; ++i) seoff[i] = exc_off[i] - exc_off[0];
+    if (ne) std::memcpy(sexc, exc + 3 * exc_off[0], 12 * (size_t)ne);
+    return submit_tail(c, n, pb, ne);
+}
+
+extern "C" int hg_submit_ascii(hg_ctx_t* c, const char* const* seqs, const int64_t* lens, int64_t n)
+{
+    if (!c || n <= 0 || !seqs || !lens) return fail(HG_ERR_ARG, "hg_submit_ascii: bad arguments");
+    if (c->async_n >= 0) return fail(HG_ERR_ARG, "hg_submit_ascii: previous batch not collected");
+    cudaSetDevice(c->ix->device);
+    int64_t bases = 0, bytes = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (lens[i] < 0 || lens[i] > INT32_MAX || (lens[i] > 0 && !seqs[i]))
+            return fail(HG_ERR_ARG, "hg_submit_ascii: bad query");
+        bases += lens[i], bytes += (int64_t)padded_bytes(lens[i]);
+    }
+    if (n > c->max_n || bases > c->max_bases || bytes > (int64_t)c->packed.n)
+        return fail(HG_ERR_CAPACITY, "hg_submit_ascii: batch exceeds the context capacity");
+    int r = async_staging(c);
+    if (r) return r;
+    const int64_t M = c->max_n + 1;
+    int64_t *spoff = c->h_i64, *seoff = c->h_i64 + M;
+    int32_t *sqlen = c->h_i32, *sexc = c->h_i32 + 2 * M;
+    int64_t pb = 0;
+    for (int64_t i = 0; i < n; ++i) spoff[i] = pb, pb += (int64_t)padded_bytes(lens[i]), sqlen[i] = (int32_t)lens[i];
+    // pass 1: bases straight into the pinned staging, queries in parallel
+    std::vector<uint8_t> has_exc((size_t)n);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i) {
+        uint8_t* out = c->h_packed + spoff[i];
+        const size_t nb = padded_bytes(lens[i]);
+        has_exc[i] = pack_one(reinterpret_cast<const unsigned char*>(seqs[i]), lens[i], out) ? 1 : 0;
+        const size_t used = (size_t)(lens[i] + 3) / 4;
+        if (nb > used) std::memset(out + used, 0, nb - used);
+    }
+    // pass 2: exception runs of the queries that hold any
+    int64_t ne = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        seoff[i] = ne;
+        if (!has_exc[i]) continue;
+        const int64_t k = exc_runs(reinterpret_cast<const unsigned char*>(seqs[i]), lens[i], nullptr);
+        if (ne + k > c->exc_cap) return fail(HG_ERR_CAPACITY, "hg_submit_ascii: exception runs exceed the context capacity");
+        exc_runs(reinterpret_cast<const unsigned char*>(seqs[i]), lens[i], sexc + 3 * ne);
+        ne += k;
+    }
+    seoff[n] = ne;
+    return submit_tail(c, n, pb, ne);
 }
 
 extern "C" int hg_poll(hg_ctx_t* c)

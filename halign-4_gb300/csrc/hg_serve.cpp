@@ -1,0 +1,343 @@
+// hg_serve.cpp - the continuous-batching request loop behind hg_serve_*
+// (include/halign_gb300.h): a FIFO of submitted requests, a pool of
+// contexts over one resident index, and a scheduler thread that admits,
+// submits (hg_submit_ascii), polls and collects micro-batches.
+//
+// Host code only; every alignment runs through the context calls of the C
+// ABI.  Requests are independent, so a request's result in the mix is its
+// result alone.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/halign_gb300.h"
+#include "hg_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    std::string seq;              // freed once submitted
+    Clock::time_point t_in;
+    double latency_ms = 0;
+    uint32_t status = 0;
+    std::vector<uint32_t> cigar;  // filled when finished
+    bool returned = false;        // handed out by hg_serve_result
+};
+
+struct Slot {
+    hg_ctx_t* ctx = nullptr;
+    std::vector<int64_t> ids;     // requests of the micro-batch in flight
+    std::vector<uint32_t> cig;
+    std::vector<int64_t> off;
+    std::vector<uint8_t> ins;
+    std::vector<uint32_t> st;
+};
+
+}  // namespace
+
+struct hg_server {
+    hg_index_t* ix = nullptr;
+    int device = 0;
+    int64_t slot_q = 0, slot_b = 0;
+    int64_t arena_bytes = 0;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request> reqs;     // request id - base_id indexes it
+    int64_t base_id = 0;
+    std::deque<int64_t> pending;  // submitted, not yet admitted
+    std::deque<int64_t> done;     // finished, not yet returned
+    std::vector<float> lat;       // latencies of finished requests (stats)
+    int64_t bases_done = 0, batches = 0;
+    Clock::time_point t_first, t_last;
+    bool have_first = false;
+    bool stop = false;
+    int error = HG_OK;
+    std::string error_msg;
+    std::thread sched;
+};
+
+namespace {
+
+int64_t arena_of(hg_index_t* ix, int64_t q, int64_t b, hg_ctx_t** out)
+{
+    size_t f0 = 0, f1 = 0, tot = 0;
+    cudaMemGetInfo(&f0, &tot);
+    const int r = hg_ctx_create(ix, q, b, out);
+    if (r) return -r;
+    cudaMemGetInfo(&f1, &tot);
+    return f0 > f1 ? (int64_t)(f0 - f1) : 0;
+}
+
+// Fills slot s with the oldest waiting requests; returns their ids (empty:
+// nothing waiting).  Called with the lock held.
+void admit(hg_server* S, std::vector<int64_t>& take, std::vector<const char*>& ptr, std::vector<int64_t>& len)
+{
+    take.clear(), ptr.clear(), len.clear();
+    int64_t bases = 0;
+    while (!S->pending.empty() && (int64_t)take.size() < S->slot_q) {
+        const int64_t id = S->pending.front();
+        Request& r = S->reqs[(size_t)(id - S->base_id)];
+        if (!take.empty() && bases + (int64_t)r.seq.size() > S->slot_b) break;
+        S->pending.pop_front();
+        take.push_back(id);
+        ptr.push_back(r.seq.data());
+        len.push_back((int64_t)r.seq.size());
+        bases += (int64_t)r.seq.size();
+    }
+}
+
+void fail_all(hg_server* S, int code, const std::string& msg)
+{
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->error = code;
+    S->error_msg = msg;
+    S->cv_done.notify_all();
+}
+
+void scheduler(hg_server* S)
+{
+    cudaSetDevice(S->device);
+    std::vector<int> free_slots;
+    for (int i = (int)S->slots.size() - 1; i >= 0; --i) free_slots.push_back(i);
+    std::vector<int> busy;
+    std::vector<int64_t> take, len;
+    std::vector<const char*> ptr;
+    for (;;) {
+        bool progressed = false;
+        // admit and submit into every free context
+        while (!free_slots.empty()) {
+            {
+                std::unique_lock<std::mutex> lock(S->mu);
+                if (S->pending.empty()) {
+                    if (S->stop && busy.empty()) return;
+                    if (busy.empty()) {
+                        S->cv_work.wait(lock, [&] { return S->stop || !S->pending.empty(); });
+                        if (S->pending.empty()) return;
+                    } else {
+                        break;
+                    }
+                }
+                admit(S, take, ptr, len);
+            }
+            if (take.empty()) break;
+            const int s = free_slots.back();
+            free_slots.pop_back();
+            // the request strings stay put until collection (only the scheduler
+            // frees them), so packing runs without the lock
+            const int r = hg_submit_ascii(S->slots[s].ctx, ptr.data(), len.data(), (int64_t)take.size());
+            if (r) {
+                fail_all(S, r, hg_last_error());
+                return;
+            }
+            S->slots[s].ids = take;
+            busy.push_back(s);
+            {
+                std::lock_guard<std::mutex> lock(S->mu);
+                ++S->batches;
+            }
+            progressed = true;
+        }
+        // collect finished micro-batches
+        for (size_t k = 0; k < busy.size();) {
+            const int s = busy[k];
+            Slot& sl = S->slots[s];
+            const int p = hg_poll(sl.ctx);
+            if (p < 0) {
+                fail_all(S, -p, hg_last_error());
+                return;
+            }
+            if (p == 0) {
+                ++k;
+                continue;
+            }
+            const size_t n = sl.ids.size();
+            int64_t bases = 0;
+            {
+                std::lock_guard<std::mutex> lock(S->mu);
+                for (int64_t id : sl.ids) bases += (int64_t)S->reqs[(size_t)(id - S->base_id)].seq.size();
+            }
+            sl.cig.resize((size_t)bases / 8 + 64 * n + 1024);  // a few ops per kilobase; grown below if short
+            sl.off.resize(n + 1), sl.ins.resize(n), sl.st.resize(n);
+            int r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(), sl.st.data());
+            if (r == HG_ERR_CAPACITY) {  // rare: CIGARs longer than the first guess; the worst case fits
+                sl.cig.resize((size_t)bases + n * (size_t)(hg::index_length(S->ix) + 4));
+                r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(),
+                               sl.st.data());
+            }
+            if (r && r != HG_ERR_LENGTH_MISMATCH) {
+                fail_all(S, r, hg_last_error());
+                return;
+            }
+            const auto now = Clock::now();
+            {
+                std::lock_guard<std::mutex> lock(S->mu);
+                for (size_t j = 0; j < n; ++j) {
+                    Request& q = S->reqs[(size_t)(sl.ids[j] - S->base_id)];
+                    q.cigar.assign(sl.cig.begin() + sl.off[j], sl.cig.begin() + sl.off[j + 1]);
+                    q.status = sl.st[j];
+                    q.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_in).count();
+                    std::string().swap(q.seq);
+                    S->lat.push_back((float)q.latency_ms);
+                    S->done.push_back(sl.ids[j]);
+                }
+                S->bases_done += bases;
+                S->t_last = now;
+            }
+            S->cv_done.notify_all();
+            sl.ids.clear();
+            free_slots.push_back(s);
+            busy.erase(busy.begin() + (long)k);
+            progressed = true;
+        }
+        if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+}  // namespace
+
+extern "C" int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries, int64_t slot_bases,
+                               int64_t budget_bytes, hg_server_t** out)
+{
+    if (!ix || !out || n_slots <= 0 || slot_queries <= 0 || slot_bases <= 0 || budget_bytes <= 0)
+        return hg::set_error(HG_ERR_ARG, "hg_serve_create: bad arguments");
+    int dev = 0;
+    if (hg_index_device(ix, &dev, nullptr, 0) != HG_OK) return HG_ERR_ARG;
+    cudaSetDevice(dev);
+    auto* S = new hg_server();
+    S->ix = ix, S->device = dev, S->slot_q = slot_queries, S->slot_b = slot_bases;
+    for (int i = 0; i < n_slots; ++i) {
+        hg_ctx_t* c = nullptr;
+        const int64_t bytes = arena_of(ix, slot_queries, slot_bases, &c);
+        if (bytes < 0) {
+            hg_serve_destroy(S);
+            return (int)-bytes;
+        }
+        if (S->arena_bytes + bytes > budget_bytes) {  // the budget holds no more contexts
+            hg_ctx_destroy(c);
+            break;
+        }
+        S->arena_bytes += bytes;
+        S->slots.push_back(Slot{});
+        S->slots.back().ctx = c;
+    }
+    if (S->slots.empty()) {
+        hg_serve_destroy(S);
+        return hg::set_error(HG_ERR_CAPACITY, "hg_serve_create: one context does not fit the device-memory budget");
+    }
+    S->sched = std::thread(scheduler, S);
+    *out = S;
+    return HG_OK;
+}
+
+extern "C" void hg_serve_destroy(hg_server_t* S)
+{
+    if (!S) return;
+    {
+        std::lock_guard<std::mutex> lock(S->mu);
+        S->stop = true;
+        S->pending.clear();
+    }
+    S->cv_work.notify_all();
+    if (S->sched.joinable()) S->sched.join();
+    for (auto& sl : S->slots) hg_ctx_destroy(sl.ctx);
+    delete S;
+}
+
+extern "C" int64_t hg_serve_submit(hg_server_t* S, const char* seq, int64_t len)
+{
+    if (!S || len < 0 || (len > 0 && !seq)) return -hg::set_error(HG_ERR_ARG, "hg_serve_submit: bad arguments");
+    if (len > S->slot_b) return -hg::set_error(HG_ERR_CAPACITY, "hg_serve_submit: request longer than slot_bases");
+    int64_t id;
+    {
+        std::lock_guard<std::mutex> lock(S->mu);
+        if (S->error) return -hg::set_error(S->error, S->error_msg);
+        Request r;
+        r.seq.assign(seq, (size_t)len);
+        r.t_in = Clock::now();
+        if (!S->have_first) S->t_first = r.t_in, S->have_first = true;
+        id = S->base_id + (int64_t)S->reqs.size();
+        S->reqs.push_back(std::move(r));
+        S->pending.push_back(id);
+    }
+    S->cv_work.notify_one();
+    return id;
+}
+
+extern "C" int hg_serve_result(hg_server_t* S, int64_t* id, uint32_t* status, double* latency_ms, uint32_t* cigar,
+                               int64_t cap, int64_t* n_cigar, int timeout_ms)
+{
+    if (!S || !id) return -hg::set_error(HG_ERR_ARG, "hg_serve_result: bad arguments");
+    std::unique_lock<std::mutex> lock(S->mu);
+    auto ready = [&] { return !S->done.empty() || S->error; };
+    if (timeout_ms < 0) S->cv_done.wait(lock, ready);
+    else if (!S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), ready)) return 0;
+    if (S->done.empty()) return -hg::set_error(S->error, S->error_msg);
+    const int64_t rid = S->done.front();
+    S->done.pop_front();
+    Request& r = S->reqs[(size_t)(rid - S->base_id)];
+    *id = rid;
+    if (status) *status = r.status;
+    if (latency_ms) *latency_ms = r.latency_ms;
+    if (n_cigar) *n_cigar = (int64_t)r.cigar.size();
+    if (cigar && cap > 0) std::memcpy(cigar, r.cigar.data(), sizeof(uint32_t) * std::min<size_t>((size_t)cap, r.cigar.size()));
+    std::vector<uint32_t>().swap(r.cigar);
+    r.returned = true;
+    while (!S->reqs.empty() && S->reqs.front().returned) {  // the store keeps only unreturned requests
+        S->reqs.pop_front();
+        ++S->base_id;
+    }
+    return 1;
+}
+
+extern "C" int hg_serve_stats(hg_server_t* S, double* out, int n, int reset)
+{
+    if (!S || !out || n <= 0) return hg::set_error(HG_ERR_ARG, "hg_serve_stats: bad arguments");
+    std::lock_guard<std::mutex> lock(S->mu);
+    std::vector<float> v = S->lat;
+    double res[10] = {};
+    if (!v.empty()) {
+        std::sort(v.begin(), v.end());
+        auto pct = [&](double q) { return (double)v[std::min(v.size() - 1, (size_t)(q * (double)(v.size() - 1) + 0.5))]; };
+        double sum = 0;
+        for (float x : v) sum += x;
+        res[0] = pct(0.50), res[1] = pct(0.99), res[2] = sum / (double)v.size(), res[3] = v.back();
+    }
+    res[4] = (double)v.size(), res[5] = (double)S->bases_done, res[6] = (double)S->batches;
+    res[7] = S->have_first && !v.empty() ? std::chrono::duration<double>(S->t_last - S->t_first).count() : 0.0;
+    res[8] = (double)S->slots.size(), res[9] = (double)S->arena_bytes;
+    for (int i = 0; i < n && i < 10; ++i) out[i] = res[i];
+    if (reset) {
+        S->lat.clear();
+        S->bases_done = 0, S->batches = 0;
+        S->have_first = false;
+    }
+    return HG_OK;
+}
+
+extern "C" int hg_serve_counters(hg_server_t* S, uint32_t* counts7, uint32_t* ins, int reset)
+{
+    if (!S || !counts7 || !ins) return hg::set_error(HG_ERR_ARG, "hg_serve_counters: bad arguments");
+    const int64_t L = hg::index_length(S->ix);
+    std::vector<uint32_t> c((size_t)L * 7), i((size_t)L + 1);
+    std::fill(counts7, counts7 + 7 * L, 0u);
+    std::fill(ins, ins + L + 1, 0u);
+    for (auto& sl : S->slots) {  // uint32 sums wrap as SiteCount's counters do
+        const int r = hg_counters(sl.ctx, c.data(), i.data(), reset);
+        if (r) return r;
+        for (size_t k = 0; k < c.size(); ++k) counts7[k] += c[k];
+        for (size_t k = 0; k < i.size(); ++k) ins[k] += i[k];
+    }
+    return HG_OK;
+}

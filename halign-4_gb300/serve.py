@@ -154,3 +154,109 @@ class Server:
             tot_c = cnt if tot_c is None else tot_c + cnt
             tot_i = ins if tot_i is None else tot_i + ins
         return tot_c, tot_i
+
+
+class NativeServer:
+    """The same continuous-batching loop run by the library's scheduler thread
+    (hg_serve_*): Python only feeds requests at their arrival times and drains
+    results on a second thread, so the host path is native end to end.  The
+    device-memory budget caps the contexts created (their arenas are
+    allocated up front); every result carries its HG_ST_* status."""
+
+    STAT_KEYS = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "requests", "bases", "micro_batches", "wall_s",
+                 "contexts", "device_bytes")
+
+    def __init__(self, index: Index, n_slots: int = 8, slot_queries: int = 1024, slot_bases: int = 16_000_000,
+                 budget_bytes: int = 40 << 30):
+        import ctypes as C
+        from . import _check, lib
+        self._C, self._lib, self._check = C, lib(), _check
+        self.index = index
+        h = C.c_void_p()
+        _check(self._lib.hg_serve_create(index.h, n_slots, slot_queries, slot_bases, budget_bytes, C.byref(h)))
+        self.h = h
+
+    def stats(self, reset: bool = False) -> dict:
+        v = np.zeros(len(self.STAT_KEYS), np.float64)
+        self._check(self._lib.hg_serve_stats(self.h, v.ctypes.data_as(self._C.c_void_p), len(v), int(reset)))
+        return dict(zip(self.STAT_KEYS, (float(x) for x in v)))
+
+    def run(self, seqs: bytes, offsets: np.ndarray, arrivals: np.ndarray | None = None,
+            keep_results: bool = False) -> dict:
+        """Serve requests i = 0..n-1, submitted at arrivals[i] seconds (None:
+        all at once).  Returns the loop's statistics for these requests plus
+        per-request status (and CIGARs with keep_results)."""
+        import threading
+        C = self._C
+        n = len(offsets) - 1
+        self.stats(reset=True)
+        status = np.zeros(n, np.uint32)
+        results = {}
+        ids = np.full(n, -1, np.int64)
+        errors = []
+
+        def drain():
+            cap = 1 << 16
+            buf = np.zeros(cap, np.uint32)
+            rid, st, lat, nc = C.c_int64(), C.c_uint32(), C.c_double(), C.c_int64()
+            got = 0
+            while got < n:
+                r = self._lib.hg_serve_result(self.h, C.byref(rid), C.byref(st), C.byref(lat),
+                                              buf.ctypes.data_as(C.c_void_p), cap, C.byref(nc), 1000)
+                if r < 0:
+                    errors.append(-r)
+                    return
+                if r == 0:
+                    continue
+                got += 1
+                status[rid.value - base] = st.value
+                if keep_results:
+                    results[rid.value - base] = buf[: min(nc.value, cap)].copy()
+
+        base = None
+        t0 = time.perf_counter()
+        th = None
+        mv = memoryview(seqs)
+        for i in range(n):
+            if arrivals is not None:
+                wait = arrivals[i] - (time.perf_counter() - t0)
+                if wait > 0:
+                    time.sleep(wait)
+            rid = self._lib.hg_serve_submit(self.h, bytes(mv[offsets[i]:offsets[i + 1]]), int(offsets[i + 1] - offsets[i]))
+            if rid < 0:
+                self._check(-rid)
+            if base is None:
+                base = rid
+                th = threading.Thread(target=drain, daemon=True)
+                th.start()
+            ids[i] = rid
+        if th is not None:
+            th.join()
+        if errors:
+            self._check(errors[0])
+        out = self.stats()
+        out["status_or"] = int(np.bitwise_or.reduce(status)) if n else 0
+        out["mbp_per_s"] = out["bases"] / out["wall_s"] / 1e6 if out["wall_s"] > 0 else 0.0
+        out["status"] = status
+        out["results"] = results
+        return out
+
+    def counters(self, reset: bool = False):
+        L = self.index.L
+        cnt = np.zeros((L, 7), np.uint32)
+        ins = np.zeros(L + 1, np.uint32)
+        C = self._C
+        self._check(self._lib.hg_serve_counters(self.h, cnt.ctypes.data_as(C.c_void_p), ins.ctypes.data_as(C.c_void_p),
+                                                int(reset)))
+        return cnt, ins
+
+    def close(self):
+        if getattr(self, "h", None):
+            self._lib.hg_serve_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -174,6 +174,11 @@ int hg_set_timing(hg_ctx_t* ctx, int on);
  * the GPU; each keeps its own stream and arenas. */
 int hg_submit(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
               const int64_t* exc_off, int64_t n);
+/* hg_submit for ASCII queries (seqs[i], lens[i] bytes each): they are packed
+ * straight into the context's pinned staging (OpenMP over queries) instead of
+ * being packed by the caller and copied there, so a server's host work per
+ * request is one pass over its bytes. */
+int hg_submit_ascii(hg_ctx_t* ctx, const char* const* seqs, const int64_t* lens, int64_t n);
 int hg_poll(hg_ctx_t* ctx);
 int hg_collect(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
                uint32_t* status);
@@ -189,6 +194,41 @@ int hg_collect(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar
  * A test and debugging view of the batch kernels; no reference counterpart. */
 int hg_fetch_chain(hg_ctx_t* ctx, int64_t query, uint32_t* pos_ref, uint32_t* pos_qry, int32_t* f, int32_t* p,
                    int64_t cap, int64_t* n_anchors, int64_t* chain_end, int64_t* n_chain);
+
+/* ---- serving loop (continuous batching) ---------------------------------
+ * A request loop around one resident index: requests (one ASCII query each,
+ * copied at submission) wait in a FIFO; a scheduler thread fills every free
+ * context with the oldest waiting requests (up to slot_queries and
+ * slot_bases per micro-batch) and enqueues it asynchronously
+ * (hg_submit_ascii), polls the busy contexts and files each finished
+ * request's CIGAR and status for hg_serve_result.  Requests that arrive
+ * while others run join as contexts free up; micro-batches of different
+ * contexts overlap on the GPU.  The contexts' device arenas are allocated at
+ * creation; n_slots is reduced to what budget_bytes of device memory holds
+ * (at least one context must fit).  Submission and result calls are
+ * thread-safe.  HAlign-4 has no serving mode: this is the request-level use
+ * of the align-to-center path (RefAligner::globalAlign per request). */
+typedef struct hg_server hg_server_t;
+int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries, int64_t slot_bases, int64_t budget_bytes,
+                    hg_server_t** out);
+/* Stops the scheduler after the requests in flight finish, frees everything. */
+void hg_serve_destroy(hg_server_t* s);
+/* Queues one request; returns its id (0, 1, 2, ... in submission order) or a
+ * negative HG_ERR_* (HG_ERR_CAPACITY: longer than slot_bases). */
+int64_t hg_serve_submit(hg_server_t* s, const char* seq, int64_t len);
+/* The next finished request, waiting up to timeout_ms (< 0: no limit):
+ * returns 1 with *id, *status (HG_ST_* bits), *latency_ms (submission to
+ * result) and its CIGAR (*n_cigar ops; up to cap written, the rest dropped
+ * when cap is smaller), 0 on time-out, or a negative HG_ERR_*. */
+int hg_serve_result(hg_server_t* s, int64_t* id, uint32_t* status, double* latency_ms, uint32_t* cigar, int64_t cap,
+                    int64_t* n_cigar, int timeout_ms);
+/* Statistics since creation (or the last reset): out[0] p50 ms, [1] p99 ms,
+ * [2] mean ms, [3] max ms, [4] finished requests, [5] bases, [6] micro-
+ * batches, [7] seconds from the first submission to the last result,
+ * [8] contexts, [9] device bytes of their arenas. */
+int hg_serve_stats(hg_server_t* s, double* out, int n, int reset);
+/* Per-column counters summed over the server's contexts (hg_counters). */
+int hg_serve_counters(hg_server_t* s, uint32_t* counts7, uint32_t* ins, int reset);
 
 /* Consensus counters: counts7 = L x {A,C,G,T,U,N,-} (consensus::SiteCount,
  * include/consensus.h:78-99), ins = L+1 insertion events (slot c: I before

@@ -46,3 +46,34 @@ def test_resident_counters_cover_served_rows(gpu, pkg, serve_setup, oracle):
     cnt, ins = srv.counters()
     rows = np.stack([np.frombuffer(oracle.del_query(w.query(i), st.results[i]), np.uint8) for i in range(40)])
     assert np.array_equal(cnt, oracle.count_rows(rows))
+
+
+def test_native_server_results_identical_alone_and_in_the_mix(gpu, pkg, serve_setup):
+    """The library's own serving loop (hg_serve_*): every request's CIGAR in
+    the mix equals its CIGAR alone, statuses come back, and the resident
+    counters cover every served row."""
+    w, ix = serve_setup
+    srv = pkg.serve.NativeServer(ix, n_slots=3, slot_queries=32, slot_bases=600_000, budget_bytes=40 << 30)
+    out = srv.run(w.seqs, w.offsets, w.arrivals, keep_results=True)
+    assert out["requests"] == w.n and out["micro_batches"] > 3
+    assert out["status_or"] == 0 and out["p99_ms"] >= out["p50_ms"] > 0
+    alone_ctx = gpu.Context(ix, max_queries=1, max_bases=40_000)
+    for i in range(w.n):
+        b = gpu.pack(w.query(i), np.array([0, len(w.query(i))], np.int64))
+        assert np.array_equal(out["results"][i], alone_ctx.align(b, rows=False).cigar_of(0)), i
+    srv.close()
+
+
+def test_native_server_counters_and_budget(gpu, pkg, serve_setup, oracle):
+    w, ix = serve_setup
+    # a budget of one context's arenas creates one context only
+    probe = pkg.serve.NativeServer(ix, n_slots=1, slot_queries=16, slot_bases=400_000)
+    one = probe.stats()["device_bytes"]
+    probe.close()
+    srv = pkg.serve.NativeServer(ix, n_slots=4, slot_queries=16, slot_bases=400_000, budget_bytes=int(one * 1.5))
+    assert srv.stats()["contexts"] == 1
+    out = srv.run(w.seqs, w.offsets[:41], None, keep_results=True)
+    cnt, ins = srv.counters()
+    rows = np.stack([np.frombuffer(oracle.del_query(w.query(i), out["results"][i]), np.uint8) for i in range(40)])
+    assert np.array_equal(cnt, oracle.count_rows(rows))
+    srv.close()
