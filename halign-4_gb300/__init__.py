@@ -36,8 +36,9 @@ HG_OK = 0
 HG_ERR_LENGTH_MISMATCH = 5
 HG_ERR_CAPACITY = 4
 ST_ARENA_OVERFLOW, ST_PARTIAL_CIGAR, ST_CIGAR_OVERFLOW, ST_LENGTH_MISMATCH = 0x01, 0x02, 0x08, 0x10
-LAUNCH_KNOBS = ("seed", "anchor", "chain", "dp_small", "stitch", "rows")  # hg_ctx_set_launch order
-LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32))
+# hg_ctx_set_launch order: CTAs per SM of six stages, then two DP tier boundaries
+LAUNCH_KNOBS = ("seed", "anchor", "chain", "dp_small", "stitch", "rows", "thin_max_inner", "square_max_cells")
+LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32), (0, 32), (0, 12288))
 STAGES = ("seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count")
 
 
@@ -539,7 +540,7 @@ def project_row(qry, cigar, pad: bool = False) -> bytes:
 
 
 INT_PEAK_KEYS = ("int32_add_max_ops", "dpx_s32_ops", "dpx_s16x2_ops", "dpx_max3_s16x2_ops", "mul64_ops",
-                 "int_pipe_warp_inst")
+                 "int_pipe_warp_inst", "vsub2_ops", "vcmpgts2_ops")
 
 
 def int_peaks() -> dict:

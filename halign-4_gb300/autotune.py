@@ -1,9 +1,13 @@
-"""Autotuner for the launch shape of the batched stages.
+"""Autotuner for the launch shape of the batched stages and the DP tier
+boundaries.
 
 The stages run persistent grids (CTAs pulling queries or segments from atomic
 queues), so the grid size per SM trades occupancy against tail and queue
 contention, and the best point depends on the workload (query length, number
-of segments per query).  `tune` runs a coordinate descent over the
+of segments per query).  The two tier knobs move gap-fill segments between
+the thin, square and wavefront DP tiers (all bit-identical), trading one
+tier's latency tail against another's occupancy.  The band width is not a
+knob: bit-exactness fixes it to the reference's auto_band.  `tune` runs a coordinate descent over the
 CTAs-per-SM knobs of a context (`Context.set_launch`), scoring each candidate
 with `measure` (by default the CUDA-event time of a staged run of the batch
 already resident in the context) and keeping a change only when it is faster
@@ -32,6 +36,7 @@ def tune(measure: Callable[[Sequence[int]], float], start: Sequence[int],
          bounds: Sequence[tuple[int, int]] = LAUNCH_BOUNDS, rounds: int = 2, min_gain: float = 0.01):
     """Coordinate descent: returns (best knobs, best time, list of (knobs, time) tried)."""
     best = [int(x) for x in start]
+    bounds = list(bounds)[: len(best)]  # a shorter start tunes the leading knobs only
     best_t = measure(best)
     tried = [(list(best), best_t)]
     for _ in range(rounds):

@@ -258,6 +258,8 @@ struct BatchDev {
     int32_t* n_chain;
     int32_t* chain_meta;         // per query: best chain end (-1: none), first anchor whose speculated
                                  // predecessor was wrong (the anchor count if none); p is stored from there on
+    int32_t thin_max_inner;      // tier boundaries (launch knobs): longest query side of the thin tier,
+    int32_t square_max_cells;    // most cells of the square tier
     uint32_t* work_small;        // global segment ids per DP tier
     uint32_t* work_large;
     uint32_t* work_sorted;       // small tier sorted by shape_key (unused when work_rec is set)

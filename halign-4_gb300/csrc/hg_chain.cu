@@ -499,9 +499,9 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
                 kind = kSegMatch;  // identical equal-length sides: the DP's CIGAR is rl M
             else if (small_tier_fits(rl, ql) || medium_tier_fits(rl, ql))
                 kind = kSegDpSmall;
-            else if (thin_tier_fits(rl, ql))
+            else if (thin_tier_fits(rl, ql) && (int32_t)ql <= b.thin_max_inner)
                 kind = kSegDpThin;
-            else if (square_tier_fits(rl, ql))
+            else if (square_tier_fits(rl, ql) && (int64_t)rl * ql <= (int64_t)b.square_max_cells)
                 kind = kSegDpSquare;
             else
                 kind = kSegDpLarge;

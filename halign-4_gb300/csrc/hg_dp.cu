@@ -34,6 +34,7 @@
 
 #include "../../include/halign_gb300.h"
 #include "hg_batch.cuh"
+#include "hg_internal.h"
 
 namespace hg {
 
@@ -143,6 +144,33 @@ __device__ __forceinline__ uint32_t lane_int_z(int z0, int xt1, int vt1, int ut,
     if (MODE == 1) d |= (a > 0 ? 4u : 0u) | (b > 0 ? 8u : 0u);
     else d |= (a >= 0 ? 4u : 0u) | (b >= 0 ? 8u : 0u);
     return d;
+}
+
+// Two independent cells at once, one per 16-bit half (two segments of the
+// same shape and gap mode side by side): lane_int_z's recurrence on int16x2
+// SIMD operations, so one instruction updates both segments.  Every value
+// stays in [-32, 64], far inside int16.  Returns the two 4-bit direction
+// codes at bits 0-3 (low half) and 16-19 (high half).
+template <int MODE>
+__device__ __forceinline__ uint32_t lane16x2(uint32_t z0, uint32_t xt1, uint32_t vt1, uint32_t ut, uint32_t yt,
+                                             uint32_t& u, uint32_t& v, uint32_t& x, uint32_t& y)
+{
+    const uint32_t a0 = __vadd2(xt1, vt1), b0 = __vadd2(yt, ut);
+    const uint32_t m = __vmaxs2(z0, a0);
+    // MODE 1 (left-aligned): strict compares; MODE 2 (right-aligned): ties
+    // go the other way, i.e. >=
+    const uint32_t ca = MODE == 1 ? __vcmpgts2(a0, z0) : __vcmpges2(a0, z0);
+    const uint32_t c2 = MODE == 1 ? __vcmpgts2(b0, m) : __vcmpges2(b0, m);
+    const uint32_t z = __vmins2(__vmaxs2(m, b0), 0x00150015u);  // min(., 21)
+    u = __vsub2(z, vt1);
+    v = __vsub2(z, ut);
+    const uint32_t nzq = __vsub2(0x00060006u, z);                  // 6 - z = -(z - q)
+    const uint32_t a = __vadd2(a0, nzq), b = __vadd2(b0, nzq);
+    x = __vmaxs2(a, 0u);
+    y = __vmaxs2(b, 0u);
+    const uint32_t ce = MODE == 1 ? __vcmpgts2(a, 0u) : __vcmpges2(a, 0u);
+    const uint32_t cf = MODE == 1 ? __vcmpgts2(b, 0u) : __vcmpges2(b, 0u);
+    return (c2 & 0x00020002u) | (ca & ~c2 & 0x00010001u) | (ce & 0x00040004u) | (cf & 0x00080008u);
 }
 
 // 64 bases of 2-bit codes from base `pos` of a packed stream (base i at bits
@@ -271,6 +299,113 @@ __device__ __forceinline__ void small_segment(const IndexDev& ix, const BatchDev
     b.seg[r.sid].nops = n;
 }
 
+// Two FAST records of identical shape in one thread, one per 16-bit half
+// (lane16x2).  Direction codes: row o, inner position i at word
+// o * stride + i / 4, byte i % 4, the low nibble the first record's and the
+// high nibble the second's; words interleaved across the CTA as in
+// small_segment.  Each record's traceback then runs as small_segment's.
+template <bool TINNER, int MODE, int IMAX, int T>
+__device__ __forceinline__ void small_pair(const IndexDev& ix, const BatchDev& b, const SmallRec& r0,
+                                           const SmallRec& r1, uint32_t* dirs, int tid)
+{
+    constexpr int NW = (IMAX + 3) / 4;  // direction words per row at most
+    const int qn = (int)((r0.shape >> 8) & 0xffu), tn = (int)(r0.shape & 0xffu);
+    const int inner = TINNER ? tn : qn, outer = TINNER ? qn : tn;
+    const int stride = (inner + 3) >> 2;
+    uint32_t icp[IMAX], s1[IMAX], s2[IMAX];
+    uint64_t olo[2], ohi[2];
+    {
+        uint64_t qlo, qhi, tlo, thi, ilo[2];
+        for (int h = 0; h < 2; ++h) {
+            const SmallRec& r = h ? r1 : r0;
+            load_bases64(b.packed, r.qpos, qlo, qhi);
+            load_bases64(ix.center2, r.rs, tlo, thi);
+            ilo[h] = TINNER ? tlo : qlo;
+            olo[h] = TINNER ? qlo : tlo;
+            ohi[h] = TINNER ? qhi : thi;
+        }
+#pragma unroll
+        for (int i = 0; i < IMAX; ++i)
+            icp[i] = (uint32_t)((ilo[0] >> (2 * i)) & 3u) | (uint32_t)((ilo[1] >> (2 * i)) & 3u) << 16;
+    }
+#pragma unroll
+    for (int i = 0; i < IMAX; ++i) s1[i] = 0, s2[i] = 0;
+    const uint32_t k6 = 0x00060006u;
+    for (int o = 0; o < outer; ++o) {
+        const int sh = 2 * (o & 31);
+        const uint32_t ocp = (uint32_t)(((o < 32 ? olo[0] : ohi[0]) >> sh) & 3u) |
+                             (uint32_t)(((o < 32 ? olo[1] : ohi[1]) >> sh) & 3u) << 16;
+        uint32_t c1 = 0, c2 = o ? k6 : 0u;
+        uint32_t wd[NW];
+#pragma unroll
+        for (int k = 0; k < NW; ++k) wd[k] = 0;
+#pragma unroll
+        for (int i = 0; i < IMAX; ++i) {
+            if (i < inner) {
+                // z0 = 21 on a match, 12 on a mismatch, per half: 12 ^ (eq & (12 ^ 21))
+                const uint32_t z0 = (__vcmpeq2(icp[i], ocp) & 0x00190019u) ^ 0x000c000cu;
+                uint32_t u, v, x, y, d;
+                if (TINNER) {
+                    const uint32_t ut = o ? s1[i] : (i ? k6 : 0u), yt = o ? s2[i] : 0u;
+                    d = lane16x2<MODE>(z0, c1, c2, ut, yt, u, v, x, y);
+                    c1 = x, c2 = v, s1[i] = u, s2[i] = y;
+                } else {
+                    const uint32_t xt = o ? s1[i] : 0u, vt = o ? s2[i] : (i ? k6 : 0u);
+                    const uint32_t ut = i ? c1 : (o ? k6 : 0u), yt = i ? c2 : 0u;
+                    d = lane16x2<MODE>(z0, xt, vt, ut, yt, u, v, x, y);
+                    c1 = u, c2 = y, s1[i] = x, s2[i] = v;
+                }
+                wd[i >> 2] |= ((d | (d >> 12)) & 0xffu) << (8 * (i & 3));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NW; ++k)
+            if (k < stride) dirs[(o * stride + k) * T + tid] = wd[k];
+    }
+    for (int h = 0; h < 2; ++h) {
+        const SmallRec& r = h ? r1 : r0;
+        uint32_t* out = b.cig_seg + r.out;
+        int n = 0;
+        uint32_t run_op = 0xffu, run_len = 0;
+        auto push = [&](uint32_t op, uint32_t len) {
+            if (op == run_op) {
+                run_len += len;
+            } else {
+                if (run_len) out[n++] = run_len << 4 | run_op;
+                run_op = op, run_len = len;
+            }
+        };
+        int ti = tn - 1, qj = qn - 1, state = 0;
+        while (ti >= 0 && qj >= 0) {
+            const int o = TINNER ? qj : ti, i = TINNER ? ti : qj;
+            const uint32_t nib = (dirs[(o * stride + (i >> 2)) * T + tid] >> (8 * (i & 3) + 4 * h)) & 0xfu;
+            if (state == 0) state = nib & 3u;
+            else if (!((nib >> (state + 1)) & 1u)) state = 0;
+            if (state == 0) state = nib & 3u;
+            if (state == 0) push(0, 1), --ti, --qj;
+            else if (state == 1) push(2, 1), --ti;
+            else push(1, 1), --qj;
+        }
+        if (ti >= 0) push(2, (uint32_t)(ti + 1));
+        if (qj >= 0) push(1, (uint32_t)(qj + 1));
+        if (run_len) out[n++] = run_len << 4 | run_op;
+        b.seg[r.sid].nops = n;
+    }
+}
+
+template <int IMAX, int T>
+__device__ __forceinline__ void pair_dispatch(const IndexDev& ix, const BatchDev& b, const SmallRec& r0,
+                                              const SmallRec& r1, uint32_t* dirs, int tid, bool tinner, bool left)
+{
+    if (tinner) {
+        if (left) small_pair<true, 1, IMAX, T>(ix, b, r0, r1, dirs, tid);
+        else small_pair<true, 2, IMAX, T>(ix, b, r0, r1, dirs, tid);
+    } else {
+        if (left) small_pair<false, 1, IMAX, T>(ix, b, r0, r1, dirs, tid);
+        else small_pair<false, 2, IMAX, T>(ix, b, r0, r1, dirs, tid);
+    }
+}
+
 template <bool FAST, int IMAX, int T>
 __device__ __forceinline__ void small_dispatch(const IndexDev& ix, const BatchDev& b, const SmallRec& r,
                                                uint32_t* dirs, int tid, bool tinner, bool left)
@@ -284,28 +419,54 @@ __device__ __forceinline__ void small_dispatch(const IndexDev& ix, const BatchDe
     }
 }
 
-__global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
+// Small tier, two records per thread: consecutive records of the
+// shape-sorted list share their shape (rl, ql, gap mode, FAST) except at the
+// boundary between shapes, so a thread takes records 2w and 2w+1 and runs
+// them in the two halves of int16x2 registers (small_pair); a pair whose
+// shapes differ, or that has a record off the FAST path, runs as two single
+// records (small_segment).
+constexpr int kDpSmallPairThreads = 64;
+
+__global__ void __launch_bounds__(kDpSmallPairThreads) dp_small_kernel(IndexDev ix, BatchDev b)
 {
-    __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
+    constexpr int T = kDpSmallPairThreads;
+    __shared__ uint32_t dirs[2 * kSmallDirWords * T];
     const int tid = threadIdx.x;
     const unsigned total = min(b.queues2[1], b.queues2[3]);  // small shapes only
+    const unsigned npair = (total + 1u) / 2u;
     unsigned long long cell_sum = 0;
-    const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
-    for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
-        if (w >= total) continue;
-        const SmallRec r = b.work_rec[w];
-        const uint32_t rl = r.shape & 0xffu, ql = (r.shape >> 8) & 0xffu;
+    const unsigned wspan = (npair + 31u) & ~31u;  // whole warps iterate together for the shuffle
+    for (unsigned w = blockIdx.x * T + tid; w < wspan; w += gridDim.x * T) {
+        if (w >= npair) continue;
+        const SmallRec r0 = b.work_rec[2 * w];
+        const bool has1 = 2 * w + 1 < total;
+        SmallRec r1 = r0;
+        if (has1) r1 = b.work_rec[2 * w + 1];
+        const uint32_t rl = r0.shape & 0xffu, ql = (r0.shape >> 8) & 0xffu;
         const bool tinner = rl <= ql;
-        const bool left = (r.shape & kRecLeft) != 0;
+        const bool left = (r0.shape & kRecLeft) != 0;
         const uint32_t inner = tinner ? rl : ql;
-        if (r.shape & kRecFast) {
-            if (inner <= 4) small_dispatch<true, 4, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
-            else if (inner <= 8) small_dispatch<true, 8, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
-            else small_dispatch<true, 16, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
-        } else {
-            small_dispatch<false, 16, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+        if (has1 && r1.shape == r0.shape && (r0.shape & kRecFast)) {
+            if (inner <= 4) pair_dispatch<4, T>(ix, b, r0, r1, dirs, tid, tinner, left);
+            else if (inner <= 8) pair_dispatch<8, T>(ix, b, r0, r1, dirs, tid, tinner, left);
+            else pair_dispatch<16, T>(ix, b, r0, r1, dirs, tid, tinner, left);
+            cell_sum += 2ull * rl * ql;
+            continue;
         }
-        cell_sum += (unsigned long long)(rl * ql);
+        for (int h = 0; h < (has1 ? 2 : 1); ++h) {
+            const SmallRec& r = h ? r1 : r0;
+            const uint32_t hrl = r.shape & 0xffu, hql = (r.shape >> 8) & 0xffu;
+            const bool ht = hrl <= hql, hl = (r.shape & kRecLeft) != 0;
+            const uint32_t hin = ht ? hrl : hql;
+            if (r.shape & kRecFast) {
+                if (hin <= 4) small_dispatch<true, 4, T>(ix, b, r, dirs, tid, ht, hl);
+                else if (hin <= 8) small_dispatch<true, 8, T>(ix, b, r, dirs, tid, ht, hl);
+                else small_dispatch<true, 16, T>(ix, b, r, dirs, tid, ht, hl);
+            } else {
+                small_dispatch<false, 16, T>(ix, b, r, dirs, tid, ht, hl);
+            }
+            cell_sum += (unsigned long long)(hrl * hql);
+        }
     }
     for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
     if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
@@ -1683,7 +1844,8 @@ extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::Batc
     hg::shape_hist_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kShapeHistThreads, 0, st>>>(*b);
     hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
     hg::shape_scatter_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kScatterThreads, hg::kScatterSmem, st>>>(*ix, *b);
-    hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);
+    // half the threads per CTA of the single-record form, twice the CTAs
+    hg::dp_small_kernel<<<2 * grid, hg::kDpSmallPairThreads, 0, st>>>(*ix, *b);
     hg::dp_medium_kernel<<<grid, hg::kDpMedThreads, 0, st>>>(*ix, *b);
     return cudaGetLastError();
 }
@@ -1867,4 +2029,57 @@ extern "C" int hg_ksw_extz2_noalloc(int qlen, const uint8_t* d_query, int tlen, 
     hg::ksw_noalloc_kernel<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(a, scratch, d_cigar, (int)cap, d_ez);
     if (cudaGetLastError() != cudaSuccess) return noalloc_fail(err, err_cap, 1, "hg_ksw_extz2_noalloc: launch failed");
     return 0;
+}
+
+// ------------------------------------------------------------------------
+// Self-test of the packed cell: lane16x2 against lane_int_z over every input
+// the band-free tiers can feed a cell (z0 in {12, 16, 21}, x and y of the
+// neighbours in [0, 6], u and v in [0, 21]), both gap modes, each input in
+// the low half paired with another input in the high half.  Returns the
+// number of disagreeing (input, half) cases.
+namespace hg {
+__global__ void lane16x2_selftest_kernel(unsigned* bad)
+{
+    constexpr int NZ = 3, NX = 7, NV = 22;
+    const int total = NZ * NX * NV * NV * NX;
+    const int zs[NZ] = {12, 16, 21};
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < 2 * total; idx += gridDim.x * blockDim.x) {
+        const int mode = idx >= total ? 2 : 1;
+        int k = idx % total;
+        const int lo[5] = {zs[k % NZ], (k / NZ) % NX, (k / (NZ * NX)) % NV, (k / (NZ * NX * NV)) % NV,
+                           (k / (NZ * NX * NV * NV)) % NX};
+        k = (k * 7919 + 17) % total;  // another input for the high half
+        const int hi[5] = {zs[k % NZ], (k / NZ) % NX, (k / (NZ * NX)) % NV, (k / (NZ * NX * NV)) % NV,
+                           (k / (NZ * NX * NV * NV)) % NX};
+        uint32_t pk[5];
+        for (int j = 0; j < 5; ++j) pk[j] = (uint32_t)lo[j] | (uint32_t)hi[j] << 16;
+        uint32_t u2, v2, x2, y2;
+        const uint32_t d2 = mode == 1 ? lane16x2<1>(pk[0], pk[1], pk[2], pk[3], pk[4], u2, v2, x2, y2)
+                                      : lane16x2<2>(pk[0], pk[1], pk[2], pk[3], pk[4], u2, v2, x2, y2);
+        for (int h = 0; h < 2; ++h) {
+            const int* in = h ? hi : lo;
+            int u, v, x, y;
+            const uint32_t d = mode == 1 ? lane_int_z<1>(in[0], in[1], in[2], in[3], in[4], u, v, x, y)
+                                         : lane_int_z<2>(in[0], in[1], in[2], in[3], in[4], u, v, x, y);
+            const int sh = 16 * h;
+            const bool ok = ((d2 >> sh) & 0xfu) == d && (int)(int16_t)(u2 >> sh) == u &&
+                            (int)(int16_t)(v2 >> sh) == v && (int)(int16_t)(x2 >> sh) == x &&
+                            (int)(int16_t)(y2 >> sh) == y;
+            if (!ok) atomicAdd(bad, 1u);
+        }
+    }
+}
+}  // namespace hg
+
+extern "C" int hg_dp_lane_selftest(uint32_t* mismatches)
+{
+    if (!mismatches) return hg::set_error(HG_ERR_ARG, "hg_dp_lane_selftest: bad arguments");
+    unsigned* d = nullptr;
+    HG_CUDA(cudaMalloc(&d, sizeof(unsigned)));
+    cudaMemset(d, 0, sizeof(unsigned));
+    hg::lane16x2_selftest_kernel<<<304, 256>>>(d);
+    const cudaError_t e = cudaMemcpy(mismatches, d, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return hg::cuda_error(e, "hg_dp_lane_selftest");
+    return HG_OK;
 }

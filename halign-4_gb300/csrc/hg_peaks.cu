@@ -12,6 +12,8 @@
 //   [4] 64-bit multiply-add (splitmix64's multiplies), ops = 1
 //   [5] integer-pipe warp instructions per second: [1]'s kernel issues one
 //       instruction per step and chain
+//   [6] __vsub2 (16x2 subtract, plus one xor per step), lane ops = 2
+//   [7] __vcmpgts2 (16x2 signed compare to masks, plus one add), lane ops = 2
 // The chains feed on values loaded at run time and the results are stored,
 // so nothing folds away.  Measured on GB300 (ncu instruction counts): the
 // compiler fuses [0]'s add and max into one integer-pipe instruction, so [0]
@@ -109,6 +111,40 @@ __global__ void __launch_bounds__(256) peak_mul64(const int32_t* in, int32_t* ou
     out[blockIdx.x * blockDim.x + threadIdx.x] = (int32_t)(s ^ (s >> 32));
 }
 
+// 16x2 SIMD add / subtract / compare without DPX: the other operations a
+// packed DP cell needs.
+__global__ void __launch_bounds__(256) peak_vsub2(const int32_t* in, int32_t* out)
+{
+    unsigned x[kPeakChains];
+    const unsigned k = (unsigned)in[threadIdx.x & 7];
+#pragma unroll
+    for (int i = 0; i < kPeakChains; ++i) x[i] = (unsigned)in[16 + i] + threadIdx.x;
+    for (int it = 0; it < kPeakIters; ++it) {
+#pragma unroll
+        for (int i = 0; i < kPeakChains; ++i) x[i] = __vsub2(x[(i + 1) & 7], x[i] ^ k);
+    }
+    unsigned s = 0;
+#pragma unroll
+    for (int i = 0; i < kPeakChains; ++i) s ^= x[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = (int32_t)s;
+}
+
+__global__ void __launch_bounds__(256) peak_vcmpgt2(const int32_t* in, int32_t* out)
+{
+    unsigned x[kPeakChains];
+    const unsigned k = (unsigned)in[threadIdx.x & 7];
+#pragma unroll
+    for (int i = 0; i < kPeakChains; ++i) x[i] = (unsigned)in[16 + i] + threadIdx.x;
+    for (int it = 0; it < kPeakIters; ++it) {
+#pragma unroll
+        for (int i = 0; i < kPeakChains; ++i) x[i] = __vcmpgts2(x[(i + 1) & 7], x[i]) + k;
+    }
+    unsigned s = 0;
+#pragma unroll
+    for (int i = 0; i < kPeakChains; ++i) s ^= x[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = (int32_t)s;
+}
+
 }  // namespace hg
 
 extern "C" int hg_int_peaks(double* out, int n)
@@ -136,13 +172,16 @@ extern "C" int hg_int_peaks(double* out, int n)
         return hg::set_error(HG_ERR_CUDA, "hg_int_peaks: upload");
     }
     using K = void (*)(const int32_t*, int32_t*);
-    const K kernels[5] = {hg::peak_add_max, hg::peak_dpx_s32, hg::peak_dpx_s16x2, hg::peak_max3_s16x2,
-                          hg::peak_mul64};
-    // element operations per inner step per chain
-    const double ops[5] = {2.0, 2.0, 4.0, 4.0, 1.0};
-    const double iters[5] = {hg::kPeakIters, hg::kPeakIters, hg::kPeakIters, hg::kPeakIters, hg::kPeakIters / 4};
-    double res[6] = {};
-    for (int k = 0; k < 5 && rc == HG_OK; ++k) {
+    const K kernels[7] = {hg::peak_add_max, hg::peak_dpx_s32, hg::peak_dpx_s16x2, hg::peak_max3_s16x2,
+                          hg::peak_mul64, hg::peak_vsub2, hg::peak_vcmpgt2};
+    // element operations per inner step per chain (the last two: one xor or
+    // add each, counted as the 16x2 operation's two lanes only)
+    const double ops[7] = {2.0, 2.0, 4.0, 4.0, 1.0, 2.0, 2.0};
+    const double iters[7] = {hg::kPeakIters, hg::kPeakIters, hg::kPeakIters, hg::kPeakIters, hg::kPeakIters / 4,
+                             hg::kPeakIters, hg::kPeakIters};
+    double res[9] = {};
+    const int slot[7] = {0, 1, 2, 3, 4, 6, 7};
+    for (int k = 0; k < 7 && rc == HG_OK; ++k) {
         kernels[k]<<<blocks, threads>>>(d_in, d_out);  // warm-up
         float best = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
@@ -157,10 +196,10 @@ extern "C" int hg_int_peaks(double* out, int n)
             cudaEventElapsedTime(&ms, e0, e1);
             best = ms < best ? ms : best;
         }
-        res[k] = (double)blocks * threads * hg::kPeakChains * iters[k] * ops[k] / (best * 1e-3);
+        res[slot[k]] = (double)blocks * threads * hg::kPeakChains * iters[k] * ops[k] / (best * 1e-3);
     }
     res[5] = res[1] / 2.0 / 32.0;  // one instruction (two element ops) per lane and step, 32 lanes per warp
     cleanup();
-    for (int i = 0; i < n && i < 6; ++i) out[i] = res[i];
+    for (int i = 0; i < n && i < 8; ++i) out[i] = res[i];
     return rc;
 }

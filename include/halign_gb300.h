@@ -129,10 +129,15 @@ int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* 
                     uint8_t* rows, int64_t row_stride, uint32_t* status);
 /* Launch shape of the sub-batch stages, in CTAs per SM: [0] seed (1..32),
  * [1] anchor (1..6), [2] chain (1..64), [3] dp_small (1..32), [4] stitch
- * (1..32), [5] rows (1..32).  Defaults 6 6 12 12 8 6.  Setting them drops the
- * context's cached CUDA graphs (the autotuner, halign-4_gb300/autotune.py,
- * searches them).  No reference counterpart: launch geometry. */
-#define HG_LAUNCH_KNOBS 6
+ * (1..32), [5] rows (1..32); and two DP tier boundaries: [6] the longest
+ * query side the thin tier takes (0..32; 0 switches the tier off), [7] the
+ * most cells the square tier takes (0..12288).  Segments a tier declines go
+ * to the next one (thin, square, then the wavefront or exact tiers); every
+ * tier computes the same alignment, so the knobs change speed only.
+ * Defaults 6 6 12 12 8 6 32 12288.  Setting them drops the context's cached
+ * CUDA graphs (the autotuner, halign-4_gb300/autotune.py, searches them).
+ * No reference counterpart: launch geometry. */
+#define HG_LAUNCH_KNOBS 8
 int hg_ctx_set_launch(hg_ctx_t* ctx, const int32_t* ctas_per_sm, int n);
 int hg_ctx_get_launch(const hg_ctx_t* ctx, int32_t* ctas_per_sm, int n);
 
@@ -158,10 +163,16 @@ int hg_staged_flags(hg_ctx_t* ctx, uint32_t* flags);
  * full-grid kernels (about 20 ms in all): out[0] int32 add + max element
  * operations per second, out[1] DPX max(a + b, c) on int32, out[2] the same
  * on int16x2, out[3] DPX three-way max on int16x2, out[4] 64-bit
- * multiply-adds, out[5] integer-pipe warp instructions per second.
- * n <= 6 values are written.  The roofline of this integer path; no
+ * multiply-adds, out[5] integer-pipe warp instructions per second, out[6]
+ * int16x2 subtracts, out[7] int16x2 compares.  n <= 8 values are written.  The roofline of this integer path; no
  * reference counterpart. */
 int hg_int_peaks(double* out, int n);
+
+/* Self-test of the small DP tier's two-cells-per-instruction form (int16x2
+ * SIMD): every input a band-free cell can see, both gap modes, against the
+ * int32 cell; *mismatches gets the disagreeing cases (0 expected).  Test
+ * support; no reference counterpart. */
+int hg_dp_lane_selftest(uint32_t* mismatches);
 
 /* Enable per-stage event timing for staged runs (off by default). */
 int hg_set_timing(hg_ctx_t* ctx, int on);

@@ -260,3 +260,33 @@ def test_extend_align_vs_oracle(gpu, oracle, pkg):
         w = oracle.auto_band(len(ref), len(qry))
         _, want = oracle.ksw_extz2(dna5[qry], dna5[ref], 5, MAT, 6, 2, w, zd, 50, 0x40 | 0x02 | 0x10)
         assert np.array_equal(out[:n], want), it
+
+
+def test_packed_dp_cell_equals_int32_cell(gpu):
+    """The small tier's int16x2 cell (two segments per instruction) against
+    the int32 cell over every input a band-free cell can see, both gap
+    modes, with different inputs in the two halves."""
+    import ctypes as C
+    L = gpu.lib()
+    L.hg_dp_lane_selftest.argtypes = [C.c_void_p]
+    bad = C.c_uint32(123)
+    gpu._check(L.hg_dp_lane_selftest(C.byref(bad)))
+    assert bad.value == 0
+
+
+@pytest.mark.parametrize("name,n", [("divergent", 60), ("uneven", 120), ("serve", 40)])
+def test_tier_boundary_knobs_do_not_change_results(gpu, pkg, name, n):
+    """The thin and square tiers switched off, or narrowed, move their
+    segments to other tiers: the CIGARs stay identical."""
+    w = getattr(pkg.synth, name)(n)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=n, max_bases=int(w.total_bases) + 1024)
+    b = gpu.pack(w.seqs, w.offsets)
+    base = ctx.align(b, rows=True)
+    default = ctx.get_launch()
+    for thin, sq in ((0, 0), (8, 2000), (32, 0), (0, 12288)):
+        ctx.set_launch(default[:6] + [thin, sq])
+        got = ctx.align(b, rows=True)
+        assert np.array_equal(got.cigar, base.cigar) and np.array_equal(got.cigar_off, base.cigar_off), (thin, sq)
+        assert np.array_equal(got.rows, base.rows)
+    ctx.set_launch(default)
