@@ -138,6 +138,7 @@ def lib() -> C.CDLL:
     L.hg_count_rows.argtypes = [vp, i64, i64, i64, vp, i32]
     L.hg_int_peaks.argtypes = [vp, i32]
     L.hg_submit_ascii.argtypes = [vp, vp, vp, i64]
+    L.hg_align_fasta.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, i32, i32, i64, vp]
     L.hg_serve_create.argtypes = [vp, i32, i64, i64, i64, C.POINTER(vp)]
     L.hg_serve_destroy.argtypes = [vp]
     L.hg_serve_submit.argtypes = [vp, C.c_char_p, i64]
@@ -559,6 +560,17 @@ def extend_align_ksw2(ref, qry, zdrop: int = 200) -> np.ndarray:
     if n < 0:
         _check(-n)
     return c[:n].copy()
+
+
+def align_fasta(center_fasta, queries_fasta, out_fasta, k: int = 15, w: int = 10,
+                chunk_queries: int = 50000) -> int:
+    """Aligned FASTA of a query FASTA against the first record of a center
+    FASTA, in the reference CLI's --keep-length output order (hg_align_fasta).
+    Returns the number of queries aligned."""
+    n = C.c_int64()
+    _check(lib().hg_align_fasta(str(center_fasta).encode(), str(queries_fasta).encode(), str(out_fasta).encode(),
+                                k, w, chunk_queries, C.byref(n)))
+    return n.value
 
 
 def count_rows(rows: np.ndarray, counts: np.ndarray | None = None) -> np.ndarray:

@@ -1,0 +1,244 @@
+// hg_fasta.cpp - streaming FASTA in, aligned FASTA out (hg_align_fasta):
+// the file edge of the align-to-center path with the reader, the GPU and
+// the writer overlapped.
+//
+// A reader thread parses the query FASTA into chunks (HAlign-4's
+// KseqReader::next, src/utils/seq_io.cpp:134-155: sequence lines joined,
+// a trailing '\r' dropped), the calling thread packs each chunk (hg_pack)
+// and aligns it with rows (hg_align_batch), and a writer thread writes the
+// rows in the reference's output order (mergeAlignedResults with
+// --keep-length, src/align/ref_aligner.cpp:676-740): the center record,
+// then every row whose CIGAR has an insertion, then every other row, each
+// group in input order.  Insertion rows go straight to the output; the
+// others go to a side file appended at the end, so nothing is held in
+// memory beyond two chunks.
+#include <algorithm>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/halign_gb300.h"
+#include "hg_internal.h"
+
+namespace {
+
+struct Chunk {
+    std::vector<std::string> names;
+    std::string seqs;
+    std::vector<int64_t> offs{0};
+    // alignment results
+    std::vector<uint8_t> rows, has_ins;
+    int64_t stride = 0;
+    bool last = false;
+};
+
+template <typename T>
+class Queue {  // bounded hand-off between two threads
+public:
+    explicit Queue(size_t cap) : cap_(cap) {}
+    void push(T v)
+    {
+        std::unique_lock<std::mutex> l(mu_);
+        not_full_.wait(l, [&] { return q_.size() < cap_; });
+        q_.push_back(std::move(v));
+        not_empty_.notify_one();
+    }
+    T pop()
+    {
+        std::unique_lock<std::mutex> l(mu_);
+        not_empty_.wait(l, [&] { return !q_.empty(); });
+        T v = std::move(q_.front());
+        q_.pop_front();
+        not_full_.notify_one();
+        return v;
+    }
+
+private:
+    size_t cap_;
+    std::deque<T> q_;
+    std::mutex mu_;
+    std::condition_variable not_full_, not_empty_;
+};
+
+// Record reader with kseq's FASTA conventions: the header's first word is
+// the name, the rest the description; sequence lines are joined.
+class Reader {
+public:
+    explicit Reader(const char* path) : f_(path, std::ios::binary) {}
+    bool ok() const { return (bool)f_; }
+    bool next(std::string& name, std::string& desc, std::string& seq)
+    {
+        std::string line;
+        if (pending_.empty()) {
+            while (std::getline(f_, line))
+                if (!line.empty() && line[0] == '>') {
+                    pending_ = line;
+                    break;
+                }
+            if (pending_.empty()) return false;
+        }
+        std::string head = pending_.substr(1);
+        pending_.clear();
+        if (!head.empty() && head.back() == '\r') head.pop_back();
+        const size_t sp = head.find_first_of(" \t");
+        name = head.substr(0, sp);
+        desc = sp == std::string::npos ? std::string() : head.substr(head.find_first_not_of(" \t", sp));
+        seq.clear();
+        while (std::getline(f_, line)) {
+            if (!line.empty() && line[0] == '>') {
+                pending_ = line;
+                break;
+            }
+            seq += line;
+            if (seq.size() > 1 && seq.back() == '\r') seq.pop_back();
+        }
+        return true;
+    }
+
+private:
+    std::ifstream f_;
+    std::string pending_;
+};
+
+}  // namespace
+
+extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k,
+                              int w, int64_t chunk_queries, int64_t* n_aligned)
+{
+    if (!center_fasta || !queries_fasta || !out_fasta || chunk_queries <= 0)
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: bad arguments");
+    Reader cr(center_fasta);
+    std::string cname, cdesc, cseq;
+    if (!cr.ok() || !cr.next(cname, cdesc, cseq) || cseq.empty())
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: no center record in " + std::string(center_fasta));
+    hg_index_t* ix = nullptr;
+    int r = hg_index_create(cseq.data(), (int64_t)cseq.size(), k, w, nullptr, &ix);
+    if (r) return r;
+    const int64_t L = (int64_t)cseq.size();
+    Reader qr(queries_fasta);
+    if (!qr.ok()) {
+        hg_index_destroy(ix);
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: cannot read " + std::string(queries_fasta));
+    }
+    std::ofstream out(out_fasta, std::ios::binary);
+    const std::string rest_path = std::string(out_fasta) + ".rest";
+    std::ofstream rest(rest_path, std::ios::binary);
+    if (!out || !rest) {
+        hg_index_destroy(ix);
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: cannot write " + std::string(out_fasta));
+    }
+    out << '>' << cname << (cdesc.empty() ? "" : " ") << cdesc << '\n' << cseq << '\n';
+    // reader thread
+    Queue<Chunk> in_q(2), out_q(2);
+    std::thread reader([&] {
+        std::string name, desc, seq;
+        for (;;) {
+            Chunk c;
+            bool more = true;
+            while ((int64_t)c.names.size() < chunk_queries && (more = qr.next(name, desc, seq))) {
+                c.names.push_back(name);
+                c.seqs += seq;
+                c.offs.push_back((int64_t)c.seqs.size());
+            }
+            c.last = !more;
+            const bool last = c.last;
+            in_q.push(std::move(c));
+            if (last) return;
+        }
+    });
+    // writer thread: insertion rows to the output, the others to the side file
+    std::thread writer([&] {
+        for (;;) {
+            Chunk c = out_q.pop();
+            for (size_t i = 0; i < c.names.size(); ++i) {
+                std::ofstream& o = c.has_ins[i] ? out : rest;
+                o.put('>');
+                o << c.names[i];
+                o.put('\n');
+                o.write(reinterpret_cast<const char*>(c.rows.data()) + i * c.stride, (std::streamsize)L);
+                o.put('\n');
+            }
+            if (c.last) return;
+        }
+    });
+    // align chunk by chunk
+    hg_ctx_t* ctx = nullptr;
+    int64_t ctx_bases = 0;
+    int64_t total = 0;
+    int rc = HG_OK;
+    std::string err;
+    for (bool last = false; !last;) {
+        Chunk c = in_q.pop();
+        last = c.last;
+        const int64_t n = (int64_t)c.names.size();
+        if (n > 0 && rc == HG_OK) {
+            int64_t maxlen = 0;
+            for (int64_t i = 0; i < n; ++i) maxlen = std::max(maxlen, c.offs[i + 1] - c.offs[i]);
+            // sub-batches of the chunk hold about chunk_queries center-length
+            // queries; a longer query than the context holds gets a new one
+            if (!ctx || maxlen > ctx_bases) {
+                if (ctx) hg_ctx_destroy(ctx), ctx = nullptr;
+                // (at most ~0.9 Gbp per sub-batch: the arenas scale with it)
+                ctx_bases = std::max<int64_t>(std::min<int64_t>(chunk_queries * (L + L / 4 + 64), 900000000),
+                                              2 * maxlen);
+                rc = hg_ctx_create(ix, chunk_queries, ctx_bases, &ctx);
+            }
+            int64_t pb = 0, ne = 0;
+            std::vector<uint8_t> packed;
+            std::vector<int64_t> poff((size_t)n), eoff((size_t)n + 1);
+            std::vector<int32_t> exc, qlen((size_t)n);
+            if (rc == HG_OK) rc = hg_pack(c.seqs.data(), c.offs.data(), n, nullptr, 0, nullptr, nullptr, 0, nullptr, &pb, &ne);
+            if (rc == HG_OK) {
+                packed.resize((size_t)std::max<int64_t>(pb, 16));
+                exc.resize((size_t)std::max<int64_t>(ne, 1) * 3);
+                rc = hg_pack(c.seqs.data(), c.offs.data(), n, packed.data(), (int64_t)packed.size(), poff.data(),
+                             exc.data(), ne, eoff.data(), nullptr, nullptr);
+            }
+            if (rc == HG_OK) {
+                for (int64_t i = 0; i < n; ++i) qlen[i] = (int32_t)(c.offs[i + 1] - c.offs[i]);
+                c.stride = (L + 15) / 16 * 16;
+                c.rows.resize((size_t)(n * c.stride));
+                c.has_ins.resize((size_t)n);
+                std::vector<int64_t> coff((size_t)n + 1);
+                std::vector<uint32_t> st((size_t)n);
+                std::vector<uint32_t> cig((size_t)(c.seqs.size() / 8 + 64 * n + 1024));
+                rc = hg_align_batch(ctx, packed.data(), poff.data(), qlen.data(), exc.data(), eoff.data(), n,
+                                    cig.data(), (int64_t)cig.size(), coff.data(), c.has_ins.data(), c.rows.data(),
+                                    c.stride, st.data());
+                if (rc == HG_ERR_CAPACITY) {  // CIGARs longer than the first guess: the worst case fits
+                    cig.resize((size_t)(c.seqs.size() + n * (L + 4)));
+                    rc = hg_align_batch(ctx, packed.data(), poff.data(), qlen.data(), exc.data(), eoff.data(), n,
+                                        cig.data(), (int64_t)cig.size(), coff.data(), c.has_ins.data(), c.rows.data(),
+                                        c.stride, st.data());
+                }
+            }
+            if (rc) err = hg_last_error();
+            else total += n;
+        }
+        if (rc) {  // keep the threads moving; the output is abandoned
+            c.names.clear();
+        }
+        std::string().swap(c.seqs);
+        out_q.push(std::move(c));
+    }
+    reader.join();
+    writer.join();
+    if (ctx) hg_ctx_destroy(ctx);
+    hg_index_destroy(ix);
+    rest.close();
+    if (rc == HG_OK) {  // the rows without insertions follow the insertion rows
+        std::ifstream in(rest_path, std::ios::binary);
+        if (in.peek() != std::ifstream::traits_type::eof()) out << in.rdbuf();
+    }
+    out.close();
+    std::remove(rest_path.c_str());
+    if (rc) return hg::set_error(rc, err);
+    if (n_aligned) *n_aligned = total;
+    return out ? HG_OK : hg::set_error(HG_ERR_ARG, "hg_align_fasta: write failed");
+}

@@ -206,6 +206,20 @@ int hg_collect(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar
 int hg_fetch_chain(hg_ctx_t* ctx, int64_t query, uint32_t* pos_ref, uint32_t* pos_qry, int32_t* f, int32_t* p,
                    int64_t cap, int64_t* n_anchors, int64_t* chain_end, int64_t* n_chain);
 
+/* ---- files: query FASTA in, aligned FASTA out ---------------------------
+ * The align-to-center run of the reference CLI with --keep-length
+ * (halign4 -c center.fa -i queries.fa --keep-length), streamed: the first
+ * record of center_fasta is the center (k, w: --kmer-size, --kmer-window);
+ * queries are read in chunks of chunk_queries records (KseqReader::next,
+ * src/utils/seq_io.cpp:134-155), aligned with rows on the GPU while the next
+ * chunk is read and the previous one written, and written in the reference's
+ * order (src/align/ref_aligner.cpp:676-740): the center record, then every
+ * row with an insertion, then the others, each group in input order, one
+ * line per row.  *n_aligned (may be NULL) gets the query count.  Errors as
+ * hg_align_batch's (HG_ERR_LENGTH_MISMATCH where the reference throws). */
+int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k, int w,
+                   int64_t chunk_queries, int64_t* n_aligned);
+
 /* ---- serving loop (continuous batching) ---------------------------------
  * A request loop around one resident index: requests (one ASCII query each,
  * copied at submission) wait in a FIFO; a scheduler thread fills every free

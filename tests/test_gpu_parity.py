@@ -430,3 +430,18 @@ def test_low_complexity_vs_oracle(gpu, oracle, pkg):
     res = ctx.align(gpu.pack(seqs, offs), rows=False, check=False)
     for i, q in enumerate(cases):
         assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
+
+
+@pytest.mark.parametrize("chunk", [1000, 237])
+def test_streamed_fasta_identical_to_reference_cli(gpu, pkg, golden, tmp_path, chunk):
+    """FASTA files in, aligned FASTA out, streamed in chunks (the reader, the
+    GPU and the writer overlapped): byte-identical to the reference CLI's
+    output on the 1,000 mito queries, whatever the chunk size."""
+    w = pkg.synth.mito(1000)
+    pkg.synth.write_fasta(str(tmp_path), "center", w.center, w, "synthetic mito center seed0")
+    out = tmp_path / "out.fa"
+    n = gpu.align_fasta(tmp_path / "center.fa", tmp_path / "queries.fa", out, 15, 10, chunk)
+    assert n == 1000
+    data = out.read_bytes()
+    assert len(data) == golden.meta["mito1000_cli_fasta_bytes"]
+    assert hashlib.sha256(data).hexdigest() == golden.meta["mito1000_cli_fasta_sha256"]
