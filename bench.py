@@ -447,6 +447,92 @@ def run_stream(args, pkg):
     return 0
 
 
+def _oracle_check_multiref(args_tuple):
+    refs, queries, bests, cigs = args_tuple
+    from oracle.oracle import Oracle
+    o = Oracle()
+    sks = [o.sketch(r) for r in refs]
+    mz = [o.extract_minimizer(r) for r in refs]
+    bad_b = bad_c = 0
+    for q, b, c in zip(queries, bests, cigs):
+        ob, _ = o.best_reference(o.sketch(q), sks)
+        bad_b += int(ob != b)
+        bad_c += int(not np.array_equal(o.align_query(refs[ob], mz[ob][0], mz[ob][1], q), c))
+    return bad_b, bad_c, len(queries)
+
+
+def run_multiref(args, pkg):
+    """Multi-reference mode (several references of one length, each query
+    aligned to its best reference by MinHash jaccard): the device selection
+    alone (sketch + jaccard over the resident reference sketches, one
+    launch, CUDA events) and end to end through hg_refset_align with host
+    buffers (H2D, selection, per-reference batches, rows back), with an
+    oracle check of a sample (best reference and CIGAR)."""
+    import multiprocessing as mp
+    pool = mp.get_context("spawn").Pool(max(1, (os.cpu_count() or 2) - 2))
+    n, n_refs = args.queries, args.refs
+    w = pkg.synth.multiref(n, n_refs=n_refs, ref_len=16569)
+    sub = min(n, 50_000)
+    rs = pkg.RefSet(w.refs, max_queries=sub, max_bases=sub * 16700)
+    b = pkg.pack(w.seqs, w.offsets)
+    k = 15
+    kmers = int(np.maximum(b.qlen.astype(np.int64) - k + 1, 0).sum())
+    for _ in range(args.warmup):
+        rs.select(b)
+    sel_ms = []
+    for _ in range(args.steps):
+        best, jac = rs.select(b)
+        sel_ms.append(rs.last_select_ms())
+    t0 = time.perf_counter()
+    res = rs.align(b, keep_length=True, rows=True)
+    t_keep = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res_c = rs.align(b, keep_length=False, rows=True)
+    t_cons = time.perf_counter() - t0
+    idx = list(range(0, n, max(1, n // max(1, args.check_sample))))[: args.check_sample]
+    pending = [pool.apply_async(_oracle_check_multiref, ((w.refs, [w.query(i) for i in idx[a:a + 50]],
+                                                          [int(res.best[i]) for i in idx[a:a + 50]],
+                                                          [res.cigar_of(i).copy() for i in idx[a:a + 50]]),))
+               for a in range(0, len(idx), 50)]
+    bad_b = bad_c = n_chk = 0
+    for r in pending:
+        x, y, z = r.get()
+        bad_b, bad_c, n_chk = bad_b + x, bad_c + y, n_chk + z
+    pool.close()
+    ms = float(np.median(sel_ms))
+    # the oracle's sketch + selection on one host core, over a sample
+    from oracle.oracle import Oracle
+    o = Oracle()
+    sks = [o.sketch(r) for r in w.refs]
+    t0, cb = time.perf_counter(), 0
+    for i in range(0, min(n, 300)):
+        o.best_reference(o.sketch(w.query(i)), sks)
+        cb += len(w.query(i))
+    cpu_sel = cb / (time.perf_counter() - t0) / 1e6
+    line = {"metric": "multi-reference selection and alignment", "mode": "multiref", "unit": "Mbp/s",
+            "config": {"workload": f"multiref: {n} queries x ~16,569 bp, {n_refs} references of 16,569 bp "
+                                   "(3% substitution variants of one center), queries 1% sub, 0.1%+0.1% indels; "
+                                   "k=15, w=10, sketch size 2000, seed 42",
+                       "queries": n, "bases": b.bases, "kmers": kmers},
+            "select_kernel": {"ms": round(ms, 3), "mbp_per_s": round(b.bases / ms / 1e3, 3),
+                              "kmer_hashes_per_s": round(kmers / ms * 1e3, 1),
+                              "input_gb_per_s": round(b.packed.nbytes / ms / 1e6, 3),
+                              "timing": "CUDA events around the one sketch + selection launch, median of steps"},
+            "cpu_baseline_select": {"value": round(cpu_sel, 3), "unit": "Mbp/s", "cores": 1, "kind": "port",
+                                    "sample": "sketch + best reference of the first 300 queries"},
+            "e2e_keep_length": {"mbp_per_s": round(b.bases / t_keep / 1e6, 3), "s": round(t_keep, 3),
+                                "timed": "hg_refset_align with host buffers: upload, selection, one batch per "
+                                         "reference, rows back"},
+            "e2e_consensus_recheck": {"mbp_per_s": round(b.bases / t_cons / 1e6, 3), "s": round(t_cons, 3)},
+            "chosen_reference_counts": np.bincount(res.best, minlength=n_refs).tolist(),
+            "parity_sample": {"checked_queries": n_chk, "best_ref_mismatches": bad_b, "cigar_mismatches": bad_c,
+                              "status_or": int(np.bitwise_or.reduce(res.status)) | int(np.bitwise_or.reduce(
+                                  res_c.status)), "against": "oracle sketch/jaccard selection and CIGAR"}}
+    rs.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_impl_reference(args, rank, world):
     """The reference's CPU path (the oracle restatement) on the host cores."""
     if rank != 0:
@@ -502,6 +588,9 @@ def main():
     ap.add_argument("--stream-chunk", type=int, default=0,
                     help="stream the workload in generated chunks of this many queries and check a full-size "
                          "sample against the oracle (the stated-size checks)")
+    ap.add_argument("--multiref", action="store_true",
+                    help="multi-reference mode: device selection and per-reference alignment (--queries, --refs)")
+    ap.add_argument("--refs", type=int, default=4)
     ap.add_argument("--serve-million", action="store_true",
                     help="serve --serve-requests requests (10^6 stated) and check the resident counters")
     ap.add_argument("--check-sample", type=int, default=10000,
@@ -516,6 +605,8 @@ def main():
     pkg.lib()
     if pkg.device_count() == 0:
         raise SystemExit("bench: no CUDA device")
+    if args.multiref:
+        return run_multiref(args, pkg)
     if args.stream_chunk > 0:
         return run_stream(args, pkg)
     if args.serve_million:

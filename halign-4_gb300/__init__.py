@@ -148,6 +148,17 @@ def lib() -> C.CDLL:
     L.hg_serve_counters.argtypes = [vp, vp, vp, i32]
     L.hg_extend_align_ksw2.argtypes = [C.c_char_p, i64, C.c_char_p, i64, i32, vp, i64]
     L.hg_extend_align_ksw2.restype = i64
+    L.hg_sketch_batch.argtypes = [vp, vp, vp, vp, vp, i64, i32, i32, i32, i32, vp, i64, vp]
+    L.hg_refset_create.argtypes = [vp, vp, i32, i32, i32, i32, i32, vp, i64, i64, C.POINTER(vp)]
+    L.hg_refset_destroy.argtypes = [vp]
+    L.hg_refset_destroy.restype = None
+    L.hg_refset_info.argtypes = [vp, vp, vp, vp]
+    L.hg_refset_sketch.argtypes = [vp, i32, vp, i64, vp]
+    L.hg_refset_consensus.argtypes = [vp, vp, i64, vp]
+    L.hg_refset_set_consensus.argtypes = [vp, C.c_char_p, i64]
+    L.hg_refset_select.argtypes = [vp, vp, vp, vp, vp, vp, i64, vp, vp]
+    L.hg_refset_align.argtypes = [vp, vp, vp, vp, vp, vp, i64, i32, vp, vp, vp, i64, vp, vp, vp, i64, vp]
+    L.hg_refset_last_ms.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -571,6 +582,110 @@ def align_fasta(center_fasta, queries_fasta, out_fasta, k: int = 15, w: int = 10
     _check(lib().hg_align_fasta(str(center_fasta).encode(), str(queries_fasta).encode(), str(out_fasta).encode(),
                                 k, w, chunk_queries, C.byref(n)))
     return n.value
+
+
+SKETCH_MAX = 8192  # HG_SKETCH_MAX
+
+
+def sketch_batch(b: Packed, k: int = 15, sketch_size: int = 2000, noncanonical: bool = True,
+                 seed: int = 42) -> list[np.ndarray]:
+    """mash::sketchFromSequence of every query of a packed batch on the
+    device (hg_sketch_batch): per query the sorted distinct bottom-sketch_size
+    hashes."""
+    s = max(int(sketch_size), 0)
+    out = np.zeros((max(b.n, 1), max(s, 1)), np.uint64)
+    cnt = np.zeros(max(b.n, 1), np.int32)
+    _check(lib().hg_sketch_batch(_p(b.packed), _p(b.poff), _p(b.qlen), _p(b.exc), _p(b.exc_off), b.n, k, s,
+                                 int(noncanonical), seed, _p(out), out.shape[1], _p(cnt)))
+    return [out[i, : cnt[i]].copy() for i in range(b.n)]
+
+
+@dataclass
+class RefAlignResult(AlignResult):
+    best: np.ndarray | None = None     # int32[n]: chosen reference
+    jaccard: np.ndarray | None = None  # float64[n]
+
+
+class RefSet:
+    """Multi-reference mode (hg_refset_*): resident indexes and sketches of
+    several references, best-reference selection and alignment."""
+
+    def __init__(self, refs, k: int = 15, w: int = 10, sketch_size: int = 2000, seed: int = 42,
+                 prm: Params | None = None, max_queries: int = 16384, max_bases: int = 1 << 28):
+        self.refs = [_bytes(r) for r in refs]
+        arr = (C.c_char_p * len(self.refs))(*self.refs)
+        lens = np.array([len(r) for r in self.refs], np.int64)
+        h = C.c_void_p()
+        _check(lib().hg_refset_create(C.cast(arr, C.c_void_p), _p(lens), len(self.refs), k, w, sketch_size, seed,
+                                      C.byref(prm) if prm is not None else None, max_queries, max_bases, C.byref(h)))
+        self.h = h
+        self.max_len = int(lens.max())
+
+    def sketch(self, r: int) -> np.ndarray:
+        n = C.c_int64()
+        out = np.zeros(SKETCH_MAX, np.uint64)
+        _check(lib().hg_refset_sketch(self.h, r, _p(out), len(out), C.byref(n)))
+        return out[: n.value].copy()
+
+    def consensus(self) -> bytes:
+        n, clen = C.c_int64(), C.c_int64()
+        _check(lib().hg_refset_info(self.h, None, None, C.byref(clen)))
+        buf = C.create_string_buffer(max(clen.value, 1))
+        _check(lib().hg_refset_consensus(self.h, buf, len(buf), C.byref(n)))
+        return buf.raw[: n.value]
+
+    def set_consensus(self, seq) -> None:
+        b = _bytes(seq)
+        _check(lib().hg_refset_set_consensus(self.h, b, len(b)))
+
+    def select(self, b: Packed) -> tuple[np.ndarray, np.ndarray]:
+        best = np.zeros(max(b.n, 1), np.int32)
+        jac = np.zeros(max(b.n, 1), np.float64)
+        _check(lib().hg_refset_select(self.h, _p(b.packed), _p(b.poff), _p(b.qlen), _p(b.exc), _p(b.exc_off), b.n,
+                                      _p(best), _p(jac)))
+        return best[: b.n], jac[: b.n]
+
+    def last_select_ms(self) -> float:
+        """Device time of the last select's sketch + selection launch."""
+        ms = C.c_float()
+        _check(lib().hg_refset_last_ms(self.h, C.byref(ms)))
+        return float(ms.value)
+
+    def align(self, b: Packed, keep_length: bool = True, rows: bool = True, check: bool = True) -> RefAlignResult:
+        n = b.n
+        clen = C.c_int64()
+        _check(lib().hg_refset_info(self.h, None, None, C.byref(clen)))
+        L = max(self.max_len, clen.value)
+        stride = (L + 15) // 16 * 16
+        best = np.zeros(max(n, 1), np.int32)
+        jac = np.zeros(max(n, 1), np.float64)
+        for worst in (False, True):
+            cap = (b.bases + n * (L + 4)) if worst else (b.bases // 8 + 64 * n + 1024)
+            cig = np.zeros(max(cap, 1), np.uint32)
+            off = np.zeros(n + 1, np.int64)
+            has_ins = np.zeros(max(n, 1), np.uint8)
+            status = np.zeros(max(n, 1), np.uint32)
+            rbuf = np.zeros((n, stride), np.uint8) if rows else None
+            code = lib().hg_refset_align(self.h, _p(b.packed), _p(b.poff), _p(b.qlen), _p(b.exc), _p(b.exc_off), n,
+                                         int(keep_length), _p(best), _p(jac), _p(cig), len(cig), _p(off),
+                                         _p(has_ins), _p(rbuf), stride if rows else 0, _p(status))
+            if code != HG_ERR_CAPACITY:
+                break
+        if check or code not in (HG_OK, HG_ERR_LENGTH_MISMATCH):
+            _check(code)
+        return RefAlignResult(cig[: off[-1]] if n else cig[:0], off, has_ins[:n], status[:n],
+                              rbuf if rows else None, best[:n], jac[:n])
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().hg_refset_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def count_rows(rows: np.ndarray, counts: np.ndarray | None = None) -> np.ndarray:

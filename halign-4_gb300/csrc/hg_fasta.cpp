@@ -2,6 +2,13 @@
 // the file edge of the align-to-center path with the reader, the GPU and
 // the writer overlapped.
 //
+// The center FASTA holds one record (aligned to, as the reference CLI's -c)
+// or several of one length (multi-reference mode with --keep-length: each
+// query is aligned to its best reference, hg_refset_align; the reference
+// CLI runs its external MSA over the references first, and its output here
+// matches that MSA returning them unchanged).  The output starts with the
+// center record(s) through the reference's clean_table.
+//
 // A reader thread parses the query FASTA into chunks (HAlign-4's
 // KseqReader::next, src/utils/seq_io.cpp:134-155: sequence lines joined,
 // a trailing '\r' dropped), the calling thread packs each chunk (hg_pack)
@@ -108,19 +115,57 @@ private:
 
 }  // namespace
 
+namespace {
+
+// clean_table (include/utils.h:161-191): A C G T U (either case) and '-'
+// kept in upper case, every other byte 'N'; the reference CLI writes the
+// center / reference records through it (writeConsensusAndReferences,
+// src/align/ref_aligner.cpp:541-556).
+std::string cleaned(const std::string& s)
+{
+    std::string o(s);
+    for (char& c : o) {
+        switch (c) {
+        case 'A': case 'a': c = 'A'; break;
+        case 'C': case 'c': c = 'C'; break;
+        case 'G': case 'g': c = 'G'; break;
+        case 'T': case 't': c = 'T'; break;
+        case 'U': case 'u': c = 'U'; break;
+        case '-': break;
+        default: c = 'N';
+        }
+    }
+    return o;
+}
+
+}  // namespace
+
 extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k,
                               int w, int64_t chunk_queries, int64_t* n_aligned)
 {
     if (!center_fasta || !queries_fasta || !out_fasta || chunk_queries <= 0)
         return hg::set_error(HG_ERR_ARG, "hg_align_fasta: bad arguments");
+    // the center FASTA: one record (align to its consensus) or several
+    // (multi-reference mode: each query to its best reference)
     Reader cr(center_fasta);
-    std::string cname, cdesc, cseq;
-    if (!cr.ok() || !cr.next(cname, cdesc, cseq) || cseq.empty())
+    std::vector<std::string> cnames, cdescs, cseqs;
+    {
+        std::string name, desc, seq;
+        while (cr.ok() && cr.next(name, desc, seq)) cnames.push_back(name), cdescs.push_back(desc), cseqs.push_back(seq);
+    }
+    if (cseqs.empty() || cseqs[0].empty())
         return hg::set_error(HG_ERR_ARG, "hg_align_fasta: no center record in " + std::string(center_fasta));
+    const bool multi = cseqs.size() > 1;
+    const int64_t L = (int64_t)cseqs[0].size();
+    for (const auto& s : cseqs)
+        if ((int64_t)s.size() != L)
+            return hg::set_error(HG_ERR_ARG, "hg_align_fasta: references of different lengths (the reference CLI "
+                                             "aligns them with its external MSA tool first)");
     hg_index_t* ix = nullptr;
-    int r = hg_index_create(cseq.data(), (int64_t)cseq.size(), k, w, nullptr, &ix);
+    hg_refset_t* rs = nullptr;
+    int r = HG_OK;
+    if (!multi) r = hg_index_create(cseqs[0].data(), L, k, w, nullptr, &ix);
     if (r) return r;
-    const int64_t L = (int64_t)cseq.size();
     Reader qr(queries_fasta);
     if (!qr.ok()) {
         hg_index_destroy(ix);
@@ -133,7 +178,8 @@ extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fast
         hg_index_destroy(ix);
         return hg::set_error(HG_ERR_ARG, "hg_align_fasta: cannot write " + std::string(out_fasta));
     }
-    out << '>' << cname << (cdesc.empty() ? "" : " ") << cdesc << '\n' << cseq << '\n';
+    for (size_t i = 0; i < cseqs.size(); ++i)
+        out << '>' << cnames[i] << (cdescs[i].empty() ? "" : " ") << cdescs[i] << '\n' << cleaned(cseqs[i]) << '\n';
     // reader thread
     Queue<Chunk> in_q(2), out_q(2);
     std::thread reader([&] {
@@ -182,12 +228,21 @@ extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fast
             for (int64_t i = 0; i < n; ++i) maxlen = std::max(maxlen, c.offs[i + 1] - c.offs[i]);
             // sub-batches of the chunk hold about chunk_queries center-length
             // queries; a longer query than the context holds gets a new one
-            if (!ctx || maxlen > ctx_bases) {
+            if ((!ctx && !rs) || maxlen > ctx_bases) {
                 if (ctx) hg_ctx_destroy(ctx), ctx = nullptr;
+                if (rs) hg_refset_destroy(rs), rs = nullptr;
                 // (at most ~0.9 Gbp per sub-batch: the arenas scale with it)
                 ctx_bases = std::max<int64_t>(std::min<int64_t>(chunk_queries * (L + L / 4 + 64), 900000000),
                                               2 * maxlen);
-                rc = hg_ctx_create(ix, chunk_queries, ctx_bases, &ctx);
+                if (!multi) {
+                    rc = hg_ctx_create(ix, chunk_queries, ctx_bases, &ctx);
+                } else {  // RefAligner's settings: sketch size 2000, seed 42
+                    std::vector<const char*> ptr;
+                    std::vector<int64_t> lens;
+                    for (const auto& s : cseqs) ptr.push_back(s.data()), lens.push_back((int64_t)s.size());
+                    rc = hg_refset_create(ptr.data(), lens.data(), (int)cseqs.size(), k, w, 2000, 42, nullptr,
+                                          chunk_queries, ctx_bases, &rs);
+                }
             }
             int64_t pb = 0, ne = 0;
             std::vector<uint8_t> packed;
@@ -208,14 +263,18 @@ extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fast
                 std::vector<int64_t> coff((size_t)n + 1);
                 std::vector<uint32_t> st((size_t)n);
                 std::vector<uint32_t> cig((size_t)(c.seqs.size() / 8 + 64 * n + 1024));
-                rc = hg_align_batch(ctx, packed.data(), poff.data(), qlen.data(), exc.data(), eoff.data(), n,
-                                    cig.data(), (int64_t)cig.size(), coff.data(), c.has_ins.data(), c.rows.data(),
-                                    c.stride, st.data());
+                auto run = [&] {
+                    return multi ? hg_refset_align(rs, packed.data(), poff.data(), qlen.data(), exc.data(),
+                                                   eoff.data(), n, 1, nullptr, nullptr, cig.data(), (int64_t)cig.size(),
+                                                   coff.data(), c.has_ins.data(), c.rows.data(), c.stride, st.data())
+                                 : hg_align_batch(ctx, packed.data(), poff.data(), qlen.data(), exc.data(),
+                                                  eoff.data(), n, cig.data(), (int64_t)cig.size(), coff.data(),
+                                                  c.has_ins.data(), c.rows.data(), c.stride, st.data());
+                };
+                rc = run();
                 if (rc == HG_ERR_CAPACITY) {  // CIGARs longer than the first guess: the worst case fits
                     cig.resize((size_t)(c.seqs.size() + n * (L + 4)));
-                    rc = hg_align_batch(ctx, packed.data(), poff.data(), qlen.data(), exc.data(), eoff.data(), n,
-                                        cig.data(), (int64_t)cig.size(), coff.data(), c.has_ins.data(), c.rows.data(),
-                                        c.stride, st.data());
+                    rc = run();
                 }
             }
             if (rc) err = hg_last_error();
@@ -230,6 +289,7 @@ extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fast
     reader.join();
     writer.join();
     if (ctx) hg_ctx_destroy(ctx);
+    if (rs) hg_refset_destroy(rs);
     hg_index_destroy(ix);
     rest.close();
     if (rc == HG_OK) {  // the rows without insertions follow the insertion rows

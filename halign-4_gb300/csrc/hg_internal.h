@@ -78,6 +78,13 @@ struct Workspace {
 // The calling thread's workspace for the current device (created on first use).
 int workspace(Workspace** out);
 
+// hg_index_create with the DP center chosen: dp_consensus aligns against
+// the consensus of the single record (RefAligner with one reference aligns
+// to consensus_seq, src/align/ref_aligner.cpp:242-245), otherwise against
+// the record as given (one of several references, :232-240).
+int index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params, bool dp_consensus,
+                 hg_index_t** out);
+
 // Length of an index's center.
 int64_t index_length(const hg_index_t* ix);
 

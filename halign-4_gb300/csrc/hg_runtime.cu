@@ -453,6 +453,12 @@ std::vector<float> hg::log2_table(int n)
 extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params,
                                hg_index_t** out)
 {
+    return hg::index_create(center, len, k, w, params, true, out);
+}
+
+int hg::index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params, bool dp_consensus,
+                     hg_index_t** out)
+{
     if (!out || !center || len <= 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_index_create: bad arguments");
     if (k <= 0 || k > 31 || w <= 0 || w >= 256) return fail(HG_ERR_ARG, "hg_index_create: need 0<k<=31, 0<w<256");
     if (hg_device_count() <= 0) return fail(HG_ERR_CUDA, "hg_index_create: no CUDA device");
@@ -506,9 +512,11 @@ extern "C" int hg_index_create(const char* center, int64_t len, int k, int w, co
     }
     std::vector<ulonglong2> tab(tsize);
     for (uint32_t i = 0; i < tsize; ++i) tab[i].x = tkey[i], tab[i].y = tval[i];
-    // DP center (consensus of the single record) in DNA5 codes
+    // DP center in DNA5 codes: the consensus of the single record (one
+    // center), or the record itself (one reference of several)
     std::vector<uint8_t> cdp((size_t)len);
-    for (int64_t i = 0; i < len; ++i) cdp[i] = hg::dna5_of(consensus_letter((uint8_t)center[i]));
+    for (int64_t i = 0; i < len; ++i)
+        cdp[i] = hg::dna5_of(dp_consensus ? consensus_letter((uint8_t)center[i]) : (uint8_t)center[i]);
     // 2-bit copy for the small DP tier's register loads (64 bytes of slack: it reads 24 bytes at a time)
     std::vector<uint8_t> c2((size_t)(len + 3) / 4 + 64, 0);
     int cplain = 1;

@@ -16,6 +16,8 @@ five benchmark configurations:
 * ``serve``      29,903 bp center, substrings of uniform length 500..29,903,
                  0.5% divergence (0.4% substitutions, 0.05% + 0.05% indels,
                  mean 3), Poisson arrivals.
+* ``multiref``   several references of one length (substitution variants of
+                 one center) and full-length queries mutated from a random one.
 
 All generation is vectorised (numpy PCG64), so the same seed gives the same
 bytes on x86-64 and aarch64.  Queries come back as one concatenated ``bytes``
@@ -38,6 +40,8 @@ class Workload:
     offsets: np.ndarray  # int64, len n+1
     names: list[str]
     arrivals: np.ndarray | None = None  # seconds, serving workloads only
+    refs: list[bytes] | None = None     # multi-reference workloads: the references
+    src_ref: np.ndarray | None = None   # multi-reference workloads: the reference each query came from
 
     @property
     def n(self) -> int:
@@ -191,6 +195,34 @@ def serve(n: int = 2000, seed: int = 5, center_len: int = 29903, rate: float = 2
     out, offs = _substring_queries(center, lens, rng, 0.004, 0.0005, 0.0005, 3.0)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
     return Workload("serve", center, out.tobytes(), offs, _names("r", chunk * n, n), arrivals)
+
+
+def multiref(n: int = 200, n_refs: int = 4, seed: int = 6, ref_len: int = 5000, ref_div: float = 0.03,
+             chunk: int = 0) -> Workload:
+    """Multi-reference mode: ``n_refs`` references of one length (a uniform
+    center with ``ref_div`` substitutions each, so that they stay aligned
+    column by column) and full-length queries mutated from a random one of
+    them (1% substitutions, 0.1% + 0.1% indels, mean 3)."""
+    base = np.frombuffer(random_center(ref_len, seed), np.uint8)
+    rng_r = np.random.Generator(np.random.PCG64([seed, 2]))
+    ref_arr, _ = mutate_batch(base, np.zeros(n_refs, np.int64), np.full(n_refs, ref_len, np.int64), rng_r, ref_div,
+                              0.0, 0.0, 3.0)
+    refs = [ref_arr[r * ref_len:(r + 1) * ref_len].tobytes() for r in range(n_refs)]
+    rng = np.random.Generator(np.random.PCG64([seed, 1, chunk]))
+    src_ref = rng.integers(0, n_refs, n)
+    out, offs = mutate_batch(ref_arr, src_ref * ref_len, np.full(n, ref_len, np.int64), rng, 0.01, 0.001, 0.001, 3.0)
+    return Workload("multiref", refs[0], out.tobytes(), offs, _names("m", chunk * n, n), refs=refs,
+                    src_ref=src_ref)
+
+
+def write_refs_fasta(path: str, refs: list[bytes]) -> None:
+    """The reference FASTA of a multi-reference run: records ref<i> with a
+    description, 80 columns per line."""
+    with open(path, "wb") as f:
+        for r, s in enumerate(refs):
+            f.write(b">ref%d reference %d\n" % (r, r))
+            for i in range(0, len(s), 80):
+                f.write(s[i:i + 80] + b"\n")
 
 
 def pack_2bit(seqs: bytes, offsets: np.ndarray, align: int = 16):

@@ -208,15 +208,20 @@ int hg_fetch_chain(hg_ctx_t* ctx, int64_t query, uint32_t* pos_ref, uint32_t* po
 
 /* ---- files: query FASTA in, aligned FASTA out ---------------------------
  * The align-to-center run of the reference CLI with --keep-length
- * (halign4 -c center.fa -i queries.fa --keep-length), streamed: the first
- * record of center_fasta is the center (k, w: --kmer-size, --kmer-window);
- * queries are read in chunks of chunk_queries records (KseqReader::next,
- * src/utils/seq_io.cpp:134-155), aligned with rows on the GPU while the next
- * chunk is read and the previous one written, and written in the reference's
- * order (src/align/ref_aligner.cpp:676-740): the center record, then every
- * row with an insertion, then the others, each group in input order, one
- * line per row.  *n_aligned (may be NULL) gets the query count.  Errors as
- * hg_align_batch's (HG_ERR_LENGTH_MISMATCH where the reference throws). */
+ * (halign4 -c center.fa -i queries.fa --keep-length), streamed: one record
+ * in center_fasta is the center (k, w: --kmer-size, --kmer-window); several
+ * records (of one length) are multi-reference mode, each query aligned to
+ * its best reference (hg_refset_align; sketch size 2000, seed 42, as the
+ * CLI), the output being the CLI's when its MSA tool returns the references
+ * unchanged.  Queries are read in chunks of chunk_queries records
+ * (KseqReader::next, src/utils/seq_io.cpp:134-155), aligned with rows on the
+ * GPU while the next chunk is read and the previous one written, and written
+ * in the reference's order (src/align/ref_aligner.cpp:676-740): the center
+ * record(s) through clean_table, then every row with an insertion, then the
+ * others, each group in input order, one line per row.  *n_aligned (may be
+ * NULL) gets the query count.  Errors as hg_align_batch's
+ * (HG_ERR_LENGTH_MISMATCH where the reference throws); HG_ERR_ARG for
+ * references of different lengths. */
 int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k, int w,
                    int64_t chunk_queries, int64_t* n_aligned);
 
@@ -406,6 +411,66 @@ int64_t hg_global_align_mm2(hg_index_t* ix, const char* qry, int64_t qlen, const
  * (src/align/ref_aligner.cpp:91-125): the plain single-query path. */
 int64_t hg_align_query(hg_index_t* ix, const char* qry, int64_t qlen, uint32_t* cigar, int64_t cap,
                        uint32_t* status);
+
+/* ---- multi-reference mode ------------------------------------------------
+ * Replaces RefAligner with several records in the reference FASTA
+ * (src/align/ref_aligner.cpp:21-70 and 212-283): MinHash sketches
+ * (mash::sketchFromSequence, src/mash/mash.cpp:32-117; non-canonical
+ * k-mers, the path's setting), the first reference of largest jaccard
+ * (mash::jaccard, :120-164; selection loop :232-241), alignment to it, and
+ * the consensus re-check without --keep-length (:273-282). */
+
+/* Largest sketch_size one CTA holds in shared memory (the reference's default
+ * is 2000). */
+#define HG_SKETCH_MAX 8192
+
+/* mash::sketchFromSequence for every query of a packed batch (hg_pack
+ * format): the sketch_size smallest distinct getHash2bit hashes (XXH3-64,
+ * src/mash/hash.cpp) of the valid k-mers, ascending, into
+ * hashes[i * stride ...], their number into counts[i].  k outside 1..32 or
+ * a query shorter than k gives an empty sketch, as in the reference (k = 32
+ * reproduces its mask of 0: every code is 0).  noncanonical = 0 hashes
+ * min(forward, reverse-complement) codes. */
+int hg_sketch_batch(const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
+                    const int64_t* exc_off, int64_t n, int k, int sketch_size, int noncanonical, int seed,
+                    uint64_t* hashes, int64_t stride, int32_t* counts);
+
+/* Resident reference set: per reference an index (hg_index_create; one
+ * reference aligns to its consensus, one of several to itself, as RefAligner
+ * does), its sketch, and one batch context created on first use
+ * (max_queries / max_bases as hg_ctx_create).  With references of one
+ * length the consensus of the re-check path is built as the reference
+ * builds it from the references' alignment when its MSA tool returns them
+ * unchanged (generateConsensusSequence, batch size 4096); otherwise give it
+ * with hg_refset_set_consensus.  seed is RefAligner's random_seed (42). */
+typedef struct hg_refset hg_refset_t;
+int hg_refset_create(const char* const* refs, const int64_t* lens, int n_refs, int k, int w, int sketch_size,
+                     int seed, const hg_params_t* params, int64_t max_queries, int64_t max_bases, hg_refset_t** out);
+void hg_refset_destroy(hg_refset_t* rs);
+int hg_refset_info(const hg_refset_t* rs, int* n_refs, int64_t* max_len, int64_t* consensus_len);
+int hg_refset_sketch(const hg_refset_t* rs, int ref, uint64_t* hashes, int64_t cap, int64_t* n);
+int hg_refset_consensus(const hg_refset_t* rs, char* out, int64_t cap, int64_t* len);
+int hg_refset_set_consensus(hg_refset_t* rs, const char* seq, int64_t len);
+
+/* Best reference of every query of a packed batch: best[i] the first
+ * reference of largest jaccard, jaccard[i] its value (one device launch). */
+int hg_refset_select(hg_refset_t* rs, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                     const int32_t* exc, const int64_t* exc_off, int64_t n, int32_t* best, double* jaccard);
+
+/* Device time of the last hg_refset_select launch (sketch + selection
+ * kernel, CUDA events on the set's stream), in milliseconds. */
+int hg_refset_last_ms(const hg_refset_t* rs, float* select_ms);
+
+/* alignOneQueryToRef for a batch.  keep_length != 0: every query aligned to
+ * its best reference (rows have that reference's length; row_stride >= the
+ * longest reference); keep_length == 0: aligned to the consensus (the
+ * reference's discarded first alignment is not run).  One reference: aligned
+ * to it either way.  best / jaccard (optional) get the selection; the other
+ * outputs are hg_align_batch's, in input order. */
+int hg_refset_align(hg_refset_t* rs, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
+                    const int32_t* exc, const int64_t* exc_off, int64_t n, int keep_length, int32_t* best,
+                    double* jaccard, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins,
+                    uint8_t* rows, int64_t row_stride, uint32_t* status);
 
 #ifdef __cplusplus
 }

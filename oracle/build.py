@@ -37,14 +37,14 @@ REF_LIB_CPP = [
     "consensus/consensus.cpp",
     "utils/file_io.cpp",
     "utils/seq_io.cpp",
+    "mash/mash.cpp",
+    "mash/hash.cpp",
 ]
 REF_CLI_CPP = [
     "halign4.cpp",
     "align/ref_aligner.cpp",
     "utils/preprocess.cpp",
     "utils/cmd.cpp",
-    "mash/mash.cpp",
-    "mash/hash.cpp",
     "consensus/selector.cpp",
 ]
 REF_C = ["align/ksw2_extz2_sse.c", "mash/xxhash.c"]
@@ -110,11 +110,11 @@ def build_ref(force: bool = False) -> Path | None:
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(lambda j: _run(j[0]), todo))
     names = lambda rels: [str(obj / (Path(r).stem + ".o")) for r in rels]  # noqa: E731
-    lib_objs = [str(h)] + names(REF_LIB_CPP) + [str(obj / "ksw2_extz2_sse.o")]
+    lib_objs = [str(h)] + names(REF_LIB_CPP) + [str(obj / "ksw2_extz2_sse.o"), str(obj / "xxhash.o")]
     if force or todo or not lib.exists():
         _run(["g++", "-shared", "-fopenmp", "-o", str(lib), *lib_objs, "-lz"])
     if force or todo or not cli.exists():
-        _run(["g++", "-fopenmp", "-o", str(cli), *lib_objs, *names(REF_CLI_CPP), str(obj / "xxhash.o"), "-lz"])
+        _run(["g++", "-fopenmp", "-o", str(cli), *lib_objs, *names(REF_CLI_CPP), "-lz"])
     return lib
 
 

@@ -1202,3 +1202,99 @@ char ho_pick_consensus(const uint32_t* k)
     if (k[4] > best) best = k[4], ch = 'U';
     return ch;
 }
+
+/* ------------------------------------------------------------------ MinHash */
+
+static uint64_t rotl64(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+
+static uint32_t bswap32(uint32_t x)
+{
+    return (x >> 24) | ((x >> 8) & 0xff00u) | ((x << 8) & 0xff0000u) | (x << 24);
+}
+
+uint64_t ho_hash2bit(uint64_t code, uint32_t seed32)
+{ /* getHash2bit (src/mash/hash.cpp): XXH3 64-bit of the 8 big-endian bytes of
+   * code.  XXH3 for a 4..8-byte input: the seed's low word byte-swapped into
+   * its high word; the input read as two little-endian words (first word on
+   * top); xored with (secret[8..15] ^ secret[16..23]) - seed, where the two
+   * secret words are little-endian reads of the default 192-byte secret; then
+   * the rrmxmx finaliser with the input length (8). */
+    uint64_t seed = seed32;
+    seed ^= (uint64_t)bswap32((uint32_t)seed) << 32;
+    const uint32_t w_hi = bswap32((uint32_t)(code >> 32)), w_lo = bswap32((uint32_t)code);
+    const uint64_t bitflip = 0xc73ab174c5ecd5a2ULL - seed;
+    uint64_t h = (((uint64_t)w_hi << 32) + w_lo) ^ bitflip;
+    h ^= rotl64(h, 49) ^ rotl64(h, 24);
+    h *= 0x9FB21C651E98DF25ULL;
+    h ^= (h >> 35) + 8;
+    h *= 0x9FB21C651E98DF25ULL;
+    return h ^ (h >> 28);
+}
+
+static int cmp_u64(const void* a, const void* b)
+{
+    const uint64_t x = *(const uint64_t*)a, y = *(const uint64_t*)b;
+    return x < y ? -1 : x > y;
+}
+
+int64_t ho_sketch(const char* seq, int64_t n, int k, int64_t sketch_size, int noncanonical, int seed,
+                  uint64_t* out)
+{ /* mash::sketchFromSequence (src/mash/mash.cpp:32-117).  Its max-heap plus
+   * seen-set keeps exactly the sketch_size smallest distinct hashes seen so
+   * far, so the result is the sorted distinct hashes cut to sketch_size. */
+    if (k <= 0 || sketch_size <= 0 || n < k || k > 32) return 0;
+    /* (1 << 2k) - 1 with the shift count taken mod 64, as x86-64 and AArch64
+     * shifts do: at k = 32 the reference's mask is 0 and every code is 0 */
+    const uint64_t mask = (1ULL << ((2 * k) & 63)) - 1ULL;
+    const int shift = 2 * (k - 1);
+    uint64_t* h = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(n - k + 1));
+    int64_t m = 0, valid = 0;
+    uint64_t fwd = 0, rev = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const unsigned c = nt4((unsigned char)seq[i]); /* mash::nt4_table (include/mash.h:15-32) */
+        if (c >= 4) {
+            fwd = rev = 0, valid = 0;
+            continue;
+        }
+        fwd = ((fwd << 2) | c) & mask;
+        rev = (rev >> 2) | ((uint64_t)(3u ^ c) << shift);
+        if (valid < k) ++valid;
+        if (valid < k) continue;
+        const uint64_t code = noncanonical ? fwd : (fwd < rev ? fwd : rev);
+        h[m++] = ho_hash2bit(code, (uint32_t)seed);
+    }
+    qsort(h, (size_t)m, sizeof(uint64_t), cmp_u64);
+    int64_t u = 0;
+    for (int64_t i = 0; i < m && u < sketch_size; ++i)
+        if (i == 0 || h[i] != h[i - 1]) out[u++] = h[i];
+    free(h);
+    return u;
+}
+
+double ho_jaccard(const uint64_t* a, int64_t na, const uint64_t* b, int64_t nb)
+{ /* mash::jaccard (src/mash/mash.cpp:120-164) with the two-pointer
+   * intersectionSizeSortedUnique (:204-230) */
+    if (na == 0 && nb == 0) return 1.0;
+    if (na == 0 || nb == 0) return 0.0;
+    int64_t i = 0, j = 0, inter = 0;
+    while (i < na && j < nb) {
+        if (a[i] < b[j]) ++i;
+        else if (b[j] < a[i]) ++j;
+        else ++inter, ++i, ++j;
+    }
+    const int64_t uni = na < nb ? na : nb;
+    return (double)inter / (double)uni;
+}
+
+int32_t ho_best_reference(const uint64_t* q, int64_t nq, const uint64_t* ref_h, const int64_t* ref_off,
+                          int32_t n_refs, double* best_j)
+{ /* src/align/ref_aligner.cpp:232-241 */
+    double best = -1.0;
+    int32_t idx = 0;
+    for (int32_t r = 0; r < n_refs; ++r) {
+        const double j = ho_jaccard(q, nq, ref_h + ref_off[r], ref_off[r + 1] - ref_off[r]);
+        if (j > best) best = j, idx = r;
+    }
+    if (best_j) *best_j = best;
+    return idx;
+}

@@ -124,6 +124,25 @@ void ho_count_rows(const char* rows, int64_t n_rows, int64_t L, uint32_t* counts
 void ho_count_insertions(const uint32_t* c, int64_t n, uint32_t* ins, int64_t L);
 char ho_pick_consensus(const uint32_t* counts7);
 
+/* Multi-reference mode (MinHash).
+ * ho_hash2bit: getHash2bit (src/mash/hash.cpp), i.e. XXH3_64bits_withSeed of
+ *   the 8 big-endian bytes of a 2-bit k-mer code (xxHash 0.8.3, vendored as
+ *   include/xxhash.h; the 4..8-byte input branch of the published XXH3).
+ * ho_sketch: mash::sketchFromSequence (src/mash/mash.cpp:32-117): the
+ *   sketch_size smallest distinct hashes of the valid k-mers, ascending.
+ *   Returns the count written (<= sketch_size).
+ * ho_jaccard: mash::jaccard (src/mash/mash.cpp:120-164) over sorted
+ *   distinct sketches: |a & b| / min(|a|, |b|), 1 when both are empty.
+ * ho_best_reference: the selection loop of RefAligner::alignOneQueryToRef
+ *   (src/align/ref_aligner.cpp:232-241): first reference of largest
+ *   jaccard, strict '>' from -1. */
+uint64_t ho_hash2bit(uint64_t code, uint32_t seed);
+int64_t ho_sketch(const char* seq, int64_t n, int k, int64_t sketch_size, int noncanonical, int seed,
+                  uint64_t* out);
+double ho_jaccard(const uint64_t* a, int64_t na, const uint64_t* b, int64_t nb);
+int32_t ho_best_reference(const uint64_t* q, int64_t nq, const uint64_t* ref_h, const int64_t* ref_off,
+                          int32_t n_refs, double* best_j);
+
 #ifdef __cplusplus
 }
 #endif

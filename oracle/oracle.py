@@ -81,6 +81,14 @@ class Oracle(_Common):
         L.ho_last_ring_oob.restype = C.c_int64
         L.ho_cigar_has_insertion.argtypes = [vp, i64]
         L.ho_cigar_has_insertion.restype = i32
+        L.ho_hash2bit.argtypes = [C.c_uint64, C.c_uint32]
+        L.ho_hash2bit.restype = C.c_uint64
+        L.ho_sketch.argtypes = [C.c_char_p, i64, i32, i64, i32, i32, vp]
+        L.ho_sketch.restype = i64
+        L.ho_jaccard.argtypes = [vp, i64, vp, i64]
+        L.ho_jaccard.restype = C.c_double
+        L.ho_best_reference.argtypes = [vp, i64, vp, vp, C.c_int32, vp]
+        L.ho_best_reference.restype = C.c_int32
 
     def last_ring_oob(self) -> int:
         return int(self.lib.ho_last_ring_oob())
@@ -239,6 +247,31 @@ class Oracle(_Common):
         c = np.ascontiguousarray(cigar, np.uint32)
         return bool(self.lib.ho_cigar_has_insertion(_p(c), len(c)))
 
+    # ---- multi-reference mode (MinHash) ----
+    def hash2bit(self, code: int, seed: int = 42) -> int:
+        return int(self.lib.ho_hash2bit(code, seed))
+
+    def sketch(self, seq, k=15, sketch_size=2000, noncanonical=True, seed=42) -> np.ndarray:
+        b = _bytes(seq)
+        out = np.zeros(max(1, min(sketch_size, len(b) + 1)), np.uint64)
+        n = self.lib.ho_sketch(b, len(b), k, sketch_size, int(noncanonical), seed, _p(out))
+        return out[:n].copy()
+
+    def jaccard(self, a, b) -> float:
+        a = np.ascontiguousarray(a, np.uint64)
+        b = np.ascontiguousarray(b, np.uint64)
+        return float(self.lib.ho_jaccard(_p(a), len(a), _p(b), len(b)))
+
+    def best_reference(self, q, ref_sketches) -> tuple[int, float]:
+        q = np.ascontiguousarray(q, np.uint64)
+        flat = np.ascontiguousarray(np.concatenate([np.asarray(r, np.uint64) for r in ref_sketches] or
+                                                   [np.zeros(0, np.uint64)]), np.uint64)
+        off = np.zeros(len(ref_sketches) + 1, np.int64)
+        np.cumsum([len(r) for r in ref_sketches], out=off[1:])
+        bj = np.zeros(1, np.float64)
+        r = self.lib.ho_best_reference(_p(q), len(q), _p(flat), _p(off), len(ref_sketches), _p(bj))
+        return int(r), float(bj[0])
+
 
 class Reference(_Common):
     """The unmodified reference sources (only where oracle/_ref was built)."""
@@ -280,10 +313,32 @@ class Reference(_Common):
         L.ref_extend_align_ksw2.restype = i64
         L.ref_generate_consensus.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.c_uint64, i64, vp, i64]
         L.ref_generate_consensus.restype = i64
+        L.ref_hash2bit.argtypes = [C.c_uint64, C.c_uint32]
+        L.ref_hash2bit.restype = C.c_uint64
+        L.ref_sketch.argtypes = [C.c_char_p, i64, i32, i64, i32, i32, vp, i64]
+        L.ref_sketch.restype = i64
+        L.ref_jaccard.argtypes = [vp, i64, vp, i64, i32]
+        L.ref_jaccard.restype = C.c_double
 
     @staticmethod
     def _split(a):
         return [a[f] for f in ("hash", "rid_ref", "pos_ref", "rid_qry", "pos_qry", "span")]
+
+    def hash2bit(self, code: int, seed: int = 42) -> int:
+        return int(self.lib.ref_hash2bit(code, seed))
+
+    def sketch(self, seq, k=15, sketch_size=2000, noncanonical=True, seed=42) -> np.ndarray:
+        b = _bytes(seq)
+        cap = max(1, min(sketch_size, len(b) + 1))
+        out = np.zeros(cap, np.uint64)
+        n = self.lib.ref_sketch(b, len(b), k, sketch_size, int(noncanonical), seed, _p(out), cap)
+        assert n >= 0
+        return out[:n].copy()
+
+    def jaccard(self, a, b, k=15) -> float:
+        a = np.ascontiguousarray(a, np.uint64)
+        b = np.ascontiguousarray(b, np.uint64)
+        return float(self.lib.ref_jaccard(_p(a), len(a), _p(b), len(b), k))
 
     def extract_minimizer(self, seq, k=15, w=10, non_canonical=True):
         b = _bytes(seq)

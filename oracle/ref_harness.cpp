@@ -18,13 +18,18 @@
 //   ref_align_query       -> RefAligner::globalAlign body  (src/align/ref_aligner.cpp:91-125)
 //   ref_del_query         -> cigar::delQueryToRefByCigar   (src/align/cigar.cpp:212-299)
 //   ref_pick_consensus    -> consensus::pickConsensusChar  (src/consensus/consensus.cpp:18-35)
+//   ref_hash2bit          -> getHash2bit                   (src/mash/hash.cpp)
+//   ref_sketch            -> mash::sketchFromSequence      (src/mash/mash.cpp:32-117)
+//   ref_jaccard           -> mash::jaccard                 (src/mash/mash.cpp:120-164)
 //   ref_align_batch       -> the OpenMP schedule(dynamic,1) query loop of
 //                            RefAligner::alignQueryToRef (src/align/ref_aligner.cpp:362-372)
 //                            over RefAligner::globalAlign, without the sketch.
 #include "align.h"
 #include "anchor.h"
 #include "consensus.h"
+#include "hash.h"
 #include "ksw2.h"
+#include "mash.h"
 #include "seed.h"
 
 #include <omp.h>
@@ -340,5 +345,28 @@ char ref_pick_consensus(const uint32_t* counts)
 }
 
 int ref_auto_band(int qlen, int tlen) { return align::auto_band(qlen, tlen); }
+
+uint64_t ref_hash2bit(uint64_t code, uint32_t seed) { return getHash2bit(code, seed); }
+
+// mash::sketchFromSequence into out (capacity cap); returns the sketch size
+int64_t ref_sketch(const char* seq, int64_t n, int k, int64_t sketch_size, int noncanonical, int seed, uint64_t* out,
+                   int64_t cap)
+{
+    const mash::Sketch sk = mash::sketchFromSequence(std::string(seq, static_cast<size_t>(n)), static_cast<size_t>(k),
+                                                     static_cast<size_t>(sketch_size), noncanonical != 0, seed);
+    const int64_t m = static_cast<int64_t>(sk.hashes.size());
+    if (m > cap) return -m;
+    std::memcpy(out, sk.hashes.data(), sizeof(uint64_t) * static_cast<size_t>(m));
+    return m;
+}
+
+double ref_jaccard(const uint64_t* a, int64_t na, const uint64_t* b, int64_t nb, int k)
+{
+    mash::Sketch x, y;
+    x.k = y.k = static_cast<size_t>(k);
+    x.hashes.assign(a, a + na);
+    y.hashes.assign(b, b + nb);
+    return mash::jaccard(x, y);
+}
 
 }  // extern "C"

@@ -231,6 +231,76 @@ def dropin_cases(R: Reference):
                              limit, bs)
 
 
+def mash_vectors(R: Reference, seed=21):
+    """mash::sketchFromSequence / getHash2bit / jaccard outputs of the
+    reference on sequences with N, lowercase and U, repetitive and short
+    ones, several k, sketch sizes and seeds."""
+    rng = np.random.default_rng(seed)
+    seqs, prm, sks = [], [], []
+    for it in range(48):
+        n = int(rng.choice([0, 3, 14, 15, 40, 700, 2500, 9000]))
+        s = _seq(rng, n, noisy=it % 2 == 0)
+        if it % 5 == 0:
+            s = (b"ACGTTGCAAG" * (n // 10 + 1))[:n]  # few distinct k-mers
+        if it % 7 == 0 and n > 100:  # an N-run
+            a = int(rng.integers(0, n - 60))
+            s = s[:a] + b"N" * 50 + s[a + 50:]
+        k = int(rng.choice([15, 15, 21, 5, 31, 32, 1]))
+        sz = int(rng.choice([2000, 2000, 10, 1, 300, 8192]))
+        nc = int(it % 4 != 3)
+        sd = int(rng.choice([42, 0, 7]))
+        seqs.append(np.frombuffer(s, np.uint8)), prm.append([k, sz, nc, sd]), sks.append(R.sketch(s, k, sz, bool(nc), sd))
+    sf, so = ragged(seqs, np.uint8)
+    kf, ko = ragged(sks, np.uint64)
+    codes = rng.integers(0, 2**62, 64, dtype=np.int64).astype(np.uint64)
+    hashes = np.array([[R.hash2bit(int(c), sd) for sd in (42, 0, 7, 2**31 - 1)] for c in codes], np.uint64)
+    # jaccard over default sketches (one empty) and truncated ones
+    base = [R.sketch(_seq(rng, 3000, False)) for _ in range(3)]
+    base.append(R.sketch(b""))
+    pairs = base + [base[0][:100], base[1][50:2000]]
+    jf, jo = ragged(pairs, np.uint64)
+    jac = np.array([[R.jaccard(a, b) for b in pairs] for a in pairs], np.float64)
+    np.savez_compressed(OUT / "mash_sketch.npz", seq=sf, seq_off=so, params=np.array(prm, np.int64), sketch=kf,
+                        sketch_off=ko, codes=codes, hashes=hashes, jac_sk=jf, jac_sk_off=jo, jaccard=jac)
+
+
+def multiref_cli_digest(w):
+    """The reference CLI in multi-reference mode (several records in -c) with
+    --keep-length and an MSA command that copies its input."""
+    d = Path(tempfile.mkdtemp(prefix="halign_golden_mr_"))
+    try:
+        synth.write_refs_fasta(str(d / "refs.fa"), w.refs)
+        synth.write_fasta(str(d), "unused", b"A", w)
+        cmd = [str(ROOT / "oracle/_ref/halign4"), "-i", str(d / "queries.fa"), "-o", str(d / "out.fa"), "-c",
+               str(d / "refs.fa"), "--keep-length", "-p", "cp {input} {output}", "-t", "1",
+               "--kmer-size", "15", "--kmer-window", "10", "-w", str(d / "wd"), "--save-workdir"]
+        subprocess.run(cmd, check=True, capture_output=True)
+        data = (d / "out.fa").read_bytes()
+        # the reference each query was aligned to, from the SAM records' RNAME
+        rname = {}
+        for sam in ("thread0.sam", "thread0_insertion.sam"):
+            for line in (d / "wd" / "result" / sam).read_text().splitlines():
+                if line and not line.startswith("@"):
+                    f = line.split("\t")
+                    rname[f[0]] = int(f[2][3:])
+        best = [rname[nm] for nm in w.names]
+        return hashlib.sha256(data).hexdigest(), len(data), data.count(b"\n") // 2, best
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def mash_fixtures(R: Reference):
+    mash_vectors(R)
+    w = synth.multiref(200)
+    digest, nbytes, nrec, best = multiref_cli_digest(w)
+    meta = json.loads((OUT / "meta.json").read_text())
+    meta.update({"multiref200_cli_fasta_sha256": digest, "multiref200_cli_fasta_bytes": nbytes,
+                 "multiref200_cli_records": nrec, "multiref200_best_ref": best,
+                 "multiref_cli": "halign4 -i queries.fa -o out.fa -c refs.fa --keep-length -p 'cp {input} {output}' "
+                                 "-t 1 --kmer-size 15 --kmer-window 10 (four references of one length)"})
+    (OUT / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+
+
 def cli_fasta_digest(w, threads=1):
     d = Path(tempfile.mkdtemp(prefix="halign_golden_"))
     try:
@@ -250,6 +320,9 @@ def main():
     if sys.argv[1:] == ["--dropin"]:  # only the C++-surface fixtures
         ksw_nongeneric_vectors(R)
         dropin_cases(R)
+        return
+    if sys.argv[1:] == ["--mash"]:  # only the multi-reference fixtures
+        mash_fixtures(R)
         return
     ksw_vectors(R)
     ksw_nongeneric_vectors(R)
@@ -277,6 +350,7 @@ def main():
         "uneven_with_n_runs": has_n,
     }
     (OUT / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+    mash_fixtures(R)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, os.path.getsize(p))
 
