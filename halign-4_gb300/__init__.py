@@ -144,10 +144,17 @@ def lib() -> C.CDLL:
     L.hg_serve_submit.argtypes = [vp, C.c_char_p, i64]
     L.hg_serve_submit.restype = i64
     L.hg_serve_result.argtypes = [vp, vp, vp, vp, vp, i64, vp, i32]
+    L.hg_serve_submit_many.argtypes = [vp, vp, vp, i64]
+    L.hg_serve_submit_many.restype = i64
+    L.hg_serve_results.argtypes = [vp, i64, vp, vp, vp, vp, i64, vp, i32]
+    L.hg_serve_results.restype = i64
     L.hg_serve_stats.argtypes = [vp, vp, i32, i32]
     L.hg_serve_counters.argtypes = [vp, vp, vp, i32]
     L.hg_extend_align_ksw2.argtypes = [C.c_char_p, i64, C.c_char_p, i64, i32, vp, i64]
     L.hg_extend_align_ksw2.restype = i64
+    L.hg_last_cells.argtypes = [vp, vp, vp]
+    L.hg_build_center.argtypes = [C.c_char_p, i64, vp, i64, vp]
+    L.hg_align_fasta_consensus.argtypes = [C.c_char_p, C.c_char_p, i32, i32, i64, i64, vp]
     L.hg_sketch_batch.argtypes = [vp, vp, vp, vp, vp, i64, i32, i32, i32, i32, vp, i64, vp]
     L.hg_refset_create.argtypes = [vp, vp, i32, i32, i32, i32, i32, vp, i64, i64, C.POINTER(vp)]
     L.hg_refset_destroy.argtypes = [vp]
@@ -401,6 +408,13 @@ class Context:
         la, ce = C.c_int64(), C.c_int64()
         _check(lib().hg_last_timing(self.h, C.byref(tot), _p(st), C.byref(la), C.byref(ce)))
         return tot.value, dict(zip(STAGES, st.tolist())), la.value
+
+    def last_cells(self) -> tuple[int, int]:
+        """(cells, match_cells) of the last staged run: the GCUPS work unit and
+        its part in match segments (emitted without a DP)."""
+        a, m = C.c_int64(), C.c_int64()
+        _check(lib().hg_last_cells(self.h, C.byref(a), C.byref(m)))
+        return a.value, m.value
 
     def work(self):
         """Work totals since the context was created: anchors, segment
@@ -686,6 +700,27 @@ class RefSet:
             self.close()
         except Exception:
             pass
+
+
+def build_center(queries_fasta, cons_n: int = 1000) -> bytes:
+    """The center the CLI builds without -c (hg_build_center): consensus of
+    the cons_n longest records (which must share one length)."""
+    n = C.c_int64()
+    code = lib().hg_build_center(str(queries_fasta).encode(), cons_n, None, 0, C.byref(n))
+    if code not in (HG_OK, HG_ERR_CAPACITY):
+        _check(code)
+    buf = C.create_string_buffer(max(n.value, 1))
+    _check(lib().hg_build_center(str(queries_fasta).encode(), cons_n, buf, len(buf), C.byref(n)))
+    return buf.raw[: n.value]
+
+
+def align_fasta_consensus(queries_fasta, out_fasta, k: int = 15, w: int = 10, cons_n: int = 1000,
+                          chunk_queries: int = 50000) -> int:
+    """The CLI's run without a center file (hg_align_fasta_consensus)."""
+    n = C.c_int64()
+    _check(lib().hg_align_fasta_consensus(str(queries_fasta).encode(), str(out_fasta).encode(), k, w, cons_n,
+                                          chunk_queries, C.byref(n)))
+    return n.value
 
 
 def count_rows(rows: np.ndarray, counts: np.ndarray | None = None) -> np.ndarray:

@@ -312,6 +312,7 @@ struct BatchDev {
     unsigned int* queues2;       // [0] seed fast-path queue; [1] start of the medium small-tier records; [2] square queue;
                                  // [3] small-tier records (the small list without its holes)
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
+    unsigned long long* match_cells;  // the part of `cells` in match segments (emitted without a DP)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };
 

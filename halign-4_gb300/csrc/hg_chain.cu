@@ -688,7 +688,10 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
             slot = slot + __shfl_sync(FULL, sincl, 31);
         }
         if (open && lane == 0) put_match(o_sid, o_rs, o_qs, o_len);
-        if (lane == 0 && match_cells && b.cells) atomicAdd(b.cells, match_cells);
+        if (lane == 0 && match_cells && b.cells) {
+            atomicAdd(b.cells, match_cells);
+            atomicAdd(b.match_cells, match_cells);
+        }
         if (lane == 0) b.s_n[q] = (int32_t)nkept;
     }
     small_holes();  // the rest of this warp's last block

@@ -3,9 +3,10 @@
 // Layout conventions (all device buffers live in HBM, owned by an hg_index
 // or an hg_ctx handle):
 //   * queries: 2-bit packed, A=0 C=1 G=2 T=3, base i of a query at bits
-//     2*(i%4) of byte i/4; every query starts on a 16-byte boundary so a CTA
-//     streams it with aligned uint4 loads.  Bytes that are not A/C/G/T are
-//     kept losslessly as exception runs {start, len, byte}.
+//     2*(i%4) of byte i/4; every query starts on a 16-byte boundary and keeps
+//     64 bytes of slack, so kernels read its bases as 8-byte words (two
+//     adjacent words funnel-shifted into a register window).  Bytes that are
+//     not A/C/G/T are kept losslessly as exception runs {start, len, byte}.
 //   * the center: one DNA5 code per base (ScoreChar2Idx, include/align.h:72-89)
 //     for the gap-fill DP, plus a minimizer hash table (see hg_index).
 #pragma once

@@ -147,30 +147,40 @@ __device__ __forceinline__ uint32_t lane_int_z(int z0, int xt1, int vt1, int ut,
 }
 
 // Two independent cells at once, one per 16-bit half (two segments of the
-// same shape and gap mode side by side): lane_int_z's recurrence on int16x2
-// SIMD operations, so one instruction updates both segments.  Every value
-// stays in [-32, 64], far inside int16.  Returns the two 4-bit direction
-// codes at bits 0-3 (low half) and 16-19 (high half).
+// same shape and gap mode side by side): lane_int_z's recurrence on both
+// halves of 32-bit words.  Every value carries a bias of kPB per half, so
+// each half stays non-negative and below 0x8000 (real values lie in
+// [-32, 64]); plain 32-bit adds and subtracts then act on both halves at
+// once with no carry or borrow crossing between them, and the unsigned
+// 16x2 max / min order biased values as the signed ones would.  A
+// comparison p > q (p >= q) is bit 15 of a half of 0x7fff + p - q
+// (0x8000 + p - q).  Returns the two 4-bit direction codes at bits 0-3
+// (low half) and 16-19 (high half).
+constexpr uint32_t kPB = 64;
+constexpr uint32_t kPB2 = kPB * 0x00010001u;
+
 template <int MODE>
 __device__ __forceinline__ uint32_t lane16x2(uint32_t z0, uint32_t xt1, uint32_t vt1, uint32_t ut, uint32_t yt,
                                              uint32_t& u, uint32_t& v, uint32_t& x, uint32_t& y)
 {
-    const uint32_t a0 = __vadd2(xt1, vt1), b0 = __vadd2(yt, ut);
-    const uint32_t m = __vmaxs2(z0, a0);
+    const uint32_t a0 = xt1 + vt1 - kPB2, b0 = yt + ut - kPB2;
+    const uint32_t m = __vmaxu2(z0, a0);
+    const uint32_t z = __vminu2(__vmaxu2(m, b0), (21u + kPB) * 0x00010001u);  // min(., 21)
+    u = z + kPB2 - vt1;
+    v = z + kPB2 - ut;
+    const uint32_t a = a0 - z + (6u + kPB) * 0x00010001u;  // a0 - (z - q)
+    const uint32_t b = b0 - z + (6u + kPB) * 0x00010001u;
+    x = __vmaxu2(a, kPB2);
+    y = __vmaxu2(b, kPB2);
     // MODE 1 (left-aligned): strict compares; MODE 2 (right-aligned): ties
     // go the other way, i.e. >=
-    const uint32_t ca = MODE == 1 ? __vcmpgts2(a0, z0) : __vcmpges2(a0, z0);
-    const uint32_t c2 = MODE == 1 ? __vcmpgts2(b0, m) : __vcmpges2(b0, m);
-    const uint32_t z = __vmins2(__vmaxs2(m, b0), 0x00150015u);  // min(., 21)
-    u = __vsub2(z, vt1);
-    v = __vsub2(z, ut);
-    const uint32_t nzq = __vsub2(0x00060006u, z);                  // 6 - z = -(z - q)
-    const uint32_t a = __vadd2(a0, nzq), b = __vadd2(b0, nzq);
-    x = __vmaxs2(a, 0u);
-    y = __vmaxs2(b, 0u);
-    const uint32_t ce = MODE == 1 ? __vcmpgts2(a, 0u) : __vcmpges2(a, 0u);
-    const uint32_t cf = MODE == 1 ? __vcmpgts2(b, 0u) : __vcmpges2(b, 0u);
-    return (c2 & 0x00020002u) | (ca & ~c2 & 0x00010001u) | (ce & 0x00040004u) | (cf & 0x00080008u);
+    constexpr uint32_t K = MODE == 1 ? 0x7fff7fffu : 0x80008000u;
+    const uint32_t fa = a0 + K - z0;   // a0 > z0
+    const uint32_t fc = b0 + K - m;    // b0 > max(z0, a0)
+    const uint32_t fe = a + K - kPB2;  // a > 0
+    const uint32_t ff = b + K - kPB2;  // b > 0
+    constexpr uint32_t H = 0x80008000u;
+    return ((fc & H) >> 14) | ((fa & ~fc & H) >> 15) | ((fe & H) >> 13) | ((ff & H) >> 12);
 }
 
 // 64 bases of 2-bit codes from base `pos` of a packed stream (base i at bits
@@ -328,30 +338,33 @@ __device__ __forceinline__ void small_pair(const IndexDev& ix, const BatchDev& b
         for (int i = 0; i < IMAX; ++i)
             icp[i] = (uint32_t)((ilo[0] >> (2 * i)) & 3u) | (uint32_t)((ilo[1] >> (2 * i)) & 3u) << 16;
     }
+    // (biased by kPB per half: lane16x2's representation)
 #pragma unroll
-    for (int i = 0; i < IMAX; ++i) s1[i] = 0, s2[i] = 0;
-    const uint32_t k6 = 0x00060006u;
+    for (int i = 0; i < IMAX; ++i) s1[i] = kPB2, s2[i] = kPB2;
+    const uint32_t k6 = (6u + kPB) * 0x00010001u, k0 = kPB2;
     for (int o = 0; o < outer; ++o) {
         const int sh = 2 * (o & 31);
         const uint32_t ocp = (uint32_t)(((o < 32 ? olo[0] : ohi[0]) >> sh) & 3u) |
                              (uint32_t)(((o < 32 ? olo[1] : ohi[1]) >> sh) & 3u) << 16;
-        uint32_t c1 = 0, c2 = o ? k6 : 0u;
+        uint32_t c1 = k0, c2 = o ? k6 : k0;
         uint32_t wd[NW];
 #pragma unroll
         for (int k = 0; k < NW; ++k) wd[k] = 0;
 #pragma unroll
         for (int i = 0; i < IMAX; ++i) {
             if (i < inner) {
-                // z0 = 21 on a match, 12 on a mismatch, per half: 12 ^ (eq & (12 ^ 21))
-                const uint32_t z0 = (__vcmpeq2(icp[i], ocp) & 0x00190019u) ^ 0x000c000cu;
+                // z0 = 21 on a match, 12 on a mismatch, per half (biased):
+                // mismatch flag t in {0, 1}, z0 = 21 + kPB - 9 t
+                const uint32_t t = __vminu2(icp[i] ^ ocp, 0x00010001u);
+                const uint32_t z0 = (21u + kPB) * 0x00010001u - 9u * t;
                 uint32_t u, v, x, y, d;
                 if (TINNER) {
-                    const uint32_t ut = o ? s1[i] : (i ? k6 : 0u), yt = o ? s2[i] : 0u;
+                    const uint32_t ut = o ? s1[i] : (i ? k6 : k0), yt = o ? s2[i] : k0;
                     d = lane16x2<MODE>(z0, c1, c2, ut, yt, u, v, x, y);
                     c1 = x, c2 = v, s1[i] = u, s2[i] = y;
                 } else {
-                    const uint32_t xt = o ? s1[i] : 0u, vt = o ? s2[i] : (i ? k6 : 0u);
-                    const uint32_t ut = i ? c1 : (o ? k6 : 0u), yt = i ? c2 : 0u;
+                    const uint32_t xt = o ? s1[i] : k0, vt = o ? s2[i] : (i ? k6 : k0);
+                    const uint32_t ut = i ? c1 : (o ? k6 : k0), yt = i ? c2 : k0;
                     d = lane16x2<MODE>(z0, xt, vt, ut, yt, u, v, x, y);
                     c1 = u, c2 = y, s1[i] = x, s2[i] = v;
                 }
@@ -362,34 +375,43 @@ __device__ __forceinline__ void small_pair(const IndexDev& ix, const BatchDev& b
         for (int k = 0; k < NW; ++k)
             if (k < stride) dirs[(o * stride + k) * T + tid] = wd[k];
     }
-    for (int h = 0; h < 2; ++h) {
-        const SmallRec& r = h ? r1 : r0;
-        uint32_t* out = b.cig_seg + r.out;
-        int n = 0;
-        uint32_t run_op = 0xffu, run_len = 0;
-        auto push = [&](uint32_t op, uint32_t len) {
-            if (op == run_op) {
-                run_len += len;
-            } else {
-                if (run_len) out[n++] = run_len << 4 | run_op;
-                run_op = op, run_len = len;
-            }
-        };
-        int ti = tn - 1, qj = qn - 1, state = 0;
-        while (ti >= 0 && qj >= 0) {
-            const int o = TINNER ? qj : ti, i = TINNER ? ti : qj;
-            const uint32_t nib = (dirs[(o * stride + (i >> 2)) * T + tid] >> (8 * (i & 3) + 4 * h)) & 0xfu;
-            if (state == 0) state = nib & 3u;
-            else if (!((nib >> (state + 1)) & 1u)) state = 0;
-            if (state == 0) state = nib & 3u;
-            if (state == 0) push(0, 1), --ti, --qj;
-            else if (state == 1) push(2, 1), --ti;
-            else push(1, 1), --qj;
+    // both tracebacks step together: two independent dependency chains
+    // (direction reads and state updates) in flight per thread
+    uint32_t* out[2] = {b.cig_seg + r0.out, b.cig_seg + r1.out};
+    int n[2] = {0, 0}, ti[2] = {tn - 1, tn - 1}, qj[2] = {qn - 1, qn - 1}, state[2] = {0, 0};
+    uint32_t run_op[2] = {0xffu, 0xffu}, run_len[2] = {0, 0};
+    auto push = [&](int h, uint32_t op, uint32_t len) {
+        if (op == run_op[h]) {
+            run_len[h] += len;
+        } else {
+            if (run_len[h]) out[h][n[h]++] = run_len[h] << 4 | run_op[h];
+            run_op[h] = op, run_len[h] = len;
         }
-        if (ti >= 0) push(2, (uint32_t)(ti + 1));
-        if (qj >= 0) push(1, (uint32_t)(qj + 1));
-        if (run_len) out[n++] = run_len << 4 | run_op;
-        b.seg[r.sid].nops = n;
+    };
+    for (;;) {
+        const bool act0 = ti[0] >= 0 && qj[0] >= 0, act1 = ti[1] >= 0 && qj[1] >= 0;
+        if (!act0 && !act1) break;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!(h ? act1 : act0)) continue;
+            const int o = TINNER ? qj[h] : ti[h], i = TINNER ? ti[h] : qj[h];
+            const uint32_t nib = (dirs[(o * stride + (i >> 2)) * T + tid] >> (8 * (i & 3) + 4 * h)) & 0xfu;
+            int st = state[h];
+            if (st == 0) st = nib & 3u;
+            else if (!((nib >> (st + 1)) & 1u)) st = 0;
+            if (st == 0) st = nib & 3u;
+            state[h] = st;
+            if (st == 0) push(h, 0, 1), --ti[h], --qj[h];
+            else if (st == 1) push(h, 2, 1), --ti[h];
+            else push(h, 1, 1), --qj[h];
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (ti[h] >= 0) push(h, 2, (uint32_t)(ti[h] + 1));
+        if (qj[h] >= 0) push(h, 1, (uint32_t)(qj[h] + 1));
+        if (run_len[h]) out[h][n[h]++] = run_len[h] << 4 | run_op[h];
+        b.seg[(h ? r1 : r0).sid].nops = n[h];
     }
 }
 
@@ -2052,7 +2074,7 @@ __global__ void lane16x2_selftest_kernel(unsigned* bad)
         const int hi[5] = {zs[k % NZ], (k / NZ) % NX, (k / (NZ * NX)) % NV, (k / (NZ * NX * NV)) % NV,
                            (k / (NZ * NX * NV * NV)) % NX};
         uint32_t pk[5];
-        for (int j = 0; j < 5; ++j) pk[j] = (uint32_t)lo[j] | (uint32_t)hi[j] << 16;
+        for (int j = 0; j < 5; ++j) pk[j] = (uint32_t)(lo[j] + (int)kPB) | (uint32_t)(hi[j] + (int)kPB) << 16;
         uint32_t u2, v2, x2, y2;
         const uint32_t d2 = mode == 1 ? lane16x2<1>(pk[0], pk[1], pk[2], pk[3], pk[4], u2, v2, x2, y2)
                                       : lane16x2<2>(pk[0], pk[1], pk[2], pk[3], pk[4], u2, v2, x2, y2);
@@ -2062,9 +2084,9 @@ __global__ void lane16x2_selftest_kernel(unsigned* bad)
             const uint32_t d = mode == 1 ? lane_int_z<1>(in[0], in[1], in[2], in[3], in[4], u, v, x, y)
                                          : lane_int_z<2>(in[0], in[1], in[2], in[3], in[4], u, v, x, y);
             const int sh = 16 * h;
-            const bool ok = ((d2 >> sh) & 0xfu) == d && (int)(int16_t)(u2 >> sh) == u &&
-                            (int)(int16_t)(v2 >> sh) == v && (int)(int16_t)(x2 >> sh) == x &&
-                            (int)(int16_t)(y2 >> sh) == y;
+            auto val = [&](uint32_t w) { return (int)((w >> sh) & 0xffffu) - (int)kPB; };
+            const bool ok = ((d2 >> sh) & 0xfu) == d && val(u2) == u && val(v2) == v && val(x2) == x &&
+                            val(y2) == y;
             if (!ok) atomicAdd(bad, 1u);
         }
     }

@@ -138,23 +138,11 @@ std::string cleaned(const std::string& s)
     return o;
 }
 
-}  // namespace
-
-extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k,
-                              int w, int64_t chunk_queries, int64_t* n_aligned)
+// The streamed run once the center record(s) are known.
+int align_stream(const std::vector<std::string>& cnames, const std::vector<std::string>& cdescs,
+                 const std::vector<std::string>& cseqs, const char* queries_fasta, const char* out_fasta, int k, int w,
+                 int64_t chunk_queries, int64_t* n_aligned)
 {
-    if (!center_fasta || !queries_fasta || !out_fasta || chunk_queries <= 0)
-        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: bad arguments");
-    // the center FASTA: one record (align to its consensus) or several
-    // (multi-reference mode: each query to its best reference)
-    Reader cr(center_fasta);
-    std::vector<std::string> cnames, cdescs, cseqs;
-    {
-        std::string name, desc, seq;
-        while (cr.ok() && cr.next(name, desc, seq)) cnames.push_back(name), cdescs.push_back(desc), cseqs.push_back(seq);
-    }
-    if (cseqs.empty() || cseqs[0].empty())
-        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: no center record in " + std::string(center_fasta));
     const bool multi = cseqs.size() > 1;
     const int64_t L = (int64_t)cseqs[0].size();
     for (const auto& s : cseqs)
@@ -301,4 +289,90 @@ extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fast
     if (rc) return hg::set_error(rc, err);
     if (n_aligned) *n_aligned = total;
     return out ? HG_OK : hg::set_error(HG_ERR_ARG, "hg_align_fasta: write failed");
+}
+
+}  // namespace
+
+extern "C" int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k,
+                              int w, int64_t chunk_queries, int64_t* n_aligned)
+{
+    if (!center_fasta || !queries_fasta || !out_fasta || chunk_queries <= 0)
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: bad arguments");
+    // the center FASTA: one record (align to its consensus) or several
+    // (multi-reference mode: each query to its best reference)
+    Reader cr(center_fasta);
+    std::vector<std::string> cnames, cdescs, cseqs;
+    {
+        std::string name, desc, seq;
+        while (cr.ok() && cr.next(name, desc, seq)) cnames.push_back(name), cdescs.push_back(desc), cseqs.push_back(seq);
+    }
+    if (cseqs.empty() || cseqs[0].empty())
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta: no center record in " + std::string(center_fasta));
+    return align_stream(cnames, cdescs, cseqs, queries_fasta, out_fasta, k, w, chunk_queries, n_aligned);
+}
+
+extern "C" int hg_build_center(const char* queries_fasta, int64_t cons_n, char* out, int64_t cap, int64_t* len)
+{
+    if (!queries_fasta || cons_n <= 0 || !len) return hg::set_error(HG_ERR_ARG, "hg_build_center: bad arguments");
+    // preprocessInputFasta's Top-K (src/utils/preprocess.cpp:111-150,
+    // TopKLongestSelector, src/consensus/selector.cpp): the cons_n longest
+    // records, ties to the earlier record, ordered longest first
+    std::vector<std::pair<int64_t, int64_t>> lens;  // (length, input order)
+    {
+        Reader r(queries_fasta);
+        if (!r.ok()) return hg::set_error(HG_ERR_ARG, "hg_build_center: cannot read " + std::string(queries_fasta));
+        std::string name, desc, seq;
+        for (int64_t i = 0; r.next(name, desc, seq); ++i) lens.emplace_back((int64_t)seq.size(), i);
+    }
+    if (lens.empty()) return hg::set_error(HG_ERR_ARG, "hg_build_center: no record in " + std::string(queries_fasta));
+    auto better = [](const std::pair<int64_t, int64_t>& a, const std::pair<int64_t, int64_t>& b) {
+        return a.first != b.first ? a.first > b.first : a.second < b.second;
+    };
+    const size_t kk = (size_t)std::min<int64_t>(cons_n, (int64_t)lens.size());
+    std::partial_sort(lens.begin(), lens.begin() + (long)kk, lens.end(), better);
+    lens.resize(kk);
+    std::vector<std::pair<int64_t, int64_t>> by_order(lens);
+    std::sort(by_order.begin(), by_order.end(), [](auto& a, auto& b) { return a.second < b.second; });
+    std::vector<std::string> rows(kk);
+    {
+        Reader r(queries_fasta);
+        std::string name, desc, seq;
+        size_t j = 0;
+        for (int64_t i = 0; j < kk && r.next(name, desc, seq); ++i) {
+            if (i != by_order[j].second) continue;
+            const size_t rank = (size_t)(std::lower_bound(lens.begin(), lens.end(), by_order[j], better) - lens.begin());
+            rows[rank] = cleaned(seq);  // preprocessing cleans every record
+            ++j;
+        }
+    }
+    // the MSA of the selection is the caller's tool; without one the records
+    // must already share one length (the CLI with an MSA command that copies)
+    for (const auto& s : rows)
+        if (s.size() != rows[0].size())
+            return hg::set_error(HG_ERR_ARG, "hg_build_center: the selected records differ in length (the reference "
+                                             "CLI aligns them with its external MSA tool first)");
+    std::string cons;
+    const int rc = hg::consensus_of_rows(rows, (size_t)cons_n, cons);
+    if (rc) return rc;
+    *len = (int64_t)cons.size();
+    if ((int64_t)cons.size() > cap || (!out && !cons.empty()))
+        return hg::set_error(HG_ERR_CAPACITY, "hg_build_center: cap below the center length");
+    std::memcpy(out, cons.data(), cons.size());
+    return HG_OK;
+}
+
+extern "C" int hg_align_fasta_consensus(const char* queries_fasta, const char* out_fasta, int k, int w, int64_t cons_n,
+                                        int64_t chunk_queries, int64_t* n_aligned)
+{
+    if (!queries_fasta || !out_fasta || chunk_queries <= 0 || cons_n <= 0)
+        return hg::set_error(HG_ERR_ARG, "hg_align_fasta_consensus: bad arguments");
+    int64_t L = 0;
+    int rc = hg_build_center(queries_fasta, cons_n, nullptr, 0, &L);
+    if (rc != HG_OK && rc != HG_ERR_CAPACITY) return rc;
+    std::string cons((size_t)L, '\0');
+    rc = hg_build_center(queries_fasta, cons_n, cons.data(), L, &L);
+    if (rc) return rc;
+    if (cons.empty()) return hg::set_error(HG_ERR_ARG, "hg_align_fasta_consensus: empty center");
+    // the CLI writes the center as ">consensus" (consensus::writeConsensusFasta)
+    return align_stream({"consensus"}, {""}, {cons}, queries_fasta, out_fasta, k, w, chunk_queries, n_aligned);
 }

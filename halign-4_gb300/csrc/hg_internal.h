@@ -85,6 +85,11 @@ int workspace(Workspace** out);
 int index_create(const char* center, int64_t len, int k, int w, const hg_params_t* params, bool dp_consensus,
                  hg_index_t** out);
 
+// generateConsensusSequence over aligned records of one length (at most
+// `limit` of them, 0 = all; batch size 4096 with the reference's dropped
+// record after each full batch): the per-column majority, on the device.
+int consensus_of_rows(const std::vector<std::string>& recs, size_t limit, std::string& out);
+
 // Length of an index's center.
 int64_t index_length(const hg_index_t* ix);
 

@@ -216,33 +216,42 @@ int cons_ctx_of(hg_refset_t* R, hg_ctx_t** out)
     return HG_OK;
 }
 
-// generateConsensusSequence (src/consensus/consensus.cpp:611-703) over the
-// references as the aligned records, batch size 4096: SiteCount per column
-// (hg_count_rows on the device), the record read after each full batch
-// dropped as the reference's loop does, pickConsensusChar per column.
+// The consensus of the references when they share one length (their
+// alignment by an MSA command that returns them unchanged); otherwise none.
 int refs_consensus(const std::vector<std::string>& refs, std::string& out)
 {
-    const size_t L = refs[0].size();
     for (const auto& r : refs)
-        if (r.size() != L) return HG_OK;  // no consensus without an alignment of the references
+        if (r.size() != refs[0].size()) return HG_OK;
+    return hg::consensus_of_rows(refs, 0, out);
+}
+
+}  // namespace
+
+// generateConsensusSequence (src/consensus/consensus.cpp:611-703) over
+// aligned records of one length, batch size 4096: SiteCount per column
+// (hg_count_rows on the device) over at most `limit` records (0: all), the
+// record read after each full batch dropped as the reference's loop does,
+// pickConsensusChar per column.
+int hg::consensus_of_rows(const std::vector<std::string>& recs, size_t limit, std::string& out)
+{
+    if (recs.empty()) return set_error(HG_ERR_ARG, "consensus: no records");
+    const size_t L = recs[0].size();
     const size_t batch = 4096;
     std::vector<uint32_t> counts(7 * L, 0);
     std::string rows;
-    size_t i = 0;
-    while (i < refs.size()) {
+    size_t i = 0, num = 0;
+    while (i < recs.size() && (limit == 0 || num < limit)) {
         rows.clear();
         size_t m = 0;
-        for (; m < batch && i < refs.size(); ++m, ++i) rows += refs[i];
+        for (; m < batch && i < recs.size() && (limit == 0 || num < limit); ++m, ++i, ++num) rows += recs[i];
         const int rc = hg_count_rows(rows.data(), (int64_t)m, (int64_t)L, (int64_t)L, counts.data(), 1);
         if (rc) return rc;
-        if (m == batch && i < refs.size()) ++i;  // read, then dropped
+        if (m == batch && i < recs.size()) ++i;  // read, then dropped
     }
     out.resize(L);
     for (size_t c = 0; c < L; ++c) out[c] = pick_consensus(&counts[7 * c]);
     return HG_OK;
 }
-
-}  // namespace
 
 extern "C" int hg_sketch_batch(const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
                                const int64_t* exc_off, int64_t n, int k, int sketch_size, int noncanonical, int seed,

@@ -739,7 +739,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = c->cig_seg.alloc(c->cig_cap)) || (e = c->cig.alloc(c->cig_cap)) ||
         (e = c->n_cig.alloc(max_queries)) || (e = c->has_ins.alloc(max_queries)) ||
         (e = c->rows.alloc((size_t)max_queries * c->row_stride)) || (e = c->counts.alloc(L * 7)) ||
-        (e = c->ins.alloc(L + 1)) || (e = c->status.alloc(max_queries)) || (e = c->control.alloc(kControlWords)) || (e = c->cells.alloc(1)) || (e = c->work.alloc(4)) ||
+        (e = c->ins.alloc(L + 1)) || (e = c->status.alloc(max_queries)) || (e = c->control.alloc(kControlWords)) || (e = c->cells.alloc(2)) || (e = c->work.alloc(4)) ||
         (e = c->cig_off.alloc(max_queries + 1)) || (e = c->cig_compact.alloc(max_bases / 4 + 1024))) {
         hg_ctx_destroy(c);
         return cuda_fail(e, "hg_ctx_create: device allocation");
@@ -749,7 +749,7 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         return cuda_fail(e, "hg_ctx_create: memset");
     }
     cudaMemset(c->counts.p, 0, sizeof(uint32_t) * L * 7);
-    cudaMemset(c->cells.p, 0, sizeof(unsigned long long));
+    cudaMemset(c->cells.p, 0, 2 * sizeof(unsigned long long));
     cudaMemset(c->work.p, 0, 4 * sizeof(unsigned long long));
     cudaMemset(c->ins.p, 0, sizeof(uint32_t) * (L + 1));
     for (auto& ev : c->ev) cudaEventCreate(&ev);
@@ -864,6 +864,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.n_large = reinterpret_cast<unsigned int*>(ctl + 8);
     b.n_exact = reinterpret_cast<unsigned int*>(ctl + 9);
     b.cells = c->cells.p;
+    b.match_cells = c->cells.p + 1;
     b.a_base = c->a_base.p, b.a_n = c->a_n.p, b.ent_cnt = c->ent_cnt.p;
     b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
     b.chain_meta = c->chain_meta.p;
@@ -1451,7 +1452,7 @@ extern "C" int hg_run_staged(hg_ctx_t* c)
     c->last_total_ms = 0;
     std::fill(c->last_stage_ms, c->last_stage_ms + 8, 0.0f);
     c->last_launches = 0;
-    HG_CUDA(cudaMemsetAsync(c->cells.p, 0, sizeof(unsigned long long), c->st));
+    HG_CUDA(cudaMemsetAsync(c->cells.p, 0, 2 * sizeof(unsigned long long), c->st));
     HG_CUDA(cudaMemsetAsync(c->run_flags.p, 0, sizeof(uint32_t), c->st));
     HG_CUDA(cudaEventRecord(c->run_ev[0], c->st));
     for (const SubPlan& sp : c->staged_plan) {
@@ -1482,6 +1483,18 @@ extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int
         HG_CUDA(cudaMemcpy(&v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
         *cells = (int64_t)v;
     }
+    return HG_OK;
+}
+
+extern "C" int hg_last_cells(hg_ctx_t* c, int64_t* cells, int64_t* match_cells)
+{
+    if (!c) return fail(HG_ERR_ARG, "hg_last_cells: null context");
+    cudaSetDevice(c->ix->device);
+    HG_CUDA(cudaStreamSynchronize(c->st));
+    unsigned long long v[2] = {0, 0};
+    HG_CUDA(cudaMemcpy(v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
+    if (cells) *cells = (int64_t)v[0];
+    if (match_cells) *match_cells = (int64_t)v[1];
     return HG_OK;
 }
 

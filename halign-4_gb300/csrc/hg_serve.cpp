@@ -275,6 +275,75 @@ extern "C" int64_t hg_serve_submit(hg_server_t* S, const char* seq, int64_t len)
     return id;
 }
 
+extern "C" int64_t hg_serve_submit_many(hg_server_t* S, const char* seqs, const int64_t* offsets, int64_t n)
+{
+    if (!S || n < 0 || (n > 0 && (!seqs || !offsets)))
+        return -hg::set_error(HG_ERR_ARG, "hg_serve_submit_many: bad arguments");
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t len = offsets[i + 1] - offsets[i];
+        if (len < 0) return -hg::set_error(HG_ERR_ARG, "hg_serve_submit_many: offsets not ascending");
+        if (len > S->slot_b) return -hg::set_error(HG_ERR_CAPACITY, "hg_serve_submit_many: request longer than slot_bases");
+    }
+    // the copies are made before the lock; one time stamp for the burst
+    std::vector<Request> burst((size_t)n);
+    const auto now = Clock::now();
+    for (int64_t i = 0; i < n; ++i) {
+        burst[i].seq.assign(seqs + offsets[i], (size_t)(offsets[i + 1] - offsets[i]));
+        burst[i].t_in = now;
+    }
+    int64_t first;
+    {
+        std::lock_guard<std::mutex> lock(S->mu);
+        if (S->error) return -hg::set_error(S->error, S->error_msg);
+        if (!S->have_first && n) S->t_first = now, S->have_first = true;
+        first = S->base_id + (int64_t)S->reqs.size();
+        for (int64_t i = 0; i < n; ++i) {
+            S->reqs.push_back(std::move(burst[i]));
+            S->pending.push_back(first + i);
+        }
+    }
+    S->cv_work.notify_one();
+    return first;
+}
+
+extern "C" int64_t hg_serve_results(hg_server_t* S, int64_t max_n, int64_t* ids, uint32_t* status,
+                                    double* latency_ms, uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off,
+                                    int timeout_ms)
+{
+    if (!S || max_n <= 0 || !ids || !cigar_off || (cigar_cap > 0 && !cigar))
+        return -hg::set_error(HG_ERR_ARG, "hg_serve_results: bad arguments");
+    std::unique_lock<std::mutex> lock(S->mu);
+    auto ready = [&] { return !S->done.empty() || S->error; };
+    if (timeout_ms < 0) S->cv_done.wait(lock, ready);
+    else if (!S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), ready)) return 0;
+    if (S->done.empty()) return -hg::set_error(S->error, S->error_msg);
+    int64_t m = 0, used = 0;
+    cigar_off[0] = 0;
+    while (m < max_n && !S->done.empty()) {
+        const int64_t rid = S->done.front();
+        Request& r = S->reqs[(size_t)(rid - S->base_id)];
+        const int64_t nc = (int64_t)r.cigar.size();
+        if (used + nc > cigar_cap) {
+            if (m == 0) return -hg::set_error(HG_ERR_CAPACITY, "hg_serve_results: cigar_cap below the next CIGAR");
+            break;
+        }
+        S->done.pop_front();
+        ids[m] = rid;
+        if (status) status[m] = r.status;
+        if (latency_ms) latency_ms[m] = r.latency_ms;
+        if (nc) std::memcpy(cigar + used, r.cigar.data(), sizeof(uint32_t) * (size_t)nc);
+        used += nc;
+        cigar_off[++m] = used;
+        std::vector<uint32_t>().swap(r.cigar);
+        r.returned = true;
+    }
+    while (!S->reqs.empty() && S->reqs.front().returned) {
+        S->reqs.pop_front();
+        ++S->base_id;
+    }
+    return m;
+}
+
 extern "C" int hg_serve_result(hg_server_t* S, int64_t* id, uint32_t* status, double* latency_ms, uint32_t* cigar,
                                int64_t cap, int64_t* n_cigar, int timeout_ms)
 {

@@ -1,5 +1,5 @@
 // hg_shim.cpp - the C++ call surface of HAlign-4's seed.h, anchor.h,
-// align.h, ksw2.h and consensus.h (include/halign4/*.h) over the GB300 C ABI
+// align.h, ksw2.h, consensus.h and mash.h (include/halign4/*.h) over the GB300 C ABI
 // (include/halign_gb300.h).  Built into libhalign4_dropin.so, which links
 // libhalign_gb300.so; HAlign-4 links this library in place of the reference
 // sources of those functions (minimizer.cpp, anchor.cpp, align.cpp,
@@ -16,7 +16,9 @@
 // with the C ABI's message (ksw_extz2_sse, a C function, leaves the reset
 // result instead).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
+#include <limits>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -30,6 +32,7 @@
 #include "halign4/anchor.h"
 #include "halign4/consensus.h"
 #include "halign4/ksw2.h"
+#include "halign4/mash.h"
 #include "halign4/seed.h"
 #include "halign_gb300.h"
 
@@ -671,3 +674,83 @@ std::string generateConsensusSequence(const FilePath& aligned_fasta, const FileP
     return cons;
 }
 }  // namespace consensus
+
+// ------------------------------------------------------------------ MinHash
+
+namespace mash
+{
+Sketch sketchFromSequence(const std::string& seq, std::size_t k, std::size_t sketch_size, bool noncanonical, int seed)
+{
+    Sketch sk;
+    sk.k = k;
+    sk.noncanonical = noncanonical;
+    if (k == 0 || sketch_size == 0 || seq.size() < k || k > 32) return sk;
+    if (sketch_size > (std::size_t)HG_SKETCH_MAX)
+        throw std::invalid_argument("mash::sketchFromSequence: sketch_size above HG_SKETCH_MAX");
+    const int64_t off[2] = {0, (int64_t)seq.size()};
+    int64_t pb = 0, ne = 0;
+    if (hg_pack(seq.data(), off, 1, nullptr, 0, nullptr, nullptr, 0, nullptr, &pb, &ne) != HG_OK)
+        raise("sketchFromSequence");
+    std::vector<uint8_t> packed((size_t)std::max<int64_t>(pb, 16));
+    std::vector<int32_t> exc((size_t)std::max<int64_t>(ne, 1) * 3);
+    int64_t poff = 0, eoff[2] = {0, 0};
+    if (hg_pack(seq.data(), off, 1, packed.data(), (int64_t)packed.size(), &poff, exc.data(), ne, eoff, nullptr,
+                nullptr) != HG_OK)
+        raise("sketchFromSequence");
+    const int32_t qlen = (int32_t)seq.size();
+    std::vector<uint64_t> h(sketch_size);
+    int32_t cnt = 0;
+    if (hg_sketch_batch(packed.data(), &poff, &qlen, exc.data(), eoff, 1, (int)k, (int)sketch_size,
+                        noncanonical ? 1 : 0, seed, h.data(), (int64_t)sketch_size, &cnt) != HG_OK)
+        raise("sketchFromSequence");
+    sk.hashes.assign(h.begin(), h.begin() + cnt);
+    return sk;
+}
+
+std::size_t intersectionSizeSortedUnique(const std::vector<hash_t>& a, const std::vector<hash_t>& b) noexcept
+{
+    std::size_t i = 0, j = 0, n = 0;
+    while (i < a.size() && j < b.size()) {
+        if (a[i] < b[j]) ++i;
+        else if (b[j] < a[i]) ++j;
+        else ++n, ++i, ++j;
+    }
+    return n;
+}
+
+double jaccard(const Sketch& a, const Sketch& b)
+{
+    if (a.k != b.k) throw std::invalid_argument("mash::jaccard: mismatched k");
+    if (a.hashes.empty() && b.hashes.empty()) return 1.0;
+    if (a.hashes.empty() || b.hashes.empty()) return 0.0;
+    const std::size_t inter = intersectionSizeSortedUnique(a.hashes, b.hashes);
+    return (double)inter / (double)std::min(a.hashes.size(), b.hashes.size());
+}
+
+double mashDistanceFromJaccard(double j, std::size_t k)
+{
+    if (k == 0) throw std::invalid_argument("mash::mashDistanceFromJaccard: k must be > 0");
+    if (!(j > 0.0)) return std::numeric_limits<double>::infinity();
+    if (j >= 1.0) return 0.0;
+    const double x = (2.0 * j) / (1.0 + j);
+    if (!(x > 0.0)) return std::numeric_limits<double>::infinity();
+    return -std::log(x) / (double)k;
+}
+
+double aniFromJaccard(double j, std::size_t k)
+{
+    if (k == 0) throw std::invalid_argument("mash::aniFromJaccard: k must be > 0");
+    if (!(j > 0.0)) return 0.0;
+    if (j >= 1.0) return 1.0;
+    const double x = (2.0 * j) / (1.0 + j);
+    if (!(x > 0.0)) return 0.0;
+    return std::min(1.0, std::max(0.0, std::pow(x, 1.0 / (double)k)));
+}
+
+double aniFromMashDistance(double d)
+{
+    if (!std::isfinite(d)) return 0.0;
+    if (d <= 0.0) return 1.0;
+    return std::min(1.0, std::max(0.0, std::exp(-d)));
+}
+}  // namespace mash

@@ -196,40 +196,50 @@ class NativeServer:
         errors = []
 
         def drain():
-            cap = 1 << 16
+            max_n, cap = 4096, 1 << 22
             buf = np.zeros(cap, np.uint32)
-            rid, st, lat, nc = C.c_int64(), C.c_uint32(), C.c_double(), C.c_int64()
+            rid = np.zeros(max_n, np.int64)
+            st = np.zeros(max_n, np.uint32)
+            coff = np.zeros(max_n + 1, np.int64)
+            vp = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
             got = 0
             while got < n:
-                r = self._lib.hg_serve_result(self.h, C.byref(rid), C.byref(st), C.byref(lat),
-                                              buf.ctypes.data_as(C.c_void_p), cap, C.byref(nc), 1000)
-                if r < 0:
-                    errors.append(-r)
+                m = self._lib.hg_serve_results(self.h, max_n, vp(rid), vp(st), None, vp(buf), cap, vp(coff), 1000)
+                if m < 0:
+                    errors.append(-m)
                     return
-                if r == 0:
-                    continue
-                got += 1
-                status[rid.value - base] = st.value
+                status[rid[:m] - base] = st[:m]
                 if keep_results:
-                    results[rid.value - base] = buf[: min(nc.value, cap)].copy()
+                    for j in range(m):
+                        results[int(rid[j] - base)] = buf[coff[j]: coff[j + 1]].copy()
+                got += m
 
-        base = None
+        # requests whose arrival time has passed are queued together (one
+        # hg_serve_submit_many per loop turn), the rest when they are due
+        raw = np.frombuffer(seqs, np.uint8) if len(seqs) else np.zeros(1, np.uint8)
+        offsets = np.ascontiguousarray(offsets, np.int64)
         t0 = time.perf_counter()
-        th = None
-        mv = memoryview(seqs)
-        for i in range(n):
-            if arrivals is not None:
-                wait = arrivals[i] - (time.perf_counter() - t0)
-                if wait > 0:
-                    time.sleep(wait)
-            rid = self._lib.hg_serve_submit(self.h, bytes(mv[offsets[i]:offsets[i + 1]]), int(offsets[i + 1] - offsets[i]))
-            if rid < 0:
-                self._check(-rid)
+        base, th, i = None, None, 0
+        while i < n:
+            if arrivals is None:
+                j = n
+            else:
+                now = time.perf_counter() - t0
+                j = int(np.searchsorted(arrivals, now, side="right"))
+                if j <= i:
+                    time.sleep(max(0.0, min(arrivals[i] - now, 0.001)))
+                    continue
+            rel = offsets[i:j + 1] - offsets[i]
+            first = self._lib.hg_serve_submit_many(self.h, C.c_void_p(raw.ctypes.data + int(offsets[i])),
+                                                   rel.ctypes.data_as(C.c_void_p), j - i)
+            if first < 0:
+                self._check(-first)
             if base is None:
-                base = rid
+                base = first - i
                 th = threading.Thread(target=drain, daemon=True)
                 th.start()
-            ids[i] = rid
+            ids[i:j] = np.arange(first, first + (j - i))
+            i = j
         if th is not None:
             th.join()
         if errors:

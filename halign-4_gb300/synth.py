@@ -215,6 +215,28 @@ def multiref(n: int = 200, n_refs: int = 4, seed: int = 6, ref_len: int = 5000, 
                     src_ref=src_ref)
 
 
+def center_build(n_full: int = 40, n_part: int = 160, seed: int = 21, center_len: int = 5000) -> Workload:
+    """Queries for a run that builds its own center (no center file):
+    ``n_full`` full-length substitution variants of a uniform center (2%
+    substitutions, so that they keep its length and are the longest
+    records) shuffled among ``n_part`` shorter substrings (1,500..4,899 bp,
+    1% substitutions, 0.1% + 0.1% indels)."""
+    base = np.frombuffer(random_center(center_len, seed), np.uint8)
+    rng = np.random.Generator(np.random.PCG64([seed, 1]))
+    full, fo = mutate_batch(base, np.zeros(n_full, np.int64), np.full(n_full, center_len, np.int64), rng, 0.02, 0.0,
+                            0.0, 3.0)
+    lens = rng.integers(1500, center_len - 100, n_part)
+    starts = rng.integers(0, center_len - lens + 1)
+    part, po = mutate_batch(base, starts, lens, rng, 0.01, 0.001, 0.001, 3.0)
+    recs = [full[fo[i]:fo[i + 1]].tobytes() for i in range(n_full)] + [part[po[i]:po[i + 1]].tobytes()
+                                                                      for i in range(n_part)]
+    order = rng.permutation(len(recs))
+    seqs = [recs[i] for i in order]
+    offs = np.zeros(len(seqs) + 1, np.int64)
+    np.cumsum([len(x) for x in seqs], out=offs[1:])
+    return Workload("center_build", base.tobytes(), b"".join(seqs), offs, _names("c", 0, len(seqs)))
+
+
 def write_refs_fasta(path: str, refs: list[bytes]) -> None:
     """The reference FASTA of a multi-reference run: records ref<i> with a
     description, 80 columns per line."""

@@ -149,6 +149,10 @@ int hg_last_timing(hg_ctx_t* ctx, float* total_ms, float* stage_ms, int64_t* lau
 /* cells: extz2 band cells of the last hg_run_staged, i.e. the sum over DP
  * calls of sum_r (en0 - st0 + 1) with the band bounds of
  * src/align/ksw2_extz2_sse.c:107-110 (the GCUPS numerator). */
+/* The same cells and the part of them in match segments, whose extz2
+ * result (d M) is emitted without running the DP: cells - match_cells is
+ * what the DP kernels computed. */
+int hg_last_cells(hg_ctx_t* ctx, int64_t* cells, int64_t* match_cells);
 /* Work totals of every batched sub-batch since the context was created:
  * counts[0] anchors (after the collect_anchors filters), counts[1] segment
  * records (a run of match segments and anchor spans counts once),
@@ -225,6 +229,24 @@ int hg_fetch_chain(hg_ctx_t* ctx, int64_t query, uint32_t* pos_ref, uint32_t* po
 int hg_align_fasta(const char* center_fasta, const char* queries_fasta, const char* out_fasta, int k, int w,
                    int64_t chunk_queries, int64_t* n_aligned);
 
+/* Center construction without a center file (the CLI run without -c):
+ * preprocessInputFasta's Top-K of the queries (src/utils/preprocess.cpp:
+ * 111-150; TopKLongestSelector, src/consensus/selector.cpp: the cons_n
+ * longest records, ties to the earlier one), each through clean_table, then
+ * generateConsensusSequence over them (src/consensus/consensus.cpp:611-703,
+ * at most cons_n records, batch size 4096) on the device.  The reference
+ * runs its external MSA over the selection first; here the selected records
+ * must already share one length (HG_ERR_ARG otherwise), which is the CLI's
+ * result when its MSA command returns them unchanged.  *len gets the center
+ * length; HG_ERR_CAPACITY when cap is smaller (out may then be NULL). */
+int hg_build_center(const char* queries_fasta, int64_t cons_n, char* out, int64_t cap, int64_t* len);
+
+/* halign4 -i queries.fa --keep-length --cons-n cons_n (no -c), streamed:
+ * hg_build_center, then hg_align_fasta's run against that center, written
+ * as the record ">consensus" first. */
+int hg_align_fasta_consensus(const char* queries_fasta, const char* out_fasta, int k, int w, int64_t cons_n,
+                             int64_t chunk_queries, int64_t* n_aligned);
+
 /* ---- serving loop (continuous batching) ---------------------------------
  * A request loop around one resident index: requests (one ASCII query each,
  * copied at submission) wait in a FIFO; a scheduler thread fills every free
@@ -246,6 +268,18 @@ void hg_serve_destroy(hg_server_t* s);
 /* Queues one request; returns its id (0, 1, 2, ... in submission order) or a
  * negative HG_ERR_* (HG_ERR_CAPACITY: longer than slot_bases). */
 int64_t hg_serve_submit(hg_server_t* s, const char* seq, int64_t len);
+/* Queues a burst of n requests (concatenated in seqs, request i at
+ * [offsets[i], offsets[i+1])) under one lock and one time stamp; returns the
+ * first id (the burst's ids are consecutive) or a negative HG_ERR_*
+ * (nothing queued). */
+int64_t hg_serve_submit_many(hg_server_t* s, const char* seqs, const int64_t* offsets, int64_t n);
+/* Up to max_n finished requests at once, waiting up to timeout_ms for the
+ * first (< 0: no limit): ids[j], status[j], latency_ms[j] (optional) and the
+ * CIGARs concatenated in cigar with cigar_off[0..m]; stops before a CIGAR
+ * that would pass cigar_cap.  Returns m (0 on time-out) or a negative
+ * HG_ERR_* (HG_ERR_CAPACITY when not even the first CIGAR fits). */
+int64_t hg_serve_results(hg_server_t* s, int64_t max_n, int64_t* ids, uint32_t* status, double* latency_ms,
+                         uint32_t* cigar, int64_t cigar_cap, int64_t* cigar_off, int timeout_ms);
 /* The next finished request, waiting up to timeout_ms (< 0: no limit):
  * returns 1 with *id, *status (HG_ST_* bits), *latency_ms (submission to
  * result) and its CIGAR (*n_cigar ops; up to cap written, the rest dropped

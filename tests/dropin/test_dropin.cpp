@@ -31,6 +31,7 @@
 #include "anchor.h"
 #include "consensus.h"
 #include "ksw2.h"
+#include "mash.h"
 #include "seed.h"
 
 namespace {
@@ -356,6 +357,23 @@ void golden_cases(const std::string& path)
             std::string want;
             in >> want;
             check(cigar::cigarToString(c) == want, id + " cigarToString");
+        } else if (tag == "SK") {
+            int k, sz, nc, sd;
+            size_t len;
+            in >> k >> sz >> nc >> sd >> len;
+            const std::string s = read_seq(in);
+            const auto want = read_list<uint64_t>(in);
+            const mash::Sketch sk = mash::sketchFromSequence(s, (size_t)k, (size_t)sz, nc != 0, sd);
+            check(sk.hashes == want && sk.k == (size_t)k, id + " mash::sketchFromSequence");
+        } else if (tag == "JC") {
+            mash::Sketch a, b;
+            in >> a.k;
+            b.k = a.k;
+            a.hashes = read_list<uint64_t>(in);
+            b.hashes = read_list<uint64_t>(in);
+            double want;
+            in >> want;
+            check(mash::jaccard(a, b) == want, id + " mash::jaccard");
         }
     }
     check(n > 100, "golden fixture holds the expected cases");

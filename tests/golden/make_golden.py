@@ -218,6 +218,20 @@ def dropin_cases(R: Reference):
     for it in range(6):
         c = R.global_align_ksw2(_seq(rng, 200), _seq(rng, 180))
         L.append(f"CS {arr(c)} {R.cigar_str(c)}")
+    # mash::sketchFromSequence and jaccard (own generator: the cases above stay as they were)
+    rs = np.random.default_rng(78)
+    sks = []
+    for it in range(10):
+        s = _seq(rs, int(rs.choice([0, 20, 800, 3000])), noisy=it % 2 == 0)
+        k, sz, nc, sd = int(rs.choice([15, 21, 32])), int(rs.choice([2000, 50, 1])), int(it % 3 != 2), int(
+            rs.choice([42, 0]))
+        h = R.sketch(s, k, sz, bool(nc), sd)
+        L.append(f"SK {k} {sz} {nc} {sd} {len(s)} {s.decode() if s else '-'} {arr(h)}")
+        if k == 15 and nc and sz == 2000 and sd == 42:
+            sks.append(h)
+    base = R.sketch(_seq(rs, 2500, False))
+    for o in sks + [base[:300], np.zeros(0, np.uint64)]:
+        L.append(f"JC 15 {arr(base)} {arr(o)} {R.jaccard(base, o)!r}")
     (OUT / "dropin_cases.txt").write_text("\n".join(L) + "\n")
     # generateConsensusSequence: batches of 3 (the reference skips one record
     # between full batches) and a record limit
@@ -289,6 +303,34 @@ def multiref_cli_digest(w):
         shutil.rmtree(d, ignore_errors=True)
 
 
+def center_cli_digest(w, cons_n=40):
+    """The reference CLI without a center file (it builds the center from
+    the --cons-n longest queries) with --keep-length and an MSA command that
+    copies its input."""
+    d = Path(tempfile.mkdtemp(prefix="halign_golden_cc_"))
+    try:
+        synth.write_fasta(str(d), "unused", b"A", w)
+        cmd = [str(ROOT / "oracle/_ref/halign4"), "-i", str(d / "queries.fa"), "-o", str(d / "out.fa"),
+               "--keep-length", "-p", "cp {input} {output}", "-t", "1", "--kmer-size", "15", "--kmer-window", "10",
+               "--cons-n", str(cons_n), "-w", str(d / "wd")]
+        subprocess.run(cmd, check=True, capture_output=True)
+        data = (d / "out.fa").read_bytes()
+        return hashlib.sha256(data).hexdigest(), len(data), data.count(b"\n") // 2
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def center_fixtures():
+    w = synth.center_build()
+    digest, nbytes, nrec = center_cli_digest(w)
+    meta = json.loads((OUT / "meta.json").read_text())
+    meta.update({"center_build_cli_fasta_sha256": digest, "center_build_cli_fasta_bytes": nbytes,
+                 "center_build_cli_records": nrec,
+                 "center_build_cli": "halign4 -i queries.fa -o out.fa --keep-length -p 'cp {input} {output}' -t 1 "
+                                     "--kmer-size 15 --kmer-window 10 --cons-n 40 (no -c)"})
+    (OUT / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+
+
 def mash_fixtures(R: Reference):
     mash_vectors(R)
     w = synth.multiref(200)
@@ -324,6 +366,9 @@ def main():
     if sys.argv[1:] == ["--mash"]:  # only the multi-reference fixtures
         mash_fixtures(R)
         return
+    if sys.argv[1:] == ["--center"]:  # only the center-construction fixture
+        center_fixtures()
+        return
     ksw_vectors(R)
     ksw_nongeneric_vectors(R)
     dropin_cases(R)
@@ -351,6 +396,7 @@ def main():
     }
     (OUT / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
     mash_fixtures(R)
+    center_fixtures()
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, os.path.getsize(p))
 

@@ -27,6 +27,8 @@ EXPORTS = [
     "cigar::appendCigar(", "cigar::getRefLength(", "cigar::getQueryLength(",
     "consensus::pickConsensusChar(", "consensus::writeConsensusFasta(", "consensus::writeCountsJson(",
     "consensus::generateConsensusSequence(", "ksw_extz2_sse",
+    "mash::sketchFromSequence(", "mash::jaccard(", "mash::mashDistanceFromJaccard(", "mash::aniFromJaccard(",
+    "mash::aniFromMashDistance(", "mash::intersectionSizeSortedUnique(",
 ]
 
 
@@ -65,3 +67,29 @@ def test_dropin_reference_answers_on_gpu(gpu, tmp_path):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "failed 0" in r.stdout
+
+
+# the reference sources whose definitions the drop-in library replaces
+REPLACED = ["minimizer", "anchor", "align", "cigar", "ksw2_extz2_sse", "consensus", "mash"]
+# the rest of the reference CLI, linked unchanged
+KEPT = ["halign4", "ref_aligner", "preprocess", "cmd", "selector", "seq_io", "file_io", "hash", "xxhash"]
+
+
+def test_reference_cli_links_against_the_dropin(native, tmp_path):
+    """The reference's own CLI objects (compiled from the unmodified sources
+    by oracle/build.py, where the reference tree exists) link with
+    libhalign4_dropin.so standing in for the seven replaced sources: every
+    symbol the reference's callers need is defined by the drop-in."""
+    obj = ROOT / "oracle" / "_ref" / "obj"
+    if not all((obj / f"{n}.o").exists() for n in KEPT):
+        pytest.skip("reference objects not built on this host")
+    exe = tmp_path / "halign4_dropin"
+    r = subprocess.run([os.environ.get("CXX", "g++"), "-fopenmp", "-o", str(exe), *[str(obj / f"{n}.o") for n in KEPT],
+                        f"-L{BUILD}", "-lhalign4_dropin", "-lhalign_gb300", f"-Wl,-rpath,{BUILD}", "-lz"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    # and none of the replaced sources' objects was needed
+    nm = subprocess.run(["nm", "-C", "--defined-only", str(exe)], capture_output=True, text=True).stdout
+    for sym in ("minimizer::extractMinimizer(", "anchor::chainAnchors(", "align::globalAlignMM2(",
+                "mash::sketchFromSequence(", "consensus::generateConsensusSequence("):
+        assert sym not in nm, sym

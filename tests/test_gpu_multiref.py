@@ -134,3 +134,22 @@ def test_align_fasta_rejects_references_of_different_lengths(gpu, pkg, tmp_path)
     pkg.synth.write_fasta(str(tmp_path), "unused", b"A", w)
     with pytest.raises(gpu.HalignError):
         gpu.align_fasta(tmp_path / "refs.fa", tmp_path / "queries.fa", tmp_path / "o.fa")
+
+
+def test_build_center_and_align_equal_reference_cli(gpu, pkg, golden, oracle, tmp_path):
+    """The CLI run without a center file: Top-K of the 40 longest queries,
+    their consensus on the device, every query aligned to it; the FASTA
+    equals the reference CLI's."""
+    from tests.test_center_oracle import built_center
+    w = pkg.synth.center_build()
+    pkg.synth.write_fasta(str(tmp_path), "unused", b"A", w)
+    assert gpu.build_center(tmp_path / "queries.fa", 40) == built_center(oracle, w, 40)
+    for chunk in (200, 33):
+        out = tmp_path / f"c{chunk}.fa"
+        assert gpu.align_fasta_consensus(tmp_path / "queries.fa", out, cons_n=40, chunk_queries=chunk) == w.n
+        data = out.read_bytes()
+        assert len(data) == golden.meta["center_build_cli_fasta_bytes"], chunk
+        assert hashlib.sha256(data).hexdigest() == golden.meta["center_build_cli_fasta_sha256"], chunk
+    # a selection of records of different lengths needs the external MSA
+    with pytest.raises(gpu.HalignError):
+        gpu.build_center(tmp_path / "queries.fa", 41)
