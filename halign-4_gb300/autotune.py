@@ -6,7 +6,8 @@ queues), so the grid size per SM trades occupancy against tail and queue
 contention, and the best point depends on the workload (query length, number
 of segments per query).  The two tier knobs move gap-fill segments between
 the thin, square and wavefront DP tiers (all bit-identical), trading one
-tier's latency tail against another's occupancy.  The band width is not a
+tier's latency tail against another's occupancy, and an on/off knob picks
+the small tier's int32 or packed int16x2 form.  The band width is not a
 knob: bit-exactness fixes it to the reference's auto_band.  `tune` runs a coordinate descent over the
 CTAs-per-SM knobs of a context (`Context.set_launch`), scoring each candidate
 with `measure` (by default the CUDA-event time of a staged run of the batch
@@ -24,7 +25,10 @@ from . import LAUNCH_BOUNDS, LAUNCH_KNOBS
 
 
 def candidates(value: int, lo: int, hi: int) -> list[int]:
-    """Neighbours of a knob value: halved, 3/4, 3/2 and doubled, within bounds."""
+    """Neighbours of a knob value: halved, 3/4, 3/2 and doubled, within bounds
+    (both values of an on/off knob)."""
+    if (lo, hi) == (0, 1):
+        return [0, 1]
     out = {value}
     for v in (value // 2, (value * 3) // 4, (value * 3 + 1) // 2, value * 2):
         if lo <= v <= hi:

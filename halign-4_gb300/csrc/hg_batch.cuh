@@ -313,6 +313,7 @@ struct BatchDev {
                                  // [3] small-tier records (the small list without its holes)
     unsigned long long* cells;   // extz2 band cells computed: sum over DP calls of sum_r (en0 - st0 + 1)
     unsigned long long* match_cells;  // the part of `cells` in match segments (emitted without a DP)
+    int small_pair;              // small tier: two records per thread in int16x2 halves (else int32, one)
     uint32_t* run_flags;         // OR of every query status since the last reset
 };
 

@@ -441,15 +441,46 @@ __device__ __forceinline__ void small_dispatch(const IndexDev& ix, const BatchDe
     }
 }
 
+// Small tier, one record per thread (int32 lanes).
+__global__ void __launch_bounds__(kDpSmallThreads) dp_small_kernel(IndexDev ix, BatchDev b)
+{
+    __shared__ uint32_t dirs[kSmallDirWords * kDpSmallThreads];
+    const int tid = threadIdx.x;
+    const unsigned total = min(b.queues2[1], b.queues2[3]);  // small shapes only
+    unsigned long long cell_sum = 0;
+    const unsigned wspan = (total + 31u) & ~31u;  // whole warps iterate together for the shuffle
+    for (unsigned w = blockIdx.x * kDpSmallThreads + tid; w < wspan; w += gridDim.x * kDpSmallThreads) {
+        if (w >= total) continue;
+        const SmallRec r = b.work_rec[w];
+        const uint32_t rl = r.shape & 0xffu, ql = (r.shape >> 8) & 0xffu;
+        const bool tinner = rl <= ql;
+        const bool left = (r.shape & kRecLeft) != 0;
+        const uint32_t inner = tinner ? rl : ql;
+        if (r.shape & kRecFast) {
+            if (inner <= 4) small_dispatch<true, 4, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+            else if (inner <= 8) small_dispatch<true, 8, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+            else small_dispatch<true, 16, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+        } else {
+            small_dispatch<false, 16, kDpSmallThreads>(ix, b, r, dirs, tid, tinner, left);
+        }
+        cell_sum += (unsigned long long)(rl * ql);
+    }
+    for (int o = 16; o > 0; o >>= 1) cell_sum += __shfl_xor_sync(0xffffffffu, cell_sum, o);
+    if ((tid & 31) == 0 && cell_sum && b.cells) atomicAdd(b.cells, cell_sum);
+}
+
 // Small tier, two records per thread: consecutive records of the
 // shape-sorted list share their shape (rl, ql, gap mode, FAST) except at the
 // boundary between shapes, so a thread takes records 2w and 2w+1 and runs
 // them in the two halves of int16x2 registers (small_pair); a pair whose
 // shapes differ, or that has a record off the FAST path, runs as two single
-// records (small_segment).
+// records (small_segment).  Half the instructions per cell of the int32
+// form, but half the warps per SM for the same direction store: on the
+// mito workload it measured 5% slower (latency-bound at that occupancy), so
+// it is a launch knob (HG_LAUNCH_KNOBS entry 8) the autotuner can choose.
 constexpr int kDpSmallPairThreads = 64;
 
-__global__ void __launch_bounds__(kDpSmallPairThreads) dp_small_kernel(IndexDev ix, BatchDev b)
+__global__ void __launch_bounds__(kDpSmallPairThreads) dp_small_pair_kernel(IndexDev ix, BatchDev b)
 {
     constexpr int T = kDpSmallPairThreads;
     __shared__ uint32_t dirs[2 * kSmallDirWords * T];
@@ -1866,8 +1897,10 @@ extern "C" cudaError_t hg_launch_dp_small(const hg::IndexDev* ix, const hg::Batc
     hg::shape_hist_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kShapeHistThreads, 0, st>>>(*b);
     hg::shape_scan_kernel<<<1, 1024, 0, st>>>(*b);
     hg::shape_scatter_kernel<<<grid / 4 > 0 ? grid / 4 : 1, hg::kScatterThreads, hg::kScatterSmem, st>>>(*ix, *b);
-    // half the threads per CTA of the single-record form, twice the CTAs
-    hg::dp_small_kernel<<<2 * grid, hg::kDpSmallPairThreads, 0, st>>>(*ix, *b);
+    if (b->small_pair)  // half the threads per CTA of the single-record form, twice the CTAs
+        hg::dp_small_pair_kernel<<<2 * grid, hg::kDpSmallPairThreads, 0, st>>>(*ix, *b);
+    else
+        hg::dp_small_kernel<<<grid, hg::kDpSmallThreads, 0, st>>>(*ix, *b);
     hg::dp_medium_kernel<<<grid, hg::kDpMedThreads, 0, st>>>(*ix, *b);
     return cudaGetLastError();
 }

@@ -34,7 +34,8 @@ size_t hg_sketch_smem(int sketch_size, int* cap);
 cudaError_t hg_launch_sketch(const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
                              const int64_t* exc_off, int n, int k, int s, int noncanonical, int seed, uint64_t* out,
                              int64_t out_stride, int32_t* out_n, const uint64_t* ref_h, const int64_t* ref_off,
-                             int n_refs, int32_t* best, double* best_j, unsigned* queue, int sms, cudaStream_t st);
+                             int n_refs, const ulonglong2* ref_tab, uint32_t ref_tab_mask, int32_t* best,
+                             double* best_j, unsigned* queue, int sms, cudaStream_t st);
 }
 
 namespace {
@@ -116,8 +117,8 @@ int sketch_batch(DevBatch& B, DevBuf<uint64_t>& dout, DevBuf<int32_t>& dn, DevBu
         (e = DevBatch::fit(queue, 1)))
         return hg::cuda_error(e, "hg_sketch_batch: buffers");
     HG_CUDA(hg_launch_sketch(B.packed.p, B.poff.p, B.qlen.p, B.exc.p, B.eoff.p, (int)n, k, s, noncanonical, seed,
-                             dout.p, (int64_t)per, dn.p, nullptr, nullptr, 0, nullptr, nullptr, queue.p, sm_count(),
-                             st));
+                             dout.p, (int64_t)per, dn.p, nullptr, nullptr, 0, nullptr, 0u, nullptr, nullptr, queue.p,
+                             sm_count(), st));
     if (n) {
         HG_CUDA(cudaMemcpyAsync(counts, dn.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, st));
         if (s > 0)
@@ -164,12 +165,32 @@ struct hg_refset {
     cudaStream_t st = nullptr;
     DevBuf<uint64_t> ref_h, sk_out;
     DevBuf<int64_t> ref_off;
+    DevBuf<ulonglong2> ref_tab;  // up to 64 references: hash -> mask of the references holding it
+    uint32_t ref_tab_mask = 0;
     DevBuf<int32_t> best, sk_n;
     DevBuf<double> best_j;
     DevBuf<unsigned> queue;
     DevBatch batch;
     cudaEvent_t ev[2] = {nullptr, nullptr};  // around the last selection launch
     float last_ms = 0.0f;
+    // grow-only pinned staging of one reference's group: packed inputs and rows
+    struct Pinned {
+        uint8_t* p = nullptr;
+        size_t n = 0;
+        cudaError_t fit(size_t want)
+        {
+            if (want <= n) return cudaSuccess;
+            if (p) cudaFreeHost(p);
+            p = nullptr, n = 0;
+            const cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&p), want, cudaHostAllocDefault);
+            if (e == cudaSuccess) n = want;
+            return e;
+        }
+        ~Pinned()
+        {
+            if (p) cudaFreeHost(p);
+        }
+    } h_packed, h_rows;
     ~hg_refset()
     {
         cudaSetDevice(device);
@@ -346,6 +367,23 @@ extern "C" int hg_refset_create(const char* const* refs, const int64_t* lens, in
                 (e = cudaMemcpy(R->ref_off.p, roff.data(), 8 * roff.size(), cudaMemcpyHostToDevice)))
                 rc = hg::cuda_error(e, "hg_refset_create: reference sketches");
         }
+        // with up to 64 references, an open-addressing table hash -> mask of
+        // the references whose sketch holds it (load <= 1/2, linear probing)
+        if (!rc && n_refs <= 64) {
+            uint32_t size = 16;
+            while (size < 2 * flat.size() + 16) size <<= 1;
+            std::vector<ulonglong2> tab(size, ulonglong2{0, 0});
+            for (int r = 0; r < n_refs; ++r)
+                for (uint64_t h : R->sk[r]) {
+                    uint32_t sl = (uint32_t)h & (size - 1);
+                    while (tab[sl].y != 0 && tab[sl].x != h) sl = (sl + 1) & (size - 1);
+                    tab[sl].x = h, tab[sl].y |= 1ull << r;
+                }
+            R->ref_tab_mask = size - 1;
+            if ((e = R->ref_tab.alloc(size)) ||
+                (e = cudaMemcpy(R->ref_tab.p, tab.data(), sizeof(ulonglong2) * size, cudaMemcpyHostToDevice)))
+                rc = hg::cuda_error(e, "hg_refset_create: reference table");
+        }
     }
     if (!rc) rc = refs_consensus(R->refs, R->consensus);
     if (rc) {
@@ -415,7 +453,8 @@ extern "C" int hg_refset_select(hg_refset_t* R, const uint8_t* packed, const int
     HG_CUDA(cudaEventRecord(R->ev[0], R->st));
     HG_CUDA(hg_launch_sketch(R->batch.packed.p, R->batch.poff.p, R->batch.qlen.p, R->batch.exc.p, R->batch.eoff.p,
                              (int)n, R->k, R->s, 1, R->seed, nullptr, 0, nullptr, R->ref_h.p, R->ref_off.p,
-                             (int)R->refs.size(), R->best.p, R->best_j.p, R->queue.p, sm_count(), R->st));
+                             (int)R->refs.size(), R->ref_tab.p, R->ref_tab_mask, R->best.p, R->best_j.p, R->queue.p,
+                             sm_count(), R->st));
     HG_CUDA(cudaEventRecord(R->ev[1], R->st));
     if (n) {
         HG_CUDA(cudaMemcpyAsync(best, R->best.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, R->st));
@@ -473,7 +512,6 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
     if (!status) st_l.resize((size_t)n), status = st_l.data();
     int first_err = HG_OK;
     std::string first_msg;
-    std::vector<uint8_t> gp, grows;
     std::vector<int64_t> gpoff, geoff;
     std::vector<int32_t> gq, gexc;
     std::vector<uint8_t> gins;
@@ -487,42 +525,49 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
         // gather the group's inputs
         int64_t pb = 0, ne = 0, bases = 0;
         for (int64_t i : m) pb += (int64_t)padded_bytes(qlen[i]), ne += exc_off[i + 1] - exc_off[i], bases += qlen[i];
-        gp.resize((size_t)std::max<int64_t>(pb, 16));
+        cudaError_t pe = R->h_packed.fit((size_t)std::max<int64_t>(pb, 16));
+        if (!pe && rows) pe = R->h_rows.fit((size_t)(ng * row_stride));
+        if (pe) return hg::cuda_error(pe, "hg_refset_align: pinned staging");
+        uint8_t* gp = R->h_packed.p;
+        uint8_t* grows = rows ? R->h_rows.p : nullptr;
         gpoff.resize((size_t)ng), geoff.resize((size_t)ng + 1), gq.resize((size_t)ng);
         gexc.resize((size_t)std::max<int64_t>(ne, 1) * 3);
         int64_t o = 0, eo = 0;
         geoff[0] = 0;
-        for (int64_t j = 0; j < ng; ++j) {
+        for (int64_t j = 0; j < ng; ++j) {  // offsets first, then the copies in parallel
             const int64_t i = m[(size_t)j];
             gpoff[j] = o, gq[j] = qlen[i];
-            std::memcpy(gp.data() + o, packed + poff[i], padded_bytes(qlen[i]));
             o += (int64_t)padded_bytes(qlen[i]);
-            const int64_t ei = exc_off[i + 1] - exc_off[i];
-            if (ei) std::memcpy(gexc.data() + 3 * eo, exc + 3 * exc_off[i], 12 * (size_t)ei);
-            eo += ei;
+            eo += exc_off[i + 1] - exc_off[i];
             geoff[j + 1] = eo;
+        }
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t j = 0; j < ng; ++j) {
+            const int64_t i = m[(size_t)j];
+            std::memcpy(gp + gpoff[j], packed + poff[i], padded_bytes(qlen[i]));
+            const int64_t ei = exc_off[i + 1] - exc_off[i];
+            if (ei) std::memcpy(gexc.data() + 3 * geoff[j], exc + 3 * exc_off[i], 12 * (size_t)ei);
         }
         const int64_t L = (int64_t)R->refs[r].size();
         int64_t cap = bases / 8 + 64 * ng + 1024;
         cig_g[r].resize((size_t)cap), off_g[r].resize((size_t)ng + 1);
         gins.resize((size_t)ng), gst.resize((size_t)ng);
-        if (rows) grows.resize((size_t)(ng * row_stride));
-        rc = hg_align_batch(c, gp.data(), gpoff.data(), gq.data(), gexc.data(), geoff.data(), ng, cig_g[r].data(), cap,
-                            off_g[r].data(), gins.data(), rows ? grows.data() : nullptr, row_stride, gst.data());
+        rc = hg_align_batch(c, gp, gpoff.data(), gq.data(), gexc.data(), geoff.data(), ng, cig_g[r].data(), cap,
+                            off_g[r].data(), gins.data(), grows, row_stride, gst.data());
         if (rc == HG_ERR_CAPACITY) {  // CIGARs longer than the first guess: the worst case fits
             cap = bases + ng * (L + 4);
             cig_g[r].resize((size_t)cap);
-            rc = hg_align_batch(c, gp.data(), gpoff.data(), gq.data(), gexc.data(), geoff.data(), ng, cig_g[r].data(),
-                                cap, off_g[r].data(), gins.data(), rows ? grows.data() : nullptr, row_stride,
-                                gst.data());
+            rc = hg_align_batch(c, gp, gpoff.data(), gq.data(), gexc.data(), geoff.data(), ng, cig_g[r].data(),
+                                cap, off_g[r].data(), gins.data(), grows, row_stride, gst.data());
         }
         if (rc && rc != HG_ERR_LENGTH_MISMATCH && rc != HG_ERR_CIGAR) return rc;
         if (rc && !first_err) first_err = rc, first_msg = hg_last_error();
+#pragma omp parallel for schedule(dynamic, 64)
         for (int64_t j = 0; j < ng; ++j) {
             const int64_t i = m[(size_t)j];
             n_cig[i] = off_g[r][j + 1] - off_g[r][j];
             has_ins[i] = gins[j], status[i] = gst[j];
-            if (rows) std::memcpy(rows + i * row_stride, grows.data() + j * row_stride, (size_t)row_stride);
+            if (rows) std::memcpy(rows + i * row_stride, grows + j * row_stride, (size_t)row_stride);
         }
     }
     // CIGARs in input order
@@ -531,8 +576,9 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
     if (n && cigar_off[n] > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_refset_align: cigar buffer too small");
     for (int r = 0; r < n_refs; ++r) {
         const auto& m = members[(size_t)r];
-        for (size_t j = 0; j < m.size(); ++j) {
-            const int64_t i = m[j];
+#pragma omp parallel for schedule(dynamic, 256)
+        for (int64_t j = 0; j < (int64_t)m.size(); ++j) {
+            const int64_t i = m[(size_t)j];
             if (n_cig[i]) std::memcpy(cigar + cigar_off[i], cig_g[r].data() + off_g[r][j], 4 * (size_t)n_cig[i]);
         }
     }

@@ -119,7 +119,7 @@ struct hg_ctx {
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
     cudaStream_t st3 = nullptr;                            // side stream of the one-warp wavefront and exact tiers
     // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
-    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells};
+    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells, 0};
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, join3_ev = nullptr;
     int sms = 1;
     int64_t max_n = 0, max_bases = 0, exc_cap = 0;
@@ -762,8 +762,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
 // per-CTA scratch slice in range.  Cached graphs are dropped.
 extern "C" int hg_ctx_set_launch(hg_ctx_t* c, const int32_t* ctas_per_sm, int n)
 {
-    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1, 0, 0};
-    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32, hg::kThinMaxInner, hg::kSquareMaxCells};
+    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1, 0, 0, 0};
+    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32, hg::kThinMaxInner, hg::kSquareMaxCells, 1};
     if (!c || !ctas_per_sm || n < 0 || n > HG_LAUNCH_KNOBS) return fail(HG_ERR_ARG, "hg_ctx_set_launch: bad arguments");
     for (int i = 0; i < n; ++i)
         if (ctas_per_sm[i] < lo[i] || ctas_per_sm[i] > hi[i])
@@ -869,6 +869,7 @@ hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t
     b.seg = c->seg.p, b.scap = c->scap, b.s_base = c->s_base.p, b.s_n = c->s_n.p, b.n_chain = c->n_chain.p;
     b.chain_meta = c->chain_meta.p;
     b.thin_max_inner = c->launch[6], b.square_max_cells = c->launch[7];
+    b.small_pair = c->launch[8];
     b.work_small = c->work_small.p, b.work_large = c->work_large.p, b.wcap = c->scap;
     b.work_sorted = c->work_sorted.p, b.work_key = c->work_key.p, b.shape_hist = c->shape_hist.p;
     b.work_wave = c->work_wave.p, b.work_wave_key = c->work_wave_key.p, b.work_wave_sorted = c->work_wave_sorted.p;

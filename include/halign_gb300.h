@@ -133,11 +133,13 @@ int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* 
  * query side the thin tier takes (0..32; 0 switches the tier off), [7] the
  * most cells the square tier takes (0..12288).  Segments a tier declines go
  * to the next one (thin, square, then the wavefront or exact tiers); every
- * tier computes the same alignment, so the knobs change speed only.
- * Defaults 6 6 12 12 8 6 32 12288.  Setting them drops the context's cached
- * CUDA graphs (the autotuner, halign-4_gb300/autotune.py, searches them).
- * No reference counterpart: launch geometry. */
-#define HG_LAUNCH_KNOBS 8
+ * tier computes the same alignment, so the knobs change speed only.  [8]
+ * small-tier form (0: one segment per thread in int32 lanes; 1: two
+ * same-shape segments per thread in the 16-bit halves of 32-bit words).
+ * Defaults 6 6 12 12 8 6 32 12288 0.  Setting them drops the context's
+ * cached CUDA graphs (the autotuner, halign-4_gb300/autotune.py, searches
+ * them).  No reference counterpart: launch geometry. */
+#define HG_LAUNCH_KNOBS 9
 int hg_ctx_set_launch(hg_ctx_t* ctx, const int32_t* ctas_per_sm, int n);
 int hg_ctx_get_launch(const hg_ctx_t* ctx, int32_t* ctas_per_sm, int n);
 

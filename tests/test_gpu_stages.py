@@ -274,19 +274,21 @@ def test_packed_dp_cell_equals_int32_cell(gpu):
     assert bad.value == 0
 
 
-@pytest.mark.parametrize("name,n", [("divergent", 60), ("uneven", 120), ("serve", 40)])
+@pytest.mark.parametrize("name,n", [("divergent", 60), ("uneven", 120), ("serve", 40), ("mito", 60)])
 def test_tier_boundary_knobs_do_not_change_results(gpu, pkg, name, n):
     """The thin and square tiers switched off, or narrowed, move their
-    segments to other tiers: the CIGARs stay identical."""
+    segments to other tiers, and the small tier runs in either form: the
+    CIGARs stay identical."""
     w = getattr(pkg.synth, name)(n)
     ix = gpu.Index(w.center)
     ctx = gpu.Context(ix, max_queries=n, max_bases=int(w.total_bases) + 1024)
     b = gpu.pack(w.seqs, w.offsets)
     base = ctx.align(b, rows=True)
     default = ctx.get_launch()
-    for thin, sq in ((0, 0), (8, 2000), (32, 0), (0, 12288)):
-        ctx.set_launch(default[:6] + [thin, sq])
+    for thin, sq, pair in ((0, 0, 0), (8, 2000, 1), (32, 0, 0), (0, 12288, 1), (32, 12288, 1)):
+        ctx.set_launch(default[:6] + [thin, sq, pair])
         got = ctx.align(b, rows=True)
-        assert np.array_equal(got.cigar, base.cigar) and np.array_equal(got.cigar_off, base.cigar_off), (thin, sq)
+        assert np.array_equal(got.cigar, base.cigar) and np.array_equal(got.cigar_off, base.cigar_off), (thin, sq,
+                                                                                                      pair)
         assert np.array_equal(got.rows, base.rows)
     ctx.set_launch(default)
