@@ -256,7 +256,7 @@ def measure_plain(pkg, ctx, w, n_plain: int):
             "note": "host-timed hg_align_plain vs hg_align_batch (both with H2D/D2H) on the same queries"}
 
 
-def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 20000):
+def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 60000):
     """The serving loop (hg_serve_*, scheduler in the library) on the serve
     workload (Poisson arrivals, 500..29,903 bp substrings of a 29,903 bp
     center, 0.5% divergence): p50/p99 at `rate` req/s; saturation (n_sat
@@ -265,13 +265,14 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 20000):
     rate (Poisson arrivals) for latency at load."""
     w = pkg.synth.serve(n_req, rate=rate)
     ix = pkg.Index(w.center)
-    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=1024, slot_bases=16_000_000, budget_bytes=40 << 30)
+    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=4096, slot_bases=64_000_000, budget_bytes=100 << 30)
     srv.run(w.seqs, w.offsets[: min(w.n, 400) + 1], None)  # warm-up
     st = srv.run(w.seqs, w.offsets, w.arrivals)
     ws = pkg.synth.serve(n_sat, rate=rate, chunk=1)
     sat = srv.run(ws.seqs, ws.offsets, None)
     # the same requests as one batch, device-resident and through the host-buffer call
-    ctx = pkg.Context(ix, max_queries=ws.n, max_bases=int(ws.total_bases) + 1024)
+    sub = 20000  # the batched denominator in 20,000-request sub-batches (two compute lanes)
+    ctx = pkg.Context(ix, max_queries=sub, max_bases=sub * 29903)
     b = pkg.pack(ws.seqs, ws.offsets)
     ctx.stage(b)
     for _ in range(2):
@@ -292,7 +293,7 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 20000):
     keep = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "requests", "micro_batches", "mbp_per_s", "status_or")
     out = {k: st[k] for k in keep}
     out.update({"rate_req_per_s": rate, "center_bp": len(w.center), "loop": "native (hg_serve_*)",
-                "contexts": int(st["contexts"]), "device_bytes": int(st["device_bytes"]), "budget_bytes": 40 << 30,
+                "contexts": int(st["contexts"]), "device_bytes": int(st["device_bytes"]), "budget_bytes": 100 << 30,
                 "saturation": {k: sat[k] for k in keep},
                 "batched_same_requests_mbp_per_s": batched, "batched_same_requests_e2e_mbp_per_s": batched_e2e,
                 "saturation_frac_of_batched": sat["mbp_per_s"] / batched,
@@ -320,7 +321,7 @@ def run_serve_million(args, pkg):
     n_chunks = -(-args.serve_requests // chunk)
     w0 = pkg.synth.serve(min(chunk, args.serve_requests), chunk=0)
     ix = pkg.Index(w0.center)
-    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=1024, slot_bases=16_000_000, budget_bytes=40 << 30)
+    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=4096, slot_bases=64_000_000, budget_bytes=100 << 30)
     ctx = pkg.Context(ix, max_queries=chunk, max_bases=chunk * 29903)
     pending, served, bases, t_serve, p99s, st_or = [], 0, 0, 0.0, [], 0
     for c in range(n_chunks):

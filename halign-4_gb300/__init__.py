@@ -38,8 +38,8 @@ HG_ERR_CAPACITY = 4
 ST_ARENA_OVERFLOW, ST_PARTIAL_CIGAR, ST_CIGAR_OVERFLOW, ST_LENGTH_MISMATCH = 0x01, 0x02, 0x08, 0x10
 # hg_ctx_set_launch order: CTAs per SM of six stages, then two DP tier boundaries
 LAUNCH_KNOBS = ("seed", "anchor", "chain", "dp_small", "stitch", "rows", "thin_max_inner", "square_max_cells",
-                "small_pair")
-LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32), (0, 32), (0, 12288), (0, 1))
+                "small_pair", "lanes")
+LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32), (0, 32), (0, 12288), (0, 1), (1, 2))
 STAGES = ("seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count")
 
 

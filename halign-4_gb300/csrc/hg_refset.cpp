@@ -488,23 +488,38 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
     if (!jaccard) jac_l.resize((size_t)n), jaccard = jac_l.data();
     int rc = hg_refset_select(R, packed, poff, qlen, exc, exc_off, n, best, jaccard);
     if (rc) return rc;
-    // one reference, or the consensus re-check: one batch over the caller's arrays
+    // the batches: with --keep-length and several references, the queries of
+    // each reference; otherwise every query against the one reference or the
+    // consensus (the re-check).  Each runs through pinned staging and comes
+    // back in input order.
+    struct Group {
+        hg_ctx_t* ctx = nullptr;
+        int64_t L = 0;
+        std::vector<int64_t> m;
+    };
+    std::vector<Group> groups;
     if (n_refs == 1 || !keep_length) {
-        hg_ctx_t* c = nullptr;
-        rc = n_refs == 1 ? ctx_of(R, 0, &c) : cons_ctx_of(R, &c);
+        Group g;
+        rc = n_refs == 1 ? ctx_of(R, 0, &g.ctx) : cons_ctx_of(R, &g.ctx);
         if (rc) return rc;
-        if (rows && row_stride < hg::index_length(n_refs == 1 ? R->ix[0] : R->cons_ix))
-            return fail(HG_ERR_ARG, "hg_refset_align: row_stride below the aligned-to length");
-        return hg_align_batch(c, packed, poff, qlen, exc, exc_off, n, cigar, cigar_cap, cigar_off, has_ins, rows,
-                              row_stride, status);
+        g.L = hg::index_length(n_refs == 1 ? R->ix[0] : R->cons_ix);
+        g.m.resize((size_t)n);
+        for (int64_t i = 0; i < n; ++i) g.m[(size_t)i] = i;
+        groups.push_back(std::move(g));
+    } else {
+        groups.resize((size_t)n_refs);
+        for (int64_t i = 0; i < n; ++i) groups[(size_t)best[i]].m.push_back(i);
+        for (int r = 0; r < n_refs; ++r) {
+            groups[(size_t)r].L = (int64_t)R->refs[(size_t)r].size();
+            if (!groups[(size_t)r].m.empty() && (rc = ctx_of(R, r, &groups[(size_t)r].ctx))) return rc;
+        }
     }
-    if (rows && row_stride < max_len) return fail(HG_ERR_ARG, "hg_refset_align: row_stride below the longest reference");
-    // --keep-length with several references: the queries of each reference
-    // as one batch, results put back in input order
-    std::vector<std::vector<int64_t>> members((size_t)n_refs);
-    for (int64_t i = 0; i < n; ++i) members[(size_t)best[i]].push_back(i);
-    std::vector<std::vector<uint32_t>> cig_g((size_t)n_refs);
-    std::vector<std::vector<int64_t>> off_g((size_t)n_refs);
+    for (const auto& g : groups)
+        if (rows && !g.m.empty() && row_stride < g.L)
+            return fail(HG_ERR_ARG, "hg_refset_align: row_stride below the aligned-to length");
+    const int n_groups = (int)groups.size();
+    std::vector<std::vector<uint32_t>> cig_g((size_t)n_groups);
+    std::vector<std::vector<int64_t>> off_g((size_t)n_groups);
     std::vector<int64_t> n_cig((size_t)n, 0);
     std::vector<uint8_t> ins_l;
     std::vector<uint32_t> st_l;
@@ -516,12 +531,11 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
     std::vector<int32_t> gq, gexc;
     std::vector<uint8_t> gins;
     std::vector<uint32_t> gst;
-    for (int r = 0; r < n_refs; ++r) {
-        const auto& m = members[(size_t)r];
+    for (int r = 0; r < n_groups; ++r) {
+        const auto& m = groups[(size_t)r].m;
         const int64_t ng = (int64_t)m.size();
         if (!ng) continue;
-        hg_ctx_t* c = nullptr;
-        if ((rc = ctx_of(R, r, &c))) return rc;
+        hg_ctx_t* c = groups[(size_t)r].ctx;
         // gather the group's inputs
         int64_t pb = 0, ne = 0, bases = 0;
         for (int64_t i : m) pb += (int64_t)padded_bytes(qlen[i]), ne += exc_off[i + 1] - exc_off[i], bases += qlen[i];
@@ -548,7 +562,7 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
             const int64_t ei = exc_off[i + 1] - exc_off[i];
             if (ei) std::memcpy(gexc.data() + 3 * geoff[j], exc + 3 * exc_off[i], 12 * (size_t)ei);
         }
-        const int64_t L = (int64_t)R->refs[r].size();
+        const int64_t L = groups[(size_t)r].L;
         int64_t cap = bases / 8 + 64 * ng + 1024;
         cig_g[r].resize((size_t)cap), off_g[r].resize((size_t)ng + 1);
         gins.resize((size_t)ng), gst.resize((size_t)ng);
@@ -574,8 +588,8 @@ extern "C" int hg_refset_align(hg_refset_t* R, const uint8_t* packed, const int6
     cigar_off[0] = 0;
     for (int64_t i = 0; i < n; ++i) cigar_off[i + 1] = cigar_off[i] + n_cig[i];
     if (n && cigar_off[n] > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_refset_align: cigar buffer too small");
-    for (int r = 0; r < n_refs; ++r) {
-        const auto& m = members[(size_t)r];
+    for (int r = 0; r < n_groups; ++r) {
+        const auto& m = groups[(size_t)r].m;
 #pragma omp parallel for schedule(dynamic, 256)
         for (int64_t j = 0; j < (int64_t)m.size(); ++j) {
             const int64_t i = m[(size_t)j];

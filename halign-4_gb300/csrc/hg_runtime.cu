@@ -119,7 +119,11 @@ struct hg_ctx {
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
     cudaStream_t st3 = nullptr;                            // side stream of the one-warp wavefront and exact tiers
     // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
-    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells, 0};
+    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells, 0, 2};
+    // second compute lane: a context of the same capacity on its own streams
+    // that runs every other sub-batch of a multi-sub-batch run (knob 9 = 2)
+    hg_ctx* peer = nullptr;
+    cudaEvent_t lane_ev = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, join3_ev = nullptr;
     int sms = 1;
     int64_t max_n = 0, max_bases = 0, exc_cap = 0;
@@ -214,6 +218,7 @@ struct hg_ctx {
     bool run_recorded = false;
     float last_total_ms = 0, last_stage_ms[8] = {};
     int64_t last_launches = 0, last_cells = 0;
+    int lanes_used = 1;  // lanes of the last staged run
 };
 
 extern "C" const char* hg_last_error(void) { return g_err.c_str(); }
@@ -762,8 +767,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
 // per-CTA scratch slice in range.  Cached graphs are dropped.
 extern "C" int hg_ctx_set_launch(hg_ctx_t* c, const int32_t* ctas_per_sm, int n)
 {
-    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1, 0, 0, 0};
-    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32, hg::kThinMaxInner, hg::kSquareMaxCells, 1};
+    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1, 0, 0, 0, 1};
+    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32, hg::kThinMaxInner, hg::kSquareMaxCells, 1, 2};
     if (!c || !ctas_per_sm || n < 0 || n > HG_LAUNCH_KNOBS) return fail(HG_ERR_ARG, "hg_ctx_set_launch: bad arguments");
     for (int i = 0; i < n; ++i)
         if (ctas_per_sm[i] < lo[i] || ctas_per_sm[i] > hi[i])
@@ -772,6 +777,11 @@ extern "C" int hg_ctx_set_launch(hg_ctx_t* c, const int32_t* ctas_per_sm, int n)
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
     for (int i = 0; i < n; ++i) c->launch[i] = ctas_per_sm[i];
+    if (c->peer) {
+        const int r = hg_ctx_set_launch(c->peer, ctas_per_sm, n);
+        c->peer->launch[9] = 1;  // the second lane never opens a third
+        return r;
+    }
     return HG_OK;
 }
 
@@ -786,6 +796,8 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
 {
     if (!c) return;
     cudaSetDevice(c->ix->device);
+    if (c->peer) hg_ctx_destroy(c->peer), c->peer = nullptr;
+    if (c->lane_ev) cudaEventDestroy(c->lane_ev);
     if (c->st) cudaStreamSynchronize(c->st);
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     if (c->h_packed) cudaFreeHost(c->h_packed);
@@ -940,6 +952,30 @@ int enqueue_stages(hg_ctx_t* c, const hg::BatchDev& b, bool timed)
     HG_CUDA(hg_launch_status_or(c->status.p, n, c->run_flags.p, c->control.p, b.s_n, c->work.p, st));
     (void)kStageNames;
     return HG_OK;
+}
+
+// The second compute lane of a multi-sub-batch run (nullptr: one lane).  The
+// peer is created on first use with the context's capacity and launch
+// knobs; when the device has no room for it the context stays at one lane.
+hg_ctx_t* lane_peer(hg_ctx_t* c)
+{
+    if (c->launch[9] < 2) return nullptr;
+    if (!c->peer) {
+        hg_ctx_t* p = nullptr;
+        const std::string saved = g_err;
+        if (hg_ctx_create(c->ix, c->max_n, c->max_bases, &p) != HG_OK ||
+            cudaEventCreateWithFlags(&c->lane_ev, cudaEventDisableTiming) != cudaSuccess) {
+            if (p) hg_ctx_destroy(p);
+            cudaGetLastError();
+            g_err = saved;
+            c->launch[9] = 1;
+            return nullptr;
+        }
+        std::copy(c->launch, c->launch + HG_LAUNCH_KNOBS, p->launch);
+        p->launch[9] = 1;
+        c->peer = p;
+    }
+    return c->peer;
 }
 
 int run_sub(hg_ctx_t* c, const hg::BatchDev& b, bool use_graph)
@@ -1150,29 +1186,37 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         HG_CUDA(cudaEventRecord(c->pipe[slot].in_ready, is));
         return HG_OK;
     };
-    if ((r = issue_inputs(0))) return r;
-    int64_t cig_base = 0;
-    for (int k = 0; k < K; ++k) {
+    // lanes: with two, the odd sub-batches compute on the second lane's
+    // arenas and streams, and sub-batch k+1 is enqueued before k's offsets are
+    // read (its lane's scratch is not reused before that read)
+    hg_ctx_t* P = K > 1 ? lane_peer(c) : nullptr;
+    auto lane_of = [&](int k) -> hg_ctx_t* { return (P && (k & 1)) ? P : c; };
+    auto rows_of = [&](int k) -> uint8_t* {
+        return (k & 1) ? (P ? P->rows.p : c->rows2.p) : c->rows.p;
+    };
+    auto enqueue_compute = [&](int k) -> int {
         const SubPlan& sp = plans[(size_t)k];
         const int slot = k & 1;
         auto& PS = c->pipe[slot];
         const InView V = in_view(c, slot);
-        const int64_t f = sp.first, m = sp.n;
-        uint8_t* rbuf = slot ? c->rows2.p : c->rows.p;
-        cudaStream_t st = c->st;
+        hg_ctx_t* L = lane_of(k);
+        const int64_t m = sp.n;
+        uint8_t* rbuf = rows_of(k);
+        cudaStream_t st = L->st;
         HG_CUDA(cudaStreamWaitEvent(st, PS.in_ready, 0));
         if (rows) HG_CUDA(cudaStreamWaitEvent(st, c->rows_ev[slot], 0));  // its last read-back is done
-        hg::BatchDev b = batch_view(c, (int)m, V.packed, V.poff, V.qlen, V.exc, V.exc_off, V.order, V.hoff, V.coff);
+        hg::BatchDev b = batch_view(L, (int)m, V.packed, V.poff, V.qlen, V.exc, V.exc_off, V.order, V.hoff, V.coff);
         if (rbuf) b.rows = rbuf;
-        if ((r = run_sub(c, b, true))) return r;
-        compact_offsets_kernel<<<1, 1024, 0, st>>>(c->n_cig.p, (int)m, c->cig_off.p);
+        int rr = run_sub(L, b, true);
+        if (rr) return rr;
+        compact_offsets_kernel<<<1, 1024, 0, st>>>(L->n_cig.p, (int)m, L->cig_off.p);
         HG_CUDA(cudaGetLastError());
-        HG_CUDA(cudaMemcpyAsync(PS.h_off, c->cig_off.p, 8 * ((size_t)m + 1), cudaMemcpyDeviceToHost, st));
-        HG_CUDA(cudaMemcpyAsync(PS.h_status, c->status.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, st));
-        if (has_ins) HG_CUDA(cudaMemcpyAsync(PS.h_ins, c->has_ins.p, (size_t)m, cudaMemcpyDeviceToHost, st));
+        HG_CUDA(cudaMemcpyAsync(PS.h_off, L->cig_off.p, 8 * ((size_t)m + 1), cudaMemcpyDeviceToHost, st));
+        HG_CUDA(cudaMemcpyAsync(PS.h_status, L->status.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, st));
+        if (has_ins) HG_CUDA(cudaMemcpyAsync(PS.h_ins, L->has_ins.p, (size_t)m, cudaMemcpyDeviceToHost, st));
         HG_CUDA(cudaEventRecord(PS.off_ev, st));
         HG_CUDA(cudaStreamWaitEvent(st, PS.cfree, 0));  // the slot's previous CIGARs have copied out
-        compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(c->cig.p, V.coff, c->n_cig.p, c->cig_off.p, (int)m, V.compact,
+        compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(L->cig.p, V.coff, L->n_cig.p, L->cig_off.p, (int)m, V.compact,
                                                         (int64_t)V.compact_n, 0);
         HG_CUDA(cudaGetLastError());
         HG_CUDA(cudaEventRecord(PS.in_free, st));
@@ -1180,6 +1224,7 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         // the rows copy out behind the small read-backs above (copies in one
         // direction share an engine in order, and the offsets gate the next launch)
         if (rows) {
+            const int64_t f = sp.first;
             HG_CUDA(cudaStreamWaitEvent(c->cst, PS.done, 0));
             if (row_stride == c->row_stride)
                 HG_CUDA(cudaMemcpyAsync(rows + f * row_stride, rbuf, (size_t)row_stride * (size_t)m,
@@ -1189,8 +1234,17 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
                                           (size_t)c->ix->L, (size_t)m, cudaMemcpyDeviceToHost, c->cst));
             HG_CUDA(cudaEventRecord(c->rows_ev[slot], c->cst));
         }
-        if (k + 1 < K && (r = issue_inputs(k + 1))) return r;  // host work and upload overlap this compute
-        // the offsets decide the copy before the next sub-batch may overwrite the scratch
+        return HG_OK;
+    };
+    int64_t cig_base = 0;
+    auto read_back = [&](int k) -> int {
+        const SubPlan& sp = plans[(size_t)k];
+        const int slot = k & 1;
+        auto& PS = c->pipe[slot];
+        const InView V = in_view(c, slot);
+        hg_ctx_t* L = lane_of(k);
+        const int64_t f = sp.first, m = sp.n;
+        // the offsets decide the copy before the lane's scratch may be overwritten
         HG_CUDA(cudaEventSynchronize(PS.off_ev));
         const int64_t total = PS.h_off[m];
         if (cig_base + total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_align_batch: cigar buffer too small");
@@ -1200,22 +1254,32 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
                 HG_CUDA(cudaMemcpyAsync(cigar + cig_base, V.compact, 4 * (size_t)total, cudaMemcpyDeviceToHost, c->cst));
             HG_CUDA(cudaEventRecord(PS.cfree, c->cst));
         } else {  // more CIGAR words than the buffer: copy in pieces now
-            HG_CUDA(cudaStreamSynchronize(st));
+            HG_CUDA(cudaStreamSynchronize(L->st));
             for (int64_t done = 0; done < total; done += (int64_t)V.compact_n) {
                 const int64_t cnt = std::min((int64_t)V.compact_n, total - done);
-                compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(c->cig.p, V.coff, c->n_cig.p, c->cig_off.p, (int)m,
-                                                                V.compact, cnt, done);
+                compact_copy_kernel<<<c->sms * 4, 256, 0, L->st>>>(L->cig.p, V.coff, L->n_cig.p, L->cig_off.p, (int)m,
+                                                                   V.compact, cnt, done);
                 HG_CUDA(cudaGetLastError());
                 HG_CUDA(cudaMemcpyAsync(cigar + cig_base + done, V.compact, 4 * (size_t)cnt, cudaMemcpyDeviceToHost,
-                                        st));
+                                        L->st));
             }
-            HG_CUDA(cudaStreamSynchronize(st));
+            HG_CUDA(cudaStreamSynchronize(L->st));
         }
         for (int64_t i = 0; i <= m; ++i) cigar_off[f + i] = cig_base + PS.h_off[i];
         std::memcpy(status + f, PS.h_status, 4 * (size_t)m);
         if (has_ins) std::memcpy(has_ins + f, PS.h_ins, (size_t)m);
         cig_base += total;
+        return HG_OK;
+    };
+    if ((r = issue_inputs(0))) return r;
+    if (P && (r = enqueue_compute(0))) return r;
+    for (int k = 0; k < K; ++k) {
+        if (!P && (r = enqueue_compute(k))) return r;
+        if (k + 1 < K && (r = issue_inputs(k + 1))) return r;  // host work and upload overlap this compute
+        if (P && k + 1 < K && (r = enqueue_compute(k + 1))) return r;
+        if ((r = read_back(k))) return r;
     }
+    if (P) HG_CUDA(cudaStreamSynchronize(P->st));
     HG_CUDA(cudaStreamSynchronize(c->cst));
     HG_CUDA(cudaStreamSynchronize(c->st));
     return status_error(status, n);
@@ -1391,6 +1455,13 @@ extern "C" int hg_counters(hg_ctx_t* c, uint32_t* counts7, uint32_t* ins, int re
         HG_CUDA(cudaMemset(c->counts.p, 0, 4 * (size_t)L * 7));
         HG_CUDA(cudaMemset(c->ins.p, 0, 4 * (size_t)(L + 1)));
     }
+    if (c->peer) {  // rows aligned on the second lane (uint32 sums wrap as SiteCount's do)
+        std::vector<uint32_t> pc(counts7 ? (size_t)L * 7 : 0), pi(ins ? (size_t)L + 1 : 0);
+        int r = hg_counters(c->peer, counts7 ? pc.data() : nullptr, ins ? pi.data() : nullptr, reset);
+        if (r) return r;
+        for (size_t i = 0; i < pc.size(); ++i) counts7[i] += pc[i];
+        for (size_t i = 0; i < pi.size(); ++i) ins[i] += pi[i];
+    }
     return HG_OK;
 }
 
@@ -1453,16 +1524,33 @@ extern "C" int hg_run_staged(hg_ctx_t* c)
     c->last_total_ms = 0;
     std::fill(c->last_stage_ms, c->last_stage_ms + 8, 0.0f);
     c->last_launches = 0;
+    // every other sub-batch on the second lane (its own arenas and streams),
+    // reading the staged inputs; the run's end waits for both lanes
+    hg_ctx_t* P = (c->timing || c->staged_plan.size() < 2) ? nullptr : lane_peer(c);
     HG_CUDA(cudaMemsetAsync(c->cells.p, 0, 2 * sizeof(unsigned long long), c->st));
     HG_CUDA(cudaMemsetAsync(c->run_flags.p, 0, sizeof(uint32_t), c->st));
     HG_CUDA(cudaEventRecord(c->run_ev[0], c->st));
-    for (const SubPlan& sp : c->staged_plan) {
+    if (P) {
+        P->last_launches = 0;
+        HG_CUDA(cudaStreamWaitEvent(P->st, c->run_ev[0], 0));
+        HG_CUDA(cudaMemsetAsync(P->cells.p, 0, 2 * sizeof(unsigned long long), P->st));
+        HG_CUDA(cudaMemsetAsync(P->run_flags.p, 0, sizeof(uint32_t), P->st));
+    }
+    c->lanes_used = P ? 2 : 1;
+    for (size_t k = 0; k < c->staged_plan.size(); ++k) {
+        const SubPlan& sp = c->staged_plan[k];
         const int64_t f = sp.first;
+        hg_ctx_t* L = (P && (k & 1)) ? P : c;
         // exception offsets of the sub-batch are global: rebase through exc_off view
-        const hg::BatchDev b = batch_view(c, (int)sp.n, c->s_packed.p, c->s_poff.p + f, c->s_qlen.p + f, c->s_exc.p,
+        const hg::BatchDev b = batch_view(L, (int)sp.n, c->s_packed.p, c->s_poff.p + f, c->s_qlen.p + f, c->s_exc.p,
                                           c->s_exc_off.p + f, c->s_order.p + f, c->s_hoff.p + f, c->s_coff.p + f);
-        int r = run_sub(c, b, true);
+        int r = run_sub(L, b, true);
         if (r) return r;
+    }
+    if (P) {
+        HG_CUDA(cudaEventRecord(c->lane_ev, P->st));
+        HG_CUDA(cudaStreamWaitEvent(c->st, c->lane_ev, 0));
+        c->last_launches += P->last_launches;
     }
     HG_CUDA(cudaEventRecord(c->run_ev[1], c->st));
     c->run_recorded = true;
@@ -1480,9 +1568,10 @@ extern "C" int hg_last_timing(hg_ctx_t* c, float* total_ms, float* stage_ms, int
     if (stage_ms) std::copy(c->last_stage_ms, c->last_stage_ms + 8, stage_ms);
     if (launches) *launches = c->last_launches;
     if (cells) {
-        unsigned long long v = 0;
-        HG_CUDA(cudaMemcpy(&v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
-        *cells = (int64_t)v;
+        int64_t v = 0;
+        int r = hg_last_cells(c, &v, nullptr);
+        if (r) return r;
+        *cells = v;
     }
     return HG_OK;
 }
@@ -1492,10 +1581,14 @@ extern "C" int hg_last_cells(hg_ctx_t* c, int64_t* cells, int64_t* match_cells)
     if (!c) return fail(HG_ERR_ARG, "hg_last_cells: null context");
     cudaSetDevice(c->ix->device);
     HG_CUDA(cudaStreamSynchronize(c->st));
-    unsigned long long v[2] = {0, 0};
+    unsigned long long v[2] = {0, 0}, w[2] = {0, 0};
     HG_CUDA(cudaMemcpy(v, c->cells.p, sizeof(v), cudaMemcpyDeviceToHost));
-    if (cells) *cells = (int64_t)v[0];
-    if (match_cells) *match_cells = (int64_t)v[1];
+    if (c->peer && c->lanes_used == 2) {  // the second lane's sub-batches
+        HG_CUDA(cudaStreamSynchronize(c->peer->st));
+        HG_CUDA(cudaMemcpy(w, c->peer->cells.p, sizeof(w), cudaMemcpyDeviceToHost));
+    }
+    if (cells) *cells = (int64_t)(v[0] + w[0]);
+    if (match_cells) *match_cells = (int64_t)(v[1] + w[1]);
     return HG_OK;
 }
 
@@ -1507,6 +1600,13 @@ extern "C" int hg_ctx_work(hg_ctx_t* c, int64_t* counts, int n)
     unsigned long long v[4] = {0, 0, 0, 0};
     HG_CUDA(cudaMemcpy(v, c->work.p, sizeof(v), cudaMemcpyDeviceToHost));
     for (int i = 0; i < n && i < 4; ++i) counts[i] = (int64_t)v[i];
+    if (c->peer) {  // work of the second lane's sub-batches
+        int64_t w[4] = {0, 0, 0, 0};
+        HG_CUDA(cudaStreamSynchronize(c->peer->st));
+        int r = hg_ctx_work(c->peer, w, n < 4 ? n : 4);
+        if (r) return r;
+        for (int i = 0; i < n && i < 4; ++i) counts[i] += w[i];
+    }
     return HG_OK;
 }
 
@@ -1516,6 +1616,11 @@ extern "C" int hg_staged_flags(hg_ctx_t* c, uint32_t* flags)
     cudaSetDevice(c->ix->device);
     HG_CUDA(cudaStreamSynchronize(c->st));
     HG_CUDA(cudaMemcpy(flags, c->run_flags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (c->peer && c->lanes_used == 2) {
+        uint32_t f2 = 0;
+        HG_CUDA(cudaMemcpy(&f2, c->peer->run_flags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+        *flags |= f2;
+    }
     return HG_OK;
 }
 

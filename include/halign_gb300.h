@@ -136,10 +136,15 @@ int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* 
  * tier computes the same alignment, so the knobs change speed only.  [8]
  * small-tier form (0: one segment per thread in int32 lanes; 1: two
  * same-shape segments per thread in the 16-bit halves of 32-bit words).
- * Defaults 6 6 12 12 8 6 32 12288 0.  Setting them drops the context's
- * cached CUDA graphs (the autotuner, halign-4_gb300/autotune.py, searches
- * them).  No reference counterpart: launch geometry. */
-#define HG_LAUNCH_KNOBS 9
+ * [9] compute lanes of a staged run of several sub-batches (1 or 2): with 2,
+ * every other sub-batch runs on a second context of the same capacity and
+ * its own streams (created on first use, so the device memory of the
+ * context doubles; without room for it the context keeps one lane), and the
+ * two overlap on the GPU.  Defaults 6 6 12 12 8 6 32 12288 0 2.  Setting
+ * them drops the context's cached CUDA graphs (the autotuner,
+ * halign-4_gb300/autotune.py, searches them).  No reference counterpart:
+ * launch geometry. */
+#define HG_LAUNCH_KNOBS 10
 int hg_ctx_set_launch(hg_ctx_t* ctx, const int32_t* ctas_per_sm, int n);
 int hg_ctx_get_launch(const hg_ctx_t* ctx, int32_t* ctas_per_sm, int n);
 

@@ -286,9 +286,33 @@ def test_tier_boundary_knobs_do_not_change_results(gpu, pkg, name, n):
     base = ctx.align(b, rows=True)
     default = ctx.get_launch()
     for thin, sq, pair in ((0, 0, 0), (8, 2000, 1), (32, 0, 0), (0, 12288, 1), (32, 12288, 1)):
-        ctx.set_launch(default[:6] + [thin, sq, pair])
+        ctx.set_launch(default[:6] + [thin, sq, pair] + default[9:])
         got = ctx.align(b, rows=True)
         assert np.array_equal(got.cigar, base.cigar) and np.array_equal(got.cigar_off, base.cigar_off), (thin, sq,
                                                                                                       pair)
         assert np.array_equal(got.rows, base.rows)
     ctx.set_launch(default)
+
+
+def test_second_lane_covers_the_same_work(gpu, pkg):
+    """A staged run of several sub-batches on one lane and on two: the same
+    counters, status, DP cells and work totals (every other sub-batch runs
+    on the second lane's own arenas)."""
+    w = pkg.synth.mito(120)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=32, max_bases=32 * 16700)
+    ctx.stage(gpu.pack(w.seqs, w.offsets))
+    knobs = ctx.get_launch()
+    out = []
+    for lanes in (1, 2):
+        ctx.set_launch(knobs[:9] + [lanes])
+        ctx.counters(reset=True)
+        w0 = np.array(list(ctx.work().values()))
+        ctx.run_staged()
+        ctx.last_timing()
+        cnt, ins = ctx.counters(reset=True)
+        out.append((cnt, ins, ctx.staged_flags(), ctx.last_cells(), np.array(list(ctx.work().values())) - w0))
+    (c1, i1, f1, l1, k1), (c2, i2, f2, l2, k2) = out
+    assert np.array_equal(c1, c2) and np.array_equal(i1, i2)
+    assert f1 == f2 == 0 and l1 == l2
+    assert np.array_equal(k1, k2)
