@@ -54,8 +54,8 @@ PORT_VS_REF_X86 = {"threads_1": 0.98, "threads_8": 0.96}
 
 # Warp instructions per query base of the stage kernels, from their ncu
 # captures on the mito workload (profiles/kernels_mito4k.md).
-MITO_INST_PER_BASE = {"seed": 273.3e6 / 66.3e6, "anchor": 71.0e6 / 66.3e6, "chain": 420.3e6 / 66.3e6,
-                      "rows": 92.9e6 / 66.3e6}
+MITO_INST_PER_BASE = {"seed": 273.3e6 / 66.3e6, "anchor": 71.0e6 / 66.3e6, "chain": 420.4e6 / 66.3e6,
+                      "rows": 32.6e6 / 66.3e6}
 
 
 def log(*a):
@@ -272,7 +272,8 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 60000):
     sat = srv.run(ws.seqs, ws.offsets, None)
     # the same requests as one batch, device-resident and through the host-buffer call
     sub = 20000  # the batched denominator in 20,000-request sub-batches (two compute lanes)
-    ctx = pkg.Context(ix, max_queries=sub, max_bases=sub * 29903)
+    lens = np.diff(ws.offsets)
+    ctx = pkg.Context(ix, max_queries=sub, max_bases=max(int(lens[i:i + sub].sum()) for i in range(0, ws.n, sub)) + 1024)
     b = pkg.pack(ws.seqs, ws.offsets)
     ctx.stage(b)
     for _ in range(2):
@@ -322,7 +323,7 @@ def run_serve_million(args, pkg):
     w0 = pkg.synth.serve(min(chunk, args.serve_requests), chunk=0)
     ix = pkg.Index(w0.center)
     srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=4096, slot_bases=64_000_000, budget_bytes=100 << 30)
-    ctx = pkg.Context(ix, max_queries=chunk, max_bases=chunk * 29903)
+    ctx = pkg.Context(ix, max_queries=chunk, max_bases=chunk * 20000)  # requests average 15.2 kb
     pending, served, bases, t_serve, p99s, st_or = [], 0, 0, 0.0, [], 0
     for c in range(n_chunks):
         m = min(chunk, args.serve_requests - c * chunk)
@@ -623,7 +624,9 @@ def main():
         shard.check_distinct_devices(gpu_bus, dist.dist)  # two ranks on one GPU would overstate throughput
     sub = min(args.sub_batch, args.queries)
     lens = np.diff(w.offsets)
-    ctx = pkg.Context(ix, max_queries=sub, max_bases=int(min(lens.sum(), sub * int(lens.max()))) + 1024)
+    # capacity: the largest base count of `sub` consecutive queries (the sub-batches the batch splits into)
+    chunk_bases = max(int(lens[i:i + sub].sum()) for i in range(0, len(lens), sub))
+    ctx = pkg.Context(ix, max_queries=sub, max_bases=chunk_bases + 1024)
     ctx.stage(b)
     tuning = None
     if not args.no_tune:
@@ -728,6 +731,7 @@ def main():
     if n_cig_words is None:
         n_cig_words = 64 * b.n
     plain = measure_plain(pkg, ctx, w, args.plain_queries) if args.plain_queries > 0 else None
+    ctx.close()  # (and its second lane) before the serving measurement allocates its own contexts
     serving = None if args.no_serve or rank != 0 else measure_serving(pkg, args.serve_requests, 2000.0)
     peak, peak_kind = load_peaks()
     # dominant stage (one kernel launch per sub-batch) and its algorithmic

@@ -963,8 +963,15 @@ hg_ctx_t* lane_peer(hg_ctx_t* c)
     if (!c->peer) {
         hg_ctx_t* p = nullptr;
         const std::string saved = g_err;
-        if (hg_ctx_create(c->ix, c->max_n, c->max_bases, &p) != HG_OK ||
-            cudaEventCreateWithFlags(&c->lane_ev, cudaEventDisableTiming) != cudaSuccess) {
+        // the second lane must leave room: at least an eighth of the device
+        // (and 16 GB) free after it, for the host-buffer path's second input
+        // set and the caller's other work
+        size_t free_b = 0, total_b = 0;
+        bool ok = hg_ctx_create(c->ix, c->max_n, c->max_bases, &p) == HG_OK &&
+                  cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+                  free_b >= std::max<size_t>(total_b / 8, (size_t)16 << 30);
+        if (ok && !c->lane_ev) ok = cudaEventCreateWithFlags(&c->lane_ev, cudaEventDisableTiming) == cudaSuccess;
+        if (!ok) {
             if (p) hg_ctx_destroy(p);
             cudaGetLastError();
             g_err = saved;
