@@ -18,7 +18,6 @@
 #include <vector>
 
 #include <cuda_runtime.h>
-#include <omp.h>
 
 #include "../../include/halign_gb300.h"
 #include "hg_internal.h"
@@ -67,6 +66,7 @@ struct hg_server {
     int error = HG_OK;
     std::string error_msg;
     std::vector<std::thread> workers;
+    std::mutex pack_mu;  // packing uses every host core: one micro-batch at a time
 };
 
 namespace {
@@ -109,14 +109,13 @@ void fail_all(hg_server* S, int code, const std::string& msg)
 }
 
 // One worker thread per context: admit the oldest waiting requests (under
-// the lock, so micro-batches leave the FIFO in order), pack and submit them,
-// wait for the context, collect, and publish the results.  Workers pack and
-// collect in parallel, so the host side scales with the contexts.
+// the lock, so micro-batches leave the FIFO in order), pack and submit them
+// (one micro-batch at a time: packing is an OpenMP loop over all host
+// cores), wait for the context, collect, and publish the results; waiting,
+// collecting and publishing of different contexts run in parallel.
 void worker(hg_server* S, int s)
 {
     cudaSetDevice(S->device);
-    // the host cores are shared by the workers' packing loops
-    omp_set_num_threads(std::max(1, omp_get_num_procs() / (int)S->slots.size()));
     Slot& sl = S->slots[s];
     std::vector<int64_t> take, len;
     std::vector<const char*> ptr;
@@ -131,7 +130,11 @@ void worker(hg_server* S, int s)
         }
         // the request strings stay put until their results are published (only
         // this worker frees them), so packing runs without the lock
-        int r = hg_submit_ascii(sl.ctx, ptr.data(), len.data(), (int64_t)take.size());
+        int r;
+        {  // one micro-batch packs at a time, on all host cores (its OpenMP loop)
+            std::lock_guard<std::mutex> pack_lock(S->pack_mu);
+            r = hg_submit_ascii(sl.ctx, ptr.data(), len.data(), (int64_t)take.size());
+        }
         if (r) {
             fail_all(S, r, hg_last_error());
             return;
