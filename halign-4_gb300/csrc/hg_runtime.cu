@@ -210,7 +210,8 @@ struct hg_ctx {
     int32_t* h_i32 = nullptr;      // qlen, order, exc (2 x max_n + exc_cap x 3)
     uint8_t* h_has_ins = nullptr;
     uint32_t* h_status = nullptr;
-    cudaEvent_t done_ev = nullptr;
+    cudaEvent_t done_ev = nullptr;     // blocking-sync: a waiting host thread sleeps instead of spinning
+    cudaEvent_t collected_ev = nullptr;
     int64_t async_n = -1;
     bool timing = false;
     cudaEvent_t ev[10] = {};
@@ -806,6 +807,7 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
     if (c->h_has_ins) cudaFreeHost(c->h_has_ins);
     if (c->h_status) cudaFreeHost(c->h_status);
     if (c->done_ev) cudaEventDestroy(c->done_ev);
+    if (c->collected_ev) cudaEventDestroy(c->collected_ev);
     if (c->ist) cudaStreamSynchronize(c->ist), cudaStreamDestroy(c->ist);
     for (auto& ps : c->pipe) {
         if (ps.h_off) cudaFreeHost(ps.h_off);
@@ -1661,7 +1663,8 @@ int async_staging(hg_ctx_t* c)
         cudaHostAlloc(&c->h_i32, sizeof(int32_t) * (2 * M + 3 * c->exc_cap), cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc(&c->h_has_ins, (size_t)M, cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc(&c->h_status, sizeof(uint32_t) * M, cudaHostAllocDefault) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->done_ev, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreateWithFlags(&c->done_ev, cudaEventDisableTiming | cudaEventBlockingSync) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->collected_ev, cudaEventDisableTiming | cudaEventBlockingSync) != cudaSuccess)
         return fail(HG_ERR_NOMEM, "hg_submit: pinned staging allocation");
     return HG_OK;
 }
@@ -1804,7 +1807,8 @@ extern "C" int hg_collect(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64
         HG_CUDA(cudaGetLastError());
         HG_CUDA(cudaMemcpyAsync(cigar + done, c->cig_compact.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, c->st));
     }
-    HG_CUDA(cudaStreamSynchronize(c->st));
+    HG_CUDA(cudaEventRecord(c->collected_ev, c->st));
+    HG_CUDA(cudaEventSynchronize(c->collected_ev));
     for (int64_t i = 0; i <= n; ++i) cigar_off[i] = off[i];
     if (has_ins) std::memcpy(has_ins, c->h_has_ins, (size_t)n);
     if (status) std::memcpy(status, c->h_status, 4 * (size_t)n);
