@@ -1,7 +1,7 @@
 // hg_serve.cpp - the continuous-batching request loop behind hg_serve_*
 // (include/halign_gb300.h): a FIFO of submitted requests, a pool of
-// contexts over one resident index, and one worker thread per context that
-// admits, submits (hg_submit_ascii), waits for and collects micro-batches.
+// contexts over one resident index, and a scheduler thread that admits,
+// submits (hg_submit_ascii), polls and collects micro-batches.
 //
 // Host code only; every alignment runs through the context calls of the C
 // ABI.  Requests are independent, so a request's result in the mix is its
@@ -65,8 +65,7 @@ struct hg_server {
     bool stop = false;
     int error = HG_OK;
     std::string error_msg;
-    std::vector<std::thread> workers;
-    std::mutex pack_mu;  // packing uses every host core: one micro-batch at a time
+    std::thread sched;
 };
 
 namespace {
@@ -105,73 +104,104 @@ void fail_all(hg_server* S, int code, const std::string& msg)
     S->error = code;
     S->error_msg = msg;
     S->cv_done.notify_all();
-    S->cv_work.notify_all();  // the other workers stop too
 }
 
-// One worker thread per context: admit the oldest waiting requests (under
-// the lock, so micro-batches leave the FIFO in order), pack and submit them
-// (one micro-batch at a time: packing is an OpenMP loop over all host
-// cores), wait for the context, collect, and publish the results; waiting,
-// collecting and publishing of different contexts run in parallel.
-void worker(hg_server* S, int s)
+void scheduler(hg_server* S)
 {
     cudaSetDevice(S->device);
-    Slot& sl = S->slots[s];
+    std::vector<int> free_slots;
+    for (int i = (int)S->slots.size() - 1; i >= 0; --i) free_slots.push_back(i);
+    std::vector<int> busy;
     std::vector<int64_t> take, len;
     std::vector<const char*> ptr;
-    std::vector<std::vector<uint32_t>> cigs;
     for (;;) {
-        {
-            std::unique_lock<std::mutex> lock(S->mu);
-            S->cv_work.wait(lock, [&] { return S->stop || S->error || !S->pending.empty(); });
-            if (S->error || S->pending.empty()) return;  // stopping with nothing left
-            admit(S, take, ptr, len);
-            ++S->batches;
-        }
-        // the request strings stay put until their results are published (only
-        // this worker frees them), so packing runs without the lock
-        int r;
-        {  // one micro-batch packs at a time, on all host cores (its OpenMP loop)
-            std::lock_guard<std::mutex> pack_lock(S->pack_mu);
-            r = hg_submit_ascii(sl.ctx, ptr.data(), len.data(), (int64_t)take.size());
-        }
-        if (r) {
-            fail_all(S, r, hg_last_error());
-            return;
-        }
-        const size_t n = take.size();
-        int64_t bases = 0;
-        for (int64_t x : len) bases += x;
-        sl.cig.resize((size_t)bases / 8 + 64 * n + 1024);  // a few ops per kilobase; grown below if short
-        sl.off.resize(n + 1), sl.ins.resize(n), sl.st.resize(n);
-        r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(), sl.st.data());
-        if (r == HG_ERR_CAPACITY) {  // rare: CIGARs longer than the first guess; the worst case fits
-            sl.cig.resize((size_t)bases + n * (size_t)(hg::index_length(S->ix) + 4));
-            r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(),
-                           sl.st.data());
-        }
-        if (r && r != HG_ERR_LENGTH_MISMATCH) {
-            fail_all(S, r, hg_last_error());
-            return;
-        }
-        const auto now = Clock::now();
-        cigs.resize(n);
-        for (size_t j = 0; j < n; ++j) cigs[j].assign(sl.cig.begin() + sl.off[j], sl.cig.begin() + sl.off[j + 1]);
-        {
-            std::lock_guard<std::mutex> lock(S->mu);
-            for (size_t j = 0; j < n; ++j) {
-                Request& q = S->reqs[(size_t)(take[j] - S->base_id)];
-                q.cigar.swap(cigs[j]);
-                q.status = sl.st[j];
-                q.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_in).count();
-                std::string().swap(q.seq);
-                S->lat.push_back((float)q.latency_ms);
-                S->done.push_back(take[j]);
+        bool progressed = false;
+        // admit and submit into every free context
+        while (!free_slots.empty()) {
+            {
+                std::unique_lock<std::mutex> lock(S->mu);
+                if (S->pending.empty()) {
+                    if (S->stop && busy.empty()) return;
+                    if (busy.empty()) {
+                        S->cv_work.wait(lock, [&] { return S->stop || !S->pending.empty(); });
+                        if (S->pending.empty()) return;
+                    } else {
+                        break;
+                    }
+                }
+                admit(S, take, ptr, len);
             }
-            S->bases_done += bases;
-            S->t_last = now;
+            if (take.empty()) break;
+            const int s = free_slots.back();
+            free_slots.pop_back();
+            // the request strings stay put until collection (only the scheduler
+            // frees them), so packing runs without the lock
+            const int r = hg_submit_ascii(S->slots[s].ctx, ptr.data(), len.data(), (int64_t)take.size());
+            if (r) {
+                fail_all(S, r, hg_last_error());
+                return;
+            }
+            S->slots[s].ids = take;
+            busy.push_back(s);
+            {
+                std::lock_guard<std::mutex> lock(S->mu);
+                ++S->batches;
+            }
+            progressed = true;
         }
-        S->cv_done.notify_all();
+        // collect finished micro-batches
+        for (size_t k = 0; k < busy.size();) {
+            const int s = busy[k];
+            Slot& sl = S->slots[s];
+            const int p = hg_poll(sl.ctx);
+            if (p < 0) {
+                fail_all(S, -p, hg_last_error());
+                return;
+            }
+            if (p == 0) {
+                ++k;
+                continue;
+            }
+            const size_t n = sl.ids.size();
+            int64_t bases = 0;
+            {
+                std::lock_guard<std::mutex> lock(S->mu);
+                for (int64_t id : sl.ids) bases += (int64_t)S->reqs[(size_t)(id - S->base_id)].seq.size();
+            }
+            sl.cig.resize((size_t)bases / 8 + 64 * n + 1024);  // a few ops per kilobase; grown below if short
+            sl.off.resize(n + 1), sl.ins.resize(n), sl.st.resize(n);
+            int r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(), sl.st.data());
+            if (r == HG_ERR_CAPACITY) {  // rare: CIGARs longer than the first guess; the worst case fits
+                sl.cig.resize((size_t)bases + n * (size_t)(hg::index_length(S->ix) + 4));
+                r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(),
+                               sl.st.data());
+            }
+            if (r && r != HG_ERR_LENGTH_MISMATCH) {
+                fail_all(S, r, hg_last_error());
+                return;
+            }
+            const auto now = Clock::now();
+            {
+                std::lock_guard<std::mutex> lock(S->mu);
+                for (size_t j = 0; j < n; ++j) {
+                    Request& q = S->reqs[(size_t)(sl.ids[j] - S->base_id)];
+                    q.cigar.assign(sl.cig.begin() + sl.off[j], sl.cig.begin() + sl.off[j + 1]);
+                    q.status = sl.st[j];
+                    q.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_in).count();
+                    std::string().swap(q.seq);
+                    S->lat.push_back((float)q.latency_ms);
+                    S->done.push_back(sl.ids[j]);
+                }
+                S->bases_done += bases;
+                S->t_last = now;
+            }
+            S->cv_done.notify_all();
+            sl.ids.clear();
+            free_slots.push_back(s);
+            busy.erase(busy.begin() + (long)k);
+            progressed = true;
+        }
+        if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
@@ -206,7 +236,7 @@ extern "C" int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries
         hg_serve_destroy(S);
         return hg::set_error(HG_ERR_CAPACITY, "hg_serve_create: one context does not fit the device-memory budget");
     }
-    for (int i = 0; i < (int)S->slots.size(); ++i) S->workers.emplace_back(worker, S, i);
+    S->sched = std::thread(scheduler, S);
     *out = S;
     return HG_OK;
 }
@@ -220,8 +250,7 @@ extern "C" void hg_serve_destroy(hg_server_t* S)
         S->pending.clear();
     }
     S->cv_work.notify_all();
-    for (auto& t : S->workers)
-        if (t.joinable()) t.join();
+    if (S->sched.joinable()) S->sched.join();
     for (auto& sl : S->slots) hg_ctx_destroy(sl.ctx);
     delete S;
 }
@@ -258,6 +287,7 @@ extern "C" int64_t hg_serve_submit_many(hg_server_t* S, const char* seqs, const 
     // the copies are made before the lock; one time stamp for the burst
     std::vector<Request> burst((size_t)n);
     const auto now = Clock::now();
+#pragma omp parallel for schedule(dynamic, 64)
     for (int64_t i = 0; i < n; ++i) {
         burst[i].seq.assign(seqs + offsets[i], (size_t)(offsets[i + 1] - offsets[i]));
         burst[i].t_in = now;
