@@ -265,7 +265,7 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 60000):
     rate (Poisson arrivals) for latency at load."""
     w = pkg.synth.serve(n_req, rate=rate)
     ix = pkg.Index(w.center)
-    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=4096, slot_bases=64_000_000, budget_bytes=100 << 30)
+    srv = pkg.serve.NativeServer(ix, n_slots=4, slot_queries=8192, slot_bases=128_000_000, budget_bytes=100 << 30)
     srv.run(w.seqs, w.offsets[: min(w.n, 400) + 1], None)  # warm-up
     st = srv.run(w.seqs, w.offsets, w.arrivals)
     ws = pkg.synth.serve(n_sat, rate=rate, chunk=1)
@@ -322,7 +322,7 @@ def run_serve_million(args, pkg):
     n_chunks = -(-args.serve_requests // chunk)
     w0 = pkg.synth.serve(min(chunk, args.serve_requests), chunk=0)
     ix = pkg.Index(w0.center)
-    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=4096, slot_bases=64_000_000, budget_bytes=100 << 30)
+    srv = pkg.serve.NativeServer(ix, n_slots=4, slot_queries=8192, slot_bases=128_000_000, budget_bytes=100 << 30)
     ctx = pkg.Context(ix, max_queries=chunk, max_bases=chunk * 20000)  # requests average 15.2 kb
     pending, served, bases, t_serve, p99s, st_or = [], 0, 0, 0.0, [], 0
     for c in range(n_chunks):
