@@ -1,7 +1,8 @@
 // hg_serve.cpp - the continuous-batching request loop behind hg_serve_*
 // (include/halign_gb300.h): a FIFO of submitted requests, a pool of
-// contexts over one resident index, and a scheduler thread that admits,
-// submits (hg_submit_ascii), polls and collects micro-batches.
+// contexts over one resident index, a submitting thread that admits and
+// packs micro-batches into free contexts (hg_submit_ascii) and a collecting
+// thread that polls, collects and files them, so packing and filing overlap.
 //
 // Host code only; every alignment runs through the context calls of the C
 // ABI.  Requests are independent, so a request's result in the mix is its
@@ -42,6 +43,7 @@ struct Slot {
     std::vector<int64_t> off;
     std::vector<uint8_t> ins;
     std::vector<uint32_t> st;
+    int state = 0;  // 0 free, 1 packing (submitting thread), 2 in flight (collecting thread)
 };
 
 }  // namespace
@@ -53,7 +55,7 @@ struct hg_server {
     int64_t arena_bytes = 0;
     std::vector<Slot> slots;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_work, cv_done, cv_busy;
     std::deque<Request> reqs;     // request id - base_id indexes it
     int64_t base_id = 0;
     std::deque<int64_t> pending;  // submitted, not yet admitted
@@ -65,7 +67,8 @@ struct hg_server {
     bool stop = false;
     int error = HG_OK;
     std::string error_msg;
-    std::thread sched;
+    bool submitter_done = false;
+    std::thread sub, col;
 };
 
 namespace {
@@ -104,64 +107,93 @@ void fail_all(hg_server* S, int code, const std::string& msg)
     S->error = code;
     S->error_msg = msg;
     S->cv_done.notify_all();
+    S->cv_work.notify_all();
+    S->cv_busy.notify_all();
 }
 
-void scheduler(hg_server* S)
+// Submitting thread: whenever a context is free and requests wait, admit the
+// oldest (under the lock, so micro-batches leave the FIFO in order), pack
+// them on all host cores (hg_submit_ascii's OpenMP loop) and enqueue them;
+// the context is then the collecting thread's to poll.
+void submitter(hg_server* S)
 {
     cudaSetDevice(S->device);
-    std::vector<int> free_slots;
-    for (int i = (int)S->slots.size() - 1; i >= 0; --i) free_slots.push_back(i);
-    std::vector<int> busy;
     std::vector<int64_t> take, len;
     std::vector<const char*> ptr;
+    const int ns = (int)S->slots.size();
     for (;;) {
-        bool progressed = false;
-        // admit and submit into every free context
-        while (!free_slots.empty()) {
-            {
-                std::unique_lock<std::mutex> lock(S->mu);
-                if (S->pending.empty()) {
-                    if (S->stop && busy.empty()) return;
-                    if (busy.empty()) {
-                        S->cv_work.wait(lock, [&] { return S->stop || !S->pending.empty(); });
-                        if (S->pending.empty()) return;
-                    } else {
-                        break;
-                    }
-                }
-                admit(S, take, ptr, len);
-            }
-            if (take.empty()) break;
-            const int s = free_slots.back();
-            free_slots.pop_back();
-            // the request strings stay put until collection (only the scheduler
-            // frees them), so packing runs without the lock
-            const int r = hg_submit_ascii(S->slots[s].ctx, ptr.data(), len.data(), (int64_t)take.size());
-            if (r) {
-                fail_all(S, r, hg_last_error());
+        int s = -1;
+        {
+            std::unique_lock<std::mutex> lock(S->mu);
+            S->cv_work.wait(lock, [&] {
+                if (S->error || (S->stop && S->pending.empty())) return true;
+                if (S->pending.empty()) return false;
+                for (const Slot& sl : S->slots)
+                    if (sl.state == 0) return true;
+                return false;
+            });
+            if (S->error || (S->stop && S->pending.empty())) {
+                S->submitter_done = true;
+                S->cv_busy.notify_all();
                 return;
             }
+            for (int i = 0; i < ns && s < 0; ++i)
+                if (S->slots[i].state == 0) s = i;
+            admit(S, take, ptr, len);
             S->slots[s].ids = take;
-            busy.push_back(s);
-            {
-                std::lock_guard<std::mutex> lock(S->mu);
-                ++S->batches;
-            }
-            progressed = true;
+            S->slots[s].state = 1;  // packing
+            ++S->batches;
         }
-        // collect finished micro-batches
-        for (size_t k = 0; k < busy.size();) {
-            const int s = busy[k];
+        // the request strings stay put until their results are filed (only the
+        // collecting thread frees them), so packing runs without the lock
+        const int r = hg_submit_ascii(S->slots[s].ctx, ptr.data(), len.data(), (int64_t)take.size());
+        if (r) {
+            fail_all(S, r, hg_last_error());
+            return;
+        }
+        {
+            std::lock_guard<std::mutex> lock(S->mu);
+            S->slots[s].state = 2;  // in flight
+        }
+        S->cv_busy.notify_all();
+    }
+}
+
+// Collecting thread: poll the contexts in flight, collect a finished one's
+// CIGARs and statuses, file them per request and free the context.
+void collector(hg_server* S)
+{
+    cudaSetDevice(S->device);
+    const int ns = (int)S->slots.size();
+    std::vector<int> inflight;
+    std::vector<std::vector<uint32_t>> cigs;
+    for (;;) {
+        inflight.clear();
+        {
+            std::unique_lock<std::mutex> lock(S->mu);
+            S->cv_busy.wait(lock, [&] {
+                if (S->error) return true;
+                bool busy = false;
+                for (const Slot& sl : S->slots) {
+                    if (sl.state == 2) return true;
+                    busy = busy || sl.state != 0;
+                }
+                return S->submitter_done && !busy;
+            });
+            if (S->error) return;
+            for (int i = 0; i < ns; ++i)
+                if (S->slots[i].state == 2) inflight.push_back(i);
+            if (inflight.empty()) return;  // the submitter stopped and nothing is left
+        }
+        bool progressed = false;
+        for (const int s : inflight) {
             Slot& sl = S->slots[s];
             const int p = hg_poll(sl.ctx);
             if (p < 0) {
                 fail_all(S, -p, hg_last_error());
                 return;
             }
-            if (p == 0) {
-                ++k;
-                continue;
-            }
+            if (p == 0) continue;
             const size_t n = sl.ids.size();
             int64_t bases = 0;
             {
@@ -181,11 +213,13 @@ void scheduler(hg_server* S)
                 return;
             }
             const auto now = Clock::now();
+            cigs.resize(n);
+            for (size_t j = 0; j < n; ++j) cigs[j].assign(sl.cig.begin() + sl.off[j], sl.cig.begin() + sl.off[j + 1]);
             {
                 std::lock_guard<std::mutex> lock(S->mu);
                 for (size_t j = 0; j < n; ++j) {
                     Request& q = S->reqs[(size_t)(sl.ids[j] - S->base_id)];
-                    q.cigar.assign(sl.cig.begin() + sl.off[j], sl.cig.begin() + sl.off[j + 1]);
+                    q.cigar.swap(cigs[j]);
                     q.status = sl.st[j];
                     q.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_in).count();
                     std::string().swap(q.seq);
@@ -194,11 +228,11 @@ void scheduler(hg_server* S)
                 }
                 S->bases_done += bases;
                 S->t_last = now;
+                sl.ids.clear();
+                sl.state = 0;
             }
             S->cv_done.notify_all();
-            sl.ids.clear();
-            free_slots.push_back(s);
-            busy.erase(busy.begin() + (long)k);
+            S->cv_work.notify_all();
             progressed = true;
         }
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
@@ -236,7 +270,8 @@ extern "C" int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries
         hg_serve_destroy(S);
         return hg::set_error(HG_ERR_CAPACITY, "hg_serve_create: one context does not fit the device-memory budget");
     }
-    S->sched = std::thread(scheduler, S);
+    S->sub = std::thread(submitter, S);
+    S->col = std::thread(collector, S);
     *out = S;
     return HG_OK;
 }
@@ -250,7 +285,8 @@ extern "C" void hg_serve_destroy(hg_server_t* S)
         S->pending.clear();
     }
     S->cv_work.notify_all();
-    if (S->sched.joinable()) S->sched.join();
+    if (S->sub.joinable()) S->sub.join();
+    if (S->col.joinable()) S->col.join();
     for (auto& sl : S->slots) hg_ctx_destroy(sl.ctx);
     delete S;
 }

@@ -157,7 +157,7 @@ class Server:
 
 
 class NativeServer:
-    """The same continuous-batching loop run by the library's scheduler thread
+    """The same continuous-batching loop run by the library's threads
     (hg_serve_*): Python only feeds requests at their arrival times and drains
     results on a second thread, so the host path is native end to end.  The
     device-memory budget caps the contexts created (their arenas are

@@ -256,11 +256,11 @@ int hg_align_fasta_consensus(const char* queries_fasta, const char* out_fasta, i
 
 /* ---- serving loop (continuous batching) ---------------------------------
  * A request loop around one resident index: requests (one ASCII query each,
- * copied at submission) wait in a FIFO; a scheduler thread fills every free
- * context with the oldest waiting requests (up to slot_queries and
+ * copied at submission) wait in a FIFO; a submitting thread fills every
+ * free context with the oldest waiting requests (up to slot_queries and
  * slot_bases per micro-batch) and enqueues it asynchronously
- * (hg_submit_ascii), polls the busy contexts and files each finished
- * request's CIGAR and status for hg_serve_result.  Requests that arrive
+ * (hg_submit_ascii), and a collecting thread polls the busy contexts and
+ * files each finished request's CIGAR and status for hg_serve_result.  Requests that arrive
  * while others run join as contexts free up; micro-batches of different
  * contexts overlap on the GPU.  The contexts' device arenas are allocated at
  * creation; n_slots is reduced to what budget_bytes of device memory holds
@@ -270,7 +270,7 @@ int hg_align_fasta_consensus(const char* queries_fasta, const char* out_fasta, i
 typedef struct hg_server hg_server_t;
 int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries, int64_t slot_bases, int64_t budget_bytes,
                     hg_server_t** out);
-/* Stops the scheduler after the requests in flight finish, frees everything. */
+/* Stops the loop after the requests in flight finish, frees everything. */
 void hg_serve_destroy(hg_server_t* s);
 /* Queues one request; returns its id (0, 1, 2, ... in submission order) or a
  * negative HG_ERR_* (HG_ERR_CAPACITY: longer than slot_bases). */
