@@ -468,21 +468,46 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDe
     }
 }
 
-// Sequential replay of extractMinimizer for the queries whose deque
-// overflows, with the reference's ring indexing (RingMinQueue::idx subtracts
-// the capacity once).  Ring entries past the capacity live in spare slots of
-// the warp's ring, i.e. they behave as plain memory (the reference writes
-// past its vector there).  One warp per query: per chunk of 32 positions the
-// lanes decode the bases, build the k-mer codes by a shuffle scan and hash
-// them; lane 0 runs the ring over the chunk in shared memory (the only
-// sequential part); the lanes then look the chunk's emitted minimizers up in
-// the center index together and write them in order.
+// Replay of extractMinimizer (src/seed/minimizer.cpp:103-177) for the
+// queries whose window deque overflows, with the reference's RingMinQueue
+// (src/seed/minimizer.cpp:35-97).  The ring leaves the ideal monotone-deque
+// behaviour only when a push finds it full: at a k-mer that ends win + 1
+// consecutive strictly increasing hashes of one N-free run.  Before that,
+// and again once its logical contents equal the ideal deque's, what it emits
+// follows from the hashes alone.  One warp per query, 32 bases per step, in
+// one of two modes:
+//  * ideal: each lane takes one k-mer: the window minimum over a hash
+//    history in shared memory (ties to the later position), an emission when
+//    it differs from the previous k-mer's, and whether the k-mer leaving the
+//    window is popped at the front.  Front pops are the only moves of the
+//    ring's head slot, which is all the ring state this mode keeps.
+//  * exact: from the first push that finds the ring full, lane 0 runs the
+//    ring with the reference's indexing (RingMinQueue::idx subtracts the
+//    capacity once; entries past the capacity live in spare slots, i.e.
+//    behave as plain memory, the reference writing past its vector there).
+//    Entering it rebuilds the ring: the win live entries are the last win
+//    k-mers, in consecutive slots from the head.  After each step the warp
+//    compares the ring's logical contents with the ideal deque (the suffix
+//    minima of the window); when they are equal the ring behaves ideally
+//    until the next overflow, and the warp returns to the ideal mode.
+// Each step's emissions are looked up in the center index together and
+// written in order.
 constexpr int kExactWarps = 4;
 constexpr int kExactBlocks = 64;
 
+// Hash history slots (a power of two holding a window plus a step), from
+// the ring size 2 w + 16.
+__host__ __device__ __forceinline__ int exact_hist_slots(int ring_slots)
+{
+    const int w = (ring_slots - 16) / 2;
+    int s = 64;
+    while (s < w + 64) s <<= 1;
+    return s;
+}
+
 __host__ __device__ __forceinline__ size_t exact_warp_bytes(int ring_slots)
 {
-    return ((size_t)ring_slots * 12 + 32 * 20 + 15) & ~(size_t)15;
+    return ((size_t)exact_hist_slots(ring_slots) * 8 + (size_t)ring_slots * 12 + 32 * 12 + 15) & ~(size_t)15;
 }
 
 __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev ix, BatchDev b, SeedOut so)
@@ -491,13 +516,16 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const int RS = b.ring_slots;
-    uint64_t* hs = ex_smem + wl * (exact_warp_bytes(RS) / 8);  // chunk hashes
-    uint64_t* eh = hs + 32;                                     // chunk emissions: hash
-    uint64_t* rh = eh + 32;                                     // ring: hash
-    uint32_t* ep = reinterpret_cast<uint32_t*>(rh + RS);        // chunk emissions: position
-    uint32_t* rp = ep + 32;                                     // ring: position
+    const uint32_t HM = (uint32_t)exact_hist_slots(RS) - 1u;
+    uint64_t* hist = ex_smem + wl * (exact_warp_bytes(RS) / 8);  // hash of k-mer p at p & HM
+    uint64_t* eh = hist + HM + 1;                                 // exact-mode emissions: hash
+    uint64_t* rh = eh + 32;                                       // ring: hash
+    uint32_t* ep = reinterpret_cast<uint32_t*>(rh + RS);          // exact-mode emissions: position
+    uint32_t* rp = ep + 32;                                       // ring: position
+    const unsigned le = lane == 31 ? FULL : (2u << lane) - 1u;   // lanes <= this one
+    const unsigned lt = (1u << lane) - 1u;                        // lanes < this one
     const unsigned total = *b.n_exact;
-    const int k = ix.k;
+    const uint32_t k = (uint32_t)ix.k;
     const uint64_t kmask = (1ULL << (2 * k)) - 1ULL;
     const uint32_t last_slot = (uint32_t)RS - 1;
     for (unsigned wi = blockIdx.x * kExactWarps + wl; wi < total; wi += gridDim.x * kExactWarps) {
@@ -507,24 +535,26 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
         int64_t ecur = b.exc_off[q];
         const int64_t e1 = b.exc_off[q + 1];
         const int64_t hb = b.hoff[q];
-        const uint32_t nk = n - (uint32_t)k + 1;
+        const uint32_t nk = n - k + 1;
         const uint32_t win = (uint32_t)ix.w < nk ? (uint32_t)ix.w : nk;
         for (int t = lane; t < RS; t += 32) rh[t] = 0, rp[t] = 0;
-        uint64_t last_h = 0, prev = 0;
-        uint32_t valid = 0, head = 0, size = 0, last_p = 0;
-        bool has_last = false;
+        uint64_t prev = 0, last_h = 0;
+        uint32_t run_base = 0, runlen = 0, m_prev = 0;        // carried from the previous step
+        uint32_t head = 0, size = 0, valid = 0, last_p = 0;   // ring state (head in both modes)
+        bool exact = false, has_last = false;
         int n_hits = 0, n_match = 0;
         __syncwarp();
         for (uint32_t i0 = 0; i0 < n; i0 += 32) {
             const uint32_t i = i0 + (uint32_t)lane;
+            const bool inq = i < n;
             uint32_t c = 0;
-            if (i < n) {
+            if (inq) {
                 c = packed_code(pk, i);
                 for (int64_t ee = ecur; ee < e1 && (uint32_t)b.exc[ee * 3] <= i; ++ee)
                     if (i < (uint32_t)(b.exc[ee * 3] + b.exc[ee * 3 + 1])) c = nt4_of((uint8_t)b.exc[ee * 3 + 2]);
             }
             while (ecur < e1 && (uint32_t)(b.exc[ecur * 3] + b.exc[ecur * 3 + 1]) <= i0 + 32u) ++ecur;
-            const unsigned badm = __ballot_sync(FULL, i < n && c >= 4);
+            const unsigned badm = __ballot_sync(FULL, inq && c >= 4);
             // codes of positions i0 .. i, newest in the low bits
             uint64_t x = (uint64_t)(c & 3u);
 #pragma unroll
@@ -544,72 +574,196 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
                 code = fwd < r ? fwd : r;
             }
             const unsigned strm = __ballot_sync(FULL, strand);
-            hs[lane] = splitmix64(code) >> 8;
+            // first base of each lane's N-free run; the k-mer ending here is valid when k bases of it precede
+            const unsigned bl = badm & le;
+            const uint32_t rb = bl ? i0 + (uint32_t)(32 - __clz(bl)) : run_base;
+            const bool kv = inq && c < 4 && i + 1 >= rb + k;
+            const uint32_t pos = i + 1 - k;
+            const uint64_t h = splitmix64(code) >> 8;
+            if (kv) hist[pos & HM] = h;
+            run_base = __shfl_sync(FULL, rb, 31);
             __syncwarp();
-            int ne = 0;
-            unsigned esm = 0;  // strand bit of each emission
-            if (lane == 0) {
-                const uint32_t lim = min(32u, n - i0);
-                for (uint32_t l = 0; l < lim; ++l) {
-                    if (badm >> l & 1u) {
-                        valid = 0, head = size = 0, has_last = false;
-                        continue;
+            // length of the run of strict hash increases ending at each k-mer
+            const bool inc = kv && pos > rb && hist[(pos - 1) & HM] < h;
+            const unsigned z = ~__ballot_sync(FULL, inc) & le;
+            const uint32_t rl = z ? (uint32_t)lane - (31u - (uint32_t)__clz(z)) : runlen + (uint32_t)lane + 1u;
+            runlen = __shfl_sync(FULL, rl, 31);
+            uint32_t start = 0;
+            if (!exact) {
+                const unsigned ovm = __ballot_sync(FULL, kv && rl >= win);  // the push finds the ring full
+                const int L = ovm ? __ffs(ovm) - 1 : 32;
+                const bool act = lane < L && kv && pos + 1 >= win;
+                uint64_t hm = ~0ULL;
+                uint32_t m = 0;
+                bool fp = false;
+                if (act) {
+                    const uint32_t lo = max(rb, pos + 1 - win);
+                    for (uint32_t j = lo; j <= pos; ++j) {
+                        const uint64_t y = hist[j & HM];
+                        if (y <= hm) hm = y, m = j;
                     }
-                    if (valid < (uint32_t)k) ++valid;
-                    if (valid < (uint32_t)k) continue;
-                    const uint32_t pos = i0 + l + 1 - (uint32_t)k;
-                    const uint64_t h = hs[l];
-                    while (size) {
-                        uint32_t bi = head + size - 1;
-                        if (bi >= win) bi -= win;
-                        if (rh[min(bi, last_slot)] >= h) --size;
-                        else break;
+                    fp = pos >= rb + win && hist[(pos - win) & HM] < hm;  // k-mer pos - win leaves at the front
+                }
+                uint32_t mp = __shfl_up_sync(FULL, m, 1);
+                if (lane == 0) mp = m_prev;
+                const bool em = act && (!(pos > rb && pos >= win) || m != mp);
+                m_prev = __shfl_sync(FULL, m, 31);
+                unsigned fpm = __ballot_sync(FULL, fp);
+                const unsigned bm = badm & (L >= 32 ? FULL : (1u << L) - 1u);
+                if (bm) {  // an N cleared the ring: count the front pops after the last one
+                    const int bn = 31 - __clz(bm);
+                    head = 0;
+                    fpm &= bn == 31 ? 0u : ~((2u << bn) - 1u);
+                }
+                head = (head + (uint32_t)__popc(fpm)) % win;
+                const unsigned emm = __ballot_sync(FULL, em);
+                if (emm) {
+                    if (so.mode == 0) {
+                        const uint32_t ent = em ? index_find(ix, hm) : kEmptyKey;
+                        const bool hit = ent != kEmptyKey;
+                        const unsigned mm = __ballot_sync(FULL, hit);
+                        if (hit) {
+                            const int r = n_match + __popc(mm & lt);
+                            b.hit_pos[hb + r] = m;
+                            b.hit_ent[hb + r] = ent;
+                        }
+                        n_match += __popc(mm);
+                    } else if (em) {
+                        const int r = n_hits + __popc(emm & lt);
+                        so.hx[hb + r] = (hm << 8) | (uint64_t)(uint8_t)k;
+                        so.hy[hb + r] = ((uint64_t)(strand ? 0x80000000u : 0u) << 32) | (uint64_t)m;
                     }
-                    {
-                        uint32_t bi = head + size;
-                        if (bi >= win) bi -= win;
-                        bi = min(bi, last_slot);
-                        rh[bi] = h, rp[bi] = pos;
-                        ++size;
+                    n_hits += __popc(emm);
+                }
+                if (L < 32) {  // rebuild the full ring before the push of k-mer P
+                    const uint32_t P = i0 + (uint32_t)L + 1 - k;
+                    for (uint32_t t = (uint32_t)lane; t < win; t += 32) {
+                        uint32_t s = head + t;
+                        if (s >= win) s -= win;
+                        rh[s] = hist[(P - win + t) & HM];
+                        rp[s] = P - win + t;
                     }
-                    if (pos + 1 < win) continue;
-                    const uint32_t ws = pos + 1 - win;
-                    while (size && rp[head] < ws) head = head + 1 >= win ? head + 1 - win : head + 1, --size;
-                    if (size) {
-                        const uint64_t ch = rh[head];
-                        const uint32_t cp = rp[head];
-                        if (!has_last || ch != last_h || cp != last_p) {
-                            eh[ne] = ch, ep[ne] = cp;
-                            esm |= (strm >> l & 1u) << ne;
-                            ++ne;
-                            last_h = ch, last_p = cp, has_last = true;
+                    size = win, valid = k, has_last = true;
+                    last_h = hist[(P - win) & HM], last_p = P - win;
+                    exact = true, start = (uint32_t)L;
+                    __syncwarp();
+                }
+            }
+            if (exact) {
+                int ne = 0;
+                unsigned esm = 0;  // strand bit of each emission
+                if (lane == 0) {
+                    const uint32_t lim = min(32u, n - i0);
+                    for (uint32_t l = start; l < lim; ++l) {
+                        if (badm >> l & 1u) {
+                            valid = 0, head = size = 0, has_last = false;
+                            continue;
+                        }
+                        if (valid < k) ++valid;
+                        if (valid < k) continue;
+                        const uint32_t p = i0 + l + 1 - k;
+                        const uint64_t hh = hist[p & HM];
+                        while (size) {
+                            uint32_t bi = head + size - 1;
+                            if (bi >= win) bi -= win;
+                            if (rh[min(bi, last_slot)] >= hh) --size;
+                            else break;
+                        }
+                        {
+                            uint32_t bi = head + size;
+                            if (bi >= win) bi -= win;
+                            bi = min(bi, last_slot);
+                            rh[bi] = hh, rp[bi] = p;
+                            ++size;
+                        }
+                        if (p + 1 < win) continue;
+                        const uint32_t ws = p + 1 - win;
+                        while (size && rp[head] < ws) head = head + 1 >= win ? head + 1 - win : head + 1, --size;
+                        if (size) {
+                            const uint64_t ch = rh[head];
+                            const uint32_t cp = rp[head];
+                            if (!has_last || ch != last_h || cp != last_p) {
+                                eh[ne] = ch, ep[ne] = cp;
+                                esm |= (strm >> l & 1u) << ne;
+                                ++ne;
+                                last_h = ch, last_p = cp, has_last = true;
+                            }
                         }
                     }
                 }
-            }
-            ne = __shfl_sync(FULL, ne, 0);
-            esm = __shfl_sync(FULL, esm, 0);
-            __syncwarp();
-            if (ne) {
-                const bool act = lane < ne;
-                const uint64_t ch = act ? eh[lane] : 0;
-                const uint32_t cp = act ? ep[lane] : 0;
-                if (so.mode == 0) {
-                    const uint32_t ent = act ? index_find(ix, ch) : kEmptyKey;
-                    const bool hit = act && ent != kEmptyKey;
-                    const unsigned mm = __ballot_sync(FULL, hit);
-                    if (hit) {
-                        const int r = n_match + __popc(mm & ((1u << lane) - 1u));
-                        b.hit_pos[hb + r] = cp;
-                        b.hit_ent[hb + r] = ent;
+                ne = __shfl_sync(FULL, ne, 0);
+                esm = __shfl_sync(FULL, esm, 0);
+                head = __shfl_sync(FULL, head, 0);
+                size = __shfl_sync(FULL, size, 0);
+                valid = __shfl_sync(FULL, valid, 0);
+                has_last = __shfl_sync(FULL, (int)has_last, 0) != 0;
+                last_h = __shfl_sync(FULL, last_h, 0);
+                last_p = __shfl_sync(FULL, last_p, 0);
+                __syncwarp();
+                if (ne) {
+                    const bool act = lane < ne;
+                    const uint64_t ch = act ? eh[lane] : 0;
+                    const uint32_t cp = act ? ep[lane] : 0;
+                    if (so.mode == 0) {
+                        const uint32_t ent = act ? index_find(ix, ch) : kEmptyKey;
+                        const bool hit = act && ent != kEmptyKey;
+                        const unsigned mm = __ballot_sync(FULL, hit);
+                        if (hit) {
+                            const int r = n_match + __popc(mm & lt);
+                            b.hit_pos[hb + r] = cp;
+                            b.hit_ent[hb + r] = ent;
+                        }
+                        n_match += __popc(mm);
+                    } else if (act) {
+                        so.hx[hb + n_hits + lane] = (ch << 8) | (uint64_t)(uint8_t)k;
+                        so.hy[hb + n_hits + lane] =
+                            ((uint64_t)((esm >> lane & 1u) ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
                     }
-                    n_match += __popc(mm);
-                } else if (act) {
-                    so.hx[hb + n_hits + lane] = (ch << 8) | (uint64_t)(uint8_t)k;
-                    so.hy[hb + n_hits + lane] =
-                        ((uint64_t)((esm >> lane & 1u) ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
+                    n_hits += ne;
                 }
-                n_hits += ne;
+                // back to the ideal mode once the ring holds the ideal deque of the step's last k-mer
+                if (i0 + 32 < n && __shfl_sync(FULL, (int)(kv && pos + 1 >= win), 31)) {
+                    const uint32_t hp = i0 + 32 - k;
+                    uint32_t tot = 0;
+                    uint64_t cmin = ~0ULL;  // minimum hash after the current group's k-mers
+                    for (int pass = 0; pass < 2; ++pass) {
+                        uint32_t before = 0;
+                        bool bad = false;
+                        cmin = ~0ULL;
+                        for (uint32_t g = 0; g < win; g += 32) {
+                            const uint32_t t = g + (uint32_t)lane;  // k-mer hp - t
+                            const bool in = t < win && hp >= run_base + t;
+                            const uint64_t y = in ? hist[(hp - t) & HM] : ~0ULL;
+                            uint64_t pm = y;
+#pragma unroll
+                            for (int d = 1; d < 32; d <<= 1) {
+                                const uint64_t o = __shfl_up_sync(FULL, pm, d);
+                                if (lane >= d && o < pm) pm = o;
+                            }
+                            uint64_t ex = __shfl_up_sync(FULL, pm, 1);
+                            if (lane == 0) ex = ~0ULL;
+                            if (cmin < ex) ex = cmin;
+                            const bool f = in && y < ex;  // a suffix minimum: in the ideal deque
+                            const unsigned fm = __ballot_sync(FULL, f);
+                            if (pass == 1 && f) {
+                                const uint32_t r = tot - (before + (uint32_t)__popc(fm & le));  // deque index
+                                uint32_t s = head + r;
+                                if (s >= win) s -= win;
+                                if (rp[min(s, last_slot)] != hp - t) bad = true;
+                            }
+                            before += (uint32_t)__popc(fm);
+                            const uint64_t gm = __shfl_sync(FULL, pm, 31);
+                            if (gm < cmin) cmin = gm;
+                        }
+                        if (pass == 0) {
+                            tot = before;
+                            if (tot != size) break;
+                        } else if (!__any_sync(FULL, bad)) {
+                            exact = false;
+                            m_prev = last_p;
+                        }
+                    }
+                }
             }
             __syncwarp();
         }
@@ -619,7 +773,6 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
         }
     }
 }
-
 }  // namespace hg
 
 extern "C" cudaError_t hg_launch_seed(const hg::IndexDev* ix, const hg::BatchDev* b, int mode, uint64_t* hx,

@@ -332,6 +332,41 @@ def test_batch_window_overflow_vs_oracle(gpu, oracle, pkg):
         assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
 
 
+def test_minimizer_replay_many_overflows_vs_oracle(gpu, oracle, pkg):
+    """Several deque overflows per query, some a few k-mers apart (inside one
+    32-base step of the replay, or before the ring is back to the ideal
+    deque), with N runs between them: the replay's switches between its
+    ideal and exact modes, through the single-call extraction and through
+    the batched path's CIGARs."""
+    from tests.test_oracle_pin import increasing_run
+    rng = np.random.default_rng(52)
+    center = pkg.synth.random_center(6000, 21)
+    cmx, cmy = oracle.extract_minimizer(center)
+    cases = []
+    for it, (k, w) in enumerate([(15, 10), (15, 10), (15, 11), (11, 3), (21, 2), (15, 1), (13, 5), (15, 10)]):
+        parts = [center[int(rng.integers(0, 3000)):][:int(rng.integers(0, 400))]]
+        for r in range(int(rng.integers(2, 6))):
+            run = increasing_run(rng, k, w + int(rng.integers(0, 3)))
+            assert run is not None
+            parts.append(run[-int(rng.integers(w + 20, 80)):].encode())
+            if rng.random() < 0.3:
+                parts.append(b"N" * int(rng.integers(1, 30)))
+            parts.append(np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, int(rng.integers(0, 90)))].tobytes())
+        s = b"".join(parts)
+        ox, oy = oracle.extract_minimizer(s, k, w, True)
+        gx, gy = gpu.extract_minimizer(s, k, w, True)
+        assert np.array_equal(ox, gx) and np.array_equal(oy, gy), (it, k, w, len(s))
+        if k == 15 and w == 10:
+            cases.append(s)
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=16, max_bases=len(seqs) + 1024)
+    res = ctx.align(gpu.pack(seqs, offs), rows=False, check=False)
+    for i, q in enumerate(cases):
+        assert np.array_equal(res.cigar_of(i), oracle.align_query(center, cmx, cmy, q)), i
+
+
 def test_global_align_mm2_vs_oracle(gpu, oracle, pkg):
     """The single-call globalAlignMM2 with caller anchors (the anchors
     collect_anchors makes for each query, shuffled: the call sorts them as
