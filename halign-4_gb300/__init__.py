@@ -38,8 +38,9 @@ HG_ERR_CAPACITY = 4
 ST_ARENA_OVERFLOW, ST_PARTIAL_CIGAR, ST_CIGAR_OVERFLOW, ST_LENGTH_MISMATCH = 0x01, 0x02, 0x08, 0x10
 # hg_ctx_set_launch order: CTAs per SM of six stages, then two DP tier boundaries
 LAUNCH_KNOBS = ("seed", "anchor", "chain", "dp_small", "stitch", "rows", "thin_max_inner", "square_max_cells",
-                "small_pair", "lanes")
-LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32), (0, 32), (0, 12288), (0, 1), (1, 2))
+                "small_pair", "lanes", "tail_share")
+LAUNCH_BOUNDS = ((1, 32), (1, 6), (1, 64), (1, 32), (1, 32), (1, 32), (0, 32), (0, 12288), (0, 1), (1, 2), (0, 24))
+DEVICE_KNOBS = 10  # the leading knobs a staged (device-resident) run depends on; tail_share is the host path's
 STAGES = ("seed", "anchor", "chain", "dp_small", "dp_large", "stitch", "rows", "count")
 
 
@@ -104,6 +105,7 @@ def lib() -> C.CDLL:
     batch_args = [vp, vp, vp, vp, vp, vp, i64, vp, i64, vp, vp, vp, i64, vp]
     L.hg_align_batch.argtypes = batch_args
     L.hg_align_plain.argtypes = batch_args
+    L.hg_align_ascii.argtypes = [vp, vp, vp, i64, vp, i64, vp, vp, vp, i64, vp]
     L.hg_stage.argtypes = [vp, vp, vp, vp, vp, vp, i64]
     L.hg_run_staged.argtypes = [vp]
     L.hg_fetch_staged.argtypes = [vp, vp, i64, vp, vp, vp, i64, vp]
@@ -350,6 +352,23 @@ class Context:
         if check or code not in (HG_OK, HG_ERR_LENGTH_MISMATCH):
             _check(code)
         return self._result(cig, off, has_ins, status, rbuf, b.n)
+
+    def align_ascii(self, seqs, offsets, rows: bool = True, check: bool = True) -> AlignResult:
+        """hg_align_ascii: ASCII queries (query i = seqs[offsets[i]:offsets[i+1]])
+        uploaded per sub-batch and packed on the device."""
+        s = np.frombuffer(seqs, np.uint8) if isinstance(seqs, (bytes, bytearray)) else np.ascontiguousarray(seqs, np.uint8)
+        offs = np.ascontiguousarray(offsets, np.int64)
+        n = len(offs) - 1
+        bases = int(offs[-1] - offs[0]) if n > 0 else 0
+        for worst in (False, True):
+            cig, off, has_ins, status, rbuf, stride = self._outputs(n, bases, rows, worst)
+            code = lib().hg_align_ascii(self.h, _p(s), _p(offs), n, _p(cig), len(cig), _p(off), _p(has_ins),
+                                        _p(rbuf), stride if rows else 0, _p(status))
+            if code != 4:  # HG_ERR_CAPACITY: retry once with the worst-case buffer
+                break
+        if check or code not in (HG_OK, HG_ERR_LENGTH_MISMATCH):
+            _check(code)
+        return self._result(cig, off, has_ins, status, rbuf, n)
 
     # device-resident form
     def stage(self, b: Packed):

@@ -44,6 +44,8 @@ cudaError_t hg_launch_status_or(const uint32_t*, int, uint32_t*, const unsigned 
                                 unsigned long long*, cudaStream_t);
 size_t hg_ksw_scratch_bytes(int, int, int, int);
 cudaError_t hg_prepare_kernels(void);
+cudaError_t hg_launch_ascii_pack(const uint8_t*, const int64_t*, int, const int64_t*, uint8_t*, int32_t*, int64_t*,
+                                 int32_t*, int64_t, int32_t*, int, cudaStream_t);
 cudaError_t hg_launch_ksw_single(int, const uint8_t*, int, const uint8_t*, int, const int8_t*, int, int, int, int,
                                  int, int, uint8_t*, uint32_t*, int, void*, cudaStream_t);
 }
@@ -119,7 +121,7 @@ struct hg_ctx {
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
     cudaStream_t st3 = nullptr;                            // side stream of the one-warp wavefront and exact tiers
     // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
-    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells, 0, 2};
+    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells, 0, 2, 10};
     // second compute lane: a context of the same capacity on its own streams
     // that runs every other sub-batch of a multi-sub-batch run (knob 9 = 2)
     hg_ctx* peer = nullptr;
@@ -165,7 +167,7 @@ struct hg_ctx {
     DevBuf<uint8_t> has_ins;
     DevBuf<uint8_t> rows, rows2;                         // rows2: second buffer while rows of the previous sub-batch copy out
     cudaStream_t cst = nullptr;                          // copy stream for row read-back
-    cudaEvent_t rows_ev[2] = {nullptr, nullptr}, comp_ev = nullptr;
+    cudaEvent_t rows_ev[4] = {nullptr, nullptr, nullptr, nullptr}, comp_ev = nullptr;  // one per row buffer
     DevBuf<uint32_t> counts, ins, status;
     // control block: queues[8], cursors (a, s, dp), n_small, n_large
     DevBuf<unsigned long long> control;
@@ -183,13 +185,19 @@ struct hg_ctx {
         DevBuf<int64_t> poff, exc_off, hoff, coff;
         DevBuf<int32_t> qlen, exc, order;
         DevBuf<uint32_t> compact;
+        // ASCII input (hg_align_ascii): the sub-batch's bytes and offsets,
+        // run counts, the exception-capacity flag and its pinned copy
+        DevBuf<uint8_t> ascii;
+        DevBuf<int64_t> aoff;
+        DevBuf<int32_t> nrun, excflag;
+        int32_t* h_excflag = nullptr;
         int64_t* h_off = nullptr;
         uint32_t* h_status = nullptr;
         uint8_t* h_ins = nullptr;
         cudaEvent_t in_ready = nullptr, in_free = nullptr, off_ev = nullptr, done = nullptr, cfree = nullptr;
-    } pipe[2];
+    } pipe[4];  // slot 0's device inputs are the context's own
     cudaStream_t ist = nullptr;
-    bool pipe_ready = false;
+    int pipe_slots = 0;  // slots set up
     // staged full batch (device-resident form)
     std::vector<SubPlan> staged_plan;
     std::vector<int32_t> staged_qlen;
@@ -717,6 +725,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
         (e = cudaStreamCreateWithFlags(&c->cst, cudaStreamNonBlocking)) ||
         (e = cudaEventCreateWithFlags(&c->rows_ev[0], cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&c->rows_ev[1], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&c->rows_ev[2], cudaEventDisableTiming)) ||
+        (e = cudaEventCreateWithFlags(&c->rows_ev[3], cudaEventDisableTiming)) ||
         (e = cudaEventCreateWithFlags(&c->comp_ev, cudaEventDisableTiming)) ||
         (e = c->packed.alloc(max_bases / 4 + 16 * max_queries + 64)) || (e = c->poff.alloc(max_queries)) ||
         (e = c->exc_off.alloc(max_queries + 1)) || (e = c->hoff.alloc(max_queries)) ||
@@ -768,8 +778,8 @@ extern "C" int hg_ctx_create(hg_index_t* ix, int64_t max_queries, int64_t max_ba
 // per-CTA scratch slice in range.  Cached graphs are dropped.
 extern "C" int hg_ctx_set_launch(hg_ctx_t* c, const int32_t* ctas_per_sm, int n)
 {
-    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1, 0, 0, 0, 1};
-    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32, hg::kThinMaxInner, hg::kSquareMaxCells, 1, 2};
+    static const int32_t lo[HG_LAUNCH_KNOBS] = {1, 1, 1, 1, 1, 1, 0, 0, 0, 1, 0};
+    static const int32_t hi[HG_LAUNCH_KNOBS] = {32, 6, 64, 32, 32, 32, hg::kThinMaxInner, hg::kSquareMaxCells, 1, 2, 24};
     if (!c || !ctas_per_sm || n < 0 || n > HG_LAUNCH_KNOBS) return fail(HG_ERR_ARG, "hg_ctx_set_launch: bad arguments");
     for (int i = 0; i < n; ++i)
         if (ctas_per_sm[i] < lo[i] || ctas_per_sm[i] > hi[i])
@@ -813,6 +823,7 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
         if (ps.h_off) cudaFreeHost(ps.h_off);
         if (ps.h_status) cudaFreeHost(ps.h_status);
         if (ps.h_ins) cudaFreeHost(ps.h_ins);
+        if (ps.h_excflag) cudaFreeHost(ps.h_excflag);
         for (cudaEvent_t e : {ps.in_ready, ps.in_free, ps.off_ev, ps.done, ps.cfree})
             if (e) cudaEventDestroy(e);
     }
@@ -843,7 +854,8 @@ std::vector<SubPlan> plan(hg_ctx_t* c, const int64_t* poff, const int32_t* qlen,
     while (i < n) {
         SubPlan p{i, 0, 0, 0, 0};
         while (i < n) {
-            const int64_t b = qlen[i], by = (int64_t)padded_bytes(qlen[i]), ex = exc_off[i + 1] - exc_off[i];
+            const int64_t b = qlen[i], by = (int64_t)padded_bytes(qlen[i]);
+            const int64_t ex = exc_off ? exc_off[i + 1] - exc_off[i] : 0;  // ASCII input: checked on the device
             if (p.n > 0 && (p.n + 1 > c->max_n || p.bases + b > c->max_bases ||
                             p.bytes + by > (int64_t)c->packed.n || p.excs + ex > c->exc_cap))
                 break;
@@ -853,6 +865,62 @@ std::vector<SubPlan> plan(hg_ctx_t* c, const int64_t* poff, const int32_t* qlen,
     }
     (void)poff;
     return out;
+}
+
+// Host-buffer calls: the first sub-batch's inputs upload before anything
+// computes, and the last sub-batches' outputs (the rows above all) copy out
+// after everything has.  With s = launch knob 10 (0 = off) and at least
+// 32 MB to move, the edges are re-cut into small parts: the first two
+// sub-batches' queries into parts of s, s, 50 - s and 50 - s percent of
+// their bases, the last two into 50 - s, 50 - s, s and s percent (with
+// three sub-batches or fewer, all queries into s, s, 50 - 2s, 50 - 2s, s
+// and s percent).  The two lanes then start after a small upload each, and
+// the large parts' outputs copy out while the small last parts compute.  A
+// cut that would exceed the context's capacity keeps the sub-batches.
+std::vector<SubPlan> edge_split(hg_ctx_t* c, const std::vector<SubPlan>& plans, const int32_t* qlen,
+                                const int64_t* exc_off, bool rows, bool ascii)
+{
+    const size_t K = plans.size();
+    const int64_t s = c->launch[10];
+    if (K == 0 || s <= 0) return plans;
+    const int64_t n = plans[K - 1].first + plans[K - 1].n - plans[0].first;
+    int64_t bases = 0;
+    for (const SubPlan& p : plans) bases += p.bases;
+    const int64_t moved = (rows ? n * c->row_stride : 0) + (ascii ? bases : bases / 4);
+    if (n < 16 || moved < (32LL << 20)) return plans;
+    bool ok = true;
+    // queries [f, e) cut at the given cumulative percentages of their bases
+    auto recut = [&](int64_t f, int64_t e, std::initializer_list<int64_t> pct, std::vector<SubPlan>& out) {
+        int64_t B = 0;
+        for (int64_t i = f; i < e; ++i) B += qlen[i];
+        int64_t i = f, acc = 0, cum = 0;
+        const size_t np = pct.size();
+        size_t part = 0;
+        for (int64_t p_pct : pct) {
+            cum += p_pct;
+            const int64_t lim = B * cum / 100;
+            const bool last = ++part == np;
+            SubPlan p{i, 0, 0, 0, 0};
+            while (i < e && (p.n == 0 || last || acc + qlen[i] <= lim)) {
+                const int64_t by = (int64_t)padded_bytes(qlen[i]), ex = exc_off ? exc_off[i + 1] - exc_off[i] : 0;
+                p.n++, p.bases += qlen[i], p.bytes += by, p.excs += ex, acc += qlen[i], ++i;
+            }
+            if (!p.n) continue;
+            if (p.n > c->max_n || p.bases > c->max_bases || p.bytes > (int64_t)c->packed.n || p.excs > c->exc_cap)
+                ok = false;
+            out.push_back(p);
+        }
+    };
+    std::vector<SubPlan> out;
+    auto end_of = [&](size_t k) { return plans[k].first + plans[k].n; };
+    if (K <= 3) {
+        recut(plans[0].first, end_of(K - 1), {s, s, 50 - 2 * s, 50 - 2 * s, s, s}, out);
+    } else {
+        recut(plans[0].first, end_of(1), {s, s, 50 - s, 50 - s}, out);
+        out.insert(out.end(), plans.begin() + 2, plans.end() - 2);
+        recut(plans[K - 2].first, end_of(K - 1), {50 - s, 50 - s, s, s}, out);
+    }
+    return ok ? out : plans;
 }
 
 hg::BatchDev batch_view(hg_ctx_t* c, int n, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
@@ -1114,30 +1182,56 @@ InView in_view(hg_ctx_t* c, int slot)
     if (slot == 0)
         return {c->packed.p, c->poff.p, c->exc_off.p, c->hoff.p, c->coff.p, c->qlen.p, c->exc.p, c->order.p,
                 c->cig_compact.p, c->cig_compact.n};
-    auto& q = c->pipe[1];
+    auto& q = c->pipe[slot];
     return {q.packed.p, q.poff.p, q.exc_off.p, q.hoff.p, q.coff.p, q.qlen.p, q.exc.p, q.order.p, q.compact.p, q.compact.n};
 }
 
-int pipe_setup(hg_ctx_t* c)
+// Input slots 0 .. want-1 (2 or 4), set up on first use: device inputs
+// (slot 0 uses the context's own), pinned read-back staging and events.
+// Returns the slots available: 4 only when their memory could be had.
+int pipe_setup(hg_ctx_t* c, int want, int* have)
 {
-    if (c->pipe_ready) return HG_OK;
     const size_t M = (size_t)c->max_n;
-    auto& q = c->pipe[1];
     cudaError_t e;
-    if ((e = q.packed.alloc(c->packed.n)) || (e = q.poff.alloc(M)) || (e = q.exc_off.alloc(M + 1)) ||
-        (e = q.hoff.alloc(M)) || (e = q.coff.alloc(M)) || (e = q.qlen.alloc(M)) || (e = q.exc.alloc(c->exc.n)) ||
-        (e = q.order.alloc(M)) || (e = q.compact.alloc(c->cig_compact.n)) ||
-        (e = cudaStreamCreateWithFlags(&c->ist, cudaStreamNonBlocking)))
-        return cuda_fail(e, "hg_align_batch: pipeline buffers");
-    for (auto& ps : c->pipe) {
-        if ((e = cudaHostAlloc(&ps.h_off, 8 * (M + 1), cudaHostAllocDefault)) ||
-            (e = cudaHostAlloc(&ps.h_status, 4 * M, cudaHostAllocDefault)) ||
-            (e = cudaHostAlloc(&ps.h_ins, M, cudaHostAllocDefault)))
+    if (!c->ist && (e = cudaStreamCreateWithFlags(&c->ist, cudaStreamNonBlocking)))
+        return cuda_fail(e, "hg_align_batch: input stream");
+    for (int s = c->pipe_slots; s < want; ++s) {
+        auto& q = c->pipe[s];
+        if (s > 0 && ((e = q.packed.alloc(c->packed.n)) || (e = q.poff.alloc(M)) || (e = q.exc_off.alloc(M + 1)) ||
+                      (e = q.hoff.alloc(M)) || (e = q.coff.alloc(M)) || (e = q.qlen.alloc(M)) ||
+                      (e = q.exc.alloc(c->exc.n)) || (e = q.order.alloc(M)) || (e = q.compact.alloc(c->cig_compact.n)))) {
+            q.packed.free(), q.poff.free(), q.exc_off.free(), q.hoff.free(), q.coff.free(), q.qlen.free();
+            q.exc.free(), q.order.free(), q.compact.free();
+            cudaGetLastError();
+            if (s >= 2) break;  // two slots are enough to run
+            return cuda_fail(e, "hg_align_batch: pipeline buffers");
+        }
+        if ((e = cudaHostAlloc(&q.h_off, 8 * (M + 1), cudaHostAllocDefault)) ||
+            (e = cudaHostAlloc(&q.h_status, 4 * M, cudaHostAllocDefault)) ||
+            (e = cudaHostAlloc(&q.h_ins, M, cudaHostAllocDefault)))
             return cuda_fail(e, "hg_align_batch: pinned pipeline staging");
-        for (cudaEvent_t* ev : {&ps.in_ready, &ps.in_free, &ps.off_ev, &ps.done, &ps.cfree})
+        for (cudaEvent_t* ev : {&q.in_ready, &q.in_free, &q.off_ev, &q.done, &q.cfree})
             if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming))) return cuda_fail(e, "hg_align_batch: events");
+        c->pipe_slots = s + 1;
     }
-    c->pipe_ready = true;
+    *have = std::min(want, c->pipe_slots);
+    return HG_OK;
+}
+
+// Buffers of the ASCII input form, per pipeline slot (allocated on first use).
+int ascii_setup(hg_ctx_t* c, int slots)
+{
+    const size_t M = (size_t)c->max_n;
+    for (int s = 0; s < slots; ++s) {
+        auto& ps = c->pipe[s];
+        if (ps.ascii.p) continue;
+        cudaError_t e;
+        if ((e = ps.ascii.alloc((size_t)c->max_bases + 16)) || (e = ps.aoff.alloc(M + 1)) || (e = ps.nrun.alloc(M)) ||
+            (e = ps.excflag.alloc(1)) || (e = cudaHostAlloc(&ps.h_excflag, 4, cudaHostAllocDefault))) {
+            ps.ascii.free();
+            return cuda_fail(e, "hg_align_ascii: input buffers");
+        }
+    }
     return HG_OK;
 }
 
@@ -1152,29 +1246,50 @@ int pipe_setup(hg_ctx_t* c)
 int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_t* packed, const int64_t* poff,
                     const int32_t* qlen, const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar,
                     int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows, int64_t row_stride,
-                    uint32_t* status)
+                    uint32_t* status, const uint8_t* ascii = nullptr, const int64_t* aoffs = nullptr)
 {
-    int r = pipe_setup(c);
-    if (r) return r;
-    if (rows && !c->rows2.p) HG_CUDA(c->rows2.alloc((size_t)c->max_n * c->row_stride));
     const int K = (int)plans.size();
-    std::vector<int32_t> order[2];
-    std::vector<int64_t> hoff[2], coff[2], spoff[2], seoff[2];
+    // lanes: with two, the odd sub-batches compute on the second lane's
+    // arenas and streams; four input slots (two per lane) let a lane's next
+    // inputs upload while it computes
+    hg_ctx_t* P = K > 1 ? lane_peer(c) : nullptr;
+    int NS = 2;
+    int r = pipe_setup(c, P && K > 2 ? 4 : 2, &NS);
+    if (r) return r;
+    if (NS != 4) NS = 2;
+    if (ascii && (r = ascii_setup(c, NS))) return r;
+    auto slot_of = [&](int k) { return k % NS; };
+    if (rows && !c->rows2.p) HG_CUDA(c->rows2.alloc((size_t)c->max_n * c->row_stride));
+    std::vector<int32_t> order[4];
+    std::vector<int64_t> hoff[4], coff[4], spoff[4], seoff[4];
     for (const SubPlan& sp : plans)
         if (sp.n > c->max_n || sp.bases > c->max_bases)
             return fail(HG_ERR_CAPACITY, "query " + std::to_string(sp.first) + " exceeds the context capacity");
     auto issue_inputs = [&](int k) -> int {
         const SubPlan& sp = plans[(size_t)k];
-        const int slot = k & 1;
+        const int slot = slot_of(k);
         const InView V = in_view(c, slot);
         const int64_t f = sp.first, m = sp.n;
         sub_arrays(c, qlen + f, m, order[slot], hoff[slot], coff[slot]);
         spoff[slot].resize((size_t)m), seoff[slot].resize((size_t)m + 1);
         int64_t pb = 0;
         for (int64_t i = 0; i < m; ++i) spoff[slot][i] = pb, pb += (int64_t)padded_bytes(qlen[f + i]);
-        for (int64_t i = 0; i <= m; ++i) seoff[slot][i] = exc_off[f + i] - exc_off[f];
         cudaStream_t is = c->ist;
-        HG_CUDA(cudaStreamWaitEvent(is, c->pipe[slot].in_free, 0));  // sub-batch k-2 is done with the slot
+        HG_CUDA(cudaStreamWaitEvent(is, c->pipe[slot].in_free, 0));  // sub-batch k-NS is done with the slot
+        if (ascii) {  // the bytes as they are; the compute stream packs them
+            auto& PS = c->pipe[slot];
+            HG_CUDA(cudaMemcpyAsync(PS.ascii.p, ascii + aoffs[f], (size_t)(aoffs[f + m] - aoffs[f]),
+                                    cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(PS.aoff.p, aoffs + f, 8 * ((size_t)m + 1), cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(V.poff, spoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(V.qlen, qlen + f, 4 * (size_t)m, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(V.order, order[slot].data(), 4 * (size_t)m, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(V.hoff, hoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(V.coff, coff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaEventRecord(PS.in_ready, is));
+            return HG_OK;
+        }
+        for (int64_t i = 0; i <= m; ++i) seoff[slot][i] = exc_off[f + i] - exc_off[f];
         bool contiguous = true;
         for (int64_t i = 1; i < m && contiguous; ++i) contiguous = poff[f + i] == poff[f] + spoff[slot][i];
         if (contiguous) {
@@ -1195,17 +1310,28 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         HG_CUDA(cudaEventRecord(c->pipe[slot].in_ready, is));
         return HG_OK;
     };
-    // lanes: with two, the odd sub-batches compute on the second lane's
-    // arenas and streams, and sub-batch k+1 is enqueued before k's offsets are
-    // read (its lane's scratch is not reused before that read)
-    hg_ctx_t* P = K > 1 ? lane_peer(c) : nullptr;
     auto lane_of = [&](int k) -> hg_ctx_t* { return (P && (k & 1)) ? P : c; };
+    // row buffers: with two lanes each lane alternates between two of them
+    // when it runs more than one sub-batch, so no sub-batch waits for the
+    // read-back of the one before it on its lane
+    bool rows4 = false;
+    if (rows && P && K > 2) {
+        if (!P->rows2.p && P->rows2.alloc((size_t)P->max_n * P->row_stride) != cudaSuccess) {
+            P->rows2.p = nullptr, P->rows2.n = 0;
+            cudaGetLastError();
+        }
+        rows4 = P->rows2.p != nullptr;
+    }
+    auto rbuf_of = [&](int k) -> int { return P ? ((k & 1) | (rows4 ? (k & 2) : 0)) : (k & 1); };
     auto rows_of = [&](int k) -> uint8_t* {
-        return (k & 1) ? (P ? P->rows.p : c->rows2.p) : c->rows.p;
+        const int r = rbuf_of(k);
+        if (!P) return r ? c->rows2.p : c->rows.p;
+        hg_ctx_t* L = (r & 1) ? P : c;
+        return (r & 2) ? L->rows2.p : L->rows.p;
     };
     auto enqueue_compute = [&](int k) -> int {
         const SubPlan& sp = plans[(size_t)k];
-        const int slot = k & 1;
+        const int slot = slot_of(k);
         auto& PS = c->pipe[slot];
         const InView V = in_view(c, slot);
         hg_ctx_t* L = lane_of(k);
@@ -1213,7 +1339,10 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         uint8_t* rbuf = rows_of(k);
         cudaStream_t st = L->st;
         HG_CUDA(cudaStreamWaitEvent(st, PS.in_ready, 0));
-        if (rows) HG_CUDA(cudaStreamWaitEvent(st, c->rows_ev[slot], 0));  // its last read-back is done
+        if (rows) HG_CUDA(cudaStreamWaitEvent(st, c->rows_ev[rbuf_of(k)], 0));  // its last read-back is done
+        if (ascii)
+            HG_CUDA(hg_launch_ascii_pack(PS.ascii.p, PS.aoff.p, (int)m, V.poff, V.packed, PS.nrun.p, V.exc_off, V.exc,
+                                         c->exc_cap, PS.excflag.p, c->sms, st));
         hg::BatchDev b = batch_view(L, (int)m, V.packed, V.poff, V.qlen, V.exc, V.exc_off, V.order, V.hoff, V.coff);
         if (rbuf) b.rows = rbuf;
         int rr = run_sub(L, b, true);
@@ -1223,6 +1352,7 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         HG_CUDA(cudaMemcpyAsync(PS.h_off, L->cig_off.p, 8 * ((size_t)m + 1), cudaMemcpyDeviceToHost, st));
         HG_CUDA(cudaMemcpyAsync(PS.h_status, L->status.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, st));
         if (has_ins) HG_CUDA(cudaMemcpyAsync(PS.h_ins, L->has_ins.p, (size_t)m, cudaMemcpyDeviceToHost, st));
+        if (ascii) HG_CUDA(cudaMemcpyAsync(PS.h_excflag, PS.excflag.p, 4, cudaMemcpyDeviceToHost, st));
         HG_CUDA(cudaEventRecord(PS.off_ev, st));
         HG_CUDA(cudaStreamWaitEvent(st, PS.cfree, 0));  // the slot's previous CIGARs have copied out
         compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(L->cig.p, V.coff, L->n_cig.p, L->cig_off.p, (int)m, V.compact,
@@ -1241,20 +1371,24 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
             else
                 HG_CUDA(cudaMemcpy2DAsync(rows + f * row_stride, (size_t)row_stride, rbuf, (size_t)c->row_stride,
                                           (size_t)c->ix->L, (size_t)m, cudaMemcpyDeviceToHost, c->cst));
-            HG_CUDA(cudaEventRecord(c->rows_ev[slot], c->cst));
+            HG_CUDA(cudaEventRecord(c->rows_ev[rbuf_of(k)], c->cst));
         }
         return HG_OK;
     };
     int64_t cig_base = 0;
     auto read_back = [&](int k) -> int {
         const SubPlan& sp = plans[(size_t)k];
-        const int slot = k & 1;
+        const int slot = slot_of(k);
         auto& PS = c->pipe[slot];
         const InView V = in_view(c, slot);
         hg_ctx_t* L = lane_of(k);
         const int64_t f = sp.first, m = sp.n;
         // the offsets decide the copy before the lane's scratch may be overwritten
         HG_CUDA(cudaEventSynchronize(PS.off_ev));
+        if (ascii && *PS.h_excflag)
+            return fail(HG_ERR_CAPACITY, "hg_align_ascii: the exception runs (bytes other than A/C/G/T) of queries " +
+                                             std::to_string(f) + ".. exceed the context's " +
+                                             std::to_string(c->exc_cap) + " per sub-batch; pack them with hg_pack");
         const int64_t total = PS.h_off[m];
         if (cig_base + total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_align_batch: cigar buffer too small");
         if (total <= (int64_t)V.compact_n) {
@@ -1280,13 +1414,36 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         cig_base += total;
         return HG_OK;
     };
-    if ((r = issue_inputs(0))) return r;
-    if (P && (r = enqueue_compute(0))) return r;
-    for (int k = 0; k < K; ++k) {
-        if (!P && (r = enqueue_compute(k))) return r;
-        if (k + 1 < K && (r = issue_inputs(k + 1))) return r;  // host work and upload overlap this compute
-        if (P && k + 1 < K && (r = enqueue_compute(k + 1))) return r;
-        if ((r = read_back(k))) return r;
+    // an error returns only after the copies already issued into the
+    // caller's buffers have finished
+    auto drain = [&](int rc) -> int {
+        cudaStreamSynchronize(c->ist);
+        if (P) cudaStreamSynchronize(P->st);
+        cudaStreamSynchronize(c->st);
+        cudaStreamSynchronize(c->cst);
+        return rc;
+    };
+    if ((r = issue_inputs(0))) return drain(r);
+    if (P) {
+        // sub-batch k+1 (the other lane) is enqueued before k's offsets are
+        // read; k+2 (this lane, the next slot) has its inputs on the way
+        // while k computes and is enqueued once k's offsets are read (the
+        // lane's scratch is not reused before that read)
+        if ((r = enqueue_compute(0)) || (r = issue_inputs(1)) || (r = enqueue_compute(1))) return drain(r);
+        for (int k = 0; k < K; ++k) {
+            if (k + 2 < K && NS == 4 && (r = issue_inputs(k + 2))) return drain(r);
+            if ((r = read_back(k))) return drain(r);
+            if (k + 2 < K) {
+                if (NS != 4 && (r = issue_inputs(k + 2))) return drain(r);
+                if ((r = enqueue_compute(k + 2))) return drain(r);
+            }
+        }
+    } else {
+        for (int k = 0; k < K; ++k) {
+            if ((r = enqueue_compute(k))) return drain(r);
+            if (k + 1 < K && (r = issue_inputs(k + 1))) return drain(r);  // host work and upload overlap this compute
+            if ((r = read_back(k))) return drain(r);
+        }
     }
     if (P) HG_CUDA(cudaStreamSynchronize(P->st));
     HG_CUDA(cudaStreamSynchronize(c->cst));
@@ -1309,7 +1466,8 @@ int align_impl(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const in
         cigar_off[0] = 0;
         return HG_OK;
     }
-    const auto plans = plan(c, poff, qlen, exc_off, n);
+    auto plans = plan(c, poff, qlen, exc_off, n);
+    if (!plain) plans = edge_split(c, plans, qlen, exc_off, rows != nullptr, false);
     if (!plain && plans.size() > 1)
         return align_pipelined(c, plans, packed, poff, qlen, exc, exc_off, n, cigar, cigar_cap, cigar_off, has_ins,
                                rows, row_stride, status);
@@ -1417,6 +1575,32 @@ extern "C" int hg_align_plain(hg_ctx_t* ctx, const uint8_t* packed, const int64_
 {
     return align_impl(ctx, packed, poff, qlen, exc, exc_off, n, cigar, cigar_cap, cigar_off, has_ins, rows,
                       row_stride, status, true);
+}
+
+extern "C" int hg_align_ascii(hg_ctx_t* c, const char* seqs, const int64_t* offsets, int64_t n, uint32_t* cigar,
+                              int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows,
+                              int64_t row_stride, uint32_t* status)
+{
+    if (!c || n < 0 || (n && (!seqs || !offsets || !cigar || !cigar_off)))
+        return fail(HG_ERR_ARG, "hg_align_ascii: bad arguments");
+    if (rows && row_stride < c->ix->L) return fail(HG_ERR_ARG, "hg_align_ascii: row_stride < center length");
+    if (n == 0) {
+        cigar_off[0] = 0;
+        return HG_OK;
+    }
+    std::vector<int32_t> qlen((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t len = offsets[i + 1] - offsets[i];
+        if (len < 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_align_ascii: bad query length");
+        qlen[(size_t)i] = (int32_t)len;
+    }
+    cudaSetDevice(c->ix->device);
+    std::vector<uint32_t> st_local;
+    if (!status) st_local.resize((size_t)n), status = st_local.data();
+    auto plans = plan(c, nullptr, qlen.data(), nullptr, n);
+    plans = edge_split(c, plans, qlen.data(), nullptr, rows != nullptr, true);
+    return align_pipelined(c, plans, nullptr, nullptr, qlen.data(), nullptr, nullptr, n, cigar, cigar_cap, cigar_off,
+                           has_ins, rows, row_stride, status, reinterpret_cast<const uint8_t*>(seqs), offsets);
 }
 
 extern "C" int hg_fetch_chain(hg_ctx_t* c, int64_t query, uint32_t* pos_ref, uint32_t* pos_qry, int32_t* f,

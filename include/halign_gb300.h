@@ -113,6 +113,20 @@ int hg_align_batch(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, co
                    const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar, int64_t cigar_cap,
                    int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows, int64_t row_stride, uint32_t* status);
 
+/* hg_align_batch on ASCII queries (query i = seqs[offsets[i] .. offsets[i+1]),
+ * the reference's std::string bytes), packed on the device: each sub-batch's
+ * bytes upload as they are while the previous one computes, and kernels pack
+ * them into hg_pack's format on the stream that aligns them, so no host pass
+ * reads the bases.  Outputs, errors and results are hg_align_batch's on
+ * hg_pack's output.  HG_ERR_CAPACITY when a sub-batch holds more exception
+ * runs (runs of one byte other than A/C/G/T) than max_bases / 16 + 4096:
+ * pack such input with hg_pack.  `seqs` in pinned memory (cudaHostAlloc)
+ * lets the uploads overlap the compute; pageable memory is staged by the
+ * driver on the calling thread. */
+int hg_align_ascii(hg_ctx_t* ctx, const char* seqs, const int64_t* offsets, int64_t n, uint32_t* cigar,
+                   int64_t cigar_cap, int64_t* cigar_off, uint8_t* has_ins, uint8_t* rows, int64_t row_stride,
+                   uint32_t* status);
+
 /* Same computation, one launch sequence per query (the plain form). */
 int hg_align_plain(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
                    const int32_t* exc, const int64_t* exc_off, int64_t n, uint32_t* cigar, int64_t cigar_cap,
@@ -140,11 +154,16 @@ int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* 
  * every other sub-batch runs on a second context of the same capacity and
  * its own streams (created on first use, so the device memory of the
  * context doubles; without room for it the context keeps one lane), and the
- * two overlap on the GPU.  Defaults 6 6 12 12 8 6 32 12288 0 2.  Setting
+ * two overlap on the GPU.  [10] host-buffer calls moving 32 MB or more
+ * (inputs + rows): the first two and the last two sub-batches are re-cut
+ * so that the first and the last two parts hold s percent (0..24; 0 = off)
+ * of their bases each: both lanes start after a small upload, and the rows
+ * of the large parts copy to the host while the small last parts compute.
+ * Defaults 6 6 12 12 8 6 32 12288 0 2 10.  Setting
  * them drops the context's cached CUDA graphs (the autotuner,
  * halign-4_gb300/autotune.py, searches them).  No reference counterpart:
  * launch geometry. */
-#define HG_LAUNCH_KNOBS 10
+#define HG_LAUNCH_KNOBS 11
 int hg_ctx_set_launch(hg_ctx_t* ctx, const int32_t* ctas_per_sm, int n);
 int hg_ctx_get_launch(const hg_ctx_t* ctx, int32_t* ctas_per_sm, int n);
 

@@ -425,6 +425,95 @@ def test_pipelined_sub_batches_equal_one_batch(gpu, pkg):
     _same_result(sub.align(b, rows=True, check=False), one, w.n)  # reused pipeline buffers and graphs
 
 
+@pytest.mark.parametrize("cap", [700, 1300, 3000])
+def test_host_path_edge_split_equals_staged(gpu, pkg, cap):
+    """32 MB or more to move: the host-buffer call re-cuts its first and
+    last sub-batches into small edge parts (four sub-batches: the first two
+    and the last two; three or fewer: all of them), on two lanes with two
+    row buffers each; CIGARs, flags and rows equal the device-resident
+    run's."""
+    w = pkg.synth.mito(2600)
+    b = gpu.pack(w.seqs, w.offsets)
+    ix = gpu.Index(w.center)
+    ctx = gpu.Context(ix, max_queries=cap, max_bases=cap * 16700)
+    got = ctx.align(b, rows=True, check=False)
+    again = ctx.align(b, rows=True, check=False)  # reused buffers and graphs
+    one = gpu.Context(ix, max_queries=w.n, max_bases=w.n * 16700)  # the whole batch as one sub-batch
+    one.stage(b)
+    one.run_staged()
+    want = one.fetch_staged(rows=True)
+    _same_result(got, want, w.n)
+    _same_result(again, want, w.n)
+    _same_result(ctx.align_ascii(w.seqs, w.offsets, rows=True, check=False), want, w.n)
+
+
+def _ascii_cases(pkg, rng, center, n):
+    """Queries with exception bytes of every kind: N runs, lower case, U,
+    IUPAC codes, runs of alternating bytes, an exception at either end."""
+    cases = []
+    for i in range(n):
+        a = int(rng.integers(0, len(center) - 3000))
+        q = bytearray(center[a:a + int(rng.integers(1500, 3000))])
+        kind = i % 6
+        if kind == 1:
+            p, r = int(rng.integers(0, len(q) - 60)), int(rng.integers(1, 60))
+            q[p:p + r] = b"N" * r
+        if kind == 2:
+            q = bytearray(bytes(q).lower()) if i % 12 == 2 else bytearray(bytes(q[:700]).lower() + bytes(q[700:]))
+        if kind == 3:
+            for p in rng.integers(0, len(q), 12):
+                q[int(p)] = b"RYKMSWBDHVNU"[int(rng.integers(0, 12))]
+        if kind == 4:
+            p = int(rng.integers(0, len(q) - 40))
+            q[p:p + 40] = b"NANRNNRRNU" * 4
+        if kind == 5:
+            q[0:1] = b"n"
+            q[-3:] = b"NNN"
+        cases.append(bytes(q))
+    return cases
+
+
+@pytest.mark.parametrize("cap", [37, 1000])
+def test_align_ascii_equals_packed_path(gpu, pkg, cap):
+    """hg_align_ascii (bytes uploaded per sub-batch, packed and their
+    exception runs listed on the device) returns exactly what hg_pack +
+    hg_align_batch return: CIGARs, flags, status and rows (which carry the
+    exception bytes back)."""
+    rng = np.random.default_rng(61)
+    center = pkg.synth.random_center(8000, 23)
+    cases = _ascii_cases(pkg, rng, center, 180)
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=cap, max_bases=cap * 3000 + 1024)
+    want = ctx.align(gpu.pack(seqs, offs), rows=True, check=False)
+    for _ in range(2):
+        _same_result(ctx.align_ascii(seqs, offs, rows=True, check=False), want, len(cases))
+    got = ctx.align_ascii(seqs, offs, rows=False, check=False)
+    for i in range(len(cases)):
+        assert np.array_equal(got.cigar_of(i), want.cigar_of(i)), i
+
+
+def test_align_ascii_exception_capacity(gpu, pkg):
+    """More exception runs in a sub-batch than max_bases / 16 + 4096: a
+    capacity error (no query reads past the run buffer), and the context
+    aligns the next batch correctly."""
+    rng = np.random.default_rng(62)
+    center = pkg.synth.random_center(6000, 24)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=40, max_bases=40 * 6000)
+    bad = [b"NA" * 2500 + center[:1000] for _ in range(10)]  # 2,500 runs each, 25,000 > 19,096
+    seqs = b"".join(bad)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in bad])]).astype(np.int64)
+    with pytest.raises(RuntimeError, match="exception runs"):
+        ctx.align_ascii(seqs, offs, rows=True)
+    cases = _ascii_cases(pkg, rng, center, 30)
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    _same_result(ctx.align_ascii(seqs, offs, rows=True, check=False),
+                 ctx.align(gpu.pack(seqs, offs), rows=True, check=False), len(cases))
+
+
 def test_pipelined_cigar_overflow_copies_in_pieces(gpu, pkg, oracle):
     """Sub-batches whose CIGARs outgrow the compaction buffer (short unrelated
     queries against a long center: global alignments with many ops) are
