@@ -420,11 +420,14 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
         uint32_t rpos = 0, qpos = 0, slot = 0, nkept = 0;
         // consecutive match segments (and anchor spans, which are match
         // segments) become one record of their summed length: their ops are
-        // all M and merge in the CIGAR anyway.  A run still open at the end of
-        // a 32-segment chunk is carried (record id, start, length so far).
+        // all M and merge in the CIGAR anyway.  Segments tile the center and
+        // the query and a match is diagonal, so a run (empty segments inside
+        // it included) spans from its first segment's start to its last
+        // segment's end.  A run still open at the end of a 32-segment chunk is
+        // carried (record id, start).
         bool open = false;
-        uint32_t o_sid = 0, o_rs = 0, o_qs = 0, o_len = 0;
-        unsigned long long match_cells = 0;  // added to the cell total once per query
+        uint32_t o_sid = 0, o_rs = 0, o_qs = 0;
+        unsigned long long match_cells = 0;  // this lane's part, added to the cell total once per query
         auto put_match = [&](uint32_t id, uint32_t mrs, uint32_t mqs, uint32_t mlen) {
             Seg g;
             g.rs = mrs, g.qs = mqs, g.rl = mlen, g.ql = mlen;
@@ -507,22 +510,18 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
                 kind = kSegDpLarge;
             // the reference runs extz2 on a match segment too (full band: rl x rl
             // cells); count them so the cell total stays the reference's work unit
-            match_cells += __reduce_add_sync(FULL, act && kind == kSegMatch ? rl * rl : 0u);
+            if (act && kind == kSegMatch) match_cells += (unsigned long long)rl * rl;
             const bool keep = act && kind != kSegEmpty;
             const unsigned kmask = __ballot_sync(FULL, keep);
             const bool isM = keep && kind == kSegMatch;
             const unsigned mmask = __ballot_sync(FULL, isM);
             if (kmask == mmask) {  // every kept segment is a match (or none is kept): one run, no DP
-                if (mmask) {
-                    const uint32_t tot = __reduce_add_sync(FULL, isM ? rl : 0u);
-                    if (!open) {
-                        const int h = __ffs(mmask) - 1;
-                        o_rs = __shfl_sync(FULL, rs, h), o_qs = __shfl_sync(FULL, qs, h);
-                        o_sid = (uint32_t)sb + nkept, o_len = 0;
-                        ++nkept;
-                        open = true;
-                    }
-                    o_len += tot;
+                if (mmask && !open) {
+                    const int h = __ffs(mmask) - 1;
+                    o_rs = __shfl_sync(FULL, rs, h), o_qs = __shfl_sync(FULL, qs, h);
+                    o_sid = (uint32_t)sb + nkept;
+                    ++nkept;
+                    open = true;
                 }
                 rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
                 qpos = (uint32_t)__shfl_sync(FULL, iq, 31);
@@ -537,27 +536,22 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
             const uint32_t sid = (uint32_t)sb + nkept + (uint32_t)__popc(rmask & below);
             // a carried run ends where this chunk's first kept segment is not a match
             if (open && kmask && !((mmask >> (__ffs(kmask) - 1)) & 1u)) {
-                if (lane == 0) put_match(o_sid, o_rs, o_qs, o_len);
+                if (lane == 0) put_match(o_sid, o_rs, o_qs, rpos - o_rs);
                 open = false;
             }
-            // match runs: length so far = prefix sum since the run head (or the carried run)
-            const uint32_t mlen = isM ? rl : 0u;
-            const uint32_t minc = warp_incl_sum(mlen);
+            // match runs: this lane's run head (-1: the carried run)
             const unsigned hm = __ballot_sync(FULL, isM && !cont);
             const unsigned hup = hm & ((2u << lane) - 1u);
-            const int h = hup ? 31 - __clz(hup) : -1;  // this lane's run head (-1: the carried run)
+            const int h = hup ? 31 - __clz(hup) : -1;
             const int hs = h >= 0 ? h : 0;
-            const uint32_t h_exc = __shfl_sync(FULL, minc - mlen, hs);
             const uint32_t h_sid = __shfl_sync(FULL, sid, hs), h_rs = __shfl_sync(FULL, rs, hs),
                            h_qs = __shfl_sync(FULL, qs, hs);
-            const uint32_t run_len = h >= 0 ? minc - h_exc : o_len + minc;
             const uint32_t r_sid = h >= 0 ? h_sid : o_sid, r_rs = h >= 0 ? h_rs : o_rs, r_qs = h >= 0 ? h_qs : o_qs;
             const unsigned ka = kmask & ~((2u << lane) - 1u);  // kept segments after this one
-            if (isM && ka && !((mmask >> (__ffs(ka) - 1)) & 1u)) put_match(r_sid, r_rs, r_qs, run_len);
+            if (isM && ka && !((mmask >> (__ffs(ka) - 1)) & 1u)) put_match(r_sid, r_rs, r_qs, (uint32_t)ir - r_rs);
             if (kmask) {  // the chunk's last kept segment decides what is carried
                 const int last = 31 - __clz(kmask);
                 if ((mmask >> last) & 1u) {
-                    o_len = __shfl_sync(FULL, run_len, last);
                     o_sid = __shfl_sync(FULL, r_sid, last);
                     o_rs = __shfl_sync(FULL, r_rs, last);
                     o_qs = __shfl_sync(FULL, r_qs, last);
@@ -567,7 +561,8 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
                 }
             }
             const uint32_t need = (seg_is_dp(kind) && act) ? rl + ql : 0;
-            const uint32_t sincl = warp_incl_sum(need);
+            const unsigned mdp = __ballot_sync(FULL, need != 0);
+            const uint32_t sincl = mdp ? warp_incl_sum(need) : 0u;
             const uint32_t my_slot = slot + sincl - need;
             if (rec && !isM) {
                 Seg g;
@@ -580,25 +575,9 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
             }
             nkept += (uint32_t)__popc(rmask);
             // tier work lists (warp-aggregated appends): small, thin, one-warp
-            // wavefront, CTA wavefront, exact
-            const bool dp_big = act && (kind == kSegDpLarge || kind == kSegGlobal);
-            const bool wv = dp_big && wave_eligible(rl, ql);
-            const bool wv_warp = wv && min(rl, ql) <= (uint32_t)kWaveWarpMaxInner;
+            // wavefront, CTA wavefront, exact; a chunk whose DP segments all
+            // go to the small tier (the common case) skips the others
             const unsigned ms = __ballot_sync(FULL, act && kind == kSegDpSmall);
-            const unsigned ml = __ballot_sync(FULL, dp_big && !wv);
-            const unsigned mw = __ballot_sync(FULL, wv_warp);
-            const unsigned mx = __ballot_sync(FULL, wv && !wv_warp);
-            const unsigned mt = __ballot_sync(FULL, act && kind == kSegDpThin);
-            const unsigned mq = __ballot_sync(FULL, act && kind == kSegDpSquare);
-            unsigned bs = 0, bl = 0, bw = 0, bx = 0, bt = 0, bq = 0;
-            if (lane == 0) {
-                if (mq) bq = atomicAdd(b.n_sq, (unsigned)__popc(mq));
-                if (mt) bt = atomicAdd(b.n_thin, (unsigned)__popc(mt));
-
-                if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
-                if (mw) bw = atomicAdd(b.n_wave, (unsigned)__popc(mw));
-                if (mx) bx = atomicAdd(b.n_wide, (unsigned)__popc(mx));
-            }
             if (ms) {
                 const uint32_t nms = (uint32_t)__popc(ms);
                 if (nms > sm_left) {
@@ -607,87 +586,108 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
                     if (lane == 0) nb = atomicAdd(b.n_small, kSmallBlock);
                     sm_base = __shfl_sync(FULL, nb, 0), sm_left = kSmallBlock;
                 }
-                bs = sm_base, sm_base += nms, sm_left -= nms;
-            }
-            bl = __shfl_sync(FULL, bl, 0);
-            bw = __shfl_sync(FULL, bw, 0);
-            bx = __shfl_sync(FULL, bx, 0);
-            bt = __shfl_sync(FULL, bt, 0);
-            bq = __shfl_sync(FULL, bq, 0);
-            if (ms >> lane & 1u) {
-                const unsigned w = bs + __popc(ms & below);
-                if ((int64_t)w < b.wcap) {
-                    b.work_small[w] = sid;
-                    if (b.work_key) {
-                        Seg g;
-                        g.rl = rl, g.ql = ql, g.kind = kind | flags;
-                        b.work_key[w] = shape_key(g);
-                    }
-                } else {
-                    atomicOr(&b.status[q], kStArenaOverflow);
-                }
-            }
-            // (the small-tier shape histogram is counted from work_key by shape_hist_kernel)
-            if (ml >> lane & 1u) {
-                const unsigned w = bl + __popc(ml & below);
-                if ((int64_t)w < b.wcap) b.work_large[w] = sid;
-                else atomicOr(&b.status[q], kStArenaOverflow);
-            }
-            uint32_t wkey = 0xffffffffu;
-            if (mw >> lane & 1u) {
-                const unsigned w = bw + __popc(mw & below);
-                wkey = wave_key(rl, ql, (flags & kSegLeft) != 0);
-                if ((int64_t)w < b.wcap) {
-                    b.work_wave[w] = sid;
-                    b.work_wave_key[w] = wkey;
-                } else {
-                    atomicOr(&b.status[q], kStArenaOverflow);
-                }
-            }
-            if (mw) {
-                const unsigned peers = __match_any_sync(FULL, wkey);
-                if ((mw >> lane & 1u) && lane == __ffs(peers) - 1) atomicAdd(&b.wave_hist[wkey], __popc(peers));
-            }
-            if (mx >> lane & 1u) {
-                const unsigned w = bx + __popc(mx & below);
-                if ((int64_t)w < b.wcap) b.work_wide[w] = sid;
-                else atomicOr(&b.status[q], kStArenaOverflow);
-            }
-            uint32_t tkey = 0xffffffffu;  // counted in the histogram only when placed
-            if (mt >> lane & 1u) {
-                const unsigned w = bt + __popc(mt & below);
-                if ((int64_t)w < b.wcap) {
-                    tkey = thin_key(rl, ql, (flags & kSegLeft) != 0);
-                    b.work_thin[w] = sid;
-                    b.work_thin_key[w] = tkey;
-                } else {
-                    atomicOr(&b.status[q], kStArenaOverflow);
-                }
-            }
-            if (mt) {
-                const unsigned peers = __match_any_sync(FULL, tkey);
-                if (tkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.thin_hist[tkey], __popc(peers));
-            }
-            if (mq) {
-                uint32_t qkey = 0xffffffffu;  // counted in the histogram only when placed
-                if (mq >> lane & 1u) {
-                    const unsigned w = bq + __popc(mq & below);
+                const uint32_t bs = sm_base;
+                sm_base += nms, sm_left -= nms;
+                if (ms >> lane & 1u) {
+                    const unsigned w = bs + __popc(ms & below);
                     if ((int64_t)w < b.wcap) {
-                        qkey = square_key(rl, ql, (flags & kSegLeft) != 0);
-                        b.work_sq[w] = sid;
-                        b.work_sq_key[w] = qkey;
+                        b.work_small[w] = sid;
+                        if (b.work_key) {
+                            Seg g;
+                            g.rl = rl, g.ql = ql, g.kind = kind | flags;
+                            b.work_key[w] = shape_key(g);
+                        }
                     } else {
                         atomicOr(&b.status[q], kStArenaOverflow);
                     }
                 }
-                const unsigned peers = __match_any_sync(FULL, qkey);
-                if (qkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.sq_hist[qkey], __popc(peers));
+                // (the small-tier shape histogram is counted from work_key by shape_hist_kernel)
+            }
+            if (mdp != ms) {
+                const bool dp_big = act && (kind == kSegDpLarge || kind == kSegGlobal);
+                const bool wv = dp_big && wave_eligible(rl, ql);
+                const bool wv_warp = wv && min(rl, ql) <= (uint32_t)kWaveWarpMaxInner;
+                const unsigned ml = __ballot_sync(FULL, dp_big && !wv);
+                const unsigned mw = __ballot_sync(FULL, wv_warp);
+                const unsigned mx = __ballot_sync(FULL, wv && !wv_warp);
+                const unsigned mt = __ballot_sync(FULL, act && kind == kSegDpThin);
+                const unsigned mq = __ballot_sync(FULL, act && kind == kSegDpSquare);
+                unsigned bl = 0, bw = 0, bx = 0, bt = 0, bq = 0;
+                if (lane == 0) {
+                    if (mq) bq = atomicAdd(b.n_sq, (unsigned)__popc(mq));
+                    if (mt) bt = atomicAdd(b.n_thin, (unsigned)__popc(mt));
+                    if (ml) bl = atomicAdd(b.n_large, (unsigned)__popc(ml));
+                    if (mw) bw = atomicAdd(b.n_wave, (unsigned)__popc(mw));
+                    if (mx) bx = atomicAdd(b.n_wide, (unsigned)__popc(mx));
+                }
+                bl = __shfl_sync(FULL, bl, 0);
+                bw = __shfl_sync(FULL, bw, 0);
+                bx = __shfl_sync(FULL, bx, 0);
+                bt = __shfl_sync(FULL, bt, 0);
+                bq = __shfl_sync(FULL, bq, 0);
+                if (ml >> lane & 1u) {
+                    const unsigned w = bl + __popc(ml & below);
+                    if ((int64_t)w < b.wcap) b.work_large[w] = sid;
+                    else atomicOr(&b.status[q], kStArenaOverflow);
+                }
+                uint32_t wkey = 0xffffffffu;
+                if (mw >> lane & 1u) {
+                    const unsigned w = bw + __popc(mw & below);
+                    wkey = wave_key(rl, ql, (flags & kSegLeft) != 0);
+                    if ((int64_t)w < b.wcap) {
+                        b.work_wave[w] = sid;
+                        b.work_wave_key[w] = wkey;
+                    } else {
+                        atomicOr(&b.status[q], kStArenaOverflow);
+                    }
+                }
+                if (mw) {
+                    const unsigned peers = __match_any_sync(FULL, wkey);
+                    if ((mw >> lane & 1u) && lane == __ffs(peers) - 1) atomicAdd(&b.wave_hist[wkey], __popc(peers));
+                }
+                if (mx >> lane & 1u) {
+                    const unsigned w = bx + __popc(mx & below);
+                    if ((int64_t)w < b.wcap) b.work_wide[w] = sid;
+                    else atomicOr(&b.status[q], kStArenaOverflow);
+                }
+                uint32_t tkey = 0xffffffffu;  // counted in the histogram only when placed
+                if (mt >> lane & 1u) {
+                    const unsigned w = bt + __popc(mt & below);
+                    if ((int64_t)w < b.wcap) {
+                        tkey = thin_key(rl, ql, (flags & kSegLeft) != 0);
+                        b.work_thin[w] = sid;
+                        b.work_thin_key[w] = tkey;
+                    } else {
+                        atomicOr(&b.status[q], kStArenaOverflow);
+                    }
+                }
+                if (mt) {
+                    const unsigned peers = __match_any_sync(FULL, tkey);
+                    if (tkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.thin_hist[tkey], __popc(peers));
+                }
+                if (mq) {
+                    uint32_t qkey = 0xffffffffu;  // counted in the histogram only when placed
+                    if (mq >> lane & 1u) {
+                        const unsigned w = bq + __popc(mq & below);
+                        if ((int64_t)w < b.wcap) {
+                            qkey = square_key(rl, ql, (flags & kSegLeft) != 0);
+                            b.work_sq[w] = sid;
+                            b.work_sq_key[w] = qkey;
+                        } else {
+                            atomicOr(&b.status[q], kStArenaOverflow);
+                        }
+                    }
+                    const unsigned peers = __match_any_sync(FULL, qkey);
+                    if (qkey != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(&b.sq_hist[qkey], __popc(peers));
+                }
             }
             rpos = (uint32_t)__shfl_sync(FULL, ir, 31);
             qpos = (uint32_t)__shfl_sync(FULL, iq, 31);
             slot = slot + __shfl_sync(FULL, sincl, 31);
         }
-        if (open && lane == 0) put_match(o_sid, o_rs, o_qs, o_len);
+        if (open && lane == 0) put_match(o_sid, o_rs, o_qs, rpos - o_rs);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) match_cells += __shfl_xor_sync(FULL, match_cells, o);
         if (lane == 0 && match_cells && b.cells) {
             atomicAdd(b.cells, match_cells);
             atomicAdd(b.match_cells, match_cells);
