@@ -134,47 +134,72 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
         // keeps (f_i, p_i) unless some candidate j <= i-2 totals more than f_i
         // (ties do not improve; where the scan stops then does not matter).
         // A total is at most f_j + min(span, dg) (the gap penalty is >= 0), so
-        // the candidates i-kNear .. i-2 are bounded one by one (scored exactly
+        // the candidates i-kNear1 .. i-2 are bounded one by one (scored exactly
         // only when the bound fails) and all older ones at once through the
-        // prefix maximum of f; an anchor the bounds do not clear runs the
-        // reference's scan (lane l takes anchor ib + l; the first anchor whose
-        // result differs ends it).
-        constexpr int kNear = 8;
+        // prefix maximum of f; where that prefix bound fails, i-kNear ..
+        // i-kNear1-1 are bounded one by one and the older ones through the
+        // prefix maximum up to i-kNear-1.  An anchor the bounds do not clear
+        // runs the reference's scan (lane l takes anchor ib + l; the first
+        // anchor whose result differs ends it).
+        constexpr int kNear1 = 4, kNear = 8;
         int bad = A;
-        int32_t mcarry = INT32_MIN;  // max f over anchors 0 .. ib - kNear - 2
+        int32_t mcarry = INT32_MIN;  // max f over anchors 0 .. ib - kNear1 - 2
+        int32_t pm1 = INT32_MIN;     // the previous chunk's mf1 (lane l: anchor ib - 32 + l)
         for (int ib = 0; ib < A && bad == A; ib += 32) {
             const int i = ib + lane;
-            const int jf = i - kNear - 1;  // max f over 0 .. jf: the bound of the older candidates
-            int32_t mf = (jf >= 0 && jf < A) ? f[jf] : INT32_MIN;
+            // mf1: max f over 0 .. i - kNear1 - 1; mf2: over 0 .. i - kNear - 1 (mf1 of anchor i - 4)
+            const int jf = i - kNear1 - 1;
+            int32_t mf1 = (jf >= 0 && jf < A) ? f[jf] : INT32_MIN;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const int32_t v = __shfl_up_sync(FULL, mf, o);
-                if (lane >= o) mf = max(mf, v);
+                const int32_t v = __shfl_up_sync(FULL, mf1, o);
+                if (lane >= o) mf1 = max(mf1, v);
             }
-            mf = max(mf, mcarry);
-            mcarry = __shfl_sync(FULL, mf, 31);
+            mf1 = max(mf1, mcarry);
+            mcarry = __shfl_sync(FULL, mf1, 31);
+            const int32_t up4 = __shfl_up_sync(FULL, mf1, kNear - kNear1);
+            const int32_t prev4 = __shfl_sync(FULL, pm1, (lane + 32 - (kNear - kNear1)) & 31);
+            const int32_t mf2 = lane >= kNear - kNear1 ? up4 : prev4;
+            pm1 = mf1;
             int mine = A;
             if (i > 0 && i < A) {
                 const uint32_t ri = ar[i], qv = aq[i];
                 const int32_t fi = f[i];
-                bool ok = mf == INT32_MIN || (int64_t)mf + span <= (int64_t)fi;
-                // all near candidates' fields are loaded before any is tested
-                uint32_t nr[kNear - 1], nq[kNear - 1];
-                int32_t nf[kNear - 1];
+                // one near candidate: cleared by its bound or by its exact score
+                auto near_ok = [&](uint32_t rc, uint32_t qc, int32_t fc) -> bool {
+                    const int32_t dg = min((int32_t)(qv - qc), (int32_t)(ri - rc));
+                    if ((int64_t)fc + min(span, dg) <= (int64_t)fi) return true;
+                    const int32_t sc = chain_score(ix, lg2, ri, qv, rc, qc, span);
+                    return sc == INT32_MIN || (int64_t)fc + sc <= (int64_t)fi;
+                };
+                // candidates i-2 .. i-kNear1 one by one (fields loaded before any is tested)
+                uint32_t nr[kNear1 - 1], nq[kNear1 - 1];
+                int32_t nf[kNear1 - 1];
 #pragma unroll
-                for (int d = 2; d <= kNear; ++d) {
+                for (int d = 2; d <= kNear1; ++d) {
                     const int j = max(i - d, 0);
                     nr[d - 2] = ar[j], nq[d - 2] = aq[j], nf[d - 2] = f[j];
                 }
+                bool near = true;
 #pragma unroll
-                for (int d = 2; d <= kNear; ++d) {
-                    if (i - d < 0) break;
-                    const uint32_t rc = nr[d - 2], qc = nq[d - 2];
-                    const int32_t fc = nf[d - 2];
-                    const int32_t dg = min((int32_t)(qv - qc), (int32_t)(ri - rc));
-                    if ((int64_t)fc + min(span, dg) <= (int64_t)fi) continue;
-                    const int32_t sc = chain_score(ix, lg2, ri, qv, rc, qc, span);
-                    if (sc != INT32_MIN && (int64_t)fc + sc > (int64_t)fi) ok = false;
+                for (int d = 2; d <= kNear1; ++d)
+                    if (i - d >= 0 && !near_ok(nr[d - 2], nq[d - 2], nf[d - 2])) near = false;
+                // older candidates at once through mf1; where that bound fails,
+                // i-kNear1-1 .. i-kNear one by one and the older ones through mf2
+                bool ok = near && (mf1 == INT32_MIN || (int64_t)mf1 + span <= (int64_t)fi);
+                if (near && !ok) {
+                    ok = mf2 == INT32_MIN || (int64_t)mf2 + span <= (int64_t)fi;
+                    uint32_t mr[kNear - kNear1], mq[kNear - kNear1];
+                    int32_t mfv[kNear - kNear1];
+#pragma unroll
+                    for (int d = kNear1 + 1; d <= kNear; ++d) {
+                        const int j = max(i - d, 0);
+                        mr[d - kNear1 - 1] = ar[j], mq[d - kNear1 - 1] = aq[j], mfv[d - kNear1 - 1] = f[j];
+                    }
+#pragma unroll
+                    for (int d = kNear1 + 1; d <= kNear; ++d)
+                        if (i - d >= 0 && !near_ok(mr[d - kNear1 - 1], mq[d - kNear1 - 1], mfv[d - kNear1 - 1]))
+                            ok = false;
                 }
                 if (!ok) {
                     const int jmin = max(0, i - ix.max_iter);
