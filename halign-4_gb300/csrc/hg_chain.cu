@@ -93,40 +93,44 @@ __global__ void __launch_bounds__(kChainWarps * 32, 8) chain_kernel(IndexDev ix,
         // of 32 (lane l takes anchor 32c + l, so loads are coalesced): a warp
         // scan composes the steps x -> max(span, x + s) and applies them to the
         // last f of the previous chunk.
-        constexpr int64_t kNeg = -((int64_t)1 << 40);
-        int64_t carry = kNeg;
-        uint32_t pr = 0, pqv = 0;  // positions of anchor c0 - 1 (the previous chunk's last)
-        uint32_t nar = lane < A ? ar[lane] : 0u, naq = lane < A ? aq[lane] : 0u;  // chunk 0
-        for (int c0 = 0; c0 < A; c0 += 32) {
-            const int i = c0 + lane;
-            const uint32_t ri = nar, qv = naq;
-            nar = i + 32 < A ? ar[i + 32] : 0u;  // next chunk, loaded ahead
-            naq = i + 32 < A ? aq[i + 32] : 0u;
-            uint32_t rj = __shfl_up_sync(FULL, ri, 1), qj = __shfl_up_sync(FULL, qv, 1);
-            if (lane == 0) rj = pr, qj = pqv;
-            pr = __shfl_sync(FULL, ri, 31), pqv = __shfl_sync(FULL, qv, 31);
-            int64_t sv = kNeg;
-            if (i > 0 && i < A) {
-                if ((int32_t)(ri - rj) <= ix.max_dist_x) {  // i-1 inside the window of i
-                    const int32_t sc = chain_score(ix, lg2, ri, qv, rj, qj, span);
-                    if (sc != INT32_MIN) sv = sc;
+        // The pairs run in 32-bit values below 2^28 query bases (f <= query
+        // length + span, so -2^29 stays below every f), in 64-bit above.
+        auto speculate = [&](auto zero) {
+            using T = decltype(zero);
+            constexpr T kNeg = sizeof(T) == 4 ? (T)-(1 << 29) : (T) - ((int64_t)1 << 40);
+            T carry = kNeg;
+            uint32_t pr = 0, pqv = 0;  // positions of anchor c0 - 1 (the previous chunk's last)
+            uint32_t nar = lane < A ? ar[lane] : 0u, naq = lane < A ? aq[lane] : 0u;  // chunk 0
+            for (int c0 = 0; c0 < A; c0 += 32) {
+                const int i = c0 + lane;
+                const uint32_t ri = nar, qv = naq;
+                nar = i + 32 < A ? ar[i + 32] : 0u;  // next chunk, loaded ahead
+                naq = i + 32 < A ? aq[i + 32] : 0u;
+                uint32_t rj = __shfl_up_sync(FULL, ri, 1), qj = __shfl_up_sync(FULL, qv, 1);
+                if (lane == 0) rj = pr, qj = pqv;
+                pr = __shfl_sync(FULL, ri, 31), pqv = __shfl_sync(FULL, qv, 31);
+                T sv = kNeg;
+                if (i > 0 && i < A) {
+                    if ((int32_t)(ri - rj) <= ix.max_dist_x) {  // i-1 inside the window of i
+                        const int32_t sc = chain_score(ix, lg2, ri, qv, rj, qj, span);
+                        if (sc != INT32_MIN) sv = (T)sc;
+                    }
                 }
-            }
-            int64_t fa = i < A ? (int64_t)span : kNeg, fb = i < A ? sv : 0;  // lanes past the end: identity
+                T fa = i < A ? (T)span : kNeg, fb = i < A ? sv : (T)0;  // lanes past the end: identity
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {  // inclusive scan: compose left steps first
-                const int64_t la = __shfl_up_sync(FULL, fa, o), lb = __shfl_up_sync(FULL, fb, o);
-                if (lane >= o) fa = max(fa, la + fb), fb = max(lb + fb, 2 * kNeg);
+                for (int o = 1; o < 32; o <<= 1) {  // inclusive scan: compose left steps first
+                    const T la = __shfl_up_sync(FULL, fa, o), lb = __shfl_up_sync(FULL, fb, o);
+                    if (lane >= o) fa = max(fa, (T)(la + fb)), fb = max((T)(lb + fb), (T)(2 * kNeg));
+                }
+                const T fi = max(fa, (T)(carry + fb));
+                // p_i = i-1 exactly when f_{i-1} + s_i > span, i.e. when f_i > span:
+                // p is not stored, spec_p() derives it from f
+                if (i < A) f[i] = (int32_t)fi;
+                carry = __shfl_sync(FULL, fi, 31);
             }
-            const int64_t fi = max(fa, carry + fb);
-            int64_t fprev = __shfl_up_sync(FULL, fi, 1);
-            if (lane == 0) fprev = carry;
-            // p_i = i-1 exactly when fprev + sv > span, i.e. when f_i > span:
-            // p is not stored, spec_p() derives it from f
-            if (i < A) f[i] = (int32_t)fi;
-            (void)fprev;
-            carry = __shfl_sync(FULL, fi, 31);
-        }
+        };
+        if (b.qlen[q] < (1 << 28)) speculate((int32_t)0);
+        else speculate((int64_t)0);
         __syncwarp();
         // the speculated predecessor of anchor j (f_j > span: j-1, else none)
         auto spec_p = [&](int j, int32_t fj) -> int32_t { return fj > span ? j - 1 : -1; };
