@@ -54,7 +54,7 @@ PORT_VS_REF_X86 = {"threads_1": 0.98, "threads_8": 0.96}
 
 # Warp instructions per query base of the stage kernels, from their ncu
 # captures on the mito workload (profiles/kernels_mito4k.md).
-MITO_INST_PER_BASE = {"seed": 273.3e6 / 66.3e6, "anchor": 71.0e6 / 66.3e6, "chain": 420.4e6 / 66.3e6,
+MITO_INST_PER_BASE = {"seed": 273.3e6 / 66.3e6, "anchor": 71.0e6 / 66.3e6, "chain": 319.6e6 / 66.3e6,
                       "rows": 32.6e6 / 66.3e6}
 
 
@@ -760,7 +760,7 @@ def main():
     # from its ncu capture on the mito workload (4,000 queries, 66.3 Mbp),
     # scaled to one launch (one sub-batch) of this run
     mito_dram_per_base = {"seed": (17.17e6 + 24.66e6) / 66.3e6, "anchor": (81.10e6 + 38.27e6) / 66.3e6,
-                          "chain": (279.47e6 + 61.87e6) / 66.3e6, "rows": (18.44e6 + 7.78e6) / 66.3e6}
+                          "chain": (296.61e6 + 62.36e6) / 66.3e6, "rows": (18.44e6 + 7.78e6) / 66.3e6}
     traffic = None
     if args.workload == "mito" and top in mito_dram_per_base:
         traffic = int(round(mito_dram_per_base[top] * B / n_sub))

@@ -490,8 +490,9 @@ __global__ void __launch_bounds__(kSeedThreads) seed_kernel(IndexDev ix, BatchDe
 //    compares the ring's logical contents with the ideal deque (the suffix
 //    minima of the window); when they are equal the ring behaves ideally
 //    until the next overflow, and the warp returns to the ideal mode.
-// Each step's emissions are looked up in the center index together and
-// written in order.
+// Emissions of both modes queue in shared memory in position order and are
+// looked up in the center index and written 32 at a time; each step's
+// packed bytes are loaded one step ahead.
 constexpr int kExactWarps = 4;
 constexpr int kExactBlocks = 64;
 
@@ -507,7 +508,7 @@ __host__ __device__ __forceinline__ int exact_hist_slots(int ring_slots)
 
 __host__ __device__ __forceinline__ size_t exact_warp_bytes(int ring_slots)
 {
-    return ((size_t)exact_hist_slots(ring_slots) * 8 + (size_t)ring_slots * 12 + 32 * 12 + 15) & ~(size_t)15;
+    return ((size_t)exact_hist_slots(ring_slots) * 8 + (size_t)ring_slots * 12 + 64 * 16 + 15) & ~(size_t)15;
 }
 
 __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev ix, BatchDev b, SeedOut so)
@@ -518,10 +519,11 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
     const int RS = b.ring_slots;
     const uint32_t HM = (uint32_t)exact_hist_slots(RS) - 1u;
     uint64_t* hist = ex_smem + wl * (exact_warp_bytes(RS) / 8);  // hash of k-mer p at p & HM
-    uint64_t* eh = hist + HM + 1;                                 // exact-mode emissions: hash
-    uint64_t* rh = eh + 32;                                       // ring: hash
-    uint32_t* ep = reinterpret_cast<uint32_t*>(rh + RS);          // exact-mode emissions: position
-    uint32_t* rp = ep + 32;                                       // ring: position
+    uint64_t* eh = hist + HM + 1;                                 // emission queue: hash
+    uint64_t* rh = eh + 64;                                       // ring: hash
+    uint32_t* ep = reinterpret_cast<uint32_t*>(rh + RS);          // emission queue: position
+    uint32_t* es = ep + 64;                                       // emission queue: strand bit
+    uint32_t* rp = es + 64;                                       // ring: position
     const unsigned le = lane == 31 ? FULL : (2u << lane) - 1u;   // lanes <= this one
     const unsigned lt = (1u << lane) - 1u;                        // lanes < this one
     const unsigned total = *b.n_exact;
@@ -543,13 +545,47 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
         uint32_t head = 0, size = 0, valid = 0, last_p = 0;   // ring state (head in both modes)
         bool exact = false, has_last = false;
         int n_hits = 0, n_match = 0;
+        int nq = 0;  // queued emissions (<= 63)
+        // the first cnt (<= 32) queued emissions: looked up and written in
+        // order; the rest move to the front of the queue
+        auto flush = [&](int cnt) {
+            const bool act = lane < cnt;
+            const uint64_t ch = act ? eh[lane] : 0;
+            const uint32_t cp = act ? ep[lane] : 0, cs = act ? es[lane] : 0;
+            if (so.mode == 0) {
+                const uint32_t ent = act ? index_find(ix, ch) : kEmptyKey;
+                const bool hit = act && ent != kEmptyKey;
+                const unsigned mm = __ballot_sync(FULL, hit);
+                if (hit) {
+                    const int r = n_match + __popc(mm & lt);
+                    b.hit_pos[hb + r] = cp;
+                    b.hit_ent[hb + r] = ent;
+                }
+                n_match += __popc(mm);
+            } else if (act) {
+                so.hx[hb + n_hits + lane] = (ch << 8) | (uint64_t)(uint8_t)k;
+                so.hy[hb + n_hits + lane] = ((uint64_t)(cs ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
+            }
+            n_hits += cnt;
+            const int rest = nq - cnt;
+            const bool mv = lane < rest;
+            const uint64_t mh = mv ? eh[cnt + lane] : 0;
+            const uint32_t mp = mv ? ep[cnt + lane] : 0, ms = mv ? es[cnt + lane] : 0;
+            __syncwarp();
+            if (mv) eh[lane] = mh, ep[lane] = mp, es[lane] = ms;
+            __syncwarp();
+            nq = rest;
+        };
+        uint32_t pk_next = lane < (int)n ? pk[lane >> 2] : 0u;  // the packed byte of this lane's base, a step ahead
         __syncwarp();
         for (uint32_t i0 = 0; i0 < n; i0 += 32) {
             const uint32_t i = i0 + (uint32_t)lane;
             const bool inq = i < n;
+            const uint32_t pkb = pk_next;
+            pk_next = i + 32 < n ? pk[(i + 32) >> 2] : 0u;
             uint32_t c = 0;
             if (inq) {
-                c = packed_code(pk, i);
+                c = (pkb >> ((i & 3u) * 2u)) & 3u;
                 for (int64_t ee = ecur; ee < e1 && (uint32_t)b.exc[ee * 3] <= i; ++ee)
                     if (i < (uint32_t)(b.exc[ee * 3] + b.exc[ee * 3 + 1])) c = nt4_of((uint8_t)b.exc[ee * 3 + 2]);
             }
@@ -617,24 +653,11 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
                 }
                 head = (head + (uint32_t)__popc(fpm)) % win;
                 const unsigned emm = __ballot_sync(FULL, em);
-                if (emm) {
-                    if (so.mode == 0) {
-                        const uint32_t ent = em ? index_find(ix, hm) : kEmptyKey;
-                        const bool hit = ent != kEmptyKey;
-                        const unsigned mm = __ballot_sync(FULL, hit);
-                        if (hit) {
-                            const int r = n_match + __popc(mm & lt);
-                            b.hit_pos[hb + r] = m;
-                            b.hit_ent[hb + r] = ent;
-                        }
-                        n_match += __popc(mm);
-                    } else if (em) {
-                        const int r = n_hits + __popc(emm & lt);
-                        so.hx[hb + r] = (hm << 8) | (uint64_t)(uint8_t)k;
-                        so.hy[hb + r] = ((uint64_t)(strand ? 0x80000000u : 0u) << 32) | (uint64_t)m;
-                    }
-                    n_hits += __popc(emm);
+                if (em) {
+                    const int r = nq + __popc(emm & lt);
+                    eh[r] = hm, ep[r] = m, es[r] = strand ? 1u : 0u;
                 }
+                nq += __popc(emm);
                 if (L < 32) {  // rebuild the full ring before the push of k-mer P
                     const uint32_t P = i0 + (uint32_t)L + 1 - k;
                     for (uint32_t t = (uint32_t)lane; t < win; t += 32) {
@@ -651,7 +674,6 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
             }
             if (exact) {
                 int ne = 0;
-                unsigned esm = 0;  // strand bit of each emission
                 if (lane == 0) {
                     const uint32_t lim = min(32u, n - i0);
                     for (uint32_t l = start; l < lim; ++l) {
@@ -683,8 +705,7 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
                             const uint64_t ch = rh[head];
                             const uint32_t cp = rp[head];
                             if (!has_last || ch != last_h || cp != last_p) {
-                                eh[ne] = ch, ep[ne] = cp;
-                                esm |= (strm >> l & 1u) << ne;
+                                eh[nq + ne] = ch, ep[nq + ne] = cp, es[nq + ne] = strm >> l & 1u;
                                 ++ne;
                                 last_h = ch, last_p = cp, has_last = true;
                             }
@@ -692,7 +713,6 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
                     }
                 }
                 ne = __shfl_sync(FULL, ne, 0);
-                esm = __shfl_sync(FULL, esm, 0);
                 head = __shfl_sync(FULL, head, 0);
                 size = __shfl_sync(FULL, size, 0);
                 valid = __shfl_sync(FULL, valid, 0);
@@ -700,27 +720,7 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
                 last_h = __shfl_sync(FULL, last_h, 0);
                 last_p = __shfl_sync(FULL, last_p, 0);
                 __syncwarp();
-                if (ne) {
-                    const bool act = lane < ne;
-                    const uint64_t ch = act ? eh[lane] : 0;
-                    const uint32_t cp = act ? ep[lane] : 0;
-                    if (so.mode == 0) {
-                        const uint32_t ent = act ? index_find(ix, ch) : kEmptyKey;
-                        const bool hit = act && ent != kEmptyKey;
-                        const unsigned mm = __ballot_sync(FULL, hit);
-                        if (hit) {
-                            const int r = n_match + __popc(mm & lt);
-                            b.hit_pos[hb + r] = cp;
-                            b.hit_ent[hb + r] = ent;
-                        }
-                        n_match += __popc(mm);
-                    } else if (act) {
-                        so.hx[hb + n_hits + lane] = (ch << 8) | (uint64_t)(uint8_t)k;
-                        so.hy[hb + n_hits + lane] =
-                            ((uint64_t)((esm >> lane & 1u) ? 0x80000000u : 0u) << 32) | (uint64_t)cp;
-                    }
-                    n_hits += ne;
-                }
+                nq += ne;
                 // back to the ideal mode once the ring holds the ideal deque of the step's last k-mer
                 if (i0 + 32 < n && __shfl_sync(FULL, (int)(kv && pos + 1 >= win), 31)) {
                     const uint32_t hp = i0 + 32 - k;
@@ -766,7 +766,9 @@ __global__ void __launch_bounds__(kExactWarps * 32) seed_exact_kernel(IndexDev i
                 }
             }
             __syncwarp();
+            if (nq >= 32) flush(32);
         }
+        while (nq > 0) flush(nq < 32 ? nq : 32);
         if (lane == 0) {
             b.n_hits[q] = n_hits;
             b.n_matched[q] = n_match;
