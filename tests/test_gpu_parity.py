@@ -156,7 +156,8 @@ def test_staged_equals_batched(gpu, pkg):
     b = gpu.pack(w.seqs, w.offsets)
     r1 = ctx.align(b, rows=True)
     ctx.stage(b)
-    ctx.run_staged()
+    ctx.run_staged()  # a new sub-batch shape: direct launches
+    ctx.run_staged()  # seen before: captured into a graph and launched
     ctx.run_staged()  # replay of the captured graph
     r2 = ctx.fetch_staged(rows=True)
     assert np.array_equal(r1.cigar, r2.cigar) and np.array_equal(r1.rows, r2.rows)
