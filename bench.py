@@ -724,7 +724,7 @@ def main():
         e_wall = dist.max((time.perf_counter() - t0) / e2e_steps)
         # from ASCII: hg_align_ascii on the queries' bytes in pinned memory
         # (uploaded per sub-batch and packed on the device), every step
-        asc_steps = max(1, min(args.steps, 3))
+        asc_steps = max(1, args.steps)
         seqs_u8 = pin(np.frombuffer(w.seqs, np.uint8))
         offs64 = np.ascontiguousarray(w.offsets, np.int64)
 
@@ -732,7 +732,11 @@ def main():
             pkg._check(L.hg_align_ascii(ctx.h, P(seqs_u8), P(offs64), b.n, P(cig_out), len(cig_out), P(off_out),
                                         P(ins_out), P(rows_out), rows_out.shape[1], P(st_out)))
 
-        call_ascii()
+        # warm-up: the pinned input was just allocated (a large allocation
+        # measured slowing the calls right after it), and the first call sets
+        # up the ASCII buffers
+        for _ in range(max(2, args.warmup)):
+            call_ascii()
         t0 = time.perf_counter()
         for _ in range(asc_steps):
             call_ascii()

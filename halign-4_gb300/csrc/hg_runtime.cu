@@ -122,7 +122,7 @@ struct hg_ctx {
     cudaStream_t st2 = nullptr;                            // side stream of the CTA wavefront tier
     cudaStream_t st3 = nullptr;                            // side stream of the one-warp wavefront and exact tiers
     // CTAs per SM of the seed, anchor, chain, dp_small, stitch and rows launches (hg_ctx_set_launch)
-    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareMaxCells, 0, 2, 10};
+    int32_t launch[HG_LAUNCH_KNOBS] = {6, 6, 12, 12, 8, 6, hg::kThinMaxInner, hg::kSquareDefaultCells, 0, 2, 10};
     // second compute lane: a context of the same capacity on its own streams
     // that runs every other sub-batch of a multi-sub-batch run (knob 9 = 2)
     hg_ctx* peer = nullptr;

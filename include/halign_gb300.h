@@ -159,7 +159,7 @@ int hg_fetch_staged(hg_ctx_t* ctx, uint32_t* cigar, int64_t cigar_cap, int64_t* 
  * so that the first and the last two parts hold s percent (0..24; 0 = off)
  * of their bases each: both lanes start after a small upload, and the rows
  * of the large parts copy to the host while the small last parts compute.
- * Defaults 6 6 12 12 8 6 32 12288 0 2 10.  Setting
+ * Defaults 6 6 12 12 8 6 32 3072 0 2 10.  Setting
  * them drops the context's cached CUDA graphs (the autotuner,
  * halign-4_gb300/autotune.py, searches them).  No reference counterpart:
  * launch geometry. */
