@@ -257,7 +257,7 @@ def measure_plain(pkg, ctx, w, n_plain: int):
             "note": "host-timed hg_align_plain vs hg_align_batch (both with H2D/D2H) on the same queries"}
 
 
-def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 60000):
+def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 240000):
     """The serving loop (hg_serve_*, scheduler in the library) on the serve
     workload (Poisson arrivals, 500..29,903 bp substrings of a 29,903 bp
     center, 0.5% divergence): p50/p99 at `rate` req/s; saturation (n_sat

@@ -85,11 +85,12 @@ int64_t arena_of(hg_index_t* ix, int64_t q, int64_t b, hg_ctx_t** out)
 
 // Fills slot s with the oldest waiting requests; returns their ids (empty:
 // nothing waiting).  Called with the lock held.
-void admit(hg_server* S, std::vector<int64_t>& take, std::vector<const char*>& ptr, std::vector<int64_t>& len)
+void admit(hg_server* S, std::vector<int64_t>& take, std::vector<const char*>& ptr, std::vector<int64_t>& len,
+           int64_t max_q)
 {
     take.clear(), ptr.clear(), len.clear();
     int64_t bases = 0;
-    while (!S->pending.empty() && (int64_t)take.size() < S->slot_q) {
+    while (!S->pending.empty() && (int64_t)take.size() < max_q) {
         const int64_t id = S->pending.front();
         Request& r = S->reqs[(size_t)(id - S->base_id)];
         if (!take.empty() && bases + (int64_t)r.seq.size() > S->slot_b) break;
@@ -112,7 +113,8 @@ void fail_all(hg_server* S, int code, const std::string& msg)
 }
 
 // Submitting thread: whenever a context is free and requests wait, admit the
-// oldest (under the lock, so micro-batches leave the FIFO in order), pack
+// oldest (under the lock, so micro-batches leave the FIFO in order; fewer
+// while most contexts are idle), pack
 // them on all host cores (hg_submit_ascii's OpenMP loop) and enqueue them;
 // the context is then the collecting thread's to poll.
 void submitter(hg_server* S)
@@ -137,9 +139,16 @@ void submitter(hg_server* S)
                 S->cv_busy.notify_all();
                 return;
             }
-            for (int i = 0; i < ns && s < 0; ++i)
-                if (S->slots[i].state == 0) s = i;
-            admit(S, take, ptr, len);
+            int busy = 0;
+            for (int i = 0; i < ns; ++i) {
+                if (S->slots[i].state == 0 && s < 0) s = i;
+                busy += S->slots[i].state != 0;
+            }
+            // ramp: with b contexts busy a micro-batch takes at most (b + 1) / ns
+            // of a context's queries, so an idle GPU starts after a short packing
+            // pass instead of a full one; with all others busy it takes a full one
+            const int64_t max_q = std::max<int64_t>(std::min<int64_t>(S->slot_q, 1024), S->slot_q * (busy + 1) / ns);
+            admit(S, take, ptr, len, max_q);
             S->slots[s].ids = take;
             S->slots[s].state = 1;  // packing
             ++S->batches;
