@@ -715,7 +715,10 @@ def main():
                                     rows_out.shape[1], P(st_out))
             pkg._check(code)
 
-        call()
+        # warm-up: the pinned buffers were just allocated (a large allocation
+        # measured slowing the calls right after it)
+        for _ in range(max(2, args.warmup)):
+            call()
         dist.barrier()
         e2e_steps = args.steps
         t0 = time.perf_counter()
