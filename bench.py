@@ -266,7 +266,7 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 240000):
     rate (Poisson arrivals) for latency at load."""
     w = pkg.synth.serve(n_req, rate=rate)
     ix = pkg.Index(w.center)
-    srv = pkg.serve.NativeServer(ix, n_slots=4, slot_queries=8192, slot_bases=128_000_000, budget_bytes=100 << 30)
+    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=6144, slot_bases=96_000_000, budget_bytes=120 << 30)
     srv.run(w.seqs, w.offsets[: min(w.n, 400) + 1], None)  # warm-up
     st = srv.run(w.seqs, w.offsets, w.arrivals)
     ws = pkg.synth.serve(n_sat, rate=rate, chunk=1)
@@ -295,7 +295,7 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 240000):
     keep = ("p50_ms", "p99_ms", "mean_ms", "max_ms", "requests", "micro_batches", "mbp_per_s", "status_or")
     out = {k: st[k] for k in keep}
     out.update({"rate_req_per_s": rate, "center_bp": len(w.center), "loop": "native (hg_serve_*)",
-                "contexts": int(st["contexts"]), "device_bytes": int(st["device_bytes"]), "budget_bytes": 100 << 30,
+                "contexts": int(st["contexts"]), "device_bytes": int(st["device_bytes"]), "budget_bytes": 120 << 30,
                 "saturation": {k: sat[k] for k in keep},
                 "batched_same_requests_mbp_per_s": batched, "batched_same_requests_e2e_mbp_per_s": batched_e2e,
                 "saturation_frac_of_batched": sat["mbp_per_s"] / batched,
