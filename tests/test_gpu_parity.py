@@ -446,6 +446,12 @@ def test_host_path_edge_split_equals_staged(gpu, pkg, cap):
     _same_result(got, want, w.n)
     _same_result(again, want, w.n)
     _same_result(ctx.align_ascii(w.seqs, w.offsets, rows=True, check=False), want, w.n)
+    # one lane (two input slots, two row buffers), and no edge cut
+    knobs = ctx.get_launch()
+    for lanes, share in ((1, 10), (2, 0), (1, 0)):
+        ctx.set_launch(knobs[:9] + [lanes, share])
+        _same_result(ctx.align(b, rows=True, check=False), want, w.n)
+        _same_result(ctx.align_ascii(w.seqs, w.offsets, rows=True, check=False), want, w.n)
 
 
 def _ascii_cases(pkg, rng, center, n):
@@ -493,6 +499,21 @@ def test_align_ascii_equals_packed_path(gpu, pkg, cap):
     got = ctx.align_ascii(seqs, offs, rows=False, check=False)
     for i in range(len(cases)):
         assert np.array_equal(got.cigar_of(i), want.cigar_of(i)), i
+
+
+def test_align_ascii_empty_and_single(gpu, pkg, oracle):
+    """hg_align_ascii with no query, one empty query among others, and a
+    single query: the same results as the packed path."""
+    center = pkg.synth.random_center(4000, 25)
+    ix = gpu.Index(center)
+    ctx = gpu.Context(ix, max_queries=8, max_bases=8 * 4100)
+    res = ctx.align_ascii(b"", np.zeros(1, np.int64), rows=True)
+    assert len(res.cigar_off) == 1 and res.cigar_off[0] == 0
+    for cases in ([center[100:3900]], [b"", center[:2000], b"", center[1000:4000]]):
+        seqs = b"".join(cases)
+        offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+        _same_result(ctx.align_ascii(seqs, offs, rows=True, check=False),
+                     ctx.align(gpu.pack(seqs, offs), rows=True, check=False), len(cases))
 
 
 def test_align_ascii_exception_capacity(gpu, pkg):
