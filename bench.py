@@ -266,7 +266,7 @@ def measure_serving(pkg, n_req: int, rate: float, n_sat: int = 240000):
     rate (Poisson arrivals) for latency at load."""
     w = pkg.synth.serve(n_req, rate=rate)
     ix = pkg.Index(w.center)
-    srv = pkg.serve.NativeServer(ix, n_slots=8, slot_queries=6144, slot_bases=96_000_000, budget_bytes=120 << 30)
+    srv = pkg.serve.NativeServer(ix, n_slots=12, slot_queries=4096, slot_bases=64_000_000, budget_bytes=120 << 30)
     srv.run(w.seqs, w.offsets[: min(w.n, 400) + 1], None)  # warm-up
     st = srv.run(w.seqs, w.offsets, w.arrivals)
     ws = pkg.synth.serve(n_sat, rate=rate, chunk=1)
