@@ -124,6 +124,14 @@ def test_bad_arguments_rejected_on_host(pkg, native):
                        np.zeros(25, np.int8).ctypes.data, 6, 2, -1, -1, 0, 0x02, ez.ctypes.data, None, 0)
     assert r == -2
     assert b"symbol >= m" in L.hg_last_error()
+    # hg_align_ascii: no context, missing buffers, or a negative query length
+    offs = np.array([0, 8, 4], np.int64)
+    seqs = np.frombuffer(b"ACGTACGT", np.uint8)
+    out = np.zeros(64, np.uint32)
+    coff = np.zeros(3, np.int64)
+    assert L.hg_align_ascii(None, seqs.ctypes.data, offs.ctypes.data, 2, out.ctypes.data, 64, coff.ctypes.data,
+                            None, None, 0, None) == 2
+    assert L.hg_align_ascii(None, None, None, -1, None, 0, None, None, None, 0, None) == 2
 
 
 def test_auto_band_matches_oracle(oracle):
