@@ -25,6 +25,13 @@ __device__ __forceinline__ uint32_t ascii_code(uint32_t ch)
 
 constexpr int kPackThreads = 256;
 
+// One warp per query, 128 bases (32 output bytes) per step: lane l takes the
+// 4 bases of output byte j = j0 + l from two 32-bit words of the query's
+// bytes (one funnel shift for the query's alignment), packs them with the
+// SWAR test of hg_pack (((c >> 1) ^ (c >> 2)) & 3 maps A C G T to 0 1 2 3;
+// rebuilding the bytes from the codes confirms them) and only falls back to
+// a byte loop where a word holds another byte or the query's end.  Run
+// starts need the byte before each lane's first: the previous lane's last.
 __global__ void __launch_bounds__(kPackThreads) ascii_pack_kernel(const uint8_t* ascii, const int64_t* aoff, int n,
                                                                   const int64_t* poff, uint8_t* packed, int32_t* nrun)
 {
@@ -37,21 +44,41 @@ __global__ void __launch_bounds__(kPackThreads) ascii_pack_kernel(const uint8_t*
         const int64_t len = aoff[q + 1] - aoff[q];
         uint8_t* out = packed + poff[q];
         const int64_t nb = (len + 3) / 4, pad = (nb + 15) / 16 * 16;
+        // the query's bytes as aligned words (the buffer starts aligned and
+        // keeps slack after the last query, so the word past a query's end is
+        // readable; bytes past the end are masked below)
+        const uint32_t mis = (uint32_t)((uintptr_t)s & 3u);
+        const uint32_t* sw = reinterpret_cast<const uint32_t*>(s - mis);
+        uint32_t carry = 0;  // the byte before this step's first base (0: none)
         int runs = 0;
-        for (int64_t j = lane; j < pad; j += 32) {
+        for (int64_t j0 = 0; j0 < pad; j0 += 32) {
+            const int64_t j = j0 + lane;
+            uint32_t v = 0;
+            if (j < nb) {
+                const uint32_t w0 = sw[j], w1 = sw[j + 1];
+                v = __funnelshift_r(w0, w1, 8u * mis);
+            }
+            uint32_t prev = __shfl_up_sync(FULL, v, 1) >> 24;
+            if (lane == 0) prev = carry;
+            carry = __shfl_sync(FULL, v, 31) >> 24;
+            const int64_t t0 = 4 * j;
             uint32_t byte = 0;
             if (j < nb) {
-                const int64_t t0 = 4 * j;
-                uint32_t prev = t0 > 0 ? s[t0 - 1] : 0u;
-                bool prevx = t0 > 0 && ascii_code(prev) > 3;
-                for (int u = 0; u < 4 && t0 + u < len; ++u) {
-                    const uint32_t ch = s[t0 + u], c = ascii_code(ch);
-                    if (c < 4) byte |= c << (2 * u);
-                    else if (!prevx || ch != prev) ++runs;
-                    prevx = c > 3, prev = ch;
+                const uint32_t cd = ((v >> 1) ^ (v >> 2)) & 0x03030303u;
+                const uint32_t b0 = cd & 0x01010101u, b1 = (cd >> 1) & 0x01010101u;
+                if (t0 + 4 <= len && 0x41414141u + 2u * b0 + 6u * b1 + 11u * (b0 & b1) == v) {
+                    byte = (cd & 3u) | ((cd >> 6) & 0xCu) | ((cd >> 12) & 0x30u) | ((cd >> 18) & 0xC0u);
+                } else {  // another byte, or the query's end, in this word
+                    bool prevx = t0 > 0 && ascii_code(prev) > 3;
+                    for (int u = 0; u < 4 && t0 + u < len; ++u) {
+                        const uint32_t ch = (v >> (8 * u)) & 0xffu, c = ascii_code(ch);
+                        if (c < 4) byte |= c << (2 * u);
+                        else if (!prevx || ch != prev) ++runs;
+                        prevx = c > 3, prev = ch;
+                    }
                 }
             }
-            out[j] = (uint8_t)byte;
+            if (j < pad) out[j] = (uint8_t)byte;
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) runs += __shfl_xor_sync(FULL, runs, d);
