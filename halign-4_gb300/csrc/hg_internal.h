@@ -93,6 +93,20 @@ int consensus_of_rows(const std::vector<std::string>& recs, size_t limit, std::s
 // Length of an index's center.
 int64_t index_length(const hg_index_t* ix);
 
+// Asynchronous submission (hg_submit's form) of n ASCII queries of lengths
+// lens[] whose bytes lie in pinned host memory as `runs` runs of
+// consecutive queries back to back (run r: run_bytes[r] bytes at
+// run_ptr[r]): the runs upload as they are and the device packs them
+// (hg_align_ascii's packing).  The bytes must stay in place until the batch
+// is collected.  hg_collect then returns HG_ERR_CAPACITY when the batch's
+// exception runs exceeded the context's buffer; async_exc_overflow tells
+// that case from a short CIGAR buffer.  prepare_pinned_ascii allocates the
+// device and pinned buffers of this form up front.
+int prepare_pinned_ascii(hg_ctx_t* c);
+int submit_pinned_ascii(hg_ctx_t* c, const char* const* run_ptr, const int64_t* run_bytes, int runs,
+                        const int64_t* lens, int64_t n);
+bool async_exc_overflow(const hg_ctx_t* c);
+
 // Minimizers of one sequence through the batch seed kernel (hg_index_create
 // and hg_extract_minimizer).
 int run_extract(int k, int w, int non_canonical, const char* seq, int64_t len, std::vector<uint64_t>& xs,

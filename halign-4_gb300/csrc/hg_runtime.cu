@@ -232,6 +232,8 @@ struct hg_ctx {
     cudaEvent_t done_ev = nullptr;     // blocking-sync: a waiting host thread sleeps instead of spinning
     cudaEvent_t collected_ev = nullptr;
     int64_t async_n = -1;
+    bool async_ascii = false;   // the batch in flight is packed on the device (its capacity flag is read back)
+    bool async_exc_over = false;  // the last hg_collect failed on that flag
     bool timing = false;
     cudaEvent_t ev[10] = {};
     cudaEvent_t run_ev[2] = {};
@@ -1896,8 +1898,12 @@ int async_staging(hg_ctx_t* c)
 
 // The staged micro-batch (packed bases at h_packed, per-query offsets,
 // lengths and exception runs in h_i64 / h_i32) goes up and through the
-// stages on the context stream; results come back behind done_ev.
-int submit_tail(hg_ctx_t* c, int64_t n, int64_t pb, int64_t ne)
+// stages on the context stream; results come back behind done_ev.  With
+// `runs` the bases are ASCII in pinned memory instead (run r: run_bytes[r]
+// bytes of consecutive queries at run_ptr[r], query offsets in h_i64's
+// second block): they go up as they are and the device packs them.
+int submit_tail(hg_ctx_t* c, int64_t n, int64_t pb, int64_t ne, const char* const* run_ptr = nullptr,
+                const int64_t* run_bytes = nullptr, int runs = 0)
 {
     const int64_t M = c->max_n + 1;
     int64_t *spoff = c->h_i64, *seoff = c->h_i64 + M, *shoff = c->h_i64 + 2 * M, *scoff = c->h_i64 + 3 * M;
@@ -1907,14 +1913,28 @@ int submit_tail(hg_ctx_t* c, int64_t n, int64_t pb, int64_t ne)
     sub_arrays(c, sqlen, n, order, hoff, coff);
     for (int64_t i = 0; i < n; ++i) sorder[i] = order[i], shoff[i] = hoff[i], scoff[i] = coff[i];
     cudaStream_t st = c->st;
-    HG_CUDA(cudaMemcpyAsync(c->packed.p, c->h_packed, (size_t)pb, cudaMemcpyHostToDevice, st));
-    if (ne) HG_CUDA(cudaMemcpyAsync(c->exc.p, sexc, 12 * (size_t)ne, cudaMemcpyHostToDevice, st));
+    auto& PS = c->pipe[0];
+    if (run_ptr) {
+        int64_t at = 0;
+        for (int r = 0; r < runs; ++r) {
+            if (run_bytes[r])
+                HG_CUDA(cudaMemcpyAsync(PS.ascii.p + at, run_ptr[r], (size_t)run_bytes[r], cudaMemcpyHostToDevice, st));
+            at += run_bytes[r];
+        }
+        HG_CUDA(cudaMemcpyAsync(PS.aoff.p, seoff, 8 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+    } else {
+        HG_CUDA(cudaMemcpyAsync(c->packed.p, c->h_packed, (size_t)pb, cudaMemcpyHostToDevice, st));
+        if (ne) HG_CUDA(cudaMemcpyAsync(c->exc.p, sexc, 12 * (size_t)ne, cudaMemcpyHostToDevice, st));
+        HG_CUDA(cudaMemcpyAsync(c->exc_off.p, seoff, 8 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+    }
     HG_CUDA(cudaMemcpyAsync(c->poff.p, spoff, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
     HG_CUDA(cudaMemcpyAsync(c->qlen.p, sqlen, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
-    HG_CUDA(cudaMemcpyAsync(c->exc_off.p, seoff, 8 * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
     HG_CUDA(cudaMemcpyAsync(c->order.p, sorder, 4 * (size_t)n, cudaMemcpyHostToDevice, st));
     HG_CUDA(cudaMemcpyAsync(c->hoff.p, shoff, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
     HG_CUDA(cudaMemcpyAsync(c->coff.p, scoff, 8 * (size_t)n, cudaMemcpyHostToDevice, st));
+    if (run_ptr)
+        HG_CUDA(hg_launch_ascii_pack(PS.ascii.p, PS.aoff.p, (int)n, c->poff.p, c->packed.p, PS.nrun.p, c->exc_off.p,
+                                     c->exc.p, c->exc_cap, PS.excflag.p, c->sms, st));
     const hg::BatchDev b = batch_view(c, (int)n, c->packed.p, c->poff.p, c->qlen.p, c->exc.p, c->exc_off.p,
                                       c->order.p, c->hoff.p, c->coff.p);
     int r = run_sub(c, b, false);
@@ -1924,12 +1944,54 @@ int submit_tail(hg_ctx_t* c, int64_t n, int64_t pb, int64_t ne)
     HG_CUDA(cudaMemcpyAsync(c->h_i64 + 4 * M, c->cig_off.p, 8 * ((size_t)n + 1), cudaMemcpyDeviceToHost, st));
     HG_CUDA(cudaMemcpyAsync(c->h_has_ins, c->has_ins.p, (size_t)n, cudaMemcpyDeviceToHost, st));
     HG_CUDA(cudaMemcpyAsync(c->h_status, c->status.p, 4 * (size_t)n, cudaMemcpyDeviceToHost, st));
+    if (run_ptr) HG_CUDA(cudaMemcpyAsync(PS.h_excflag, PS.excflag.p, 4, cudaMemcpyDeviceToHost, st));
     HG_CUDA(cudaEventRecord(c->done_ev, st));
     c->async_n = n;
+    c->async_ascii = run_ptr != nullptr;
     return HG_OK;
 }
 
 }  // namespace
+
+int hg::prepare_pinned_ascii(hg_ctx_t* c)
+{
+    cudaSetDevice(c->ix->device);
+    int r = ascii_setup(c, 1);
+    return r ? r : async_staging(c);
+}
+
+int hg::submit_pinned_ascii(hg_ctx_t* c, const char* const* run_ptr, const int64_t* run_bytes, int runs,
+                            const int64_t* lens, int64_t n)
+{
+    if (!c || n <= 0 || runs < 0 || (runs > 0 && (!run_ptr || !run_bytes)) || !lens)
+        return fail(HG_ERR_ARG, "submit_pinned_ascii: bad arguments");
+    if (c->async_n >= 0) return fail(HG_ERR_ARG, "submit_pinned_ascii: previous batch not collected");
+    cudaSetDevice(c->ix->device);
+    int64_t bases = 0, bytes = 0, up = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        if (lens[i] < 0 || lens[i] > INT32_MAX) return fail(HG_ERR_ARG, "submit_pinned_ascii: bad query");
+        bases += lens[i], bytes += (int64_t)padded_bytes(lens[i]);
+    }
+    for (int r = 0; r < runs; ++r) up += run_bytes[r];
+    if (up != bases) return fail(HG_ERR_ARG, "submit_pinned_ascii: the runs do not hold the queries' bytes");
+    if (n > c->max_n || bases > c->max_bases || bytes > (int64_t)c->packed.n)
+        return fail(HG_ERR_CAPACITY, "submit_pinned_ascii: batch exceeds the context capacity");
+    int r = ascii_setup(c, 1);
+    if (r || (r = async_staging(c))) return r;
+    const int64_t M = c->max_n + 1;
+    int64_t *spoff = c->h_i64, *saoff = c->h_i64 + M;
+    int32_t* sqlen = c->h_i32;
+    int64_t pb = 0, ab = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        spoff[i] = pb, pb += (int64_t)padded_bytes(lens[i]);
+        saoff[i] = ab, ab += lens[i];
+        sqlen[i] = (int32_t)lens[i];
+    }
+    saoff[n] = ab;
+    return submit_tail(c, n, pb, 0, run_ptr, run_bytes, runs);
+}
+
+bool hg::async_exc_overflow(const hg_ctx_t* c) { return c && c->async_exc_over; }
 
 extern "C" int hg_submit(hg_ctx_t* c, const uint8_t* packed, const int64_t* poff, const int32_t* qlen,
                          const int32_t* exc, const int64_t* exc_off, int64_t n)
@@ -2021,6 +2083,12 @@ extern "C" int hg_collect(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64
     cudaSetDevice(c->ix->device);
     HG_CUDA(cudaEventSynchronize(c->done_ev));
     const int64_t n = c->async_n, M = c->max_n + 1;
+    c->async_exc_over = c->async_ascii && *c->pipe[0].h_excflag;
+    if (c->async_exc_over) {  // the device packing found more exception runs than the context holds
+        c->async_n = -1;
+        return fail(HG_ERR_CAPACITY, "hg_collect: the exception runs (bytes other than A/C/G/T) of the batch exceed "
+                                     "the context's " + std::to_string(c->exc_cap));
+    }
     const int64_t* off = c->h_i64 + 4 * M;
     const int64_t total = off[n];
     if (total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_collect: cigar buffer too small");

@@ -1,8 +1,9 @@
 // hg_serve.cpp - the continuous-batching request loop behind hg_serve_*
-// (include/halign_gb300.h): a FIFO of submitted requests, a pool of
-// contexts over one resident index, a submitting thread that admits and
-// packs micro-batches into free contexts (hg_submit_ascii) and a collecting
-// thread that polls, collects and files them, so packing and filing overlap.
+// (include/halign_gb300.h): a FIFO of submitted requests whose bytes are
+// copied into a ring of pinned host memory, a pool of contexts over one
+// resident index, a submitting thread that admits micro-batches into free
+// contexts (their bytes upload straight from the ring and the device packs
+// them) and a collecting thread that polls, collects and files them.
 //
 // Host code only; every alignment runs through the context calls of the C
 // ABI.  Requests are independent, so a request's result in the mix is its
@@ -28,7 +29,8 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 struct Request {
-    std::string seq;              // freed once submitted
+    int64_t pos = 0, len = 0;     // bytes at ring position pos (monotonic; ring offset pos % capacity)
+    bool released = false;        // filed: its ring bytes may be reused
     Clock::time_point t_in;
     double latency_ms = 0;
     uint32_t status = 0;
@@ -55,7 +57,15 @@ struct hg_server {
     int64_t arena_bytes = 0;
     std::vector<Slot> slots;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done, cv_busy;
+    std::condition_variable cv_work, cv_done, cv_busy, cv_space;
+    // request bytes: a ring of pinned host memory.  Positions grow without
+    // bound (offset = position % ring_cap); a request never wraps (it starts
+    // at the next lap when it would).  Writers take submit_mu, so ring order
+    // is id order: the ring is free from the oldest unreleased request's
+    // position (ring_tail) up to ring_head, the end of the last reservation.
+    char* ring = nullptr;
+    int64_t ring_cap = 0, ring_head = 0, ring_tail = 0, ring_pushed = 0, rel_id = 0;
+    std::mutex submit_mu;
     std::deque<Request> reqs;     // request id - base_id indexes it
     int64_t base_id = 0;
     std::deque<int64_t> pending;  // submitted, not yet admitted
@@ -77,29 +87,60 @@ int64_t arena_of(hg_index_t* ix, int64_t q, int64_t b, hg_ctx_t** out)
 {
     size_t f0 = 0, f1 = 0, tot = 0;
     cudaMemGetInfo(&f0, &tot);
-    const int r = hg_ctx_create(ix, q, b, out);
+    int r = hg_ctx_create(ix, q, b, out);
     if (r) return -r;
+    if ((r = hg::prepare_pinned_ascii(*out))) {  // the device-packing buffers count against the budget too
+        hg_ctx_destroy(*out);
+        *out = nullptr;
+        return -r;
+    }
     cudaMemGetInfo(&f1, &tot);
     return f0 > f1 ? (int64_t)(f0 - f1) : 0;
 }
 
-// Fills slot s with the oldest waiting requests; returns their ids (empty:
-// nothing waiting).  Called with the lock held.
-void admit(hg_server* S, std::vector<int64_t>& take, std::vector<const char*>& ptr, std::vector<int64_t>& len,
-           int64_t max_q)
+// Fills slot s with the oldest waiting requests: their ids, lengths and the
+// runs of the ring that hold their bytes back to back (one run, or two where
+// the ring wraps).  Called with the lock held.
+void admit(hg_server* S, std::vector<int64_t>& take, std::vector<int64_t>& len, std::vector<const char*>& run_ptr,
+           std::vector<int64_t>& run_bytes, int64_t max_q)
 {
-    take.clear(), ptr.clear(), len.clear();
-    int64_t bases = 0;
+    take.clear(), len.clear(), run_ptr.clear(), run_bytes.clear();
+    int64_t bases = 0, end = -1;
     while (!S->pending.empty() && (int64_t)take.size() < max_q) {
         const int64_t id = S->pending.front();
-        Request& r = S->reqs[(size_t)(id - S->base_id)];
-        if (!take.empty() && bases + (int64_t)r.seq.size() > S->slot_b) break;
+        const Request& r = S->reqs[(size_t)(id - S->base_id)];
+        if (!take.empty() && bases + r.len > S->slot_b) break;
         S->pending.pop_front();
         take.push_back(id);
-        ptr.push_back(r.seq.data());
-        len.push_back((int64_t)r.seq.size());
-        bases += (int64_t)r.seq.size();
+        len.push_back(r.len);
+        bases += r.len;
+        if (r.len == 0) continue;
+        if (r.pos == end && end % S->ring_cap != 0) {
+            run_bytes.back() += r.len;
+        } else {
+            run_ptr.push_back(S->ring + r.pos % S->ring_cap);
+            run_bytes.push_back(r.len);
+        }
+        end = r.pos + r.len;
     }
+}
+
+// After requests were released: the ring is free up to the oldest
+// unreleased request (or the last pushed byte).  Called with the lock held.
+void advance_ring(hg_server* S)
+{
+    const int64_t end = S->base_id + (int64_t)S->reqs.size();
+    S->rel_id = std::max(S->rel_id, S->base_id);
+    while (S->rel_id < end && S->reqs[(size_t)(S->rel_id - S->base_id)].released) ++S->rel_id;
+    S->ring_tail = S->rel_id < end ? S->reqs[(size_t)(S->rel_id - S->base_id)].pos : S->ring_pushed;
+}
+
+// Ring position of a request of len bytes after head: the next lap's start
+// when it would wrap.
+int64_t ring_place(const hg_server* S, int64_t head, int64_t len)
+{
+    const int64_t off = head % S->ring_cap;
+    return len > 0 && off + len > S->ring_cap ? head + (S->ring_cap - off) : head;
 }
 
 void fail_all(hg_server* S, int code, const std::string& msg)
@@ -110,18 +151,19 @@ void fail_all(hg_server* S, int code, const std::string& msg)
     S->cv_done.notify_all();
     S->cv_work.notify_all();
     S->cv_busy.notify_all();
+    S->cv_space.notify_all();
 }
 
 // Submitting thread: whenever a context is free and requests wait, admit the
 // oldest (under the lock, so micro-batches leave the FIFO in order; fewer
-// while most contexts are idle), pack
-// them on all host cores (hg_submit_ascii's OpenMP loop) and enqueue them;
-// the context is then the collecting thread's to poll.
+// while most contexts are idle) and enqueue them: their ring bytes upload as
+// they are and the device packs them; the context is then the collecting
+// thread's to poll.
 void submitter(hg_server* S)
 {
     cudaSetDevice(S->device);
-    std::vector<int64_t> take, len;
-    std::vector<const char*> ptr;
+    std::vector<int64_t> take, len, run_bytes;
+    std::vector<const char*> run_ptr;
     const int ns = (int)S->slots.size();
     for (;;) {
         int s = -1;
@@ -145,17 +187,18 @@ void submitter(hg_server* S)
                 busy += S->slots[i].state != 0;
             }
             // ramp: with b contexts busy a micro-batch takes at most (b + 1) / ns
-            // of a context's queries, so an idle GPU starts after a short packing
-            // pass instead of a full one; with all others busy it takes a full one
+            // of a context's queries, so an idle GPU starts on a small micro-batch
+            // instead of a full one; with all others busy it takes a full one
             const int64_t max_q = std::max<int64_t>(std::min<int64_t>(S->slot_q, 1024), S->slot_q * (busy + 1) / ns);
-            admit(S, take, ptr, len, max_q);
+            admit(S, take, len, run_ptr, run_bytes, max_q);
             S->slots[s].ids = take;
             S->slots[s].state = 1;  // packing
             ++S->batches;
         }
-        // the request strings stay put until their results are filed (only the
-        // collecting thread frees them), so packing runs without the lock
-        const int r = hg_submit_ascii(S->slots[s].ctx, ptr.data(), len.data(), (int64_t)take.size());
+        // the ring bytes stay put until the requests are filed (only the
+        // collecting thread releases them), so this runs without the lock
+        const int r = hg::submit_pinned_ascii(S->slots[s].ctx, run_ptr.data(), run_bytes.data(), (int)run_ptr.size(),
+                                              len.data(), (int64_t)take.size());
         if (r) {
             fail_all(S, r, hg_last_error());
             return;
@@ -207,12 +250,13 @@ void collector(hg_server* S)
             int64_t bases = 0;
             {
                 std::lock_guard<std::mutex> lock(S->mu);
-                for (int64_t id : sl.ids) bases += (int64_t)S->reqs[(size_t)(id - S->base_id)].seq.size();
+                for (int64_t id : sl.ids) bases += S->reqs[(size_t)(id - S->base_id)].len;
             }
             sl.cig.resize((size_t)bases / 8 + 64 * n + 1024);  // a few ops per kilobase; grown below if short
             sl.off.resize(n + 1), sl.ins.resize(n), sl.st.resize(n);
             int r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(), sl.st.data());
-            if (r == HG_ERR_CAPACITY) {  // rare: CIGARs longer than the first guess; the worst case fits
+            if (r == HG_ERR_CAPACITY && !hg::async_exc_overflow(sl.ctx)) {
+                // rare: CIGARs longer than the first guess; the worst case fits
                 sl.cig.resize((size_t)bases + n * (size_t)(hg::index_length(S->ix) + 4));
                 r = hg_collect(sl.ctx, sl.cig.data(), (int64_t)sl.cig.size(), sl.off.data(), sl.ins.data(),
                                sl.st.data());
@@ -231,10 +275,11 @@ void collector(hg_server* S)
                     q.cigar.swap(cigs[j]);
                     q.status = sl.st[j];
                     q.latency_ms = std::chrono::duration<double, std::milli>(now - q.t_in).count();
-                    std::string().swap(q.seq);
+                    q.released = true;
                     S->lat.push_back((float)q.latency_ms);
                     S->done.push_back(sl.ids[j]);
                 }
+                advance_ring(S);
                 S->bases_done += bases;
                 S->t_last = now;
                 sl.ids.clear();
@@ -242,6 +287,7 @@ void collector(hg_server* S)
             }
             S->cv_done.notify_all();
             S->cv_work.notify_all();
+            S->cv_space.notify_all();
             progressed = true;
         }
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
@@ -279,6 +325,15 @@ extern "C" int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries
         hg_serve_destroy(S);
         return hg::set_error(HG_ERR_CAPACITY, "hg_serve_create: one context does not fit the device-memory budget");
     }
+    // the ring holds what every context can take at once and as much again
+    // waiting; it is pinned, so micro-batches upload from it directly
+    S->ring_cap = std::max<int64_t>(2 * (int64_t)S->slots.size() * slot_bases, 1 << 20);
+    if (cudaHostAlloc(reinterpret_cast<void**>(&S->ring), (size_t)S->ring_cap, cudaHostAllocDefault) != cudaSuccess) {
+        cudaGetLastError();
+        S->ring = nullptr;
+        hg_serve_destroy(S);
+        return hg::set_error(HG_ERR_NOMEM, "hg_serve_create: pinned request ring");
+    }
     S->sub = std::thread(submitter, S);
     S->col = std::thread(collector, S);
     *out = S;
@@ -294,62 +349,99 @@ extern "C" void hg_serve_destroy(hg_server_t* S)
         S->pending.clear();
     }
     S->cv_work.notify_all();
+    S->cv_space.notify_all();
     if (S->sub.joinable()) S->sub.join();
     if (S->col.joinable()) S->col.join();
     for (auto& sl : S->slots) hg_ctx_destroy(sl.ctx);
+    if (S->ring) cudaFreeHost(S->ring);
     delete S;
 }
+
+namespace {
+
+// Queues requests i = 0..n-1 (bytes at seqs + offsets[i] .. offsets[i+1])
+// with one time stamp: in chunks, each reserved in the ring under the lock
+// (waiting while it is full), copied without it and then queued, so the
+// submitting thread starts on the first chunk while later ones copy.
+// Returns the first id or a negative HG_ERR_*.
+int64_t enqueue(hg_server* S, const char* seqs, const int64_t* offsets, int64_t n, const char* who)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t len = offsets[i + 1] - offsets[i];
+        if (len < 0) return -hg::set_error(HG_ERR_ARG, std::string(who) + ": offsets not ascending");
+        if (len > S->slot_b) return -hg::set_error(HG_ERR_CAPACITY, std::string(who) + ": request longer than slot_bases");
+    }
+    const auto now = Clock::now();
+    std::lock_guard<std::mutex> writer(S->submit_mu);  // ring order = id order
+    if (n == 0) {
+        std::lock_guard<std::mutex> lock(S->mu);
+        return S->base_id + (int64_t)S->reqs.size();
+    }
+    int64_t first = -1;
+    std::vector<int64_t> pos;
+    for (int64_t i = 0; i < n;) {
+        int64_t j = i;
+        {
+            std::unique_lock<std::mutex> lock(S->mu);
+            auto fits = [&](int64_t len) {
+                return ring_place(S, S->ring_head, len) + len - S->ring_tail <= S->ring_cap;
+            };
+            S->cv_space.wait(lock, [&] { return S->error || S->stop || fits(offsets[i + 1] - offsets[i]); });
+            if (S->error) return -hg::set_error(S->error, S->error_msg);
+            if (S->stop) return -hg::set_error(HG_ERR_ARG, std::string(who) + ": the server is stopping");
+            pos.clear();
+            int64_t bytes = 0;
+            while (j < n && j - i < 8192 && bytes < (64 << 20)) {
+                const int64_t len = offsets[j + 1] - offsets[j];
+                if (!fits(len)) break;
+                const int64_t p = ring_place(S, S->ring_head, len);
+                pos.push_back(p);
+                S->ring_head = p + len;
+                bytes += len;
+                ++j;
+            }
+        }
+        const int64_t m = j - i;
+#pragma omp parallel for schedule(dynamic, 64) if (m > 256)
+        for (int64_t k = 0; k < m; ++k) {
+            const int64_t len = offsets[i + k + 1] - offsets[i + k];
+            if (len) std::memcpy(S->ring + pos[(size_t)k] % S->ring_cap, seqs + offsets[i + k], (size_t)len);
+        }
+        {
+            std::lock_guard<std::mutex> lock(S->mu);
+            if (S->error) return -hg::set_error(S->error, S->error_msg);
+            if (!S->have_first) S->t_first = now, S->have_first = true;
+            const int64_t id0 = S->base_id + (int64_t)S->reqs.size();
+            if (first < 0) first = id0;
+            for (int64_t k = 0; k < m; ++k) {
+                Request r;
+                r.pos = pos[(size_t)k], r.len = offsets[i + k + 1] - offsets[i + k];
+                r.t_in = now;
+                S->reqs.push_back(std::move(r));
+                S->pending.push_back(id0 + k);
+            }
+            S->ring_pushed = S->ring_head;
+        }
+        S->cv_work.notify_one();
+        i = j;
+    }
+    return first;
+}
+
+}  // namespace
 
 extern "C" int64_t hg_serve_submit(hg_server_t* S, const char* seq, int64_t len)
 {
     if (!S || len < 0 || (len > 0 && !seq)) return -hg::set_error(HG_ERR_ARG, "hg_serve_submit: bad arguments");
-    if (len > S->slot_b) return -hg::set_error(HG_ERR_CAPACITY, "hg_serve_submit: request longer than slot_bases");
-    int64_t id;
-    {
-        std::lock_guard<std::mutex> lock(S->mu);
-        if (S->error) return -hg::set_error(S->error, S->error_msg);
-        Request r;
-        r.seq.assign(seq, (size_t)len);
-        r.t_in = Clock::now();
-        if (!S->have_first) S->t_first = r.t_in, S->have_first = true;
-        id = S->base_id + (int64_t)S->reqs.size();
-        S->reqs.push_back(std::move(r));
-        S->pending.push_back(id);
-    }
-    S->cv_work.notify_one();
-    return id;
+    const int64_t off[2] = {0, len};
+    return enqueue(S, seq, off, 1, "hg_serve_submit");
 }
 
 extern "C" int64_t hg_serve_submit_many(hg_server_t* S, const char* seqs, const int64_t* offsets, int64_t n)
 {
     if (!S || n < 0 || (n > 0 && (!seqs || !offsets)))
         return -hg::set_error(HG_ERR_ARG, "hg_serve_submit_many: bad arguments");
-    for (int64_t i = 0; i < n; ++i) {
-        const int64_t len = offsets[i + 1] - offsets[i];
-        if (len < 0) return -hg::set_error(HG_ERR_ARG, "hg_serve_submit_many: offsets not ascending");
-        if (len > S->slot_b) return -hg::set_error(HG_ERR_CAPACITY, "hg_serve_submit_many: request longer than slot_bases");
-    }
-    // the copies are made before the lock; one time stamp for the burst
-    std::vector<Request> burst((size_t)n);
-    const auto now = Clock::now();
-#pragma omp parallel for schedule(dynamic, 64)
-    for (int64_t i = 0; i < n; ++i) {
-        burst[i].seq.assign(seqs + offsets[i], (size_t)(offsets[i + 1] - offsets[i]));
-        burst[i].t_in = now;
-    }
-    int64_t first;
-    {
-        std::lock_guard<std::mutex> lock(S->mu);
-        if (S->error) return -hg::set_error(S->error, S->error_msg);
-        if (!S->have_first && n) S->t_first = now, S->have_first = true;
-        first = S->base_id + (int64_t)S->reqs.size();
-        for (int64_t i = 0; i < n; ++i) {
-            S->reqs.push_back(std::move(burst[i]));
-            S->pending.push_back(first + i);
-        }
-    }
-    S->cv_work.notify_one();
-    return first;
+    return enqueue(S, seqs, offsets, n, "hg_serve_submit_many");
 }
 
 extern "C" int64_t hg_serve_results(hg_server_t* S, int64_t max_n, int64_t* ids, uint32_t* status,

@@ -205,8 +205,8 @@ class NativeServer:
             got = 0
             while got < n:
                 m = self._lib.hg_serve_results(self.h, max_n, vp(rid), vp(st), None, vp(buf), cap, vp(coff), 1000)
-                if m < 0:
-                    errors.append(-m)
+                if m < 0:  # the message is this thread's: carry it to the caller
+                    errors.append((-m, self._lib.hg_last_error().decode(errors="replace")))
                     return
                 status[rid[:m] - base] = st[:m]
                 if keep_results:
@@ -243,7 +243,8 @@ class NativeServer:
         if th is not None:
             th.join()
         if errors:
-            self._check(errors[0])
+            from . import HalignError
+            raise HalignError(*errors[0])
         out = self.stats()
         out["status_or"] = int(np.bitwise_or.reduce(status)) if n else 0
         out["mbp_per_s"] = out["bases"] / out["wall_s"] / 1e6 if out["wall_s"] > 0 else 0.0

@@ -275,11 +275,14 @@ int hg_align_fasta_consensus(const char* queries_fasta, const char* out_fasta, i
 
 /* ---- serving loop (continuous batching) ---------------------------------
  * A request loop around one resident index: requests (one ASCII query each,
- * copied at submission) wait in a FIFO; a submitting thread fills every
- * free context with the oldest waiting requests (up to slot_queries and
- * slot_bases per micro-batch) and enqueues it asynchronously
- * (hg_submit_ascii), and a collecting thread polls the busy contexts and
- * files each finished request's CIGAR and status for hg_serve_result.  Requests that arrive
+ * copied at submission into a ring of pinned host memory of 2 x contexts x
+ * slot_bases bytes) wait in a FIFO; a submitting thread fills every free
+ * context with the oldest waiting requests (up to slot_queries and
+ * slot_bases per micro-batch) and enqueues it asynchronously - its bytes
+ * upload straight from the ring and the device packs them (hg_align_ascii's
+ * packing) - and a collecting thread polls the busy contexts, files each
+ * finished request's CIGAR and status for hg_serve_result and frees its ring
+ * bytes.  Requests that arrive
  * while others run join as contexts free up; micro-batches of different
  * contexts overlap on the GPU.  The contexts' device arenas are allocated at
  * creation; n_slots is reduced to what budget_bytes of device memory holds
@@ -292,12 +295,17 @@ int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries, int64_t s
 /* Stops the loop after the requests in flight finish, frees everything. */
 void hg_serve_destroy(hg_server_t* s);
 /* Queues one request; returns its id (0, 1, 2, ... in submission order) or a
- * negative HG_ERR_* (HG_ERR_CAPACITY: longer than slot_bases). */
+ * negative HG_ERR_* (HG_ERR_CAPACITY: longer than slot_bases).  Waits while
+ * the request ring is full.  A micro-batch whose bytes other than A/C/G/T
+ * form more runs than its context holds (slot_bases / 16 + 4096) fails the
+ * loop with HG_ERR_CAPACITY. */
 int64_t hg_serve_submit(hg_server_t* s, const char* seq, int64_t len);
 /* Queues a burst of n requests (concatenated in seqs, request i at
- * [offsets[i], offsets[i+1])) under one lock and one time stamp; returns the
+ * [offsets[i], offsets[i+1])) with one time stamp, in chunks that join the
+ * FIFO as they are copied (waiting while the ring is full); returns the
  * first id (the burst's ids are consecutive) or a negative HG_ERR_*
- * (nothing queued). */
+ * (nothing queued on a bad argument; on a loop failure in mid-burst the
+ * queued part fails with the loop). */
 int64_t hg_serve_submit_many(hg_server_t* s, const char* seqs, const int64_t* offsets, int64_t n);
 /* Up to max_n finished requests at once, waiting up to timeout_ms for the
  * first (< 0: no limit): ids[j], status[j], latency_ms[j] (optional) and the

@@ -77,3 +77,78 @@ def test_native_server_counters_and_budget(gpu, pkg, serve_setup, oracle):
     rows = np.stack([np.frombuffer(oracle.del_query(w.query(i), out["results"][i]), np.uint8) for i in range(40)])
     assert np.array_equal(cnt, oracle.count_rows(rows))
     srv.close()
+
+
+def _alone(gpu, ix, seqs, offs):
+    ctx = gpu.Context(ix, max_queries=1, max_bases=40_000)
+    out = []
+    for i in range(len(offs) - 1):
+        q = seqs[offs[i]:offs[i + 1]]
+        out.append(ctx.align(gpu.pack(q, np.array([0, len(q)], np.int64)), rows=False, check=False).cigar_of(0))
+    return out
+
+
+def test_native_server_burst_larger_than_its_ring(gpu, pkg, serve_setup):
+    """A burst of ~3.6 MB into a 1 MB request ring: submission waits for
+    space, the ring wraps several times, micro-batches upload from it in one
+    or two runs, and every CIGAR equals the request's CIGAR alone."""
+    w, ix = serve_setup
+    srv = pkg.serve.NativeServer(ix, n_slots=2, slot_queries=8, slot_bases=60_000, budget_bytes=40 << 30)
+    assert int(w.offsets[-1]) > 3 << 20
+    out = srv.run(w.seqs, w.offsets, None, keep_results=True)
+    assert out["requests"] == w.n and out["status_or"] == 0
+    alone = _alone(gpu, ix, w.seqs, w.offsets)
+    for i in range(w.n):
+        assert np.array_equal(out["results"][i], alone[i]), i
+    srv.close()
+
+
+def test_native_server_exception_bytes_and_empty_requests(gpu, pkg, serve_setup):
+    """Requests with bytes other than A/C/G/T (N runs, lower case, IUPAC
+    codes, exceptions at either end) and empty requests: the device packing
+    of the serving loop gives the host packing's CIGARs."""
+    w, ix = serve_setup
+    rng = np.random.default_rng(17)
+    center = w.center
+    cases = []
+    for i in range(60):
+        a = int(rng.integers(0, len(center) - 3000))
+        q = bytearray(center[a:a + int(rng.integers(1500, 3000))])
+        kind = i % 6
+        if kind == 1:
+            p, r = int(rng.integers(0, len(q) - 60)), int(rng.integers(1, 60))
+            q[p:p + r] = b"N" * r
+        if kind == 2:
+            q = bytearray(bytes(q[:700]).lower() + bytes(q[700:]))
+        if kind == 3:
+            for p in rng.integers(0, len(q), 12):
+                q[int(p)] = b"RYKMSWBDHVNU"[int(rng.integers(0, 12))]
+        if kind == 4:
+            p = int(rng.integers(0, len(q) - 40))
+            q[p:p + 40] = b"NANRNNRRNU" * 4
+        if kind == 5:
+            q[0:1] = b"n"
+            q[-3:] = b"NNN"
+        cases.append(bytes(q) if i % 20 != 7 else b"")
+    seqs = b"".join(cases)
+    offs = np.concatenate([[0], np.cumsum([len(x) for x in cases])]).astype(np.int64)
+    srv = pkg.serve.NativeServer(ix, n_slots=3, slot_queries=16, slot_bases=40_000, budget_bytes=40 << 30)
+    out = srv.run(seqs, offs, None, keep_results=True)
+    assert out["requests"] == len(cases)
+    alone = _alone(gpu, ix, seqs, offs)
+    for i in range(len(cases)):
+        assert np.array_equal(out["results"][i], alone[i]), i
+    srv.close()
+
+
+def test_native_server_exception_capacity_fails_the_loop(gpu, pkg, serve_setup):
+    """More exception runs than a context holds (one per byte of a 20 kb
+    request of alternating bytes) fail the loop with HG_ERR_CAPACITY, found
+    by the device packing and reported when the micro-batch is collected."""
+    w, ix = serve_setup
+    bad = b"NR" * 10_000
+    srv = pkg.serve.NativeServer(ix, n_slots=1, slot_queries=4, slot_bases=40_000, budget_bytes=40 << 30)
+    with pytest.raises(pkg.HalignError) as e:
+        srv.run(bad, np.array([0, len(bad)], np.int64), None)
+    assert e.value.code == pkg.HG_ERR_CAPACITY and "exception runs" in str(e.value)
+    srv.close()
