@@ -229,6 +229,12 @@ struct hg_ctx {
     int32_t* h_i32 = nullptr;      // qlen, order, exc (2 x max_n + exc_cap x 3)
     uint8_t* h_has_ins = nullptr;
     uint32_t* h_status = nullptr;
+    // the batch's compacted CIGARs, written by the device straight into
+    // mapped pinned memory at the end of the batch (up to h_cig_cap ops), so
+    // a collect needs no device work when they fit
+    uint32_t* h_cig = nullptr;
+    uint32_t* h_cig_dev = nullptr;
+    int64_t h_cig_cap = 0;
     cudaEvent_t done_ev = nullptr;     // blocking-sync: a waiting host thread sleeps instead of spinning
     cudaEvent_t collected_ev = nullptr;
     int64_t async_n = -1;
@@ -826,6 +832,7 @@ extern "C" void hg_ctx_destroy(hg_ctx_t* c)
     if (c->st) cudaStreamSynchronize(c->st);
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     if (c->h_packed) cudaFreeHost(c->h_packed);
+    if (c->h_cig) cudaFreeHost(c->h_cig);
     if (c->h_i64) cudaFreeHost(c->h_i64);
     if (c->h_i32) cudaFreeHost(c->h_i32);
     if (c->h_has_ins) cudaFreeHost(c->h_has_ins);
@@ -1885,7 +1892,10 @@ int async_staging(hg_ctx_t* c)
 {
     if (c->h_packed) return HG_OK;
     const int64_t M = c->max_n + 1;
-    if (cudaHostAlloc(&c->h_packed, c->packed.n, cudaHostAllocDefault) != cudaSuccess ||
+    c->h_cig_cap = c->max_bases / 8 + 64 * c->max_n + 1024;  // a few ops per kilobase; longer ones go the slow way
+    if ((!c->h_cig && cudaHostAlloc(&c->h_cig, sizeof(uint32_t) * (size_t)c->h_cig_cap, cudaHostAllocMapped) != cudaSuccess) ||
+        cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->h_cig_dev), c->h_cig, 0) != cudaSuccess ||
+        cudaHostAlloc(&c->h_packed, c->packed.n, cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc(&c->h_i64, sizeof(int64_t) * 5 * M, cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc(&c->h_i32, sizeof(int32_t) * (2 * M + 3 * c->exc_cap), cudaHostAllocDefault) != cudaSuccess ||
         cudaHostAlloc(&c->h_has_ins, (size_t)M, cudaHostAllocDefault) != cudaSuccess ||
@@ -1940,6 +1950,9 @@ int submit_tail(hg_ctx_t* c, int64_t n, int64_t pb, int64_t ne, const char* cons
     int r = run_sub(c, b, false);
     if (r) return r;
     compact_offsets_kernel<<<1, 1024, 0, st>>>(c->n_cig.p, (int)n, c->cig_off.p);
+    HG_CUDA(cudaGetLastError());
+    compact_copy_kernel<<<c->sms * 4, 256, 0, st>>>(c->cig.p, c->coff.p, c->n_cig.p, c->cig_off.p, (int)n, c->h_cig_dev,
+                                                    c->h_cig_cap, 0);
     HG_CUDA(cudaGetLastError());
     HG_CUDA(cudaMemcpyAsync(c->h_i64 + 4 * M, c->cig_off.p, 8 * ((size_t)n + 1), cudaMemcpyDeviceToHost, st));
     HG_CUDA(cudaMemcpyAsync(c->h_has_ins, c->has_ins.p, (size_t)n, cudaMemcpyDeviceToHost, st));
@@ -2092,16 +2105,20 @@ extern "C" int hg_collect(hg_ctx_t* c, uint32_t* cigar, int64_t cigar_cap, int64
     const int64_t* off = c->h_i64 + 4 * M;
     const int64_t total = off[n];
     if (total > cigar_cap) return fail(HG_ERR_CAPACITY, "hg_collect: cigar buffer too small");
-    const int64_t piece = (int64_t)c->cig_compact.n;
-    for (int64_t done = 0; done < total; done += piece) {
-        const int64_t m = std::min(piece, total - done);
-        compact_copy_kernel<<<c->sms, 256, 0, c->st>>>(c->cig.p, c->coff.p, c->n_cig.p, c->cig_off.p, (int)n,
-                                                       c->cig_compact.p, m, done);
-        HG_CUDA(cudaGetLastError());
-        HG_CUDA(cudaMemcpyAsync(cigar + done, c->cig_compact.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, c->st));
+    if (total <= c->h_cig_cap) {  // already in host memory
+        if (total) std::memcpy(cigar, c->h_cig, 4 * (size_t)total);
+    } else {
+        const int64_t piece = (int64_t)c->cig_compact.n;
+        for (int64_t done = 0; done < total; done += piece) {
+            const int64_t m = std::min(piece, total - done);
+            compact_copy_kernel<<<c->sms, 256, 0, c->st>>>(c->cig.p, c->coff.p, c->n_cig.p, c->cig_off.p, (int)n,
+                                                           c->cig_compact.p, m, done);
+            HG_CUDA(cudaGetLastError());
+            HG_CUDA(cudaMemcpyAsync(cigar + done, c->cig_compact.p, 4 * (size_t)m, cudaMemcpyDeviceToHost, c->st));
+        }
+        HG_CUDA(cudaEventRecord(c->collected_ev, c->st));
+        HG_CUDA(cudaEventSynchronize(c->collected_ev));
     }
-    HG_CUDA(cudaEventRecord(c->collected_ev, c->st));
-    HG_CUDA(cudaEventSynchronize(c->collected_ev));
     for (int64_t i = 0; i <= n; ++i) cigar_off[i] = off[i];
     if (has_ins) std::memcpy(has_ins, c->h_has_ins, (size_t)n);
     if (status) std::memcpy(status, c->h_status, 4 * (size_t)n);

@@ -152,3 +152,45 @@ def test_native_server_exception_capacity_fails_the_loop(gpu, pkg, serve_setup):
         srv.run(bad, np.array([0, len(bad)], np.int64), None)
     assert e.value.code == pkg.HG_ERR_CAPACITY and "exception runs" in str(e.value)
     srv.close()
+
+
+def test_native_server_concurrent_submitters(gpu, pkg, serve_setup):
+    """Four threads submit requests one at a time (hg_serve_submit) into a
+    small ring while a fifth takes results one at a time (hg_serve_result):
+    every id comes back once, with the CIGAR of the request that got it."""
+    import ctypes as C
+    import threading
+    w, ix = serve_setup
+    lib = pkg.lib()
+    srv = pkg.serve.NativeServer(ix, n_slots=2, slot_queries=8, slot_bases=60_000, budget_bytes=40 << 30)
+    n = w.n
+    req_of_id = {}
+    lock = threading.Lock()
+
+    def submit(part):
+        for i in range(part, n, 4):
+            q = w.query(i)
+            rid = lib.hg_serve_submit(srv.h, q, len(q))
+            assert rid >= 0
+            with lock:
+                req_of_id[rid] = i
+
+    threads = [threading.Thread(target=submit, args=(p,)) for p in range(4)]
+    for t in threads:
+        t.start()
+    got = {}
+    cig = np.zeros(1 << 16, np.uint32)
+    rid, st, lat, nc = C.c_int64(), C.c_uint32(), C.c_double(), C.c_int64()
+    while len(got) < n:
+        r = lib.hg_serve_result(srv.h, C.byref(rid), C.byref(st), C.byref(lat), cig.ctypes.data_as(C.c_void_p),
+                                len(cig), C.byref(nc), 10_000)
+        assert r == 1, r
+        assert rid.value not in got and st.value == 0
+        got[rid.value] = cig[:nc.value].copy()
+    for t in threads:
+        t.join()
+    alone = _alone(gpu, ix, w.seqs, w.offsets)
+    assert sorted(req_of_id) == sorted(got)
+    for k, v in got.items():
+        assert np.array_equal(v, alone[req_of_id[k]]), k
+    srv.close()
