@@ -239,6 +239,31 @@ def integer_roofline(pkg, args, stages, top, top_ms, bases, local, clocks):
     return roof
 
 
+def measure_link(nbytes: int = 1 << 30, reps: int = 3) -> dict:
+    """Pinned-memory copy rates of this host's link to the GPU (one 1 GiB
+    copy each way, median of reps, CUDA events on one stream).  The
+    host-buffer call overlaps its copies with compute, so its step cannot
+    be shorter than the copies' time at these rates."""
+    import torch
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    st = torch.cuda.Stream()
+    rates = {}
+    with torch.cuda.stream(st):
+        for name, dst, src in (("h2d", dev, host), ("d2h", host, dev)):
+            ms = []
+            for _ in range(reps + 1):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                dst.copy_(src, non_blocking=True)
+                e1.record(st)
+                e1.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            rates[name] = nbytes / (sorted(ms[1:])[len(ms[1:]) // 2] / 1e3) / 1e9
+    del dev, host
+    return rates
+
+
 def measure_plain(pkg, ctx, w, n_plain: int):
     """The plain form (one launch sequence per query, hg_align_plain) on the
     first n_plain queries, and the batched form on the same queries."""
@@ -759,8 +784,13 @@ def main():
         parity = {"checked_queries": int(len(pick)), "mismatches": int(mism), "against": "oracle CIGARs"}
         h2d = b.nbytes
         d2h = 4 * n_cig_words + 8 * (b.n + 1) + b.n + 4 * b.n + b.n * ix.L
+        link = measure_link()
         e2e = {"value": round(world * b.bases / e_wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1000 * e_wall, 3), "steps": e2e_steps,
+               "link": {"h2d_gb_per_s": round(link["h2d"], 1), "d2h_gb_per_s": round(link["d2h"], 1),
+                        "copy_ms_per_step": round(1000 * (h2d / link["h2d"] + d2h / link["d2h"]) / 1e9, 3),
+                        "note": "pinned 1 GiB copies on this host; the call overlaps copies with compute, so its "
+                                "step is bounded below by the device step and by these copies"},
                "input": "2-bit packed host buffers (the C ABI's input format)",
                "from_ascii": {"value": round(world * b.bases / a_wall / 1e6, 3), "unit": UNIT,
                               "ms_per_step": round(1000 * a_wall, 3), "steps": asc_steps,
