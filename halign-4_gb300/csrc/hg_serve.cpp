@@ -326,13 +326,20 @@ extern "C" int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries
         return hg::set_error(HG_ERR_CAPACITY, "hg_serve_create: one context does not fit the device-memory budget");
     }
     // the ring holds what every context can take at once and as much again
-    // waiting; it is pinned, so micro-batches upload from it directly
-    S->ring_cap = std::max<int64_t>(2 * (int64_t)S->slots.size() * slot_bases, 1 << 20);
-    if (cudaHostAlloc(reinterpret_cast<void**>(&S->ring), (size_t)S->ring_cap, cudaHostAllocDefault) != cudaSuccess) {
+    // waiting (at most 8 GiB unless one request needs more: a request of up
+    // to slot_bases always fits, wrap included, in 2 x slot_bases); it is
+    // pinned, so micro-batches upload from it directly.  Where the host
+    // cannot pin that much, smaller rings down to that floor are tried.
+    const int64_t floor_b = std::max<int64_t>(2 * slot_bases, 1 << 20);
+    S->ring_cap = std::max(floor_b, std::min<int64_t>(2 * (int64_t)S->slots.size() * slot_bases, 8LL << 30));
+    while (cudaHostAlloc(reinterpret_cast<void**>(&S->ring), (size_t)S->ring_cap, cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         S->ring = nullptr;
-        hg_serve_destroy(S);
-        return hg::set_error(HG_ERR_NOMEM, "hg_serve_create: pinned request ring");
+        if (S->ring_cap <= floor_b) {
+            hg_serve_destroy(S);
+            return hg::set_error(HG_ERR_NOMEM, "hg_serve_create: pinned request ring");
+        }
+        S->ring_cap = std::max(floor_b, S->ring_cap / 2);
     }
     S->sub = std::thread(submitter, S);
     S->col = std::thread(collector, S);

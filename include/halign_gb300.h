@@ -276,15 +276,15 @@ int hg_align_fasta_consensus(const char* queries_fasta, const char* out_fasta, i
 /* ---- serving loop (continuous batching) ---------------------------------
  * A request loop around one resident index: requests (one ASCII query each,
  * copied at submission into a ring of pinned host memory of 2 x contexts x
- * slot_bases bytes) wait in a FIFO; a submitting thread fills every free
- * context with the oldest waiting requests (up to slot_queries and
- * slot_bases per micro-batch) and enqueues it asynchronously - its bytes
- * upload straight from the ring and the device packs them (hg_align_ascii's
- * packing) - and a collecting thread polls the busy contexts, files each
- * finished request's CIGAR and status for hg_serve_result and frees its ring
- * bytes.  Requests that arrive
- * while others run join as contexts free up; micro-batches of different
- * contexts overlap on the GPU.  The contexts' device arenas are allocated at
+ * slot_bases bytes, at most 8 GiB or 2 x slot_bases if that is more) wait
+ * in a FIFO; a submitting thread fills every free context with the oldest
+ * waiting requests (up to slot_queries and slot_bases per micro-batch) and
+ * enqueues it asynchronously - its bytes upload straight from the ring and
+ * the device packs them (hg_align_ascii's packing) - and a collecting
+ * thread polls the busy contexts, files each finished request's CIGAR and
+ * status for hg_serve_result and frees its ring bytes.  Requests that
+ * arrive while others run join as contexts free up; micro-batches of
+ * different contexts overlap on the GPU.  The contexts' device arenas are allocated at
  * creation; n_slots is reduced to what budget_bytes of device memory holds
  * (at least one context must fit).  Submission and result calls are
  * thread-safe.  HAlign-4 has no serving mode: this is the request-level use
