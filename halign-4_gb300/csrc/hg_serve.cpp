@@ -23,6 +23,7 @@
 
 #include "../../include/halign_gb300.h"
 #include "hg_internal.h"
+#include "hg_ring.h"
 
 namespace {
 
@@ -58,13 +59,12 @@ struct hg_server {
     std::vector<Slot> slots;
     std::mutex mu;
     std::condition_variable cv_work, cv_done, cv_busy, cv_space;
-    // request bytes: a ring of pinned host memory.  Positions grow without
-    // bound (offset = position % ring_cap); a request never wraps (it starts
-    // at the next lap when it would).  Writers take submit_mu, so ring order
-    // is id order: the ring is free from the oldest unreleased request's
-    // position (ring_tail) up to ring_head, the end of the last reservation.
+    // request bytes: a ring of pinned host memory (hg_ring.h).  Writers take
+    // submit_mu, so ring order is id order and the ring is free before the
+    // oldest unreleased request (rel_id).
     char* ring = nullptr;
-    int64_t ring_cap = 0, ring_head = 0, ring_tail = 0, ring_pushed = 0, rel_id = 0;
+    hg::ByteRing rb;
+    int64_t rel_id = 0;
     std::mutex submit_mu;
     std::deque<Request> reqs;     // request id - base_id indexes it
     int64_t base_id = 0;
@@ -115,10 +115,10 @@ void admit(hg_server* S, std::vector<int64_t>& take, std::vector<int64_t>& len, 
         len.push_back(r.len);
         bases += r.len;
         if (r.len == 0) continue;
-        if (r.pos == end && end % S->ring_cap != 0) {
+        if (S->rb.continues(end, r.pos)) {
             run_bytes.back() += r.len;
         } else {
-            run_ptr.push_back(S->ring + r.pos % S->ring_cap);
+            run_ptr.push_back(S->ring + S->rb.offset(r.pos));
             run_bytes.push_back(r.len);
         }
         end = r.pos + r.len;
@@ -126,21 +126,14 @@ void admit(hg_server* S, std::vector<int64_t>& take, std::vector<int64_t>& len, 
 }
 
 // After requests were released: the ring is free up to the oldest
-// unreleased request (or the last pushed byte).  Called with the lock held.
+// unreleased request (or all queued bytes).  Called with the lock held.
 void advance_ring(hg_server* S)
 {
     const int64_t end = S->base_id + (int64_t)S->reqs.size();
     S->rel_id = std::max(S->rel_id, S->base_id);
     while (S->rel_id < end && S->reqs[(size_t)(S->rel_id - S->base_id)].released) ++S->rel_id;
-    S->ring_tail = S->rel_id < end ? S->reqs[(size_t)(S->rel_id - S->base_id)].pos : S->ring_pushed;
-}
-
-// Ring position of a request of len bytes after head: the next lap's start
-// when it would wrap.
-int64_t ring_place(const hg_server* S, int64_t head, int64_t len)
-{
-    const int64_t off = head % S->ring_cap;
-    return len > 0 && off + len > S->ring_cap ? head + (S->ring_cap - off) : head;
+    if (S->rel_id < end) S->rb.release_before(S->reqs[(size_t)(S->rel_id - S->base_id)].pos);
+    else S->rb.release_all();
 }
 
 void fail_all(hg_server* S, int code, const std::string& msg)
@@ -331,15 +324,15 @@ extern "C" int hg_serve_create(hg_index_t* ix, int n_slots, int64_t slot_queries
     // pinned, so micro-batches upload from it directly.  Where the host
     // cannot pin that much, smaller rings down to that floor are tried.
     const int64_t floor_b = std::max<int64_t>(2 * slot_bases, 1 << 20);
-    S->ring_cap = std::max(floor_b, std::min<int64_t>(2 * (int64_t)S->slots.size() * slot_bases, 8LL << 30));
-    while (cudaHostAlloc(reinterpret_cast<void**>(&S->ring), (size_t)S->ring_cap, cudaHostAllocDefault) != cudaSuccess) {
+    S->rb.cap = std::max(floor_b, std::min<int64_t>(2 * (int64_t)S->slots.size() * slot_bases, 8LL << 30));
+    while (cudaHostAlloc(reinterpret_cast<void**>(&S->ring), (size_t)S->rb.cap, cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         S->ring = nullptr;
-        if (S->ring_cap <= floor_b) {
+        if (S->rb.cap <= floor_b) {
             hg_serve_destroy(S);
             return hg::set_error(HG_ERR_NOMEM, "hg_serve_create: pinned request ring");
         }
-        S->ring_cap = std::max(floor_b, S->ring_cap / 2);
+        S->rb.cap = std::max(floor_b, S->rb.cap / 2);
     }
     S->sub = std::thread(submitter, S);
     S->col = std::thread(collector, S);
@@ -390,20 +383,15 @@ int64_t enqueue(hg_server* S, const char* seqs, const int64_t* offsets, int64_t 
         int64_t j = i;
         {
             std::unique_lock<std::mutex> lock(S->mu);
-            auto fits = [&](int64_t len) {
-                return ring_place(S, S->ring_head, len) + len - S->ring_tail <= S->ring_cap;
-            };
-            S->cv_space.wait(lock, [&] { return S->error || S->stop || fits(offsets[i + 1] - offsets[i]); });
+            S->cv_space.wait(lock, [&] { return S->error || S->stop || S->rb.fits(offsets[i + 1] - offsets[i]); });
             if (S->error) return -hg::set_error(S->error, S->error_msg);
             if (S->stop) return -hg::set_error(HG_ERR_ARG, std::string(who) + ": the server is stopping");
             pos.clear();
             int64_t bytes = 0;
             while (j < n && j - i < 8192 && bytes < (64 << 20)) {
                 const int64_t len = offsets[j + 1] - offsets[j];
-                if (!fits(len)) break;
-                const int64_t p = ring_place(S, S->ring_head, len);
-                pos.push_back(p);
-                S->ring_head = p + len;
+                if (!S->rb.fits(len)) break;
+                pos.push_back(S->rb.reserve(len));
                 bytes += len;
                 ++j;
             }
@@ -412,7 +400,7 @@ int64_t enqueue(hg_server* S, const char* seqs, const int64_t* offsets, int64_t 
 #pragma omp parallel for schedule(dynamic, 64) if (m > 256)
         for (int64_t k = 0; k < m; ++k) {
             const int64_t len = offsets[i + k + 1] - offsets[i + k];
-            if (len) std::memcpy(S->ring + pos[(size_t)k] % S->ring_cap, seqs + offsets[i + k], (size_t)len);
+            if (len) std::memcpy(S->ring + S->rb.offset(pos[(size_t)k]), seqs + offsets[i + k], (size_t)len);
         }
         {
             std::lock_guard<std::mutex> lock(S->mu);
@@ -427,7 +415,7 @@ int64_t enqueue(hg_server* S, const char* seqs, const int64_t* offsets, int64_t 
                 S->reqs.push_back(std::move(r));
                 S->pending.push_back(id0 + k);
             }
-            S->ring_pushed = S->ring_head;
+            S->rb.publish();
         }
         S->cv_work.notify_one();
         i = j;
