@@ -240,27 +240,50 @@ def integer_roofline(pkg, args, stages, top, top_ms, bases, local, clocks):
 
 
 def measure_link(nbytes: int = 1 << 30, reps: int = 3) -> dict:
-    """Pinned-memory copy rates of this host's link to the GPU (one 1 GiB
-    copy each way, median of reps, CUDA events on one stream).  The
-    host-buffer call overlaps its copies with compute, so its step cannot
-    be shorter than the copies' time at these rates."""
+    """Pinned-memory copy rates of this host's link to the GPU: one 1 GiB
+    copy each way, and both directions at once on two streams (median of
+    reps, CUDA events).  The host-buffer call overlaps its copies with
+    compute, so its step cannot be shorter than the copies' time at these
+    rates."""
     import torch
     dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    dev2 = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
     host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
-    st = torch.cuda.Stream()
+    host2 = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    st, st2 = torch.cuda.Stream(), torch.cuda.Stream()
     rates = {}
-    with torch.cuda.stream(st):
-        for name, dst, src in (("h2d", dev, host), ("d2h", host, dev)):
-            ms = []
-            for _ in range(reps + 1):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def median(ms):
+        ms = sorted(ms[1:])
+        return ms[len(ms) // 2]
+
+    for name, dst, src in (("h2d", dev, host), ("d2h", host, dev)):
+        ms = []
+        for _ in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(st):
                 e0.record(st)
                 dst.copy_(src, non_blocking=True)
                 e1.record(st)
-                e1.synchronize()
-                ms.append(e0.elapsed_time(e1))
-            rates[name] = nbytes / (sorted(ms[1:])[len(ms[1:]) // 2] / 1e3) / 1e9
-    del dev, host
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        rates[name] = nbytes / (median(ms) / 1e3) / 1e9
+    ms = []
+    for _ in range(reps + 1):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        st2.wait_event(e0)
+        with torch.cuda.stream(st):
+            dev.copy_(host, non_blocking=True)
+            e1.record(st)
+        with torch.cuda.stream(st2):
+            host2.copy_(dev2, non_blocking=True)
+            e2.record(st2)
+        e1.synchronize()
+        e2.synchronize()
+        ms.append(max(e0.elapsed_time(e1), e0.elapsed_time(e2)))
+    rates["both"] = 2 * nbytes / (median(ms) / 1e3) / 1e9
+    del dev, dev2, host, host2
     return rates
 
 
@@ -788,6 +811,7 @@ def main():
         e2e = {"value": round(world * b.bases / e_wall / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(1000 * e_wall, 3), "steps": e2e_steps,
                "link": {"h2d_gb_per_s": round(link["h2d"], 1), "d2h_gb_per_s": round(link["d2h"], 1),
+                        "both_ways_gb_per_s": round(link["both"], 1),
                         "copy_ms_per_step": round(1000 * (h2d / link["h2d"] + d2h / link["d2h"]) / 1e9, 3),
                         "note": "pinned 1 GiB copies on this host; the call overlaps copies with compute, so its "
                                 "step is bounded below by the device step and by these copies"},
