@@ -211,8 +211,12 @@ int hg_set_timing(hg_ctx_t* ctx, int on);
  * batch (within the context's capacity) on the context's stream and returns;
  * hg_poll returns 1 once its results are ready (0 while running, < 0 on
  * error); hg_collect copies them out in hg_align_batch's layout and frees the
- * context for the next hg_submit.  Several contexts of one index overlap on
- * the GPU; each keeps its own stream and arenas. */
+ * context for the next hg_submit.  The batch's last kernel writes its
+ * compacted CIGARs into mapped pinned memory of the context (up to
+ * max_bases / 8 + 64 x max_queries + 1024 ops), so a collect within that
+ * size is a host copy with no device work; longer ones are copied out from
+ * the device in pieces.  Several contexts of one index overlap on the GPU;
+ * each keeps its own stream and arenas. */
 int hg_submit(hg_ctx_t* ctx, const uint8_t* packed, const int64_t* poff, const int32_t* qlen, const int32_t* exc,
               const int64_t* exc_off, int64_t n);
 /* hg_submit for ASCII queries (seqs[i], lens[i] bytes each): they are packed
